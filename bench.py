@@ -1,0 +1,384 @@
+"""Benchmark of the GI/lighting stage: 1080p GI+denoise frames.
+
+One step = one frame of the stage on the 1920x1080 workload (40-box room,
+2048 VPLs with 6x128^2 FP16 distance cubes, 4 point lights, 4x2048^2 CSM,
+<= 64 VPLs per 16x16 tile, K = 8 samples per pixel, 5 denoise passes):
+VPL visibility cull, deferred PBR + CSM, tile cull, GI gather, merge +
+4 a-trous passes with temporal reprojection and composite, through
+sgi_render_frame. The 8-frame seeded camera path rotates, so consecutive steps
+read different G-buffers and CSMs (8 x 126 MB of per-frame inputs, above the
+129 MB L2) and L2 is additionally flushed before every timed step.
+
+value  = Mpix/s with inputs resident in HBM (CUDA events around each frame).
+e2e    = Mpix/s through the C ABI with the frame's G-buffer and light records
+         copied from pinned host memory and the HDR frame copied back, every step.
+--impl reference times the CPU restatement of the reference shaders (FP32
+oracle, all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "1080p GI+denoise Mpix/s (plain a-trous path)"
+UNIT = "Mpix/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["hd", "small"], default="hd")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name):
+    from stratusgfx_gb300 import scene as S
+    return S.HD if name == "hd" else S.SMALL
+
+
+# ------------------------------------------------------------- clocks ----
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx = float(parts[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------- algorithmic bytes ----
+def pass_bytes(w, num_points: int) -> dict:
+    """Bytes each pass must move per launch (each input read once, each output written once)."""
+    P = w.width * w.height
+    cube = 2 if w.cube_format == 1 else 4
+    gather = P * (4 + 4 + 4 + 4 + 2 + 2 + 8 + w.samples * cube)
+    merge_or_atrous = P * (8 + 4 + 4 + 8)
+    final = P * (8 + 4 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 8 + 2 + 8 + 8 + 2)
+    denoise = merge_or_atrous * (w.denoise_passes - 1) + final
+    deferred = P * (4 + 4 + 4 + 4 + 2 + 2 + 8) + 4 * w.csm_resolution ** 2 * 4
+    tiles = P * (4 + 4)
+    vis = w.num_vpls * (64 + 8 + 4 + 1)
+    return {"vpl_cull": vis, "direct": deferred, "tile_cull": tiles, "gather": gather, "denoise": denoise}
+
+
+PASS_NAMES = ["vpl_cull", "direct", "tile_cull", "gather", "denoise"]
+
+
+def traffic_from_profiles(kernel: str):
+    """dram bytes per launch recorded from an ncu capture in profiles/ (None if absent)."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+# --------------------------------------------------------- our arm ----
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    from stratusgfx_gb300 import abi, stage
+    from stratusgfx_gb300 import scene as S
+
+    torch.cuda.set_device(local_rank)
+    w = workload(args.workload)
+    P = w.width * w.height
+    sc = S.workload_scene(w, 1234 + 2 + rank)
+    ds = stage.DeviceScene(sc, w)
+    cfg = stage.workload_config(w)
+    st = stage.GiStage(cfg)
+    st.set_lights(ds.vpls, ds.entries, ds.points)
+    st.set_timing(True)
+    frames = len(sc.cameras) - 1
+    out = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    fps = 60.0
+    torch.cuda.synchronize()
+    launches0 = st.launch_count()
+
+    def frame(step):
+        k = step % frames + 1
+        st.set_shadow_maps(ds.csms[k], ds.cubes)
+        st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * step, fps)
+
+    for s in range(args.warmup):
+        frame(s)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    pass_ms = np.zeros(len(PASS_NAMES))
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    launches_before = st.launch_count()
+    for s in range(args.steps):
+        flush.fill_(float(s))                    # evict L2 (256 MB > 129 MB), outside the events
+        starts[s].record()
+        frame(args.warmup + s)
+        ends[s].record()
+        pass_ms += np.array(st.pass_times())     # synchronises on the frame's last event
+    torch.cuda.synchronize()
+    launches_timed = st.launch_count() - launches_before
+    clock = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = float(sum(ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * P * args.steps / (total_ms / 1e3) / 1e6
+
+    # ---- e2e: host buffers through the public API (ABI), copies inside the timed region
+    host_g = [g.pinned_clone() for g in ds.gbuffers]
+    host_vpls = ds.vpls.cpu().pin_memory()
+    host_entries = ds.entries.cpu().pin_memory()
+    host_points = ds.points.cpu().pin_memory() if ds.points is not None else None
+    dev_vpls = torch.empty_like(ds.vpls)
+    dev_entries = torch.empty_like(ds.entries)
+    dev_points = torch.empty_like(ds.points) if ds.points is not None else None
+    slots = [stage.GBufferTensors(w.height, w.width, "cuda") for _ in range(2)]
+    host_out = torch.empty((w.height, w.width, 4), dtype=torch.float16).pin_memory()
+    st2 = stage.GiStage(cfg)
+    h2d = slots[0].nbytes()
+    h2d += host_vpls.numel() * 4 + host_entries.numel() * 4 + (host_points.numel() * 4 if host_points is not None else 0)
+    d2h = host_out.numel() * 2
+    slots[0].copy_from(host_g[0])
+    slots[1].copy_from(host_g[0])
+
+    def e2e_frame(step):
+        k = step % frames + 1
+        cur, prev = slots[step % 2], slots[(step + 1) % 2]
+        cur.copy_from(host_g[k], non_blocking=True)
+        dev_vpls.copy_(host_vpls, non_blocking=True)
+        dev_entries.copy_(host_entries, non_blocking=True)
+        if dev_points is not None:
+            dev_points.copy_(host_points, non_blocking=True)
+        st2.set_lights(dev_vpls, dev_entries, dev_points)
+        st2.set_shadow_maps(ds.csms[k], ds.cubes)
+        st2.render_frame(cur, prev, ds.camera(k), out, 1000.0 + 16.0 * step, fps)
+        host_out.copy_(out, non_blocking=True)
+
+    for s in range(args.warmup):
+        e2e_frame(s)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for s in range(args.steps):
+        e2e_frame(args.warmup + s)
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * P * args.steps / (e2e_ms / 1e3) / 1e6
+
+    # ---- roofline of the dominant pass
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs") or 6800.0
+    peak_src = "measured" if peaks.get("hbm_gbs") else "fallback"
+    pb = pass_bytes(w, len(sc.points))
+    per_pass = {}
+    for i, name in enumerate(PASS_NAMES):
+        avg = pass_ms[i] / args.steps
+        gbs = pb[name] / (avg / 1e3) / 1e9 if avg > 0 else 0.0
+        per_pass[name] = {"ms": round(avg, 4), "alg_bytes": pb[name], "gbs": round(gbs, 1),
+                          "frac_hbm": round(gbs / hbm_peak, 4)}
+    dom = max(PASS_NAMES, key=lambda n: per_pass[n]["ms"])
+    roof = {"bound": "hbm", "kernel": dom, "achieved": per_pass[dom]["gbs"], "peak": hbm_peak, "unit": "GB/s",
+            "frac": per_pass[dom]["frac_hbm"], "traffic": traffic_from_profiles(dom), "peak_source": peak_src}
+
+    result = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w.name, "resolution": f"{w.width}x{w.height}", "vpls": w.num_vpls,
+                   "cube": f"6x{w.cube_size}^2 {'fp16' if w.cube_format == 1 else 'fp32'}",
+                   "csm": f"4x{w.csm_resolution}^2 fp32", "point_lights": w.num_points, "tile": w.tile_size,
+                   "max_vpls_per_tile": w.max_per_tile, "samples_per_pixel": w.samples,
+                   "denoise_passes": w.denoise_passes, "frames": frames, "gi_mode": "tiled",
+                   "l2": "flushed (256 MB write) before every timed frame; 8 rotating frames of inputs",
+                   "parallelism": f"replicas{world}"},
+        "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms / args.steps, 4)},
+        "gpu_launches": int(launches_timed),
+        "roofline": roof,
+        "passes": per_pass,
+        "clocks": clock,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline_from_device(ds, sc, w, cfg)
+    st.close()
+    st2.close()
+    return result
+
+
+def cpu_baseline_from_device(ds, sc, w, cfg):
+    """FP32 oracle (CPU restatement of the reference shaders) on one full frame of the same workload,
+    on the inputs the GPU generated (copied to host); all host threads."""
+    from oracle import binding as O
+    hg = [O.HostGBuffer(w.height, w.width, g.numpy()) for g in ds.gbuffers[:3]]
+    hs = O.HostScene.__new__(O.HostScene)
+    hs.scene, hs.w = sc, w
+    hs.gbuffers = hg
+    hs.csm_depth = [ds.csm_depth[k].cpu().numpy() for k in range(3)]
+    from stratusgfx_gb300 import stage
+    hs.csms = [stage.csm_struct(sc, k, hs.csm_depth[k].ctypes.data, w.csm_resolution) for k in range(3)]
+    storage = ds.cube_storage.cpu().numpy()
+    if storage.dtype == np.int16:
+        storage = storage.view(np.uint16)
+    hs.cube_storage = storage
+    hs.cubes = O.cube_struct(storage, w.cube_format, sc.layers_per_atlas)
+    H, W = w.height, w.width
+    gi = np.zeros((H, W, 4), np.float32)
+    hist = np.zeros((H, W), np.float32)
+    t0 = time.perf_counter()
+    nf = 0
+    for k in (1, 2):
+        r = O.frame(32, cfg, hs, k, gi, hist, 1000.0 + 16.0 * k, 60.0)
+        gi, hist = r["gi"], r["hist"]
+        nf += 1
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": round(nf * W * H / dt / 1e6, 4), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{nf} full {W}x{H} frames of the same workload through the FP32 oracle (OpenMP), "
+                      f"{dt:.1f} s"}
+
+
+# ---------------------------------------------------- reference arm ----
+def run_reference(args):
+    """The reference's path restated on the CPU (its GLSL needs an OpenGL driver, unavailable on this machine):
+    FP32 oracle with all host threads; inputs from the oracle's CPU ray caster."""
+    from oracle import binding as O
+    from stratusgfx_gb300 import stage
+    from stratusgfx_gb300 import scene as S
+    w = workload(args.workload)
+    sc = S.workload_scene(w, 1234 + 2)
+    t0 = time.perf_counter()
+    hs = O.HostScene(sc, w)
+    gen_s = time.perf_counter() - t0
+    cfg = stage.workload_config(w)
+    H, W = w.height, w.width
+    frames = len(sc.cameras) - 1
+    gi = np.zeros((H, W, 4), np.float32)
+    hist = np.zeros((H, W), np.float32)
+    steps = max(1, min(args.steps, 6))
+    warm = max(0, min(args.warmup, 1))
+    for s in range(warm):
+        k = s % frames + 1
+        r = O.frame(32, cfg, hs, k, gi, hist, 1000.0 + 16.0 * s, 60.0)
+        gi, hist = r["gi"], r["hist"]
+    t0 = time.perf_counter()
+    for s in range(steps):
+        k = (warm + s) % frames + 1
+        r = O.frame(32, cfg, hs, k, gi, hist, 1000.0 + 16.0 * s, 60.0)
+        gi, hist = r["gi"], r["hist"]
+    dt = time.perf_counter() - t0
+    value = steps * W * H / dt / 1e6
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warm,
+            "ms_per_step": round(dt / steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": w.name, "resolution": f"{W}x{H}", "gi_mode": "tiled",
+                       "samples_per_pixel": w.samples, "denoise_passes": w.denoise_passes},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{steps} full frames (of --steps {args.steps}) through the FP32 CPU "
+                                       f"restatement of the reference shaders; input generation {gen_s:.1f} s "
+                                       f"untimed"},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    from __graft_entry__ import build
+    build()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    res = run_ours(args, rank, world, local_rank)
+    if rank == 0:
+        print(json.dumps(res))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,282 @@
+/*
+ * sgi.h - C ABI of the GB300-native VPL global-illumination and deferred
+ * lighting stage (StratusGFX RendererBackend GI/lighting drop-in).
+ *
+ * The reference stage is a set of private RendererBackend methods driven by
+ * GL uniforms and SSBO bindings:
+ *   PerformVirtualPointLightCullingStage1_   Source/Engine/StratusRendererBackend.cpp:1578-1661
+ *   PerformVirtualPointLightCullingStage2_   Source/Engine/StratusRendererBackend.cpp:1666-1814
+ *   ComputeVirtualPointLightGlobalIllumination_
+ *                                            Source/Engine/StratusRendererBackend.cpp:1816-1952
+ *   deferred lighting block of RenderScene   Source/Engine/StratusRendererBackend.cpp:2011-2038
+ *   InitLights_ / InitCoreCSMData_           Source/Engine/StratusRendererBackend.cpp:2452-2604
+ * What the drop-in keeps is the data contract: G-buffer formats
+ * (StratusRendererBackend.cpp:384-424), GI/denoise buffer formats (:510-589),
+ * the std430 structs (Source/Engine/StratusGpuCommon.h:217-307) and the
+ * shadow-map conventions (:348-352, :2397-2449).
+ *
+ * Conventions
+ *  - Every image is W*H texels, row-major, row 0 = bottom (GL window space):
+ *    pixel (x, y) has fragment centre (x+0.5, y+0.5) and uv ((x+0.5)/W, (y+0.5)/H).
+ *  - Formats: RGB8 textures are held in 4-byte RGBA8 texels (the alpha byte is
+ *    ignored), RGB16F textures in 8-byte RGBA16F texels.
+ *  - All buffer pointers passed to sgi_* are DEVICE pointers unless stated.
+ *    The caller owns every input and output buffer; the context owns scratch
+ *    (compacted VPL lists, per-tile lists, reservoirs, ping-pong targets and
+ *    the denoiser history).
+ *  - Calls are asynchronous on the given stream (a cudaStream_t passed as
+ *    void*; NULL = legacy default stream). No call synchronises with the host
+ *    except sgi_read_debug and sgi_get_pass_times. One context per stream.
+ *  - Errors are status codes; nothing throws across the ABI. The text of the
+ *    last error of a context is returned by sgi_last_error.
+ */
+#ifndef SGI_H_
+#define SGI_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGI_ABI_VERSION 1
+
+typedef int32_t sgi_status;
+#define SGI_OK            0
+#define SGI_ERR_ARG      (-1)  /* bad argument: null pointer, size, mode */
+#define SGI_ERR_OOM      (-2)  /* device allocation failed */
+#define SGI_ERR_CUDA     (-3)  /* CUDA runtime error (launch or copy) */
+#define SGI_ERR_TIMEOUT  (-4)  /* a bounded device wait gave up */
+#define SGI_ERR_CAP      (-5)  /* a size exceeds a configured capacity */
+#define SGI_ERR_STATE    (-6)  /* call order: e.g. lighting before lights were set */
+
+/* ------------------------------------------------------------------------ */
+/* std430 records (byte-identical to the reference structs)                  */
+/* ------------------------------------------------------------------------ */
+
+/* GpuVplData, Source/Engine/StratusGpuCommon.h:217-232; VplData in
+ * Source/Shaders/vpl_common.glsl:48-56. 64 bytes. */
+typedef struct sgi_vpl {
+    float position[4];
+    float color[4];
+    float specular_position[4];
+    float radius;
+    float far_plane;
+    float intensity;
+    float pad_;
+} sgi_vpl;
+
+/* GpuPointLight, Source/Engine/StratusGpuCommon.h:261-270; PointLight in
+ * Source/Shaders/pbr.fs:16-22. 48 bytes. */
+typedef struct sgi_point_light {
+    float position[4];
+    float color[4];
+    float radius;
+    float far_plane;
+    float pad_[2];
+} sgi_point_light;
+
+/* GpuAtlasEntry, Source/Engine/StratusGpuCommon.h:274-277; AtlasEntry in
+ * Source/Shaders/pbr.glsl:75-78. 8 bytes. */
+typedef struct sgi_atlas_entry {
+    int32_t index;   /* which cube-map atlas */
+    int32_t layer;   /* cube layer inside that atlas */
+} sgi_atlas_entry;
+
+/* GpuVplStage1PerTileOutputs, Source/Engine/StratusGpuCommon.h:192-196. */
+typedef struct sgi_tile_stage1 {
+    float average_position[4];
+    float average_normal[4];
+} sgi_tile_stage1;
+
+/* ------------------------------------------------------------------------ */
+/* Configuration (RendererSettings subset, StratusRendererBackend.h:186-294) */
+/* ------------------------------------------------------------------------ */
+
+/* Which VPL set the GI gather samples from. */
+#define SGI_GI_REFERENCE 0  /* global compacted list, vpl_pbr_gi.fs:145-151 */
+#define SGI_GI_TILED     1  /* per-tile nearest-L list (culling stage 2) */
+
+/* Storage format of the VPL distance cube maps. */
+#define SGI_CUBE_F32     0
+#define SGI_CUBE_F16     1
+#define SGI_CUBE_UNORM16 2  /* the reference's GL_DEPTH_COMPONENT16 */
+
+#define SGI_MAX_ATLASES          14   /* MAX_TOTAL_SHADOW_ATLASES, pbr.glsl:70 */
+#define SGI_MAX_VPLS_BEFORE_CULL 10000 /* MAX_TOTAL_VPLS_BEFORE_CULLING, vpl_common.glsl:7 */
+#define SGI_MAX_VPLS_PER_FRAME   4480 /* MAX_TOTAL_VPLS_PER_FRAME = 14*320, vpl_common.glsl:8 */
+#define SGI_MAX_TILE_LIST        64
+#define SGI_MAX_DENOISE_PASSES   8
+#define SGI_MAX_POINT_LIGHTS     256
+
+typedef struct sgi_config {
+    int32_t width;                 /* viewport width in pixels  */
+    int32_t height;                /* viewport height in pixels */
+    int32_t max_vpls;              /* capacity of sgi_set_lights (<= 10000) */
+    int32_t max_visible;           /* cap of the compacted list (reference 4480) */
+    int32_t tile_size;             /* tile edge in pixels, 8..32 (reference 5, configs 16) */
+    int32_t max_vpls_per_tile;     /* L, 1..64 (reference 12) */
+    int32_t gi_mode;               /* SGI_GI_REFERENCE or SGI_GI_TILED */
+    int32_t samples_per_pixel;     /* 0 = reference adaptive 2..10 (vpl_pbr_gi.fs:138-143), else fixed K */
+    int32_t denoise_passes;        /* 2..8: pass 0 merges reservoirs, the last is final (reference 4) */
+    int32_t debug_keep_passes;     /* nonzero: keep each denoise pass output for sgi_read_debug */
+    float   min_roughness;         /* RendererSettings minRoughness_ = 0.08 */
+    int32_t use_perceptual_roughness; /* RendererSettings usePerceptualRoughness = true */
+    float   min_gi_occlusion_factor;  /* RendererSettings minGiOcclusionFactor_ = 0.95 */
+    float   emission_strength;     /* RendererSettings emissionStrength_ = 0 */
+    float   fog_density;           /* RendererSettings fogDensity_ = 0 */
+    float   fog_color[3];          /* fog.glsl:3 default vec3(0.5) */
+    float   point_light_ambient_intensity; /* pbr.glsl:66 default 0.003 */
+} sgi_config;
+
+/* Fills cfg with the reference defaults for a W x H viewport. */
+void sgi_config_defaults(sgi_config* cfg, int32_t width, int32_t height);
+
+/* ------------------------------------------------------------------------ */
+/* Per-frame inputs                                                           */
+/* ------------------------------------------------------------------------ */
+
+/* G-buffer, formats of RendererBackend::InitGBuffer_ (StratusRendererBackend.cpp:384-424). */
+typedef struct sgi_gbuffer {
+    const float*    depth;      /* DEPTH FP32 window depth in [0,1] */
+    const uint32_t* normal;     /* RGB8 0.5*n+0.5 */
+    const uint32_t* albedo;     /* RGBA8 base colour, alpha = emissive.r */
+    const uint16_t* base_reflectivity; /* RG8 (reflectance, emissive.g) */
+    const uint32_t* roughness_metallic_ambient; /* RGB8 (roughness, metallic, emissive.b) */
+    const uint32_t* velocity;   /* RG16F uv(current) - uv(previous) */
+    const float*    id;         /* R32F draw id */
+    const uint16_t* ssao;       /* R16F blurred occlusion */
+} sgi_gbuffer;
+
+/* RendererFrame camera fields (StratusRendererBackend.h:297-323). Matrices are
+ * column-major (glm), GL clip conventions (NDC z in [-1,1]). */
+typedef struct sgi_camera {
+    float inv_proj_view[16];
+    float view_position[4];
+} sgi_camera;
+
+/* Directional light + cascaded shadow map (pbr.glsl:53-63, set by
+ * InitCoreCSMData_ StratusRendererBackend.cpp:2452-2474 and InitLights_ :2583-2596). */
+typedef struct sgi_csm {
+    const float* depth;            /* DEVICE [num_cascades][resolution][resolution] FP32 window depth */
+    int32_t resolution;
+    int32_t num_cascades;          /* must be 4 */
+    float   cascade_proj_view[4][16];  /* cascadeProjViews[i] (projectionViewSample) */
+    float   cascade_planes[3][4];      /* cascadePlanes[i] = cascades[i+1].cascadePlane */
+    float   light_direction[4];    /* infiniteLightDirection (unit, towards the light) */
+    float   light_color[4];        /* infiniteLightColor = luminance */
+    float   znear;                 /* infiniteLightZnear */
+    float   zfar;                  /* infiniteLightZfar */
+    float   depth_bias;            /* infiniteLightDepthBias */
+    float   pad_;
+} sgi_csm;
+
+/* VPL distance cube maps: samplerCubeArray shadowCubeMaps[MAX_TOTAL_SHADOW_ATLASES]
+ * (vpl_pbr_gi.fs:69). Atlas a holds layers_per_atlas cubes laid out
+ * [layer][face +X,-X,+Y,-Y,+Z,-Z][t][s], texel = saturate(distance / farPlane)
+ * (shadowVpl.fs:26-34). */
+typedef struct sgi_cube_atlas {
+    const void* atlas[SGI_MAX_ATLASES];  /* DEVICE pointers */
+    int32_t num_atlases;
+    int32_t layers_per_atlas;
+    int32_t face_size;
+    int32_t format;                      /* SGI_CUBE_* */
+} sgi_cube_atlas;
+
+typedef struct sgi_frame_params {
+    float time;               /* RNG seed z (uniform float time), milliseconds */
+    float frames_per_second;  /* uniform framesPerSecond = 1 / deltaSeconds */
+} sgi_frame_params;
+
+/* ------------------------------------------------------------------------ */
+/* Context                                                                    */
+/* ------------------------------------------------------------------------ */
+
+typedef struct sgi_ctx sgi_ctx;
+
+int32_t     sgi_abi_version(void);
+const char* sgi_status_string(sgi_status s);
+
+/* Allocates the context and its scratch on the current CUDA device.
+ * Replaces the buffer setup of RendererBackend::UpdateWindowDimensions_
+ * (StratusRendererBackend.cpp:437-589). */
+sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out);
+sgi_status sgi_destroy(sgi_ctx* ctx);
+const char* sgi_last_error(const sgi_ctx* ctx);
+
+/* Uploads this frame's VPL records (and their cube-atlas slots) and point
+ * lights. Replaces InitVplFrameData_ (StratusRendererBackend.cpp:1281-1292)
+ * and the point-light SSBO uploads of InitLights_ (:2535-2552). `entries` is
+ * indexed like `vpls`. Device pointers; copied device-to-device on `stream`. */
+sgi_status sgi_set_lights(sgi_ctx* ctx,
+                          const sgi_vpl* vpls, const sgi_atlas_entry* entries, int32_t num_vpls,
+                          const sgi_point_light* points, int32_t num_points,
+                          void* stream);
+
+/* Binds the directional light's CSM and the VPL cube atlases (caller-owned
+ * device memory; pointers and matrices are copied into the context). */
+sgi_status sgi_set_shadow_maps(sgi_ctx* ctx, const sgi_csm* csm, const sgi_cube_atlas* cubes);
+
+/* VPL visibility cull: viscull_vpls.cs dispatched by
+ * PerformVirtualPointLightCullingStage1_ (StratusRendererBackend.cpp:1578-1661).
+ * Stable compaction in ascending VPL index; no host readback. */
+sgi_status sgi_cull_vpls(sgi_ctx* ctx, void* stream);
+
+/* Per-tile culling: vpl_tiled_deferred_culling_stage1.cs + _stage2.cs
+ * (dispatch at StratusRendererBackend.cpp:1733-1783). */
+sgi_status sgi_cull_tiles(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera* cam, void* stream);
+
+/* Deferred PBR + CSM lighting: pbr.fs with INFINITE_LIGHTING_ENABLED, the
+ * RenderScene block at StratusRendererBackend.cpp:2011-2038.
+ * hdr_out: RGB16F (8-byte texels) W*H. */
+sgi_status sgi_direct_lighting(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera* cam,
+                               void* hdr_out, void* stream);
+
+/* GI gather + spatiotemporal denoise + composite:
+ * ComputeVirtualPointLightGlobalIllumination_ (StratusRendererBackend.cpp:1816-1952).
+ * hdr_in = lighting colour buffer ("screen"), hdr_out = lightingFbo colour
+ * (both RGB16F 8-byte texels). `prev` is the previous frame's G-buffer (only
+ * normal, depth and id are read). Updates the context's history. */
+sgi_status sgi_global_illumination(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer* prev,
+                                   const sgi_camera* cam, const void* hdr_in, void* hdr_out,
+                                   const sgi_frame_params* params, void* stream);
+
+/* The whole stage in reference order: VPL cull, direct lighting, tile cull,
+ * GI gather, denoise, composite (RenderScene :1982-1987 and :2011-2045). */
+sgi_status sgi_render_frame(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer* prev,
+                            const sgi_camera* cam, const sgi_frame_params* params,
+                            void* hdr_out, void* stream);
+
+/* Clears the denoiser history (vplGIDenoisedPrevFrameFbo). */
+sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream);
+
+/* Synchronous copies of context scratch for parity tests.
+ * which: SGI_DEBUG_*; writes at most `bytes` to host_dst; *needed (if not
+ * NULL) receives the full size. */
+#define SGI_DEBUG_VISIBLE_INDEX   0  /* int32 [1 + max_vpls]: count, then original indices */
+#define SGI_DEBUG_COMPACT_VPLS    1  /* sgi_vpl [max_visible] */
+#define SGI_DEBUG_COMPACT_ENTRIES 2  /* sgi_atlas_entry [max_visible] */
+#define SGI_DEBUG_TILE_STAGE1     3  /* sgi_tile_stage1 [tiles] */
+#define SGI_DEBUG_TILE_LISTS      4  /* int32 [tiles][1 + L]: count, compacted indices */
+#define SGI_DEBUG_RESERVOIR       5  /* RGBA16F [W*H]: gather output (vplColor, validSamples) */
+#define SGI_DEBUG_GI_HISTORY      6  /* RGB16F [W*H]: this frame's denoised GI (giColor) */
+#define SGI_DEBUG_HISTORY_DEPTH   7  /* R16F [W*H]: accumulated history length */
+#define SGI_DEBUG_DIRECT          8  /* RGB16F [W*H]: direct lighting of sgi_render_frame */
+#define SGI_DEBUG_PASS_BASE      16  /* + k: RGBA16F [W*H] reservoir output of denoise pass k */
+sgi_status sgi_read_debug(sgi_ctx* ctx, int32_t which, void* host_dst, size_t bytes, size_t* needed);
+
+/* Per-pass GPU times (ms) of the last sgi_render_frame when timing is on:
+ * [0] vpl cull, [1] direct lighting, [2] tile cull, [3] gather, [4] denoise. */
+#define SGI_NUM_PASS_TIMES 5
+sgi_status sgi_set_timing(sgi_ctx* ctx, int32_t enabled);
+sgi_status sgi_get_pass_times(sgi_ctx* ctx, float* ms, int32_t n);
+
+/* Kernel launches the context issued since creation (all sgi_* calls). */
+int64_t sgi_launch_count(const sgi_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SGI_H_ */

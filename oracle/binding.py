@@ -1,0 +1,231 @@
+"""ctypes binding of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Used by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg as the
+checker / CPU baseline. Parity of the oracle itself is UNPINNED by the
+reference (StratusGFX has no golden vectors; its GLSL needs an OpenGL driver).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+from oracle import build as _build  # noqa: E402
+from stratusgfx_gb300 import abi  # noqa: E402  (struct layouts of include/sgi.h only)
+
+_lib = None
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        lib = C.CDLL(_build.build())
+        P = C.c_void_p
+        sig = {
+            "oracle_version": (C.c_int, []),
+            "oracle_random3": (C.c_float, [C.c_float, C.c_float, C.c_float]),
+            "oracle_hash": (C.c_uint32, [C.c_uint32]),
+            "oracle_exp_f32": (C.c_float, [C.c_float]),
+            "oracle_pow128_f32": (C.c_float, [C.c_float]),
+            "oracle_f32_to_f16": (C.c_uint16, [C.c_float]),
+            "oracle_f16_to_f32": (C.c_float, [C.c_uint16]),
+            "oracle_world_from_depth": (None, [C.c_int, C.c_double, C.c_double, C.c_double, P, P]),
+            "oracle_vpl_brdf": (None, [C.c_int, P, C.POINTER(abi.Config), P]),
+            "oracle_infinite_shadow": (None, [C.c_int, C.POINTER(abi.Csm), P, P, C.c_int, C.c_int, P]),
+            "oracle_vis_cull": (C.c_int, [C.c_int, P, C.c_int, C.POINTER(abi.Csm), C.c_int, P]),
+            "oracle_tile_stage1": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.Camera), P]),
+            "oracle_tile_stage2": (None, [C.c_int, C.POINTER(abi.Config), P, P, C.c_int, P]),
+            "oracle_gather": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.Camera), P,
+                                     P, C.c_int, P, C.POINTER(abi.CubeAtlas), C.c_float, P]),
+            "oracle_denoise": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.GBuffer),
+                                      P, P, P, P, C.c_int, C.POINTER(abi.FrameParams), P, P, P, P]),
+            "oracle_deferred": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.Camera),
+                                       P, C.c_int, C.POINTER(abi.Csm), P]),
+            "oracle_scene_gbuffer": (None, [P, C.c_int, C.POINTER(abi.SceneCamera), C.c_int, C.c_int, P, P, P, P, P,
+                                            P, P, P]),
+            "oracle_scene_csm": (None, [P, C.c_int, C.POINTER(abi.Csm), P, P]),
+            "oracle_scene_cube_atlas": (None, [P, C.c_int, P, P, C.c_int, C.POINTER(abi.CubeAtlas)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _dt(prec):
+    return np.float32 if prec == 32 else np.float64
+
+
+class HostGBuffer:
+    """numpy G-buffer planes (same shapes/dtypes as stage.GBufferTensors)."""
+
+    NAMES = ("depth", "normal", "albedo", "base_reflectivity", "rma", "velocity", "id", "ssao")
+
+    def __init__(self, H, W, arrays=None):
+        if arrays is None:
+            arrays = dict(depth=np.zeros((H, W), np.float32), normal=np.zeros((H, W, 4), np.uint8),
+                          albedo=np.zeros((H, W, 4), np.uint8), base_reflectivity=np.zeros((H, W, 2), np.uint8),
+                          rma=np.zeros((H, W, 4), np.uint8), velocity=np.zeros((H, W, 2), np.float16),
+                          id=np.zeros((H, W), np.float32), ssao=np.zeros((H, W), np.float16))
+        for k in self.NAMES:
+            setattr(self, k, np.ascontiguousarray(arrays[k]))
+
+    def struct(self) -> abi.GBuffer:
+        return abi.GBuffer(*[getattr(self, k).ctypes.data for k in self.NAMES])
+
+    def arrays(self):
+        return {k: getattr(self, k) for k in self.NAMES}
+
+
+def scene_gbuffer(boxes, cam: abi.SceneCamera, W, H) -> HostGBuffer:
+    g = HostGBuffer(H, W)
+    load().oracle_scene_gbuffer(_p(boxes), boxes.shape[0], C.byref(cam), W, H, *[_p(getattr(g, k)) for k in g.NAMES])
+    return g
+
+
+def scene_csm(boxes, csm: abi.Csm, inv: np.ndarray, R) -> np.ndarray:
+    out = np.zeros((4, R, R), np.float32)
+    inv = np.ascontiguousarray(inv, dtype=np.float32)
+    load().oracle_scene_csm(_p(boxes), boxes.shape[0], C.byref(csm), _p(inv), _p(out))
+    return out
+
+
+def scene_cubes(boxes, vpls, entries, face, fmt, layers=320):
+    n = vpls.shape[0]
+    na = max(1, (n + layers - 1) // layers)
+    storage = np.zeros((na, layers, 6, face, face), np.float32 if fmt == abi.SGI_CUBE_F32 else np.uint16)
+    at = abi.CubeAtlas()
+    for a in range(na):
+        at.atlas[a] = storage[a].ctypes.data
+    at.num_atlases, at.layers_per_atlas, at.face_size, at.format = na, layers, face, fmt
+    if n:
+        v = np.ascontiguousarray(vpls, dtype=np.float32)
+        e = np.ascontiguousarray(entries, dtype=np.int32)
+        load().oracle_scene_cube_atlas(_p(boxes), boxes.shape[0], _p(v), _p(e), n, C.byref(at))
+    return storage, at
+
+
+def cube_struct(storage: np.ndarray, fmt: int, layers: int = 320) -> abi.CubeAtlas:
+    at = abi.CubeAtlas()
+    for a in range(storage.shape[0]):
+        at.atlas[a] = storage[a].ctypes.data
+    at.num_atlases, at.layers_per_atlas, at.face_size, at.format = storage.shape[0], layers, storage.shape[-1], fmt
+    return at
+
+
+def vis_cull(prec, vpls, csm: abi.Csm, cap):
+    n = vpls.shape[0]
+    idx = np.zeros(1 + max(n, 1), np.int32)
+    v = np.ascontiguousarray(vpls, dtype=np.float32)
+    load().oracle_vis_cull(prec, _p(v), n, C.byref(csm), cap, _p(idx))
+    return idx
+
+
+def tile_stage1(prec, cfg, g: HostGBuffer, cam: abi.Camera):
+    T = ((cfg.width + cfg.tile_size - 1) // cfg.tile_size) * ((cfg.height + cfg.tile_size - 1) // cfg.tile_size)
+    out = np.zeros((T, 8), _dt(prec))
+    load().oracle_tile_stage1(prec, C.byref(cfg), C.byref(g.struct()), C.byref(cam), _p(out))
+    return out
+
+
+def tile_stage2(prec, cfg, stage1, cvpls, count):
+    T = stage1.shape[0]
+    lists = np.zeros((T, 1 + cfg.max_vpls_per_tile), np.int32)
+    s1 = np.ascontiguousarray(stage1, dtype=_dt(prec))
+    cv = np.ascontiguousarray(cvpls, dtype=np.float32)
+    load().oracle_tile_stage2(prec, C.byref(cfg), _p(s1), _p(cv), count, _p(lists))
+    return lists
+
+
+def gather(prec, cfg, g: HostGBuffer, cam, cvpls, centries, count, lists, cubes: abi.CubeAtlas, time):
+    res = np.zeros((cfg.height, cfg.width, 4), _dt(prec))
+    lists_arr = None if lists is None else np.ascontiguousarray(lists, dtype=np.int32)
+    cv = np.ascontiguousarray(cvpls, dtype=np.float32)
+    ce = np.ascontiguousarray(centries, dtype=np.int32)
+    load().oracle_gather(prec, C.byref(cfg), C.byref(g.struct()), C.byref(cam), _p(cv), _p(ce), count,
+                         _p(lists_arr), C.byref(cubes), time, _p(res))
+    return res
+
+
+def denoise(prec, cfg, cur: HostGBuffer, prev: HostGBuffer, reservoir, hdr_in, gi_prev, hist_prev, num_visible,
+            time, fps, keep_passes=False):
+    H, W = cfg.height, cfg.width
+    dt = _dt(prec)
+    comb = np.zeros((H, W, 4), dt)
+    gi = np.zeros((H, W, 4), dt)
+    hist = np.zeros((H, W), dt)
+    passes = np.zeros((cfg.denoise_passes, H, W, 4), dt) if keep_passes else None
+    keep = [np.ascontiguousarray(a, dtype=dt) for a in (reservoir, hdr_in, gi_prev, hist_prev)]
+    fp = abi.FrameParams(time, fps)
+    load().oracle_denoise(prec, C.byref(cfg), C.byref(cur.struct()), C.byref(prev.struct()),
+                          *[_p(a) for a in keep], num_visible, C.byref(fp), _p(comb), _p(gi), _p(hist), _p(passes))
+    return comb, gi, hist, passes
+
+
+def deferred(prec, cfg, g: HostGBuffer, cam, points, csm: abi.Csm):
+    out = np.zeros((cfg.height, cfg.width, 4), _dt(prec))
+    npts = 0 if points is None else points.shape[0]
+    pts = None if points is None else np.ascontiguousarray(points, dtype=np.float32)
+    load().oracle_deferred(prec, C.byref(cfg), C.byref(g.struct()), C.byref(cam), _p(pts), npts, C.byref(csm), _p(out))
+    return out
+
+
+class HostScene:
+    """CPU-side inputs of a workload (oracle ray caster) with host-pointer structs."""
+
+    def __init__(self, scene, w):
+        from stratusgfx_gb300 import stage  # struct builders only
+        self.scene, self.w = scene, w
+        H, W = w.height, w.width
+        self.gbuffers = [scene_gbuffer(scene.boxes, stage.scene_camera_struct(scene, k), W, H)
+                         for k in range(len(scene.cameras))]
+        R = w.csm_resolution
+        self.csm_depth, self.csms = [], []
+        for k in range(len(scene.cameras)):
+            placeholder = stage.csm_struct(scene, k, 0, R)
+            d = scene_csm(scene.boxes, placeholder, scene.csms[k].inv_cascade_proj_view, R)
+            self.csm_depth.append(d)
+            self.csms.append(stage.csm_struct(scene, k, d.ctypes.data, R))
+        self.cube_storage, self.cubes = scene_cubes(scene.boxes, scene.vpls, scene.entries, w.cube_size,
+                                                    w.cube_format, scene.layers_per_atlas)
+
+    def camera(self, k):
+        from stratusgfx_gb300 import stage
+        return stage.camera_struct(self.scene, k)
+
+
+def frame(prec, cfg, hs: HostScene, k: int, gi_prev, hist_prev, time, fps, keep=False):
+    """The whole stage for camera k (k >= 1; k - 1 is the previous frame), like sgi_render_frame.
+    Returns a dict of every intermediate."""
+    sc = hs.scene
+    cam = hs.camera(k)
+    csm = hs.csms[k]
+    idx = vis_cull(prec, sc.vpls, csm, cfg.max_visible)
+    count = int(idx[0])
+    order = idx[1:1 + count]
+    cv = np.ascontiguousarray(sc.vpls[order])
+    ce = np.ascontiguousarray(sc.entries[order])
+    direct = deferred(prec, cfg, hs.gbuffers[k], cam, sc.points if len(sc.points) else None, csm)
+    direct_in = direct
+    s1 = lists = None
+    if cfg.gi_mode == abi.SGI_GI_TILED:
+        s1 = tile_stage1(prec, cfg, hs.gbuffers[k], cam)
+        lists = tile_stage2(prec, cfg, s1, cv, count)
+    res = gather(prec, cfg, hs.gbuffers[k], cam, cv, ce, count, lists, hs.cubes, time)
+    comb, gi, hist, passes = denoise(prec, cfg, hs.gbuffers[k], hs.gbuffers[k - 1], res, direct_in, gi_prev,
+                                     hist_prev, count, time, fps, keep)
+    return dict(visible_index=idx, count=count, direct=direct, stage1=s1, lists=lists, reservoir=res,
+                combined=comb, gi=gi, hist=hist, passes=passes)

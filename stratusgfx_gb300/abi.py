@@ -1,0 +1,169 @@
+"""ctypes mirror of include/sgi.h and include/sgi_scene.h, and the loader of libsgi.so.
+
+The library is built in-tree by ``stratusgfx_gb300.build``; importing this
+module never falls back to anything else: a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+SGI_OK = 0
+SGI_ERR_ARG = -1
+SGI_ERR_OOM = -2
+SGI_ERR_CUDA = -3
+SGI_ERR_TIMEOUT = -4
+SGI_ERR_CAP = -5
+SGI_ERR_STATE = -6
+
+SGI_GI_REFERENCE = 0
+SGI_GI_TILED = 1
+SGI_CUBE_F32 = 0
+SGI_CUBE_F16 = 1
+SGI_CUBE_UNORM16 = 2
+SGI_MAX_ATLASES = 14
+SGI_MAX_VPLS_BEFORE_CULL = 10000
+SGI_MAX_VPLS_PER_FRAME = 4480
+SGI_NUM_PASS_TIMES = 5
+
+SGI_DEBUG_VISIBLE_INDEX = 0
+SGI_DEBUG_COMPACT_VPLS = 1
+SGI_DEBUG_COMPACT_ENTRIES = 2
+SGI_DEBUG_TILE_STAGE1 = 3
+SGI_DEBUG_TILE_LISTS = 4
+SGI_DEBUG_RESERVOIR = 5
+SGI_DEBUG_GI_HISTORY = 6
+SGI_DEBUG_HISTORY_DEPTH = 7
+SGI_DEBUG_DIRECT = 8
+SGI_DEBUG_PASS_BASE = 16
+
+
+class Vpl(C.Structure):           # GpuVplData, 64 B
+    _fields_ = [("position", C.c_float * 4), ("color", C.c_float * 4), ("specular_position", C.c_float * 4),
+                ("radius", C.c_float), ("far_plane", C.c_float), ("intensity", C.c_float), ("pad_", C.c_float)]
+
+
+class PointLight(C.Structure):    # GpuPointLight, 48 B
+    _fields_ = [("position", C.c_float * 4), ("color", C.c_float * 4), ("radius", C.c_float),
+                ("far_plane", C.c_float), ("pad_", C.c_float * 2)]
+
+
+class AtlasEntry(C.Structure):    # GpuAtlasEntry, 8 B
+    _fields_ = [("index", C.c_int32), ("layer", C.c_int32)]
+
+
+class Config(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("max_vpls", C.c_int32), ("max_visible", C.c_int32),
+                ("tile_size", C.c_int32), ("max_vpls_per_tile", C.c_int32), ("gi_mode", C.c_int32),
+                ("samples_per_pixel", C.c_int32), ("denoise_passes", C.c_int32), ("debug_keep_passes", C.c_int32),
+                ("min_roughness", C.c_float), ("use_perceptual_roughness", C.c_int32),
+                ("min_gi_occlusion_factor", C.c_float), ("emission_strength", C.c_float),
+                ("fog_density", C.c_float), ("fog_color", C.c_float * 3),
+                ("point_light_ambient_intensity", C.c_float)]
+
+
+class GBuffer(C.Structure):
+    _fields_ = [("depth", C.c_void_p), ("normal", C.c_void_p), ("albedo", C.c_void_p),
+                ("base_reflectivity", C.c_void_p), ("roughness_metallic_ambient", C.c_void_p),
+                ("velocity", C.c_void_p), ("id", C.c_void_p), ("ssao", C.c_void_p)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("inv_proj_view", C.c_float * 16), ("view_position", C.c_float * 4)]
+
+
+class Csm(C.Structure):
+    _fields_ = [("depth", C.c_void_p), ("resolution", C.c_int32), ("num_cascades", C.c_int32),
+                ("cascade_proj_view", (C.c_float * 16) * 4), ("cascade_planes", (C.c_float * 4) * 3),
+                ("light_direction", C.c_float * 4), ("light_color", C.c_float * 4), ("znear", C.c_float),
+                ("zfar", C.c_float), ("depth_bias", C.c_float), ("pad_", C.c_float)]
+
+
+class CubeAtlas(C.Structure):
+    _fields_ = [("atlas", C.c_void_p * SGI_MAX_ATLASES), ("num_atlases", C.c_int32),
+                ("layers_per_atlas", C.c_int32), ("face_size", C.c_int32), ("format", C.c_int32)]
+
+
+class FrameParams(C.Structure):
+    _fields_ = [("time", C.c_float), ("frames_per_second", C.c_float)]
+
+
+class Box(C.Structure):           # sgi_box, 64 B
+    _fields_ = [("min", C.c_float * 4), ("max", C.c_float * 4), ("albedo", C.c_float * 4), ("roughness", C.c_float),
+                ("metallic", C.c_float), ("reflectance", C.c_float), ("id", C.c_float)]
+
+
+class SceneCamera(C.Structure):
+    _fields_ = [("proj_view", C.c_float * 16), ("inv_proj_view", C.c_float * 16),
+                ("prev_proj_view", C.c_float * 16), ("position", C.c_float * 4)]
+
+
+assert C.sizeof(Vpl) == 64 and C.sizeof(PointLight) == 48 and C.sizeof(AtlasEntry) == 8 and C.sizeof(Box) == 64
+
+EXPORTS = {
+    "sgi_abi_version": (C.c_int32, []),
+    "sgi_status_string": (C.c_char_p, [C.c_int32]),
+    "sgi_config_defaults": (None, [C.POINTER(Config), C.c_int32, C.c_int32]),
+    "sgi_create": (C.c_int32, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
+    "sgi_destroy": (C.c_int32, [C.c_void_p]),
+    "sgi_last_error": (C.c_char_p, [C.c_void_p]),
+    "sgi_set_lights": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
+    "sgi_set_shadow_maps": (C.c_int32, [C.c_void_p, C.POINTER(Csm), C.POINTER(CubeAtlas)]),
+    "sgi_cull_vpls": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "sgi_cull_tiles": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(Camera), C.c_void_p]),
+    "sgi_direct_lighting": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(Camera), C.c_void_p, C.c_void_p]),
+    "sgi_global_illumination": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(GBuffer), C.POINTER(Camera),
+                                            C.c_void_p, C.c_void_p, C.POINTER(FrameParams), C.c_void_p]),
+    "sgi_render_frame": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(GBuffer), C.POINTER(Camera),
+                                     C.POINTER(FrameParams), C.c_void_p, C.c_void_p]),
+    "sgi_reset_history": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "sgi_read_debug": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "sgi_set_timing": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "sgi_get_pass_times": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
+    "sgi_launch_count": (C.c_int64, [C.c_void_p]),
+    "sgi_scene_gbuffer": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(SceneCamera), C.c_int32, C.c_int32,
+                                      C.POINTER(GBuffer), C.c_void_p]),
+    "sgi_scene_csm": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(Csm), C.POINTER((C.c_float * 16) * 4), C.c_void_p]),
+    "sgi_scene_cube_atlas": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                         C.POINTER(CubeAtlas), C.c_void_p]),
+}
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False) -> C.CDLL:
+    """Loads libsgi.so (declaring every exported signature). Raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"libsgi.so is not built ({path}); run python -m stratusgfx_gb300.build")
+        _build.build()
+    lib = C.CDLL(path)
+    for name, (res, args) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class SgiError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"sgi status {status}: {msg}")
+        self.status = status
+
+
+def check(status: int, ctx=None) -> None:
+    if status != SGI_OK:
+        lib = load()
+        msg = lib.sgi_last_error(ctx).decode() if ctx else lib.sgi_status_string(status).decode()
+        raise SgiError(status, msg)

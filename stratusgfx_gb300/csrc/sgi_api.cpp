@@ -1,0 +1,494 @@
+// sgi_api.cpp - C ABI of the GI/lighting stage (include/sgi.h) and of the
+// scene generator (include/sgi_scene.h).
+//
+// Host orchestration that replaces, per frame and without any GPU->CPU sync:
+//   RendererBackend::PerformVirtualPointLightCullingStage1_  StratusRendererBackend.cpp:1578-1661
+//   RendererBackend::PerformVirtualPointLightCullingStage2_  :1666-1814 (the MapMemory readback
+//       at :1675 is gone: atlas slots travel with the compacted list on the device)
+//   RendererBackend::ComputeVirtualPointLightGlobalIllumination_ :1816-1952
+//   the deferred lighting block of RenderScene               :2011-2038
+// Status codes instead of exceptions (the reference throws at :70-72, :1083, :2659).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/sgi.h"
+#include "../../include/sgi_scene.h"
+#include "sgi_internal.h"
+
+struct sgi_ctx {
+    sgi_config cfg;
+    sgi::ShadeConfig sc;
+    std::string err;
+    int64_t launches = 0;
+    int device = 0;
+
+    // lights
+    sgi_vpl* vpls = nullptr;
+    sgi_atlas_entry* entries = nullptr;
+    int32_t num_vpls = 0;
+    sgi_point_light* points = nullptr;
+    int32_t num_points = 0;
+    bool lights_set = false;
+    bool maps_set = false;
+    sgi_csm csm;
+    sgi_cube_atlas cubes;
+
+    // culling scratch
+    uint8_t* flags = nullptr;
+    sgi_vpl* cv = nullptr;
+    sgi_atlas_entry* ce = nullptr;
+    int32_t* visible_index = nullptr;
+    sgi_tile_stage1* stage1 = nullptr;
+    int32_t* lists = nullptr;
+    int32_t num_tiles = 0;
+    bool culled = false;
+
+    // GI scratch
+    uint2* reservoir = nullptr;
+    uint2* ping[2] = {nullptr, nullptr};
+    uint2* pass_bufs[SGI_MAX_DENOISE_PASSES] = {};
+    uint2* direct = nullptr;
+    uint2* gi_hist[2] = {nullptr, nullptr};
+    uint16_t* hist_depth[2] = {nullptr, nullptr};
+    int hist_cur = 0;
+
+    // timing
+    bool timing = false;
+    cudaEvent_t ev[SGI_NUM_PASS_TIMES + 1] = {};
+    bool have_times = false;
+};
+
+namespace {
+
+sgi_status fail(sgi_ctx* c, sgi_status s, const std::string& msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+sgi_status cuda_fail(sgi_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? SGI_ERR_OOM : SGI_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define SGI_CUDA(ctx, call, what)                           \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+template <class T> cudaError_t dalloc(T** p, size_t count) {
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+size_t pixels(const sgi_config& c) { return (size_t)c.width * (size_t)c.height; }
+
+sgi_status validate_config(const sgi_config* cfg, std::string& why) {
+    if (!cfg) { why = "config is NULL"; return SGI_ERR_ARG; }
+    if (cfg->width < 1 || cfg->height < 1 || cfg->width > 16384 || cfg->height > 16384) {
+        why = "width/height must be in [1, 16384]"; return SGI_ERR_ARG;
+    }
+    if (cfg->max_vpls < 1 || cfg->max_vpls > SGI_MAX_VPLS_BEFORE_CULL) {
+        why = "max_vpls must be in [1, 10000]"; return SGI_ERR_ARG;
+    }
+    if (cfg->max_visible < 1 || cfg->max_visible > SGI_MAX_VPLS_BEFORE_CULL) {
+        why = "max_visible must be in [1, 10000]"; return SGI_ERR_ARG;
+    }
+    if (cfg->tile_size != 8 && cfg->tile_size != 16 && cfg->tile_size != 32) {
+        why = "tile_size must be 8, 16 or 32"; return SGI_ERR_ARG;
+    }
+    if (cfg->max_vpls_per_tile < 1 || cfg->max_vpls_per_tile > SGI_MAX_TILE_LIST) {
+        why = "max_vpls_per_tile must be in [1, 64]"; return SGI_ERR_ARG;
+    }
+    if (cfg->gi_mode != SGI_GI_REFERENCE && cfg->gi_mode != SGI_GI_TILED) { why = "bad gi_mode"; return SGI_ERR_ARG; }
+    if (cfg->samples_per_pixel < 0 || cfg->samples_per_pixel > 1024) {
+        why = "samples_per_pixel must be in [0, 1024]"; return SGI_ERR_ARG;
+    }
+    if (cfg->denoise_passes < 2 || cfg->denoise_passes > SGI_MAX_DENOISE_PASSES) {
+        why = "denoise_passes must be in [2, 8]"; return SGI_ERR_ARG;
+    }
+    return SGI_OK;
+}
+
+bool gbuffer_ok(const sgi_gbuffer* g, bool need_all) {
+    if (!g || !g->depth || !g->normal) return false;
+    if (!need_all) return true;
+    return g->albedo && g->base_reflectivity && g->roughness_metallic_ambient && g->velocity && g->id && g->ssao;
+}
+
+sgi::ShadeConfig make_shade(const sgi_config& c) {
+    sgi::ShadeConfig s;
+    s.min_roughness = c.min_roughness;
+    s.perceptual = c.use_perceptual_roughness;
+    s.fog_density = c.fog_density;
+    for (int k = 0; k < 3; ++k) s.fog_color[k] = c.fog_color[k];
+    s.point_ambient = c.point_light_ambient_intensity;
+    s.min_gi_occlusion = c.min_gi_occlusion_factor;
+    s.emission_strength = c.emission_strength;
+    return s;
+}
+
+void free_all(sgi_ctx* c) {
+    void* ptrs[] = {c->vpls, c->entries, c->points, c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
+                    c->reservoir, c->ping[0], c->ping[1], c->direct, c->gi_hist[0], c->gi_hist[1],
+                    c->hist_depth[0], c->hist_depth[1]};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    for (auto* p : c->pass_bufs) if (p) cudaFree(p);
+    for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+}
+
+inline void record(sgi_ctx* c, int k, cudaStream_t s) {
+    if (c->timing) cudaEventRecord(c->ev[k], s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t sgi_abi_version(void) { return SGI_ABI_VERSION; }
+
+const char* sgi_status_string(sgi_status s) {
+    switch (s) {
+        case SGI_OK: return "ok";
+        case SGI_ERR_ARG: return "invalid argument";
+        case SGI_ERR_OOM: return "out of device memory";
+        case SGI_ERR_CUDA: return "CUDA error";
+        case SGI_ERR_TIMEOUT: return "device wait timed out";
+        case SGI_ERR_CAP: return "capacity exceeded";
+        case SGI_ERR_STATE: return "invalid call order";
+        default: return "unknown status";
+    }
+}
+
+void sgi_config_defaults(sgi_config* cfg, int32_t width, int32_t height) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->width = width;
+    cfg->height = height;
+    cfg->max_vpls = SGI_MAX_VPLS_BEFORE_CULL;
+    cfg->max_visible = SGI_MAX_VPLS_PER_FRAME;
+    cfg->tile_size = 16;
+    cfg->max_vpls_per_tile = 12;
+    cfg->gi_mode = SGI_GI_REFERENCE;
+    cfg->samples_per_pixel = 0;
+    cfg->denoise_passes = 4;
+    cfg->debug_keep_passes = 0;
+    cfg->min_roughness = 0.08f;
+    cfg->use_perceptual_roughness = 1;
+    cfg->min_gi_occlusion_factor = 0.95f;
+    cfg->emission_strength = 0.0f;
+    cfg->fog_density = 0.0f;
+    cfg->fog_color[0] = cfg->fog_color[1] = cfg->fog_color[2] = 0.5f;
+    cfg->point_light_ambient_intensity = 0.003f;
+}
+
+const char* sgi_last_error(const sgi_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int64_t sgi_launch_count(const sgi_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
+    if (!out) return SGI_ERR_ARG;
+    *out = nullptr;
+    std::string why;
+    sgi_status st = validate_config(cfg, why);
+    if (st != SGI_OK) return st;
+    sgi_ctx* c = new (std::nothrow) sgi_ctx();
+    if (!c) return SGI_ERR_OOM;
+    c->cfg = *cfg;
+    c->sc = make_shade(*cfg);
+    std::memset(&c->csm, 0, sizeof(c->csm));
+    std::memset(&c->cubes, 0, sizeof(c->cubes));
+    cudaGetDevice(&c->device);
+    const int ts = cfg->tile_size;
+    c->num_tiles = ((cfg->width + ts - 1) / ts) * ((cfg->height + ts - 1) / ts);
+    const size_t P = pixels(*cfg);
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t r) { if (e == cudaSuccess && r != cudaSuccess) e = r; };
+    chk(dalloc(&c->vpls, cfg->max_vpls));
+    chk(dalloc(&c->entries, cfg->max_vpls));
+    chk(dalloc(&c->points, SGI_MAX_POINT_LIGHTS));
+    chk(dalloc(&c->flags, cfg->max_vpls));
+    chk(dalloc(&c->cv, cfg->max_visible));
+    chk(dalloc(&c->ce, cfg->max_visible));
+    chk(dalloc(&c->visible_index, 1 + (size_t)cfg->max_vpls));
+    chk(dalloc(&c->stage1, c->num_tiles));
+    chk(dalloc(&c->lists, (size_t)c->num_tiles * (1 + cfg->max_vpls_per_tile)));
+    chk(dalloc(&c->reservoir, P));
+    chk(dalloc(&c->ping[0], P));
+    chk(dalloc(&c->ping[1], P));
+    chk(dalloc(&c->direct, P));
+    chk(dalloc(&c->gi_hist[0], P));
+    chk(dalloc(&c->gi_hist[1], P));
+    chk(dalloc(&c->hist_depth[0], P));
+    chk(dalloc(&c->hist_depth[1], P));
+    if (cfg->debug_keep_passes)
+        for (int k = 0; k < cfg->denoise_passes; ++k) chk(dalloc(&c->pass_bufs[k], P));
+    for (auto& ev : c->ev) chk(cudaEventCreate(&ev));
+    if (e == cudaSuccess) chk(cudaMemset(c->visible_index, 0, sizeof(int32_t) * (1 + (size_t)cfg->max_vpls)));
+    if (e == cudaSuccess) chk(cudaMemset(c->gi_hist[0], 0, P * sizeof(uint2)));
+    if (e == cudaSuccess) chk(cudaMemset(c->gi_hist[1], 0, P * sizeof(uint2)));
+    if (e == cudaSuccess) chk(cudaMemset(c->hist_depth[0], 0, P * sizeof(uint16_t)));
+    if (e == cudaSuccess) chk(cudaMemset(c->hist_depth[1], 0, P * sizeof(uint16_t)));
+    if (e == cudaSuccess) chk(cudaDeviceSynchronize());
+    if (e != cudaSuccess) {
+        free_all(c);
+        delete c;
+        return e == cudaErrorMemoryAllocation ? SGI_ERR_OOM : SGI_ERR_CUDA;
+    }
+    *out = c;
+    return SGI_OK;
+}
+
+sgi_status sgi_destroy(sgi_ctx* ctx) {
+    if (!ctx) return SGI_ERR_ARG;
+    cudaDeviceSynchronize();
+    free_all(ctx);
+    delete ctx;
+    return SGI_OK;
+}
+
+sgi_status sgi_set_lights(sgi_ctx* ctx, const sgi_vpl* vpls, const sgi_atlas_entry* entries, int32_t num_vpls,
+                          const sgi_point_light* points, int32_t num_points, void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (num_vpls < 0 || num_points < 0) return fail(ctx, SGI_ERR_ARG, "negative light count");
+    if (num_vpls > ctx->cfg.max_vpls) return fail(ctx, SGI_ERR_CAP, "num_vpls exceeds max_vpls");
+    if (num_points > SGI_MAX_POINT_LIGHTS) return fail(ctx, SGI_ERR_CAP, "num_points exceeds 256");
+    if (num_vpls > 0 && (!vpls || !entries)) return fail(ctx, SGI_ERR_ARG, "vpls/entries NULL");
+    if (num_points > 0 && !points) return fail(ctx, SGI_ERR_ARG, "points NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (num_vpls > 0) {
+        SGI_CUDA(ctx, cudaMemcpyAsync(ctx->vpls, vpls, sizeof(sgi_vpl) * num_vpls, cudaMemcpyDefault, s), "copy vpls");
+        SGI_CUDA(ctx, cudaMemcpyAsync(ctx->entries, entries, sizeof(sgi_atlas_entry) * num_vpls, cudaMemcpyDefault, s),
+                 "copy atlas entries");
+    }
+    if (num_points > 0)
+        SGI_CUDA(ctx, cudaMemcpyAsync(ctx->points, points, sizeof(sgi_point_light) * num_points, cudaMemcpyDefault, s),
+                 "copy point lights");
+    ctx->num_vpls = num_vpls;
+    ctx->num_points = num_points;
+    ctx->lights_set = true;
+    ctx->culled = false;
+    return SGI_OK;
+}
+
+sgi_status sgi_set_shadow_maps(sgi_ctx* ctx, const sgi_csm* csm, const sgi_cube_atlas* cubes) {
+    if (!ctx || !csm || !cubes) return fail(ctx, SGI_ERR_ARG, "NULL csm or cube atlas");
+    if (!csm->depth || csm->resolution < 1 || csm->num_cascades != 4)
+        return fail(ctx, SGI_ERR_ARG, "csm needs a depth pointer, resolution >= 1 and 4 cascades");
+    if (cubes->num_atlases < 0 || cubes->num_atlases > SGI_MAX_ATLASES || cubes->face_size < 1 ||
+        cubes->layers_per_atlas < 0 || cubes->format < SGI_CUBE_F32 || cubes->format > SGI_CUBE_UNORM16)
+        return fail(ctx, SGI_ERR_ARG, "bad cube atlas description");
+    for (int a = 0; a < cubes->num_atlases; ++a)
+        if (!cubes->atlas[a]) return fail(ctx, SGI_ERR_ARG, "NULL cube atlas pointer");
+    ctx->csm = *csm;
+    ctx->cubes = *cubes;
+    ctx->maps_set = true;
+    return SGI_OK;
+}
+
+sgi_status sgi_cull_vpls(sgi_ctx* ctx, void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (!ctx->lights_set || !ctx->maps_set) return fail(ctx, SGI_ERR_STATE, "set lights and shadow maps first");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (ctx->num_vpls == 0) {
+        SGI_CUDA(ctx, cudaMemsetAsync(ctx->visible_index, 0, sizeof(int32_t), s), "clear visible count");
+    } else {
+        SGI_CUDA(ctx, sgi::launch_vis_flags(ctx->vpls, ctx->num_vpls, ctx->csm, ctx->flags, s), "vpl_vis_flags");
+        SGI_CUDA(ctx, sgi::launch_compact(ctx->vpls, ctx->entries, ctx->flags, ctx->num_vpls, ctx->cfg.max_visible,
+                                          ctx->cv, ctx->ce, ctx->visible_index, s), "vpl_compact");
+        ctx->launches += 2;
+    }
+    ctx->culled = true;
+    return SGI_OK;
+}
+
+sgi_status sgi_cull_tiles(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera* cam, void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (!gbuffer_ok(gbuf, false) || !cam) return fail(ctx, SGI_ERR_ARG, "NULL G-buffer depth/normal or camera");
+    if (!ctx->culled) return fail(ctx, SGI_ERR_STATE, "sgi_cull_vpls must run before sgi_cull_tiles");
+    cudaStream_t s = (cudaStream_t)stream;
+    SGI_CUDA(ctx, sgi::launch_tile_stage1(ctx->cfg, *gbuf, *cam, ctx->stage1, s), "tile_stage1");
+    SGI_CUDA(ctx, sgi::launch_tile_stage2(ctx->cfg, ctx->stage1, ctx->cv, ctx->visible_index, ctx->lists, s),
+             "tile_stage2");
+    ctx->launches += 2;
+    return SGI_OK;
+}
+
+sgi_status sgi_direct_lighting(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera* cam, void* hdr_out,
+                               void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (!gbuffer_ok(gbuf, true) || !cam || !hdr_out) return fail(ctx, SGI_ERR_ARG, "NULL G-buffer, camera or output");
+    if (!ctx->lights_set || !ctx->maps_set) return fail(ctx, SGI_ERR_STATE, "set lights and shadow maps first");
+    SGI_CUDA(ctx, sgi::launch_deferred(ctx->cfg, ctx->sc, *gbuf, *cam, ctx->points, ctx->num_points, ctx->csm,
+                                       (uint2*)hdr_out, (cudaStream_t)stream), "deferred_pbr_csm");
+    ctx->launches += 1;
+    return SGI_OK;
+}
+
+static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer* prev, const sgi_camera* cam,
+                         const void* hdr_in, void* hdr_out, const sgi_frame_params* params, cudaStream_t s,
+                         int ev_gather) {
+    const sgi_config& cfg = ctx->cfg;
+    SGI_CUDA(ctx, sgi::launch_gather(cfg, ctx->sc, *cur, *cam, ctx->cv, ctx->ce, ctx->visible_index, ctx->lists,
+                                     ctx->cubes, params->time, ctx->reservoir, s), "vpl_gather");
+    ctx->launches += 1;
+    record(ctx, ev_gather + 1, s);
+    sgi::DenoiseLaunch d;
+    std::memset(&d, 0, sizeof(d));
+    d.width = cfg.width; d.height = cfg.height; d.passes = cfg.denoise_passes;
+    d.time = params->time; d.fps = params->frames_per_second;
+    d.cur = *cur;
+    d.prev_depth = prev->depth; d.prev_normal = prev->normal; d.prev_id = prev->id;
+    d.hdr_in = (const uint2*)hdr_in; d.hdr_out = (uint2*)hdr_out;
+    d.gi_prev = ctx->gi_hist[ctx->hist_cur]; d.gi_out = ctx->gi_hist[1 - ctx->hist_cur];
+    d.hist_prev = ctx->hist_depth[ctx->hist_cur]; d.hist_out = ctx->hist_depth[1 - ctx->hist_cur];
+    d.visible_index = ctx->visible_index;
+    const uint2* in = ctx->reservoir;
+    for (int pass = 0; pass < cfg.denoise_passes; ++pass) {
+        const bool final = pass == cfg.denoise_passes - 1;
+        uint2* out = cfg.debug_keep_passes ? ctx->pass_bufs[pass] : (final ? nullptr : ctx->ping[pass & 1]);
+        d.pass = pass; d.res_in = in; d.res_out = out;
+        SGI_CUDA(ctx, sgi::launch_denoise_pass(d, s), "denoise_pass");
+        ctx->launches += 1;
+        in = out;
+    }
+    ctx->hist_cur = 1 - ctx->hist_cur;
+    return SGI_OK;
+}
+
+static bool frame_args_ok(const sgi_gbuffer* cur, const sgi_gbuffer* prev, const sgi_camera* cam,
+                          const sgi_frame_params* params) {
+    return gbuffer_ok(cur, true) && prev && prev->depth && prev->normal && prev->id && cam && params &&
+           params->frames_per_second > 0.0f;
+}
+
+sgi_status sgi_global_illumination(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer* prev,
+                                   const sgi_camera* cam, const void* hdr_in, void* hdr_out,
+                                   const sgi_frame_params* params, void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (!frame_args_ok(cur, prev, cam, params) || !hdr_in || !hdr_out)
+        return fail(ctx, SGI_ERR_ARG, "NULL frame argument or frames_per_second <= 0");
+    if (!ctx->culled || !ctx->maps_set) return fail(ctx, SGI_ERR_STATE, "cull VPLs (and tiles) first");
+    return run_gi(ctx, cur, prev, cam, hdr_in, hdr_out, params, (cudaStream_t)stream, 2);
+}
+
+sgi_status sgi_render_frame(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer* prev, const sgi_camera* cam,
+                            const sgi_frame_params* params, void* hdr_out, void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (!frame_args_ok(cur, prev, cam, params) || !hdr_out)
+        return fail(ctx, SGI_ERR_ARG, "NULL frame argument or frames_per_second <= 0");
+    cudaStream_t s = (cudaStream_t)stream;
+    record(ctx, 0, s);
+    sgi_status st = sgi_cull_vpls(ctx, stream);
+    if (st != SGI_OK) return st;
+    record(ctx, 1, s);
+    st = sgi_direct_lighting(ctx, cur, cam, ctx->direct, stream);
+    if (st != SGI_OK) return st;
+    record(ctx, 2, s);
+    if (ctx->cfg.gi_mode == SGI_GI_TILED) {
+        st = sgi_cull_tiles(ctx, cur, cam, stream);
+        if (st != SGI_OK) return st;
+    }
+    record(ctx, 3, s);
+    st = run_gi(ctx, cur, prev, cam, ctx->direct, hdr_out, params, s, 3);
+    if (st != SGI_OK) return st;
+    record(ctx, 5, s);
+    ctx->have_times = ctx->timing;
+    return SGI_OK;
+}
+
+sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t P = pixels(ctx->cfg);
+    for (int k = 0; k < 2; ++k) {
+        SGI_CUDA(ctx, cudaMemsetAsync(ctx->gi_hist[k], 0, P * sizeof(uint2), s), "clear gi history");
+        SGI_CUDA(ctx, cudaMemsetAsync(ctx->hist_depth[k], 0, P * sizeof(uint16_t), s), "clear history depth");
+    }
+    ctx->hist_cur = 0;
+    return SGI_OK;
+}
+
+sgi_status sgi_read_debug(sgi_ctx* ctx, int32_t which, void* host_dst, size_t bytes, size_t* needed) {
+    if (!ctx) return SGI_ERR_ARG;
+    const size_t P = pixels(ctx->cfg);
+    const void* src = nullptr;
+    size_t size = 0;
+    switch (which) {
+        case SGI_DEBUG_VISIBLE_INDEX: src = ctx->visible_index; size = sizeof(int32_t) * (1 + (size_t)ctx->cfg.max_vpls); break;
+        case SGI_DEBUG_COMPACT_VPLS: src = ctx->cv; size = sizeof(sgi_vpl) * ctx->cfg.max_visible; break;
+        case SGI_DEBUG_COMPACT_ENTRIES: src = ctx->ce; size = sizeof(sgi_atlas_entry) * ctx->cfg.max_visible; break;
+        case SGI_DEBUG_TILE_STAGE1: src = ctx->stage1; size = sizeof(sgi_tile_stage1) * ctx->num_tiles; break;
+        case SGI_DEBUG_TILE_LISTS:
+            src = ctx->lists; size = sizeof(int32_t) * ctx->num_tiles * (1 + (size_t)ctx->cfg.max_vpls_per_tile); break;
+        case SGI_DEBUG_RESERVOIR: src = ctx->reservoir; size = P * sizeof(uint2); break;
+        case SGI_DEBUG_GI_HISTORY: src = ctx->gi_hist[ctx->hist_cur]; size = P * sizeof(uint2); break;
+        case SGI_DEBUG_HISTORY_DEPTH: src = ctx->hist_depth[ctx->hist_cur]; size = P * sizeof(uint16_t); break;
+        case SGI_DEBUG_DIRECT: src = ctx->direct; size = P * sizeof(uint2); break;
+        default:
+            if (which >= SGI_DEBUG_PASS_BASE && which < SGI_DEBUG_PASS_BASE + ctx->cfg.denoise_passes &&
+                ctx->pass_bufs[which - SGI_DEBUG_PASS_BASE]) {
+                src = ctx->pass_bufs[which - SGI_DEBUG_PASS_BASE];
+                size = P * sizeof(uint2);
+            } else {
+                return fail(ctx, SGI_ERR_ARG, "unknown debug buffer (pass buffers need debug_keep_passes)");
+            }
+    }
+    if (needed) *needed = size;
+    if (!host_dst) return SGI_OK;
+    SGI_CUDA(ctx, cudaDeviceSynchronize(), "synchronize before debug read");
+    SGI_CUDA(ctx, cudaMemcpy(host_dst, src, bytes < size ? bytes : size, cudaMemcpyDeviceToHost), "debug read");
+    return SGI_OK;
+}
+
+sgi_status sgi_set_timing(sgi_ctx* ctx, int32_t enabled) {
+    if (!ctx) return SGI_ERR_ARG;
+    ctx->timing = enabled != 0;
+    ctx->have_times = false;
+    return SGI_OK;
+}
+
+sgi_status sgi_get_pass_times(sgi_ctx* ctx, float* ms, int32_t n) {
+    if (!ctx || !ms || n < 1) return SGI_ERR_ARG;
+    if (!ctx->have_times) return fail(ctx, SGI_ERR_STATE, "no timed sgi_render_frame yet");
+    SGI_CUDA(ctx, cudaEventSynchronize(ctx->ev[SGI_NUM_PASS_TIMES]), "event sync");
+    for (int k = 0; k < SGI_NUM_PASS_TIMES && k < n; ++k) {
+        float t = 0.0f;
+        SGI_CUDA(ctx, cudaEventElapsedTime(&t, ctx->ev[k], ctx->ev[k + 1]), "event elapsed");
+        ms[k] = t;
+    }
+    return SGI_OK;
+}
+
+// ------------------------------------------------------------ scene ABI --
+sgi_status sgi_scene_gbuffer(const sgi_box* boxes, int32_t num_boxes, const sgi_scene_camera* cam, int32_t width,
+                             int32_t height, const sgi_gbuffer* out, void* stream) {
+    if (!boxes || num_boxes < 1 || !cam || width < 1 || height < 1 || !gbuffer_ok(out, true)) return SGI_ERR_ARG;
+    cudaError_t e = sgi::launch_scene_gbuffer(boxes, num_boxes, *cam, width, height, *out, (cudaStream_t)stream);
+    return e == cudaSuccess ? SGI_OK : (e == cudaErrorInvalidValue ? SGI_ERR_CAP : SGI_ERR_CUDA);
+}
+
+sgi_status sgi_scene_csm(const sgi_box* boxes, int32_t num_boxes, const sgi_csm* csm,
+                         const float inv_cascade_proj_view[4][16], void* stream) {
+    if (!boxes || num_boxes < 1 || !csm || !csm->depth || csm->resolution < 1 || csm->num_cascades != 4 ||
+        !inv_cascade_proj_view)
+        return SGI_ERR_ARG;
+    cudaError_t e = sgi::launch_scene_csm(boxes, num_boxes, *csm, inv_cascade_proj_view, (cudaStream_t)stream);
+    return e == cudaSuccess ? SGI_OK : (e == cudaErrorInvalidValue ? SGI_ERR_CAP : SGI_ERR_CUDA);
+}
+
+sgi_status sgi_scene_cube_atlas(const sgi_box* boxes, int32_t num_boxes, const sgi_vpl* vpls,
+                                const sgi_atlas_entry* entries, int32_t count, const sgi_cube_atlas* atlas,
+                                void* stream) {
+    if (!boxes || num_boxes < 1 || !vpls || !entries || count < 0 || !atlas || atlas->face_size < 1)
+        return SGI_ERR_ARG;
+    if (count == 0) return SGI_OK;
+    cudaError_t e = sgi::launch_scene_cubes(boxes, num_boxes, vpls, entries, count, *atlas, (cudaStream_t)stream);
+    return e == cudaSuccess ? SGI_OK : (e == cudaErrorInvalidValue ? SGI_ERR_CAP : SGI_ERR_CUDA);
+}
+
+}  // extern "C"

@@ -1,0 +1,69 @@
+// sgi_internal.h - launch wrappers shared by the host layer (sgi_api.cpp) and
+// the CUDA translation units. Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/sgi.h"
+#include "../../include/sgi_scene.h"
+
+namespace sgi {
+
+// Device-side constants of the shading passes (RendererSettings subset).
+struct ShadeConfig {
+    float min_roughness;
+    int32_t perceptual;
+    float fog_density;
+    float fog_color[3];
+    float point_ambient;
+    float min_gi_occlusion;
+    float emission_strength;
+};
+
+struct DenoiseLaunch {
+    int32_t width, height;
+    int32_t pass;            // 0 .. passes-1
+    int32_t passes;
+    float time;
+    float fps;
+    sgi_gbuffer cur;         // depth, normal, albedo, velocity, id of this frame
+    const float* prev_depth;
+    const uint32_t* prev_normal;
+    const float* prev_id;
+    const uint2* res_in;     // RGBA16F reservoir of the previous pass (gather output for pass 0)
+    uint2* res_out;          // RGBA16F (may be null on the final pass)
+    const uint2* hdr_in;     // screen, RGB16F
+    uint2* hdr_out;          // combined, RGB16F (final pass)
+    const uint2* gi_prev;    // prevIndirectIllumination, RGB16F
+    uint2* gi_out;           // giColor, RGB16F (final pass)
+    const uint16_t* hist_prev;  // historyDepth, R16F
+    uint16_t* hist_out;         // newHistoryDepth, R16F (final pass)
+    const int32_t* visible_index;  // [0] = numVisible
+};
+
+cudaError_t launch_vis_flags(const sgi_vpl* vpls, int32_t n, const sgi_csm& csm, uint8_t* flags, cudaStream_t s);
+cudaError_t launch_compact(const sgi_vpl* vpls, const sgi_atlas_entry* entries, const uint8_t* flags, int32_t n,
+                           int32_t cap, sgi_vpl* cv, sgi_atlas_entry* ce, int32_t* visible_index, cudaStream_t s);
+cudaError_t launch_tile_stage1(const sgi_config& cfg, const sgi_gbuffer& g, const sgi_camera& cam,
+                               sgi_tile_stage1* out, cudaStream_t s);
+cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1, const sgi_vpl* cv,
+                               const int32_t* visible_index, int32_t* lists, cudaStream_t s);
+cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam,
+                          const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index,
+                          const int32_t* lists, const sgi_cube_atlas& cubes, float time, uint2* reservoir,
+                          cudaStream_t s);
+cudaError_t launch_denoise_pass(const DenoiseLaunch& d, cudaStream_t s);
+cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
+                            const sgi_camera& cam, const sgi_point_light* points, int32_t num_points,
+                            const sgi_csm& csm, uint2* hdr_out, cudaStream_t s);
+
+// scene generation (sgi_scene.cu)
+cudaError_t launch_scene_gbuffer(const sgi_box* boxes, int32_t nb, const sgi_scene_camera& cam, int32_t W,
+                                 int32_t H, const sgi_gbuffer& out, cudaStream_t s);
+cudaError_t launch_scene_csm(const sgi_box* boxes, int32_t nb, const sgi_csm& csm, const float (*inv)[16],
+                             cudaStream_t s);
+cudaError_t launch_scene_cubes(const sgi_box* boxes, int32_t nb, const sgi_vpl* vpls, const sgi_atlas_entry* entries,
+                               int32_t count, const sgi_cube_atlas& atlas, cudaStream_t s);
+
+}  // namespace sgi

@@ -1,0 +1,687 @@
+// sgi_kernels.cu - the GI/lighting hot path on sm_103a.
+//
+// Kernels (reference shader each restates, paths relative to the StratusGFX root):
+//   vpl_vis_flags / vpl_compact  viscull_vpls.cs:47-120
+//   tile_stage1                  vpl_tiled_deferred_culling_stage1.cs:50-90
+//   tile_stage2                  vpl_tiled_deferred_culling_stage2.cs:61-129
+//   vpl_gather                   vpl_pbr_gi.fs:81-207
+//   denoise_pass                 vpl_pbr_gi_denoise.fs:142-435
+//   deferred_pbr_csm             pbr.fs:82-145 (+ pbr.glsl:158-227)
+//
+// Compiled with -fmad=false (see sgi_math.cuh): results are bit-reproducible.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sgi_internal.h"
+#include "sgi_math.cuh"
+
+namespace sgi {
+
+// ------------------------------------------------------------------ texels --
+SGI_D uint2 ld_u2(const uint2* p, size_t i) { return __ldg(p + i); }
+SGI_D void unpack_h4(uint2 t, float& a, float& b, float& c, float& d) {
+    a = h2f((uint16_t)(t.x & 0xffffu)); b = h2f((uint16_t)(t.x >> 16));
+    c = h2f((uint16_t)(t.y & 0xffffu)); d = h2f((uint16_t)(t.y >> 16));
+}
+SGI_D uint2 pack_h4(float a, float b, float c, float d) {
+    return make_uint2((uint32_t)f2h(a) | ((uint32_t)f2h(b) << 16), (uint32_t)f2h(c) | ((uint32_t)f2h(d) << 16));
+}
+
+// Bilinear sample (LINEAR, CLAMP_TO_EDGE) at uv of a scalar image.
+template <class F> SGI_D float bilinear(F fetch, int W, int H, float s, float t) {
+    float u = s * float(W) - 0.5f, v = t * float(H) - 0.5f;
+    float fu = floorf(u), fv = floorf(v);
+    float a = u - fu, b = v - fv;
+    int i0 = tex_index(fu, W), i1 = tex_index(fu + 1.0f, W);
+    int j0 = tex_index(fv, H), j1 = tex_index(fv + 1.0f, H);
+    float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    return ((fetch(i0, j0) * w00 + fetch(i1, j0) * w10) + fetch(i0, j1) * w01) + fetch(i1, j1) * w11;
+}
+
+// ------------------------------------------------------------------- CSM --
+// texture(sampler2DArrayShadow) with LINEAR + LEQUAL: bilinear weights over
+// the four 0/1 compare results.
+SGI_D float csm_pcf(const float* __restrict__ base, int R, float s, float t, float ref) {
+    float u = s * float(R) - 0.5f, v = t * float(R) - 0.5f;
+    float fu = floorf(u), fv = floorf(v);
+    float a = u - fu, b = v - fv;
+    int i0 = tex_index(fu, R), i1 = tex_index(fu + 1.0f, R);
+    int j0 = tex_index(fv, R), j1 = tex_index(fv + 1.0f, R);
+    float c00 = ref <= __ldg(base + (size_t)j0 * R + i0) ? 1.0f : 0.0f;
+    float c10 = ref <= __ldg(base + (size_t)j0 * R + i1) ? 1.0f : 0.0f;
+    float c01 = ref <= __ldg(base + (size_t)j1 * R + i0) ? 1.0f : 0.0f;
+    float c11 = ref <= __ldg(base + (size_t)j1 * R + i1) ? 1.0f : 0.0f;
+    float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    return ((c00 * w00 + c10 * w10) + c01 * w01) + c11 * w11;
+}
+
+// calculateInfiniteShadowValue, pbr.glsl:158-227: lit fraction.
+SGI_D float infinite_shadow(const sgi_csm& csm, V3 fragPos, V3 normal, bool useDepthBias) {
+    V3 blends = v3(dot4(csm.cascade_planes[0], fragPos), dot4(csm.cascade_planes[1], fragPos),
+                   dot4(csm.cascade_planes[2], fragPos));
+    float bias = csm.depth_bias / (csm.zfar - csm.znear);
+    if (!useDepthBias) bias = 0.0f;
+    V3 L = v3(csm.light_direction[0], csm.light_direction[1], csm.light_direction[2]);
+    V3 position = fragPos + normal * (1.0f - saturate(dot(normal, L))) * 1.0f;
+    bool beyond2 = blends.y >= 0.0f;
+    bool beyond3 = blends.z >= 0.0f;
+    int index1 = beyond2 ? 2 : 0;
+    int index2 = beyond3 ? 3 : 1;
+    V4 c1 = mat4_mul(csm.cascade_proj_view[index1], position.x, position.y, position.z, 1.0f);
+    V4 c2 = mat4_mul(csm.cascade_proj_view[index2], position.x, position.y, position.z, 1.0f);
+    V3 cc1 = v3(c1.x / c1.w, c1.y / c1.w, c1.z / c1.w) * 0.5f + v3s(0.5f);
+    V3 cc2 = v3(c2.x / c2.w, c2.y / c2.w, c2.z / c2.w) * 0.5f + v3s(0.5f);
+    float depth1 = cc1.z;
+    float depth2 = beyond3 ? saturate(cc2.z) : cc2.z;
+    float weight = beyond2 ? saturate(blends.y) - saturate(blends.z) : 1.0f - saturate(blends.x);
+    const int R = csm.resolution;
+    float wh = 1.0f / float(R);
+    const float* b1 = csm.depth + (size_t)index1 * R * R;
+    const float* b2 = csm.depth + (size_t)index2 * R * R;
+    float ref1 = depth1 - bias, ref2 = depth2 - bias;
+    float light1 = 0.0f, light2 = 0.0f, samples = 0.0f;
+#pragma unroll
+    for (int yi = -1; yi <= 1; ++yi) {
+#pragma unroll
+        for (int xi = -1; xi <= 1; ++xi) {
+            float ox = float(xi) * wh, oy = float(yi) * wh;
+            light1 += csm_pcf(b1, R, cc1.x + ox, cc1.y + oy, ref1);
+            light2 += csm_pcf(b2, R, cc2.x + ox, cc2.y + oy, ref2);
+            samples += 1.0f;
+        }
+    }
+    return mixf(light2, light1, weight) * (1.0f / samples);
+}
+
+// ------------------------------------------------------------- cube maps --
+SGI_D float cube_fetch(const sgi_cube_atlas& at, sgi_atlas_entry e, V3 d) {
+    if (e.index < 0 || e.index >= at.num_atlases || e.layer < 0 || e.layer >= at.layers_per_atlas) return 1.0f;
+    float ax = gabs(d.x), ay = gabs(d.y), az = gabs(d.z);
+    int face; float sc, tc, ma;
+    if (ax >= ay && ax >= az) {
+        ma = ax;
+        if (d.x >= 0.0f) { face = 0; sc = -d.z; tc = -d.y; } else { face = 1; sc = d.z; tc = -d.y; }
+    } else if (ay >= az) {
+        ma = ay;
+        if (d.y >= 0.0f) { face = 2; sc = d.x; tc = d.z; } else { face = 3; sc = d.x; tc = -d.z; }
+    } else {
+        ma = az;
+        if (d.z >= 0.0f) { face = 4; sc = d.x; tc = -d.y; } else { face = 5; sc = -d.x; tc = -d.y; }
+    }
+    float s = 0.5f * (sc / ma + 1.0f);
+    float t = 0.5f * (tc / ma + 1.0f);
+    const int n = at.face_size;
+    int i = nearest_index(s, n), j = nearest_index(t, n);
+    size_t off = (((size_t)e.layer * 6 + face) * n + j) * n + i;
+    const void* base = at.atlas[e.index];
+    if (at.format == SGI_CUBE_F16) return h2f(__ldg((const unsigned short*)base + off));
+    if (at.format == SGI_CUBE_F32) return __ldg((const float*)base + off);
+    return float(__ldg((const unsigned short*)base + off)) / 65535.0f;
+}
+
+// calculateShadowValue1Sample, pbr.glsl:116-136 (1 = occluded)
+SGI_D float shadow_1sample(const sgi_cube_atlas& at, sgi_atlas_entry e, float farPlane, V3 fragPos, V3 lightPos,
+                           float lightNormalDot, float minBias) {
+    V3 fragDir = fragPos - lightPos;
+    float currentDepth = length(fragDir);
+    float bias = currentDepth * gmax(minBias, saturate(lightNormalDot) * 0.03f);
+    float depth = cube_fetch(at, e, fragDir);
+    depth = depth * farPlane;
+    return (currentDepth - bias) > depth ? 1.0f : 0.0f;
+}
+
+// =========================================================== VPL vis cull --
+__global__ void vpl_vis_flags_kernel(const sgi_vpl* __restrict__ vpls, int n, sgi_csm csm,
+                                     uint8_t* __restrict__ flags) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 pos = __ldg(reinterpret_cast<const float4*>(vpls + i));
+    V3 p = v3(pos.x, pos.y, pos.z);
+    V3 L = v3(csm.light_direction[0], csm.light_direction[1], csm.light_direction[2]);
+    float shadowFactor = 1.0f - infinite_shadow(csm, p, L, false);
+    flags[i] = shadowFactor < 1.0f ? 1 : 0;
+}
+
+// Stable compaction in ascending VPL index by one 1024-thread block: ballot
+// prefix within each warp, exclusive scan of the 32 warp counts, running base
+// across chunks of 1024 flags. Replaces the 8-thread atomicAdd loop of
+// viscull_vpls.cs:85-98 (whose order is nondeterministic).
+__global__ void __launch_bounds__(1024) vpl_compact_kernel(const sgi_vpl* __restrict__ vpls,
+                                                           const sgi_atlas_entry* __restrict__ entries,
+                                                           const uint8_t* __restrict__ flags, int n, int cap,
+                                                           sgi_vpl* __restrict__ cv, sgi_atlas_entry* __restrict__ ce,
+                                                           int32_t* __restrict__ visible_index) {
+    __shared__ int warp_count[32];
+    __shared__ int warp_base[32];
+    __shared__ int chunk_total;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int base = 0;
+    for (int start = 0; start < n; start += 1024) {
+        int i = start + tid;
+        bool f = i < n && flags[i] != 0;
+        unsigned m = __ballot_sync(0xffffffffu, f);
+        int within = __popc(m & ((1u << lane) - 1u));
+        if (lane == 0) warp_count[warp] = __popc(m);
+        __syncthreads();
+        if (warp == 0) {
+            int c = warp_count[lane];
+            int incl = c;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += t;
+            }
+            warp_base[lane] = incl - c;
+            if (lane == 31) chunk_total = incl;
+        }
+        __syncthreads();
+        if (f) {
+            int k = base + warp_base[warp] + within;
+            if (k < cap) {
+                const float4* src = reinterpret_cast<const float4*>(vpls + i);
+                float4* dst = reinterpret_cast<float4*>(cv + k);
+                dst[0] = __ldg(src); dst[1] = __ldg(src + 1); dst[2] = __ldg(src + 2); dst[3] = __ldg(src + 3);
+                ce[k] = entries[i];
+                visible_index[1 + k] = i;
+            }
+        }
+        base += chunk_total;
+        __syncthreads();
+    }
+    if (tid == 0) visible_index[0] = base < cap ? base : cap;
+}
+
+cudaError_t launch_vis_flags(const sgi_vpl* vpls, int32_t n, const sgi_csm& csm, uint8_t* flags, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    vpl_vis_flags_kernel<<<(n + 127) / 128, 128, 0, s>>>(vpls, n, csm, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact(const sgi_vpl* vpls, const sgi_atlas_entry* entries, const uint8_t* flags, int32_t n,
+                           int32_t cap, sgi_vpl* cv, sgi_atlas_entry* ce, int32_t* visible_index, cudaStream_t s) {
+    vpl_compact_kernel<<<1, 1024, 0, s>>>(vpls, entries, flags, n, cap, cv, ce, visible_index);
+    return cudaGetLastError();
+}
+
+// ============================================================ tile cull --
+// Stage 1: one block per tile (tile_size^2 threads). Per-tile mean world
+// position and normalised mean normal; the sums use the warp butterfly order
+// (xor 16, 8, 4, 2, 1, then xor nw/2 .. 1 over the warp totals).
+SGI_D float butterfly(float v) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+__global__ void tile_stage1_kernel(int W, int H, int ts, int tiles_x, sgi_gbuffer g, sgi_camera cam,
+                                   sgi_tile_stage1* __restrict__ out) {
+    __shared__ float wsum[32][6];
+    const int tile = blockIdx.x;
+    const int tx = tile % tiles_x, ty = tile / tiles_x;
+    const int l = threadIdx.x;
+    const int x = tx * ts + l % ts, y = ty * ts + l / ts;
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (x < W && y < H) {
+        size_t i = (size_t)y * W + x;
+        float u = (float(x) + 0.5f) / float(W), vv = (float(y) + 0.5f) / float(H);
+        V3 p = world_from_depth(u, vv, __ldg(g.depth + i), cam.inv_proj_view);
+        V3 n = decode_normal(__ldg(g.normal + i));
+        v[0] = p.x; v[1] = p.y; v[2] = p.z; v[3] = n.x; v[4] = n.y; v[5] = n.z;
+    }
+    const int lane = l & 31, warp = l >> 5, nw = (ts * ts) >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) v[c] = butterfly(v[c]);
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) wsum[warp][c] = v[c];
+    }
+    __syncthreads();
+    if (warp == 0) {
+        float w[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) w[c] = lane < nw ? wsum[lane][c] : 0.0f;
+        for (int off = nw >> 1; off >= 1; off >>= 1) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) w[c] = w[c] + __shfl_xor_sync(0xffffffffu, w[c], off);
+        }
+        if (lane == 0) {
+            int cx = W - tx * ts < ts ? W - tx * ts : ts;
+            int cy = H - ty * ts < ts ? H - ty * ts : ts;
+            float cnt = float(cx * cy);
+            V3 ap = v3(w[0], w[1], w[2]) / cnt;
+            V3 an = v3(w[3], w[4], w[5]) / cnt;
+            an = normalize(an);
+            sgi_tile_stage1 o;
+            o.average_position[0] = ap.x; o.average_position[1] = ap.y; o.average_position[2] = ap.z;
+            o.average_position[3] = 1.0f;
+            o.average_normal[0] = an.x; o.average_normal[1] = an.y; o.average_normal[2] = an.z;
+            o.average_normal[3] = 1.0f;
+            out[tile] = o;
+        }
+    }
+}
+
+cudaError_t launch_tile_stage1(const sgi_config& cfg, const sgi_gbuffer& g, const sgi_camera& cam,
+                               sgi_tile_stage1* out, cudaStream_t s) {
+    const int ts = cfg.tile_size;
+    const int tx = (cfg.width + ts - 1) / ts, ty = (cfg.height + ts - 1) / ts;
+    tile_stage1_kernel<<<tx * ty, ts * ts, 0, s>>>(cfg.width, cfg.height, ts, tx, g, cam, out);
+    return cudaGetLastError();
+}
+
+// Stage 2: one warp per tile, 8 tiles per block. The candidate list (L <= 64
+// slots, key = distance/radius) lives in registers, slot s in lane s % 32.
+// VPLs are visited in ascending compacted index; a candidate is inserted iff
+// its key is strictly below the current L-th key, at the position after all
+// keys <= it (strict '<' of vpl_tiled_deferred_culling_stage2.cs:100-121), so
+// the list equals the first L of the stable sort by key.
+constexpr int kStage2Chunk = 1024;
+
+__global__ void __launch_bounds__(256) tile_stage2_kernel(int num_tiles, int L,
+                                                          const sgi_tile_stage1* __restrict__ s1,
+                                                          const sgi_vpl* __restrict__ cv,
+                                                          const int32_t* __restrict__ visible_index,
+                                                          int32_t* __restrict__ lists) {
+    __shared__ float4 sv[kStage2Chunk];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tile = blockIdx.x * (blockDim.x >> 5) + warp;
+    const bool active = tile < num_tiles;
+    const int count = __ldg(visible_index);
+    V3 fragPos = v3s(0.0f), normal = v3s(0.0f);
+    if (active) {
+        fragPos = v3(s1[tile].average_position[0], s1[tile].average_position[1], s1[tile].average_position[2]);
+        normal = v3(s1[tile].average_normal[0], s1[tile].average_normal[1], s1[tile].average_normal[2]);
+    }
+    float k0 = kFloatMax, k1 = kFloatMax;
+    int i0 = -1, i1 = -1;
+    int num = 0;
+    float thresh = kFloatMax;
+    for (int base = 0; base < count; base += kStage2Chunk) {
+        const int cn = count - base < kStage2Chunk ? count - base : kStage2Chunk;
+        __syncthreads();
+        for (int j = threadIdx.x; j < cn; j += blockDim.x) {
+            const float* rec = reinterpret_cast<const float*>(cv + base + j);
+            sv[j] = make_float4(__ldg(rec + 0), __ldg(rec + 1), __ldg(rec + 2), __ldg(rec + 12));
+        }
+        __syncthreads();
+        if (!active) continue;
+        for (int j = 0; j < cn; j += 32) {
+            bool cand = false;
+            float ratio = 0.0f;
+            if (j + lane < cn) {
+                float4 lv = sv[j + lane];
+                V3 lmf = v3(lv.x, lv.y, lv.z) - fragPos;
+                float side = dot(normal, lmf);
+                if (!(side < 0.0f)) {
+                    float d = length(lmf);
+                    ratio = d / lv.w;
+                    cand = !(ratio > 1.0f) && ratio < thresh;
+                }
+            }
+            unsigned m = __ballot_sync(FULL, cand);
+            while (m) {
+                const int b = __ffs(m) - 1;
+                m &= m - 1u;
+                const float r = __shfl_sync(FULL, ratio, b);
+                if (!(r < thresh)) continue;
+                const int p = __popc(__ballot_sync(FULL, k0 <= r)) + __popc(__ballot_sync(FULL, k1 <= r));
+                float k0u = __shfl_up_sync(FULL, k0, 1);
+                int i0u = __shfl_up_sync(FULL, i0, 1);
+                float k1u = __shfl_up_sync(FULL, k1, 1);
+                int i1u = __shfl_up_sync(FULL, i1, 1);
+                const float k31 = __shfl_sync(FULL, k0, 31);
+                const int i31 = __shfl_sync(FULL, i0, 31);
+                if (lane == 0) { k1u = k31; i1u = i31; }
+                const int kidx = base + j + b;
+                const int s0 = lane, s1i = lane + 32;
+                if (s0 < L) {
+                    if (s0 == p) { k0 = r; i0 = kidx; } else if (s0 > p) { k0 = k0u; i0 = i0u; }
+                }
+                if (s1i < L) {
+                    if (s1i == p) { k1 = r; i1 = kidx; } else if (s1i > p) { k1 = k1u; i1 = i1u; }
+                }
+                num = num + 1 < L ? num + 1 : L;
+                thresh = (L - 1) < 32 ? __shfl_sync(FULL, k0, L - 1) : __shfl_sync(FULL, k1, L - 33);
+            }
+        }
+    }
+    if (!active) return;
+    int32_t* o = lists + (size_t)tile * (1 + L);
+    if (lane == 0) o[0] = num;
+    if (lane < L) o[1 + lane] = lane < num ? i0 : -1;
+    if (lane + 32 < L) o[33 + lane] = lane + 32 < num ? i1 : -1;
+}
+
+cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1, const sgi_vpl* cv,
+                               const int32_t* visible_index, int32_t* lists, cudaStream_t s) {
+    const int ts = cfg.tile_size;
+    const int T = ((cfg.width + ts - 1) / ts) * ((cfg.height + ts - 1) / ts);
+    tile_stage2_kernel<<<(T + 7) / 8, 256, 0, s>>>(T, cfg.max_vpls_per_tile, s1, cv, visible_index, lists);
+    return cudaGetLastError();
+}
+
+// ================================================================ gather --
+struct GatherParams {
+    int W, H, ts, tiles_x, L, tiled, spp;
+    ShadeConfig sc;
+    sgi_gbuffer g;
+    sgi_camera cam;
+    const sgi_vpl* cv;
+    const sgi_atlas_entry* ce;
+    const int32_t* visible_index;
+    const int32_t* lists;
+    sgi_cube_atlas cubes;
+    float time;
+    uint2* reservoir;
+};
+
+// vpl_pbr_gi.fs:81-207, one thread per pixel.
+__global__ void __launch_bounds__(256) vpl_gather_kernel(GatherParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= p.W || y >= p.H) return;
+    const size_t i = (size_t)y * p.W + x;
+    ShadeParams sp{p.sc.min_roughness, p.sc.perceptual, p.sc.fog_density,
+                   {p.sc.fog_color[0], p.sc.fog_color[1], p.sc.fog_color[2]}, p.sc.point_ambient};
+    const float u = (float(x) + 0.5f) / float(p.W), v = (float(y) + 0.5f) / float(p.H);
+    const V3 fragPos = world_from_depth(u, v, __ldg(p.g.depth + i), p.cam.inv_proj_view);
+    const V3 viewPos = v3(p.cam.view_position[0], p.cam.view_position[1], p.cam.view_position[2]);
+    const V3 viewDir = normalize(viewPos - fragPos);
+    const float distToCamera = length(viewPos - fragPos);
+    const uint32_t alb = __ldg(p.g.albedo + i);
+    V3 baseColor = v3(gmax(unorm8(alb, 0), 0.01f), gmax(unorm8(alb, 1), 0.01f), gmax(unorm8(alb, 2), 0.01f));
+    const V3 normal = decode_normal(__ldg(p.g.normal + i));
+    const uint32_t rma = __ldg(p.g.roughness_metallic_ambient + i);
+    const float roughness = gmax(0.5f, unorm8(rma, 0));
+    const float metallic = unorm8(rma, 1);
+    const float ao = gclamp(h2f(__ldg(p.g.ssao + i)), 0.35f, 1.0f);
+    const float ambient = unorm8(rma, 2);
+    const float refl = float(__ldg(p.g.base_reflectivity + i) & 0xffu) / 255.0f;
+    const V3 baseRefl = v3s(refl);
+    const float roughnessWeight = 1.0f - roughness;
+    V3 vplColor = v3s(0.0f);
+    const float seedX = float(x) + 0.5f, seedY = float(y) + 0.5f;
+    float seedZ = p.time;
+    float validSamples = 0.0f;
+    const float distRatio = gmin(1.0f - distToCamera / 1000.0f, 1.0f);
+    int sampleCount;
+    if (p.spp > 0) {
+        sampleCount = p.spp;
+    } else {
+        int maxSamplesPerPixel = (int)mixf(2.0f, 10.0f, roughnessWeight);
+        int samplesMax = (int)(float(maxSamplesPerPixel) * distRatio);
+        sampleCount = samplesMax > 1 ? samplesMax : 1;
+    }
+    const int32_t* list = nullptr;
+    int candidates;
+    if (p.tiled) {
+        const int tile = (y / p.ts) * p.tiles_x + (x / p.ts);
+        list = p.lists + (size_t)tile * (1 + p.L);
+        candidates = __ldg(list);
+    } else {
+        candidates = __ldg(p.visible_index);
+    }
+    if (candidates > 0) {
+        const float minGi = p.sc.min_gi_occlusion;
+        for (int s = 0, resamples = 0; s < sampleCount; ++s) {
+            const float rnd = random3(seedX, seedY, seedZ);
+            seedZ += 10000.0f;
+            int lightIndex;
+            if (list) {
+                int r = (int)(float(candidates) * rnd);
+                lightIndex = __ldg(list + 1 + (r < candidates - 1 ? r : candidates - 1));
+            } else {
+                lightIndex = (int)(float(candidates - 1) * rnd);
+            }
+            const float4* rec = reinterpret_cast<const float4*>(p.cv + lightIndex);
+            const float4 pos = __ldg(rec);
+            const float4 spec = __ldg(rec + 2);
+            const float4 misc = __ldg(rec + 3);   // radius, farPlane, intensity
+            const sgi_atlas_entry entry = p.ce[lightIndex];
+            const V3 lightPosition = v3(pos.x, pos.y, pos.z);
+            const V3 lmf = lightPosition - fragPos;
+            const float lightRadius = misc.x;
+            const float distance = length(lmf);
+            if (resamples < 5) {
+                float sideCheck = dot(normal, normalize(lmf));
+                if (sideCheck < 0.0f || distance > lightRadius) { ++resamples; --s; continue; }
+            }
+            const float distanceRatio = gclamp((2.0f * distance) / lightRadius, 0.0f, 1.0f);
+            const float distAttenuation = distanceRatio;
+            const float4 col = __ldg(rec + 1);
+            const V3 lightColor = v3(col.x, col.y, col.z);
+            float shadowFactor = distToCamera < 500.0f
+                                     ? shadow_1sample(p.cubes, entry, misc.y, fragPos, lightPosition,
+                                                      dot(lightPosition - fragPos, normal), 0.1f)
+                                     : 0.0f;
+            shadowFactor = gmin(shadowFactor, mixf(minGi, 1.0f, distanceRatio));
+            float reweight = 1.0f;
+            if (shadowFactor > 0.0f) reweight = (1.0f - distAttenuation) * minGi + distAttenuation;
+            validSamples += reweight;
+            const V3 tmp = ao * vpl_lighting2(fragPos, baseColor, normal, viewDir, v3(spec.x, spec.y, spec.z),
+                                              lightPosition, lightColor, distToCamera, lightRadius, roughness,
+                                              metallic, ambient, baseRefl, sp);
+            vplColor = vplColor + (1.0f - shadowFactor) * tmp;
+        }
+    }
+    validSamples = gmax(validSamples, 1.0f);
+    const V3 b = vmin(vplColor, kHalfMax);
+    p.reservoir[i] = pack_h4(b.x, b.y, b.z, validSamples);
+}
+
+cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam,
+                          const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index,
+                          const int32_t* lists, const sgi_cube_atlas& cubes, float time, uint2* reservoir,
+                          cudaStream_t s) {
+    GatherParams p;
+    p.W = cfg.width; p.H = cfg.height; p.ts = cfg.tile_size;
+    p.tiles_x = (cfg.width + cfg.tile_size - 1) / cfg.tile_size;
+    p.L = cfg.max_vpls_per_tile; p.tiled = cfg.gi_mode == SGI_GI_TILED; p.spp = cfg.samples_per_pixel;
+    p.sc = sc; p.g = g; p.cam = cam; p.cv = cv; p.ce = ce; p.visible_index = visible_index; p.lists = lists;
+    p.cubes = cubes; p.time = time; p.reservoir = reservoir;
+    dim3 block(16, 16);
+    dim3 grid((cfg.width + 15) / 16, (cfg.height + 15) / 16);
+    vpl_gather_kernel<<<grid, block, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+// =============================================================== denoise --
+// One pass of vpl_pbr_gi_denoise.fs:275-435 (pass 0 merges reservoirs, the
+// last pass reprojects and composites).
+__global__ void __launch_bounds__(256) denoise_pass_kernel(DenoiseLaunch d) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = d.width, H = d.height;
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * W + x;
+    const int multiplier = (1 << d.pass) - 1;
+    const bool final = d.pass == d.passes - 1;
+    const bool merge = d.pass == 0;
+    const float u = (float(x) + 0.5f) / float(W), v = (float(y) + 0.5f) / float(H);
+    const V3 centerNormal = decode_normal(__ldg(d.cur.normal + i));
+    const float centerDepth = __ldg(d.cur.depth + i);
+    float rf0 = 0.0f, rf1 = 0.0f, rf2 = 0.0f, rf3 = 0.0f;
+    if (merge) {
+        // computeMergedReservoir, vpl_pbr_gi_denoise.fs:192-273 (centre only)
+        float cr0 = 0.0f, cr1 = 0.0f, cr2 = 0.0f, cr3 = 0.0f;
+        const float depthCutoff = 0.1f * centerDepth;
+        float runningSum = 0.0f;
+        const float probabilisticWeight = 1.0f / float(__ldg(d.visible_index));
+        const V3 currNormal = decode_normal(__ldg(d.cur.normal + i));
+        if (!(dot(centerNormal, currNormal) < 0.906f)) {
+            const float currDepth = __ldg(d.cur.depth + i);
+            if (!(gabs(currDepth - centerDepth) > depthCutoff)) {
+                float a, b, c, e;
+                unpack_h4(ld_u2(d.res_in, i), a, b, c, e);
+                const float randUpdate = random3(float(x) + 0.5f, float(y) + 0.5f, d.time);
+                const float probability = e * probabilisticWeight;
+                cr3 += probability;
+                if (randUpdate < (probability / cr3)) {
+                    cr0 += a; cr1 += b; cr2 += c;
+                    runningSum += e;
+                }
+            }
+        }
+        rf0 = cr0; rf1 = cr1; rf2 = cr2; rf3 = runningSum;
+    } else {
+        const int step = 1 + multiplier;
+        for (int dx = -2; dx <= 2; ++dx) {
+            int xx = x + dx * step;
+            xx = xx < 0 ? 0 : (xx > W - 1 ? W - 1 : xx);
+            for (int dy = -2; dy <= 2; ++dy) {
+                int yy = y + dy * step;
+                yy = yy < 0 ? 0 : (yy > H - 1 ? H - 1 : yy);
+                const size_t j = (size_t)yy * W + xx;
+                float a, b, c, e;
+                unpack_h4(ld_u2(d.res_in, j), a, b, c, e);
+                float filtered;
+                if (dx == 0 && dy == 0) {
+                    filtered = 1.0f;
+                } else {   // filterInput, vpl_pbr_gi_denoise.fs:142-190
+                    const float currDepth = __ldg(d.cur.depth + j);
+                    const float wz = expf_ieee(-gabs(centerDepth - currDepth)) / 1.0f;
+                    const V3 currNormal = decode_normal(__ldg(d.cur.normal + j));
+                    float wn = gmax(0.0f, dot(centerNormal, currNormal));
+                    wn = pow128(wn);
+                    filtered = wn * wz * 1.0f;
+                }
+                rf0 = rf0 + filtered * a;
+                rf1 = rf1 + filtered * b;
+                rf2 = rf2 + filtered * c;
+                rf3 = rf3 + filtered * e;
+            }
+        }
+    }
+    const float den = gmax(kEps, rf3);
+    const V3 shadowFactor = v3(rf0 / den, rf1 / den, rf2 / den);
+    if (!final) {
+        d.res_out[i] = pack_h4(shadowFactor.x, shadowFactor.y, shadowFactor.z, 1.0f);
+        return;
+    }
+    if (d.res_out) d.res_out[i] = pack_h4(shadowFactor.x, shadowFactor.y, shadowFactor.z, 1.0f);
+    // indirectIllumination: the gather colour output baseColor + 1e-5 as RGB16F
+    const uint32_t alb = __ldg(d.cur.albedo + i);
+    const V3 gi = v3(h2f(f2h(gmax(unorm8(alb, 0), 0.01f) + kEps)), h2f(f2h(gmax(unorm8(alb, 1), 0.01f) + kEps)),
+                     h2f(f2h(gmax(unorm8(alb, 2), 0.01f) + kEps)));
+    float s0, s1, s2, s3;
+    unpack_h4(ld_u2(d.hdr_in, i), s0, s1, s2, s3);
+    const V3 screen = v3(s0, s1, s2);
+    const uint32_t vel = __ldg(d.cur.velocity + i);
+    const float pu = u - h2f((uint16_t)(vel & 0xffffu)), pv = v - h2f((uint16_t)(vel >> 16));
+    float historyAccum = h2f(__ldg(d.hist_prev + i));
+    float accumMultiplier = 1.0f;
+    const V3 currGi = shadowFactor;
+    const float* pd = d.prev_depth;
+    const uint32_t* pn = d.prev_normal;
+    const float prevCenterDepth = bilinear([&](int ii, int jj) { return __ldg(pd + (size_t)jj * W + ii); }, W, H, pu, pv);
+    const V3 pnv = v3(bilinear([&](int ii, int jj) { return unorm8(__ldg(pn + (size_t)jj * W + ii), 0); }, W, H, pu, pv),
+                      bilinear([&](int ii, int jj) { return unorm8(__ldg(pn + (size_t)jj * W + ii), 1); }, W, H, pu, pv),
+                      bilinear([&](int ii, int jj) { return unorm8(__ldg(pn + (size_t)jj * W + ii), 2); }, W, H, pu, pv));
+    const V3 prevCenterNormal = normalize(pnv * 2.0f - v3s(1.0f));
+    const uint2* gp = d.gi_prev;
+    auto gch = [&](int ii, int jj, int ch) {
+        float a, b, c, e;
+        unpack_h4(ld_u2(gp, (size_t)jj * W + ii), a, b, c, e);
+        return ch == 0 ? a : (ch == 1 ? b : c);
+    };
+    const V3 prevGi = v3(bilinear([&](int ii, int jj) { return gch(ii, jj, 0); }, W, H, pu, pv),
+                         bilinear([&](int ii, int jj) { return gch(ii, jj, 1); }, W, H, pu, pv),
+                         bilinear([&](int ii, int jj) { return gch(ii, jj, 2); }, W, H, pu, pv));
+    const float currId = __ldg(d.cur.id + i);
+    const float prevId = __ldg(d.prev_id + (size_t)nearest_index(pv, H) * W + nearest_index(pu, W));
+    const float wn = gmax(0.0f, dot(centerNormal, prevCenterNormal));
+    const float wz = expf_ieee(-gabs(centerDepth - prevCenterDepth));
+    const float wid = currId != prevId ? 0.0f : 1.0f;
+    float similarity = wn * wz * wid;
+    if (similarity < 0.99f) { similarity = 0.0f; accumMultiplier = 0.0f; }
+    historyAccum = gmin(1.0f + historyAccum * accumMultiplier, d.fps);
+    const float maxAccumulationFactor = 1.0f / historyAccum;
+    const V3 illumAvg = vmix(prevGi, currGi, maxAccumulationFactor);
+    const V3 comb = screen + gi * illumAvg;
+    d.hdr_out[i] = pack_h4(comb.x, comb.y, comb.z, 1.0f);
+    d.gi_out[i] = pack_h4(illumAvg.x, illumAvg.y, illumAvg.z, 1.0f);
+    d.hist_out[i] = f2h(historyAccum);
+}
+
+cudaError_t launch_denoise_pass(const DenoiseLaunch& d, cudaStream_t s) {
+    dim3 block(32, 8);
+    dim3 grid((d.width + 31) / 32, (d.height + 7) / 8);
+    denoise_pass_kernel<<<grid, block, 0, s>>>(d);
+    return cudaGetLastError();
+}
+
+// ============================================================== deferred --
+struct DeferredParams {
+    int W, H;
+    ShadeConfig sc;
+    sgi_gbuffer g;
+    sgi_camera cam;
+    const sgi_point_light* points;
+    int num_points;
+    sgi_csm csm;
+    uint2* out;
+};
+
+// pbr.fs:82-145: non-shadow-casting point lights + the directional light
+// with its CSM (INFINITE_LIGHTING_ENABLED).
+__global__ void __launch_bounds__(256) deferred_pbr_csm_kernel(DeferredParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= p.W || y >= p.H) return;
+    const size_t i = (size_t)y * p.W + x;
+    ShadeParams sp{p.sc.min_roughness, p.sc.perceptual, p.sc.fog_density,
+                   {p.sc.fog_color[0], p.sc.fog_color[1], p.sc.fog_color[2]}, p.sc.point_ambient};
+    const float u = (float(x) + 0.5f) / float(p.W), v = (float(y) + 0.5f) / float(p.H);
+    const V3 fragPos = world_from_depth(u, v, __ldg(p.g.depth + i), p.cam.inv_proj_view);
+    const V3 viewPos = v3(p.cam.view_position[0], p.cam.view_position[1], p.cam.view_position[2]);
+    const V3 viewMinusFrag = viewPos - fragPos;
+    const V3 viewDir = normalize(viewMinusFrag);
+    const float viewDist = length(viewMinusFrag);
+    const uint32_t alb = __ldg(p.g.albedo + i);
+    const V3 baseColor = v3(unorm8(alb, 0), unorm8(alb, 1), unorm8(alb, 2));
+    const float albedoA = unorm8(alb, 3);
+    const V3 normal = decode_normal(__ldg(p.g.normal + i));
+    const uint32_t rma = __ldg(p.g.roughness_metallic_ambient + i);
+    const float roughness = unorm8(rma, 0), metallic = unorm8(rma, 1), rmeB = unorm8(rma, 2);
+    const float ambient = h2f(__ldg(p.g.ssao + i));
+    const uint32_t br = __ldg(p.g.base_reflectivity + i);
+    const float reflR = float(br & 0xffu) / 255.0f, reflG = float(br >> 8) / 255.0f;
+    const V3 emissive = v3(albedoA, reflG, rmeB);
+    V3 color = v3s(0.0f);
+    for (int l = 0; l < p.num_points; ++l) {
+        const float4* rec = reinterpret_cast<const float4*>(p.points + l);
+        const float4 lp4 = __ldg(rec), lc4 = __ldg(rec + 1), m4 = __ldg(rec + 2);
+        const V3 lp = v3(lp4.x, lp4.y, lp4.z), lc = v3(lc4.x, lc4.y, lc4.z);
+        const float distance = length(lp - fragPos);
+        if (distance < m4.x) {
+            // calculatePointLighting2, pbr2.glsl:593-611
+            const V3 lightDir = lp - fragPos;
+            color = color + lighting_burley(lc, lightDir, viewDir, normal, baseColor, viewDist, length(lc) / 12.0f,
+                                            roughness, metallic, ambient, 1.0f - 0.0f, v3s(reflR),
+                                            quadratic_atten(lightDir), sp.point_ambient, sp);
+        }
+    }
+    const V3 lightDir = v3(p.csm.light_direction[0], p.csm.light_direction[1], p.csm.light_direction[2]);
+    const V3 lightColor = v3(p.csm.light_color[0], p.csm.light_color[1], p.csm.light_color[2]);
+    const float shadowFactor = infinite_shadow(p.csm, fragPos, normal, true);
+    // calculateDirectionalLighting, pbr2.glsl:576-591, called with 1 - shadowFactor
+    color = color + lighting_burley(lightColor, lightDir, viewDir, normal, baseColor, viewDist, 0.0f, roughness,
+                                    metallic, ambient, 1.0f - (1.0f - shadowFactor), v3s(reflR), 1.0f, 0.0f, sp);
+    const V3 o = vmin(color + emissive * p.sc.emission_strength, kHalfMax);
+    p.out[i] = pack_h4(o.x, o.y, o.z, 1.0f);
+}
+
+cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
+                            const sgi_camera& cam, const sgi_point_light* points, int32_t num_points,
+                            const sgi_csm& csm, uint2* hdr_out, cudaStream_t s) {
+    DeferredParams p;
+    p.W = cfg.width; p.H = cfg.height; p.sc = sc; p.g = g; p.cam = cam; p.points = points;
+    p.num_points = num_points; p.csm = csm; p.out = hdr_out;
+    dim3 block(32, 8);
+    dim3 grid((cfg.width + 31) / 32, (cfg.height + 7) / 8);
+    deferred_pbr_csm_kernel<<<grid, block, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace sgi

@@ -1,0 +1,253 @@
+// sgi_math.cuh - device-side shading math of the GI/lighting stage.
+//
+// Every translation unit that includes this header is compiled with
+// -fmad=false, -prec-div=true and -prec-sqrt=true: each +, -, *, / and sqrtf
+// below is one correctly rounded binary32 operation, evaluated in the order
+// the expression tree gives. That makes the results reproducible on any
+// IEEE-754 machine, which is how the per-pixel results are checked bit for
+// bit against a CPU restatement of the StratusGFX shaders. No CUDA math-library
+// transcendental is called: exp is computed by Cody-Waite range reduction
+// plus a degree-7 Taylor polynomial, and pow only appears with the integer
+// exponents 5 and 128.
+//
+// GLSL built-in semantics used throughout (GLSL 4.60 spec wording):
+//   min(x, y) = y < x ? y : x,  max(x, y) = x < y ? y : x,
+//   clamp(x, a, b) = min(max(x, a), b),  mix(x, y, a) = x*(1-a) + y*a.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace sgi {
+
+#define SGI_D __device__ __forceinline__
+
+constexpr float kPi = 3.14159265359f;          // common.glsl:3
+constexpr float kEps = 0.00001f;               // PREVENT_DIV_BY_ZERO, common.glsl:4
+constexpr float kHalfMax = 65504.0f;           // HALF_FLOAT_MAX, common.glsl:6
+constexpr float kFloatMax = 3.402823466e+38f;  // FLOAT_MAX, common.glsl:7
+
+SGI_D float gmin(float x, float y) { return y < x ? y : x; }
+SGI_D float gmax(float x, float y) { return x < y ? y : x; }
+SGI_D float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+SGI_D float saturate(float x) { return gclamp(x, 0.0f, 1.0f); }
+SGI_D float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+SGI_D float gabs(float x) { return x < 0.0f ? -x : x; }
+
+// exp(x): Cody & Waite (1980) reduction x = k*ln2 + r with ln2 split into a
+// 15-bit head (exact products for |k| < 512) and a tail, exp(r) by its Taylor
+// series to r^7 in Horner form, then exact scaling by 2^k.
+SGI_D float expf_ieee(float x) {
+    if (x != x) return x;
+    if (x > 88.72283935546875f) return __int_as_float(0x7f800000);
+    if (x < -103.97283935546875f) return 0.0f;
+    float kf = floorf(x * 1.44269502162933349609375f + 0.5f);
+    int k = (int)kf;
+    float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187045037746429443359375e-06f;
+    float p = r * (1.0f / 5040.0f) + (1.0f / 720.0f);
+    p = p * r + (1.0f / 120.0f);
+    p = p * r + (1.0f / 24.0f);
+    p = p * r + (1.0f / 6.0f);
+    p = p * r + 0.5f;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    if (k > 127) { p = p * 1.7014118346046923e+38f; k -= 127; }
+    if (k < -126) { p = p * 1.1754943508222875e-38f; k += 126; }
+    return p * __int_as_float((k + 127) << 23);
+}
+SGI_D float pow5(float x) { float x2 = x * x; float x4 = x2 * x2; return x4 * x; }
+SGI_D float pow128(float x) {
+    float y = x * x; y = y * y; y = y * y; y = y * y; y = y * y; y = y * y; y = y * y; return y;
+}
+
+// ---------------------------------------------------------------- vectors --
+struct V3 { float x, y, z; };
+SGI_D V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+SGI_D V3 v3s(float s) { return V3{s, s, s}; }
+SGI_D V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+SGI_D V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+SGI_D V3 operator*(V3 a, V3 b) { return V3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+SGI_D V3 operator/(V3 a, V3 b) { return V3{a.x / b.x, a.y / b.y, a.z / b.z}; }
+SGI_D V3 operator*(V3 a, float s) { return V3{a.x * s, a.y * s, a.z * s}; }
+SGI_D V3 operator*(float s, V3 a) { return V3{s * a.x, s * a.y, s * a.z}; }
+SGI_D V3 operator/(V3 a, float s) { return V3{a.x / s, a.y / s, a.z / s}; }
+SGI_D V3 operator+(V3 a, float s) { return V3{a.x + s, a.y + s, a.z + s}; }
+SGI_D V3 operator-(V3 a, float s) { return V3{a.x - s, a.y - s, a.z - s}; }
+SGI_D V3 operator-(float s, V3 a) { return V3{s - a.x, s - a.y, s - a.z}; }
+SGI_D V3 operator/(float s, V3 a) { return V3{s / a.x, s / a.y, s / a.z}; }
+SGI_D float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+SGI_D float length(V3 a) { return sqrtf(dot(a, a)); }
+SGI_D V3 normalize(V3 a) { return a / sqrtf(dot(a, a)); }
+SGI_D V3 vmin(V3 a, float s) { return V3{gmin(a.x, s), gmin(a.y, s), gmin(a.z, s)}; }
+SGI_D V3 vmix(V3 x, V3 y, float a) { return x * (1.0f - a) + y * a; }
+
+struct V4 { float x, y, z, w; };
+// column-major mat4 times (x, y, z, w), column-wise accumulation
+SGI_D V4 mat4_mul(const float* m, float x, float y, float z, float w) {
+    V4 r;
+    r.x = ((m[0] * x + m[4] * y) + m[8] * z) + m[12] * w;
+    r.y = ((m[1] * x + m[5] * y) + m[9] * z) + m[13] * w;
+    r.z = ((m[2] * x + m[6] * y) + m[10] * z) + m[14] * w;
+    r.w = ((m[3] * x + m[7] * y) + m[11] * z) + m[15] * w;
+    return r;
+}
+SGI_D float dot4(const float* pl, V3 p) { return ((pl[0] * p.x + pl[1] * p.y) + pl[2] * p.z) + pl[3] * 1.0f; }
+
+// worldPositionFromDepth, common.glsl:143-155
+SGI_D V3 world_from_depth(float u, float v, float depth, const float* inv_pv) {
+    float z = depth * 2.0f - 1.0f;
+    V4 w = mat4_mul(inv_pv, u * 2.0f - 1.0f, v * 2.0f - 1.0f, z, 1.0f);
+    return V3{w.x / w.w, w.y / w.w, w.z / w.w};
+}
+
+// hash / floatConstruct / random(vec3), common.glsl:183-214
+SGI_D uint32_t ghash(uint32_t x) {
+    x += (x << 10u); x ^= (x >> 6u); x += (x << 3u); x ^= (x >> 11u); x += (x << 15u);
+    return x;
+}
+SGI_D float random3(float sx, float sy, float sz) {
+    uint32_t h = ghash(__float_as_uint(sx) ^ ghash(__float_as_uint(sy)) ^ ghash(__float_as_uint(sz)));
+    return __uint_as_float((h & 0x007FFFFFu) | 0x3F800000u) - 1.0f;
+}
+
+SGI_D float unorm8(uint32_t t, int ch) { return float((t >> (8 * ch)) & 0xffu) / 255.0f; }
+SGI_D V3 decode_normal(uint32_t t) {   // normalize(rgb * 2 - 1), common.glsl:216-220
+    V3 c = v3(unorm8(t, 0), unorm8(t, 1), unorm8(t, 2));
+    return normalize(c * 2.0f - v3s(1.0f));
+}
+SGI_D float h2f(uint16_t h) { return __half2float(__ushort_as_half(h)); }
+SGI_D uint16_t f2h(float f) { return __half_as_ushort(__float2half_rn(f)); }
+
+// clamped texel index of a floor'ed coordinate (NaN -> 0)
+SGI_D int tex_index(float f, int n) {
+    if (f >= float(n - 1)) return n - 1;
+    if (f >= 0.0f) return (int)f;
+    return 0;
+}
+SGI_D int nearest_index(float s, int n) { return tex_index(floorf(s * float(n)), n); }
+
+// ------------------------------------------------------- shading library --
+struct ShadeParams {
+    float min_roughness;
+    int perceptual;
+    float fog_density;
+    float fog_color[3];
+    float point_ambient;
+};
+
+// applyFog, fog.glsl:38-42
+SGI_D V3 apply_fog(V3 color, float dist, float intensity, const ShadeParams& sp) {
+    float f = expf_ieee(-sp.fog_density * dist);
+    V3 fc = v3(sp.fog_color[0], sp.fog_color[1], sp.fog_color[2]) * intensity;
+    return color * f + fc * (1.0f - f);
+}
+// NDF_GGX, pbr2.glsl:51-55
+SGI_D float ndf_ggx(float NdotH, float r) {
+    float r2 = r * r;
+    float f = (NdotH * r2 - NdotH) * NdotH + 1.0f;
+    return r2 / gmax(kPi * f * f, kEps);
+}
+// Visibility_G_SmithGGX, pbr2.glsl:59-64
+SGI_D float vis_smith_ggx(float NdotV, float NdotL, float r) {
+    float a2 = r * r;
+    float ggxv = NdotL * sqrtf((NdotV - a2 * NdotV) * NdotV + a2);
+    float ggxl = NdotV * sqrtf((NdotL - a2 * NdotL) * NdotL + a2);
+    return 0.5f / gmax(ggxv + ggxl, kEps);
+}
+// Fr_Fresnel_Schlick, pbr2.glsl:73-76
+SGI_D V3 fr_fresnel(float u, V3 f0) { float f = pow5(1.0f - u); return v3s(f) + f0 * (1.0f - f); }
+// Fd_Fresnel_Schlick, pbr2.glsl:85-88
+SGI_D float fd_fresnel(float u, float f0, float f90) { float f = pow5(1.0f - u); return f0 + (f90 - f0) * f; }
+// Fd_Burley, pbr2.glsl:91-96
+SGI_D float fd_burley(float NdotV, float NdotL, float LdotH, float r) {
+    float f90 = 0.5f + 2.0f * r * LdotH * LdotH;
+    float ls = fd_fresnel(NdotL, 1.0f, f90);
+    float vs = fd_fresnel(NdotV, 1.0f, f90);
+    return ls * vs * (1.0f / kPi);
+}
+// singleScatteringBRDF_Specular, pbr2.glsl:102-115
+SGI_D V3 spec_brdf(float NdotV, float NdotL, float NdotH, float LdotH, float r, V3 f0) {
+    float ndf = ndf_ggx(NdotH, r);
+    V3 fres = fr_fresnel(LdotH, f0);
+    float vis = vis_smith_ggx(NdotV, NdotL, r);
+    return (ndf * vis) * fres;
+}
+// RemapRoughness, pbr2.glsl:139-144
+SGI_D float remap_roughness(float r, const ShadeParams& sp) {
+    if (sp.perceptual) r = r * r;
+    return gmax(gmax(0.0f, sp.min_roughness), r);
+}
+// BRDF_Base, pbr2.glsl:146-168
+SGI_D void brdf_base(V3 baseColor, V3 baseRefl, float roughness, float metallic, V3 diffDivisor, V3 specMult,
+                     const ShadeParams& sp, float& remapped, V3& diffuseColor, V3& f0) {
+    remapped = remap_roughness(roughness, sp);
+    diffuseColor = (1.0f - metallic) * baseColor;
+    diffuseColor = diffuseColor / (diffDivisor + kEps);
+    f0 = 0.16f * baseRefl * baseRefl * (1.0f - metallic) + baseColor * metallic;
+    f0 = f0 * specMult;
+}
+// BRDF_DotProducts, pbr2.glsl:170-188
+SGI_D void brdf_dots(V3 V, V3 lightDir, V3 N, float& NdotV, float& NdotL, float& NdotH, float& LdotH) {
+    V3 L = normalize(lightDir);
+    V3 H = normalize(V + L);
+    NdotV = saturate(dot(N, V));
+    NdotL = saturate(dot(N, L));
+    NdotH = saturate(dot(N, H));
+    LdotH = saturate(dot(L, H));
+}
+// BRDF_Burley, pbr2.glsl:194-250
+SGI_D V3 brdf_burley(V3 lightDir, V3 V, V3 N, V3 baseColor, V3 baseRefl, float roughness, float metallic,
+                     V3 diffDivisor, V3 specMult, const ShadeParams& sp) {
+    float rr; V3 dc, f0;
+    brdf_base(baseColor, baseRefl, roughness, metallic, diffDivisor, specMult, sp, rr, dc, f0);
+    float NdotV, NdotL, NdotH, LdotH;
+    brdf_dots(V, lightDir, N, NdotV, NdotL, NdotH, LdotH);
+    V3 Fr = spec_brdf(NdotV, NdotL, NdotH, LdotH, rr, f0);
+    V3 Fd = dc * fd_burley(NdotV, NdotL, LdotH, rr);
+    return (Fd + Fr) * NdotL;
+}
+// calculateLighting_Burley, pbr2.glsl:454-478
+SGI_D V3 lighting_burley(V3 lightColor, V3 lightDir, V3 V, V3 N, V3 baseColor, float viewDist, float fogIntensity,
+                         float roughness, float metallic, float ao, float shadowFactor, V3 baseRefl, float atten,
+                         float ambientIntensity, const ShadeParams& sp) {
+    V3 brdf = brdf_burley(lightDir, V, N, baseColor, baseRefl, roughness, metallic, v3s(1.0f), v3s(1.0f), sp);
+    V3 ambient = brdf * ao * lightColor * ambientIntensity;
+    V3 finalB = brdf * lightColor;
+    return atten * (ambient + shadowFactor * apply_fog(finalB, viewDist, fogIntensity, sp));
+}
+// quadraticAttenuation, pbr.glsl:255-258
+SGI_D float quadratic_atten(V3 lightDir) { float d = length(lightDir); return 1.0f / (1.0f + d * d); }
+// vplDiffuseAttenuation / vplSpecularAttenuation, pbr.glsl:260-271
+SGI_D float vpl_atten(V3 lightDir, float radius) {
+    float d = length(lightDir);
+    float ratio = gmin(d / radius, 1.0f);
+    float minDist = mixf(10.0f, 1.0f, expf_ieee(-3.0f * ratio)) * radius;
+    return 1.0f / (minDist + 1.0f * d * d);
+}
+// calculateVirtualPointLighting2 (shadowFactor argument 0, fog intensity 0,
+// ambient intensity 0) -> calculateLighting_Lambert_SeparateDiffuseSpecular ->
+// BRDF_Lambert_SeparateDiffuseSpecular; pbr2.glsl:613-657, :541-574, :382-452.
+SGI_D V3 vpl_lighting2(V3 fragPos, V3 baseColor, V3 N, V3 V, V3 specPos, V3 diffPos, V3 lightColor, float viewDist,
+                       float radius, float roughness, float metallic, float ao, V3 baseRefl, const ShadeParams& sp) {
+    V3 specDir = specPos - fragPos;
+    V3 diffDir = diffPos - fragPos;
+    float adjusted = 1.0f - 0.0f;
+    float specAtten = vpl_atten(specDir, radius);
+    float diffAtten = vpl_atten(diffDir, radius);
+    V3 specMult = 1.0f / (baseColor + kEps);
+    float rr; V3 dc, f0;
+    brdf_base(baseColor, baseRefl, roughness, metallic, baseColor, specMult, sp, rr, dc, f0);
+    float NdotV, NdotL, NdotH, LdotH;
+    brdf_dots(V, specDir, N, NdotV, NdotL, NdotH, LdotH);
+    V3 Fr = spec_brdf(NdotV, NdotL, NdotH, LdotH, rr, f0) * NdotL;
+    brdf_dots(V, diffDir, N, NdotV, NdotL, NdotH, LdotH);
+    V3 Fd = (dc * (1.0f / kPi)) * NdotL;
+    V3 bs = specAtten * Fr;
+    V3 bd = diffAtten * Fd;
+    V3 brdf = bs + bd;
+    V3 ambient = brdf * ao * lightColor * 0.0f;
+    V3 finalB = brdf * lightColor;
+    return ambient + adjusted * apply_fog(finalB, viewDist, 0.0f, sp);
+}
+
+}  // namespace sgi

@@ -1,0 +1,71 @@
+"""Shared test utilities: uploading oracle-side inputs to the device and comparing results."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def half_bits_equal(a16: np.ndarray, b16: np.ndarray) -> np.ndarray:
+    """Elementwise equality of float16 arrays by value, NaN == NaN (any payload), +0 == -0."""
+    a = a16.astype(np.float32)
+    b = b16.astype(np.float32)
+    return (a == b) | (np.isnan(a) & np.isnan(b))
+
+
+def f32_equal(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    a = np.asarray(a, dtype=np.float32)
+    b = np.asarray(b, dtype=np.float32)
+    return (a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b)) | (a == b)
+
+
+def rel_err(gpu: np.ndarray, ref: np.ndarray) -> float:
+    g = np.asarray(gpu, dtype=np.float64)
+    r = np.asarray(ref, dtype=np.float64)
+    ok = np.isfinite(g) & np.isfinite(r)
+    d = np.abs(g - r)[ok] / np.maximum(np.abs(r[ok]), 1e-6)
+    return float(d.max()) if d.size else 0.0
+
+
+def psnr(img: np.ndarray, ref: np.ndarray) -> float:
+    x = np.asarray(img, dtype=np.float64)
+    r = np.asarray(ref, dtype=np.float64)
+    mse = float(np.mean((x - r) ** 2))
+    peak = float(np.max(np.abs(r)))
+    return float("inf") if mse == 0 else 10.0 * np.log10(peak * peak / mse)
+
+
+def assert_bit_exact(gpu, ref, what: str, eq=None):
+    eq = eq or f32_equal
+    m = eq(gpu, ref)
+    frac = float(m.mean())
+    if frac < 1.0:
+        bad = np.argwhere(~m)
+        first = tuple(bad[0])
+        raise AssertionError(f"{what}: {(~m).sum()} of {m.size} differ (exact fraction {frac:.6f}); "
+                             f"first at {first}: gpu={gpu[first]!r} oracle={ref[first]!r}; "
+                             f"max rel err {rel_err(gpu, ref):.3e}")
+
+
+def upload_gbuffer(hg, device="cuda"):
+    """oracle HostGBuffer -> stage.GBufferTensors holding the same bytes."""
+    import torch
+    from stratusgfx_gb300.stage import GBufferTensors
+    H, W = hg.depth.shape
+    g = GBufferTensors(H, W, device)
+    for name in hg.NAMES:
+        getattr(g, name).copy_(torch.from_numpy(np.ascontiguousarray(getattr(hg, name))))
+    return g
+
+
+def upload_cubes(storage: np.ndarray, fmt: int, layers: int = 320, device="cuda"):
+    import torch
+    from stratusgfx_gb300 import abi
+    t = torch.from_numpy(storage.view(np.int16) if storage.dtype == np.uint16 else storage).to(device)
+    at = abi.CubeAtlas()
+    for a in range(storage.shape[0]):
+        at.atlas[a] = t[a].data_ptr()
+    at.num_atlases, at.layers_per_atlas, at.face_size, at.format = storage.shape[0], layers, storage.shape[-1], fmt
+    return t, at
+
+
+def half4_to_f32(buf: np.ndarray, H: int, W: int) -> np.ndarray:
+    return buf.view(np.float16).reshape(H, W, 4).astype(np.float32)

@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["hd", "small"], default="hd")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling case for ncu: the same 1080p workload with a 2-frame path, "
+                         "--warmup + --steps frames of sgi_render_frame only (no e2e or CPU legs)")
     return ap.parse_args()
 
 
@@ -356,8 +359,36 @@ def run_reference(args):
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_profile(args):
+    """Frames of the workload only, for kernel captures (about 0.7 GB on the device)."""
+    import torch
+
+    from stratusgfx_gb300 import stage
+    from stratusgfx_gb300 import scene as S
+    w = workload(args.workload)
+    sc = S.make_scene(1234 + 2, w.width, w.height, w.num_boxes, w.num_vpls, 2, vpl_radius=w.vpl_radius,
+                      num_points=w.num_points, csm_resolution=w.csm_resolution)
+    ds = stage.DeviceScene(sc, w)
+    st = stage.GiStage(stage.workload_config(w))
+    st.set_lights(ds.vpls, ds.entries, ds.points)
+    out = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
+    for s in range(args.warmup + args.steps):
+        k = s % 2 + 1
+        st.set_shadow_maps(ds.csms[k], ds.cubes)
+        st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * s, 60.0)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": w.name, "frames": args.warmup + args.steps,
+                      "launches_per_frame": st.launch_count() // (args.warmup + args.steps)}))
+    st.close()
+
+
 def main():
     args = parse()
+    if args.profile:
+        from __graft_entry__ import build
+        build()
+        run_profile(args)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

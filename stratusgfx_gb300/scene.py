@@ -335,3 +335,31 @@ HD = Workload("room40_1920x1080_vpl2048_k8", 1920, 1080, 40, 2048, 4, 2048, 128,
 def workload_scene(w: Workload, seed: int) -> Scene:
     return make_scene(seed, w.width, w.height, w.num_boxes, w.num_vpls, w.frames, vpl_radius=w.vpl_radius,
                       num_points=w.num_points, csm_resolution=w.csm_resolution)
+
+
+def scene_arrays(s: Scene) -> dict:
+    """Flat arrays of a Scene (for fixtures: host math never needs to be recomputed)."""
+    d = dict(seed=np.int64(s.seed), width=np.int64(s.width), height=np.int64(s.height), boxes=s.boxes,
+             light_direction=s.light_direction, light_color=s.light_color, vpls=s.vpls, entries=s.entries,
+             points=s.points, fovy_deg=np.float64(s.fovy_deg))
+    d["cam_proj_view"] = np.stack([c.proj_view for c in s.cameras])
+    d["cam_inv_proj_view"] = np.stack([c.inv_proj_view for c in s.cameras])
+    d["cam_prev_proj_view"] = np.stack([c.prev_proj_view for c in s.cameras])
+    d["cam_position"] = np.stack([c.position for c in s.cameras])
+    d["csm_proj_view"] = np.stack([c.cascade_proj_view for c in s.csms])
+    d["csm_inv_proj_view"] = np.stack([c.inv_cascade_proj_view for c in s.csms])
+    d["csm_planes"] = np.stack([c.cascade_planes for c in s.csms])
+    d["csm_znear_zfar"] = np.array([[c.znear, c.zfar] for c in s.csms])
+    return d
+
+
+def scene_from_arrays(d) -> Scene:
+    cams = [CameraFrame(proj_view=d["cam_proj_view"][k], inv_proj_view=d["cam_inv_proj_view"][k],
+                        prev_proj_view=d["cam_prev_proj_view"][k], position=d["cam_position"][k], world=np.eye(4))
+            for k in range(d["cam_proj_view"].shape[0])]
+    csms = [CsmFrame(cascade_proj_view=d["csm_proj_view"][k], inv_cascade_proj_view=d["csm_inv_proj_view"][k],
+                     cascade_planes=d["csm_planes"][k], znear=float(d["csm_znear_zfar"][k][0]),
+                     zfar=float(d["csm_znear_zfar"][k][1])) for k in range(d["csm_proj_view"].shape[0])]
+    return Scene(seed=int(d["seed"]), width=int(d["width"]), height=int(d["height"]), boxes=d["boxes"],
+                 light_direction=d["light_direction"], light_color=d["light_color"], vpls=d["vpls"],
+                 entries=d["entries"], points=d["points"], cameras=cams, csms=csms, fovy_deg=float(d["fovy_deg"]))

@@ -256,9 +256,13 @@ def test_no_vpls_visible():
     w = S.Workload("room12_64x48_novis", 64, 48, 12, 16, 0, 256, 8, abi.SGI_CUBE_F32, 4, 3, 1)
     s = Setup(w, 5)
     v = s.sc.vpls.copy()
-    v[:, 1] = -0.25
+    rng = np.random.default_rng(0)
+    v[:, 0] = rng.uniform(4.0, 6.0, len(v))   # 1 m under the middle of the floor slab: the sun ray is blocked
+    v[:, 1] = -1.0
+    v[:, 2] = rng.uniform(4.0, 6.0, len(v))
     s.vpls = torch.from_numpy(v).cuda()
     s.sc.vpls = v
+    assert O.vis_cull(32, v, s.hs.csms[1], 16)[0] == 0
     st, cfg, out = _run_frame(s)
     assert st.read_debug(abi.SGI_DEBUG_VISIBLE_INDEX, np.int32)[0] == 0
     ref = O.frame(32, cfg, s.hs, 1, np.zeros((48, 64, 4), np.float32), np.zeros((48, 64), np.float32), TIME, FPS)

@@ -120,7 +120,7 @@ typedef struct sgi_config {
     int32_t gi_mode;               /* SGI_GI_REFERENCE or SGI_GI_TILED */
     int32_t samples_per_pixel;     /* 0 = reference adaptive 2..10 (vpl_pbr_gi.fs:138-143), else fixed K */
     int32_t denoise_passes;        /* 2..8: pass 0 merges reservoirs, the last is final (reference 4) */
-    int32_t debug_keep_passes;     /* nonzero: keep each denoise pass output for sgi_read_debug */
+    int32_t debug_keep_passes;     /* nonzero: keep the raw reservoir and each denoise pass output for sgi_read_debug */
     float   min_roughness;         /* RendererSettings minRoughness_ = 0.08 */
     int32_t use_perceptual_roughness; /* RendererSettings usePerceptualRoughness = true */
     float   min_gi_occlusion_factor;  /* RendererSettings minGiOcclusionFactor_ = 0.95 */
@@ -259,7 +259,7 @@ sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream);
 #define SGI_DEBUG_COMPACT_ENTRIES 2  /* sgi_atlas_entry [max_visible] */
 #define SGI_DEBUG_TILE_STAGE1     3  /* sgi_tile_stage1 [tiles] */
 #define SGI_DEBUG_TILE_LISTS      4  /* int32 [tiles][1 + L]: count, compacted indices */
-#define SGI_DEBUG_RESERVOIR       5  /* RGBA16F [W*H]: gather output (vplColor, validSamples) */
+#define SGI_DEBUG_RESERVOIR       5  /* RGBA16F [W*H]: gather output (vplColor, validSamples); needs debug_keep_passes */
 #define SGI_DEBUG_GI_HISTORY      6  /* RGB16F [W*H]: this frame's denoised GI (giColor) */
 #define SGI_DEBUG_HISTORY_DEPTH   7  /* R16F [W*H]: accumulated history length */
 #define SGI_DEBUG_DIRECT          8  /* RGB16F [W*H]: direct lighting of sgi_render_frame */

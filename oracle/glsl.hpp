@@ -2,11 +2,12 @@
 //
 // A C++ restatement of the GLSL built-ins and shading library that the
 // StratusGFX GI/lighting shaders use, templated on the scalar type:
-//   T = float  : the parity oracle. Every operation is a correctly rounded
-//                IEEE-754 binary32 +, -, *, /, sqrt in a fixed order (the
-//                file is compiled with -ffp-contract=off), so a CUDA kernel
-//                that evaluates the same expression trees without FMA
-//                contraction produces bit-identical results.
+//   T = float  : the parity oracle. Every operation is one correctly rounded
+//                IEEE-754 binary32 +, -, *, /, sqrt or explicit fused
+//                multiply-add, in a fixed order (the file is compiled with
+//                -ffp-contract=off, so the compiler adds no fusion of its
+//                own), so a CUDA kernel that evaluates the same expression
+//                trees produces bit-identical results.
 //   T = double : the accuracy oracle (std::exp / std::pow, no FP16 storage).
 //
 // Parity is UNPINNED by the reference: StratusGFX has no golden vectors or
@@ -15,14 +16,21 @@
 // source lines it cites (paths relative to the StratusGFX project root).
 //
 // Built-ins whose GLSL precision is implementation-defined get one fixed
-// definition here (the CUDA kernels use the same one):
+// definition here (the CUDA kernels use the same one). GLSL allows a
+// multiply-add to be fused and vector divisions to be evaluated through a
+// reciprocal, so the definitions below fuse explicitly (fma = one rounding)
+// in the places a GPU compiler would, and nowhere else:
 //   min(x,y) = y < x ? y : x ; max(x,y) = x < y ? y : x   (GLSL spec wording)
+//   dot(a,b) = fma(az, bz, fma(ay, by, ax*bx))
+//   mat4*vec4: per row fma(m3, w, fma(m2, z, fma(m1, y, m0*x)))
+//   vec / s  = vec * (1/s)  (one correctly rounded reciprocal)
+//   normalize(v) = v * (1/sqrt(dot(v,v)))
+//   mix(x,y,a) = fma(y, a, x*(1-a))
 //   exp(x)   : Cody-Waite range reduction (ln2 split hi/lo) + degree-7 Taylor
-//              polynomial in Horner form + exact power-of-two scaling.
+//              polynomial in fused Horner form + exact power-of-two scaling.
 //   pow(x,5) = (x*x)*(x*x)*x ; pow(x,128) = seven squarings (integer exponents
 //              are the only ones the path uses).
-//   normalize(v) = v / sqrt(dot(v,v)); dot = (x*x' + y*y') + z*z'.
-//   mix(x,y,a) = x*(1-a) + y*a.
+// Scalar a / b stays a correctly rounded division.
 #pragma once
 
 #include <cmath>
@@ -32,11 +40,12 @@
 namespace oracle {
 
 // ---------------------------------------------------------------- scalars --
+template <class T> inline T gfma(T a, T b, T c) { return std::fma(a, b, c); }
 template <class T> inline T gmin(T x, T y) { return y < x ? y : x; }
 template <class T> inline T gmax(T x, T y) { return x < y ? y : x; }
 template <class T> inline T gclamp(T x, T lo, T hi) { return gmin(gmax(x, lo), hi); }
 template <class T> inline T saturate(T x) { return gclamp(x, T(0), T(1)); }   // common.glsl:99-101
-template <class T> inline T mix(T x, T y, T a) { return x * (T(1) - a) + y * a; }
+template <class T> inline T mix(T x, T y, T a) { return gfma(y, a, x * (T(1) - a)); }
 template <class T> inline T gabs(T x) { return x < T(0) ? -x : x; }
 
 // exp for binary32 (see header comment). Returns exactly 1 for +-0.
@@ -47,13 +56,13 @@ inline float exp_f32(float x) {
     float kf = std::floor(x * 1.44269502162933349609375f + 0.5f);
     int k = (int)kf;
     float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187045037746429443359375e-06f;
-    float p = r * (1.0f / 5040.0f) + (1.0f / 720.0f);
-    p = p * r + (1.0f / 120.0f);
-    p = p * r + (1.0f / 24.0f);
-    p = p * r + (1.0f / 6.0f);
-    p = p * r + 0.5f;
-    p = p * r + 1.0f;
-    p = p * r + 1.0f;
+    float p = std::fma(r, 1.0f / 5040.0f, 1.0f / 720.0f);
+    p = std::fma(p, r, 1.0f / 120.0f);
+    p = std::fma(p, r, 1.0f / 24.0f);
+    p = std::fma(p, r, 1.0f / 6.0f);
+    p = std::fma(p, r, 0.5f);
+    p = std::fma(p, r, 1.0f);
+    p = std::fma(p, r, 1.0f);
     if (k > 127) { p = p * 1.7014118346046923e+38f; k -= 127; }      // 2^127
     if (k < -126) { p = p * 1.1754943508222875e-38f; k += 126; }      // 2^-126
     uint32_t bits = (uint32_t)(k + 127) << 23;
@@ -145,29 +154,32 @@ template <class T> inline V3<T> operator*(V3<T> a, V3<T> b) { return {a.x * b.x,
 template <class T> inline V3<T> operator/(V3<T> a, V3<T> b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
 template <class T> inline V3<T> operator*(V3<T> a, T s) { return {a.x * s, a.y * s, a.z * s}; }
 template <class T> inline V3<T> operator*(T s, V3<T> a) { return {s * a.x, s * a.y, s * a.z}; }
-template <class T> inline V3<T> operator/(V3<T> a, T s) { return {a.x / s, a.y / s, a.z / s}; }
+template <class T> inline V3<T> operator/(V3<T> a, T s) { T r = T(1) / s; return {a.x * r, a.y * r, a.z * r}; }
 template <class T> inline V3<T> operator+(V3<T> a, T s) { return {a.x + s, a.y + s, a.z + s}; }
 template <class T> inline V3<T> operator-(V3<T> a, T s) { return {a.x - s, a.y - s, a.z - s}; }
 template <class T> inline V3<T> operator-(T s, V3<T> a) { return {s - a.x, s - a.y, s - a.z}; }
 template <class T> inline V3<T> operator/(T s, V3<T> a) { return {s / a.x, s / a.y, s / a.z}; }
-template <class T> inline T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> inline T dot(V3<T> a, V3<T> b) { return gfma(a.z, b.z, gfma(a.y, b.y, a.x * b.x)); }
 template <class T> inline T length(V3<T> a) { return Prec<T>::sqrt(dot(a, a)); }
-template <class T> inline V3<T> normalize(V3<T> a) { return a / Prec<T>::sqrt(dot(a, a)); }
+template <class T> inline V3<T> normalize(V3<T> a) { T r = T(1) / Prec<T>::sqrt(dot(a, a)); return a * r; }
 template <class T> inline V3<T> vmin(V3<T> a, T s) { return {gmin(a.x, s), gmin(a.y, s), gmin(a.z, s)}; }
-template <class T> inline V3<T> vmix(V3<T> x, V3<T> y, T a) { return x * (T(1) - a) + y * a; }
+template <class T> inline V3<T> vmix(V3<T> x, V3<T> y, T a) {
+    T b = T(1) - a;
+    return {gfma(y.x, a, x.x * b), gfma(y.y, a, x.y * b), gfma(y.z, a, x.z * b)};
+}
 
 // column-major mat4 (glm layout) times (x,y,z,w): column-wise accumulation
 template <class T> struct V4 { T x, y, z, w; };
 template <class T> inline V4<T> mat4_mul(const float* m, T x, T y, T z, T w) {
     V4<T> r;
-    r.x = ((T(m[0]) * x + T(m[4]) * y) + T(m[8]) * z) + T(m[12]) * w;
-    r.y = ((T(m[1]) * x + T(m[5]) * y) + T(m[9]) * z) + T(m[13]) * w;
-    r.z = ((T(m[2]) * x + T(m[6]) * y) + T(m[10]) * z) + T(m[14]) * w;
-    r.w = ((T(m[3]) * x + T(m[7]) * y) + T(m[11]) * z) + T(m[15]) * w;
+    r.x = gfma(T(m[12]), w, gfma(T(m[8]), z, gfma(T(m[4]), y, T(m[0]) * x)));
+    r.y = gfma(T(m[13]), w, gfma(T(m[9]), z, gfma(T(m[5]), y, T(m[1]) * x)));
+    r.z = gfma(T(m[14]), w, gfma(T(m[10]), z, gfma(T(m[6]), y, T(m[2]) * x)));
+    r.w = gfma(T(m[15]), w, gfma(T(m[11]), z, gfma(T(m[7]), y, T(m[3]) * x)));
     return r;
 }
 template <class T> inline T dot4(const float* plane, V3<T> p) {   // dot(plane, vec4(p, 1.0))
-    return ((T(plane[0]) * p.x + T(plane[1]) * p.y) + T(plane[2]) * p.z) + T(plane[3]) * T(1);
+    return gfma(T(plane[3]), T(1), gfma(T(plane[2]), p.z, gfma(T(plane[1]), p.y, T(plane[0]) * p.x)));
 }
 
 // ---------------------------------------------------------- common.glsl --
@@ -182,7 +194,7 @@ template <class T> struct C {
 template <class T> inline V3<T> world_from_depth(T u, T v, T depth, const float* inv_pv) {
     T z = depth * T(2) - T(1);
     V4<T> w = mat4_mul<T>(inv_pv, u * T(2) - T(1), v * T(2) - T(1), z, T(1));
-    return V3<T>(w.x / w.w, w.y / w.w, w.z / w.w);
+    return V3<T>(w.x, w.y, w.z) / w.w;
 }
 
 // hash / floatConstruct / random, common.glsl:183-214 (always integer/binary32)

@@ -43,7 +43,7 @@ template <class T, class Fetch> inline T bilinear(Fetch fetch, int W, int H, T s
     int i0 = tex_index(double(fu), W), i1 = tex_index(double(fu + T(1)), W);
     int j0 = tex_index(double(fv), H), j1 = tex_index(double(fv + T(1)), H);
     T w00 = (T(1) - a) * (T(1) - b), w10 = a * (T(1) - b), w01 = (T(1) - a) * b, w11 = a * b;
-    return ((fetch(i0, j0) * w00 + fetch(i1, j0) * w10) + fetch(i0, j1) * w01) + fetch(i1, j1) * w11;
+    return gfma(fetch(i1, j1), w11, gfma(fetch(i0, j1), w01, gfma(fetch(i1, j0), w10, fetch(i0, j0) * w00)));
 }
 template <class T> inline int nearest_index(T s, int n) { return tex_index(double(std::floor(s * T(n))), n); }
 
@@ -72,7 +72,7 @@ template <class T> inline T infinite_shadow(const sgi_csm& csm, V3<T> fragPos, V
     V3<T> cc[4];
     for (int i = 0; i < 4; ++i) {
         V4<T> c = mat4_mul<T>(csm.cascade_proj_view[i], position.x, position.y, position.z, T(1));
-        V3<T> d(c.x / c.w, c.y / c.w, c.z / c.w);
+        V3<T> d = V3<T>(c.x, c.y, c.z) / c.w;
         cc[i] = d * T(0.5) + V3<T>(T(0.5));
     }
     bool beyond2 = blends.y >= T(0);
@@ -457,7 +457,7 @@ template <class T> void denoise_pixel(const DenoiseArgs<T>& a, int pass, const T
                     wn = Prec<T>::pow128(wn);                                       // sigmaN = 128
                     filtered = wn * wz * T(1);
                 }
-                for (int c = 0; c < 4; ++c) rf[c] = rf[c] + filtered * r[c];
+                for (int c = 0; c < 4; ++c) rf[c] = gfma(filtered, r[c], rf[c]);
             }
         }
     }

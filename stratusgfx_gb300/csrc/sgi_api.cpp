@@ -52,6 +52,7 @@ struct sgi_ctx {
     uint2* ping[2] = {nullptr, nullptr};
     uint2* pass_bufs[SGI_MAX_DENOISE_PASSES] = {};
     uint2* direct = nullptr;
+    float4* guide = nullptr;
     uint2* gi_hist[2] = {nullptr, nullptr};
     uint16_t* hist_depth[2] = {nullptr, nullptr};
     int hist_cur = 0;
@@ -134,7 +135,7 @@ sgi::ShadeConfig make_shade(const sgi_config& c) {
 
 void free_all(sgi_ctx* c) {
     void* ptrs[] = {c->vpls, c->entries, c->points, c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
-                    c->reservoir, c->ping[0], c->ping[1], c->direct, c->gi_hist[0], c->gi_hist[1],
+                    c->reservoir, c->ping[0], c->ping[1], c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
                     c->hist_depth[0], c->hist_depth[1]};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto* p : c->pass_bufs) if (p) cudaFree(p);
@@ -217,7 +218,8 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     chk(dalloc(&c->visible_index, 1 + (size_t)cfg->max_vpls));
     chk(dalloc(&c->stage1, c->num_tiles));
     chk(dalloc(&c->lists, (size_t)c->num_tiles * (1 + cfg->max_vpls_per_tile)));
-    chk(dalloc(&c->reservoir, P));
+    chk(dalloc(&c->reservoir, cfg->debug_keep_passes ? P : 1));
+    chk(dalloc(&c->guide, P));
     chk(dalloc(&c->ping[0], P));
     chk(dalloc(&c->ping[1], P));
     chk(dalloc(&c->direct, P));
@@ -333,13 +335,28 @@ static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer
                          const void* hdr_in, void* hdr_out, const sgi_frame_params* params, cudaStream_t s,
                          int ev_gather) {
     const sgi_config& cfg = ctx->cfg;
+    const bool keep = cfg.debug_keep_passes != 0;
+    // vpl_pbr_gi.fs, with denoise pass 0 (the centre-only reservoir merge) in its epilogue
+    sgi::GatherOut go;
+    go.merged = keep ? ctx->pass_bufs[0] : ctx->ping[0];
+    go.guide = ctx->guide;
+    go.raw = keep ? ctx->reservoir : nullptr;
     SGI_CUDA(ctx, sgi::launch_gather(cfg, ctx->sc, *cur, *cam, ctx->cv, ctx->ce, ctx->visible_index, ctx->lists,
-                                     ctx->cubes, params->time, ctx->reservoir, s), "vpl_gather");
+                                     ctx->cubes, params->time, go, s), "vpl_gather");
     ctx->launches += 1;
     record(ctx, ev_gather + 1, s);
+    // passes 1 .. n-2: a-trous at stride 2^pass (StratusRendererBackend.cpp:1912-1940)
+    const uint2* in = go.merged;
+    for (int pass = 1; pass < cfg.denoise_passes - 1; ++pass) {
+        uint2* out = keep ? ctx->pass_bufs[pass] : ctx->ping[pass & 1];
+        SGI_CUDA(ctx, sgi::launch_atrous(cfg.width, cfg.height, pass, ctx->guide, in, out, s), "atrous");
+        ctx->launches += 1;
+        in = out;
+    }
+    // pass n-1: a-trous + temporal reprojection + composite
     sgi::DenoiseLaunch d;
     std::memset(&d, 0, sizeof(d));
-    d.width = cfg.width; d.height = cfg.height; d.passes = cfg.denoise_passes;
+    d.width = cfg.width; d.height = cfg.height; d.passes = cfg.denoise_passes; d.pass = cfg.denoise_passes - 1;
     d.time = params->time; d.fps = params->frames_per_second;
     d.cur = *cur;
     d.prev_depth = prev->depth; d.prev_normal = prev->normal; d.prev_id = prev->id;
@@ -347,15 +364,11 @@ static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer
     d.gi_prev = ctx->gi_hist[ctx->hist_cur]; d.gi_out = ctx->gi_hist[1 - ctx->hist_cur];
     d.hist_prev = ctx->hist_depth[ctx->hist_cur]; d.hist_out = ctx->hist_depth[1 - ctx->hist_cur];
     d.visible_index = ctx->visible_index;
-    const uint2* in = ctx->reservoir;
-    for (int pass = 0; pass < cfg.denoise_passes; ++pass) {
-        const bool final = pass == cfg.denoise_passes - 1;
-        uint2* out = cfg.debug_keep_passes ? ctx->pass_bufs[pass] : (final ? nullptr : ctx->ping[pass & 1]);
-        d.pass = pass; d.res_in = in; d.res_out = out;
-        SGI_CUDA(ctx, sgi::launch_denoise_pass(d, s), "denoise_pass");
-        ctx->launches += 1;
-        in = out;
-    }
+    d.guide = ctx->guide;
+    d.res_in = in;
+    d.res_out = keep ? ctx->pass_bufs[cfg.denoise_passes - 1] : nullptr;
+    SGI_CUDA(ctx, sgi::launch_denoise_final(d, s), "denoise_final");
+    ctx->launches += 1;
     ctx->hist_cur = 1 - ctx->hist_cur;
     return SGI_OK;
 }
@@ -425,7 +438,9 @@ sgi_status sgi_read_debug(sgi_ctx* ctx, int32_t which, void* host_dst, size_t by
         case SGI_DEBUG_TILE_STAGE1: src = ctx->stage1; size = sizeof(sgi_tile_stage1) * ctx->num_tiles; break;
         case SGI_DEBUG_TILE_LISTS:
             src = ctx->lists; size = sizeof(int32_t) * ctx->num_tiles * (1 + (size_t)ctx->cfg.max_vpls_per_tile); break;
-        case SGI_DEBUG_RESERVOIR: src = ctx->reservoir; size = P * sizeof(uint2); break;
+        case SGI_DEBUG_RESERVOIR:
+            if (!ctx->cfg.debug_keep_passes) return fail(ctx, SGI_ERR_ARG, "the raw reservoir needs debug_keep_passes");
+            src = ctx->reservoir; size = P * sizeof(uint2); break;
         case SGI_DEBUG_GI_HISTORY: src = ctx->gi_hist[ctx->hist_cur]; size = P * sizeof(uint2); break;
         case SGI_DEBUG_HISTORY_DEPTH: src = ctx->hist_depth[ctx->hist_cur]; size = P * sizeof(uint16_t); break;
         case SGI_DEBUG_DIRECT: src = ctx->direct; size = P * sizeof(uint2); break;

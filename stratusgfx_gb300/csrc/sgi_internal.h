@@ -21,9 +21,18 @@ struct ShadeConfig {
     float emission_strength;
 };
 
+// Outputs of the gather kernel. Its epilogue also performs denoise pass 0
+// (the centre-only reservoir merge) and records the per-pixel guide that the
+// later passes read instead of re-decoding normals.
+struct GatherOut {
+    uint2* merged;           // RGBA16F pass-0 output (shadowFactor, 1)
+    float4* guide;           // decoded centre normal (xyz) and window depth (w)
+    uint2* raw;              // RGBA16F raw reservoir (vplColor, validSamples); may be null
+};
+
 struct DenoiseLaunch {
     int32_t width, height;
-    int32_t pass;            // 0 .. passes-1
+    int32_t pass;            // 1 .. passes-1
     int32_t passes;
     float time;
     float fps;
@@ -40,6 +49,7 @@ struct DenoiseLaunch {
     const uint16_t* hist_prev;  // historyDepth, R16F
     uint16_t* hist_out;         // newHistoryDepth, R16F (final pass)
     const int32_t* visible_index;  // [0] = numVisible
+    const float4* guide;     // from the gather
 };
 
 cudaError_t launch_vis_flags(const sgi_vpl* vpls, int32_t n, const sgi_csm& csm, uint8_t* flags, cudaStream_t s);
@@ -51,9 +61,13 @@ cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1,
                                const int32_t* visible_index, int32_t* lists, cudaStream_t s);
 cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam,
                           const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index,
-                          const int32_t* lists, const sgi_cube_atlas& cubes, float time, uint2* reservoir,
+                          const int32_t* lists, const sgi_cube_atlas& cubes, float time, const GatherOut& out,
                           cudaStream_t s);
-cudaError_t launch_denoise_pass(const DenoiseLaunch& d, cudaStream_t s);
+// a-trous pass `pass` (1 .. passes-2): 5x5 taps at stride 2^pass
+cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in,
+                          uint2* res_out, cudaStream_t s);
+// last pass: a-trous filter + temporal reprojection + composite
+cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s);
 cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
                             const sgi_camera& cam, const sgi_point_light* points, int32_t num_points,
                             const sgi_csm& csm, uint2* hdr_out, cudaStream_t s);

@@ -35,7 +35,7 @@ template <class F> SGI_D float bilinear(F fetch, int W, int H, float s, float t)
     int i0 = tex_index(fu, W), i1 = tex_index(fu + 1.0f, W);
     int j0 = tex_index(fv, H), j1 = tex_index(fv + 1.0f, H);
     float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
-    return ((fetch(i0, j0) * w00 + fetch(i1, j0) * w10) + fetch(i0, j1) * w01) + fetch(i1, j1) * w11;
+    return __fmaf_rn(fetch(i1, j1), w11, __fmaf_rn(fetch(i0, j1), w01, __fmaf_rn(fetch(i1, j0), w10, fetch(i0, j0) * w00)));
 }
 
 // ------------------------------------------------------------------- CSM --
@@ -52,7 +52,7 @@ SGI_D float csm_pcf(const float* __restrict__ base, int R, float s, float t, flo
     float c01 = ref <= __ldg(base + (size_t)j1 * R + i0) ? 1.0f : 0.0f;
     float c11 = ref <= __ldg(base + (size_t)j1 * R + i1) ? 1.0f : 0.0f;
     float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
-    return ((c00 * w00 + c10 * w10) + c01 * w01) + c11 * w11;
+    return __fmaf_rn(c11, w11, __fmaf_rn(c01, w01, __fmaf_rn(c10, w10, c00 * w00)));
 }
 
 // calculateInfiniteShadowValue, pbr.glsl:158-227: lit fraction.
@@ -69,8 +69,8 @@ SGI_D float infinite_shadow(const sgi_csm& csm, V3 fragPos, V3 normal, bool useD
     int index2 = beyond3 ? 3 : 1;
     V4 c1 = mat4_mul(csm.cascade_proj_view[index1], position.x, position.y, position.z, 1.0f);
     V4 c2 = mat4_mul(csm.cascade_proj_view[index2], position.x, position.y, position.z, 1.0f);
-    V3 cc1 = v3(c1.x / c1.w, c1.y / c1.w, c1.z / c1.w) * 0.5f + v3s(0.5f);
-    V3 cc2 = v3(c2.x / c2.w, c2.y / c2.w, c2.z / c2.w) * 0.5f + v3s(0.5f);
+    V3 cc1 = (v3(c1.x, c1.y, c1.z) / c1.w) * 0.5f + v3s(0.5f);
+    V3 cc2 = (v3(c2.x, c2.y, c2.z) / c2.w) * 0.5f + v3s(0.5f);
     float depth1 = cc1.z;
     float depth2 = beyond3 ? saturate(cc2.z) : cc2.z;
     float weight = beyond2 ? saturate(blends.y) - saturate(blends.z) : 1.0f - saturate(blends.x);
@@ -373,7 +373,7 @@ struct GatherParams {
     const int32_t* lists;
     sgi_cube_atlas cubes;
     float time;
-    uint2* reservoir;
+    GatherOut out;
 };
 
 // vpl_pbr_gi.fs:81-207, one thread per pixel.
@@ -467,19 +467,42 @@ __global__ void __launch_bounds__(256) vpl_gather_kernel(GatherParams p) {
     }
     validSamples = gmax(validSamples, 1.0f);
     const V3 b = vmin(vplColor, kHalfMax);
-    p.reservoir[i] = pack_h4(b.x, b.y, b.z, validSamples);
+    // The reservoir as stored in its RGBA16F target (vpl_pbr_gi.fs:205).
+    const float r0 = h2f(f2h(b.x)), r1 = h2f(f2h(b.y)), r2 = h2f(f2h(b.z)), r3 = h2f(f2h(validSamples));
+    if (p.out.raw) p.out.raw[i] = pack_h4(r0, r1, r2, r3);
+    // Denoise pass 0 for this pixel: computeMergedReservoir with minmaxNearest = 0
+    // (vpl_pbr_gi_denoise.fs:192-273) reads only the centre texel, which is this one.
+    const float depth = __ldg(p.g.depth + i);
+    float cr0 = 0.0f, cr1 = 0.0f, cr2 = 0.0f, cr3 = 0.0f;
+    const float depthCutoff = 0.1f * depth;
+    float runningSum = 0.0f;
+    const float probabilisticWeight = 1.0f / float(__ldg(p.visible_index));
+    if (!(dot(normal, normal) < 0.906f)) {
+        if (!(gabs(depth - depth) > depthCutoff)) {
+            const float randUpdate = random3(seedX, seedY, p.time);
+            const float probability = r3 * probabilisticWeight;
+            cr3 += probability;
+            if (randUpdate < (probability / cr3)) {
+                cr0 += r0; cr1 += r1; cr2 += r2;
+                runningSum += r3;
+            }
+        }
+    }
+    const float den = gmax(kEps, runningSum);
+    p.out.merged[i] = pack_h4(cr0 / den, cr1 / den, cr2 / den, 1.0f);
+    p.out.guide[i] = make_float4(normal.x, normal.y, normal.z, depth);
 }
 
 cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam,
                           const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index,
-                          const int32_t* lists, const sgi_cube_atlas& cubes, float time, uint2* reservoir,
+                          const int32_t* lists, const sgi_cube_atlas& cubes, float time, const GatherOut& out,
                           cudaStream_t s) {
     GatherParams p;
     p.W = cfg.width; p.H = cfg.height; p.ts = cfg.tile_size;
     p.tiles_x = (cfg.width + cfg.tile_size - 1) / cfg.tile_size;
     p.L = cfg.max_vpls_per_tile; p.tiled = cfg.gi_mode == SGI_GI_TILED; p.spp = cfg.samples_per_pixel;
     p.sc = sc; p.g = g; p.cam = cam; p.cv = cv; p.ce = ce; p.visible_index = visible_index; p.lists = lists;
-    p.cubes = cubes; p.time = time; p.reservoir = reservoir;
+    p.cubes = cubes; p.time = time; p.out = out;
     dim3 block(16, 16);
     dim3 grid((cfg.width + 15) / 16, (cfg.height + 15) / 16);
     vpl_gather_kernel<<<grid, block, 0, s>>>(p);
@@ -487,78 +510,80 @@ cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sg
 }
 
 // =============================================================== denoise --
-// One pass of vpl_pbr_gi_denoise.fs:275-435 (pass 0 merges reservoirs, the
-// last pass reprojects and composites).
-__global__ void __launch_bounds__(256) denoise_pass_kernel(DenoiseLaunch d) {
+// The 5x5 edge-stopping filter of vpl_pbr_gi_denoise.fs:307-327 with the
+// weights of filterInput (:142-190): w = pow(max(0, n_c . n_q), 128) *
+// exp(-|z_c - z_q|) / sigmaZ, centre weight 1, taps at stride 2^pass, clamped
+// to the edge. Normals and depths come from the gather's guide (the same
+// decoded values the shader computes per tap).
+SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __restrict__ guide,
+                         const uint2* __restrict__ res_in, V3 cn, float cd, float& rf0, float& rf1, float& rf2,
+                         float& rf3) {
+    rf0 = rf1 = rf2 = rf3 = 0.0f;
+    for (int dx = -2; dx <= 2; ++dx) {
+        int xx = x + dx * step;
+        xx = xx < 0 ? 0 : (xx > W - 1 ? W - 1 : xx);
+#pragma unroll
+        for (int dy = -2; dy <= 2; ++dy) {
+            int yy = y + dy * step;
+            yy = yy < 0 ? 0 : (yy > H - 1 ? H - 1 : yy);
+            const size_t j = (size_t)yy * W + xx;
+            float a, b, c, e;
+            unpack_h4(ld_u2(res_in, j), a, b, c, e);
+            float filtered;
+            if (dx == 0 && dy == 0) {
+                filtered = 1.0f;
+            } else {
+                const float4 gq = __ldg(guide + j);
+                const float wz = expf_ieee(-gabs(cd - gq.w)) / 1.0f;
+                float wn = gmax(0.0f, dot(cn, v3(gq.x, gq.y, gq.z)));
+                wn = pow128(wn);
+                filtered = wn * wz * 1.0f;
+            }
+            rf0 = __fmaf_rn(filtered, a, rf0);
+            rf1 = __fmaf_rn(filtered, b, rf1);
+            rf2 = __fmaf_rn(filtered, c, rf2);
+            rf3 = __fmaf_rn(filtered, e, rf3);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) atrous_kernel(int W, int H, int step, const float4* __restrict__ guide,
+                                                     const uint2* __restrict__ res_in, uint2* __restrict__ res_out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * W + x;
+    const float4 gc = __ldg(guide + i);
+    float rf0, rf1, rf2, rf3;
+    atrous_filter(x, y, W, H, step, guide, res_in, v3(gc.x, gc.y, gc.z), gc.w, rf0, rf1, rf2, rf3);
+    const float den = gmax(kEps, rf3);
+    res_out[i] = pack_h4(rf0 / den, rf1 / den, rf2 / den, 1.0f);
+}
+
+cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in,
+                          uint2* res_out, cudaStream_t s) {
+    dim3 block(32, 8);
+    dim3 grid((W + 31) / 32, (H + 7) / 8);
+    atrous_kernel<<<grid, block, 0, s>>>(W, H, 1 << pass, guide, res_in, res_out);
+    return cudaGetLastError();
+}
+
+// Final pass (final = true): the filter above, then temporal reprojection
+// (vpl_pbr_gi_denoise.fs:336-429) and the composite screen + gi * illumAvg (:431).
+__global__ void __launch_bounds__(256) denoise_final_kernel(DenoiseLaunch d) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int W = d.width, H = d.height;
     if (x >= W || y >= H) return;
     const size_t i = (size_t)y * W + x;
-    const int multiplier = (1 << d.pass) - 1;
-    const bool final = d.pass == d.passes - 1;
-    const bool merge = d.pass == 0;
     const float u = (float(x) + 0.5f) / float(W), v = (float(y) + 0.5f) / float(H);
-    const V3 centerNormal = decode_normal(__ldg(d.cur.normal + i));
-    const float centerDepth = __ldg(d.cur.depth + i);
-    float rf0 = 0.0f, rf1 = 0.0f, rf2 = 0.0f, rf3 = 0.0f;
-    if (merge) {
-        // computeMergedReservoir, vpl_pbr_gi_denoise.fs:192-273 (centre only)
-        float cr0 = 0.0f, cr1 = 0.0f, cr2 = 0.0f, cr3 = 0.0f;
-        const float depthCutoff = 0.1f * centerDepth;
-        float runningSum = 0.0f;
-        const float probabilisticWeight = 1.0f / float(__ldg(d.visible_index));
-        const V3 currNormal = decode_normal(__ldg(d.cur.normal + i));
-        if (!(dot(centerNormal, currNormal) < 0.906f)) {
-            const float currDepth = __ldg(d.cur.depth + i);
-            if (!(gabs(currDepth - centerDepth) > depthCutoff)) {
-                float a, b, c, e;
-                unpack_h4(ld_u2(d.res_in, i), a, b, c, e);
-                const float randUpdate = random3(float(x) + 0.5f, float(y) + 0.5f, d.time);
-                const float probability = e * probabilisticWeight;
-                cr3 += probability;
-                if (randUpdate < (probability / cr3)) {
-                    cr0 += a; cr1 += b; cr2 += c;
-                    runningSum += e;
-                }
-            }
-        }
-        rf0 = cr0; rf1 = cr1; rf2 = cr2; rf3 = runningSum;
-    } else {
-        const int step = 1 + multiplier;
-        for (int dx = -2; dx <= 2; ++dx) {
-            int xx = x + dx * step;
-            xx = xx < 0 ? 0 : (xx > W - 1 ? W - 1 : xx);
-            for (int dy = -2; dy <= 2; ++dy) {
-                int yy = y + dy * step;
-                yy = yy < 0 ? 0 : (yy > H - 1 ? H - 1 : yy);
-                const size_t j = (size_t)yy * W + xx;
-                float a, b, c, e;
-                unpack_h4(ld_u2(d.res_in, j), a, b, c, e);
-                float filtered;
-                if (dx == 0 && dy == 0) {
-                    filtered = 1.0f;
-                } else {   // filterInput, vpl_pbr_gi_denoise.fs:142-190
-                    const float currDepth = __ldg(d.cur.depth + j);
-                    const float wz = expf_ieee(-gabs(centerDepth - currDepth)) / 1.0f;
-                    const V3 currNormal = decode_normal(__ldg(d.cur.normal + j));
-                    float wn = gmax(0.0f, dot(centerNormal, currNormal));
-                    wn = pow128(wn);
-                    filtered = wn * wz * 1.0f;
-                }
-                rf0 = rf0 + filtered * a;
-                rf1 = rf1 + filtered * b;
-                rf2 = rf2 + filtered * c;
-                rf3 = rf3 + filtered * e;
-            }
-        }
-    }
+    const float4 gc = __ldg(d.guide + i);
+    const V3 centerNormal = v3(gc.x, gc.y, gc.z);
+    const float centerDepth = gc.w;
+    float rf0, rf1, rf2, rf3;
+    atrous_filter(x, y, W, H, 1 << d.pass, d.guide, d.res_in, centerNormal, centerDepth, rf0, rf1, rf2, rf3);
     const float den = gmax(kEps, rf3);
     const V3 shadowFactor = v3(rf0 / den, rf1 / den, rf2 / den);
-    if (!final) {
-        d.res_out[i] = pack_h4(shadowFactor.x, shadowFactor.y, shadowFactor.z, 1.0f);
-        return;
-    }
     if (d.res_out) d.res_out[i] = pack_h4(shadowFactor.x, shadowFactor.y, shadowFactor.z, 1.0f);
     // indirectIllumination: the gather colour output baseColor + 1e-5 as RGB16F
     const uint32_t alb = __ldg(d.cur.albedo + i);
@@ -604,10 +629,10 @@ __global__ void __launch_bounds__(256) denoise_pass_kernel(DenoiseLaunch d) {
     d.hist_out[i] = f2h(historyAccum);
 }
 
-cudaError_t launch_denoise_pass(const DenoiseLaunch& d, cudaStream_t s) {
+cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s) {
     dim3 block(32, 8);
     dim3 grid((d.width + 31) / 32, (d.height + 7) / 8);
-    denoise_pass_kernel<<<grid, block, 0, s>>>(d);
+    denoise_final_kernel<<<grid, block, 0, s>>>(d);
     return cudaGetLastError();
 }
 

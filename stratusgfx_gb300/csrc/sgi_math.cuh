@@ -2,17 +2,23 @@
 //
 // Every translation unit that includes this header is compiled with
 // -fmad=false, -prec-div=true and -prec-sqrt=true: each +, -, *, / and sqrtf
-// below is one correctly rounded binary32 operation, evaluated in the order
-// the expression tree gives. That makes the results reproducible on any
-// IEEE-754 machine, which is how the per-pixel results are checked bit for
-// bit against a CPU restatement of the StratusGFX shaders. No CUDA math-library
+// below is one correctly rounded binary32 operation, and multiply-adds are
+// fused only where __fmaf_rn is written, evaluated in the order the
+// expression tree gives. That makes the results reproducible on any IEEE-754
+// machine, which is how the per-pixel results are checked bit for bit against
+// a CPU restatement of the StratusGFX shaders. No CUDA math-library
 // transcendental is called: exp is computed by Cody-Waite range reduction
 // plus a degree-7 Taylor polynomial, and pow only appears with the integer
 // exponents 5 and 128.
 //
+// Implementation-defined GLSL arithmetic, fixed here: dot products, matrix
+// rows, polynomial steps and weighted sums are fused multiply-add chains;
+// a vector divided by a scalar is multiplied by the scalar's correctly
+// rounded reciprocal; normalize(v) = v * (1 / sqrt(dot(v, v))).
+//
 // GLSL built-in semantics used throughout (GLSL 4.60 spec wording):
 //   min(x, y) = y < x ? y : x,  max(x, y) = x < y ? y : x,
-//   clamp(x, a, b) = min(max(x, a), b),  mix(x, y, a) = x*(1-a) + y*a.
+//   clamp(x, a, b) = min(max(x, a), b),  mix(x, y, a) = fma(y, a, x*(1-a)).
 #pragma once
 
 #include <cuda_fp16.h>
@@ -31,7 +37,8 @@ SGI_D float gmin(float x, float y) { return y < x ? y : x; }
 SGI_D float gmax(float x, float y) { return x < y ? y : x; }
 SGI_D float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
 SGI_D float saturate(float x) { return gclamp(x, 0.0f, 1.0f); }
-SGI_D float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+SGI_D float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+SGI_D float mixf(float x, float y, float a) { return __fmaf_rn(y, a, x * (1.0f - a)); }
 SGI_D float gabs(float x) { return x < 0.0f ? -x : x; }
 
 // exp(x): Cody & Waite (1980) reduction x = k*ln2 + r with ln2 split into a
@@ -44,13 +51,13 @@ SGI_D float expf_ieee(float x) {
     float kf = floorf(x * 1.44269502162933349609375f + 0.5f);
     int k = (int)kf;
     float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187045037746429443359375e-06f;
-    float p = r * (1.0f / 5040.0f) + (1.0f / 720.0f);
-    p = p * r + (1.0f / 120.0f);
-    p = p * r + (1.0f / 24.0f);
-    p = p * r + (1.0f / 6.0f);
-    p = p * r + 0.5f;
-    p = p * r + 1.0f;
-    p = p * r + 1.0f;
+    float p = __fmaf_rn(r, 1.0f / 5040.0f, 1.0f / 720.0f);
+    p = __fmaf_rn(p, r, 1.0f / 120.0f);
+    p = __fmaf_rn(p, r, 1.0f / 24.0f);
+    p = __fmaf_rn(p, r, 1.0f / 6.0f);
+    p = __fmaf_rn(p, r, 0.5f);
+    p = __fmaf_rn(p, r, 1.0f);
+    p = __fmaf_rn(p, r, 1.0f);
     if (k > 127) { p = p * 1.7014118346046923e+38f; k -= 127; }
     if (k < -126) { p = p * 1.1754943508222875e-38f; k += 126; }
     return p * __int_as_float((k + 127) << 23);
@@ -70,34 +77,39 @@ SGI_D V3 operator*(V3 a, V3 b) { return V3{a.x * b.x, a.y * b.y, a.z * b.z}; }
 SGI_D V3 operator/(V3 a, V3 b) { return V3{a.x / b.x, a.y / b.y, a.z / b.z}; }
 SGI_D V3 operator*(V3 a, float s) { return V3{a.x * s, a.y * s, a.z * s}; }
 SGI_D V3 operator*(float s, V3 a) { return V3{s * a.x, s * a.y, s * a.z}; }
-SGI_D V3 operator/(V3 a, float s) { return V3{a.x / s, a.y / s, a.z / s}; }
+SGI_D V3 operator/(V3 a, float s) { const float r = 1.0f / s; return V3{a.x * r, a.y * r, a.z * r}; }
 SGI_D V3 operator+(V3 a, float s) { return V3{a.x + s, a.y + s, a.z + s}; }
 SGI_D V3 operator-(V3 a, float s) { return V3{a.x - s, a.y - s, a.z - s}; }
 SGI_D V3 operator-(float s, V3 a) { return V3{s - a.x, s - a.y, s - a.z}; }
 SGI_D V3 operator/(float s, V3 a) { return V3{s / a.x, s / a.y, s / a.z}; }
-SGI_D float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+SGI_D float dot(V3 a, V3 b) { return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, a.x * b.x)); }
 SGI_D float length(V3 a) { return sqrtf(dot(a, a)); }
-SGI_D V3 normalize(V3 a) { return a / sqrtf(dot(a, a)); }
+SGI_D V3 normalize(V3 a) { const float r = 1.0f / sqrtf(dot(a, a)); return a * r; }
 SGI_D V3 vmin(V3 a, float s) { return V3{gmin(a.x, s), gmin(a.y, s), gmin(a.z, s)}; }
-SGI_D V3 vmix(V3 x, V3 y, float a) { return x * (1.0f - a) + y * a; }
+SGI_D V3 vmix(V3 x, V3 y, float a) {
+    const float b = 1.0f - a;
+    return V3{__fmaf_rn(y.x, a, x.x * b), __fmaf_rn(y.y, a, x.y * b), __fmaf_rn(y.z, a, x.z * b)};
+}
 
 struct V4 { float x, y, z, w; };
 // column-major mat4 times (x, y, z, w), column-wise accumulation
 SGI_D V4 mat4_mul(const float* m, float x, float y, float z, float w) {
     V4 r;
-    r.x = ((m[0] * x + m[4] * y) + m[8] * z) + m[12] * w;
-    r.y = ((m[1] * x + m[5] * y) + m[9] * z) + m[13] * w;
-    r.z = ((m[2] * x + m[6] * y) + m[10] * z) + m[14] * w;
-    r.w = ((m[3] * x + m[7] * y) + m[11] * z) + m[15] * w;
+    r.x = __fmaf_rn(m[12], w, __fmaf_rn(m[8], z, __fmaf_rn(m[4], y, m[0] * x)));
+    r.y = __fmaf_rn(m[13], w, __fmaf_rn(m[9], z, __fmaf_rn(m[5], y, m[1] * x)));
+    r.z = __fmaf_rn(m[14], w, __fmaf_rn(m[10], z, __fmaf_rn(m[6], y, m[2] * x)));
+    r.w = __fmaf_rn(m[15], w, __fmaf_rn(m[11], z, __fmaf_rn(m[7], y, m[3] * x)));
     return r;
 }
-SGI_D float dot4(const float* pl, V3 p) { return ((pl[0] * p.x + pl[1] * p.y) + pl[2] * p.z) + pl[3] * 1.0f; }
+SGI_D float dot4(const float* pl, V3 p) {
+    return __fmaf_rn(pl[3], 1.0f, __fmaf_rn(pl[2], p.z, __fmaf_rn(pl[1], p.y, pl[0] * p.x)));
+}
 
 // worldPositionFromDepth, common.glsl:143-155
 SGI_D V3 world_from_depth(float u, float v, float depth, const float* inv_pv) {
     float z = depth * 2.0f - 1.0f;
     V4 w = mat4_mul(inv_pv, u * 2.0f - 1.0f, v * 2.0f - 1.0f, z, 1.0f);
-    return V3{w.x / w.w, w.y / w.w, w.z / w.w};
+    return V3{w.x, w.y, w.z} / w.w;
 }
 
 // hash / floatConstruct / random(vec3), common.glsl:183-214

@@ -40,7 +40,8 @@ class Setup:
         self.points = torch.from_numpy(self.sc.points).cuda() if len(self.sc.points) else None
 
     def stage(self, k=1, **cfgkw):
-        cfg = stage.workload_config(self.w, **cfgkw) if cfgkw else self.cfg
+        cfgkw.setdefault("debug_keep_passes", 1)
+        cfg = stage.workload_config(self.w, **cfgkw)
         st = stage.GiStage(cfg)
         st.set_lights(self.vpls, self.entries, self.points)
         st.set_shadow_maps(self.csm[k], self.cubes)

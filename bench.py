@@ -109,10 +109,14 @@ def pass_bytes(w, num_points: int) -> dict:
     """Bytes each pass must move per launch (each input read once, each output written once)."""
     P = w.width * w.height
     cube = 2 if w.cube_format == 1 else 4
-    gather = P * (4 + 4 + 4 + 4 + 2 + 2 + 8 + w.samples * cube)
-    merge_or_atrous = P * (8 + 4 + 4 + 8)
-    final = P * (8 + 4 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 8 + 2 + 8 + 8 + 2)
-    denoise = merge_or_atrous * (w.denoise_passes - 1) + final
+    # gather: depth, normal, albedo, rma (4 B each), reflectivity, ssao (2 B each), K cube texels;
+    # writes the pass-0 reservoir (8 B) and the guide (16 B)
+    gather = P * (4 + 4 + 4 + 4 + 2 + 2 + w.samples * cube + 8 + 16)
+    atrous = P * (8 + 16 + 8)
+    # final: reservoir, guide, albedo, screen, velocity, id, prev depth/normal/id, prev GI, history in;
+    # HDR, GI, history out
+    final = P * (8 + 16 + 4 + 8 + 4 + 4 + 4 + 4 + 4 + 8 + 2 + 8 + 8 + 2)
+    denoise = atrous * (w.denoise_passes - 2) + final
     deferred = P * (4 + 4 + 4 + 4 + 2 + 2 + 8) + 4 * w.csm_resolution ** 2 * 4
     tiles = P * (4 + 4)
     vis = w.num_vpls * (64 + 8 + 4 + 1)

@@ -269,95 +269,188 @@ cudaError_t launch_tile_stage1(const sgi_config& cfg, const sgi_gbuffer& g, cons
     return cudaGetLastError();
 }
 
-// Stage 2: one warp per tile, 8 tiles per block. The candidate list (L <= 64
-// slots, key = distance/radius) lives in registers, slot s in lane s % 32.
-// VPLs are visited in ascending compacted index; a candidate is inserted iff
-// its key is strictly below the current L-th key, at the position after all
-// keys <= it (strict '<' of vpl_tiled_deferred_culling_stage2.cs:100-121), so
-// the list equals the first L of the stable sort by key.
-constexpr int kStage2Chunk = 1024;
+// Stage 2: one warp per tile. vpl_tiled_deferred_culling_stage2.cs:61-129
+// inserts the visible VPLs, in order, into a list sorted by key =
+// distance / radius with a strict '<' (ties keep the earlier VPL) and keeps
+// the first L: the result is the first L entries of the stable sort of the
+// candidates by key. This kernel computes that set without the sequential
+// insertions, whose number depends on the VPL order:
+//   1. every candidate's key (as an order-preserving uint) goes to shared memory;
+//   2. if there are more than L candidates, a 4-round radix select (8 bits per
+//      round) finds the L-th smallest key tau and how many keys equal to tau
+//      are still needed;
+//   3. keys < tau, then the needed keys == tau in index order, are compacted;
+//   4. a 64-element warp bitonic sort orders them by (key, index).
+constexpr uint32_t kNoKey = 0xffffffffu;
 
-__global__ void __launch_bounds__(256) tile_stage2_kernel(int num_tiles, int L,
+SGI_D uint32_t order_key(float k) {     // float order -> uint order (-0 == +0)
+    const uint32_t b = __float_as_uint(k == 0.0f ? 0.0f : k);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+SGI_D bool key_less(uint32_t ka, int ia, uint32_t kb, int ib) { return ka < kb || (ka == kb && ia < ib); }
+
+// One compare-exchange stage of a bitonic network over 64 elements held as
+// (k0, i0) at position lane and (k1, i1) at position lane + 32.
+SGI_D void bitonic_stage(uint32_t& k0, int& i0, uint32_t& k1, int& i1, int size, int j, int lane) {
+    const unsigned FULL = 0xffffffffu;
+    if (j == 32) {
+        // partners are the two registers of this lane; size == 64 -> ascending
+        if (key_less(k1, i1, k0, i0)) { uint32_t tk = k0; int ti = i0; k0 = k1; i0 = i1; k1 = tk; i1 = ti; }
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        uint32_t& k = r ? k1 : k0;
+        int& id = r ? i1 : i0;
+        const int pos = lane + 32 * r;
+        const uint32_t ok = __shfl_xor_sync(FULL, k, j);
+        const int oi = __shfl_xor_sync(FULL, id, j);
+        const bool ascending = (pos & size) == 0;
+        const bool lower = (pos & j) == 0;
+        const bool other_less = key_less(ok, oi, k, id);
+        // the lower position keeps the min when ascending, the max otherwise
+        const bool take_other = (lower == ascending) ? other_less : !other_less;
+        if (take_other) { k = ok; id = oi; }
+    }
+}
+
+__global__ void __launch_bounds__(256) tile_stage2_kernel(int num_tiles, int L, int key_stride,
                                                           const sgi_tile_stage1* __restrict__ s1,
                                                           const sgi_vpl* __restrict__ cv,
                                                           const int32_t* __restrict__ visible_index,
                                                           int32_t* __restrict__ lists) {
-    __shared__ float4 sv[kStage2Chunk];
+    extern __shared__ uint32_t smem[];
     const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tile = blockIdx.x * (blockDim.x >> 5) + warp;
-    const bool active = tile < num_tiles;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    const int tile = blockIdx.x * warps + warp;
+    if (tile >= num_tiles) return;     // warps are independent: no block-wide barrier below
+    uint32_t* keys = smem + (size_t)warp * key_stride;
+    uint32_t* hist = smem + (size_t)warps * key_stride + warp * 256;
+    uint32_t* sel_k = smem + (size_t)warps * key_stride + warps * 256 + warp * 128;
+    int* sel_i = reinterpret_cast<int*>(sel_k + 64);
+    const unsigned lt_mask = (1u << lane) - 1u;
     const int count = __ldg(visible_index);
-    V3 fragPos = v3s(0.0f), normal = v3s(0.0f);
-    if (active) {
-        fragPos = v3(s1[tile].average_position[0], s1[tile].average_position[1], s1[tile].average_position[2]);
-        normal = v3(s1[tile].average_normal[0], s1[tile].average_normal[1], s1[tile].average_normal[2]);
-    }
-    float k0 = kFloatMax, k1 = kFloatMax;
-    int i0 = -1, i1 = -1;
-    int num = 0;
-    float thresh = kFloatMax;
-    for (int base = 0; base < count; base += kStage2Chunk) {
-        const int cn = count - base < kStage2Chunk ? count - base : kStage2Chunk;
-        __syncthreads();
-        for (int j = threadIdx.x; j < cn; j += blockDim.x) {
-            const float* rec = reinterpret_cast<const float*>(cv + base + j);
-            sv[j] = make_float4(__ldg(rec + 0), __ldg(rec + 1), __ldg(rec + 2), __ldg(rec + 12));
+    const V3 fragPos = v3(s1[tile].average_position[0], s1[tile].average_position[1], s1[tile].average_position[2]);
+    const V3 normal = v3(s1[tile].average_normal[0], s1[tile].average_normal[1], s1[tile].average_normal[2]);
+
+    // 1. keys of every visible VPL (kNoKey when it is not a candidate)
+    int mc = 0;
+    for (int base = 0; base < count; base += 32) {
+        const int k = base + lane;
+        bool cand = false;
+        uint32_t u = kNoKey;
+        if (k < count) {
+            const float* rec = reinterpret_cast<const float*>(cv + k);
+            const V3 lmf = v3(__ldg(rec + 0), __ldg(rec + 1), __ldg(rec + 2)) - fragPos;
+            const float side = dot(normal, lmf);
+            if (!(side < 0.0f)) {
+                const float ratio = length(lmf) / __ldg(rec + 12);
+                cand = !(ratio > 1.0f) && ratio < kFloatMax;
+                if (cand) u = order_key(ratio);
+            }
+            keys[k] = u;
         }
-        __syncthreads();
-        if (!active) continue;
-        for (int j = 0; j < cn; j += 32) {
-            bool cand = false;
-            float ratio = 0.0f;
-            if (j + lane < cn) {
-                float4 lv = sv[j + lane];
-                V3 lmf = v3(lv.x, lv.y, lv.z) - fragPos;
-                float side = dot(normal, lmf);
-                if (!(side < 0.0f)) {
-                    float d = length(lmf);
-                    ratio = d / lv.w;
-                    cand = !(ratio > 1.0f) && ratio < thresh;
+        mc += __popc(__ballot_sync(FULL, cand));
+    }
+    __syncwarp();
+    const int take = mc < L ? mc : L;
+
+    // 2. radix select of the take-th smallest key
+    uint32_t tau = kNoKey;
+    int need_eq = 0;
+    if (mc > L) {
+        uint32_t prefix = 0u, mask = 0u;
+        int remaining = L;
+        for (int shift = 24; shift >= 0; shift -= 8) {
+            for (int b = lane; b < 256; b += 32) hist[b] = 0u;
+            __syncwarp();
+            for (int k = lane; k < count; k += 32) {
+                const uint32_t u = keys[k];
+                if (u != kNoKey && (u & mask) == prefix) atomicAdd(&hist[(u >> shift) & 0xffu], 1u);
+            }
+            __syncwarp();
+            uint32_t hv[8];
+            uint32_t sum = 0u;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) { hv[j] = hist[lane * 8 + j]; sum += hv[j]; }
+            uint32_t incl = sum;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t t = __shfl_up_sync(FULL, incl, off);
+                if (lane >= off) incl += t;
+            }
+            const unsigned found = __ballot_sync(FULL, incl >= (uint32_t)remaining);
+            const int src = __ffs(found) - 1;
+            int bin = 0;
+            uint32_t below = 0u;
+            if (lane == src) {
+                uint32_t c = incl - sum;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if (c + hv[j] >= (uint32_t)remaining) { bin = lane * 8 + j; below = c; break; }
+                    c += hv[j];
                 }
             }
-            unsigned m = __ballot_sync(FULL, cand);
-            while (m) {
-                const int b = __ffs(m) - 1;
-                m &= m - 1u;
-                const float r = __shfl_sync(FULL, ratio, b);
-                if (!(r < thresh)) continue;
-                const int p = __popc(__ballot_sync(FULL, k0 <= r)) + __popc(__ballot_sync(FULL, k1 <= r));
-                float k0u = __shfl_up_sync(FULL, k0, 1);
-                int i0u = __shfl_up_sync(FULL, i0, 1);
-                float k1u = __shfl_up_sync(FULL, k1, 1);
-                int i1u = __shfl_up_sync(FULL, i1, 1);
-                const float k31 = __shfl_sync(FULL, k0, 31);
-                const int i31 = __shfl_sync(FULL, i0, 31);
-                if (lane == 0) { k1u = k31; i1u = i31; }
-                const int kidx = base + j + b;
-                const int s0 = lane, s1i = lane + 32;
-                if (s0 < L) {
-                    if (s0 == p) { k0 = r; i0 = kidx; } else if (s0 > p) { k0 = k0u; i0 = i0u; }
-                }
-                if (s1i < L) {
-                    if (s1i == p) { k1 = r; i1 = kidx; } else if (s1i > p) { k1 = k1u; i1 = i1u; }
-                }
-                num = num + 1 < L ? num + 1 : L;
-                thresh = (L - 1) < 32 ? __shfl_sync(FULL, k0, L - 1) : __shfl_sync(FULL, k1, L - 33);
-            }
+            bin = __shfl_sync(FULL, bin, src);
+            below = __shfl_sync(FULL, below, src);
+            remaining -= (int)below;
+            prefix |= (uint32_t)bin << shift;
+            mask |= 0xffu << shift;
+            __syncwarp();
         }
+        tau = prefix;
+        need_eq = remaining;
     }
-    if (!active) return;
+
+    // 3. compaction in index order: keys < tau, then the first need_eq keys == tau
+    int pos = 0, eq_seen = 0;
+    for (int base = 0; base < count; base += 32) {
+        const int k = base + lane;
+        const uint32_t u = k < count ? keys[k] : kNoKey;
+        const bool eq = u == tau && u != kNoKey;
+        const unsigned meq = __ballot_sync(FULL, eq);
+        const int eq_rank = eq_seen + __popc(meq & lt_mask);
+        const bool sel = (u < tau) || (eq && eq_rank < need_eq);
+        const unsigned ms = __ballot_sync(FULL, sel);
+        if (sel) {
+            const int p = pos + __popc(ms & lt_mask);
+            sel_k[p] = u;
+            sel_i[p] = k;
+        }
+        pos += __popc(ms);
+        eq_seen += __popc(meq);
+    }
+    __syncwarp();
+
+    // 4. sort (key, index) ascending
+    uint32_t k0 = lane < take ? sel_k[lane] : kNoKey;
+    int i0 = lane < take ? sel_i[lane] : 0x7fffffff;
+    uint32_t k1 = lane + 32 < take ? sel_k[lane + 32] : kNoKey;
+    int i1 = lane + 32 < take ? sel_i[lane + 32] : 0x7fffffff;
+    if (take > 1) {
+        for (int size = 2; size <= 64; size <<= 1)
+            for (int j = size >> 1; j >= 1; j >>= 1) bitonic_stage(k0, i0, k1, i1, size, j, lane);
+    }
     int32_t* o = lists + (size_t)tile * (1 + L);
-    if (lane == 0) o[0] = num;
-    if (lane < L) o[1 + lane] = lane < num ? i0 : -1;
-    if (lane + 32 < L) o[33 + lane] = lane + 32 < num ? i1 : -1;
+    if (lane == 0) o[0] = take;
+    if (lane < L) o[1 + lane] = lane < take ? i0 : -1;
+    if (lane + 32 < L) o[33 + lane] = lane + 32 < take ? i1 : -1;
 }
 
 cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1, const sgi_vpl* cv,
                                const int32_t* visible_index, int32_t* lists, cudaStream_t s) {
     const int ts = cfg.tile_size;
     const int T = ((cfg.width + ts - 1) / ts) * ((cfg.height + ts - 1) / ts);
-    tile_stage2_kernel<<<(T + 7) / 8, 256, 0, s>>>(T, cfg.max_vpls_per_tile, s1, cv, visible_index, lists);
+    const int key_stride = (cfg.max_visible + 31) & ~31;
+    const size_t per_warp = (size_t)key_stride * 4 + 256 * 4 + 128 * 4;
+    int warps = (int)((200u * 1024u) / per_warp);
+    warps = warps > 8 ? 8 : (warps < 1 ? 1 : warps);
+    const size_t smem = per_warp * warps;
+    cudaError_t e = cudaFuncSetAttribute(tile_stage2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    tile_stage2_kernel<<<(T + warps - 1) / warps, warps * 32, smem, s>>>(T, cfg.max_vpls_per_tile, key_stride, s1, cv,
+                                                                           visible_index, lists);
     return cudaGetLastError();
 }
 

@@ -44,6 +44,7 @@ struct sgi_ctx {
     int32_t* visible_index = nullptr;
     sgi_tile_stage1* stage1 = nullptr;
     int32_t* lists = nullptr;
+    uint32_t* tile_keys = nullptr;
     int32_t num_tiles = 0;
     bool culled = false;
 
@@ -135,7 +136,7 @@ sgi::ShadeConfig make_shade(const sgi_config& c) {
 
 void free_all(sgi_ctx* c) {
     void* ptrs[] = {c->vpls, c->entries, c->points, c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
-                    c->reservoir, c->ping[0], c->ping[1], c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
+                    c->tile_keys, c->reservoir, c->ping[0], c->ping[1], c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
                     c->hist_depth[0], c->hist_depth[1]};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto* p : c->pass_bufs) if (p) cudaFree(p);
@@ -218,6 +219,7 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     chk(dalloc(&c->visible_index, 1 + (size_t)cfg->max_vpls));
     chk(dalloc(&c->stage1, c->num_tiles));
     chk(dalloc(&c->lists, (size_t)c->num_tiles * (1 + cfg->max_vpls_per_tile)));
+    chk(dalloc(&c->tile_keys, (size_t)c->num_tiles * (size_t)((cfg->max_visible + 31) & ~31)));
     chk(dalloc(&c->reservoir, cfg->debug_keep_passes ? P : 1));
     chk(dalloc(&c->guide, P));
     chk(dalloc(&c->ping[0], P));
@@ -314,9 +316,9 @@ sgi_status sgi_cull_tiles(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camer
     if (!ctx->culled) return fail(ctx, SGI_ERR_STATE, "sgi_cull_vpls must run before sgi_cull_tiles");
     cudaStream_t s = (cudaStream_t)stream;
     SGI_CUDA(ctx, sgi::launch_tile_stage1(ctx->cfg, *gbuf, *cam, ctx->stage1, s), "tile_stage1");
-    SGI_CUDA(ctx, sgi::launch_tile_stage2(ctx->cfg, ctx->stage1, ctx->cv, ctx->visible_index, ctx->lists, s),
-             "tile_stage2");
-    ctx->launches += 2;
+    SGI_CUDA(ctx, sgi::launch_tile_stage2(ctx->cfg, ctx->stage1, ctx->cv, ctx->visible_index, ctx->tile_keys,
+                                          ctx->lists, s), "tile_stage2");
+    ctx->launches += 3;
     return SGI_OK;
 }
 

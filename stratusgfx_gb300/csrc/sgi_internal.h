@@ -57,8 +57,9 @@ cudaError_t launch_compact(const sgi_vpl* vpls, const sgi_atlas_entry* entries, 
                            int32_t cap, sgi_vpl* cv, sgi_atlas_entry* ce, int32_t* visible_index, cudaStream_t s);
 cudaError_t launch_tile_stage1(const sgi_config& cfg, const sgi_gbuffer& g, const sgi_camera& cam,
                                sgi_tile_stage1* out, cudaStream_t s);
+// keys: scratch of tiles x round_up(max_visible, 32) uint32
 cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1, const sgi_vpl* cv,
-                               const int32_t* visible_index, int32_t* lists, cudaStream_t s);
+                               const int32_t* visible_index, uint32_t* keys, int32_t* lists, cudaStream_t s);
 cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam,
                           const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index,
                           const int32_t* lists, const sgi_cube_atlas& cubes, float time, const GatherOut& out,

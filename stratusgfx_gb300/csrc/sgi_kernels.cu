@@ -315,48 +315,57 @@ SGI_D void bitonic_stage(uint32_t& k0, int& i0, uint32_t& k1, int& i1, int size,
     }
 }
 
-__global__ void __launch_bounds__(256) tile_stage2_kernel(int num_tiles, int L, int key_stride,
-                                                          const sgi_tile_stage1* __restrict__ s1,
-                                                          const sgi_vpl* __restrict__ cv,
+// 2a. keys: one thread per (tile, VPL), fully parallel; keys[tile][k] in
+// global memory (L2-resident), kNoKey when the VPL is not a candidate.
+__global__ void __launch_bounds__(256) tile_keys_kernel(int num_tiles, int key_stride,
+                                                        const sgi_tile_stage1* __restrict__ s1,
+                                                        const sgi_vpl* __restrict__ cv,
+                                                        const int32_t* __restrict__ visible_index,
+                                                        uint32_t* __restrict__ keys) {
+    const int count = __ldg(visible_index);
+    const int k = blockIdx.y * blockDim.x + threadIdx.x;
+    const int tile = blockIdx.x;
+    if (k >= count || tile >= num_tiles) return;
+    const float4 p4 = __ldg(reinterpret_cast<const float4*>(s1 + tile));
+    const float4 n4 = __ldg(reinterpret_cast<const float4*>(s1 + tile) + 1);
+    const float* rec = reinterpret_cast<const float*>(cv + k);
+    const V3 lmf = v3(__ldg(rec + 0), __ldg(rec + 1), __ldg(rec + 2)) - v3(p4.x, p4.y, p4.z);
+    const float side = dot(v3(n4.x, n4.y, n4.z), lmf);
+    uint32_t u = kNoKey;
+    if (!(side < 0.0f)) {
+        const float ratio = length(lmf) / __ldg(rec + 12);
+        if (!(ratio > 1.0f) && ratio < kFloatMax) u = order_key(ratio);
+    }
+    keys[(size_t)tile * key_stride + k] = u;
+}
+
+// 2b. select: one warp per tile over its keys.
+__global__ void __launch_bounds__(256) tile_select_kernel(int num_tiles, int L, int key_stride,
+                                                          const uint32_t* __restrict__ all_keys,
                                                           const int32_t* __restrict__ visible_index,
                                                           int32_t* __restrict__ lists) {
-    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t hist_all[8][256];
+    __shared__ uint32_t sel_all[8][128];
     const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
-    const int tile = blockIdx.x * warps + warp;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tile = blockIdx.x * 8 + warp;
     if (tile >= num_tiles) return;     // warps are independent: no block-wide barrier below
-    uint32_t* keys = smem + (size_t)warp * key_stride;
-    uint32_t* hist = smem + (size_t)warps * key_stride + warp * 256;
-    uint32_t* sel_k = smem + (size_t)warps * key_stride + warps * 256 + warp * 128;
+    uint32_t* hist = hist_all[warp];
+    uint32_t* sel_k = sel_all[warp];
     int* sel_i = reinterpret_cast<int*>(sel_k + 64);
+    const uint32_t* keys = all_keys + (size_t)tile * key_stride;
     const unsigned lt_mask = (1u << lane) - 1u;
     const int count = __ldg(visible_index);
-    const V3 fragPos = v3(s1[tile].average_position[0], s1[tile].average_position[1], s1[tile].average_position[2]);
-    const V3 normal = v3(s1[tile].average_normal[0], s1[tile].average_normal[1], s1[tile].average_normal[2]);
 
-    // 1. keys of every visible VPL (kNoKey when it is not a candidate)
     int mc = 0;
     for (int base = 0; base < count; base += 32) {
         const int k = base + lane;
-        bool cand = false;
-        uint32_t u = kNoKey;
-        if (k < count) {
-            const float* rec = reinterpret_cast<const float*>(cv + k);
-            const V3 lmf = v3(__ldg(rec + 0), __ldg(rec + 1), __ldg(rec + 2)) - fragPos;
-            const float side = dot(normal, lmf);
-            if (!(side < 0.0f)) {
-                const float ratio = length(lmf) / __ldg(rec + 12);
-                cand = !(ratio > 1.0f) && ratio < kFloatMax;
-                if (cand) u = order_key(ratio);
-            }
-            keys[k] = u;
-        }
-        mc += __popc(__ballot_sync(FULL, cand));
+        const uint32_t u = k < count ? __ldg(keys + k) : kNoKey;
+        mc += __popc(__ballot_sync(FULL, u != kNoKey));
     }
-    __syncwarp();
     const int take = mc < L ? mc : L;
 
-    // 2. radix select of the take-th smallest key
+    // radix select of the take-th smallest key
     uint32_t tau = kNoKey;
     int need_eq = 0;
     if (mc > L) {
@@ -366,7 +375,7 @@ __global__ void __launch_bounds__(256) tile_stage2_kernel(int num_tiles, int L, 
             for (int b = lane; b < 256; b += 32) hist[b] = 0u;
             __syncwarp();
             for (int k = lane; k < count; k += 32) {
-                const uint32_t u = keys[k];
+                const uint32_t u = __ldg(keys + k);
                 if (u != kNoKey && (u & mask) == prefix) atomicAdd(&hist[(u >> shift) & 0xffu], 1u);
             }
             __syncwarp();
@@ -403,11 +412,11 @@ __global__ void __launch_bounds__(256) tile_stage2_kernel(int num_tiles, int L, 
         need_eq = remaining;
     }
 
-    // 3. compaction in index order: keys < tau, then the first need_eq keys == tau
+    // compaction in index order: keys < tau, then the first need_eq keys == tau
     int pos = 0, eq_seen = 0;
-    for (int base = 0; base < count; base += 32) {
+    for (int base = 0; base < count && pos < take; base += 32) {
         const int k = base + lane;
-        const uint32_t u = k < count ? keys[k] : kNoKey;
+        const uint32_t u = k < count ? __ldg(keys + k) : kNoKey;
         const bool eq = u == tau && u != kNoKey;
         const unsigned meq = __ballot_sync(FULL, eq);
         const int eq_rank = eq_seen + __popc(meq & lt_mask);
@@ -423,7 +432,7 @@ __global__ void __launch_bounds__(256) tile_stage2_kernel(int num_tiles, int L, 
     }
     __syncwarp();
 
-    // 4. sort (key, index) ascending
+    // sort (key, index) ascending
     uint32_t k0 = lane < take ? sel_k[lane] : kNoKey;
     int i0 = lane < take ? sel_i[lane] : 0x7fffffff;
     uint32_t k1 = lane + 32 < take ? sel_k[lane + 32] : kNoKey;
@@ -439,18 +448,15 @@ __global__ void __launch_bounds__(256) tile_stage2_kernel(int num_tiles, int L, 
 }
 
 cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1, const sgi_vpl* cv,
-                               const int32_t* visible_index, int32_t* lists, cudaStream_t s) {
+                               const int32_t* visible_index, uint32_t* keys, int32_t* lists, cudaStream_t s) {
     const int ts = cfg.tile_size;
     const int T = ((cfg.width + ts - 1) / ts) * ((cfg.height + ts - 1) / ts);
     const int key_stride = (cfg.max_visible + 31) & ~31;
-    const size_t per_warp = (size_t)key_stride * 4 + 256 * 4 + 128 * 4;
-    int warps = (int)((200u * 1024u) / per_warp);
-    warps = warps > 8 ? 8 : (warps < 1 ? 1 : warps);
-    const size_t smem = per_warp * warps;
-    cudaError_t e = cudaFuncSetAttribute(tile_stage2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 kgrid(T, (cfg.max_visible + 255) / 256);
+    tile_keys_kernel<<<kgrid, 256, 0, s>>>(T, key_stride, s1, cv, visible_index, keys);
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    tile_stage2_kernel<<<(T + warps - 1) / warps, warps * 32, smem, s>>>(T, cfg.max_vpls_per_tile, key_stride, s1, cv,
-                                                                           visible_index, lists);
+    tile_select_kernel<<<(T + 7) / 8, 256, 0, s>>>(T, cfg.max_vpls_per_tile, key_stride, keys, visible_index, lists);
     return cudaGetLastError();
 }
 
@@ -470,7 +476,7 @@ struct GatherParams {
 };
 
 // vpl_pbr_gi.fs:81-207, one thread per pixel.
-__global__ void __launch_bounds__(256) vpl_gather_kernel(GatherParams p) {
+__global__ void __launch_bounds__(256, 4) vpl_gather_kernel(GatherParams p) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= p.W || y >= p.H) return;
@@ -743,7 +749,7 @@ struct DeferredParams {
 
 // pbr.fs:82-145: non-shadow-casting point lights + the directional light
 // with its CSM (INFINITE_LIGHTING_ENABLED).
-__global__ void __launch_bounds__(256) deferred_pbr_csm_kernel(DeferredParams p) {
+__global__ void __launch_bounds__(256, 4) deferred_pbr_csm_kernel(DeferredParams p) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= p.W || y >= p.H) return;

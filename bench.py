@@ -194,47 +194,79 @@ def run_ours(args, rank, world, local_rank):
     ms_per_step = total_ms / args.steps
     value = world * P * args.steps / (total_ms / 1e3) / 1e6
 
-    # ---- e2e: host buffers through the public API (ABI), copies inside the timed region
+    # ---- e2e: host buffers through the public API (ABI), copies inside the timed region.
+    # Three G-buffer slots and two output buffers: the host->device copy of frame s+1 and the
+    # device->host copy of frame s-1 run on a copy stream while frame s renders.
     host_g = [g.pinned_clone() for g in ds.gbuffers]
     host_vpls = ds.vpls.cpu().pin_memory()
     host_entries = ds.entries.cpu().pin_memory()
     host_points = ds.points.cpu().pin_memory() if ds.points is not None else None
-    dev_vpls = torch.empty_like(ds.vpls)
-    dev_entries = torch.empty_like(ds.entries)
-    dev_points = torch.empty_like(ds.points) if ds.points is not None else None
-    slots = [stage.GBufferTensors(w.height, w.width, "cuda") for _ in range(2)]
+    dev_vpls = [torch.empty_like(ds.vpls) for _ in range(2)]
+    dev_entries = [torch.empty_like(ds.entries) for _ in range(2)]
+    dev_points = [torch.empty_like(ds.points) for _ in range(2)] if ds.points is not None else [None, None]
+    slots = [stage.GBufferTensors(w.height, w.width, "cuda") for _ in range(3)]
+    outs = [torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda") for _ in range(2)]
     host_out = torch.empty((w.height, w.width, 4), dtype=torch.float16).pin_memory()
     st2 = stage.GiStage(cfg)
     h2d = slots[0].nbytes()
     h2d += host_vpls.numel() * 4 + host_entries.numel() * 4 + (host_points.numel() * 4 if host_points is not None else 0)
     d2h = host_out.numel() * 2
-    slots[0].copy_from(host_g[0])
-    slots[1].copy_from(host_g[0])
+    comp = torch.cuda.current_stream()
+    copy = torch.cuda.Stream()
 
-    def e2e_frame(step):
+    def upload(step):
+        """Frame `step`'s inputs -> slot step % 3 and light buffers step % 2, on the copy stream."""
         k = step % frames + 1
-        cur, prev = slots[step % 2], slots[(step + 1) % 2]
-        cur.copy_from(host_g[k], non_blocking=True)
-        dev_vpls.copy_(host_vpls, non_blocking=True)
-        dev_entries.copy_(host_entries, non_blocking=True)
-        if dev_points is not None:
-            dev_points.copy_(host_points, non_blocking=True)
-        st2.set_lights(dev_vpls, dev_entries, dev_points)
-        st2.set_shadow_maps(ds.csms[k], ds.cubes)
-        st2.render_frame(cur, prev, ds.camera(k), out, 1000.0 + 16.0 * step, fps)
-        host_out.copy_(out, non_blocking=True)
+        with torch.cuda.stream(copy):
+            slots[step % 3].copy_from(host_g[k], non_blocking=True)
+            dev_vpls[step % 2].copy_(host_vpls, non_blocking=True)
+            dev_entries[step % 2].copy_(host_entries, non_blocking=True)
+            if dev_points[0] is not None:
+                dev_points[step % 2].copy_(host_points, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(copy)
+        return ev
 
-    for s in range(args.warmup):
-        e2e_frame(s)
+    def e2e_run(first, n, start_event=None):
+        """Renders frames first .. first+n-1 from host inputs to host outputs (asynchronous)."""
+        if start_event is not None:
+            copy.wait_event(start_event)
+        ready = upload(first)
+        done = [None, None]       # compute finished frame s (its inputs and lights are free)
+        fetched = [None, None]    # device->host copy of frame s finished (its output buffer is free)
+        for step in range(first, first + n):
+            k = step % frames + 1
+            comp.wait_event(ready)
+            if fetched[step % 2] is not None:
+                comp.wait_event(fetched[step % 2])
+            if step + 1 < first + n:
+                if done[(step + 1) % 2] is not None:
+                    copy.wait_event(done[(step + 1) % 2])
+                ready = upload(step + 1)
+            st2.set_lights(dev_vpls[step % 2], dev_entries[step % 2], dev_points[step % 2])
+            st2.set_shadow_maps(ds.csms[k], ds.cubes)
+            st2.render_frame(slots[step % 3], slots[(step - 1) % 3], ds.camera(k), outs[step % 2],
+                             1000.0 + 16.0 * step, fps)
+            ev = torch.cuda.Event()
+            ev.record(comp)
+            done[step % 2] = ev
+            with torch.cuda.stream(copy):
+                copy.wait_event(ev)
+                host_out.copy_(outs[step % 2], non_blocking=True)
+                f = torch.cuda.Event()
+                f.record(copy)
+                fetched[step % 2] = f
+
+    slots[2].copy_from(host_g[0])              # the frame before the first one
+    e2e_run(0, args.warmup)
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for s in range(args.steps):
-        e2e_frame(args.warmup + s)
-    e1.record()
+    e0.record(comp)
+    e2e_run(args.warmup, args.steps, e0)
+    e1.record(copy)                            # after the last device->host copy
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
     if world > 1:
@@ -281,11 +313,54 @@ def run_ours(args, rank, world, local_rank):
         "passes": per_pass,
         "clocks": clock,
     }
+    if rank == 0:
+        result["quality"] = quality_vs_converged(ds, sc, w, cfg)
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline_from_device(ds, sc, w, cfg)
     st.close()
     st2.close()
     return result
+
+
+def quality_vs_converged(ds, sc, w, cfg, batches=64):
+    """PSNR of the plain path's HDR frames against the converged image: the same frame with the
+    GI term replaced by sgi_gi_target (64 batches of K = 8 = 512 samples per pixel, FP64 sums).
+    Frames 1..8 of the camera path are rendered in order (history accumulates); PSNR and MSE are
+    reduced in FP64 on the GPU."""
+    import torch
+
+    from stratusgfx_gb300 import stage
+    st = stage.GiStage(cfg)
+    st.set_lights(ds.vpls, ds.entries, ds.points)
+    H, W = w.height, w.width
+    out = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+    target = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    direct = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+    frames = len(sc.cameras) - 1
+    psnrs = []
+    t_target = 0.0
+    for k in range(1, frames + 1):
+        st.set_shadow_maps(ds.csms[k], ds.cubes)
+        cam = ds.camera(k)
+        st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], cam, out, 1000.0 + 16.0 * k, 60.0)
+        st.direct_lighting(ds.gbuffers[k], cam, direct)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        st.gi_target(ds.gbuffers[k], cam, 1000.0 + 16.0 * k, batches, target)
+        e1.record()
+        torch.cuda.synchronize()
+        t_target += e0.elapsed_time(e1)
+        alb = ds.gbuffers[k].albedo[..., :3].double() / 255.0
+        gi = torch.clamp(alb, min=0.01) + 1e-5
+        ref = direct[..., :3].double() + gi * target[..., :3].double()
+        got = out[..., :3].double()
+        mse = torch.mean((got - ref) ** 2)
+        peak = torch.max(ref)
+        psnrs.append(float(10.0 * torch.log10(peak * peak / mse)))
+    st.close()
+    return {"psnr_db_vs_converged": [round(p, 2) for p in psnrs], "target": f"{batches} x K={w.samples} samples, "
+            f"FP64 sums", "target_ms_per_frame": round(t_target / frames, 2),
+            "psnr_mean_db": round(sum(psnrs) / len(psnrs), 2)}
 
 
 def cpu_baseline_from_device(ds, sc, w, cfg):

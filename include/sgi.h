@@ -248,6 +248,17 @@ sgi_status sgi_render_frame(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuf
                             const sgi_camera* cam, const sgi_frame_params* params,
                             void* hdr_out, void* stream);
 
+/* Converged GI target (no counterpart in the reference; the reference of the
+ * denoisers' error): `batches` independent runs of the gather's per-pixel
+ * sample loop (batch b starts its seed z at time + b * 2e5) with the sums of
+ * vplColor and validSamples accumulated in FP64. Writes per pixel the float4
+ * (sum vplColor / max(sum validSamples, 1), 1) to `target` (device, W*H
+ * float4): the value the K-sample estimate plus denoiser approximates. Uses
+ * this frame's culled lists: call after sgi_cull_vpls (and sgi_cull_tiles in
+ * tiled mode). 64 batches of K = 8 give the K = 512 target. */
+sgi_status sgi_gi_target(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera* cam, float time,
+                         int32_t batches, float* target, void* stream);
+
 /* Clears the denoiser history (vplGIDenoisedPrevFrameFbo). */
 sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream);
 

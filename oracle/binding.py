@@ -48,6 +48,8 @@ def load() -> C.CDLL:
             "oracle_tile_stage2": (None, [C.c_int, C.POINTER(abi.Config), P, P, C.c_int, P]),
             "oracle_gather": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.Camera), P,
                                      P, C.c_int, P, C.POINTER(abi.CubeAtlas), C.c_float, P]),
+            "oracle_gi_target": (None, [C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.Camera), P, P,
+                                        C.c_int, P, C.POINTER(abi.CubeAtlas), C.c_float, C.c_int, P]),
             "oracle_denoise": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.GBuffer),
                                       P, P, P, P, C.c_int, C.POINTER(abi.FrameParams), P, P, P, P]),
             "oracle_deferred": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.Camera),
@@ -158,6 +160,16 @@ def gather(prec, cfg, g: HostGBuffer, cam, cvpls, centries, count, lists, cubes:
     load().oracle_gather(prec, C.byref(cfg), C.byref(g.struct()), C.byref(cam), _p(cv), _p(ce), count,
                          _p(lists_arr), C.byref(cubes), time, _p(res))
     return res
+
+
+def gi_target(cfg, g: HostGBuffer, cam, cvpls, centries, count, lists, cubes: abi.CubeAtlas, time, batches):
+    out = np.zeros((cfg.height, cfg.width, 4), np.float32)
+    lists_arr = None if lists is None else np.ascontiguousarray(lists, dtype=np.int32)
+    cv = np.ascontiguousarray(cvpls, dtype=np.float32)
+    ce = np.ascontiguousarray(centries, dtype=np.int32)
+    load().oracle_gi_target(C.byref(cfg), C.byref(g.struct()), C.byref(cam), _p(cv), _p(ce), count, _p(lists_arr),
+                            C.byref(cubes), time, batches, _p(out))
+    return out
 
 
 def denoise(prec, cfg, cur: HostGBuffer, prev: HostGBuffer, reservoir, hdr_in, gi_prev, hist_prev, num_visible,

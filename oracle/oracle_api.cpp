@@ -100,6 +100,13 @@ void oracle_gather(int prec, const sgi_config* cfg, const sgi_gbuffer* g, const 
     else gather<double>(a, (double*)reservoir);
 }
 
+void oracle_gi_target(const sgi_config* cfg, const sgi_gbuffer* g, const sgi_camera* cam, const sgi_vpl* cv,
+                      const sgi_atlas_entry* ce, int count, const int32_t* lists, const sgi_cube_atlas* cubes,
+                      float time, int batches, float* out) {
+    GatherArgs a{cfg, g, cam, cv, ce, count, lists, cubes, time};
+    gi_target(a, batches, out);
+}
+
 // hdr_in, gi_prev: [P][4]; hist_prev: [P]; all buffers of the precision's type.
 void oracle_denoise(int prec, const sgi_config* cfg, const sgi_gbuffer* cur, const sgi_gbuffer* prev,
                     const void* reservoir, const void* hdr_in, const void* gi_prev, const void* hist_prev,

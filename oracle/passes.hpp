@@ -271,8 +271,10 @@ struct GatherArgs {
     float time;
 };
 
-// vpl_pbr_gi.fs:81-207 for one pixel. Writes (min(vplColor, 65504), validSamples).
-template <class T> void gather_pixel(const GatherArgs& a, int x, int y, T* res) {
+// vpl_pbr_gi.fs:81-200 for one pixel with the seed z starting at seedZ0:
+// accumulates vplColor and validSamples over the sample loop.
+template <class T> void gather_samples(const GatherArgs& a, int x, int y, float seedZ0, V3<T>& vplColorOut,
+                                       T& validOut) {
     const sgi_config& cfg = *a.cfg;
     const sgi_gbuffer& g = *a.g;
     const int W = cfg.width, H = cfg.height;
@@ -297,7 +299,7 @@ template <class T> void gather_pixel(const GatherArgs& a, int x, int y, T* res) 
     V3<T> baseRefl(refl);
     T roughnessWeight = T(1) - roughness;
     V3<T> vplColor(T(0));
-    float seedX = float(x) + 0.5f, seedY = float(y) + 0.5f, seedZ = a.time;
+    float seedX = float(x) + 0.5f, seedY = float(y) + 0.5f, seedZ = seedZ0;
     T validSamples = 0;
     T distRatio = gmin(T(1) - distToCamera / T(1000), T(1));
     int sampleCount;
@@ -359,6 +361,15 @@ template <class T> void gather_pixel(const GatherArgs& a, int x, int y, T* res) 
             vplColor = vplColor + (T(1) - shadowFactor) * tmp;
         }
     }
+    vplColorOut = vplColor;
+    validOut = validSamples;
+}
+
+// vpl_pbr_gi.fs:81-207 for one pixel. Writes (min(vplColor, 65504), validSamples).
+template <class T> void gather_pixel(const GatherArgs& a, int x, int y, T* res) {
+    V3<T> vplColor;
+    T validSamples;
+    gather_samples<T>(a, x, y, a.time, vplColor, validSamples);
     validSamples = gmax(validSamples, T(1));
     V3<T> bounded = vmin(vplColor, C<T>::HALF_MAX());
     res[0] = Prec<T>::store16(bounded.x);
@@ -372,6 +383,28 @@ template <class T> void gather(const GatherArgs& a, T* reservoir) {
 #pragma omp parallel for schedule(dynamic, 1)
     for (int y = 0; y < H; ++y)
         for (int x = 0; x < W; ++x) gather_pixel<T>(a, x, y, reservoir + ((size_t)y * W + x) * 4);
+}
+
+// Converged target: `batches` runs of the sample loop, batch b seeded at
+// time + b * 2e5, binary32 samples summed in binary64 (the CUDA target kernel's
+// definition). out[i] = (sum vplColor / max(sum valid, 1), 1).
+inline void gi_target(const GatherArgs& a, int batches, float* out) {
+    const int W = a.cfg->width, H = a.cfg->height;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            double c0 = 0, c1 = 0, c2 = 0, w = 0;
+            for (int b = 0; b < batches; ++b) {
+                V3<float> col;
+                float valid;
+                gather_samples<float>(a, x, y, a.time + float(b) * 200000.0f, col, valid);
+                c0 += (double)col.x; c1 += (double)col.y; c2 += (double)col.z; w += (double)valid;
+            }
+            double den = w < 1.0 ? 1.0 : w;
+            float* o = out + ((size_t)y * W + x) * 4;
+            o[0] = (float)(c0 / den); o[1] = (float)(c1 / den); o[2] = (float)(c2 / den); o[3] = 1.0f;
+        }
+    }
 }
 
 template <class T> struct DenoiseArgs {

@@ -119,6 +119,8 @@ EXPORTS = {
     "sgi_render_frame": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(GBuffer), C.POINTER(Camera),
                                      C.POINTER(FrameParams), C.c_void_p, C.c_void_p]),
     "sgi_reset_history": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "sgi_gi_target": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(Camera), C.c_float, C.c_int32,
+                                  C.c_void_p, C.c_void_p]),
     "sgi_read_debug": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "sgi_set_timing": (C.c_int32, [C.c_void_p, C.c_int32]),
     "sgi_get_pass_times": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),

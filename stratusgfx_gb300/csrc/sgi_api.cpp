@@ -416,6 +416,19 @@ sgi_status sgi_render_frame(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuf
     return SGI_OK;
 }
 
+sgi_status sgi_gi_target(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera* cam, float time, int32_t batches,
+                         float* target, void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (!gbuffer_ok(gbuf, true) || !cam || !target) return fail(ctx, SGI_ERR_ARG, "NULL G-buffer, camera or target");
+    if (batches < 1 || batches > 65536) return fail(ctx, SGI_ERR_ARG, "batches must be in [1, 65536]");
+    if (!ctx->culled || !ctx->maps_set) return fail(ctx, SGI_ERR_STATE, "cull VPLs (and tiles) first");
+    SGI_CUDA(ctx, sgi::launch_gi_target(ctx->cfg, ctx->sc, *gbuf, *cam, ctx->cv, ctx->ce, ctx->visible_index,
+                                        ctx->lists, ctx->cubes, time, batches, (float4*)target, (cudaStream_t)stream),
+             "gi_target");
+    ctx->launches += 1;
+    return SGI_OK;
+}
+
 sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream) {
     if (!ctx) return SGI_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;

@@ -64,6 +64,11 @@ cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sg
                           const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index,
                           const int32_t* lists, const sgi_cube_atlas& cubes, float time, const GatherOut& out,
                           cudaStream_t s);
+// converged target: `batches` runs of the sample loop, sums in FP64 -> float4 (rgb, 1)
+cudaError_t launch_gi_target(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
+                             const sgi_camera& cam, const sgi_vpl* cv, const sgi_atlas_entry* ce,
+                             const int32_t* visible_index, const int32_t* lists, const sgi_cube_atlas& cubes,
+                             float time, int batches, float4* out, cudaStream_t s);
 // a-trous pass `pass` (1 .. passes-2): 5x5 taps at stride 2^pass
 cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in,
                           uint2* res_out, cudaStream_t s);

@@ -475,95 +475,115 @@ struct GatherParams {
     GatherOut out;
 };
 
+// Per-pixel inputs of the gather (vpl_pbr_gi.fs:99-145).
+struct PixelShade {
+    V3 fragPos, viewDir, baseColor, normal, baseRefl;
+    float distToCamera, roughness, metallic, ao, ambient;
+    int sampleCount, candidates;
+    const int32_t* list;
+};
+
+SGI_D PixelShade load_pixel(const GatherParams& p, int x, int y, size_t i) {
+    PixelShade px;
+    const float u = (float(x) + 0.5f) / float(p.W), v = (float(y) + 0.5f) / float(p.H);
+    px.fragPos = world_from_depth(u, v, __ldg(p.g.depth + i), p.cam.inv_proj_view);
+    const V3 viewPos = v3(p.cam.view_position[0], p.cam.view_position[1], p.cam.view_position[2]);
+    px.viewDir = normalize(viewPos - px.fragPos);
+    px.distToCamera = length(viewPos - px.fragPos);
+    const uint32_t alb = __ldg(p.g.albedo + i);
+    px.baseColor = v3(gmax(unorm8(alb, 0), 0.01f), gmax(unorm8(alb, 1), 0.01f), gmax(unorm8(alb, 2), 0.01f));
+    px.normal = decode_normal(__ldg(p.g.normal + i));
+    const uint32_t rma = __ldg(p.g.roughness_metallic_ambient + i);
+    px.roughness = gmax(0.5f, unorm8(rma, 0));
+    px.metallic = unorm8(rma, 1);
+    px.ao = gclamp(h2f(__ldg(p.g.ssao + i)), 0.35f, 1.0f);
+    px.ambient = unorm8(rma, 2);
+    px.baseRefl = v3s(float(__ldg(p.g.base_reflectivity + i) & 0xffu) / 255.0f);
+    const float roughnessWeight = 1.0f - px.roughness;
+    const float distRatio = gmin(1.0f - px.distToCamera / 1000.0f, 1.0f);
+    if (p.spp > 0) {
+        px.sampleCount = p.spp;
+    } else {
+        int maxSamplesPerPixel = (int)mixf(2.0f, 10.0f, roughnessWeight);
+        int samplesMax = (int)(float(maxSamplesPerPixel) * distRatio);
+        px.sampleCount = samplesMax > 1 ? samplesMax : 1;
+    }
+    px.list = nullptr;
+    if (p.tiled) {
+        const int tile = (y / p.ts) * p.tiles_x + (x / p.ts);
+        px.list = p.lists + (size_t)tile * (1 + p.L);
+        px.candidates = __ldg(px.list);
+    } else {
+        px.candidates = __ldg(p.visible_index);
+    }
+    return px;
+}
+
+// The sample loop of vpl_pbr_gi.fs:148-200 with the seed z starting at seedZ.
+SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX, float seedY, float seedZ,
+                       V3& vplColor, float& validSamples) {
+    ShadeParams sp{p.sc.min_roughness, p.sc.perceptual, p.sc.fog_density,
+                   {p.sc.fog_color[0], p.sc.fog_color[1], p.sc.fog_color[2]}, p.sc.point_ambient};
+    vplColor = v3s(0.0f);
+    validSamples = 0.0f;
+    const int candidates = px.candidates;
+    if (candidates <= 0) return;
+    const float minGi = p.sc.min_gi_occlusion;
+    const V3 fragPos = px.fragPos, normal = px.normal;
+    for (int s = 0, resamples = 0; s < px.sampleCount; ++s) {
+        const float rnd = random3(seedX, seedY, seedZ);
+        seedZ += 10000.0f;
+        int lightIndex;
+        if (px.list) {
+            int r = (int)(float(candidates) * rnd);
+            lightIndex = __ldg(px.list + 1 + (r < candidates - 1 ? r : candidates - 1));
+        } else {
+            lightIndex = (int)(float(candidates - 1) * rnd);
+        }
+        const float4* rec = reinterpret_cast<const float4*>(p.cv + lightIndex);
+        const float4 pos = __ldg(rec);
+        const float4 spec = __ldg(rec + 2);
+        const float4 misc = __ldg(rec + 3);   // radius, farPlane, intensity
+        const sgi_atlas_entry entry = p.ce[lightIndex];
+        const V3 lightPosition = v3(pos.x, pos.y, pos.z);
+        const V3 lmf = lightPosition - fragPos;
+        const float lightRadius = misc.x;
+        const float distance = length(lmf);
+        if (resamples < 5) {
+            float sideCheck = dot(normal, normalize(lmf));
+            if (sideCheck < 0.0f || distance > lightRadius) { ++resamples; --s; continue; }
+        }
+        const float distanceRatio = gclamp((2.0f * distance) / lightRadius, 0.0f, 1.0f);
+        const float distAttenuation = distanceRatio;
+        const float4 col = __ldg(rec + 1);
+        const V3 lightColor = v3(col.x, col.y, col.z);
+        float shadowFactor = px.distToCamera < 500.0f
+                                 ? shadow_1sample(p.cubes, entry, misc.y, fragPos, lightPosition,
+                                                  dot(lightPosition - fragPos, normal), 0.1f)
+                                 : 0.0f;
+        shadowFactor = gmin(shadowFactor, mixf(minGi, 1.0f, distanceRatio));
+        float reweight = 1.0f;
+        if (shadowFactor > 0.0f) reweight = (1.0f - distAttenuation) * minGi + distAttenuation;
+        validSamples += reweight;
+        const V3 tmp = px.ao * vpl_lighting2(fragPos, px.baseColor, normal, px.viewDir, v3(spec.x, spec.y, spec.z),
+                                             lightPosition, lightColor, px.distToCamera, lightRadius, px.roughness,
+                                             px.metallic, px.ambient, px.baseRefl, sp);
+        vplColor = vplColor + (1.0f - shadowFactor) * tmp;
+    }
+}
+
 // vpl_pbr_gi.fs:81-207, one thread per pixel.
 __global__ void __launch_bounds__(256, 4) vpl_gather_kernel(GatherParams p) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= p.W || y >= p.H) return;
     const size_t i = (size_t)y * p.W + x;
-    ShadeParams sp{p.sc.min_roughness, p.sc.perceptual, p.sc.fog_density,
-                   {p.sc.fog_color[0], p.sc.fog_color[1], p.sc.fog_color[2]}, p.sc.point_ambient};
-    const float u = (float(x) + 0.5f) / float(p.W), v = (float(y) + 0.5f) / float(p.H);
-    const V3 fragPos = world_from_depth(u, v, __ldg(p.g.depth + i), p.cam.inv_proj_view);
-    const V3 viewPos = v3(p.cam.view_position[0], p.cam.view_position[1], p.cam.view_position[2]);
-    const V3 viewDir = normalize(viewPos - fragPos);
-    const float distToCamera = length(viewPos - fragPos);
-    const uint32_t alb = __ldg(p.g.albedo + i);
-    V3 baseColor = v3(gmax(unorm8(alb, 0), 0.01f), gmax(unorm8(alb, 1), 0.01f), gmax(unorm8(alb, 2), 0.01f));
-    const V3 normal = decode_normal(__ldg(p.g.normal + i));
-    const uint32_t rma = __ldg(p.g.roughness_metallic_ambient + i);
-    const float roughness = gmax(0.5f, unorm8(rma, 0));
-    const float metallic = unorm8(rma, 1);
-    const float ao = gclamp(h2f(__ldg(p.g.ssao + i)), 0.35f, 1.0f);
-    const float ambient = unorm8(rma, 2);
-    const float refl = float(__ldg(p.g.base_reflectivity + i) & 0xffu) / 255.0f;
-    const V3 baseRefl = v3s(refl);
-    const float roughnessWeight = 1.0f - roughness;
-    V3 vplColor = v3s(0.0f);
+    const PixelShade px = load_pixel(p, x, y, i);
+    const V3 normal = px.normal;
     const float seedX = float(x) + 0.5f, seedY = float(y) + 0.5f;
-    float seedZ = p.time;
-    float validSamples = 0.0f;
-    const float distRatio = gmin(1.0f - distToCamera / 1000.0f, 1.0f);
-    int sampleCount;
-    if (p.spp > 0) {
-        sampleCount = p.spp;
-    } else {
-        int maxSamplesPerPixel = (int)mixf(2.0f, 10.0f, roughnessWeight);
-        int samplesMax = (int)(float(maxSamplesPerPixel) * distRatio);
-        sampleCount = samplesMax > 1 ? samplesMax : 1;
-    }
-    const int32_t* list = nullptr;
-    int candidates;
-    if (p.tiled) {
-        const int tile = (y / p.ts) * p.tiles_x + (x / p.ts);
-        list = p.lists + (size_t)tile * (1 + p.L);
-        candidates = __ldg(list);
-    } else {
-        candidates = __ldg(p.visible_index);
-    }
-    if (candidates > 0) {
-        const float minGi = p.sc.min_gi_occlusion;
-        for (int s = 0, resamples = 0; s < sampleCount; ++s) {
-            const float rnd = random3(seedX, seedY, seedZ);
-            seedZ += 10000.0f;
-            int lightIndex;
-            if (list) {
-                int r = (int)(float(candidates) * rnd);
-                lightIndex = __ldg(list + 1 + (r < candidates - 1 ? r : candidates - 1));
-            } else {
-                lightIndex = (int)(float(candidates - 1) * rnd);
-            }
-            const float4* rec = reinterpret_cast<const float4*>(p.cv + lightIndex);
-            const float4 pos = __ldg(rec);
-            const float4 spec = __ldg(rec + 2);
-            const float4 misc = __ldg(rec + 3);   // radius, farPlane, intensity
-            const sgi_atlas_entry entry = p.ce[lightIndex];
-            const V3 lightPosition = v3(pos.x, pos.y, pos.z);
-            const V3 lmf = lightPosition - fragPos;
-            const float lightRadius = misc.x;
-            const float distance = length(lmf);
-            if (resamples < 5) {
-                float sideCheck = dot(normal, normalize(lmf));
-                if (sideCheck < 0.0f || distance > lightRadius) { ++resamples; --s; continue; }
-            }
-            const float distanceRatio = gclamp((2.0f * distance) / lightRadius, 0.0f, 1.0f);
-            const float distAttenuation = distanceRatio;
-            const float4 col = __ldg(rec + 1);
-            const V3 lightColor = v3(col.x, col.y, col.z);
-            float shadowFactor = distToCamera < 500.0f
-                                     ? shadow_1sample(p.cubes, entry, misc.y, fragPos, lightPosition,
-                                                      dot(lightPosition - fragPos, normal), 0.1f)
-                                     : 0.0f;
-            shadowFactor = gmin(shadowFactor, mixf(minGi, 1.0f, distanceRatio));
-            float reweight = 1.0f;
-            if (shadowFactor > 0.0f) reweight = (1.0f - distAttenuation) * minGi + distAttenuation;
-            validSamples += reweight;
-            const V3 tmp = ao * vpl_lighting2(fragPos, baseColor, normal, viewDir, v3(spec.x, spec.y, spec.z),
-                                              lightPosition, lightColor, distToCamera, lightRadius, roughness,
-                                              metallic, ambient, baseRefl, sp);
-            vplColor = vplColor + (1.0f - shadowFactor) * tmp;
-        }
-    }
+    V3 vplColor;
+    float validSamples;
+    sample_vpls(p, px, seedX, seedY, p.time, vplColor, validSamples);
     validSamples = gmax(validSamples, 1.0f);
     const V3 b = vmin(vplColor, kHalfMax);
     // The reservoir as stored in its RGBA16F target (vpl_pbr_gi.fs:205).
@@ -605,6 +625,45 @@ cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sg
     dim3 block(16, 16);
     dim3 grid((cfg.width + 15) / 16, (cfg.height + 15) / 16);
     vpl_gather_kernel<<<grid, block, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+// Converged GI target: `batches` independent runs of the gather's sample loop
+// per pixel (batch b seeds z at time + b * 2e5, far past the previous batch's
+// draws), with sum(vplColor) and sum(validSamples) accumulated in FP64. Its
+// ratio is the limit of the per-pixel estimate the K-sample path denoises;
+// out = (sum vplColor / max(sum validSamples, 1), 1) as FP32.
+__global__ void __launch_bounds__(256, 4) gi_target_kernel(GatherParams p, int batches, float4* __restrict__ out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= p.W || y >= p.H) return;
+    const size_t i = (size_t)y * p.W + x;
+    const PixelShade px = load_pixel(p, x, y, i);
+    const float seedX = float(x) + 0.5f, seedY = float(y) + 0.5f;
+    double c0 = 0.0, c1 = 0.0, c2 = 0.0, w = 0.0;
+    for (int b = 0; b < batches; ++b) {
+        V3 col;
+        float valid;
+        sample_vpls(p, px, seedX, seedY, p.time + float(b) * 200000.0f, col, valid);
+        c0 += (double)col.x; c1 += (double)col.y; c2 += (double)col.z; w += (double)valid;
+    }
+    const double den = w < 1.0 ? 1.0 : w;
+    out[i] = make_float4((float)(c0 / den), (float)(c1 / den), (float)(c2 / den), 1.0f);
+}
+
+cudaError_t launch_gi_target(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
+                             const sgi_camera& cam, const sgi_vpl* cv, const sgi_atlas_entry* ce,
+                             const int32_t* visible_index, const int32_t* lists, const sgi_cube_atlas& cubes,
+                             float time, int batches, float4* out, cudaStream_t s) {
+    GatherParams p;
+    p.W = cfg.width; p.H = cfg.height; p.ts = cfg.tile_size;
+    p.tiles_x = (cfg.width + cfg.tile_size - 1) / cfg.tile_size;
+    p.L = cfg.max_vpls_per_tile; p.tiled = cfg.gi_mode == SGI_GI_TILED; p.spp = cfg.samples_per_pixel;
+    p.sc = sc; p.g = g; p.cam = cam; p.cv = cv; p.ce = ce; p.visible_index = visible_index; p.lists = lists;
+    p.cubes = cubes; p.time = time;
+    dim3 block(16, 16);
+    dim3 grid((cfg.width + 15) / 16, (cfg.height + 15) / 16);
+    gi_target_kernel<<<grid, block, 0, s>>>(p, batches, out);
     return cudaGetLastError();
 }
 

@@ -243,6 +243,12 @@ class GiStage:
         self._chk(self.lib.sgi_render_frame(self.ctx, C.byref(cur.struct()), C.byref(prev.struct()), C.byref(cam),
                                             C.byref(fp), C.c_void_p(_ptr(hdr_out)), _stream_ptr(stream)))
 
+    def gi_target(self, g: GBufferTensors, cam: abi.Camera, time: float, batches: int, out: torch.Tensor,
+                  stream=None):
+        """Converged GI target (float32 [H, W, 4]) after this frame's culling."""
+        self._chk(self.lib.sgi_gi_target(self.ctx, C.byref(g.struct()), C.byref(cam), time, batches,
+                                         C.c_void_p(_ptr(out)), _stream_ptr(stream)))
+
     def reset_history(self, stream=None):
         self._chk(self.lib.sgi_reset_history(self.ctx, _stream_ptr(stream)))
 

@@ -287,3 +287,24 @@ def test_abi_rejects_bad_arguments():
         assert b"max_vpls" in lib.sgi_last_error(h)
     finally:
         lib.sgi_destroy(h)
+
+
+@pytest.mark.parametrize("mode", [abi.SGI_GI_TILED, abi.SGI_GI_REFERENCE])
+def test_converged_target_bit_exact(small, mode):
+    """sgi_gi_target: batches of the sample loop summed in FP64 must equal the oracle's."""
+    st, cfg = small.stage(1, gi_mode=mode)
+    st.cull_vpls()
+    if mode == abi.SGI_GI_TILED:
+        st.cull_tiles(small.g[1], small.hs.camera(1))
+    out = torch.empty((cfg.height, cfg.width, 4), dtype=torch.float32, device="cuda")
+    st.gi_target(small.g[1], small.hs.camera(1), TIME, 6, out)
+    torch.cuda.synchronize()
+    idx = st.read_debug(abi.SGI_DEBUG_VISIBLE_INDEX, np.int32)
+    cnt = int(idx[0])
+    lists = None
+    if mode == abi.SGI_GI_TILED:
+        lists = st.read_debug(abi.SGI_DEBUG_TILE_LISTS, np.int32).reshape(-1, 1 + cfg.max_vpls_per_tile)
+    ref = O.gi_target(cfg, small.hs.gbuffers[1], small.hs.camera(1), small.sc.vpls[idx[1:1 + cnt]],
+                      small.sc.entries[idx[1:1 + cnt]], cnt, lists, small.hs.cubes, TIME, 6)
+    assert_bit_exact(out.cpu().numpy(), ref, f"converged target mode={mode}")
+    st.close()

@@ -1,0 +1,82 @@
+/*
+ * sgi_nn.h - learned kernel-predicting denoiser (KPCNN) for the GI stage.
+ *
+ * No counterpart in StratusGFX: it replaces the a-trous passes of
+ * vpl_pbr_gi_denoise.fs (ComputeVirtualPointLightGlobalIllumination_,
+ * StratusRendererBackend.cpp:1912-1940) with a U-Net (3 levels, 32/64/128
+ * channels, 3x3 convolutions) that predicts a 5x5 filter kernel and a temporal
+ * blend weight per pixel. Convolutions run on the tensor cores in BF16 with
+ * FP32 accumulation; the network is trained on the GPU by the library's own
+ * forward and backward kernels (Adam, FP32 master weights).
+ *
+ * Tensors are device pointers, NHWC, batch-major:
+ *   features  BF16 [B][H][W][16]  (kpcn_features: log1p noisy GI rgb, albedo rgb,
+ *                                  normal xyz, view distance / 10, roughness,
+ *                                  log1p 3x3 luminance variance, log1p warped
+ *                                  previous output rgb, metallic)
+ *   noisy     float4 [B][H][W]    per-pixel GI estimate (denoise pass-0 output)
+ *   prev      float4 [B][H][W]    previous denoised GI warped by the velocity
+ *   target    float4 [B][H][W]    converged GI (sgi_gi_target)
+ *   out       float4 [B][H][W]    denoised GI
+ * H and W must be multiples of 4.
+ */
+#ifndef SGI_NN_H_
+#define SGI_NN_H_
+
+#include "sgi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sgi_nn sgi_nn;
+
+typedef struct sgi_nn_config {
+    int32_t max_batch;
+    int32_t max_height;
+    int32_t max_width;
+    uint32_t seed;         /* He-normal initialisation seed */
+} sgi_nn_config;
+
+sgi_status sgi_nn_create(const sgi_nn_config* cfg, sgi_nn** out);
+sgi_status sgi_nn_destroy(sgi_nn* net);
+const char* sgi_nn_last_error(const sgi_nn* net);
+
+/* Parameters: FP32 master copy, layer by layer ([cout][3][3][cin] weights, then [cout] bias). */
+int64_t sgi_nn_num_params(const sgi_nn* net);
+sgi_status sgi_nn_get_params(sgi_nn* net, float* host, int64_t n);
+sgi_status sgi_nn_set_params(sgi_nn* net, const float* host, int64_t n);
+/* Gradients of the last sgi_nn_train_step (same layout as the parameters). */
+sgi_status sgi_nn_get_grads(sgi_nn* net, float* host, int64_t n);
+
+/* Inference: out = denoised GI. */
+sgi_status sgi_nn_forward(sgi_nn* net, const void* features, const float* noisy, const float* prev, int32_t batch,
+                          int32_t height, int32_t width, float* out, void* stream);
+
+/* One training step: forward, loss = mean |log1p(out) - log1p(target)|, backward,
+ * and (if apply_update) one Adam update with learning rate lr. *loss_host receives
+ * the loss (this call synchronises the stream when loss_host is not NULL). */
+sgi_status sgi_nn_train_step(sgi_nn* net, const void* features, const float* noisy, const float* prev,
+                             const float* target, int32_t batch, int32_t height, int32_t width, float lr,
+                             int32_t apply_update, float* loss_host, void* stream);
+
+/* Builds the network inputs of the frame last gathered by `ctx` (after
+ * sgi_global_illumination or sgi_render_frame with this frame's G-buffer):
+ * features, noisy and prev (as above, batch 1). `prev` warps the context's GI
+ * history with the velocity buffer (bilinear), like the temporal pass. */
+sgi_status sgi_nn_features(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_camera* cam, void* features,
+                           float* noisy, float* prev, void* stream);
+
+/* The GI stage with the learned denoiser in place of the a-trous passes:
+ * VPL cull, direct lighting, tile cull, GI gather, features, U-Net, kernel
+ * apply + temporal blend, composite hdr_out = screen + gi * denoised. The
+ * denoised GI becomes the context's history. */
+sgi_status sgi_render_frame_neural(sgi_ctx* ctx, sgi_nn* net, const sgi_gbuffer* cur, const sgi_gbuffer* prev,
+                                   const sgi_camera* cam, const sgi_frame_params* params, void* hdr_out,
+                                   void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SGI_NN_H_ */

@@ -95,6 +95,10 @@ class Box(C.Structure):           # sgi_box, 64 B
                 ("metallic", C.c_float), ("reflectance", C.c_float), ("id", C.c_float)]
 
 
+class NnConfig(C.Structure):
+    _fields_ = [("max_batch", C.c_int32), ("max_height", C.c_int32), ("max_width", C.c_int32), ("seed", C.c_uint32)]
+
+
 class SceneCamera(C.Structure):
     _fields_ = [("proj_view", C.c_float * 16), ("inv_proj_view", C.c_float * 16),
                 ("prev_proj_view", C.c_float * 16), ("position", C.c_float * 4)]
@@ -125,6 +129,21 @@ EXPORTS = {
     "sgi_set_timing": (C.c_int32, [C.c_void_p, C.c_int32]),
     "sgi_get_pass_times": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "sgi_launch_count": (C.c_int64, [C.c_void_p]),
+    "sgi_nn_create": (C.c_int32, [C.POINTER(NnConfig), C.POINTER(C.c_void_p)]),
+    "sgi_nn_destroy": (C.c_int32, [C.c_void_p]),
+    "sgi_nn_last_error": (C.c_char_p, [C.c_void_p]),
+    "sgi_nn_num_params": (C.c_int64, [C.c_void_p]),
+    "sgi_nn_get_params": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "sgi_nn_set_params": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "sgi_nn_get_grads": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "sgi_nn_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                   C.c_void_p, C.c_void_p]),
+    "sgi_nn_train_step": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                      C.c_int32, C.c_int32, C.c_float, C.c_int32, C.POINTER(C.c_float), C.c_void_p]),
+    "sgi_nn_features": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(Camera), C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p]),
+    "sgi_render_frame_neural": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(GBuffer), C.POINTER(GBuffer),
+                                            C.POINTER(Camera), C.POINTER(FrameParams), C.c_void_p, C.c_void_p]),
     "sgi_scene_gbuffer": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(SceneCamera), C.c_int32, C.c_int32,
                                       C.POINTER(GBuffer), C.c_void_p]),
     "sgi_scene_csm": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(Csm), C.POINTER((C.c_float * 16) * 4), C.c_void_p]),

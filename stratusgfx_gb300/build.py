@@ -23,8 +23,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # results are bit-reproducible against the CPU restatement of the shaders.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-Xcompiler", "-fPIC", "-I" + os.path.join(REPO, "include")]
-CUDA_SOURCES = ["sgi_kernels.cu", "sgi_scene.cu"]
-HOST_SOURCES = ["sgi_api.cpp"]
+CUDA_SOURCES = ["sgi_kernels.cu", "sgi_scene.cu", "sgi_nn.cu"]
+HOST_SOURCES = ["sgi_api.cpp", "sgi_nn_api.cpp"]
+# The learned denoiser is checked against the oracle within a tolerance, not bit
+# for bit, so its kernels keep the compiler's default multiply-add contraction.
+FAST_MATH_OK = {"sgi_nn.cu"}
 
 
 def _nvcc() -> str:
@@ -64,7 +67,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         o = os.path.join(OUT, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-Xptxas", "-v", "-c", s, "-o", o])
+            flags = [f for f in NVCC_FLAGS if not (src in FAST_MATH_OK and f == "-fmad=false")]
+            jobs.append([nvcc] + flags + ["-Xptxas", "-v", "-c", s, "-o", o])
     for src in HOST_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT, src.replace(".cpp", ".o"))

@@ -16,8 +16,11 @@
 #include <string>
 
 #include "../../include/sgi.h"
+#include "../../include/sgi_nn.h"
 #include "../../include/sgi_scene.h"
 #include "sgi_internal.h"
+#include "sgi_nn_internal.h"
+#include "sgi_nn_net.h"
 
 struct sgi_ctx {
     sgi_config cfg;
@@ -51,12 +54,23 @@ struct sgi_ctx {
     // GI scratch
     uint2* reservoir = nullptr;
     uint2* ping[2] = {nullptr, nullptr};
+    uint2* merged = nullptr;                // denoise pass-0 output (kept for the learned denoiser)
     uint2* pass_bufs[SGI_MAX_DENOISE_PASSES] = {};
     uint2* direct = nullptr;
     float4* guide = nullptr;
     uint2* gi_hist[2] = {nullptr, nullptr};
     uint16_t* hist_depth[2] = {nullptr, nullptr};
     int hist_cur = 0;
+    bool have_history = false;
+    const uint2* last_merged = nullptr;   // pass-0 output of the last gather
+    int feat_hist = 0;                    // history slot that was "previous" for the last gather
+    bool feat_have_history = false;
+
+    // learned-denoiser inputs/outputs (allocated on first use)
+    __nv_bfloat16* nn_feat = nullptr;
+    float4* nn_noisy = nullptr;
+    float4* nn_prev = nullptr;
+    float4* nn_den = nullptr;
 
     // timing
     bool timing = false;
@@ -136,10 +150,12 @@ sgi::ShadeConfig make_shade(const sgi_config& c) {
 
 void free_all(sgi_ctx* c) {
     void* ptrs[] = {c->vpls, c->entries, c->points, c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
-                    c->tile_keys, c->reservoir, c->ping[0], c->ping[1], c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
+                    c->tile_keys, c->reservoir, c->ping[0], c->ping[1], c->merged, c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
                     c->hist_depth[0], c->hist_depth[1]};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto* p : c->pass_bufs) if (p) cudaFree(p);
+    void* nnp[] = {c->nn_feat, c->nn_noisy, c->nn_prev, c->nn_den};
+    for (void* p : nnp) if (p) cudaFree(p);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
 }
 
@@ -224,6 +240,7 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     chk(dalloc(&c->guide, P));
     chk(dalloc(&c->ping[0], P));
     chk(dalloc(&c->ping[1], P));
+    chk(dalloc(&c->merged, P));
     chk(dalloc(&c->direct, P));
     chk(dalloc(&c->gi_hist[0], P));
     chk(dalloc(&c->gi_hist[1], P));
@@ -333,22 +350,34 @@ sgi_status sgi_direct_lighting(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_
     return SGI_OK;
 }
 
-static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer* prev, const sgi_camera* cam,
-                         const void* hdr_in, void* hdr_out, const sgi_frame_params* params, cudaStream_t s,
-                         int ev_gather) {
+// vpl_pbr_gi.fs, with denoise pass 0 (the centre-only reservoir merge) in its epilogue
+static sgi_status run_gather(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_camera* cam,
+                             const sgi_frame_params* params, cudaStream_t s) {
     const sgi_config& cfg = ctx->cfg;
     const bool keep = cfg.debug_keep_passes != 0;
-    // vpl_pbr_gi.fs, with denoise pass 0 (the centre-only reservoir merge) in its epilogue
     sgi::GatherOut go;
-    go.merged = keep ? ctx->pass_bufs[0] : ctx->ping[0];
+    go.merged = keep ? ctx->pass_bufs[0] : ctx->merged;
     go.guide = ctx->guide;
     go.raw = keep ? ctx->reservoir : nullptr;
     SGI_CUDA(ctx, sgi::launch_gather(cfg, ctx->sc, *cur, *cam, ctx->cv, ctx->ce, ctx->visible_index, ctx->lists,
                                      ctx->cubes, params->time, go, s), "vpl_gather");
     ctx->launches += 1;
+    ctx->last_merged = go.merged;
+    ctx->feat_hist = ctx->hist_cur;
+    ctx->feat_have_history = ctx->have_history;
+    return SGI_OK;
+}
+
+static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer* prev, const sgi_camera* cam,
+                         const void* hdr_in, void* hdr_out, const sgi_frame_params* params, cudaStream_t s,
+                         int ev_gather) {
+    const sgi_config& cfg = ctx->cfg;
+    const bool keep = cfg.debug_keep_passes != 0;
+    sgi_status st = run_gather(ctx, cur, cam, params, s);
+    if (st != SGI_OK) return st;
     record(ctx, ev_gather + 1, s);
     // passes 1 .. n-2: a-trous at stride 2^pass (StratusRendererBackend.cpp:1912-1940)
-    const uint2* in = go.merged;
+    const uint2* in = ctx->last_merged;
     for (int pass = 1; pass < cfg.denoise_passes - 1; ++pass) {
         uint2* out = keep ? ctx->pass_bufs[pass] : ctx->ping[pass & 1];
         SGI_CUDA(ctx, sgi::launch_atrous(cfg.width, cfg.height, pass, ctx->guide, in, out, s), "atrous");
@@ -372,6 +401,7 @@ static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer
     SGI_CUDA(ctx, sgi::launch_denoise_final(d, s), "denoise_final");
     ctx->launches += 1;
     ctx->hist_cur = 1 - ctx->hist_cur;
+    ctx->have_history = true;
     return SGI_OK;
 }
 
@@ -438,6 +468,7 @@ sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream) {
         SGI_CUDA(ctx, cudaMemsetAsync(ctx->hist_depth[k], 0, P * sizeof(uint16_t), s), "clear history depth");
     }
     ctx->hist_cur = 0;
+    ctx->have_history = false;
     return SGI_OK;
 }
 
@@ -491,6 +522,89 @@ sgi_status sgi_get_pass_times(sgi_ctx* ctx, float* ms, int32_t n) {
         SGI_CUDA(ctx, cudaEventElapsedTime(&t, ctx->ev[k], ctx->ev[k + 1]), "event elapsed");
         ms[k] = t;
     }
+    return SGI_OK;
+}
+
+// ---------------------------------------------------- learned denoiser --
+static sgi_status nn_buffers(sgi_ctx* ctx) {
+    if (ctx->nn_feat) return SGI_OK;
+    const size_t P = pixels(ctx->cfg);
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t r) { if (e == cudaSuccess && r != cudaSuccess) e = r; };
+    chk(dalloc(&ctx->nn_feat, P * 16));
+    chk(dalloc(&ctx->nn_noisy, P));
+    chk(dalloc(&ctx->nn_prev, P));
+    chk(dalloc(&ctx->nn_den, P));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "allocate denoiser buffers");
+    return SGI_OK;
+}
+
+static sgi_status run_features(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_camera* cam, __nv_bfloat16* feat,
+                               float4* noisy, float4* prevw, cudaStream_t s) {
+    sgi::nn::FeatureArgs a;
+    a.W = ctx->cfg.width; a.H = ctx->cfg.height;
+    a.merged = ctx->last_merged; a.guide = ctx->guide;
+    a.albedo = cur->albedo; a.rma = cur->roughness_metallic_ambient; a.velocity = cur->velocity;
+    a.gi_prev = ctx->gi_hist[ctx->feat_hist];
+    a.have_history = ctx->feat_have_history ? 1 : 0;
+    std::memcpy(a.inv_pv, cam->inv_proj_view, sizeof(a.inv_pv));
+    for (int k = 0; k < 3; ++k) a.cam_pos[k] = cam->view_position[k];
+    a.features = feat; a.noisy = noisy; a.prev = prevw;
+    SGI_CUDA(ctx, sgi::nn::features(a, s), "kpcn_features");
+    ctx->launches += 1;
+    return SGI_OK;
+}
+
+sgi_status sgi_nn_features(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_camera* cam, void* features, float* noisy,
+                           float* prev, void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (!gbuffer_ok(cur, true) || !cam || !features || !noisy || !prev)
+        return fail(ctx, SGI_ERR_ARG, "NULL G-buffer, camera or output");
+    if (!ctx->last_merged) return fail(ctx, SGI_ERR_STATE, "no gathered frame yet");
+    return run_features(ctx, cur, cam, (__nv_bfloat16*)features, (float4*)noisy, (float4*)prev, (cudaStream_t)stream);
+}
+
+sgi_status sgi_render_frame_neural(sgi_ctx* ctx, sgi_nn* net, const sgi_gbuffer* cur, const sgi_gbuffer* prev,
+                                   const sgi_camera* cam, const sgi_frame_params* params, void* hdr_out,
+                                   void* stream) {
+    if (!ctx || !net) return SGI_ERR_ARG;
+    if (!frame_args_ok(cur, prev, cam, params) || !hdr_out)
+        return fail(ctx, SGI_ERR_ARG, "NULL frame argument or frames_per_second <= 0");
+    const int W = ctx->cfg.width, H = ctx->cfg.height;
+    if (W % 4 || H % 4 || W > net->net.cfg.max_width * net->net.cfg.max_batch ||
+        (size_t)W * H > (size_t)net->net.cfg.max_batch * net->net.cfg.max_height * net->net.cfg.max_width)
+        return fail(ctx, SGI_ERR_CAP, "viewport exceeds the network's capacity (or is not a multiple of 4)");
+    sgi_status st = nn_buffers(ctx);
+    if (st != SGI_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    record(ctx, 0, s);
+    st = sgi_cull_vpls(ctx, stream);
+    if (st != SGI_OK) return st;
+    record(ctx, 1, s);
+    st = sgi_direct_lighting(ctx, cur, cam, ctx->direct, stream);
+    if (st != SGI_OK) return st;
+    record(ctx, 2, s);
+    if (ctx->cfg.gi_mode == SGI_GI_TILED) {
+        st = sgi_cull_tiles(ctx, cur, cam, stream);
+        if (st != SGI_OK) return st;
+    }
+    record(ctx, 3, s);
+    st = run_gather(ctx, cur, cam, params, s);
+    if (st != SGI_OK) return st;
+    record(ctx, 4, s);
+    st = run_features(ctx, cur, cam, ctx->nn_feat, ctx->nn_noisy, ctx->nn_prev, s);
+    if (st != SGI_OK) return st;
+    st = sgi_nn_forward(net, ctx->nn_feat, (const float*)ctx->nn_noisy, (const float*)ctx->nn_prev, 1, H, W,
+                        (float*)ctx->nn_den, stream);
+    if (st != SGI_OK) return fail(ctx, st, std::string("denoiser: ") + sgi_nn_last_error(net));
+    SGI_CUDA(ctx, sgi::nn::composite(ctx->nn_den, ctx->direct, cur->albedo, (uint2*)hdr_out,
+                                     ctx->gi_hist[1 - ctx->hist_cur], ctx->hist_depth[1 - ctx->hist_cur],
+                                     pixels(ctx->cfg), s), "kpcn_composite");
+    ctx->launches += 17;
+    ctx->hist_cur = 1 - ctx->hist_cur;
+    ctx->have_history = true;
+    record(ctx, 5, s);
+    ctx->have_times = ctx->timing;
     return SGI_OK;
 }
 

@@ -1,0 +1,591 @@
+// sgi_nn.cu - kernels of the learned kernel-predicting denoiser (KPCNN).
+//
+// No counterpart in StratusGFX: it stands in for the a-trous filter of
+// vpl_pbr_gi_denoise.fs. Tensors are NHWC; activations and gradients BF16,
+// accumulation FP32, master weights FP32. A tensor view is (pointer to the
+// first channel, channel stride), so skip connections are written straight
+// into channel slices of the decoder inputs and no concatenation is copied.
+//
+// 3x3 convolutions are implicit GEMMs on the tensor cores: a block computes an
+// 8 x 16 pixel tile for all output channels; the (8+2) x (16+2) input halo and
+// the weights of one input-channel chunk are staged in shared memory, and each
+// warp issues mma.m16n8k16 (BF16 in, FP32 accumulate) over its 16-pixel row
+// with A/B fragments loaded by ldmatrix.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sgi_nn_internal.h"
+
+namespace sgi {
+namespace nn {
+
+typedef __nv_bfloat16 bf16;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void ldmatrix_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+constexpr int kTileH = 8, kTileW = 16;
+constexpr int kHaloH = kTileH + 2, kHaloW = kTileW + 2;
+
+// ------------------------------------------------------------ conv 3x3 --
+// y[b, p, co] = act(bias[co] + sum_{tap, ci} w[co][tap][ci] * x[b, p + off(tap), ci]), zero padding.
+// MODE 0: bias + ReLU, 1: bias only, 2: neither (dgrad).
+template <int CIN, int COUT, int CK, int MODE>
+__global__ void __launch_bounds__(256) conv3x3_kernel(ConvArgs a) {
+    static_assert(CIN % CK == 0 && (CK == 16 || CK == 32) && COUT % 16 == 0, "shape");
+    constexpr int HP = CK + 8;            // padded channel pitch of the halo (bank-conflict free ldmatrix)
+    constexpr int WP = 9 * HP;            // padded pitch of one output channel's weights
+    constexpr int NT = COUT / 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16* halo = reinterpret_cast<bf16*>(smem_raw);
+    bf16* wsm = halo + kHaloH * kHaloW * HP;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int x0 = blockIdx.x * kTileW, y0 = blockIdx.y * kTileH, b = blockIdx.z;
+    const int H = a.H, W = a.W;
+    const bf16* xb = a.x + (size_t)b * H * W * a.xs;
+
+    float acc[NT][4];
+#pragma unroll
+    for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.0f;
+
+    for (int c0 = 0; c0 < CIN; c0 += CK) {
+        __syncthreads();
+        // input halo: (kHaloH x kHaloW) pixels x CK channels, 16-byte vectors
+        constexpr int VPP = CK / 8;
+        for (int v = tid; v < kHaloH * kHaloW * VPP; v += 256) {
+            const int pix = v / VPP, q = v % VPP;
+            const int hy = pix / kHaloW, hx = pix % kHaloW;
+            const int gy = y0 + hy - 1, gx = x0 + hx - 1;
+            uint4 val = make_uint4(0u, 0u, 0u, 0u);
+            if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+                val = *reinterpret_cast<const uint4*>(xb + ((size_t)gy * W + gx) * a.xs + c0 + q * 8);
+            *reinterpret_cast<uint4*>(halo + pix * HP + q * 8) = val;
+        }
+        // weights of this channel chunk: [COUT][9][CK]
+        for (int v = tid; v < COUT * 9 * VPP; v += 256) {
+            const int co = v / (9 * VPP), r = v % (9 * VPP);
+            const int tap = r / VPP, q = r % VPP;
+            *reinterpret_cast<uint4*>(wsm + co * WP + tap * HP + q * 8) =
+                *reinterpret_cast<const uint4*>(a.w + ((size_t)co * 9 + tap) * CIN + c0 + q * 8);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+            const int ky = tap / 3, kx = tap % 3;
+#pragma unroll
+            for (int kk = 0; kk < CK; kk += 16) {
+                uint32_t a0, a1, a2, a3;
+                const int prow = lane & 15, kcol = (lane >> 4) * 8;
+                ldmatrix_x4(smem_addr(halo + ((warp + ky) * kHaloW + prow + kx) * HP + kk + kcol), a0, a1, a2, a3);
+#pragma unroll
+                for (int n = 0; n < NT; n += 2) {
+                    const int m = lane >> 3;
+                    const int co = (n + (m >> 1)) * 8 + (lane & 7);
+                    uint32_t b0, b1, b2, b3;
+                    ldmatrix_x4(smem_addr(wsm + co * WP + tap * HP + kk + (m & 1) * 8), b0, b1, b2, b3);
+                    mma_bf16(acc[n], a0, a1, a2, a3, b0, b1);
+                    mma_bf16(acc[n + 1], a0, a1, a2, a3, b2, b3);
+                }
+            }
+        }
+    }
+    // epilogue: rows = pixels (lane >> 2, +8), columns = channels ((lane & 3) * 2, +1)
+    const int gy = y0 + warp;
+    if (gy >= H) return;
+    bf16* yb = a.y + (size_t)b * H * W * a.ys;
+#pragma unroll
+    for (int n = 0; n < NT; ++n) {
+        const int co = n * 8 + (lane & 3) * 2;
+        float bias0 = 0.0f, bias1 = 0.0f;
+        if (MODE != 2) { bias0 = a.bias[co]; bias1 = a.bias[co + 1]; }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int gx = x0 + (lane >> 2) + h * 8;
+            if (gx >= W) continue;
+            float v0 = acc[n][2 * h] + bias0, v1 = acc[n][2 * h + 1] + bias1;
+            if (MODE == 0) { v0 = fmaxf(v0, 0.0f); v1 = fmaxf(v1, 0.0f); }
+            *reinterpret_cast<__nv_bfloat162*>(yb + ((size_t)gy * W + gx) * a.ys + co) = __floats2bfloat162_rn(v0, v1);
+        }
+    }
+}
+
+template <int CIN, int COUT, int CK, int MODE>
+static cudaError_t run_conv(const ConvArgs& a, cudaStream_t s) {
+    constexpr int HP = CK + 8;
+    const size_t smem = (size_t)(kHaloH * kHaloW * HP + COUT * 9 * HP) * sizeof(bf16);
+    auto kern = conv3x3_kernel<CIN, COUT, CK, MODE>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((a.W + kTileW - 1) / kTileW, (a.H + kTileH - 1) / kTileH, a.B);
+    kern<<<grid, 256, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t conv3x3(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t s) {
+#define SGI_CONV_CASE(CI, CO, CKK)                                           \
+    if (cin == CI && cout == CO) {                                           \
+        if (mode == 0) return run_conv<CI, CO, CKK, 0>(a, s);                \
+        if (mode == 1) return run_conv<CI, CO, CKK, 1>(a, s);                \
+        return run_conv<CI, CO, CKK, 2>(a, s);                               \
+    }
+    SGI_CONV_CASE(16, 32, 16)
+    SGI_CONV_CASE(32, 32, 32)
+    SGI_CONV_CASE(32, 64, 32)
+    SGI_CONV_CASE(64, 64, 32)
+    SGI_CONV_CASE(64, 128, 32)
+    SGI_CONV_CASE(128, 128, 32)
+    SGI_CONV_CASE(192, 64, 32)
+    SGI_CONV_CASE(96, 32, 32)
+    SGI_CONV_CASE(64, 32, 32)
+    SGI_CONV_CASE(128, 64, 32)
+    SGI_CONV_CASE(64, 192, 32)
+    SGI_CONV_CASE(32, 96, 32)
+#undef SGI_CONV_CASE
+    return cudaErrorInvalidValue;
+}
+
+// dgrad weights: wt[ci][tap][co] = w[co][8 - tap][ci]
+__global__ void flip_weights_kernel(const bf16* __restrict__ w, bf16* __restrict__ wt, int cin, int cout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cin * 9 * cout) return;
+    const int ci = i / (9 * cout), r = i % (9 * cout), tap = r / cout, co = r % cout;
+    wt[i] = w[((size_t)co * 9 + (8 - tap)) * cin + ci];
+}
+
+cudaError_t flip_weights(const bf16* w, bf16* wt, int cin, int cout, cudaStream_t s) {
+    const int n = cin * 9 * cout;
+    flip_weights_kernel<<<(n + 255) / 256, 256, 0, s>>>(w, wt, cin, cout);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- wgrad --
+// dw[co][tap][ci] += sum_{b, p} dz[b, p, co] * x[b, p + off(tap), ci] (FP32, CUDA cores)
+// A block takes one 8 x 16 pixel tile and a 32 (co) x 32 (ci) slab for all 9 taps;
+// thread t owns co = t / 8 and ci = (t % 8) * 4 .. + 3 for the 9 taps (36 sums).
+__global__ void __launch_bounds__(256) wgrad_kernel(WgradArgs a) {
+    __shared__ float sdz[kTileH * kTileW][33];
+    __shared__ float sx[kHaloH * kHaloW][33];
+    const int tid = threadIdx.x;
+    const int tiles_x = (a.W + kTileW - 1) / kTileW, tiles_y = (a.H + kTileH - 1) / kTileH;
+    const int tile = blockIdx.x % (tiles_x * tiles_y), b = blockIdx.x / (tiles_x * tiles_y);
+    const int x0 = (tile % tiles_x) * kTileW, y0 = (tile / tiles_x) * kTileH;
+    const int co0 = blockIdx.y * 32, ci0 = blockIdx.z * 32;
+    const int H = a.H, W = a.W;
+    const bf16* dzb = a.dz + (size_t)b * H * W * a.dzs;
+    const bf16* xb = a.x + (size_t)b * H * W * a.xs;
+    for (int v = tid; v < kTileH * kTileW * 32; v += 256) {
+        const int p = v / 32, c = v % 32;
+        const int gy = y0 + p / kTileW, gx = x0 + p % kTileW;
+        float val = 0.0f;
+        if (gy < H && gx < W && co0 + c < a.cout) val = __bfloat162float(dzb[((size_t)gy * W + gx) * a.dzs + co0 + c]);
+        sdz[p][c] = val;
+    }
+    for (int v = tid; v < kHaloH * kHaloW * 32; v += 256) {
+        const int p = v / 32, c = v % 32;
+        const int gy = y0 + p / kHaloW - 1, gx = x0 + p % kHaloW - 1;
+        float val = 0.0f;
+        if (gy >= 0 && gy < H && gx >= 0 && gx < W && ci0 + c < a.cin)
+            val = __bfloat162float(xb[((size_t)gy * W + gx) * a.xs + ci0 + c]);
+        sx[p][c] = val;
+    }
+    __syncthreads();
+    const int co = tid >> 3, cib = (tid & 7) * 4;
+    float acc[9][4];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
+    for (int py = 0; py < kTileH; ++py) {
+        for (int px = 0; px < kTileW; ++px) {
+            const float g = sdz[py * kTileW + px][co];
+#pragma unroll
+            for (int t = 0; t < 9; ++t) {
+                const float* xr = sx[(py + t / 3) * kHaloW + px + t % 3];
+                acc[t][0] = fmaf(g, xr[cib + 0], acc[t][0]);
+                acc[t][1] = fmaf(g, xr[cib + 1], acc[t][1]);
+                acc[t][2] = fmaf(g, xr[cib + 2], acc[t][2]);
+                acc[t][3] = fmaf(g, xr[cib + 3], acc[t][3]);
+            }
+        }
+    }
+    if (co0 + co >= a.cout) return;
+#pragma unroll
+    for (int t = 0; t < 9; ++t)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (ci0 + cib + j < a.cin)
+                atomicAdd(a.dw + ((size_t)(co0 + co) * 9 + t) * a.cin + ci0 + cib + j, acc[t][j]);
+}
+
+cudaError_t wgrad(const WgradArgs& a, cudaStream_t s) {
+    const int tiles = ((a.W + kTileW - 1) / kTileW) * ((a.H + kTileH - 1) / kTileH);
+    dim3 grid(tiles * a.B, (a.cout + 31) / 32, (a.cin + 31) / 32);
+    wgrad_kernel<<<grid, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// db[c] += sum over pixels of dz[., c]
+__global__ void bias_grad_kernel(const bf16* __restrict__ dz, int dzs, int c, size_t pixels, float* __restrict__ db) {
+    const int ch = threadIdx.x % 32 + blockIdx.y * 32;
+    const int row = threadIdx.x / 32;
+    float acc = 0.0f;
+    if (ch < c)
+        for (size_t p = (size_t)blockIdx.x * 8 + row; p < pixels; p += (size_t)gridDim.x * 8)
+            acc += __bfloat162float(dz[p * dzs + ch]);
+    __shared__ float red[8][32];
+    red[row][threadIdx.x % 32] = acc;
+    __syncthreads();
+    if (row == 0 && ch < c) {
+        float s = 0.0f;
+        for (int r = 0; r < 8; ++r) s += red[r][threadIdx.x];
+        atomicAdd(db + ch, s);
+    }
+}
+
+cudaError_t bias_grad(const bf16* dz, int dzs, int c, size_t pixels, float* db, cudaStream_t s) {
+    dim3 grid(256, (c + 31) / 32);
+    bias_grad_kernel<<<grid, 256, 0, s>>>(dz, dzs, c, pixels, db);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------- elementwise / resampling --
+// dz = dy * (y > 0)
+__global__ void relu_bwd_kernel(const bf16* __restrict__ dy, int dys, const bf16* __restrict__ y, int ys,
+                                bf16* __restrict__ dz, int c, size_t pixels) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pixels * c) return;
+    const size_t p = i / c;
+    const int ch = (int)(i % c);
+    const float yv = __bfloat162float(y[p * ys + ch]);
+    dz[i] = yv > 0.0f ? dy[p * dys + ch] : __float2bfloat16(0.0f);
+}
+
+cudaError_t relu_bwd(const bf16* dy, int dys, const bf16* y, int ys, bf16* dz, int c, size_t pixels, cudaStream_t s) {
+    const size_t n = pixels * c;
+    relu_bwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dy, dys, y, ys, dz, c, pixels);
+    return cudaGetLastError();
+}
+
+// 2x2 average pooling (H, W even): out[b, y, x] = mean of in[b, 2y.., 2x..]
+__global__ void pool_fwd_kernel(const bf16* __restrict__ in, int is, bf16* __restrict__ out, int os, int B, int H,
+                                int W, int c) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int Ho = H / 2, Wo = W / 2;
+    if (i >= (size_t)B * Ho * Wo * c) return;
+    const int ch = (int)(i % c);
+    const size_t q = i / c;
+    const int xo = (int)(q % Wo), yo = (int)((q / Wo) % Ho), b = (int)(q / ((size_t)Wo * Ho));
+    const bf16* base = in + ((size_t)b * H * W) * is;
+    float s = 0.0f;
+    for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx)
+            s += __bfloat162float(base[((size_t)(2 * yo + dy) * W + 2 * xo + dx) * is + ch]);
+    out[((size_t)b * Ho * Wo + (size_t)yo * Wo + xo) * os + ch] = __float2bfloat16(0.25f * s);
+}
+
+// din[b, y, x] (+)= 0.25 * dout[b, y/2, x/2]
+__global__ void pool_bwd_kernel(const bf16* __restrict__ dout, int os, bf16* __restrict__ din, int is, int B, int H,
+                                int W, int c, int accumulate) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)B * H * W * c) return;
+    const int ch = (int)(i % c);
+    const size_t q = i / c;
+    const int x = (int)(q % W), y = (int)((q / W) % H), b = (int)(q / ((size_t)W * H));
+    const int Ho = H / 2, Wo = W / 2;
+    float v = 0.25f * __bfloat162float(dout[((size_t)b * Ho * Wo + (size_t)(y / 2) * Wo + x / 2) * os + ch]);
+    bf16* d = din + ((size_t)b * H * W + (size_t)y * W + x) * is + ch;
+    if (accumulate) v += __bfloat162float(*d);
+    *d = __float2bfloat16(v);
+}
+
+// nearest 2x upsampling: out[b, y, x] = in[b, y/2, x/2]
+__global__ void up_fwd_kernel(const bf16* __restrict__ in, int is, bf16* __restrict__ out, int os, int B, int H,
+                              int W, int c) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)B * H * W * c) return;
+    const int ch = (int)(i % c);
+    const size_t q = i / c;
+    const int x = (int)(q % W), y = (int)((q / W) % H), b = (int)(q / ((size_t)W * H));
+    const int Hi = H / 2, Wi = W / 2;
+    out[((size_t)b * H * W + (size_t)y * W + x) * os + ch] =
+        in[((size_t)b * Hi * Wi + (size_t)(y / 2) * Wi + x / 2) * is + ch];
+}
+
+// din[b, y, x] = sum of dout over the 2x2 block it was copied to
+__global__ void up_bwd_kernel(const bf16* __restrict__ dout, int os, bf16* __restrict__ din, int is, int B, int Hi,
+                              int Wi, int c) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)B * Hi * Wi * c) return;
+    const int ch = (int)(i % c);
+    const size_t q = i / c;
+    const int x = (int)(q % Wi), y = (int)((q / Wi) % Hi), b = (int)(q / ((size_t)Wi * Hi));
+    const int H = Hi * 2, W = Wi * 2;
+    float s = 0.0f;
+    for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx)
+            s += __bfloat162float(dout[((size_t)b * H * W + (size_t)(2 * y + dy) * W + 2 * x + dx) * os + ch]);
+    din[((size_t)b * Hi * Wi + (size_t)y * Wi + x) * is + ch] = __float2bfloat16(s);
+}
+
+cudaError_t pool_fwd(const bf16* in, int is, bf16* out, int os, int B, int H, int W, int c, cudaStream_t s) {
+    const size_t n = (size_t)B * (H / 2) * (W / 2) * c;
+    pool_fwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, is, out, os, B, H, W, c);
+    return cudaGetLastError();
+}
+cudaError_t pool_bwd(const bf16* dout, int os, bf16* din, int is, int B, int H, int W, int c, int acc, cudaStream_t s) {
+    const size_t n = (size_t)B * H * W * c;
+    pool_bwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dout, os, din, is, B, H, W, c, acc);
+    return cudaGetLastError();
+}
+cudaError_t up_fwd(const bf16* in, int is, bf16* out, int os, int B, int H, int W, int c, cudaStream_t s) {
+    const size_t n = (size_t)B * H * W * c;
+    up_fwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, is, out, os, B, H, W, c);
+    return cudaGetLastError();
+}
+cudaError_t up_bwd(const bf16* dout, int os, bf16* din, int is, int B, int Hi, int Wi, int c, cudaStream_t s) {
+    const size_t n = (size_t)B * Hi * Wi * c;
+    up_bwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dout, os, din, is, B, Hi, Wi, c);
+    return cudaGetLastError();
+}
+
+// --------------------------------------------------------- kernel apply --
+// logits [B, H, W, 32] (0..24: 5x5 kernel, 25: temporal blend), noisy / prev
+// [B, H, W, 4] float (rgb used). out = a * sum_k softmax(l)_k noisy(p + o_k) + (1 - a) * prev,
+// a = sigmoid(l25); neighbours clamped to the image. With a target, also the
+// loss sum of |log1p(out) - log1p(target)| and dlogits = d(mean loss)/dlogits.
+__global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t P = (size_t)a.B * a.H * a.W;
+    float loss = 0.0f;
+    if (i < P) {
+        const int x = (int)(i % a.W), y = (int)((i / a.W) % a.H);
+        const size_t img = i / ((size_t)a.W * a.H);
+        const bf16* lg = a.logits + i * 32;
+        float l[25];
+        float mx = -3.0e38f;
+#pragma unroll
+        for (int k = 0; k < 25; ++k) { l[k] = __bfloat162float(lg[k]); mx = fmaxf(mx, l[k]); }
+        float den = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 25; ++k) { l[k] = __expf(l[k] - mx); den += l[k]; }
+        const float inv = 1.0f / den;
+        float sp[3] = {0.0f, 0.0f, 0.0f};
+        float nb[25][3];
+#pragma unroll
+        for (int k = 0; k < 25; ++k) {
+            l[k] *= inv;
+            const int xx = min(max(x + k % 5 - 2, 0), a.W - 1), yy = min(max(y + k / 5 - 2, 0), a.H - 1);
+            const float4 nv = a.noisy[(img * a.H + yy) * a.W + xx];
+            nb[k][0] = nv.x; nb[k][1] = nv.y; nb[k][2] = nv.z;
+            sp[0] = fmaf(l[k], nv.x, sp[0]); sp[1] = fmaf(l[k], nv.y, sp[1]); sp[2] = fmaf(l[k], nv.z, sp[2]);
+        }
+        const float alpha = 1.0f / (1.0f + __expf(-__bfloat162float(lg[25])));
+        const float4 pv = a.prev[i];
+        const float pr[3] = {pv.x, pv.y, pv.z};
+        float o[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[c] = alpha * sp[c] + (1.0f - alpha) * pr[c];
+        if (a.out) a.out[i] = make_float4(o[0], o[1], o[2], 1.0f);
+        if (a.target) {
+            const float4 tv = a.target[i];
+            const float t[3] = {tv.x, tv.y, tv.z};
+            float dout[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float oc = fmaxf(o[c], 0.0f);
+                const float d = log1pf(oc) - log1pf(fmaxf(t[c], 0.0f));
+                loss += fabsf(d);
+                const float g = (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) / (1.0f + oc) * a.grad_scale;
+                dout[c] = o[c] > 0.0f ? g : 0.0f;
+            }
+            float dalpha = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) dalpha += dout[c] * (sp[c] - pr[c]);
+            float dw[25];
+            float dot_wdw = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 25; ++k) {
+                dw[k] = alpha * (dout[0] * nb[k][0] + dout[1] * nb[k][1] + dout[2] * nb[k][2]);
+                dot_wdw += l[k] * dw[k];
+            }
+            bf16* dl = a.dlogits + i * 32;
+#pragma unroll
+            for (int k = 0; k < 25; ++k) dl[k] = __float2bfloat16(l[k] * (dw[k] - dot_wdw));
+            dl[25] = __float2bfloat16(dalpha * alpha * (1.0f - alpha));
+#pragma unroll
+            for (int k = 26; k < 32; ++k) dl[k] = __float2bfloat16(0.0f);
+        }
+    }
+    if (a.loss) {
+        // block reduction of the loss
+        __shared__ float red[256];
+        red[threadIdx.x] = loss;
+        __syncthreads();
+        for (int s = 128; s > 0; s >>= 1) {
+            if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) atomicAdd(a.loss, red[0]);
+    }
+}
+
+cudaError_t kpcn_apply(const ApplyArgs& a, cudaStream_t s) {
+    const size_t P = (size_t)a.B * a.H * a.W;
+    kpcn_apply_kernel<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ Adam --
+__global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, bf16* __restrict__ wb, size_t n, float lr, float b1, float b2,
+                            float eps, float c1, float c2) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16(wi);
+}
+
+cudaError_t adam(float* w, const float* g, float* m, float* v, bf16* wb, size_t n, float lr, float b1, float b2,
+                 float eps, int step, cudaStream_t s) {
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    adam_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w, g, m, v, wb, n, lr, b1, b2, eps, c1, c2);
+    return cudaGetLastError();
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ w, bf16* __restrict__ wb, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) wb[i] = __float2bfloat16(w[i]);
+}
+
+cudaError_t to_bf16(const float* w, bf16* wb, size_t n, cudaStream_t s) {
+    to_bf16_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w, wb, n);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------- frame features --
+__device__ __forceinline__ float h2f_nn(uint32_t bits16) { return __half2float(__ushort_as_half((unsigned short)bits16)); }
+__device__ __forceinline__ float4 unpack4(uint2 t) {
+    return make_float4(h2f_nn(t.x & 0xffffu), h2f_nn(t.x >> 16), h2f_nn(t.y & 0xffffu), h2f_nn(t.y >> 16));
+}
+__device__ __forceinline__ float lum(float4 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+__global__ void __launch_bounds__(256) features_kernel(FeatureArgs a) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = a.W, H = a.H;
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * W + x;
+    const float4 nz = unpack4(a.merged[i]);
+    // 3x3 luminance variance of the noisy estimate
+    float s1 = 0.0f, s2 = 0.0f;
+    for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int xx = min(max(x + dx, 0), W - 1), yy = min(max(y + dy, 0), H - 1);
+            const float l = lum(unpack4(a.merged[(size_t)yy * W + xx]));
+            s1 += l; s2 += l * l;
+        }
+    const float mean = s1 / 9.0f;
+    const float var = fmaxf(s2 / 9.0f - mean * mean, 0.0f);
+    const float4 g = a.guide[i];
+    const uint32_t alb = a.albedo[i], rma = a.rma[i];
+    // view distance from the unprojected depth
+    const float u = (x + 0.5f) / W, v = (y + 0.5f) / H;
+    const float* m = a.inv_pv;
+    const float nx = u * 2.0f - 1.0f, ny = v * 2.0f - 1.0f, nzc = g.w * 2.0f - 1.0f;
+    const float wx = m[0] * nx + m[4] * ny + m[8] * nzc + m[12];
+    const float wy = m[1] * nx + m[5] * ny + m[9] * nzc + m[13];
+    const float wz = m[2] * nx + m[6] * ny + m[10] * nzc + m[14];
+    const float ww = m[3] * nx + m[7] * ny + m[11] * nzc + m[15];
+    const float px = wx / ww - a.cam_pos[0], py = wy / ww - a.cam_pos[1], pz = wz / ww - a.cam_pos[2];
+    const float dist = sqrtf(px * px + py * py + pz * pz);
+    // previous output warped by the velocity (bilinear, clamped)
+    const uint32_t vel = a.velocity[i];
+    const float pu = (u - h2f_nn(vel & 0xffffu)) * W - 0.5f, pv = (v - h2f_nn(vel >> 16)) * H - 0.5f;
+    const float fu = floorf(pu), fv = floorf(pv);
+    const float au = pu - fu, av = pv - fv;
+    const int i0 = min(max((int)fu, 0), W - 1), i1 = min(max((int)fu + 1, 0), W - 1);
+    const int j0 = min(max((int)fv, 0), H - 1), j1 = min(max((int)fv + 1, 0), H - 1);
+    const float4 p00 = unpack4(a.gi_prev[(size_t)j0 * W + i0]), p10 = unpack4(a.gi_prev[(size_t)j0 * W + i1]);
+    const float4 p01 = unpack4(a.gi_prev[(size_t)j1 * W + i0]), p11 = unpack4(a.gi_prev[(size_t)j1 * W + i1]);
+    const float w00 = (1 - au) * (1 - av), w10 = au * (1 - av), w01 = (1 - au) * av, w11 = au * av;
+    float4 pr;
+    pr.x = p00.x * w00 + p10.x * w10 + p01.x * w01 + p11.x * w11;
+    pr.y = p00.y * w00 + p10.y * w10 + p01.y * w01 + p11.y * w11;
+    pr.z = p00.z * w00 + p10.z * w10 + p01.z * w01 + p11.z * w11;
+    pr.w = 1.0f;
+    if (!a.have_history) pr = make_float4(nz.x, nz.y, nz.z, 1.0f);
+    a.noisy[i] = make_float4(nz.x, nz.y, nz.z, 1.0f);
+    a.prev[i] = pr;
+    float f[16];
+    f[0] = log1pf(fmaxf(nz.x, 0.0f)); f[1] = log1pf(fmaxf(nz.y, 0.0f)); f[2] = log1pf(fmaxf(nz.z, 0.0f));
+    f[3] = fmaxf((alb & 0xffu) / 255.0f, 0.01f); f[4] = fmaxf(((alb >> 8) & 0xffu) / 255.0f, 0.01f);
+    f[5] = fmaxf(((alb >> 16) & 0xffu) / 255.0f, 0.01f);
+    f[6] = g.x; f[7] = g.y; f[8] = g.z;
+    f[9] = dist * 0.1f;
+    f[10] = (rma & 0xffu) / 255.0f;
+    f[11] = log1pf(var);
+    f[12] = log1pf(fmaxf(pr.x, 0.0f)); f[13] = log1pf(fmaxf(pr.y, 0.0f)); f[14] = log1pf(fmaxf(pr.z, 0.0f));
+    f[15] = ((rma >> 8) & 0xffu) / 255.0f;
+    __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(a.features + i * 16);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) o[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+}
+
+cudaError_t features(const FeatureArgs& a, cudaStream_t s) {
+    dim3 block(32, 8), grid((a.W + 31) / 32, (a.H + 7) / 8);
+    features_kernel<<<grid, block, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// hdr = screen + gi * denoised, gi = RGB16F(max(albedo, 0.01) + 1e-5); history <- denoised
+__global__ void composite_kernel(const float4* __restrict__ den, const uint2* __restrict__ screen,
+                                 const uint32_t* __restrict__ albedo, uint2* __restrict__ hdr,
+                                 uint2* __restrict__ gi_out, uint16_t* __restrict__ hist_out, size_t P) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const float4 d = den[i];
+    const float4 sc = unpack4(screen[i]);
+    const uint32_t alb = albedo[i];
+    const float g0 = __half2float(__float2half_rn(fmaxf((alb & 0xffu) / 255.0f, 0.01f) + 0.00001f));
+    const float g1 = __half2float(__float2half_rn(fmaxf(((alb >> 8) & 0xffu) / 255.0f, 0.01f) + 0.00001f));
+    const float g2 = __half2float(__float2half_rn(fmaxf(((alb >> 16) & 0xffu) / 255.0f, 0.01f) + 0.00001f));
+    auto pack = [](float a0, float a1, float a2, float a3) {
+        return make_uint2((uint32_t)__half_as_ushort(__float2half_rn(a0)) |
+                              ((uint32_t)__half_as_ushort(__float2half_rn(a1)) << 16),
+                          (uint32_t)__half_as_ushort(__float2half_rn(a2)) |
+                              ((uint32_t)__half_as_ushort(__float2half_rn(a3)) << 16));
+    };
+    hdr[i] = pack(sc.x + g0 * d.x, sc.y + g1 * d.y, sc.z + g2 * d.z, 1.0f);
+    gi_out[i] = pack(d.x, d.y, d.z, 1.0f);
+    hist_out[i] = __half_as_ushort(__float2half_rn(1.0f));
+}
+
+cudaError_t composite(const float4* den, const uint2* screen, const uint32_t* albedo, uint2* hdr, uint2* gi_out,
+                      uint16_t* hist_out, size_t P, cudaStream_t s) {
+    composite_kernel<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(den, screen, albedo, hdr, gi_out, hist_out, P);
+    return cudaGetLastError();
+}
+
+}  // namespace nn
+}  // namespace sgi

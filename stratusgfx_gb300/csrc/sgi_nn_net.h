@@ -1,0 +1,56 @@
+// sgi_nn_net.h - the U-Net object behind sgi_nn (host side, internal).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/sgi_nn.h"
+
+namespace sgi {
+namespace nn {
+
+struct Net {
+    sgi_nn_config cfg{};
+    size_t nparams = 0;
+    size_t w_off[11] = {}, b_off[11] = {};
+    int64_t launches = 0;
+    std::vector<void*> allocs;
+    // parameters
+    float *w32 = nullptr, *g32 = nullptr, *m32 = nullptr, *v32 = nullptr, *loss_dev = nullptr;
+    __nv_bfloat16 *wbf = nullptr, *wflip = nullptr;
+    // activations
+    __nv_bfloat16 *E1A_ = nullptr, *D1IN = nullptr, *P1 = nullptr, *E2A_ = nullptr, *D2IN = nullptr, *P2_ = nullptr,
+                  *B1_ = nullptr, *B2_ = nullptr, *D2A_ = nullptr, *D2B_ = nullptr, *D1A_ = nullptr, *D1B_ = nullptr,
+                  *LOG = nullptr;
+    // gradients (full, half and quarter resolution scratch)
+    __nv_bfloat16 *GA = nullptr, *GB = nullptr, *GC = nullptr, *GD = nullptr, *GH1 = nullptr, *GH2 = nullptr,
+                  *GH3 = nullptr, *GQ1 = nullptr, *GQ2 = nullptr, *GQ3 = nullptr;
+    float4* fwd_out = nullptr;
+
+    ~Net();
+    void release();
+    template <class T> cudaError_t alloc(T** p, size_t n);
+    cudaError_t init(const sgi_nn_config& c);
+    cudaError_t set_params(const float* host, size_t n);
+    cudaError_t conv(int l, const __nv_bfloat16* x, int xs, __nv_bfloat16* y, int ys, int B, int H, int W,
+                     cudaStream_t s);
+    cudaError_t forward(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);
+    cudaError_t layer_backward(int l, const __nv_bfloat16* x, int xs, const __nv_bfloat16* y, int ys,
+                               const __nv_bfloat16* dy, int dys, __nv_bfloat16* dz, __nv_bfloat16* dx, int dxs, int B,
+                               int H, int W, cudaStream_t s);
+    cudaError_t backward(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);
+};
+
+}  // namespace nn
+}  // namespace sgi
+
+struct sgi_nn {
+    sgi::nn::Net net;
+    std::string err;
+    int step = 0;
+};

@@ -1,0 +1,129 @@
+"""The learned denoiser on the GPU: gradients and outputs against the float64 oracle,
+training reduces the loss, weight files round-trip, and the neural frame runs.
+
+Tolerance: activations and gradients are stored in BF16 (8 mantissa bits) between
+layers, so per-layer gradients are compared by relative L2 error <= 5e-2 and cosine
+similarity >= 0.995 against the float64 oracle fed the same BF16-rounded inputs.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import kpcn  # noqa: E402
+from stratusgfx_gb300 import abi, stage  # noqa: E402
+from stratusgfx_gb300 import scene as S  # noqa: E402
+from stratusgfx_gb300.denoiser import KpcnDenoiser  # noqa: E402
+
+
+def bf16_round(a: np.ndarray) -> np.ndarray:
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(torch.bfloat16).float().numpy()
+
+
+def random_problem(B, H, W, seed):
+    rng = np.random.default_rng(seed)
+    feat = rng.normal(0, 1, (B, H, W, 16)).astype(np.float32)
+    noisy = rng.uniform(0.0, 2.0, (B, H, W, 4)).astype(np.float32)
+    prev = rng.uniform(0.0, 2.0, (B, H, W, 4)).astype(np.float32)
+    target = rng.uniform(0.0, 2.0, (B, H, W, 4)).astype(np.float32)
+    return feat, noisy, prev, target
+
+
+def to_dev(feat, noisy, prev, target):
+    return (torch.from_numpy(feat).to("cuda", torch.bfloat16), torch.from_numpy(noisy).cuda(),
+            torch.from_numpy(prev).cuda(), torch.from_numpy(target).cuda())
+
+
+def test_gradients_match_oracle():
+    B, H, W = 2, 16, 32
+    net = KpcnDenoiser(B, H, W, seed=3)
+    p = bf16_round(net.params())           # the forward uses BF16 weights
+    net.set_params(p)
+    feat, noisy, prev, target = random_problem(B, H, W, 1)
+    f, n, pv, t = to_dev(feat, noisy, prev, target)
+    loss = net.train_step(f, n, pv, t, 0.0, update=False)
+    g = net.grads()
+    ref_loss, ref_g, _ = kpcn.loss_and_grads(p.astype(np.float64), bf16_round(feat).astype(np.float64),
+                                             noisy[..., :3].astype(np.float64), prev[..., :3].astype(np.float64),
+                                             target[..., :3].astype(np.float64))
+    assert abs(loss - ref_loss) <= 2e-2 * ref_loss
+    off = 0
+    for name, ci, co in kpcn.LAYERS:
+        for part, cnt in (("w", co * 9 * ci), ("b", co)):
+            a, b = g[off:off + cnt].astype(np.float64), ref_g[off:off + cnt]
+            off += cnt
+            rel = np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30)
+            cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30))
+            assert rel <= 5e-2 and cos >= 0.995, (name, part, rel, cos)
+    net.close()
+
+
+def test_forward_matches_oracle():
+    B, H, W = 1, 32, 32
+    net = KpcnDenoiser(B, H, W, seed=5)
+    p = bf16_round(net.params())
+    net.set_params(p)
+    feat, noisy, prev, _ = random_problem(B, H, W, 2)
+    f, n, pv, _ = to_dev(feat, noisy, prev, noisy)
+    out = torch.empty((B, H, W, 4), dtype=torch.float32, device="cuda")
+    net.forward(f, n, pv, out)
+    torch.cuda.synchronize()
+    a = kpcn.forward(kpcn.unpack(p.astype(np.float64)), bf16_round(feat).astype(np.float64))
+    ref = kpcn.apply(a["head"], noisy[..., :3].astype(np.float64), prev[..., :3].astype(np.float64))
+    got = out.cpu().numpy()[..., :3]
+    rel = np.abs(got - ref).max() / np.abs(ref).max()
+    assert rel < 2e-2, rel
+    net.close()
+
+
+def test_training_reduces_loss_and_weights_round_trip(tmp_path):
+    B, H, W = 4, 32, 32
+    net = KpcnDenoiser(B, H, W, seed=7)
+    rng = np.random.default_rng(4)
+    noisy = rng.uniform(0.0, 2.0, (B, H, W, 4)).astype(np.float32)
+    target = np.repeat(noisy.mean(axis=(1, 2), keepdims=True), H, 1).repeat(W, 2)   # a smooth target
+    feat = np.zeros((B, H, W, 16), np.float32)
+    feat[..., :3] = np.log1p(noisy[..., :3])
+    f, n, pv, t = to_dev(feat, noisy, noisy.copy(), target.astype(np.float32))
+    first = net.train_step(f, n, pv, t, 1e-3)
+    for _ in range(60):
+        last = net.train_step(f, n, pv, t, 1e-3)
+    assert last < 0.7 * first, (first, last)
+    path = str(tmp_path / "w.bin")
+    net.save(path)
+    other = KpcnDenoiser(B, H, W, seed=99)
+    other.load(path)
+    assert np.array_equal(other.params(), net.params())
+    with open(path, "r+b") as fh:       # corrupt one byte: the CRC must catch it
+        fh.seek(100)
+        b = fh.read(1)
+        fh.seek(100)
+        fh.write(bytes([b[0] ^ 0xFF]))
+    with pytest.raises(ValueError):
+        other.load(path)
+    net.close()
+    other.close()
+
+
+def test_neural_frame_runs_through_the_abi():
+    w = S.Workload("room12_128x96_vpl64", 128, 96, 12, 64, 2, 512, 16, abi.SGI_CUBE_F16, 8, 5, 2)
+    sc = S.workload_scene(w, 21)
+    ds = stage.DeviceScene(sc, w)
+    st = stage.GiStage(stage.workload_config(w))
+    st.set_lights(ds.vpls, ds.entries, ds.points)
+    net = KpcnDenoiser(1, w.height, w.width, seed=1)
+    out = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
+    for k in (1, 2):
+        st.set_shadow_maps(ds.csms[k], ds.cubes)
+        cam = ds.camera(k)
+        fp = abi.FrameParams(1000.0 + 16 * k, 60.0)
+        import ctypes as C
+        abi.check(st.lib.sgi_render_frame_neural(st.ctx, net.h, C.byref(ds.gbuffers[k].struct()),
+                                                 C.byref(ds.gbuffers[k - 1].struct()), C.byref(cam), C.byref(fp),
+                                                 C.c_void_p(out.data_ptr()), C.c_void_p(0)), st.ctx)
+    torch.cuda.synchronize()
+    o = out.float().cpu().numpy()
+    assert np.isfinite(o).all() and (o[..., :3] > 0).mean() > 0.5
+    st.close()
+    net.close()

@@ -314,7 +314,7 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clock,
     }
     if rank == 0:
-        result["quality"] = quality_vs_converged(ds, sc, w, cfg)
+        result.update(neural_vs_plain(args, ds, sc, w, cfg, flush))
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline_from_device(ds, sc, w, cfg)
     st.close()
@@ -322,11 +322,39 @@ def run_ours(args, rank, world, local_rank):
     return result
 
 
-def quality_vs_converged(ds, sc, w, cfg, batches=64):
-    """PSNR of the plain path's HDR frames against the converged image: the same frame with the
-    GI term replaced by sgi_gi_target (64 batches of K = 8 = 512 samples per pixel, FP64 sums).
-    Frames 1..8 of the camera path are rendered in order (history accumulates); PSNR and MSE are
-    reduced in FP64 on the GPU."""
+def converged_targets(ds, sc, w, cfg, batches=64):
+    """Converged GI per frame: sgi_gi_target with 64 batches of 8 samples (FP64 sums), seeded
+    independently of the frames it judges. Returns (targets, ms per frame)."""
+    import torch
+
+    from stratusgfx_gb300 import stage
+    tcfg = stage.workload_config(w, samples_per_pixel=8)
+    st = stage.GiStage(tcfg)
+    st.set_lights(ds.vpls, ds.entries, ds.points)
+    frames = len(sc.cameras) - 1
+    out = []
+    ms = 0.0
+    for k in range(1, frames + 1):
+        st.set_shadow_maps(ds.csms[k], ds.cubes)
+        cam = ds.camera(k)
+        st.cull_vpls()
+        st.cull_tiles(ds.gbuffers[k], cam)
+        t = torch.empty((w.height, w.width, 4), dtype=torch.float32, device="cuda")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        st.gi_target(ds.gbuffers[k], cam, 1000.0 + 16.0 * k + 7.0e6, batches, t)
+        e1.record()
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+        out.append(t)
+    st.close()
+    return out, ms / frames
+
+
+def psnr_vs_converged(render, ds, sc, w, cfg, targets):
+    """Renders frames 1..8 in order with render(st, k, out) on a fresh context and returns the mean
+    PSNR (dB) of the HDR frame against the converged frame screen + gi * target, and of the GI term
+    alone; FP64 reductions on the GPU."""
     import torch
 
     from stratusgfx_gb300 import stage
@@ -334,33 +362,24 @@ def quality_vs_converged(ds, sc, w, cfg, batches=64):
     st.set_lights(ds.vpls, ds.entries, ds.points)
     H, W = w.height, w.width
     out = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
-    target = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
     direct = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
-    frames = len(sc.cameras) - 1
-    psnrs = []
-    t_target = 0.0
-    for k in range(1, frames + 1):
+    full, gi_only = [], []
+    for k in range(1, len(targets) + 1):
         st.set_shadow_maps(ds.csms[k], ds.cubes)
-        cam = ds.camera(k)
-        st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], cam, out, 1000.0 + 16.0 * k, 60.0)
-        st.direct_lighting(ds.gbuffers[k], cam, direct)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        st.gi_target(ds.gbuffers[k], cam, 1000.0 + 16.0 * k, batches, target)
-        e1.record()
+        render(st, k, out)
+        st.direct_lighting(ds.gbuffers[k], ds.camera(k), direct)
         torch.cuda.synchronize()
-        t_target += e0.elapsed_time(e1)
         alb = ds.gbuffers[k].albedo[..., :3].double() / 255.0
-        gi = torch.clamp(alb, min=0.01) + 1e-5
-        ref = direct[..., :3].double() + gi * target[..., :3].double()
+        gi = (torch.clamp(alb, min=0.01) + 1e-5).half().double()
+        ref_gi = gi * targets[k - 1][..., :3].double()
+        ref = direct[..., :3].double() + ref_gi
         got = out[..., :3].double()
-        mse = torch.mean((got - ref) ** 2)
-        peak = torch.max(ref)
-        psnrs.append(float(10.0 * torch.log10(peak * peak / mse)))
+        for lst, a, r in ((full, got, ref), (gi_only, got - direct[..., :3].double(), ref_gi)):
+            mse = torch.mean((a - r) ** 2)
+            peak = torch.max(torch.abs(r))
+            lst.append(float(10.0 * torch.log10(peak * peak / mse)))
     st.close()
-    return {"psnr_db_vs_converged": [round(p, 2) for p in psnrs], "target": f"{batches} x K={w.samples} samples, "
-            f"FP64 sums", "target_ms_per_frame": round(t_target / frames, 2),
-            "psnr_mean_db": round(sum(psnrs) / len(psnrs), 2)}
+    return round(sum(full) / len(full), 2), round(sum(gi_only) / len(gi_only), 2)
 
 
 def cpu_baseline_from_device(ds, sc, w, cfg):
@@ -393,6 +412,79 @@ def cpu_baseline_from_device(ds, sc, w, cfg):
     return {"value": round(nf * W * H / dt / 1e6, 4), "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{nf} full {W}x{H} frames of the same workload through the FP32 oracle (OpenMP), "
                       f"{dt:.1f} s"}
+
+
+def time_frames(render, ds, frames, steps, warmup, flush):
+    """Mean ms per frame of render(k) over `steps` frames (L2 flushed before each, outside the events)."""
+    import torch
+    for s in range(warmup):
+        render(s % frames + 1, s)
+    torch.cuda.synchronize()
+    ms = 0.0
+    for s in range(steps):
+        flush.fill_(float(s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        render((warmup + s) % frames + 1, warmup + s)
+        e1.record()
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    return ms / steps
+
+
+def neural_vs_plain(args, ds, sc, w, cfg, flush):
+    """The metric's comparison: plain a-trous at K = 8 against the learned denoiser at K = 8, 4, 2;
+    ms/frame (device-resident) and PSNR against the converged frame. The neural configuration
+    reported is the fastest whose PSNR reaches the plain path's."""
+    import ctypes as C
+
+    import torch
+
+    from stratusgfx_gb300 import abi, denoiser, stage
+    if not os.path.exists(denoiser.WEIGHTS):
+        return {"neural": {"unavailable": f"no trained weights at {denoiser.WEIGHTS}"}}
+    targets, target_ms = converged_targets(ds, sc, w, cfg)
+    frames = len(sc.cameras) - 1
+    H, W = w.height, w.width
+    net = denoiser.KpcnDenoiser(1, H, W)
+    net.load(denoiser.WEIGHTS)
+    res = {"plain": {}, "neural": {}}
+
+    def plain_render(st, k, out):
+        st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * k, 60.0)
+
+    def neural_render(st, k, out):
+        fp = abi.FrameParams(1000.0 + 16.0 * k, 60.0)
+        abi.check(st.lib.sgi_render_frame_neural(st.ctx, net.h, C.byref(ds.gbuffers[k].struct()),
+                                                 C.byref(ds.gbuffers[k - 1].struct()), C.byref(ds.camera(k)),
+                                                 C.byref(fp), C.c_void_p(out.data_ptr()),
+                                                 stage._stream_ptr(None)), st.ctx)
+
+    out = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+    for name, render, ks in (("plain", plain_render, (8,)), ("neural", neural_render, (8, 4, 2))):
+        for K in ks:
+            kcfg = stage.workload_config(w, samples_per_pixel=K)
+            st = stage.GiStage(kcfg)
+            st.set_lights(ds.vpls, ds.entries, ds.points)
+
+            def one(k, s, st=st, render=render):
+                st.set_shadow_maps(ds.csms[k], ds.cubes)
+                render(st, k, out)
+
+            ms = time_frames(one, ds, frames, max(8, args.steps // 2), 3, flush)
+            st.close()
+            p_full, p_gi = psnr_vs_converged(render, ds, sc, w, kcfg, targets)
+            res[name][f"K{K}"] = {"ms_per_frame": round(ms, 4), "mpix_s": round(W * H / ms / 1e3, 1),
+                                  "psnr_db": p_full, "psnr_gi_db": p_gi}
+    net.close()
+    plain = res["plain"]["K8"]
+    ok = [(v["ms_per_frame"], k) for k, v in res["neural"].items() if v["psnr_gi_db"] >= plain["psnr_gi_db"]]
+    res["equal_psnr"] = ({"neural_config": min(ok)[1], "neural_ms": min(ok)[0], "plain_ms": plain["ms_per_frame"],
+                          "speedup": round(plain["ms_per_frame"] / min(ok)[0], 3)}
+                         if ok else {"neural_config": None, "note": "no neural configuration reached the plain "
+                                                                     "path's GI PSNR"})
+    res["converged_target"] = {"samples_per_pixel": 512, "accumulation": "fp64", "ms_per_frame": round(target_ms, 2)}
+    return res
 
 
 # ---------------------------------------------------- reference arm ----

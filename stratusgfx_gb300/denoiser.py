@@ -119,22 +119,27 @@ class Dataset:
 
 
 def make_dataset(num_frames: int, H: int = 256, W: int = 256, frames_per_room: int = 16, seed: int = 100,
-                 samples: int = 8, batches: int = 64, num_boxes: int = 40, num_vpls: int = 2048,
+                 samples=(2, 4, 8), batches: int = 64, num_boxes: int = 40, num_vpls: int = 2048,
                  log=print) -> Dataset:
     """Plain-path training pairs: each room (seeded generator) gets a camera path of frames_per_room
-    frames; every frame renders through sgi_render_frame (K samples, a-trous history), then its
-    features and the converged target (batches x K samples, FP64 sums)."""
-    w = S.Workload(f"train_room{num_boxes}_{W}x{H}", W, H, num_boxes, num_vpls, 4, 1024, 64, abi.SGI_CUBE_F16,
-                   samples, 5, frames_per_room)
+    frames, rendered with K samples per pixel (K cycles through `samples` room by room) through
+    sgi_render_frame (a-trous history), then its features and the converged target (batches
+    independent runs of 8 samples, FP64 sums: the same target for every K)."""
     ds = Dataset(num_frames, H, W)
-    cfg = stage.workload_config(w)
     out = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
     t0 = time.time()
     room = 0
     while ds.n < num_frames:
+        K = samples[room % len(samples)]
+        w = S.Workload(f"train_room{num_boxes}_{W}x{H}", W, H, num_boxes, num_vpls, 4, 1024, 64, abi.SGI_CUBE_F16,
+                       K, 5, frames_per_room)
+        cfg = stage.workload_config(w)
+        tcfg = stage.workload_config(w, samples_per_pixel=8)
         sc = S.workload_scene(w, seed + room)
         dsc = stage.DeviceScene(sc, w)
         st = stage.GiStage(cfg)
+        tst = stage.GiStage(tcfg)
+        tst.set_lights(dsc.vpls, dsc.entries, dsc.points)
         st.set_lights(dsc.vpls, dsc.entries, dsc.points)
         for k in range(1, len(sc.cameras)):
             if ds.n >= num_frames:
@@ -147,10 +152,14 @@ def make_dataset(num_frames: int, H: int = 256, W: int = 256, frames_per_room: i
             abi.check(st.lib.sgi_nn_features(st.ctx, C.byref(dsc.gbuffers[k].struct()), C.byref(cam),
                                              _p(ds.feat[i]), _p(ds.noisy[i]), _p(ds.prev[i]),
                                              stage._stream_ptr(None)), st.ctx)
-            st.gi_target(dsc.gbuffers[k], cam, t, batches, ds.target[i])
+            tst.set_shadow_maps(dsc.csms[k], dsc.cubes)
+            tst.cull_vpls()
+            tst.cull_tiles(dsc.gbuffers[k], cam)
+            tst.gi_target(dsc.gbuffers[k], cam, t + 7.0e6, batches, ds.target[i])
             ds.n += 1
         torch.cuda.synchronize()
         st.close()
+        tst.close()
         del dsc
         room += 1
     log(f"dataset: {ds.n} frames of {W}x{H} from {room} rooms in {time.time() - t0:.1f} s")

@@ -67,6 +67,26 @@ sgi_status sgi_nn_train_step(sgi_nn* net, const void* features, const float* noi
 sgi_status sgi_nn_features(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_camera* cam, void* features,
                            float* noisy, float* prev, void* stream);
 
+/* Convolution engine of the 3x3 layers: tcgen05.mma with TMEM accumulators
+ * (default) or warp-level mma.sync. Both accumulate BF16 products in FP32. */
+enum { SGI_NN_CONV_WARP_MMA = 0, SGI_NN_CONV_TCGEN05 = 1 };
+sgi_status sgi_nn_set_conv_path(sgi_nn* net, int32_t path);
+
+/* Synchronises the device and reads (and clears) the network's error flag:
+ * SGI_ERR_TIMEOUT when a tensor-core convolution gave up a bounded wait. */
+sgi_status sgi_nn_device_status(sgi_nn* net);
+
+/* One 3x3 convolution layer (zero padding) as the network runs it:
+ * y[b][h][w][o] = act(bias[o] + sum_{ky,kx,c} w[o][ky*3+kx][c] * x[b][h+ky-1][w+kx-1][c])
+ * with act = ReLU (mode 0), identity (mode 1) or no bias and identity (mode 2).
+ * x, y: BF16 NHWC with channel strides x_stride / y_stride (elements, multiples
+ * of 8; pointers 16-byte aligned); w: BF16 [cout][9][cin]; bias: float [cout].
+ * (cin, cout) must be one of the network's layer shapes or their transposes.
+ * err_flag: device int set to 1 if a tcgen05 wait ran out (required for that path). */
+sgi_status sgi_nn_conv3x3(int32_t path, int32_t cin, int32_t cout, int32_t mode, const void* x, int32_t x_stride,
+                          const void* w, const float* bias, void* y, int32_t y_stride, int32_t batch, int32_t height,
+                          int32_t width, int32_t* err_flag, void* stream);
+
 /* The GI stage with the learned denoiser in place of the a-trous passes:
  * VPL cull, direct lighting, tile cull, GI gather, features, U-Net, kernel
  * apply + temporal blend, composite hdr_out = screen + gi * denoised. The

@@ -106,6 +106,9 @@ class SceneCamera(C.Structure):
 
 assert C.sizeof(Vpl) == 64 and C.sizeof(PointLight) == 48 and C.sizeof(AtlasEntry) == 8 and C.sizeof(Box) == 64
 
+SGI_NN_CONV_WARP_MMA = 0
+SGI_NN_CONV_TCGEN05 = 1
+
 EXPORTS = {
     "sgi_abi_version": (C.c_int32, []),
     "sgi_status_string": (C.c_char_p, [C.c_int32]),
@@ -142,6 +145,11 @@ EXPORTS = {
                                       C.c_int32, C.c_int32, C.c_float, C.c_int32, C.POINTER(C.c_float), C.c_void_p]),
     "sgi_nn_features": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(Camera), C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p]),
+    "sgi_nn_set_conv_path": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "sgi_nn_device_status": (C.c_int32, [C.c_void_p]),
+    "sgi_nn_conv3x3": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                   C.c_void_p]),
     "sgi_render_frame_neural": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(GBuffer), C.POINTER(GBuffer),
                                             C.POINTER(Camera), C.POINTER(FrameParams), C.c_void_p, C.c_void_p]),
     "sgi_scene_gbuffer": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(SceneCamera), C.c_int32, C.c_int32,

@@ -1,10 +1,10 @@
 // sgi_nn.cu - kernels of the learned kernel-predicting denoiser (KPCNN).
 //
 // No counterpart in StratusGFX: it stands in for the a-trous filter of
-// vpl_pbr_gi_denoise.fs. Tensors are NHWC; activations and gradients BF16,
-// accumulation FP32, master weights FP32. A tensor view is (pointer to the
-// first channel, channel stride), so skip connections are written straight
-// into channel slices of the decoder inputs and no concatenation is copied.
+// vpl_pbr_gi_denoise.fs. Activations and gradients BF16, accumulation FP32,
+// master weights FP32. Tensors are strided views (View in sgi_nn_internal.h:
+// NHWC or channel-group planar), so skip connections are written straight into
+// channel slices of the decoder inputs and no concatenation is copied.
 //
 // 3x3 convolutions are implicit GEMMs on the tensor cores: a block computes an
 // 8 x 16 pixel tile for all output channels; the (8+2) x (16+2) input halo and
@@ -59,7 +59,6 @@ __global__ void __launch_bounds__(256) conv3x3_kernel(ConvArgs a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int x0 = blockIdx.x * kTileW, y0 = blockIdx.y * kTileH, b = blockIdx.z;
     const int H = a.H, W = a.W;
-    const bf16* xb = a.x + (size_t)b * H * W * a.xs;
 
     float acc[NT][4];
 #pragma unroll
@@ -75,7 +74,7 @@ __global__ void __launch_bounds__(256) conv3x3_kernel(ConvArgs a) {
             const int gy = y0 + hy - 1, gx = x0 + hx - 1;
             uint4 val = make_uint4(0u, 0u, 0u, 0u);
             if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-                val = *reinterpret_cast<const uint4*>(xb + ((size_t)gy * W + gx) * a.xs + c0 + q * 8);
+                val = *reinterpret_cast<const uint4*>(a.x.p + a.x.at(b, (size_t)gy * W + gx, c0 / 8 + q));
             *reinterpret_cast<uint4*>(halo + pix * HP + q * 8) = val;
         }
         // weights of this channel chunk: [COUT][9][CK]
@@ -109,7 +108,6 @@ __global__ void __launch_bounds__(256) conv3x3_kernel(ConvArgs a) {
     // epilogue: rows = pixels (lane >> 2, +8), columns = channels ((lane & 3) * 2, +1)
     const int gy = y0 + warp;
     if (gy >= H) return;
-    bf16* yb = a.y + (size_t)b * H * W * a.ys;
 #pragma unroll
     for (int n = 0; n < NT; ++n) {
         const int co = n * 8 + (lane & 3) * 2;
@@ -121,7 +119,8 @@ __global__ void __launch_bounds__(256) conv3x3_kernel(ConvArgs a) {
             if (gx >= W) continue;
             float v0 = acc[n][2 * h] + bias0, v1 = acc[n][2 * h + 1] + bias1;
             if (MODE == 0) { v0 = fmaxf(v0, 0.0f); v1 = fmaxf(v1, 0.0f); }
-            *reinterpret_cast<__nv_bfloat162*>(yb + ((size_t)gy * W + gx) * a.ys + co) = __floats2bfloat162_rn(v0, v1);
+            *reinterpret_cast<__nv_bfloat162*>(a.y.p + a.y.at(b, (size_t)gy * W + gx, co / 8) + co % 8) =
+                __floats2bfloat162_rn(v0, v1);
         }
     }
 }
@@ -139,6 +138,7 @@ static cudaError_t run_conv(const ConvArgs& a, cudaStream_t s) {
 }
 
 cudaError_t conv3x3(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t s) {
+    if (!view_ok(a.x) || !view_ok(a.y) || ((uintptr_t)a.w & 15)) return cudaErrorInvalidValue;
 #define SGI_CONV_CASE(CI, CO, CKK)                                           \
     if (cin == CI && cout == CO) {                                           \
         if (mode == 0) return run_conv<CI, CO, CKK, 0>(a, s);                \
@@ -188,13 +188,12 @@ __global__ void __launch_bounds__(256) wgrad_kernel(WgradArgs a) {
     const int x0 = (tile % tiles_x) * kTileW, y0 = (tile / tiles_x) * kTileH;
     const int co0 = blockIdx.y * 32, ci0 = blockIdx.z * 32;
     const int H = a.H, W = a.W;
-    const bf16* dzb = a.dz + (size_t)b * H * W * a.dzs;
-    const bf16* xb = a.x + (size_t)b * H * W * a.xs;
     for (int v = tid; v < kTileH * kTileW * 32; v += 256) {
         const int p = v / 32, c = v % 32;
         const int gy = y0 + p / kTileW, gx = x0 + p % kTileW;
         float val = 0.0f;
-        if (gy < H && gx < W && co0 + c < a.cout) val = __bfloat162float(dzb[((size_t)gy * W + gx) * a.dzs + co0 + c]);
+        if (gy < H && gx < W && co0 + c < a.cout)
+            val = __bfloat162float(a.dz.p[a.dz.at(b, (size_t)gy * W + gx, (co0 + c) / 8) + (co0 + c) % 8]);
         sdz[p][c] = val;
     }
     for (int v = tid; v < kHaloH * kHaloW * 32; v += 256) {
@@ -202,7 +201,7 @@ __global__ void __launch_bounds__(256) wgrad_kernel(WgradArgs a) {
         const int gy = y0 + p / kHaloW - 1, gx = x0 + p % kHaloW - 1;
         float val = 0.0f;
         if (gy >= 0 && gy < H && gx >= 0 && gx < W && ci0 + c < a.cin)
-            val = __bfloat162float(xb[((size_t)gy * W + gx) * a.xs + ci0 + c]);
+            val = __bfloat162float(a.x.p[a.x.at(b, (size_t)gy * W + gx, (ci0 + c) / 8) + (ci0 + c) % 8]);
         sx[p][c] = val;
     }
     __syncthreads();
@@ -233,6 +232,7 @@ __global__ void __launch_bounds__(256) wgrad_kernel(WgradArgs a) {
 }
 
 cudaError_t wgrad(const WgradArgs& a, cudaStream_t s) {
+    if (!view_ok(a.x) || !view_ok(a.dz)) return cudaErrorInvalidValue;
     const int tiles = ((a.W + kTileW - 1) / kTileW) * ((a.H + kTileH - 1) / kTileH);
     dim3 grid(tiles * a.B, (a.cout + 31) / 32, (a.cin + 31) / 32);
     wgrad_kernel<<<grid, 256, 0, s>>>(a);
@@ -240,13 +240,16 @@ cudaError_t wgrad(const WgradArgs& a, cudaStream_t s) {
 }
 
 // db[c] += sum over pixels of dz[., c]
-__global__ void bias_grad_kernel(const bf16* __restrict__ dz, int dzs, int c, size_t pixels, float* __restrict__ db) {
+__global__ void bias_grad_kernel(View dz, int c, int B, int HW, float* __restrict__ db) {
     const int ch = threadIdx.x % 32 + blockIdx.y * 32;
     const int row = threadIdx.x / 32;
     float acc = 0.0f;
+    const size_t pixels = (size_t)B * HW;
     if (ch < c)
-        for (size_t p = (size_t)blockIdx.x * 8 + row; p < pixels; p += (size_t)gridDim.x * 8)
-            acc += __bfloat162float(dz[p * dzs + ch]);
+        for (size_t p = (size_t)blockIdx.x * 8 + row; p < pixels; p += (size_t)gridDim.x * 8) {
+            const int b = (int)(p / HW);
+            acc += __bfloat162float(dz.p[dz.at(b, p - (size_t)b * HW, ch / 8) + ch % 8]);
+        }
     __shared__ float red[8][32];
     red[row][threadIdx.x % 32] = acc;
     __syncthreads();
@@ -257,109 +260,164 @@ __global__ void bias_grad_kernel(const bf16* __restrict__ dz, int dzs, int c, si
     }
 }
 
-cudaError_t bias_grad(const bf16* dz, int dzs, int c, size_t pixels, float* db, cudaStream_t s) {
+cudaError_t bias_grad(const View& dz, int c, int B, int H, int W, float* db, cudaStream_t s) {
+    if (!view_ok(dz)) return cudaErrorInvalidValue;
     dim3 grid(256, (c + 31) / 32);
-    bias_grad_kernel<<<grid, 256, 0, s>>>(dz, dzs, c, pixels, db);
+    bias_grad_kernel<<<grid, 256, 0, s>>>(dz, c, B, H * W, db);
     return cudaGetLastError();
 }
 
 // ---------------------------------------------------- elementwise / resampling --
-// dz = dy * (y > 0)
-__global__ void relu_bwd_kernel(const bf16* __restrict__ dy, int dys, const bf16* __restrict__ y, int ys,
-                                bf16* __restrict__ dz, int c, size_t pixels) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= pixels * c) return;
-    const size_t p = i / c;
-    const int ch = (int)(i % c);
-    const float yv = __bfloat162float(y[p * ys + ch]);
-    dz[i] = yv > 0.0f ? dy[p * dys + ch] : __float2bfloat16(0.0f);
+// These kernels move 8 channels (one 16-byte vector) per thread; the thread
+// index runs over (pixel, channel group) with the group fastest.
+__device__ __forceinline__ void bf8_to_f(const uint4& v, float* f) {
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { float2 t = __bfloat1622float2(h[j]); f[2 * j] = t.x; f[2 * j + 1] = t.y; }
+}
+__device__ __forceinline__ uint4 f_to_bf8(const float* f) {
+    uint4 v;
+    __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&v);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(f[2 * j], f[2 * j + 1]);
+    return v;
+}
+__device__ __forceinline__ uint4& vec8(const View& v, int b, size_t q, int g) {
+    return *reinterpret_cast<uint4*>(v.p + v.at(b, q, g));
 }
 
-cudaError_t relu_bwd(const bf16* dy, int dys, const bf16* y, int ys, bf16* dz, int c, size_t pixels, cudaStream_t s) {
-    const size_t n = pixels * c;
-    relu_bwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dy, dys, y, ys, dz, c, pixels);
-    return cudaGetLastError();
+// dz = dy * (y > 0)
+__global__ void relu_bwd_kernel(View dy, View y, View dz, int B, int HW, int g8) {
+    const unsigned n = (unsigned)B * HW * g8;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int g = (int)(i % g8);
+    const unsigned q = i / g8;
+    const int b = (int)(q / HW);
+    const size_t pix = q - (size_t)b * HW;
+    const uint4 yv = vec8(y, b, pix, g), dv = vec8(dy, b, pix, g);
+    const __nv_bfloat162* yh = reinterpret_cast<const __nv_bfloat162*>(&yv);
+    const __nv_bfloat162* dh = reinterpret_cast<const __nv_bfloat162*>(&dv);
+    uint4 o;
+    __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
+    const __nv_bfloat162 zero = __floats2bfloat162_rn(0.0f, 0.0f);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float2 yf = __bfloat1622float2(yh[j]);
+        oh[j] = __halves2bfloat162(yf.x > 0.0f ? dh[j].x : zero.x, yf.y > 0.0f ? dh[j].y : zero.y);
+    }
+    vec8(dz, b, pix, g) = o;
 }
 
 // 2x2 average pooling (H, W even): out[b, y, x] = mean of in[b, 2y.., 2x..]
-__global__ void pool_fwd_kernel(const bf16* __restrict__ in, int is, bf16* __restrict__ out, int os, int B, int H,
-                                int W, int c) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void pool_fwd_kernel(View in, View out, int B, int H, int W, int g8) {
     const int Ho = H / 2, Wo = W / 2;
-    if (i >= (size_t)B * Ho * Wo * c) return;
-    const int ch = (int)(i % c);
-    const size_t q = i / c;
-    const int xo = (int)(q % Wo), yo = (int)((q / Wo) % Ho), b = (int)(q / ((size_t)Wo * Ho));
-    const bf16* base = in + ((size_t)b * H * W) * is;
-    float s = 0.0f;
+    const unsigned n = (unsigned)B * Ho * Wo * g8;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int g = (int)(i % g8);
+    const unsigned q = i / g8;
+    const int xo = (int)(q % Wo), yo = (int)((q / Wo) % Ho), b = (int)(q / ((unsigned)Wo * Ho));
+    float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, f[8];
     for (int dy = 0; dy < 2; ++dy)
-        for (int dx = 0; dx < 2; ++dx)
-            s += __bfloat162float(base[((size_t)(2 * yo + dy) * W + 2 * xo + dx) * is + ch]);
-    out[((size_t)b * Ho * Wo + (size_t)yo * Wo + xo) * os + ch] = __float2bfloat16(0.25f * s);
+        for (int dx = 0; dx < 2; ++dx) {
+            bf8_to_f(vec8(in, b, (size_t)(2 * yo + dy) * W + 2 * xo + dx, g), f);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s[j] += f[j];
+        }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s[j] *= 0.25f;
+    vec8(out, b, (size_t)yo * Wo + xo, g) = f_to_bf8(s);
 }
 
 // din[b, y, x] (+)= 0.25 * dout[b, y/2, x/2]
-__global__ void pool_bwd_kernel(const bf16* __restrict__ dout, int os, bf16* __restrict__ din, int is, int B, int H,
-                                int W, int c, int accumulate) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (size_t)B * H * W * c) return;
-    const int ch = (int)(i % c);
-    const size_t q = i / c;
-    const int x = (int)(q % W), y = (int)((q / W) % H), b = (int)(q / ((size_t)W * H));
-    const int Ho = H / 2, Wo = W / 2;
-    float v = 0.25f * __bfloat162float(dout[((size_t)b * Ho * Wo + (size_t)(y / 2) * Wo + x / 2) * os + ch]);
-    bf16* d = din + ((size_t)b * H * W + (size_t)y * W + x) * is + ch;
-    if (accumulate) v += __bfloat162float(*d);
-    *d = __float2bfloat16(v);
+__global__ void pool_bwd_kernel(View dout, View din, int B, int H, int W, int g8, int accumulate) {
+    const unsigned n = (unsigned)B * H * W * g8;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int g = (int)(i % g8);
+    const unsigned q = i / g8;
+    const int x = (int)(q % W), y = (int)((q / W) % H), b = (int)(q / ((unsigned)W * H));
+    const int Wo = W / 2;
+    float v[8], d[8];
+    bf8_to_f(vec8(dout, b, (size_t)(y / 2) * Wo + x / 2, g), v);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] *= 0.25f;
+    uint4& dp = vec8(din, b, (size_t)y * W + x, g);
+    if (accumulate) {
+        bf8_to_f(dp, d);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] += d[j];
+    }
+    dp = f_to_bf8(v);
 }
 
 // nearest 2x upsampling: out[b, y, x] = in[b, y/2, x/2]
-__global__ void up_fwd_kernel(const bf16* __restrict__ in, int is, bf16* __restrict__ out, int os, int B, int H,
-                              int W, int c) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (size_t)B * H * W * c) return;
-    const int ch = (int)(i % c);
-    const size_t q = i / c;
-    const int x = (int)(q % W), y = (int)((q / W) % H), b = (int)(q / ((size_t)W * H));
-    const int Hi = H / 2, Wi = W / 2;
-    out[((size_t)b * H * W + (size_t)y * W + x) * os + ch] =
-        in[((size_t)b * Hi * Wi + (size_t)(y / 2) * Wi + x / 2) * is + ch];
+__global__ void up_fwd_kernel(View in, View out, int B, int H, int W, int g8) {
+    const unsigned n = (unsigned)B * H * W * g8;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int g = (int)(i % g8);
+    const unsigned q = i / g8;
+    const int x = (int)(q % W), y = (int)((q / W) % H), b = (int)(q / ((unsigned)W * H));
+    vec8(out, b, (size_t)y * W + x, g) = vec8(in, b, (size_t)(y / 2) * (W / 2) + x / 2, g);
 }
 
 // din[b, y, x] = sum of dout over the 2x2 block it was copied to
-__global__ void up_bwd_kernel(const bf16* __restrict__ dout, int os, bf16* __restrict__ din, int is, int B, int Hi,
-                              int Wi, int c) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (size_t)B * Hi * Wi * c) return;
-    const int ch = (int)(i % c);
-    const size_t q = i / c;
-    const int x = (int)(q % Wi), y = (int)((q / Wi) % Hi), b = (int)(q / ((size_t)Wi * Hi));
-    const int H = Hi * 2, W = Wi * 2;
-    float s = 0.0f;
+__global__ void up_bwd_kernel(View dout, View din, int B, int Hi, int Wi, int g8) {
+    const unsigned n = (unsigned)B * Hi * Wi * g8;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int g = (int)(i % g8);
+    const unsigned q = i / g8;
+    const int x = (int)(q % Wi), y = (int)((q / Wi) % Hi), b = (int)(q / ((unsigned)Wi * Hi));
+    const int W = Wi * 2;
+    float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, f[8];
     for (int dy = 0; dy < 2; ++dy)
-        for (int dx = 0; dx < 2; ++dx)
-            s += __bfloat162float(dout[((size_t)b * H * W + (size_t)(2 * y + dy) * W + 2 * x + dx) * os + ch]);
-    din[((size_t)b * Hi * Wi + (size_t)y * Wi + x) * is + ch] = __float2bfloat16(s);
+        for (int dx = 0; dx < 2; ++dx) {
+            bf8_to_f(vec8(dout, b, (size_t)(2 * y + dy) * W + 2 * x + dx, g), f);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s[j] += f[j];
+        }
+    vec8(din, b, (size_t)y * Wi + x, g) = f_to_bf8(s);
 }
 
-cudaError_t pool_fwd(const bf16* in, int is, bf16* out, int os, int B, int H, int W, int c, cudaStream_t s) {
-    const size_t n = (size_t)B * (H / 2) * (W / 2) * c;
-    pool_fwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, is, out, os, B, H, W, c);
+static unsigned blocks_for(size_t n) { return (unsigned)((n + 255) / 256); }
+static bool launch_ok(size_t n, int c) { return c % 8 == 0 && n <= 0xffffff00u; }   // 32-bit thread indices
+
+cudaError_t relu_bwd(const View& dy, const View& y, const View& dz, int c, int B, int H, int W, cudaStream_t s) {
+    const size_t n = (size_t)B * H * W * (c / 8);
+    if (!view_ok(dy) || !view_ok(y) || !view_ok(dz) || !launch_ok(n, c)) return cudaErrorInvalidValue;
+    if (n == 0) return cudaSuccess;
+    relu_bwd_kernel<<<blocks_for(n), 256, 0, s>>>(dy, y, dz, B, H * W, c / 8);
     return cudaGetLastError();
 }
-cudaError_t pool_bwd(const bf16* dout, int os, bf16* din, int is, int B, int H, int W, int c, int acc, cudaStream_t s) {
-    const size_t n = (size_t)B * H * W * c;
-    pool_bwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dout, os, din, is, B, H, W, c, acc);
+cudaError_t pool_fwd(const View& in, const View& out, int B, int H, int W, int c, cudaStream_t s) {
+    const size_t n = (size_t)B * (H / 2) * (W / 2) * (c / 8);
+    if (!view_ok(in) || !view_ok(out) || !launch_ok(n, c)) return cudaErrorInvalidValue;
+    if (n == 0) return cudaSuccess;
+    pool_fwd_kernel<<<blocks_for(n), 256, 0, s>>>(in, out, B, H, W, c / 8);
     return cudaGetLastError();
 }
-cudaError_t up_fwd(const bf16* in, int is, bf16* out, int os, int B, int H, int W, int c, cudaStream_t s) {
-    const size_t n = (size_t)B * H * W * c;
-    up_fwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, is, out, os, B, H, W, c);
+cudaError_t pool_bwd(const View& dout, const View& din, int B, int H, int W, int c, int acc, cudaStream_t s) {
+    const size_t n = (size_t)B * H * W * (c / 8);
+    if (!view_ok(dout) || !view_ok(din) || !launch_ok(n, c)) return cudaErrorInvalidValue;
+    if (n == 0) return cudaSuccess;
+    pool_bwd_kernel<<<blocks_for(n), 256, 0, s>>>(dout, din, B, H, W, c / 8, acc);
     return cudaGetLastError();
 }
-cudaError_t up_bwd(const bf16* dout, int os, bf16* din, int is, int B, int Hi, int Wi, int c, cudaStream_t s) {
-    const size_t n = (size_t)B * Hi * Wi * c;
-    up_bwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dout, os, din, is, B, Hi, Wi, c);
+cudaError_t up_fwd(const View& in, const View& out, int B, int H, int W, int c, cudaStream_t s) {
+    const size_t n = (size_t)B * H * W * (c / 8);
+    if (!view_ok(in) || !view_ok(out) || !launch_ok(n, c)) return cudaErrorInvalidValue;
+    if (n == 0) return cudaSuccess;
+    up_fwd_kernel<<<blocks_for(n), 256, 0, s>>>(in, out, B, H, W, c / 8);
+    return cudaGetLastError();
+}
+cudaError_t up_bwd(const View& dout, const View& din, int B, int Hi, int Wi, int c, cudaStream_t s) {
+    const size_t n = (size_t)B * Hi * Wi * (c / 8);
+    if (!view_ok(dout) || !view_ok(din) || !launch_ok(n, c)) return cudaErrorInvalidValue;
+    if (n == 0) return cudaSuccess;
+    up_bwd_kernel<<<blocks_for(n), 256, 0, s>>>(dout, din, B, Hi, Wi, c / 8);
     return cudaGetLastError();
 }
 
@@ -368,33 +426,44 @@ cudaError_t up_bwd(const bf16* dout, int os, bf16* din, int is, int B, int Hi, i
 // [B, H, W, 4] float (rgb used). out = a * sum_k softmax(l)_k noisy(p + o_k) + (1 - a) * prev,
 // a = sigmoid(l25); neighbours clamped to the image. With a target, also the
 // loss sum of |log1p(out) - log1p(target)| and dlogits = d(mean loss)/dlogits.
+constexpr int kApplyTX = 32, kApplyTY = 8;
 __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t P = (size_t)a.B * a.H * a.W;
+    // the block's 32 x 8 pixels of `noisy` with a 2-pixel edge-clamped border
+    __shared__ float4 tile[kApplyTY + 4][kApplyTX + 4];
+    __shared__ float red[8];
+    const int tx = threadIdx.x % kApplyTX, ty = threadIdx.x / kApplyTX;
+    const int x0 = blockIdx.x * kApplyTX, y0 = blockIdx.y * kApplyTY, b = blockIdx.z;
+    const int H = a.H, W = a.W;
+    const float4* nz = a.noisy + (size_t)b * H * W;
+    for (int v = threadIdx.x; v < (kApplyTY + 4) * (kApplyTX + 4); v += 256) {
+        const int hy = v / (kApplyTX + 4), hx = v % (kApplyTX + 4);
+        const int yy = min(max(y0 + hy - 2, 0), H - 1), xx = min(max(x0 + hx - 2, 0), W - 1);
+        tile[hy][hx] = nz[(size_t)yy * W + xx];
+    }
+    __syncthreads();
+    const int x = x0 + tx, y = y0 + ty;
     float loss = 0.0f;
-    if (i < P) {
-        const int x = (int)(i % a.W), y = (int)((i / a.W) % a.H);
-        const size_t img = i / ((size_t)a.W * a.H);
-        const bf16* lg = a.logits + i * 32;
+    if (x < W && y < H) {
+        const size_t q = (size_t)y * W + x, i = (size_t)b * H * W + q;
+        float lf[32];
+#pragma unroll
+        for (int g = 0; g < 4; ++g) bf8_to_f(vec8(a.logits, b, q, g), lf + 8 * g);
         float l[25];
         float mx = -3.0e38f;
 #pragma unroll
-        for (int k = 0; k < 25; ++k) { l[k] = __bfloat162float(lg[k]); mx = fmaxf(mx, l[k]); }
+        for (int k = 0; k < 25; ++k) { l[k] = lf[k]; mx = fmaxf(mx, l[k]); }
         float den = 0.0f;
 #pragma unroll
         for (int k = 0; k < 25; ++k) { l[k] = __expf(l[k] - mx); den += l[k]; }
         const float inv = 1.0f / den;
         float sp[3] = {0.0f, 0.0f, 0.0f};
-        float nb[25][3];
 #pragma unroll
         for (int k = 0; k < 25; ++k) {
             l[k] *= inv;
-            const int xx = min(max(x + k % 5 - 2, 0), a.W - 1), yy = min(max(y + k / 5 - 2, 0), a.H - 1);
-            const float4 nv = a.noisy[(img * a.H + yy) * a.W + xx];
-            nb[k][0] = nv.x; nb[k][1] = nv.y; nb[k][2] = nv.z;
+            const float4 nv = tile[ty + k / 5][tx + k % 5];
             sp[0] = fmaf(l[k], nv.x, sp[0]); sp[1] = fmaf(l[k], nv.y, sp[1]); sp[2] = fmaf(l[k], nv.z, sp[2]);
         }
-        const float alpha = 1.0f / (1.0f + __expf(-__bfloat162float(lg[25])));
+        const float alpha = 1.0f / (1.0f + __expf(-lf[25]));
         const float4 pv = a.prev[i];
         const float pr[3] = {pv.x, pv.y, pv.z};
         float o[3];
@@ -420,33 +489,39 @@ __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
             float dot_wdw = 0.0f;
 #pragma unroll
             for (int k = 0; k < 25; ++k) {
-                dw[k] = alpha * (dout[0] * nb[k][0] + dout[1] * nb[k][1] + dout[2] * nb[k][2]);
+                const float4 nv = tile[ty + k / 5][tx + k % 5];
+                dw[k] = alpha * (dout[0] * nv.x + dout[1] * nv.y + dout[2] * nv.z);
                 dot_wdw += l[k] * dw[k];
             }
-            bf16* dl = a.dlogits + i * 32;
+            float dl[32];
 #pragma unroll
-            for (int k = 0; k < 25; ++k) dl[k] = __float2bfloat16(l[k] * (dw[k] - dot_wdw));
-            dl[25] = __float2bfloat16(dalpha * alpha * (1.0f - alpha));
+            for (int k = 0; k < 25; ++k) dl[k] = l[k] * (dw[k] - dot_wdw);
+            dl[25] = dalpha * alpha * (1.0f - alpha);
 #pragma unroll
-            for (int k = 26; k < 32; ++k) dl[k] = __float2bfloat16(0.0f);
+            for (int k = 26; k < 32; ++k) dl[k] = 0.0f;
+#pragma unroll
+            for (int g = 0; g < 4; ++g) vec8(a.dlogits, b, q, g) = f_to_bf8(dl + 8 * g);
         }
     }
     if (a.loss) {
-        // block reduction of the loss
-        __shared__ float red[256];
-        red[threadIdx.x] = loss;
+        // block reduction of the loss: warp butterfly, then the 8 warp sums
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = loss;
         __syncthreads();
-        for (int s = 128; s > 0; s >>= 1) {
-            if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-            __syncthreads();
+        if (threadIdx.x == 0) {
+            float t = 0.0f;
+            for (int w = 0; w < 8; ++w) t += red[w];
+            atomicAdd(a.loss, t);
         }
-        if (threadIdx.x == 0) atomicAdd(a.loss, red[0]);
     }
 }
 
 cudaError_t kpcn_apply(const ApplyArgs& a, cudaStream_t s) {
-    const size_t P = (size_t)a.B * a.H * a.W;
-    kpcn_apply_kernel<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(a);
+    if (!view_ok(a.logits) || (a.target && !view_ok(a.dlogits))) return cudaErrorInvalidValue;
+    if (a.B < 1 || a.H < 1 || a.W < 1 || a.B > 65535) return cudaErrorInvalidValue;
+    dim3 grid((a.W + kApplyTX - 1) / kApplyTX, (a.H + kApplyTY - 1) / kApplyTY, a.B);
+    kpcn_apply_kernel<<<grid, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -95,6 +95,9 @@ cudaError_t Net::init(const sgi_nn_config& c) {
     chk(alloc(&GQ2, P4 * 128));
     chk(alloc(&GQ3, P4 * 64));
     chk(alloc(&fwd_out, P));
+    chk(alloc(&dev_err, 1));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(dev_err, 0, sizeof(int));
     if (e != cudaSuccess) return e;
     // He-normal weights, zero biases; the head starts near a box filter + half blend.
     std::vector<float> h(nparams, 0.0f);
@@ -120,56 +123,68 @@ cudaError_t Net::set_params(const float* host, size_t n) {
     return e;
 }
 
-cudaError_t Net::conv(int l, const bf16* x, int xs, bf16* y, int ys, int B, int H, int W, cudaStream_t s) {
-    ConvArgs a{x, xs, wbf + w_off[l], w32 + b_off[l], y, ys, B, H, W};
-    return conv3x3(kCin[l], kCout[l], l == HEAD ? 1 : 0, a, s);
+cudaError_t Net::conv_any(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t s) {
+    return conv_path == SGI_NN_CONV_TCGEN05 ? conv3x3_tc(cin, cout, mode, a, dev_err, s) : conv3x3(cin, cout, mode, a, s);
 }
 
+cudaError_t Net::conv(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s) {
+    ConvArgs a{x, wbf + w_off[l], w32 + b_off[l], y, B, H, W};
+    return conv_any(kCin[l], kCout[l], l == HEAD ? 1 : 0, a, s);
+}
+
+// Activations and gradients are channel-group planar ([B][C/8][H][W][8]); the
+// input features are NHWC [B][H][W][16].
 cudaError_t Net::forward(const bf16* feat, int B, int H, int W, cudaStream_t s) {
     const int H2 = H / 2, W2 = W / 2, H4 = H / 4, W4 = W / 4;
     cudaError_t e;
 #define NN_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
-    NN_TRY(conv(E1A, feat, 16, E1A_, 32, B, H, W, s));
-    NN_TRY(conv(E1B, E1A_, 32, D1IN + 64, 96, B, H, W, s));
-    NN_TRY(pool_fwd(D1IN + 64, 96, P1, 32, B, H, W, 32, s));
-    NN_TRY(conv(E2A, P1, 32, E2A_, 64, B, H2, W2, s));
-    NN_TRY(conv(E2B, E2A_, 64, D2IN + 128, 192, B, H2, W2, s));
-    NN_TRY(pool_fwd(D2IN + 128, 192, P2_, 64, B, H2, W2, 64, s));
-    NN_TRY(conv(B1, P2_, 64, B1_, 128, B, H4, W4, s));
-    NN_TRY(conv(B2, B1_, 128, B2_, 128, B, H4, W4, s));
-    NN_TRY(up_fwd(B2_, 128, D2IN, 192, B, H2, W2, 128, s));
-    NN_TRY(conv(D2A, D2IN, 192, D2A_, 64, B, H2, W2, s));
-    NN_TRY(conv(D2B, D2A_, 64, D2B_, 64, B, H2, W2, s));
-    NN_TRY(up_fwd(D2B_, 64, D1IN, 96, B, H, W, 64, s));
-    NN_TRY(conv(D1A, D1IN, 96, D1A_, 32, B, H, W, s));
-    NN_TRY(conv(D1B, D1A_, 32, D1B_, 32, B, H, W, s));
-    NN_TRY(conv(HEAD, D1B_, 32, LOG, 32, B, H, W, s));
+    const View f = nhwc_view(feat, 16, H, W);
+    const View e1a = planar_view(E1A_, 4, H, W), d1in = planar_view(D1IN, 12, H, W);
+    const View p1 = planar_view(P1, 4, H2, W2), e2a = planar_view(E2A_, 8, H2, W2);
+    const View d2in = planar_view(D2IN, 24, H2, W2), p2 = planar_view(P2_, 8, H4, W4);
+    const View b1 = planar_view(B1_, 16, H4, W4), b2 = planar_view(B2_, 16, H4, W4);
+    const View d2a = planar_view(D2A_, 8, H2, W2), d2b = planar_view(D2B_, 8, H2, W2);
+    const View d1a = planar_view(D1A_, 4, H, W), d1b = planar_view(D1B_, 4, H, W), lg = planar_view(LOG, 4, H, W);
+    NN_TRY(conv(E1A, f, e1a, B, H, W, s));
+    NN_TRY(conv(E1B, e1a, channel_slice(d1in, 64), B, H, W, s));
+    NN_TRY(pool_fwd(channel_slice(d1in, 64), p1, B, H, W, 32, s));
+    NN_TRY(conv(E2A, p1, e2a, B, H2, W2, s));
+    NN_TRY(conv(E2B, e2a, channel_slice(d2in, 128), B, H2, W2, s));
+    NN_TRY(pool_fwd(channel_slice(d2in, 128), p2, B, H2, W2, 64, s));
+    NN_TRY(conv(B1, p2, b1, B, H4, W4, s));
+    NN_TRY(conv(B2, b1, b2, B, H4, W4, s));
+    NN_TRY(up_fwd(b2, d2in, B, H2, W2, 128, s));
+    NN_TRY(conv(D2A, d2in, d2a, B, H2, W2, s));
+    NN_TRY(conv(D2B, d2a, d2b, B, H2, W2, s));
+    NN_TRY(up_fwd(d2b, d1in, B, H, W, 64, s));
+    NN_TRY(conv(D1A, d1in, d1a, B, H, W, s));
+    NN_TRY(conv(D1B, d1a, d1b, B, H, W, s));
+    NN_TRY(conv(HEAD, d1b, lg, B, H, W, s));
     launches += 15;
     return cudaSuccess;
 }
 
-// Backward of layer l: dz = relu'(dy) (or dy for the head), weight / bias
-// gradients from its input x, and (if dx) the input gradient.
-cudaError_t Net::layer_backward(int l, const bf16* x, int xs, const bf16* y, int ys, const bf16* dy, int dys, bf16* dz,
-                                bf16* dx, int dxs, int B, int H, int W, cudaStream_t s) {
+// Backward of layer l: dz = relu'(dy) (or dy for the head) into the planar
+// buffer dz_buf, weight / bias gradients from its input x, and (if dx.p) the
+// input gradient.
+cudaError_t Net::layer_backward(int l, const View& x, const View& y, const View& dy, bf16* dz_buf, const View& dx,
+                                int B, int H, int W, cudaStream_t s) {
     cudaError_t e;
-    const size_t pix = (size_t)B * H * W;
-    const bf16* g = dy;
-    int gs = dys;
+    View g = dy;
     if (l != HEAD) {
-        NN_TRY(relu_bwd(dy, dys, y, ys, dz, kCout[l], pix, s));
+        const View dz = planar_view(dz_buf, kCout[l] / 8, H, W);
+        NN_TRY(relu_bwd(dy, y, dz, kCout[l], B, H, W, s));
         g = dz;
-        gs = kCout[l];
         launches += 1;
     }
-    WgradArgs wa{x, xs, g, gs, g32 + w_off[l], kCin[l], kCout[l], B, H, W};
+    WgradArgs wa{x, g, g32 + w_off[l], kCin[l], kCout[l], B, H, W};
     NN_TRY(wgrad(wa, s));
-    NN_TRY(bias_grad(g, gs, kCout[l], pix, g32 + b_off[l], s));
+    NN_TRY(bias_grad(g, kCout[l], B, H, W, g32 + b_off[l], s));
     launches += 2;
-    if (dx) {
+    if (dx.p) {
         NN_TRY(flip_weights(wbf + w_off[l], wflip + w_off[l], kCin[l], kCout[l], s));
-        ConvArgs a{g, gs, wflip + w_off[l], nullptr, dx, dxs, B, H, W};
-        NN_TRY(conv3x3(kCout[l], kCin[l], 2, a, s));
+        ConvArgs a{g, wflip + w_off[l], nullptr, dx, B, H, W};
+        NN_TRY(conv_any(kCout[l], kCin[l], 2, a, s));
         launches += 2;
     }
     return cudaSuccess;
@@ -178,23 +193,31 @@ cudaError_t Net::layer_backward(int l, const bf16* x, int xs, const bf16* y, int
 cudaError_t Net::backward(const bf16* feat, int B, int H, int W, cudaStream_t s) {
     const int H2 = H / 2, W2 = W / 2, H4 = H / 4, W4 = W / 4;
     cudaError_t e;
+    auto full = [&](bf16* p, int c) { return planar_view(p, c / 8, H, W); };
+    auto half = [&](bf16* p, int c) { return planar_view(p, c / 8, H2, W2); };
+    auto quarter = [&](bf16* p, int c) { return planar_view(p, c / 8, H4, W4); };
+    const View none{nullptr, 8, 8, 8};
     NN_TRY(cudaMemsetAsync(g32, 0, nparams * sizeof(float), s));
     // full resolution decoder: dLOGITS in GA
-    NN_TRY(layer_backward(HEAD, D1B_, 32, LOG, 32, GA, 32, nullptr, GB, 32, B, H, W, s));      // dD1B -> GB
-    NN_TRY(layer_backward(D1B, D1A_, 32, D1B_, 32, GB, 32, GC, GA, 32, B, H, W, s));          // dD1A -> GA
-    NN_TRY(layer_backward(D1A, D1IN, 96, D1A_, 32, GA, 32, GB, GD, 96, B, H, W, s));          // dD1IN -> GD
-    NN_TRY(up_bwd(GD, 96, GH1, 64, B, H2, W2, 64, s));                                          // dD2B -> GH1
-    NN_TRY(layer_backward(D2B, D2A_, 64, D2B_, 64, GH1, 64, GH2, GH1, 64, B, H2, W2, s));        // dD2A -> GH1
-    NN_TRY(layer_backward(D2A, D2IN, 192, D2A_, 64, GH1, 64, GH2, GH3, 192, B, H2, W2, s));      // dD2IN -> GH3
-    NN_TRY(up_bwd(GH3, 192, GQ1, 128, B, H4, W4, 128, s));                                       // dB2 -> GQ1
-    NN_TRY(layer_backward(B2, B1_, 128, B2_, 128, GQ1, 128, GQ2, GQ1, 128, B, H4, W4, s));       // dB1 -> GQ1
-    NN_TRY(layer_backward(B1, P2_, 64, B1_, 128, GQ1, 128, GQ2, GQ3, 64, B, H4, W4, s));         // dP2 -> GQ3
-    NN_TRY(pool_bwd(GQ3, 64, GH3 + 128, 192, B, H2, W2, 64, 1, s));                              // skip 2
-    NN_TRY(layer_backward(E2B, E2A_, 64, D2IN + 128, 192, GH3 + 128, 192, GH2, GH1, 64, B, H2, W2, s));  // dE2A -> GH1
-    NN_TRY(layer_backward(E2A, P1, 32, E2A_, 64, GH1, 64, GH2, GH1, 32, B, H2, W2, s));          // dP1 -> GH1 (32 ch)
-    NN_TRY(pool_bwd(GH1, 32, GD + 64, 96, B, H, W, 32, 1, s));                                  // skip 1
-    NN_TRY(layer_backward(E1B, E1A_, 32, D1IN + 64, 96, GD + 64, 96, GC, GA, 32, B, H, W, s));  // dE1A -> GA
-    NN_TRY(layer_backward(E1A, feat, 16, E1A_, 32, GA, 32, GB, nullptr, 0, B, H, W, s));
+    NN_TRY(layer_backward(HEAD, full(D1B_, 32), full(LOG, 32), full(GA, 32), nullptr, full(GB, 32), B, H, W, s));
+    NN_TRY(layer_backward(D1B, full(D1A_, 32), full(D1B_, 32), full(GB, 32), GC, full(GA, 32), B, H, W, s));
+    NN_TRY(layer_backward(D1A, full(D1IN, 96), full(D1A_, 32), full(GA, 32), GB, full(GD, 96), B, H, W, s));
+    NN_TRY(up_bwd(full(GD, 96), half(GH1, 64), B, H2, W2, 64, s));                          // dD2B
+    NN_TRY(layer_backward(D2B, half(D2A_, 64), half(D2B_, 64), half(GH1, 64), GH2, half(GH1, 64), B, H2, W2, s));
+    NN_TRY(layer_backward(D2A, half(D2IN, 192), half(D2A_, 64), half(GH1, 64), GH2, half(GH3, 192), B, H2, W2, s));
+    NN_TRY(up_bwd(half(GH3, 192), quarter(GQ1, 128), B, H4, W4, 128, s));                  // dB2
+    NN_TRY(layer_backward(B2, quarter(B1_, 128), quarter(B2_, 128), quarter(GQ1, 128), GQ2, quarter(GQ1, 128), B, H4,
+                          W4, s));
+    NN_TRY(layer_backward(B1, quarter(P2_, 64), quarter(B1_, 128), quarter(GQ1, 128), GQ2, quarter(GQ3, 64), B, H4,
+                          W4, s));                                                                // dP2
+    NN_TRY(pool_bwd(quarter(GQ3, 64), channel_slice(half(GH3, 192), 128), B, H2, W2, 64, 1, s));   // skip 2
+    NN_TRY(layer_backward(E2B, half(E2A_, 64), channel_slice(half(D2IN, 192), 128), channel_slice(half(GH3, 192), 128),
+                          GH2, half(GH1, 64), B, H2, W2, s));                                     // dE2A
+    NN_TRY(layer_backward(E2A, half(P1, 32), half(E2A_, 64), half(GH1, 64), GH2, half(GH1, 32), B, H2, W2, s));  // dP1
+    NN_TRY(pool_bwd(half(GH1, 32), channel_slice(full(GD, 96), 64), B, H, W, 32, 1, s));         // skip 1
+    NN_TRY(layer_backward(E1B, full(E1A_, 32), channel_slice(full(D1IN, 96), 64), channel_slice(full(GD, 96), 64), GC,
+                          full(GA, 32), B, H, W, s));                                             // dE1A
+    NN_TRY(layer_backward(E1A, nhwc_view(feat, 16, H, W), full(E1A_, 32), full(GA, 32), GB, none, B, H, W, s));
     launches += 5;
     return cudaSuccess;
 }
@@ -275,8 +298,9 @@ sgi_status sgi_nn_forward(sgi_nn* n, const void* features, const float* noisy, c
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = n->net.forward((const __nv_bfloat16*)features, B, H, W, s);
     if (e != cudaSuccess) return nn_cuda(n, e, "forward");
-    sgi::nn::ApplyArgs a{n->net.LOG, (const float4*)noisy, (const float4*)prev, nullptr, (float4*)out, nullptr, nullptr,
-                         0.0f, B, H, W};
+    const sgi::nn::View none{nullptr, 8, 8, 8};
+    sgi::nn::ApplyArgs a{sgi::nn::planar_view(n->net.LOG, 4, H, W), (const float4*)noisy, (const float4*)prev, nullptr,
+                         (float4*)out, none, nullptr, 0.0f, B, H, W};
     e = sgi::nn::kpcn_apply(a, s);
     n->net.launches += 1;
     return e == cudaSuccess ? SGI_OK : nn_cuda(n, e, "apply");
@@ -294,8 +318,9 @@ sgi_status sgi_nn_train_step(sgi_nn* n, const void* features, const float* noisy
     e = cudaMemsetAsync(net.loss_dev, 0, sizeof(float), s);
     if (e != cudaSuccess) return nn_cuda(n, e, "loss reset");
     const size_t P = (size_t)B * H * W;
-    sgi::nn::ApplyArgs a{net.LOG, (const float4*)noisy, (const float4*)prev, (const float4*)target, nullptr, net.GA,
-                         net.loss_dev, 1.0f / (3.0f * (float)P), B, H, W};
+    sgi::nn::ApplyArgs a{sgi::nn::planar_view(net.LOG, 4, H, W), (const float4*)noisy, (const float4*)prev,
+                         (const float4*)target, nullptr, sgi::nn::planar_view(net.GA, 4, H, W), net.loss_dev,
+                         1.0f / (3.0f * (float)P), B, H, W};
     e = sgi::nn::kpcn_apply(a, s);
     if (e != cudaSuccess) return nn_cuda(n, e, "apply/loss");
     e = net.backward((const __nv_bfloat16*)features, B, H, W, s);
@@ -308,12 +333,53 @@ sgi_status sgi_nn_train_step(sgi_nn* n, const void* features, const float* noisy
     net.launches += 3;
     if (loss_host) {
         float l = 0.0f;
+        int flag = 0;
         e = cudaMemcpyAsync(&l, net.loss_dev, sizeof(float), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, net.dev_err, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return nn_cuda(n, e, "loss readback");
+        if (flag) return nn_fail(n, SGI_ERR_TIMEOUT, "a tensor-core convolution wait ran out");
         *loss_host = l / (3.0f * (float)P);
     }
     return SGI_OK;
+}
+
+sgi_status sgi_nn_set_conv_path(sgi_nn* n, int32_t path) {
+    if (!n || (path != SGI_NN_CONV_WARP_MMA && path != SGI_NN_CONV_TCGEN05)) return SGI_ERR_ARG;
+    n->net.conv_path = path;
+    return SGI_OK;
+}
+
+sgi_status sgi_nn_device_status(sgi_nn* n) {
+    if (!n) return SGI_ERR_ARG;
+    int flag = 0;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&flag, n->net.dev_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && flag) e = cudaMemset(n->net.dev_err, 0, sizeof(int));
+    if (e != cudaSuccess) return nn_cuda(n, e, "device status");
+    return flag ? nn_fail(n, SGI_ERR_TIMEOUT, "a tensor-core convolution wait ran out") : SGI_OK;
+}
+
+sgi_status sgi_nn_conv3x3(int32_t path, int32_t cin, int32_t cout, int32_t mode, const void* x, int32_t x_stride,
+                          const void* w, const float* bias, void* y, int32_t y_stride, int32_t batch, int32_t height,
+                          int32_t width, int32_t* err_flag, void* stream) {
+    if (!x || !w || !y || (mode != 2 && !bias) || mode < 0 || mode > 2) return SGI_ERR_ARG;
+    if (batch < 1 || height < 1 || width < 1 || x_stride < cin || y_stride < cout) return SGI_ERR_ARG;
+    if ((x_stride % 8) || (y_stride % 8) || ((uintptr_t)x & 15) || ((uintptr_t)y & 15) || ((uintptr_t)w & 15))
+        return SGI_ERR_ARG;
+    sgi::nn::ConvArgs a{sgi::nn::nhwc_view(x, x_stride, height, width), (const __nv_bfloat16*)w, bias,
+                        sgi::nn::nhwc_view(y, y_stride, height, width), batch, height, width};
+    cudaError_t e;
+    if (path == SGI_NN_CONV_TCGEN05) {
+        if (!err_flag) return SGI_ERR_ARG;
+        e = sgi::nn::conv3x3_tc(cin, cout, mode, a, err_flag, (cudaStream_t)stream);
+    } else if (path == SGI_NN_CONV_WARP_MMA) {
+        e = sgi::nn::conv3x3(cin, cout, mode, a, (cudaStream_t)stream);
+    } else {
+        return SGI_ERR_ARG;
+    }
+    if (e == cudaErrorInvalidValue) return SGI_ERR_ARG;
+    return e == cudaSuccess ? SGI_OK : SGI_ERR_CUDA;
 }
 
 }  // extern "C"

@@ -9,34 +9,60 @@
 namespace sgi {
 namespace nn {
 
-// NHWC tensor views: pointer at channel 0 of pixel 0, `*s` = channel stride per pixel.
+// A BF16 activation tensor [B][H][W][C] seen through element strides: element
+// (image b, pixel q = y * W + x, channel c) is at
+//   p[b * img + q * pix + (c / 8) * grp + c % 8].
+// Kernels move 8 channels (16 bytes) at a time, so p is 16-byte aligned and the
+// strides are multiples of 8. Two layouts are used:
+//   NHWC with channel stride cs: pix = cs, grp = 8, img = H * W * cs;
+//   channel-group planar [B][G][H][W][8]: pix = 8, grp = H * W * 8, img = G * H * W * 8,
+// where each 8-channel group of an image row is one contiguous run of W * 16
+// bytes (the layout the tensor-core convolution's TMA loads fetch best).
+// A channel slice (skip connections write into the decoder inputs) is the same
+// view with p advanced by c0 / 8 groups.
+struct View {
+    __nv_bfloat16* p;
+    long long pix, grp, img;
+    __host__ __device__ size_t at(int b, size_t q, int g) const {
+        return (size_t)b * (size_t)img + q * (size_t)pix + (size_t)g * (size_t)grp;
+    }
+};
+
+inline View nhwc_view(const void* p, int cs, int H, int W) {
+    return View{(__nv_bfloat16*)p, cs, 8, (long long)H * W * cs};
+}
+inline View planar_view(const void* p, int groups, int H, int W) {
+    return View{(__nv_bfloat16*)p, 8, (long long)H * W * 8, (long long)groups * H * W * 8};
+}
+inline View channel_slice(View v, int c0) { v.p += (size_t)(c0 / 8) * (size_t)v.grp; return v; }
+inline bool view_ok(const View& v) {
+    return v.p && ((uintptr_t)v.p & 15) == 0 && v.pix % 8 == 0 && v.grp % 8 == 0 && v.img % 8 == 0 && v.pix > 0 &&
+           v.grp > 0 && v.img > 0;
+}
+
 struct ConvArgs {
-    const __nv_bfloat16* x;
-    int xs;
+    View x;
     const __nv_bfloat16* w;   // [cout][9][cin] (dgrad: flipped [cin][9][cout])
     const float* bias;        // [cout], unused in mode 2
-    __nv_bfloat16* y;
-    int ys;
+    View y;
     int B, H, W;
 };
 
 struct WgradArgs {
-    const __nv_bfloat16* x;
-    int xs;
-    const __nv_bfloat16* dz;
-    int dzs;
+    View x;
+    View dz;
     float* dw;                // [cout][9][cin], accumulated
     int cin, cout;
     int B, H, W;
 };
 
 struct ApplyArgs {
-    const __nv_bfloat16* logits;  // [P][32]
+    View logits;                  // 32 channels
     const float4* noisy;          // [P]
     const float4* prev;           // [P]
     const float4* target;         // [P] or null (inference)
     float4* out;                  // [P] or null
-    __nv_bfloat16* dlogits;       // [P][32] when target
+    View dlogits;                 // 32 channels, when target
     float* loss;                  // sum of |log1p(out) - log1p(target)| (device scalar) or null
     float grad_scale;             // 1 / (3 * pixels)
     int B, H, W;
@@ -62,19 +88,22 @@ cudaError_t features(const FeatureArgs& a, cudaStream_t s);
 cudaError_t composite(const float4* den, const uint2* screen, const uint32_t* albedo, uint2* hdr, uint2* gi_out,
                       uint16_t* hist_out, size_t P, cudaStream_t s);
 cudaError_t conv3x3(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t s);
+// The same convolution on the 5th-generation tensor cores (sgi_nn_tc.cu); *err is
+// set to 1 when a bounded wait of a block ran out.
+cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err, cudaStream_t s);
 cudaError_t flip_weights(const __nv_bfloat16* w, __nv_bfloat16* wt, int cin, int cout, cudaStream_t s);
 cudaError_t wgrad(const WgradArgs& a, cudaStream_t s);
-cudaError_t bias_grad(const __nv_bfloat16* dz, int dzs, int c, size_t pixels, float* db, cudaStream_t s);
-cudaError_t relu_bwd(const __nv_bfloat16* dy, int dys, const __nv_bfloat16* y, int ys, __nv_bfloat16* dz, int c,
-                     size_t pixels, cudaStream_t s);
-cudaError_t pool_fwd(const __nv_bfloat16* in, int is, __nv_bfloat16* out, int os, int B, int H, int W, int c,
-                     cudaStream_t s);
-cudaError_t pool_bwd(const __nv_bfloat16* dout, int os, __nv_bfloat16* din, int is, int B, int H, int W, int c,
-                     int accumulate, cudaStream_t s);
-cudaError_t up_fwd(const __nv_bfloat16* in, int is, __nv_bfloat16* out, int os, int B, int H, int W, int c,
-                   cudaStream_t s);
-cudaError_t up_bwd(const __nv_bfloat16* dout, int os, __nv_bfloat16* din, int is, int B, int Hi, int Wi, int c,
-                   cudaStream_t s);
+cudaError_t bias_grad(const View& dz, int c, int B, int H, int W, float* db, cudaStream_t s);
+// dz = dy * (y > 0)
+cudaError_t relu_bwd(const View& dy, const View& y, const View& dz, int c, int B, int H, int W, cudaStream_t s);
+// 2x2 mean pooling of an H x W input
+cudaError_t pool_fwd(const View& in, const View& out, int B, int H, int W, int c, cudaStream_t s);
+// din (H x W) (+)= 0.25 * dout upsampled
+cudaError_t pool_bwd(const View& dout, const View& din, int B, int H, int W, int c, int accumulate, cudaStream_t s);
+// nearest 2x upsampling to H x W
+cudaError_t up_fwd(const View& in, const View& out, int B, int H, int W, int c, cudaStream_t s);
+// din (Hi x Wi) = sum of dout over each 2x2 block
+cudaError_t up_bwd(const View& dout, const View& din, int B, int Hi, int Wi, int c, cudaStream_t s);
 cudaError_t kpcn_apply(const ApplyArgs& a, cudaStream_t s);
 cudaError_t adam(float* w, const float* g, float* m, float* v, __nv_bfloat16* wb, size_t n, float lr, float b1,
                  float b2, float eps, int step, cudaStream_t s);

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/sgi_nn.h"
+#include "sgi_nn_internal.h"
 
 namespace sgi {
 namespace nn {
@@ -31,18 +32,19 @@ struct Net {
     __nv_bfloat16 *GA = nullptr, *GB = nullptr, *GC = nullptr, *GD = nullptr, *GH1 = nullptr, *GH2 = nullptr,
                   *GH3 = nullptr, *GQ1 = nullptr, *GQ2 = nullptr, *GQ3 = nullptr;
     float4* fwd_out = nullptr;
+    int* dev_err = nullptr;   // set by a tcgen05 convolution whose wait ran out
+    int conv_path = SGI_NN_CONV_TCGEN05;
 
     ~Net();
     void release();
     template <class T> cudaError_t alloc(T** p, size_t n);
     cudaError_t init(const sgi_nn_config& c);
     cudaError_t set_params(const float* host, size_t n);
-    cudaError_t conv(int l, const __nv_bfloat16* x, int xs, __nv_bfloat16* y, int ys, int B, int H, int W,
-                     cudaStream_t s);
+    cudaError_t conv_any(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t s);
+    cudaError_t conv(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s);
     cudaError_t forward(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);
-    cudaError_t layer_backward(int l, const __nv_bfloat16* x, int xs, const __nv_bfloat16* y, int ys,
-                               const __nv_bfloat16* dy, int dys, __nv_bfloat16* dz, __nv_bfloat16* dx, int dxs, int B,
-                               int H, int W, cudaStream_t s);
+    cudaError_t layer_backward(int l, const View& x, const View& y, const View& dy, __nv_bfloat16* dz_buf,
+                               const View& dx, int B, int H, int W, cudaStream_t s);
     cudaError_t backward(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);
 };
 

@@ -1,0 +1,429 @@
+// sgi_nn_tc.cu - 3x3 convolutions of the learned denoiser on the 5th-generation
+// tensor cores: a persistent, warp-specialised implicit GEMM with TMA loads,
+// an mbarrier ring and double-buffered TMEM accumulators.
+//
+// Tile: R consecutive rows x 128 consecutive pixels of one image, all COUT
+// output channels. Output row r of the tile is one tcgen05.mma accumulator
+// D_r[m][n] (M = 128 pixels, N = COUT) = sum over 16-channel chunks, taps t and
+// channels k of A_{r,t}[m][k] * B_t[n][k], where A_{r,t}[m][k] is input pixel
+// (y0 + r + ky - 1, x0 + m + kx - 1), channel k (zero outside the image) and
+// B_t[n][k] = w[n][t][k].
+//
+// Shared memory holds STAGES chunk buffers, each filled by two TMA loads:
+//   halo: box {8 channels, 130 pixels, R + 2 rows, 2 channel groups} of the input
+//       view (5-D map: channel in group, x, y, group, image) at (0, x0 - 1,
+//       y0 - 1, c0 / 8, b) -> [group][row][pixel][8 channels]; TMA writes zeros
+//       outside the image. A_{r,t} is then the canonical no-swizzle K-major
+//       operand starting at pixel (r + ky, kx): core matrices (8 pixels x 16
+//       bytes) 128 B apart along M, the two groups PLANE bytes apart. With the
+//       channel-group planar layout each box row is one contiguous 2080-byte run.
+//   weights: box {8 channels, COUT, 2 groups, 9 taps} of w viewed as
+//       [tap][group][n][8] -> B_t at tap * 2 * COUT * 16: core matrices 128 B
+//       apart along N, the two groups COUT * 16 B apart.
+// Roles (192 threads): warp 0 lane 0 issues the TMA loads of each chunk after
+// the MMAs of the chunk that used the buffer have completed (empty barrier,
+// tcgen05.commit); warp 1 lane 0 issues the 9 * R MMAs of each chunk when its
+// loads have landed (full barrier, complete_tx) and commits the finished tile
+// to a TMEM buffer (two buffers, so the epilogue of one tile overlaps the MMAs
+// of the next); warps 2..5 read the accumulators with tcgen05.ld (warp w owns
+// TMEM lanes 32 (w % 4) ...), add the bias, apply the ReLU and store BF16.
+// Every wait is bounded by the global timer: a role that gives up records an
+// error in *err and raises a shared abort flag that ends the other roles' waits.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "sgi_nn_internal.h"
+
+namespace sgi {
+namespace nn {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int kTcM = 128;                    // pixels per tile row (MMA M)
+constexpr int kHaloPix = kTcM + 2;           // 130
+constexpr int kRowBytes = kHaloPix * 16;     // 2080: one halo row of one 8-channel group
+constexpr int kThreads = 192;
+constexpr unsigned long long kWaitNs = 200ull * 1000ull * 1000ull;   // bound on every wait
+constexpr int kSmemBudget = 220 * 1024;
+
+__host__ __device__ constexpr int round_up(int v, int m) { return (v + m - 1) / m * m; }
+__host__ __device__ constexpr int pow2_cols(int c) {
+    return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
+}
+
+template <int COUT> struct TcShape {
+    static constexpr int R = COUT <= 64 ? 4 : (COUT <= 128 ? 2 : 1);   // output rows per tile
+    static constexpr int HALO_ROWS = R + 2;
+    static constexpr int PLANE = HALO_ROWS * kRowBytes;                // one channel group of the halo
+    static constexpr int W_OFF = round_up(2 * PLANE, 128);
+    static constexpr int WBYTES = 9 * 2 * COUT * 16;
+    static constexpr int STAGE = round_up(W_OFF + WBYTES, 128);
+    static constexpr int STAGES = kSmemBudget / STAGE < 6 ? kSmemBudget / STAGE : 6;
+    static constexpr int TMEM_COLS = pow2_cols(2 * R * COUT);          // two accumulator buffers
+    static constexpr int BUF_COLS = TMEM_COLS / 2;
+    static constexpr uint32_t TX_BYTES = 2u * HALO_ROWS * kRowBytes + WBYTES;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE + 128 /* alignment slack */ + 256 /* barriers */;
+    static_assert(STAGES >= 2, "stage ring");
+    static_assert(R * COUT <= BUF_COLS, "accumulators");
+};
+
+__device__ __forceinline__ uint32_t s_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// sm_100 shared-memory matrix descriptor: no swizzle, descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: BF16 A and B (both K-major), FP32 D, M x N.
+__host__ __device__ constexpr uint32_t instr_desc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Bounded wait for the phase of `parity`; false on timeout or when another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+    if (mbar_test(bar, parity)) return true;
+    const unsigned long long deadline = global_ns() + kWaitNs;
+    while (true) {
+        if (mbar_test(bar, parity)) return true;
+        if (*abort_flag) return false;
+        if (global_ns() > deadline) return false;
+    }
+}
+
+__device__ __forceinline__ void give_up(volatile int* abort_flag, int* err) {
+    *abort_flag = 1;
+    atomicExch(err, 1);
+}
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];\n" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            int c4, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];\n" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                 : "memory");
+}
+
+struct TcTiles {
+    int tiles_x, tiles_y, total;
+};
+
+template <int CIN, int COUT, int MODE>
+__global__ void __launch_bounds__(kThreads, 1)
+    conv3x3_tc_kernel(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_w,
+                      ConvArgs a, TcTiles tl, int* err) {
+    using S = TcShape<COUT>;
+    constexpr int R = S::R, NCH = CIN / 16;
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT >= 16 && COUT <= 256, "shape");
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    unsigned char* ctrl = smem + (size_t)S::STAGES * S::STAGE;
+    uint64_t* full = reinterpret_cast<uint64_t*>(ctrl);            // [STAGES]
+    uint64_t* empty = full + S::STAGES;                            // [STAGES]
+    uint64_t* tfull = empty + S::STAGES;                           // [2]
+    uint64_t* tempty = tfull + 2;                                  // [2]
+    uint64_t* drain = tempty + 2;                                  // [1]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_addr(tmem_slot)),
+                     "r"(S::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < S::STAGES; ++s) {
+            mbar_init(s_addr(full + s), 1);
+            mbar_init(s_addr(empty + s), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(s_addr(tfull + b), 1);
+            mbar_init(s_addr(tempty + b), 4);   // one arrival per epilogue warp
+        }
+        mbar_init(s_addr(drain), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_x)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_w)) : "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t smem_base = s_addr(smem);
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            int s = 0;
+            uint32_t ph = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
+                const int tx = t % tl.tiles_x, rest = t / tl.tiles_x;
+                const int ty = rest % tl.tiles_y, b = rest / tl.tiles_y;
+                const int x0 = tx * kTcM, y0 = ty * R;
+                for (int ch = 0; ch < NCH; ++ch) {
+                    if (!mbar_wait(s_addr(empty + s), ph ^ 1u, abort_flag)) { ok = false; break; }
+                    const uint32_t bar = s_addr(full + s);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+                                 "r"(S::TX_BYTES)
+                                 : "memory");
+                    const uint32_t st = smem_base + s * S::STAGE;
+                    tma_load_5d(st, &map_x, 0, x0 - 1, y0 - 1, ch * 2, b, bar);
+                    tma_load_4d(st + S::W_OFF, &map_w, 0, 0, ch * 2, 0, bar);
+                    if (++s == S::STAGES) { s = 0; ph ^= 1u; }
+                }
+            }
+            if (!ok) give_up(abort_flag, err);
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t IDESC = instr_desc_bf16(kTcM, COUT);
+            int s = 0, acc = 0;
+            uint32_t ph = 0, aph = 0;
+            bool ok = true, issued = false;
+            for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
+                if (!mbar_wait(s_addr(tempty + acc), aph ^ 1u, abort_flag)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t d0 = tmem + (uint32_t)(acc * S::BUF_COLS);
+                for (int ch = 0; ch < NCH; ++ch) {
+                    if (!mbar_wait(s_addr(full + s), ph, abort_flag)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t st = smem_base + s * S::STAGE;
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+#pragma unroll
+                        for (int tap = 0; tap < 9; ++tap) {
+                            const int ky = tap / 3, kx = tap % 3;
+                            const uint64_t ad = smem_desc(st + (r + ky) * kRowBytes + kx * 16, S::PLANE, 128);
+                            const uint64_t bd = smem_desc(st + S::W_OFF + tap * 2 * COUT * 16, COUT * 16, 128);
+                            const uint32_t accum = (ch > 0 || tap > 0) ? 1u : 0u;
+                            asm volatile(
+                                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                                    d0 + (uint32_t)(r * COUT)),
+                                "l"(ad), "l"(bd), "r"(IDESC), "r"(accum)
+                                : "memory");
+                        }
+                    }
+                    issued = true;
+                    mma_commit(s_addr(empty + s));   // frees the stage when these MMAs are done
+                    if (++s == S::STAGES) { s = 0; ph ^= 1u; }
+                }
+                if (!ok) break;
+                mma_commit(s_addr(tfull + acc));     // the tile's accumulators are complete
+                if (++acc == 2) { acc = 0; aph ^= 1u; }
+            }
+            if (!ok) {
+                give_up(abort_flag, err);
+                if (issued) {
+                    // let the MMAs already issued finish before the TMEM is released
+                    mma_commit(s_addr(drain));
+                    const unsigned long long deadline = global_ns() + kWaitNs;
+                    while (!mbar_test(s_addr(drain), 0) && global_ns() < deadline) {
+                    }
+                }
+            }
+        }
+    } else {
+        // ------------------------------------------------ epilogue (warps 2..5)
+        const int q = warp & 3;   // TMEM lane quarter of this warp
+        int acc = 0;
+        uint32_t aph = 0;
+        for (int t = blockIdx.x; t < tl.total; t += gridDim.x) {
+            // warp-uniform decision: tcgen05.ld below is a warp-wide (.sync.aligned) instruction
+            if (!__all_sync(0xffffffffu, mbar_wait(s_addr(tfull + acc), aph, abort_flag))) {
+                if (lane == 0) give_up(abort_flag, err);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int tx = t % tl.tiles_x, rest = t / tl.tiles_x;
+            const int ty = rest % tl.tiles_y, b = rest / tl.tiles_y;
+            const int px = tx * kTcM + q * 32 + lane;
+#pragma unroll 1
+            for (int r = 0; r < R; ++r) {
+                const int gy = ty * R + r;
+                const bool valid = px < a.W && gy < a.H;
+                const size_t pix = valid ? (size_t)gy * a.W + px : 0;
+#pragma unroll
+                for (int n0 = 0; n0 < COUT; n0 += 16) {
+                    uint32_t v[16];
+                    const uint32_t taddr =
+                        tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * S::BUF_COLS + r * COUT + n0);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                        "%12, %13, %14, %15}, [%16];\n"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    if (valid) {
+                        __nv_bfloat162 o[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            float f0 = __uint_as_float(v[2 * j]), f1 = __uint_as_float(v[2 * j + 1]);
+                            if (MODE != 2) {
+                                f0 += __ldg(a.bias + n0 + 2 * j);
+                                f1 += __ldg(a.bias + n0 + 2 * j + 1);
+                            }
+                            if (MODE == 0) { f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); }
+                            o[j] = __floats2bfloat162_rn(f0, f1);
+                        }
+                        *reinterpret_cast<uint4*>(a.y.p + a.y.at(b, pix, n0 / 8)) = *reinterpret_cast<uint4*>(&o[0]);
+                        *reinterpret_cast<uint4*>(a.y.p + a.y.at(b, pix, n0 / 8 + 1)) =
+                            *reinterpret_cast<uint4*>(&o[4]);
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(s_addr(tempty + acc)) : "memory");
+            if (++acc == 2) { acc = 0; aph ^= 1u; }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::TMEM_COLS)
+                     : "memory");
+}
+
+// ---------------------------------------------------------------- host side
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+static int sm_count() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    return n;
+}
+
+template <int CIN, int COUT, int MODE>
+static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
+    using S = TcShape<COUT>;
+    auto encode = encode_fn();
+    if (!encode) return cudaErrorNotSupported;
+    CUtensorMap mx, mw;
+    const cuuint32_t one[4] = {1, 1, 1, 1};
+    // input view: {8 channels, W, H, CIN / 8 groups, B}, box {8, 130, R + 2, 2, 1}
+    const cuuint64_t xdim[5] = {8, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)(CIN / 8), (cuuint64_t)a.B};
+    const cuuint64_t xstr[4] = {(cuuint64_t)a.x.pix * 2, (cuuint64_t)a.x.pix * a.W * 2, (cuuint64_t)a.x.grp * 2,
+                                (cuuint64_t)a.x.img * 2};
+    const cuuint32_t xbox[5] = {8, (cuuint32_t)kHaloPix, (cuuint32_t)S::HALO_ROWS, 2, 1};
+    const cuuint32_t one5[5] = {1, 1, 1, 1, 1};
+    if (encode(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void*)a.x.p, xdim, xstr, xbox, one5,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    // weights [COUT][9][CIN] viewed as {8 channels, COUT, CIN / 8 groups, 9 taps}, box {8, COUT, 2, 9}
+    const cuuint64_t wdim[4] = {8, (cuuint64_t)COUT, (cuuint64_t)(CIN / 8), 9};
+    const cuuint64_t wstr[3] = {(cuuint64_t)9 * CIN * 2, 16, (cuuint64_t)CIN * 2};
+    const cuuint32_t wbox[4] = {8, (cuuint32_t)COUT, 2, 9};
+    if (encode(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.w, wdim, wstr, wbox, one,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    TcTiles tl;
+    tl.tiles_x = (a.W + kTcM - 1) / kTcM;
+    tl.tiles_y = (a.H + S::R - 1) / S::R;
+    const long long total = (long long)tl.tiles_x * tl.tiles_y * a.B;
+    if (total > 0x7fffffffLL) return cudaErrorInvalidValue;
+    tl.total = (int)total;
+    const int sms = sm_count();
+    if (sms <= 0) return cudaErrorInvalidDevice;
+    auto kern = conv3x3_tc_kernel<CIN, COUT, MODE>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+    if (e != cudaSuccess) return e;
+    const int grid = tl.total < sms ? tl.total : sms;
+    kern<<<grid, kThreads, S::SMEM, s>>>(mx, mw, a, tl, err);
+    return cudaGetLastError();
+}
+
+cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err, cudaStream_t s) {
+    // TMA: 16-byte aligned base addresses and strides; channel groups of 8 (16 bytes)
+    if (!err || !view_ok(a.x) || !view_ok(a.y) || (((uintptr_t)a.w) & 15) || a.B < 1 || a.H < 1 || a.W < 1)
+        return cudaErrorInvalidValue;
+#define SGI_TC_CASE(CI, CO)                                                  \
+    if (cin == CI && cout == CO) {                                           \
+        if (mode == 0) return run_tc<CI, CO, 0>(a, err, s);                  \
+        if (mode == 1) return run_tc<CI, CO, 1>(a, err, s);                  \
+        return run_tc<CI, CO, 2>(a, err, s);                                 \
+    }
+    SGI_TC_CASE(16, 32)
+    SGI_TC_CASE(32, 32)
+    SGI_TC_CASE(32, 64)
+    SGI_TC_CASE(64, 64)
+    SGI_TC_CASE(64, 128)
+    SGI_TC_CASE(128, 128)
+    SGI_TC_CASE(192, 64)
+    SGI_TC_CASE(96, 32)
+    SGI_TC_CASE(64, 32)
+    SGI_TC_CASE(128, 64)
+    SGI_TC_CASE(64, 192)
+    SGI_TC_CASE(32, 96)
+#undef SGI_TC_CASE
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace nn
+}  // namespace sgi

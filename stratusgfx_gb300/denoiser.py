@@ -78,6 +78,14 @@ class KpcnDenoiser:
                                              stage._stream_ptr(stream)))
         return float(loss.value)
 
+    def set_conv_path(self, path: int):
+        """abi.SGI_NN_CONV_TCGEN05 (tcgen05.mma, TMEM accumulators) or abi.SGI_NN_CONV_WARP_MMA."""
+        self._chk(self.lib.sgi_nn_set_conv_path(self.h, path))
+
+    def device_status(self):
+        """Synchronises; raises SgiError(SGI_ERR_TIMEOUT) if a tensor-core wait ran out."""
+        self._chk(self.lib.sgi_nn_device_status(self.h))
+
     def forward(self, feat, noisy, prev, out, stream=None):
         B, H, W = feat.shape[:3]
         self._chk(self.lib.sgi_nn_forward(self.h, _p(feat), _p(noisy), _p(prev), B, H, W, _p(out),

@@ -38,9 +38,14 @@ def to_dev(feat, noisy, prev, target):
             torch.from_numpy(prev).cuda(), torch.from_numpy(target).cuda())
 
 
-def test_gradients_match_oracle():
+PATHS = [abi.SGI_NN_CONV_TCGEN05, abi.SGI_NN_CONV_WARP_MMA]
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_gradients_match_oracle(path):
     B, H, W = 2, 16, 32
     net = KpcnDenoiser(B, H, W, seed=3)
+    net.set_conv_path(path)
     p = bf16_round(net.params())           # the forward uses BF16 weights
     net.set_params(p)
     feat, noisy, prev, target = random_problem(B, H, W, 1)
@@ -63,12 +68,15 @@ def test_gradients_match_oracle():
     print("per-layer gradient error vs float64 oracle:", report)
     bad = [r for r in report if not (r[2] <= 1e-1 and r[3] >= 0.99)]
     assert not bad, report
+    net.device_status()
     net.close()
 
 
-def test_forward_matches_oracle():
-    B, H, W = 1, 32, 32
+@pytest.mark.parametrize("path", PATHS)
+def test_forward_matches_oracle(path):
+    B, H, W = 1, 32, 160
     net = KpcnDenoiser(B, H, W, seed=5)
+    net.set_conv_path(path)
     p = bf16_round(net.params())
     net.set_params(p)
     feat, noisy, prev, _ = random_problem(B, H, W, 2)
@@ -81,6 +89,7 @@ def test_forward_matches_oracle():
     got = out.cpu().numpy()[..., :3]
     rel = np.abs(got - ref).max() / np.abs(ref).max()
     assert rel < 2e-2, rel
+    net.device_status()
     net.close()
 
 

@@ -269,7 +269,8 @@ cudaError_t bias_grad(const View& dz, int c, int B, int H, int W, float* db, cud
 
 // ---------------------------------------------------- elementwise / resampling --
 // These kernels move 8 channels (one 16-byte vector) per thread; the thread
-// index runs over (pixel, channel group) with the group fastest.
+// index runs over (image, channel group, pixel) with the pixel fastest, so a
+// warp touches consecutive pixels of one group (contiguous in the planar layout).
 __device__ __forceinline__ void bf8_to_f(const uint4& v, float* f) {
     const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
 #pragma unroll
@@ -291,10 +292,9 @@ __global__ void relu_bwd_kernel(View dy, View y, View dz, int B, int HW, int g8)
     const unsigned n = (unsigned)B * HW * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int g = (int)(i % g8);
-    const unsigned q = i / g8;
-    const int b = (int)(q / HW);
-    const size_t pix = q - (size_t)b * HW;
+    const size_t pix = i % HW;
+    const unsigned bg = i / HW;
+    const int g = (int)(bg % g8), b = (int)(bg / g8);
     const uint4 yv = vec8(y, b, pix, g), dv = vec8(dy, b, pix, g);
     const __nv_bfloat162* yh = reinterpret_cast<const __nv_bfloat162*>(&yv);
     const __nv_bfloat162* dh = reinterpret_cast<const __nv_bfloat162*>(&dv);
@@ -315,9 +315,8 @@ __global__ void pool_fwd_kernel(View in, View out, int B, int H, int W, int g8) 
     const unsigned n = (unsigned)B * Ho * Wo * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int g = (int)(i % g8);
-    const unsigned q = i / g8;
-    const int xo = (int)(q % Wo), yo = (int)((q / Wo) % Ho), b = (int)(q / ((unsigned)Wo * Ho));
+    const unsigned q = i % ((unsigned)Ho * Wo), bg = i / ((unsigned)Ho * Wo);
+    const int xo = (int)(q % Wo), yo = (int)(q / Wo), g = (int)(bg % g8), b = (int)(bg / g8);
     float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, f[8];
     for (int dy = 0; dy < 2; ++dy)
         for (int dx = 0; dx < 2; ++dx) {
@@ -335,9 +334,8 @@ __global__ void pool_bwd_kernel(View dout, View din, int B, int H, int W, int g8
     const unsigned n = (unsigned)B * H * W * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int g = (int)(i % g8);
-    const unsigned q = i / g8;
-    const int x = (int)(q % W), y = (int)((q / W) % H), b = (int)(q / ((unsigned)W * H));
+    const unsigned q = i % ((unsigned)H * W), bg = i / ((unsigned)H * W);
+    const int x = (int)(q % W), y = (int)(q / W), g = (int)(bg % g8), b = (int)(bg / g8);
     const int Wo = W / 2;
     float v[8], d[8];
     bf8_to_f(vec8(dout, b, (size_t)(y / 2) * Wo + x / 2, g), v);
@@ -357,9 +355,8 @@ __global__ void up_fwd_kernel(View in, View out, int B, int H, int W, int g8) {
     const unsigned n = (unsigned)B * H * W * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int g = (int)(i % g8);
-    const unsigned q = i / g8;
-    const int x = (int)(q % W), y = (int)((q / W) % H), b = (int)(q / ((unsigned)W * H));
+    const unsigned q = i % ((unsigned)H * W), bg = i / ((unsigned)H * W);
+    const int x = (int)(q % W), y = (int)(q / W), g = (int)(bg % g8), b = (int)(bg / g8);
     vec8(out, b, (size_t)y * W + x, g) = vec8(in, b, (size_t)(y / 2) * (W / 2) + x / 2, g);
 }
 
@@ -368,9 +365,8 @@ __global__ void up_bwd_kernel(View dout, View din, int B, int Hi, int Wi, int g8
     const unsigned n = (unsigned)B * Hi * Wi * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int g = (int)(i % g8);
-    const unsigned q = i / g8;
-    const int x = (int)(q % Wi), y = (int)((q / Wi) % Hi), b = (int)(q / ((unsigned)Wi * Hi));
+    const unsigned q = i % ((unsigned)Hi * Wi), bg = i / ((unsigned)Hi * Wi);
+    const int x = (int)(q % Wi), y = (int)(q / Wi), g = (int)(bg % g8), b = (int)(bg / g8);
     const int W = Wi * 2;
     float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, f[8];
     for (int dy = 0; dy < 2; ++dy)
@@ -427,6 +423,7 @@ cudaError_t up_bwd(const View& dout, const View& din, int B, int Hi, int Wi, int
 // a = sigmoid(l25); neighbours clamped to the image. With a target, also the
 // loss sum of |log1p(out) - log1p(target)| and dlogits = d(mean loss)/dlogits.
 constexpr int kApplyTX = 32, kApplyTY = 8;
+template <bool TRAIN>
 __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
     // the block's 32 x 8 pixels of `noisy` with a 2-pixel edge-clamped border
     __shared__ float4 tile[kApplyTY + 4][kApplyTX + 4];
@@ -469,8 +466,8 @@ __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
         float o[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) o[c] = alpha * sp[c] + (1.0f - alpha) * pr[c];
-        if (a.out) a.out[i] = make_float4(o[0], o[1], o[2], 1.0f);
-        if (a.target) {
+        if (!TRAIN) a.out[i] = make_float4(o[0], o[1], o[2], 1.0f);
+        if (TRAIN) {
             const float4 tv = a.target[i];
             const float t[3] = {tv.x, tv.y, tv.z};
             float dout[3];
@@ -503,7 +500,7 @@ __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
             for (int g = 0; g < 4; ++g) vec8(a.dlogits, b, q, g) = f_to_bf8(dl + 8 * g);
         }
     }
-    if (a.loss) {
+    if (TRAIN) {
         // block reduction of the loss: warp butterfly, then the 8 warp sums
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
@@ -521,7 +518,13 @@ cudaError_t kpcn_apply(const ApplyArgs& a, cudaStream_t s) {
     if (!view_ok(a.logits) || (a.target && !view_ok(a.dlogits))) return cudaErrorInvalidValue;
     if (a.B < 1 || a.H < 1 || a.W < 1 || a.B > 65535) return cudaErrorInvalidValue;
     dim3 grid((a.W + kApplyTX - 1) / kApplyTX, (a.H + kApplyTY - 1) / kApplyTY, a.B);
-    kpcn_apply_kernel<<<grid, 256, 0, s>>>(a);
+    if (a.target) {
+        if (!a.loss || !a.target) return cudaErrorInvalidValue;
+        kpcn_apply_kernel<true><<<grid, 256, 0, s>>>(a);
+    } else {
+        if (!a.out) return cudaErrorInvalidValue;
+        kpcn_apply_kernel<false><<<grid, 256, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 

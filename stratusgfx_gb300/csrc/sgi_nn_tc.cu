@@ -67,7 +67,8 @@ template <int COUT> struct TcShape {
     static constexpr int TMEM_COLS = pow2_cols(2 * R * COUT);          // two accumulator buffers
     static constexpr int BUF_COLS = TMEM_COLS / 2;
     static constexpr uint32_t TX_BYTES = 2u * HALO_ROWS * kRowBytes + WBYTES;
-    static constexpr size_t SMEM = (size_t)STAGES * STAGE + 128 /* alignment slack */ + 256 /* barriers */;
+    static constexpr size_t SMEM =
+        (size_t)STAGES * STAGE + 128 /* alignment slack */ + 256 /* barriers */ + COUT * 4 /* bias */;
     static_assert(STAGES >= 2, "stage ring");
     static_assert(R * COUT <= BUF_COLS, "accumulators");
 };
@@ -166,6 +167,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint64_t* drain = tempty + 2;                                  // [1]
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    float* bias_s = reinterpret_cast<float*>(ctrl + 256);            // [COUT]
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 1) {
@@ -223,6 +225,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
             constexpr uint32_t IDESC = instr_desc_bf16(kTcM, COUT);
+            // Descriptors are split into a 32-bit low word (start address >> 4, leading
+            // byte offset >> 4) and a constant high word (stride byte offset >> 4,
+            // version 1). Every MMA of a chunk adds a compile-time offset to the low
+            // word of the stage's base descriptor, so the issue loop has no dependent
+            // address arithmetic.
+            constexpr uint32_t HI = (128u >> 4) | (1u << 14);
             int s = 0, acc = 0;
             uint32_t ph = 0, aph = 0;
             bool ok = true, issued = false;
@@ -234,19 +242,23 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (!mbar_wait(s_addr(full + s), ph, abort_flag)) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                     const uint32_t st = smem_base + s * S::STAGE;
+                    const uint32_t a_lo = ((st >> 4) & 0x3FFFu) | ((uint32_t)(S::PLANE >> 4) << 16);
+                    const uint32_t b_lo = (((st + S::W_OFF) >> 4) & 0x3FFFu) | ((uint32_t)(COUT * 16 >> 4) << 16);
+                    const uint32_t first = ch > 0 ? 1u : 0u;
 #pragma unroll
                     for (int r = 0; r < R; ++r) {
 #pragma unroll
                         for (int tap = 0; tap < 9; ++tap) {
                             const int ky = tap / 3, kx = tap % 3;
-                            const uint64_t ad = smem_desc(st + (r + ky) * kRowBytes + kx * 16, S::PLANE, 128);
-                            const uint64_t bd = smem_desc(st + S::W_OFF + tap * 2 * COUT * 16, COUT * 16, 128);
-                            const uint32_t accum = (ch > 0 || tap > 0) ? 1u : 0u;
+                            const uint32_t a = a_lo + (uint32_t)(((r + ky) * kRowBytes + kx * 16) >> 4);
+                            const uint32_t b = b_lo + (uint32_t)((tap * 2 * COUT * 16) >> 4);
+                            const uint32_t accum = tap > 0 ? 1u : first;
                             asm volatile(
-                                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                                "{\n .reg .pred p;\n .reg .b64 ad, bd;\n setp.ne.b32 p, %5, 0;\n"
+                                " mov.b64 ad, {%1, %3};\n mov.b64 bd, {%2, %3};\n"
+                                " tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %4, p;\n}\n" ::"r"(
                                     d0 + (uint32_t)(r * COUT)),
-                                "l"(ad), "l"(bd), "r"(IDESC), "r"(accum)
+                                "r"(a), "r"(b), "r"(HI), "r"(IDESC), "r"(accum)
                                 : "memory");
                         }
                     }
@@ -272,11 +284,20 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else {
         // ------------------------------------------------ epilogue (warps 2..5)
         const int q = warp & 3;   // TMEM lane quarter of this warp
+        const int et = tid - 64;  // 0..127
+        if (MODE != 2)
+            for (int c = et; c < COUT; c += 128) bias_s[c] = a.bias[c];
+        asm volatile("bar.sync 1, 128;\n" ::: "memory");   // epilogue warps only
         int acc = 0;
         uint32_t aph = 0;
         for (int t = blockIdx.x; t < tl.total; t += gridDim.x) {
-            // warp-uniform decision: tcgen05.ld below is a warp-wide (.sync.aligned) instruction
-            if (!__all_sync(0xffffffffu, mbar_wait(s_addr(tfull + acc), aph, abort_flag))) {
+            // one lane polls the barrier (polling from every lane competes with the MMA
+            // operand reads in shared memory); the warp then leaves or proceeds together,
+            // as tcgen05.ld below is a warp-wide (.sync.aligned) instruction
+            int ready = 0;
+            if (lane == 0) ready = mbar_wait(s_addr(tfull + acc), aph, abort_flag) ? 1 : 0;
+            ready = __shfl_sync(0xffffffffu, ready, 0);
+            if (!ready) {
                 if (lane == 0) give_up(abort_flag, err);
                 break;
             }
@@ -288,35 +309,45 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int r = 0; r < R; ++r) {
                 const int gy = ty * R + r;
                 const bool valid = px < a.W && gy < a.H;
-                const size_t pix = valid ? (size_t)gy * a.W + px : 0;
+                bf16* yp = a.y.p + a.y.at(b, valid ? (size_t)gy * a.W + px : 0, 0);
 #pragma unroll
-                for (int n0 = 0; n0 < COUT; n0 += 16) {
-                    uint32_t v[16];
+                for (int n0 = 0; n0 < COUT; n0 += 32) {
+                    uint32_t v[32];
                     const uint32_t taddr =
                         tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * S::BUF_COLS + r * COUT + n0);
                     asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-                        "%12, %13, %14, %15}, [%16];\n"
+                        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                        "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+                        "%30, %31}, [%32];\n"
                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
                           "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-                          "=r"(v[14]), "=r"(v[15])
+                          "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]),
+                          "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
+                          "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                         : "r"(taddr));
                     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
                     if (valid) {
-                        __nv_bfloat162 o[8];
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            float f0 = __uint_as_float(v[2 * j]), f1 = __uint_as_float(v[2 * j + 1]);
+                        for (int g = 0; g < 4; ++g) {
+                            float f[8];
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) f[j] = __uint_as_float(v[8 * g + j]);
                             if (MODE != 2) {
-                                f0 += __ldg(a.bias + n0 + 2 * j);
-                                f1 += __ldg(a.bias + n0 + 2 * j + 1);
+                                const float4 b0 = *reinterpret_cast<const float4*>(bias_s + n0 + 8 * g);
+                                const float4 b1 = *reinterpret_cast<const float4*>(bias_s + n0 + 8 * g + 4);
+                                f[0] += b0.x; f[1] += b0.y; f[2] += b0.z; f[3] += b0.w;
+                                f[4] += b1.x; f[5] += b1.y; f[6] += b1.z; f[7] += b1.w;
                             }
-                            if (MODE == 0) { f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); }
-                            o[j] = __floats2bfloat162_rn(f0, f1);
+                            uint4 o;
+                            __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) {
+                                float f0 = f[2 * j], f1 = f[2 * j + 1];
+                                if (MODE == 0) { f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); }
+                                oh[j] = __floats2bfloat162_rn(f0, f1);
+                            }
+                            *reinterpret_cast<uint4*>(yp + (size_t)((n0 >> 3) + g) * (size_t)a.y.grp) = o;
                         }
-                        *reinterpret_cast<uint4*>(a.y.p + a.y.at(b, pix, n0 / 8)) = *reinterpret_cast<uint4*>(&o[0]);
-                        *reinterpret_cast<uint4*>(a.y.p + a.y.at(b, pix, n0 / 8 + 1)) =
-                            *reinterpret_cast<uint4*>(&o[4]);
                     }
                 }
             }

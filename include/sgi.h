@@ -223,6 +223,26 @@ sgi_status sgi_set_shadow_maps(sgi_ctx* ctx, const sgi_csm* csm, const sgi_cube_
  * Stable compaction in ascending VPL index; no host readback. */
 sgi_status sgi_cull_vpls(sgi_ctx* ctx, void* stream);
 
+/* The VPL visibility cull without a context and without allocating anything.
+ * No counterpart in StratusGFX (its culling pass always owns its buffers); it
+ * runs the kernels of sgi_cull_vpls on caller-owned device buffers:
+ *   vpls, entries        [num_vpls] (16-byte aligned), csm: the directional CSM;
+ *   visible_vpls         [max_visible], visible_entries [max_visible];
+ *   visible_index        int32 [1 + max_visible]: the visible count (capped at
+ *                        max_visible), then the original indices, ascending.
+ * The per-VPL visibility flags live in a fixed 16384-byte array inside the
+ * library (one per device), so num_vpls may not exceed
+ * SGI_NOALLOC_CULL_MAX_VPLS: larger counts return SGI_ERR_CAP and launch nothing.
+ * Every flag a call reads is written by the same call first; nothing has to
+ * start at zero. Calls that overlap on one device (two streams, or two host
+ * threads, with work in flight at the same time) share that array and race:
+ * order them on one stream or with events. The first call on each device looks
+ * up the array's address; make that call before any stream capture begins. */
+#define SGI_NOALLOC_CULL_MAX_VPLS 16384
+sgi_status sgi_cull_vpls_noalloc(const sgi_vpl* vpls, const sgi_atlas_entry* entries, int32_t num_vpls,
+                                 const sgi_csm* csm, int32_t max_visible, sgi_vpl* visible_vpls,
+                                 sgi_atlas_entry* visible_entries, int32_t* visible_index, void* stream);
+
 /* Per-tile culling: vpl_tiled_deferred_culling_stage1.cs + _stage2.cs
  * (dispatch at StratusRendererBackend.cpp:1733-1783). */
 sgi_status sgi_cull_tiles(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera* cam, void* stream);

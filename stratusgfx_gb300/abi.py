@@ -145,6 +145,8 @@ EXPORTS = {
                                       C.c_int32, C.c_int32, C.c_float, C.c_int32, C.POINTER(C.c_float), C.c_void_p]),
     "sgi_nn_features": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(Camera), C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p]),
+    "sgi_cull_vpls_noalloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(Csm), C.c_int32, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p]),
     "sgi_nn_set_conv_path": (C.c_int32, [C.c_void_p, C.c_int32]),
     "sgi_nn_device_status": (C.c_int32, [C.c_void_p]),
     "sgi_nn_conv3x3": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,

@@ -327,6 +327,28 @@ sgi_status sgi_cull_vpls(sgi_ctx* ctx, void* stream) {
     return SGI_OK;
 }
 
+sgi_status sgi_cull_vpls_noalloc(const sgi_vpl* vpls, const sgi_atlas_entry* entries, int32_t num_vpls,
+                                 const sgi_csm* csm, int32_t max_visible, sgi_vpl* visible_vpls,
+                                 sgi_atlas_entry* visible_entries, int32_t* visible_index, void* stream) {
+    if (!csm || !visible_vpls || !visible_entries || !visible_index || max_visible < 1 || num_vpls < 0)
+        return SGI_ERR_ARG;
+    if (num_vpls > SGI_NOALLOC_CULL_MAX_VPLS) return SGI_ERR_CAP;
+    if (num_vpls > 0 && (!vpls || !entries)) return SGI_ERR_ARG;
+    if (((uintptr_t)vpls & 15) || ((uintptr_t)visible_vpls & 15) || ((uintptr_t)entries & 7) ||
+        ((uintptr_t)visible_entries & 7) || ((uintptr_t)visible_index & 3))
+        return SGI_ERR_ARG;
+    if (!csm->depth || csm->resolution < 1 || csm->num_cascades != 4) return SGI_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (num_vpls == 0) return cudaMemsetAsync(visible_index, 0, sizeof(int32_t), s) == cudaSuccess ? SGI_OK : SGI_ERR_CUDA;
+    uint8_t* flags = nullptr;
+    if (sgi::noalloc_cull_flags(&flags) != cudaSuccess) return SGI_ERR_CUDA;
+    if (sgi::launch_vis_flags(vpls, num_vpls, *csm, flags, s) != cudaSuccess) return SGI_ERR_CUDA;
+    if (sgi::launch_compact(vpls, entries, flags, num_vpls, max_visible, visible_vpls, visible_entries, visible_index,
+                            s) != cudaSuccess)
+        return SGI_ERR_CUDA;
+    return SGI_OK;
+}
+
 sgi_status sgi_cull_tiles(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera* cam, void* stream) {
     if (!ctx) return SGI_ERR_ARG;
     if (!gbuffer_ok(gbuf, false) || !cam) return fail(ctx, SGI_ERR_ARG, "NULL G-buffer depth/normal or camera");

@@ -53,6 +53,8 @@ struct DenoiseLaunch {
 };
 
 cudaError_t launch_vis_flags(const sgi_vpl* vpls, int32_t n, const sgi_csm& csm, uint8_t* flags, cudaStream_t s);
+// Device address of the fixed flag array of sgi_cull_vpls_noalloc on the current device.
+cudaError_t noalloc_cull_flags(uint8_t** flags);
 cudaError_t launch_compact(const sgi_vpl* vpls, const sgi_atlas_entry* entries, const uint8_t* flags, int32_t n,
                            int32_t cap, sgi_vpl* cv, sgi_atlas_entry* ce, int32_t* visible_index, cudaStream_t s);
 cudaError_t launch_tile_stage1(const sgi_config& cfg, const sgi_gbuffer& g, const sgi_camera& cam,

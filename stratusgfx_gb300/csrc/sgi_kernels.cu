@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "sgi_internal.h"
 #include "sgi_math.cuh"
 
@@ -189,6 +191,31 @@ __global__ void __launch_bounds__(1024) vpl_compact_kernel(const sgi_vpl* __rest
         __syncthreads();
     }
     if (tid == 0) visible_index[0] = base < cap ? base : cap;
+}
+
+// Flag array of sgi_cull_vpls_noalloc (one byte per VPL). vpl_vis_flags_kernel
+// writes every flag below the call's VPL count before vpl_compact_kernel reads
+// it, so the array is never cleared.
+static __device__ __align__(256) uint8_t g_noalloc_cull_flags[SGI_NOALLOC_CULL_MAX_VPLS];
+
+cudaError_t noalloc_cull_flags(uint8_t** flags) {
+    // looked up once per device, with that device current
+    constexpr int kMaxDevices = 64;
+    static std::mutex lock;
+    static void* addr[kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> g(lock);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_cull_flags);
+        if (e != cudaSuccess) return e;
+        addr[dev] = p;
+    }
+    *flags = static_cast<uint8_t*>(addr[dev]);
+    return cudaSuccess;
 }
 
 cudaError_t launch_vis_flags(const sgi_vpl* vpls, int32_t n, const sgi_csm& csm, uint8_t* flags, cudaStream_t s) {

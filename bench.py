@@ -433,9 +433,8 @@ def time_frames(render, ds, frames, steps, warmup, flush):
 
 
 def neural_vs_plain(args, ds, sc, w, cfg, flush):
-    """The metric's comparison: plain a-trous at K = 8 against the learned denoiser at K = 8, 4, 2;
-    ms/frame (device-resident) and PSNR against the converged frame. The neural configuration
-    reported is the fastest whose PSNR reaches the plain path's."""
+    """The metric's comparison: plain a-trous at K = 8..64 against the learned denoiser at K = 8, 4, 2;
+    ms/frame (device-resident) and PSNR against the converged frame (equal_psnr below)."""
     import ctypes as C
 
     import torch
@@ -477,20 +476,22 @@ def neural_vs_plain(args, ds, sc, w, cfg, flush):
             res[name][f"K{K}"] = {"ms_per_frame": round(ms, 4), "mpix_s": round(W * H / ms / 1e3, 1),
                                   "psnr_db": p_full, "psnr_gi_db": p_gi}
     net.close()
-    # equal PSNR: the fastest neural configuration reaching the plain K = 8 path's GI PSNR, and the
-    # cheapest plain configuration reaching the best neural configuration's GI PSNR (if any does).
-    plain = res["plain"]["K8"]
-    ok = [(v["ms_per_frame"], k) for k, v in res["neural"].items() if v["psnr_gi_db"] >= plain["psnr_gi_db"]]
-    eq = {"plain_K8_gi_psnr_db": plain["psnr_gi_db"], "plain_K8_ms": plain["ms_per_frame"]}
+    # Equal PSNR. The plain path's quality saturates with K (the a-trous filter's bias, not
+    # the sample count, bounds its error against the converged frame), so the comparison is:
+    # the plain path at its best GI PSNR, reached by its cheapest K (within 0.1 dB), against
+    # the fastest neural configuration whose GI PSNR is at least that high.
+    best_plain = max(v["psnr_gi_db"] for v in res["plain"].values())
+    plain_ref = min(((v["ms_per_frame"], k) for k, v in res["plain"].items() if v["psnr_gi_db"] >= best_plain - 0.1))
+    eq = {"plain_best_gi_psnr_db": best_plain, "plain_config": plain_ref[1], "plain_ms": plain_ref[0],
+          "plain_K8_gi_psnr_db": res["plain"]["K8"]["psnr_gi_db"], "plain_K8_ms": res["plain"]["K8"]["ms_per_frame"]}
+    ok = [(v["ms_per_frame"], k) for k, v in res["neural"].items() if v["psnr_gi_db"] >= best_plain]
     if ok:
-        eq.update({"neural_config": min(ok)[1], "neural_ms": min(ok)[0],
-                   "neural_speedup_vs_plain_K8": round(plain["ms_per_frame"] / min(ok)[0], 3)})
-    fastest_neural = min(res["neural"].items(), key=lambda kv: kv[1]["ms_per_frame"])
-    reach = [(v["ms_per_frame"], k) for k, v in res["plain"].items()
-             if v["psnr_gi_db"] >= fastest_neural[1]["psnr_gi_db"]]
-    eq["plain_config_matching_fastest_neural"] = min(reach)[1] if reach else None
-    if reach:
-        eq["speedup_at_equal_psnr"] = round(min(reach)[0] / fastest_neural[1]["ms_per_frame"], 3)
+        nk = min(ok)[1]
+        eq.update({"neural_config": nk, "neural_ms": min(ok)[0],
+                   "neural_gain_gi_db": round(res["neural"][nk]["psnr_gi_db"] - best_plain, 2),
+                   "speedup_at_equal_or_better_psnr": round(plain_ref[0] / min(ok)[0], 3)})
+    else:
+        eq["neural_config"] = None
     res["equal_psnr"] = eq
     res["converged_target"] = {"samples_per_pixel": 512, "accumulation": "fp64", "ms_per_frame": round(target_ms, 2)}
     return res

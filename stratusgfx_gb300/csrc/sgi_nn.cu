@@ -268,9 +268,10 @@ cudaError_t bias_grad(const View& dz, int c, int B, int H, int W, float* db, cud
 }
 
 // ---------------------------------------------------- elementwise / resampling --
-// These kernels move 8 channels (one 16-byte vector) per thread; the thread
-// index runs over (image, channel group, pixel) with the pixel fastest, so a
-// warp touches consecutive pixels of one group (contiguous in the planar layout).
+// These kernels move 8 channels (one 16-byte vector) per thread. The thread
+// index runs over (image, pixel, channel group) with the group fastest for NHWC
+// views (a warp covers whole pixels) and over (image, channel group, pixel)
+// with the pixel fastest for planar views (a warp covers one group's run).
 __device__ __forceinline__ void bf8_to_f(const uint4& v, float* f) {
     const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
 #pragma unroll
@@ -287,14 +288,31 @@ __device__ __forceinline__ uint4& vec8(const View& v, int b, size_t q, int g) {
     return *reinterpret_cast<uint4*>(v.p + v.at(b, q, g));
 }
 
+// thread index i -> (pixel q of npix, group g of g8, image b)
+template <bool PIXFAST>
+__device__ __forceinline__ void split_index(unsigned i, unsigned npix, int g8, unsigned& q, int& g, int& b) {
+    if (PIXFAST) {
+        q = i % npix;
+        const unsigned bg = i / npix;
+        g = (int)(bg % g8);
+        b = (int)(bg / g8);
+    } else {
+        g = (int)(i % g8);
+        const unsigned qb = i / g8;
+        q = qb % npix;
+        b = (int)(qb / npix);
+    }
+}
+
 // dz = dy * (y > 0)
+template <bool PIXFAST>
 __global__ void relu_bwd_kernel(View dy, View y, View dz, int B, int HW, int g8) {
     const unsigned n = (unsigned)B * HW * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const size_t pix = i % HW;
-    const unsigned bg = i / HW;
-    const int g = (int)(bg % g8), b = (int)(bg / g8);
+    unsigned pix;
+    int g, b;
+    split_index<PIXFAST>(i, (unsigned)HW, g8, pix, g, b);
     const uint4 yv = vec8(y, b, pix, g), dv = vec8(dy, b, pix, g);
     const __nv_bfloat162* yh = reinterpret_cast<const __nv_bfloat162*>(&yv);
     const __nv_bfloat162* dh = reinterpret_cast<const __nv_bfloat162*>(&dv);
@@ -310,13 +328,16 @@ __global__ void relu_bwd_kernel(View dy, View y, View dz, int B, int HW, int g8)
 }
 
 // 2x2 average pooling (H, W even): out[b, y, x] = mean of in[b, 2y.., 2x..]
+template <bool PIXFAST>
 __global__ void pool_fwd_kernel(View in, View out, int B, int H, int W, int g8) {
     const int Ho = H / 2, Wo = W / 2;
     const unsigned n = (unsigned)B * Ho * Wo * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const unsigned q = i % ((unsigned)Ho * Wo), bg = i / ((unsigned)Ho * Wo);
-    const int xo = (int)(q % Wo), yo = (int)(q / Wo), g = (int)(bg % g8), b = (int)(bg / g8);
+    unsigned q;
+    int g, b;
+    split_index<PIXFAST>(i, (unsigned)Ho * Wo, g8, q, g, b);
+    const int xo = (int)(q % Wo), yo = (int)(q / Wo);
     float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, f[8];
     for (int dy = 0; dy < 2; ++dy)
         for (int dx = 0; dx < 2; ++dx) {
@@ -330,12 +351,15 @@ __global__ void pool_fwd_kernel(View in, View out, int B, int H, int W, int g8) 
 }
 
 // din[b, y, x] (+)= 0.25 * dout[b, y/2, x/2]
+template <bool PIXFAST>
 __global__ void pool_bwd_kernel(View dout, View din, int B, int H, int W, int g8, int accumulate) {
     const unsigned n = (unsigned)B * H * W * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const unsigned q = i % ((unsigned)H * W), bg = i / ((unsigned)H * W);
-    const int x = (int)(q % W), y = (int)(q / W), g = (int)(bg % g8), b = (int)(bg / g8);
+    unsigned q;
+    int g, b;
+    split_index<PIXFAST>(i, (unsigned)H * W, g8, q, g, b);
+    const int x = (int)(q % W), y = (int)(q / W);
     const int Wo = W / 2;
     float v[8], d[8];
     bf8_to_f(vec8(dout, b, (size_t)(y / 2) * Wo + x / 2, g), v);
@@ -351,22 +375,28 @@ __global__ void pool_bwd_kernel(View dout, View din, int B, int H, int W, int g8
 }
 
 // nearest 2x upsampling: out[b, y, x] = in[b, y/2, x/2]
+template <bool PIXFAST>
 __global__ void up_fwd_kernel(View in, View out, int B, int H, int W, int g8) {
     const unsigned n = (unsigned)B * H * W * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const unsigned q = i % ((unsigned)H * W), bg = i / ((unsigned)H * W);
-    const int x = (int)(q % W), y = (int)(q / W), g = (int)(bg % g8), b = (int)(bg / g8);
+    unsigned q;
+    int g, b;
+    split_index<PIXFAST>(i, (unsigned)H * W, g8, q, g, b);
+    const int x = (int)(q % W), y = (int)(q / W);
     vec8(out, b, (size_t)y * W + x, g) = vec8(in, b, (size_t)(y / 2) * (W / 2) + x / 2, g);
 }
 
 // din[b, y, x] = sum of dout over the 2x2 block it was copied to
+template <bool PIXFAST>
 __global__ void up_bwd_kernel(View dout, View din, int B, int Hi, int Wi, int g8) {
     const unsigned n = (unsigned)B * Hi * Wi * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const unsigned q = i % ((unsigned)Hi * Wi), bg = i / ((unsigned)Hi * Wi);
-    const int x = (int)(q % Wi), y = (int)(q / Wi), g = (int)(bg % g8), b = (int)(bg / g8);
+    unsigned q;
+    int g, b;
+    split_index<PIXFAST>(i, (unsigned)Hi * Wi, g8, q, g, b);
+    const int x = (int)(q % Wi), y = (int)(q / Wi);
     const int W = Wi * 2;
     float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, f[8];
     for (int dy = 0; dy < 2; ++dy)
@@ -385,35 +415,40 @@ cudaError_t relu_bwd(const View& dy, const View& y, const View& dz, int c, int B
     const size_t n = (size_t)B * H * W * (c / 8);
     if (!view_ok(dy) || !view_ok(y) || !view_ok(dz) || !launch_ok(n, c)) return cudaErrorInvalidValue;
     if (n == 0) return cudaSuccess;
-    relu_bwd_kernel<<<blocks_for(n), 256, 0, s>>>(dy, y, dz, B, H * W, c / 8);
+    if (dz.grp == 8) relu_bwd_kernel<false><<<blocks_for(n), 256, 0, s>>>(dy, y, dz, B, H * W, c / 8);
+    else relu_bwd_kernel<true><<<blocks_for(n), 256, 0, s>>>(dy, y, dz, B, H * W, c / 8);
     return cudaGetLastError();
 }
 cudaError_t pool_fwd(const View& in, const View& out, int B, int H, int W, int c, cudaStream_t s) {
     const size_t n = (size_t)B * (H / 2) * (W / 2) * (c / 8);
     if (!view_ok(in) || !view_ok(out) || !launch_ok(n, c)) return cudaErrorInvalidValue;
     if (n == 0) return cudaSuccess;
-    pool_fwd_kernel<<<blocks_for(n), 256, 0, s>>>(in, out, B, H, W, c / 8);
+    if (out.grp == 8) pool_fwd_kernel<false><<<blocks_for(n), 256, 0, s>>>(in, out, B, H, W, c / 8);
+    else pool_fwd_kernel<true><<<blocks_for(n), 256, 0, s>>>(in, out, B, H, W, c / 8);
     return cudaGetLastError();
 }
 cudaError_t pool_bwd(const View& dout, const View& din, int B, int H, int W, int c, int acc, cudaStream_t s) {
     const size_t n = (size_t)B * H * W * (c / 8);
     if (!view_ok(dout) || !view_ok(din) || !launch_ok(n, c)) return cudaErrorInvalidValue;
     if (n == 0) return cudaSuccess;
-    pool_bwd_kernel<<<blocks_for(n), 256, 0, s>>>(dout, din, B, H, W, c / 8, acc);
+    if (din.grp == 8) pool_bwd_kernel<false><<<blocks_for(n), 256, 0, s>>>(dout, din, B, H, W, c / 8, acc);
+    else pool_bwd_kernel<true><<<blocks_for(n), 256, 0, s>>>(dout, din, B, H, W, c / 8, acc);
     return cudaGetLastError();
 }
 cudaError_t up_fwd(const View& in, const View& out, int B, int H, int W, int c, cudaStream_t s) {
     const size_t n = (size_t)B * H * W * (c / 8);
     if (!view_ok(in) || !view_ok(out) || !launch_ok(n, c)) return cudaErrorInvalidValue;
     if (n == 0) return cudaSuccess;
-    up_fwd_kernel<<<blocks_for(n), 256, 0, s>>>(in, out, B, H, W, c / 8);
+    if (out.grp == 8) up_fwd_kernel<false><<<blocks_for(n), 256, 0, s>>>(in, out, B, H, W, c / 8);
+    else up_fwd_kernel<true><<<blocks_for(n), 256, 0, s>>>(in, out, B, H, W, c / 8);
     return cudaGetLastError();
 }
 cudaError_t up_bwd(const View& dout, const View& din, int B, int Hi, int Wi, int c, cudaStream_t s) {
     const size_t n = (size_t)B * Hi * Wi * (c / 8);
     if (!view_ok(dout) || !view_ok(din) || !launch_ok(n, c)) return cudaErrorInvalidValue;
     if (n == 0) return cudaSuccess;
-    up_bwd_kernel<<<blocks_for(n), 256, 0, s>>>(dout, din, B, Hi, Wi, c / 8);
+    if (din.grp == 8) up_bwd_kernel<false><<<blocks_for(n), 256, 0, s>>>(dout, din, B, Hi, Wi, c / 8);
+    else up_bwd_kernel<true><<<blocks_for(n), 256, 0, s>>>(dout, din, B, Hi, Wi, c / 8);
     return cudaGetLastError();
 }
 

@@ -132,19 +132,19 @@ cudaError_t Net::conv(int l, const View& x, const View& y, int B, int H, int W, 
     return conv_any(kCin[l], kCout[l], l == HEAD ? 1 : 0, a, s);
 }
 
-// Activations and gradients are channel-group planar ([B][C/8][H][W][8]); the
-// input features are NHWC [B][H][W][16].
+// Activations, gradients and the input features are NHWC; the decoder inputs
+// D1IN (96 channels) and D2IN (192) take the skip connections as channel slices.
 cudaError_t Net::forward(const bf16* feat, int B, int H, int W, cudaStream_t s) {
     const int H2 = H / 2, W2 = W / 2, H4 = H / 4, W4 = W / 4;
     cudaError_t e;
 #define NN_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
     const View f = nhwc_view(feat, 16, H, W);
-    const View e1a = planar_view(E1A_, 4, H, W), d1in = planar_view(D1IN, 12, H, W);
-    const View p1 = planar_view(P1, 4, H2, W2), e2a = planar_view(E2A_, 8, H2, W2);
-    const View d2in = planar_view(D2IN, 24, H2, W2), p2 = planar_view(P2_, 8, H4, W4);
-    const View b1 = planar_view(B1_, 16, H4, W4), b2 = planar_view(B2_, 16, H4, W4);
-    const View d2a = planar_view(D2A_, 8, H2, W2), d2b = planar_view(D2B_, 8, H2, W2);
-    const View d1a = planar_view(D1A_, 4, H, W), d1b = planar_view(D1B_, 4, H, W), lg = planar_view(LOG, 4, H, W);
+    const View e1a = nhwc_view(E1A_, 32, H, W), d1in = nhwc_view(D1IN, 96, H, W);
+    const View p1 = nhwc_view(P1, 32, H2, W2), e2a = nhwc_view(E2A_, 64, H2, W2);
+    const View d2in = nhwc_view(D2IN, 192, H2, W2), p2 = nhwc_view(P2_, 64, H4, W4);
+    const View b1 = nhwc_view(B1_, 128, H4, W4), b2 = nhwc_view(B2_, 128, H4, W4);
+    const View d2a = nhwc_view(D2A_, 64, H2, W2), d2b = nhwc_view(D2B_, 64, H2, W2);
+    const View d1a = nhwc_view(D1A_, 32, H, W), d1b = nhwc_view(D1B_, 32, H, W), lg = nhwc_view(LOG, 32, H, W);
     NN_TRY(conv(E1A, f, e1a, B, H, W, s));
     NN_TRY(conv(E1B, e1a, channel_slice(d1in, 64), B, H, W, s));
     NN_TRY(pool_fwd(channel_slice(d1in, 64), p1, B, H, W, 32, s));
@@ -164,15 +164,15 @@ cudaError_t Net::forward(const bf16* feat, int B, int H, int W, cudaStream_t s) 
     return cudaSuccess;
 }
 
-// Backward of layer l: dz = relu'(dy) (or dy for the head) into the planar
-// buffer dz_buf, weight / bias gradients from its input x, and (if dx.p) the
-// input gradient.
+// Backward of layer l: dz = relu'(dy) (or dy for the head) into the buffer
+// dz_buf, weight / bias gradients from its input x, and (if dx.p) the input
+// gradient.
 cudaError_t Net::layer_backward(int l, const View& x, const View& y, const View& dy, bf16* dz_buf, const View& dx,
                                 int B, int H, int W, cudaStream_t s) {
     cudaError_t e;
     View g = dy;
     if (l != HEAD) {
-        const View dz = planar_view(dz_buf, kCout[l] / 8, H, W);
+        const View dz = nhwc_view(dz_buf, kCout[l], H, W);
         NN_TRY(relu_bwd(dy, y, dz, kCout[l], B, H, W, s));
         g = dz;
         launches += 1;
@@ -193,9 +193,9 @@ cudaError_t Net::layer_backward(int l, const View& x, const View& y, const View&
 cudaError_t Net::backward(const bf16* feat, int B, int H, int W, cudaStream_t s) {
     const int H2 = H / 2, W2 = W / 2, H4 = H / 4, W4 = W / 4;
     cudaError_t e;
-    auto full = [&](bf16* p, int c) { return planar_view(p, c / 8, H, W); };
-    auto half = [&](bf16* p, int c) { return planar_view(p, c / 8, H2, W2); };
-    auto quarter = [&](bf16* p, int c) { return planar_view(p, c / 8, H4, W4); };
+    auto full = [&](bf16* p, int c) { return nhwc_view(p, c, H, W); };
+    auto half = [&](bf16* p, int c) { return nhwc_view(p, c, H2, W2); };
+    auto quarter = [&](bf16* p, int c) { return nhwc_view(p, c, H4, W4); };
     const View none{nullptr, 8, 8, 8};
     NN_TRY(cudaMemsetAsync(g32, 0, nparams * sizeof(float), s));
     // full resolution decoder: dLOGITS in GA
@@ -299,7 +299,7 @@ sgi_status sgi_nn_forward(sgi_nn* n, const void* features, const float* noisy, c
     cudaError_t e = n->net.forward((const __nv_bfloat16*)features, B, H, W, s);
     if (e != cudaSuccess) return nn_cuda(n, e, "forward");
     const sgi::nn::View none{nullptr, 8, 8, 8};
-    sgi::nn::ApplyArgs a{sgi::nn::planar_view(n->net.LOG, 4, H, W), (const float4*)noisy, (const float4*)prev, nullptr,
+    sgi::nn::ApplyArgs a{sgi::nn::nhwc_view(n->net.LOG, 32, H, W), (const float4*)noisy, (const float4*)prev, nullptr,
                          (float4*)out, none, nullptr, 0.0f, B, H, W};
     e = sgi::nn::kpcn_apply(a, s);
     n->net.launches += 1;
@@ -318,8 +318,8 @@ sgi_status sgi_nn_train_step(sgi_nn* n, const void* features, const float* noisy
     e = cudaMemsetAsync(net.loss_dev, 0, sizeof(float), s);
     if (e != cudaSuccess) return nn_cuda(n, e, "loss reset");
     const size_t P = (size_t)B * H * W;
-    sgi::nn::ApplyArgs a{sgi::nn::planar_view(net.LOG, 4, H, W), (const float4*)noisy, (const float4*)prev,
-                         (const float4*)target, nullptr, sgi::nn::planar_view(net.GA, 4, H, W), net.loss_dev,
+    sgi::nn::ApplyArgs a{sgi::nn::nhwc_view(net.LOG, 32, H, W), (const float4*)noisy, (const float4*)prev,
+                         (const float4*)target, nullptr, sgi::nn::nhwc_view(net.GA, 32, H, W), net.loss_dev,
                          1.0f / (3.0f * (float)P), B, H, W};
     e = sgi::nn::kpcn_apply(a, s);
     if (e != cudaSuccess) return nn_cuda(n, e, "apply/loss");

@@ -9,17 +9,19 @@
 // (y0 + r + ky - 1, x0 + m + kx - 1), channel k (zero outside the image) and
 // B_t[n][k] = w[n][t][k].
 //
-// Shared memory holds STAGES chunk buffers, each filled by two TMA loads:
-//   halo: box {8 channels, 130 pixels, R + 2 rows, 2 channel groups} of the input
-//       view (5-D map: channel in group, x, y, group, image) at (0, x0 - 1,
-//       y0 - 1, c0 / 8, b) -> [group][row][pixel][8 channels]; TMA writes zeros
-//       outside the image. A_{r,t} is then the canonical no-swizzle K-major
-//       operand starting at pixel (r + ky, kx): core matrices (8 pixels x 16
-//       bytes) 128 B apart along M, the two groups PLANE bytes apart. With the
-//       channel-group planar layout each box row is one contiguous 2080-byte run.
-//   weights: box {8 channels, COUT, 2 groups, 9 taps} of w viewed as
-//       [tap][group][n][8] -> B_t at tap * 2 * COUT * 16: core matrices 128 B
-//       apart along N, the two groups COUT * 16 B apart.
+// Shared memory holds STAGES chunk buffers of KC input channels (KC = 16 or 32),
+// each filled by two TMA loads with the 32- or 64-byte swizzle (a pixel's KC
+// channels are one swizzle row of 2 KC bytes):
+//   halo: box {KC channels, 130 pixels, R + 2 rows, 1} of the NHWC input view at
+//       (c0, x0 - 1, y0 - 1, b) -> [row][pixel][KC], zero-filled outside the
+//       image. A_{r,t} starts at pixel (r + ky, kx) of it: a K-major operand
+//       whose 8-row groups are 8 * 2 KC bytes apart (SBO); each 16-channel MMA
+//       step advances the start by 32 bytes. The tensor core applies the swizzle
+//       to absolute shared-memory addresses, as TMA does, so the start may sit at
+//       any pixel row (descriptor base offset 0).
+//   weights: box {KC channels, COUT, 9 taps} of w [COUT][9][CIN] -> [tap][n][KC];
+//       B_t starts at tap * COUT * 2 KC bytes.
+// Both buffers start on 1024-byte boundaries.
 // Roles (192 threads): warp 0 lane 0 issues the TMA loads of each chunk after
 // the MMAs of the chunk that used the buffer have completed (empty barrier,
 // tcgen05.commit); warp 1 lane 0 issues the 9 * R MMAs of each chunk when its
@@ -46,7 +48,6 @@ typedef __nv_bfloat16 bf16;
 
 constexpr int kTcM = 128;                    // pixels per tile row (MMA M)
 constexpr int kHaloPix = kTcM + 2;           // 130
-constexpr int kRowBytes = kHaloPix * 16;     // 2080: one halo row of one 8-channel group
 constexpr int kThreads = 192;
 constexpr unsigned long long kWaitNs = 200ull * 1000ull * 1000ull;   // bound on every wait
 constexpr int kSmemBudget = 220 * 1024;
@@ -56,20 +57,23 @@ __host__ __device__ constexpr int pow2_cols(int c) {
     return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
 }
 
-template <int COUT> struct TcShape {
-    static constexpr int R = COUT <= 64 ? 4 : (COUT <= 128 ? 2 : 1);   // output rows per tile
+template <int CIN, int COUT> struct TcShape {
+    static constexpr int KC = (COUT <= 64 && CIN % 32 == 0) ? 32 : 16;  // input channels per stage
+    static constexpr int ROWB = 2 * KC;                                   // bytes per pixel row
+    static constexpr uint32_t LAYOUT = KC == 32 ? 4u : 6u;               // descriptor: 64B / 32B swizzle
+    static constexpr int R = COUT == 32 ? 4 : (COUT <= 128 ? 2 : 1);     // output rows per tile
     static constexpr int HALO_ROWS = R + 2;
-    static constexpr int PLANE = HALO_ROWS * kRowBytes;                // one channel group of the halo
-    static constexpr int W_OFF = round_up(2 * PLANE, 128);
-    static constexpr int WBYTES = 9 * 2 * COUT * 16;
-    static constexpr int STAGE = round_up(W_OFF + WBYTES, 128);
+    static constexpr int HALO = HALO_ROWS * kHaloPix * ROWB;
+    static constexpr int W_OFF = round_up(HALO, 1024);
+    static constexpr int WBYTES = 9 * COUT * ROWB;
+    static constexpr int STAGE = round_up(W_OFF + WBYTES, 1024);
     static constexpr int STAGES = kSmemBudget / STAGE < 6 ? kSmemBudget / STAGE : 6;
     static constexpr int TMEM_COLS = pow2_cols(2 * R * COUT);          // two accumulator buffers
     static constexpr int BUF_COLS = TMEM_COLS / 2;
-    static constexpr uint32_t TX_BYTES = 2u * HALO_ROWS * kRowBytes + WBYTES;
+    static constexpr uint32_t TX_BYTES = HALO + WBYTES;
     static constexpr size_t SMEM =
-        (size_t)STAGES * STAGE + 128 /* alignment slack */ + 256 /* barriers */ + COUT * 4 /* bias */;
-    static_assert(STAGES >= 2, "stage ring");
+        (size_t)STAGES * STAGE + 1024 /* alignment slack */ + 256 /* barriers */ + COUT * 4 /* bias */;
+    static_assert(CIN % KC == 0 && STAGES >= 2, "stage ring");
     static_assert(R * COUT <= BUF_COLS, "accumulators");
 };
 
@@ -131,6 +135,15 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+
 __device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
                                             int c4, uint32_t bar) {
     asm volatile(
@@ -153,12 +166,12 @@ template <int CIN, int COUT, int MODE>
 __global__ void __launch_bounds__(kThreads, 1)
     conv3x3_tc_kernel(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_w,
                       ConvArgs a, TcTiles tl, int* err) {
-    using S = TcShape<COUT>;
-    constexpr int R = S::R, NCH = CIN / 16;
+    using S = TcShape<CIN, COUT>;
+    constexpr int R = S::R, KC = S::KC, NCH = CIN / KC;
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT >= 16 && COUT <= 256, "shape");
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem =
-        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     unsigned char* ctrl = smem + (size_t)S::STAGES * S::STAGE;
     uint64_t* full = reinterpret_cast<uint64_t*>(ctrl);            // [STAGES]
     uint64_t* empty = full + S::STAGES;                            // [STAGES]
@@ -214,8 +227,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                                  "r"(S::TX_BYTES)
                                  : "memory");
                     const uint32_t st = smem_base + s * S::STAGE;
-                    tma_load_5d(st, &map_x, 0, x0 - 1, y0 - 1, ch * 2, b, bar);
-                    tma_load_4d(st + S::W_OFF, &map_w, 0, 0, ch * 2, 0, bar);
+                    tma_load_4d(st, &map_x, ch * KC, x0 - 1, y0 - 1, b, bar);
+                    tma_load_3d(st + S::W_OFF, &map_w, ch * KC, 0, 0, bar);
                     if (++s == S::STAGES) { s = 0; ph ^= 1u; }
                 }
             }
@@ -226,11 +239,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) {
             constexpr uint32_t IDESC = instr_desc_bf16(kTcM, COUT);
             // Descriptors are split into a 32-bit low word (start address >> 4, leading
-            // byte offset >> 4) and a constant high word (stride byte offset >> 4,
-            // version 1). Every MMA of a chunk adds a compile-time offset to the low
-            // word of the stage's base descriptor, so the issue loop has no dependent
-            // address arithmetic.
-            constexpr uint32_t HI = (128u >> 4) | (1u << 14);
+            // byte offset field 1) and a constant high word (stride byte offset =
+            // 8 rows, version 1, swizzle mode). Every MMA of a chunk adds a
+            // compile-time offset to the low word of the stage's base descriptor.
+            constexpr uint32_t HI = (uint32_t)((8 * S::ROWB) >> 4) | (1u << 14) | (S::LAYOUT << 29);
             int s = 0, acc = 0;
             uint32_t ph = 0, aph = 0;
             bool ok = true, issued = false;
@@ -242,24 +254,28 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (!mbar_wait(s_addr(full + s), ph, abort_flag)) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                     const uint32_t st = smem_base + s * S::STAGE;
-                    const uint32_t a_lo = ((st >> 4) & 0x3FFFu) | ((uint32_t)(S::PLANE >> 4) << 16);
-                    const uint32_t b_lo = (((st + S::W_OFF) >> 4) & 0x3FFFu) | ((uint32_t)(COUT * 16 >> 4) << 16);
+                    const uint32_t a_lo = ((st >> 4) & 0x3FFFu) | (1u << 16);
+                    const uint32_t b_lo = (((st + S::W_OFF) >> 4) & 0x3FFFu) | (1u << 16);
                     const uint32_t first = ch > 0 ? 1u : 0u;
 #pragma unroll
                     for (int r = 0; r < R; ++r) {
 #pragma unroll
                         for (int tap = 0; tap < 9; ++tap) {
-                            const int ky = tap / 3, kx = tap % 3;
-                            const uint32_t a = a_lo + (uint32_t)(((r + ky) * kRowBytes + kx * 16) >> 4);
-                            const uint32_t b = b_lo + (uint32_t)((tap * 2 * COUT * 16) >> 4);
-                            const uint32_t accum = tap > 0 ? 1u : first;
-                            asm volatile(
-                                "{\n .reg .pred p;\n .reg .b64 ad, bd;\n setp.ne.b32 p, %5, 0;\n"
-                                " mov.b64 ad, {%1, %3};\n mov.b64 bd, {%2, %3};\n"
-                                " tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %4, p;\n}\n" ::"r"(
-                                    d0 + (uint32_t)(r * COUT)),
-                                "r"(a), "r"(b), "r"(HI), "r"(IDESC), "r"(accum)
-                                : "memory");
+#pragma unroll
+                            for (int ks = 0; ks < KC / 16; ++ks) {
+                                const int ky = tap / 3, kx = tap % 3;
+                                const uint32_t a =
+                                    a_lo + (uint32_t)((((r + ky) * kHaloPix + kx) * S::ROWB + ks * 32) >> 4);
+                                const uint32_t b = b_lo + (uint32_t)((tap * COUT * S::ROWB + ks * 32) >> 4);
+                                const uint32_t accum = (tap > 0 || ks > 0) ? 1u : first;
+                                asm volatile(
+                                    "{\n .reg .pred p;\n .reg .b64 ad, bd;\n setp.ne.b32 p, %5, 0;\n"
+                                    " mov.b64 ad, {%1, %3};\n mov.b64 bd, {%2, %3};\n"
+                                    " tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %4, p;\n}\n" ::"r"(
+                                        d0 + (uint32_t)(r * COUT)),
+                                    "r"(a), "r"(b), "r"(HI), "r"(IDESC), "r"(accum)
+                                    : "memory");
+                            }
                         }
                     }
                     issued = true;
@@ -391,27 +407,26 @@ static int sm_count() {
 
 template <int CIN, int COUT, int MODE>
 static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
-    using S = TcShape<COUT>;
+    using S = TcShape<CIN, COUT>;
     auto encode = encode_fn();
     if (!encode) return cudaErrorNotSupported;
+    const CUtensorMapSwizzle swz = S::KC == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
     CUtensorMap mx, mw;
     const cuuint32_t one[4] = {1, 1, 1, 1};
-    // input view: {8 channels, W, H, CIN / 8 groups, B}, box {8, 130, R + 2, 2, 1}
-    const cuuint64_t xdim[5] = {8, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)(CIN / 8), (cuuint64_t)a.B};
-    const cuuint64_t xstr[4] = {(cuuint64_t)a.x.pix * 2, (cuuint64_t)a.x.pix * a.W * 2, (cuuint64_t)a.x.grp * 2,
-                                (cuuint64_t)a.x.img * 2};
-    const cuuint32_t xbox[5] = {8, (cuuint32_t)kHaloPix, (cuuint32_t)S::HALO_ROWS, 2, 1};
-    const cuuint32_t one5[5] = {1, 1, 1, 1, 1};
-    if (encode(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void*)a.x.p, xdim, xstr, xbox, one5,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+    // NHWC input view: {CIN channels, W, H, B}, box {KC, 130, R + 2, 1}
+    const cuuint64_t xdim[4] = {(cuuint64_t)CIN, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.B};
+    const cuuint64_t xstr[3] = {(cuuint64_t)a.x.pix * 2, (cuuint64_t)a.x.pix * a.W * 2, (cuuint64_t)a.x.img * 2};
+    const cuuint32_t xbox[4] = {(cuuint32_t)S::KC, (cuuint32_t)kHaloPix, (cuuint32_t)S::HALO_ROWS, 1};
+    if (encode(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.x.p, xdim, xstr, xbox, one,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    // weights [COUT][9][CIN] viewed as {8 channels, COUT, CIN / 8 groups, 9 taps}, box {8, COUT, 2, 9}
-    const cuuint64_t wdim[4] = {8, (cuuint64_t)COUT, (cuuint64_t)(CIN / 8), 9};
-    const cuuint64_t wstr[3] = {(cuuint64_t)9 * CIN * 2, 16, (cuuint64_t)CIN * 2};
-    const cuuint32_t wbox[4] = {8, (cuuint32_t)COUT, 2, 9};
-    if (encode(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.w, wdim, wstr, wbox, one,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+    // weights [COUT][9][CIN] viewed as {CIN channels, COUT, 9 taps}, box {KC, COUT, 9}
+    const cuuint64_t wdim[3] = {(cuuint64_t)CIN, (cuuint64_t)COUT, 9};
+    const cuuint64_t wstr[2] = {(cuuint64_t)9 * CIN * 2, (cuuint64_t)CIN * 2};
+    const cuuint32_t wbox[3] = {(cuuint32_t)S::KC, (cuuint32_t)COUT, 9};
+    if (encode(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)a.w, wdim, wstr, wbox, one,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
     TcTiles tl;
@@ -431,8 +446,9 @@ static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
 }
 
 cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err, cudaStream_t s) {
-    // TMA: 16-byte aligned base addresses and strides; channel groups of 8 (16 bytes)
-    if (!err || !view_ok(a.x) || !view_ok(a.y) || (((uintptr_t)a.w) & 15) || a.B < 1 || a.H < 1 || a.W < 1)
+    // TMA: 16-byte aligned base addresses and strides; the input's channels contiguous (NHWC view)
+    if (!err || !view_ok(a.x) || !view_ok(a.y) || a.x.grp != 8 || (((uintptr_t)a.w) & 15) || a.B < 1 || a.H < 1 ||
+        a.W < 1)
         return cudaErrorInvalidValue;
 #define SGI_TC_CASE(CI, CO)                                                  \
     if (cin == CI && cout == CO) {                                           \

@@ -127,8 +127,9 @@ cudaError_t Net::conv_any(int cin, int cout, int mode, const ConvArgs& a, cudaSt
     return conv_path == SGI_NN_CONV_TCGEN05 ? conv3x3_tc(cin, cout, mode, a, dev_err, s) : conv3x3(cin, cout, mode, a, s);
 }
 
-cudaError_t Net::conv(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s) {
+cudaError_t Net::conv(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s, const View* pool) {
     ConvArgs a{x, wbf + w_off[l], w32 + b_off[l], y, B, H, W};
+    if (pool) a.pool = *pool;
     return conv_any(kCin[l], kCout[l], l == HEAD ? 1 : 0, a, s);
 }
 
@@ -144,7 +145,26 @@ cudaError_t Net::forward(const bf16* feat, int B, int H, int W, cudaStream_t s) 
     const View d2in = nhwc_view(D2IN, 192, H2, W2), p2 = nhwc_view(P2_, 64, H4, W4);
     const View b1 = nhwc_view(B1_, 128, H4, W4), b2 = nhwc_view(B2_, 128, H4, W4);
     const View d2a = nhwc_view(D2A_, 64, H2, W2), d2b = nhwc_view(D2B_, 64, H2, W2);
-    const View d1a = nhwc_view(D1A_, 32, H, W), d1b = nhwc_view(D1B_, 32, H, W), lg = nhwc_view(LOG, 32, H, W);
+    const View d1a = nhwc_view(D1A_, 32, H, W), d1b = nhwc_view(D1B_, 32, H, W);
+    const View lg = planar_view(LOG, 4, H, W);   // logits: planar, read per channel group by the kernel apply
+    if (conv_path == SGI_NN_CONV_TCGEN05) {
+        // the tensor-core epilogues of e1b and e2b also write the pooled copies
+        NN_TRY(conv(E1A, f, e1a, B, H, W, s));
+        NN_TRY(conv(E1B, e1a, channel_slice(d1in, 64), B, H, W, s, &p1));
+        NN_TRY(conv(E2A, p1, e2a, B, H2, W2, s));
+        NN_TRY(conv(E2B, e2a, channel_slice(d2in, 128), B, H2, W2, s, &p2));
+        NN_TRY(conv(B1, p2, b1, B, H4, W4, s));
+        NN_TRY(conv(B2, b1, b2, B, H4, W4, s));
+        NN_TRY(up_fwd(b2, d2in, B, H2, W2, 128, s));
+        NN_TRY(conv(D2A, d2in, d2a, B, H2, W2, s));
+        NN_TRY(conv(D2B, d2a, d2b, B, H2, W2, s));
+        NN_TRY(up_fwd(d2b, d1in, B, H, W, 64, s));
+        NN_TRY(conv(D1A, d1in, d1a, B, H, W, s));
+        NN_TRY(conv(D1B, d1a, d1b, B, H, W, s));
+        NN_TRY(conv(HEAD, d1b, lg, B, H, W, s));
+        launches += 13;
+        return cudaSuccess;
+    }
     NN_TRY(conv(E1A, f, e1a, B, H, W, s));
     NN_TRY(conv(E1B, e1a, channel_slice(d1in, 64), B, H, W, s));
     NN_TRY(pool_fwd(channel_slice(d1in, 64), p1, B, H, W, 32, s));
@@ -199,7 +219,8 @@ cudaError_t Net::backward(const bf16* feat, int B, int H, int W, cudaStream_t s)
     const View none{nullptr, 8, 8, 8};
     NN_TRY(cudaMemsetAsync(g32, 0, nparams * sizeof(float), s));
     // full resolution decoder: dLOGITS in GA
-    NN_TRY(layer_backward(HEAD, full(D1B_, 32), full(LOG, 32), full(GA, 32), nullptr, full(GB, 32), B, H, W, s));
+    NN_TRY(layer_backward(HEAD, full(D1B_, 32), planar_view(LOG, 4, H, W), full(GA, 32), nullptr, full(GB, 32), B, H,
+                          W, s));
     NN_TRY(layer_backward(D1B, full(D1A_, 32), full(D1B_, 32), full(GB, 32), GC, full(GA, 32), B, H, W, s));
     NN_TRY(layer_backward(D1A, full(D1IN, 96), full(D1A_, 32), full(GA, 32), GB, full(GD, 96), B, H, W, s));
     NN_TRY(up_bwd(full(GD, 96), half(GH1, 64), B, H2, W2, 64, s));                          // dD2B
@@ -299,7 +320,7 @@ sgi_status sgi_nn_forward(sgi_nn* n, const void* features, const float* noisy, c
     cudaError_t e = n->net.forward((const __nv_bfloat16*)features, B, H, W, s);
     if (e != cudaSuccess) return nn_cuda(n, e, "forward");
     const sgi::nn::View none{nullptr, 8, 8, 8};
-    sgi::nn::ApplyArgs a{sgi::nn::nhwc_view(n->net.LOG, 32, H, W), (const float4*)noisy, (const float4*)prev, nullptr,
+    sgi::nn::ApplyArgs a{sgi::nn::planar_view(n->net.LOG, 4, H, W), (const float4*)noisy, (const float4*)prev, nullptr,
                          (float4*)out, none, nullptr, 0.0f, B, H, W};
     e = sgi::nn::kpcn_apply(a, s);
     n->net.launches += 1;
@@ -318,7 +339,7 @@ sgi_status sgi_nn_train_step(sgi_nn* n, const void* features, const float* noisy
     e = cudaMemsetAsync(net.loss_dev, 0, sizeof(float), s);
     if (e != cudaSuccess) return nn_cuda(n, e, "loss reset");
     const size_t P = (size_t)B * H * W;
-    sgi::nn::ApplyArgs a{sgi::nn::nhwc_view(net.LOG, 32, H, W), (const float4*)noisy, (const float4*)prev,
+    sgi::nn::ApplyArgs a{sgi::nn::planar_view(net.LOG, 4, H, W), (const float4*)noisy, (const float4*)prev,
                          (const float4*)target, nullptr, sgi::nn::nhwc_view(net.GA, 32, H, W), net.loss_dev,
                          1.0f / (3.0f * (float)P), B, H, W};
     e = sgi::nn::kpcn_apply(a, s);

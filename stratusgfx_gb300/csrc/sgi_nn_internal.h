@@ -46,6 +46,9 @@ struct ConvArgs {
     const float* bias;        // [cout], unused in mode 2
     View y;
     int B, H, W;
+    // Optional extra output of the tensor-core path (p == nullptr: none): the 2x2
+    // mean of the BF16 y, an H/2 x W/2 view (COUT <= 64).
+    View pool;
 };
 
 struct WgradArgs {

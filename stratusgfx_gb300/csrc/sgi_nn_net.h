@@ -41,7 +41,8 @@ struct Net {
     cudaError_t init(const sgi_nn_config& c);
     cudaError_t set_params(const float* host, size_t n);
     cudaError_t conv_any(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t s);
-    cudaError_t conv(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s);
+    cudaError_t conv(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s,
+                     const View* pool = nullptr);
     cudaError_t forward(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);
     cudaError_t layer_backward(int l, const View& x, const View& y, const View& dy, __nv_bfloat16* dz_buf,
                                const View& dx, int B, int H, int W, cudaStream_t s);

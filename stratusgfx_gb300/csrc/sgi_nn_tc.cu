@@ -28,7 +28,11 @@
 // loads have landed (full barrier, complete_tx) and commits the finished tile
 // to a TMEM buffer (two buffers, so the epilogue of one tile overlaps the MMAs
 // of the next); warps 2..5 read the accumulators with tcgen05.ld (warp w owns
-// TMEM lanes 32 (w % 4) ...), add the bias, apply the ReLU and store BF16.
+// TMEM lanes 32 (w % 4) ...), add the bias, apply the ReLU and store BF16 —
+// optionally also the 2x2 mean (the next level's input), so no pooling pass
+// runs. (Writing the decoder's 2x upsampled copy from the epilogue as well was
+// slower than the separate upsampling kernel: four scattered 16-byte stores per
+// channel group.)
 // Every wait is bounded by the global timer: a role that gives up records an
 // error in *err and raises a shared abort flag that ends the other roles' waits.
 #include <cuda.h>
@@ -156,6 +160,20 @@ __device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
                  : "memory");
+}
+
+__device__ __forceinline__ void bf8_unpack(const uint4& v, float* f) {
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { const float2 t = __bfloat1622float2(h[j]); f[2 * j] = t.x; f[2 * j + 1] = t.y; }
+}
+
+__device__ __forceinline__ uint4 shfl_down_u4(uint4 v, int d) {
+    v.x = __shfl_down_sync(0xffffffffu, v.x, d);
+    v.y = __shfl_down_sync(0xffffffffu, v.y, d);
+    v.z = __shfl_down_sync(0xffffffffu, v.z, d);
+    v.w = __shfl_down_sync(0xffffffffu, v.w, d);
+    return v;
 }
 
 struct TcTiles {
@@ -304,6 +322,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (MODE != 2)
             for (int c = et; c < COUT; c += 128) bias_s[c] = a.bias[c];
         asm volatile("bar.sync 1, 128;\n" ::: "memory");   // epilogue warps only
+        // the fused 2x2 mean pairs rows (r, r + 1) of one thread and pixels of lanes (2j, 2j + 1)
+        constexpr bool CAN_POOL = (R % 2 == 0) && COUT <= 64;
+        const bool pooling = CAN_POOL && a.pool.p != nullptr;
+        uint4 held[CAN_POOL ? COUT / 8 : 1];
         int acc = 0;
         uint32_t aph = 0;
         for (int t = blockIdx.x; t < tl.total; t += gridDim.x) {
@@ -325,7 +347,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int r = 0; r < R; ++r) {
                 const int gy = ty * R + r;
                 const bool valid = px < a.W && gy < a.H;
-                bf16* yp = a.y.p + a.y.at(b, valid ? (size_t)gy * a.W + px : 0, 0);
+                const size_t pix = valid ? (size_t)gy * a.W + px : 0;
+                bf16* yp = a.y.p + a.y.at(b, pix, 0);
 #pragma unroll
                 for (int n0 = 0; n0 < COUT; n0 += 32) {
                     uint32_t v[32];
@@ -342,27 +365,49 @@ __global__ void __launch_bounds__(kThreads, 1)
                           "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                         : "r"(taddr));
                     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                    if (valid) {
 #pragma unroll
-                        for (int g = 0; g < 4; ++g) {
-                            float f[8];
+                    for (int g = 0; g < 4; ++g) {
+                        const int k = (n0 >> 3) + g;   // 8-channel group
+                        float f[8];
 #pragma unroll
-                            for (int j = 0; j < 8; ++j) f[j] = __uint_as_float(v[8 * g + j]);
-                            if (MODE != 2) {
-                                const float4 b0 = *reinterpret_cast<const float4*>(bias_s + n0 + 8 * g);
-                                const float4 b1 = *reinterpret_cast<const float4*>(bias_s + n0 + 8 * g + 4);
-                                f[0] += b0.x; f[1] += b0.y; f[2] += b0.z; f[3] += b0.w;
-                                f[4] += b1.x; f[5] += b1.y; f[6] += b1.z; f[7] += b1.w;
+                        for (int j = 0; j < 8; ++j) f[j] = __uint_as_float(v[8 * g + j]);
+                        if (MODE != 2) {
+                            const float4 b0 = *reinterpret_cast<const float4*>(bias_s + n0 + 8 * g);
+                            const float4 b1 = *reinterpret_cast<const float4*>(bias_s + n0 + 8 * g + 4);
+                            f[0] += b0.x; f[1] += b0.y; f[2] += b0.z; f[3] += b0.w;
+                            f[4] += b1.x; f[5] += b1.y; f[6] += b1.z; f[7] += b1.w;
+                        }
+                        uint4 o;
+                        __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            float f0 = f[2 * j], f1 = f[2 * j + 1];
+                            if (MODE == 0) { f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); }
+                            oh[j] = __floats2bfloat162_rn(f0, f1);
+                        }
+                        if (valid) *reinterpret_cast<uint4*>(yp + (size_t)k * (size_t)a.y.grp) = o;
+                        if (CAN_POOL && pooling) {
+                            if ((r & 1) == 0) {
+                                held[CAN_POOL ? k : 0] = o;
+                            } else {
+                                // mean of (r - 1, px), (r - 1, px + 1), (r, px), (r, px + 1), summed in that order
+                                const uint4 nh = shfl_down_u4(held[CAN_POOL ? k : 0], 1), nc = shfl_down_u4(o, 1);
+                                if (valid && (lane & 1) == 0) {
+                                    float a0[8], a1[8], a2[8], a3[8], pv[8];
+                                    bf8_unpack(held[CAN_POOL ? k : 0], a0);
+                                    bf8_unpack(nh, a1);
+                                    bf8_unpack(o, a2);
+                                    bf8_unpack(nc, a3);
+#pragma unroll
+                                    for (int j = 0; j < 8; ++j) pv[j] = 0.25f * (((a0[j] + a1[j]) + a2[j]) + a3[j]);
+                                    uint4 po;
+                                    __nv_bfloat162* ph2 = reinterpret_cast<__nv_bfloat162*>(&po);
+#pragma unroll
+                                    for (int j = 0; j < 4; ++j) ph2[j] = __floats2bfloat162_rn(pv[2 * j], pv[2 * j + 1]);
+                                    *reinterpret_cast<uint4*>(
+                                        a.pool.p + a.pool.at(b, (size_t)(gy / 2) * (a.W / 2) + px / 2, k)) = po;
+                                }
                             }
-                            uint4 o;
-                            __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
-#pragma unroll
-                            for (int j = 0; j < 4; ++j) {
-                                float f0 = f[2 * j], f1 = f[2 * j + 1];
-                                if (MODE == 0) { f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); }
-                                oh[j] = __floats2bfloat162_rn(f0, f1);
-                            }
-                            *reinterpret_cast<uint4*>(yp + (size_t)((n0 >> 3) + g) * (size_t)a.y.grp) = o;
                         }
                     }
                 }
@@ -408,6 +453,7 @@ static int sm_count() {
 template <int CIN, int COUT, int MODE>
 static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
     using S = TcShape<CIN, COUT>;
+    if (a.pool.p && (!view_ok(a.pool) || S::R % 2 != 0 || COUT > 64 || (a.H | a.W) & 1)) return cudaErrorInvalidValue;
     auto encode = encode_fn();
     if (!encode) return cudaErrorNotSupported;
     const CUtensorMapSwizzle swz = S::KC == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;

@@ -176,6 +176,18 @@ __device__ __forceinline__ uint4 shfl_down_u4(uint4 v, int d) {
     return v;
 }
 
+// 32 consecutive 32-bit TMEM columns of this warp's 32 lanes (one per thread).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+
 struct TcTiles {
     int tiles_x, tiles_y, total;
 };
@@ -427,6 +439,315 @@ __global__ void __launch_bounds__(kThreads, 1)
                      : "memory");
 }
 
+// ---------------------------------- 32 output channels: row streaming, ky in N
+//
+// With COUT = 32 an MMA of N = 32 costs about as much as one of N = 96 (both are
+// bounded by reading the 128-row A operand from shared memory), so the three
+// vertical taps share one MMA. For halo row h (an image row) the tensor core
+// accumulates
+//   E_h[m][ky * 32 + n] = sum over kx, k of X[h][x0 - 1 + m + kx][k] * W[n][ky][kx][k]
+// (A = halo row h from pixel kx, B = taps (0..2, kx) stacked along N = 96), and
+// output row y is E_{y-1}[ky 0] + E_y[ky 1] + E_{y+1}[ky 2]: the same TMEM lane
+// (pixel) in three buffers, so the epilogue only adds. A CTA walks strips of
+// 128 pixels x RS_ROWS rows from the top: each halo row is loaded once, its E
+// lives in a ring of five 96-column TMEM buffers, and output row y is written as
+// soon as E_{y+1} is complete. The weights of all taps and input channels
+// (at most 55 KB, [chunk][kx][ky][n][KC]) stay in shared memory.
+template <int CIN> struct RsShape {
+    static constexpr int COUT = 32, NX = 96;
+    static constexpr int KC = CIN % 32 == 0 ? 32 : 16;
+    static constexpr int ROWB = 2 * KC;
+    static constexpr uint32_t LAYOUT = KC == 32 ? 4u : 6u;
+    static constexpr int NCH = CIN / KC;
+    static constexpr int ROWS = 16;                                 // output rows per strip
+    static constexpr uint32_t ROW_TX = kHaloPix * ROWB;             // one halo row of one chunk
+    static constexpr int STAGE = round_up(kHaloPix * ROWB, 1024);
+    static constexpr int WCH = 9 * COUT * ROWB;                     // weights of one chunk
+    static constexpr int WBYTES = NCH * WCH;
+    static constexpr int ST_OFF = round_up(WBYTES, 1024);
+    static constexpr int STAGES = (kSmemBudget - ST_OFF) / STAGE < 16 ? (kSmemBudget - ST_OFF) / STAGE : 16;
+    static constexpr int NE = 5;                                    // TMEM ring of E buffers
+    static constexpr int TMEM_COLS = 512;
+    // at least 120 KB, so that one CTA (which holds all 512 TMEM columns) runs per SM
+    static constexpr size_t SMEM_USED = (size_t)ST_OFF + (size_t)STAGES * STAGE + 1024 + 512 + COUT * 4;
+    static constexpr size_t SMEM = SMEM_USED > 120 * 1024 ? SMEM_USED : 120 * 1024;
+    static_assert(CIN % KC == 0 && WCH % 1024 == 0 && STAGES >= 4, "shape");
+    static_assert(NE * NX <= TMEM_COLS, "tmem");
+};
+
+constexpr int kRsThreads = 352;   // producer, MMA issuer, 8 epilogue warps, second MMA issuer
+
+template <int CIN, int MODE>
+__global__ void __launch_bounds__(kRsThreads, 1)
+    conv3x3_rs_kernel(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_w,
+                      ConvArgs a, TcTiles tl, int* err) {
+    using S = RsShape<CIN>;
+    constexpr int COUT = 32, NX = S::NX, NE = S::NE, NCH = S::NCH, KC = S::KC;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    unsigned char* ctrl = smem + (size_t)S::ST_OFF + (size_t)S::STAGES * S::STAGE;
+    uint64_t* full = reinterpret_cast<uint64_t*>(ctrl);            // [STAGES]
+    uint64_t* empty = full + S::STAGES;                            // [STAGES]
+    uint64_t* efull = empty + S::STAGES;                           // [NE]
+    uint64_t* eempty = efull + NE;                                 // [NE]
+    uint64_t* wbar = eempty + NE;                                  // [1]
+    uint64_t* drain = wbar + 1;                                    // [2], one per MMA issuer
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 2);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    float* bias_s = reinterpret_cast<float*>(ctrl + 512);           // [COUT]
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_addr(tmem_slot)),
+                     "r"(S::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < S::STAGES; ++s) {
+            mbar_init(s_addr(full + s), 1);
+            mbar_init(s_addr(empty + s), 1);
+        }
+        for (int e = 0; e < NE; ++e) {
+            mbar_init(s_addr(efull + e), 1);
+            mbar_init(s_addr(eempty + e), 12);  // three reads x four epilogue warps
+        }
+        mbar_init(s_addr(wbar), 1);
+        mbar_init(s_addr(drain), 1);
+        mbar_init(s_addr(drain + 1), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_x)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_w)) : "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t smem_base = s_addr(smem);
+    const uint32_t stage_base = smem_base + S::ST_OFF;
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            // resident weights: one box {KC, 32 n, 3 ky, 3 kx} per chunk
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(s_addr(wbar)),
+                         "r"((uint32_t)S::WBYTES)
+                         : "memory");
+            for (int ch = 0; ch < NCH; ++ch)
+                tma_load_4d(smem_base + ch * S::WCH, &map_w, ch * KC, 0, 0, 0, s_addr(wbar));
+            int s = 0;
+            uint32_t ph = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
+                const int sx = t % tl.tiles_x, rest = t / tl.tiles_x;
+                const int sy = rest % tl.tiles_y, b = rest / tl.tiles_y;
+                const int x0 = sx * kTcM, yb = sy * S::ROWS;
+                const int nrows = min(S::ROWS, a.H - yb);
+                for (int i = 0; i < nrows + 2 && ok; ++i) {
+                    for (int ch = 0; ch < NCH; ++ch) {
+                        if (!mbar_wait(s_addr(empty + s), ph ^ 1u, abort_flag)) { ok = false; break; }
+                        const uint32_t bar = s_addr(full + s);
+                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+                                     "r"(S::ROW_TX)
+                                     : "memory");
+                        tma_load_4d(stage_base + s * S::STAGE, &map_x, ch * KC, x0 - 1, yb - 1 + i, b, bar);
+                        if (++s == S::STAGES) { s = 0; ph ^= 1u; }
+                    }
+                }
+            }
+            if (!ok) give_up(abort_flag, err);
+        }
+    } else if (warp == 1 || warp == 10) {
+        // ------------------------------------------------ MMA issuers
+        // Two threads on different schedulers issue the MMAs: warp 1 takes the even
+        // halo rows of the CTA's sequence, warp 10 the odd ones (an issuing thread
+        // spends more cycles on its control flow than a 6-MMA row keeps the tensor
+        // core busy). Each commits its own rows' stages and E buffers.
+        if (lane == 0) {
+            const unsigned who = warp == 1 ? 0u : 1u;
+            constexpr uint32_t IDESC = instr_desc_bf16(kTcM, NX);
+            constexpr uint32_t HI = (uint32_t)((8 * S::ROWB) >> 4) | (1u << 14) | (S::LAYOUT << 29);
+            // stage of this issuer's next chunk and E buffer of its next row, with their parities
+            int s = (int)(who * NCH) % S::STAGES;
+            uint32_t ph = (who * NCH) / S::STAGES;
+            int e = (int)who;
+            uint32_t eph = 0;
+            unsigned J = 0;   // running halo-row index of this CTA
+            bool ok = mbar_wait(s_addr(wbar), 0, abort_flag), issued = false;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t w_lo = ((smem_base >> 4) & 0x3FFFu) | (1u << 16);
+            for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
+                const int sy = (t / tl.tiles_x) % tl.tiles_y;
+                const int nh = min(S::ROWS, a.H - sy * S::ROWS) + 2;
+                for (int i = 0; i < nh && ok; ++i, ++J) {
+                    if ((J & 1u) != who) continue;
+                    if (!mbar_wait(s_addr(eempty + e), eph ^ 1u, abort_flag)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t d = tmem + (uint32_t)(e * NX);
+                    for (int ch = 0; ch < NCH; ++ch) {
+                        if (!mbar_wait(s_addr(full + s), ph, abort_flag)) { ok = false; break; }
+                        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                        const uint32_t a_lo = (((stage_base + s * S::STAGE) >> 4) & 0x3FFFu) | (1u << 16);
+                        const uint32_t b_lo = w_lo + (uint32_t)((ch * S::WCH) >> 4);
+#pragma unroll
+                        for (int kx = 0; kx < 3; ++kx) {
+#pragma unroll
+                            for (int ks = 0; ks < KC / 16; ++ks) {
+                                const uint32_t av = a_lo + (uint32_t)((kx * S::ROWB + ks * 32) >> 4);
+                                const uint32_t bv = b_lo + (uint32_t)((kx * NX * S::ROWB + ks * 32) >> 4);
+                                const uint32_t accum = (ch > 0 || kx > 0 || ks > 0) ? 1u : 0u;
+                                asm volatile(
+                                    "{\n .reg .pred p;\n .reg .b64 ad, bd;\n setp.ne.b32 p, %5, 0;\n"
+                                    " mov.b64 ad, {%1, %3};\n mov.b64 bd, {%2, %3};\n"
+                                    " tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %4, p;\n}\n" ::"r"(d),
+                                    "r"(av), "r"(bv), "r"(HI), "r"(IDESC), "r"(accum)
+                                    : "memory");
+                            }
+                        }
+                        issued = true;
+                        mma_commit(s_addr(empty + s));
+                        if (++s == S::STAGES) { s = 0; ph ^= 1u; }
+                    }
+                    if (!ok) break;
+                    mma_commit(s_addr(efull + e));
+                    // skip the other issuer's row: its NCH stages and its E buffer
+                    s += NCH;
+                    if (s >= S::STAGES) { s -= S::STAGES; ph ^= 1u; }
+                    e += 2;
+                    if (e >= NE) { e -= NE; eph ^= 1u; }
+                }
+            }
+            if (!ok) {
+                give_up(abort_flag, err);
+                if (issued) {
+                    mma_commit(s_addr(drain + who));
+                    const unsigned long long deadline = global_ns() + kWaitNs;
+                    while (!mbar_test(s_addr(drain + who), 0) && global_ns() < deadline) {
+                    }
+                }
+            }
+        }
+    } else {
+        // ------------------------------------------------ epilogue (warps 2..9)
+        // Two groups of four warps (one per TMEM lane quarter) take alternate pairs of
+        // output rows, so two rows are in flight per scheduler; a pair stays in one
+        // group because the fused pooling averages rows 2k and 2k + 1 in registers.
+        // E_h is read by output rows h - 1, h and h + 1; every E buffer collects
+        // 3 reads x 4 warps = 12 arrivals before the MMA reuses it (the strip's first
+        // and last rows add the arrivals of the missing neighbours).
+        const int q = warp & 3;
+        const int grp = (warp - 2) >> 2;
+        const int et = tid - 64;
+        if (MODE != 2)
+            for (int c = et; c < COUT; c += 256) bias_s[c] = a.bias[c];
+        asm volatile("bar.sync 1, 256;\n" ::: "memory");
+        const bool pooling = a.pool.p != nullptr;
+        uint4 held[4];
+        unsigned J0 = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
+            const int sx = t % tl.tiles_x, rest = t / tl.tiles_x;
+            const int sy = rest % tl.tiles_y, b = rest / tl.tiles_y;
+            const int yb = sy * S::ROWS;
+            const int nrows = min(S::ROWS, a.H - yb);
+            const int px = sx * kTcM + q * 32 + lane;
+            for (int r = 2 * grp; r < nrows && ok; r += (r & 1) ? 3 : 1) {
+                // r runs over this group's pairs: 2g, 2g + 1, 2g + 4, 2g + 5, ...
+                const unsigned J = J0 + r;   // output row yb + r: E_J ky 0, E_{J+1} ky 1, E_{J+2} ky 2
+                int ready = 0;
+                if (lane == 0)
+                    ready = (mbar_wait(s_addr(efull + J % NE), (J / NE) & 1u, abort_flag) &&
+                             mbar_wait(s_addr(efull + (J + 1) % NE), ((J + 1) / NE) & 1u, abort_flag) &&
+                             mbar_wait(s_addr(efull + (J + 2) % NE), ((J + 2) / NE) & 1u, abort_flag))
+                                ? 1
+                                : 0;
+                ready = __shfl_sync(0xffffffffu, ready, 0);
+                if (!ready) {
+                    if (lane == 0) give_up(abort_flag, err);
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t lanes = (uint32_t)(q * 32) << 16;
+                uint32_t v0[32], v1[32], v2[32];
+                tmem_ld32(tmem + lanes + (uint32_t)((J % NE) * NX + 0), v0);
+                tmem_ld32(tmem + lanes + (uint32_t)(((J + 1) % NE) * NX + 32), v1);
+                tmem_ld32(tmem + lanes + (uint32_t)(((J + 2) % NE) * NX + 64), v2);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+                __syncwarp();
+                if (lane == 0) {
+                    const uint32_t b0 = s_addr(eempty + J % NE), b1 = s_addr(eempty + (J + 1) % NE),
+                                   b2 = s_addr(eempty + (J + 2) % NE);
+                    const int n0 = 1 + (r == 0 ? 2 : 0);
+                    const int n1 = 1 + (r == 0 ? 1 : 0) + (r == nrows - 1 ? 1 : 0);
+                    const int n2 = 1 + (r == nrows - 1 ? 2 : 0);
+                    for (int k = 0; k < n0; ++k) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(b0) : "memory");
+                    for (int k = 0; k < n1; ++k) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(b1) : "memory");
+                    for (int k = 0; k < n2; ++k) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(b2) : "memory");
+                }
+                const int y = yb + r;
+                const bool valid = px < a.W;
+                bf16* yp = a.y.p + a.y.at(b, valid ? (size_t)y * a.W + px : 0, 0);
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    float f[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        f[j] = (__uint_as_float(v0[8 * g + j]) + __uint_as_float(v1[8 * g + j])) +
+                               __uint_as_float(v2[8 * g + j]);
+                    if (MODE != 2) {
+                        const float4 c0 = *reinterpret_cast<const float4*>(bias_s + 8 * g);
+                        const float4 c1 = *reinterpret_cast<const float4*>(bias_s + 8 * g + 4);
+                        f[0] += c0.x; f[1] += c0.y; f[2] += c0.z; f[3] += c0.w;
+                        f[4] += c1.x; f[5] += c1.y; f[6] += c1.z; f[7] += c1.w;
+                    }
+                    uint4 o;
+                    __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        float f0 = f[2 * j], f1 = f[2 * j + 1];
+                        if (MODE == 0) { f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); }
+                        oh[j] = __floats2bfloat162_rn(f0, f1);
+                    }
+                    if (valid) *reinterpret_cast<uint4*>(yp + (size_t)g * (size_t)a.y.grp) = o;
+                    if (pooling) {
+                        if ((y & 1) == 0) {
+                            held[g] = o;
+                        } else {
+                            const uint4 nh = shfl_down_u4(held[g], 1), nc = shfl_down_u4(o, 1);
+                            if (valid && (lane & 1) == 0) {
+                                float a0[8], a1[8], a2[8], a3[8], pv[8];
+                                bf8_unpack(held[g], a0);
+                                bf8_unpack(nh, a1);
+                                bf8_unpack(o, a2);
+                                bf8_unpack(nc, a3);
+#pragma unroll
+                                for (int j = 0; j < 8; ++j) pv[j] = 0.25f * (((a0[j] + a1[j]) + a2[j]) + a3[j]);
+                                uint4 po;
+                                __nv_bfloat162* ph2 = reinterpret_cast<__nv_bfloat162*>(&po);
+#pragma unroll
+                                for (int j = 0; j < 4; ++j) ph2[j] = __floats2bfloat162_rn(pv[2 * j], pv[2 * j + 1]);
+                                *reinterpret_cast<uint4*>(a.pool.p +
+                                                          a.pool.at(b, (size_t)(y / 2) * (a.W / 2) + px / 2, g)) = po;
+                            }
+                        }
+                    }
+                }
+            }
+            J0 += nrows + 2;
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::TMEM_COLS)
+                     : "memory");
+}
+
 // ---------------------------------------------------------------- host side
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -491,17 +812,68 @@ static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <int CIN, int MODE>
+static cudaError_t run_rs(const ConvArgs& a, int* err, cudaStream_t s) {
+    using S = RsShape<CIN>;
+    if (a.pool.p && (!view_ok(a.pool) || (a.H | a.W) & 1)) return cudaErrorInvalidValue;
+    auto encode = encode_fn();
+    if (!encode) return cudaErrorNotSupported;
+    const CUtensorMapSwizzle swz = S::KC == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+    CUtensorMap mx, mw;
+    const cuuint32_t one[4] = {1, 1, 1, 1};
+    // NHWC input view: {CIN channels, W, H, B}, box {KC, 130, 1 row, 1}
+    const cuuint64_t xdim[4] = {(cuuint64_t)CIN, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.B};
+    const cuuint64_t xstr[3] = {(cuuint64_t)a.x.pix * 2, (cuuint64_t)a.x.pix * a.W * 2, (cuuint64_t)a.x.img * 2};
+    const cuuint32_t xbox[4] = {(cuuint32_t)S::KC, (cuuint32_t)kHaloPix, 1, 1};
+    if (encode(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.x.p, xdim, xstr, xbox, one,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    // weights [32][ky][kx][CIN] viewed as {CIN channels, 32 n, 3 ky, 3 kx}, box {KC, 32, 3, 3} -> [kx][ky][n][KC]
+    const cuuint64_t wdim[4] = {(cuuint64_t)CIN, 32, 3, 3};
+    const cuuint64_t wstr[3] = {(cuuint64_t)9 * CIN * 2, (cuuint64_t)3 * CIN * 2, (cuuint64_t)CIN * 2};
+    const cuuint32_t wbox[4] = {(cuuint32_t)S::KC, 32, 3, 3};
+    if (encode(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.w, wdim, wstr, wbox, one,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    TcTiles tl;
+    tl.tiles_x = (a.W + kTcM - 1) / kTcM;
+    tl.tiles_y = (a.H + S::ROWS - 1) / S::ROWS;
+    const long long total = (long long)tl.tiles_x * tl.tiles_y * a.B;
+    if (total > 0x7fffffffLL) return cudaErrorInvalidValue;
+    tl.total = (int)total;
+    const int sms = sm_count();
+    if (sms <= 0) return cudaErrorInvalidDevice;
+    auto kern = conv3x3_rs_kernel<CIN, MODE>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+    if (e != cudaSuccess) return e;
+    const int grid = tl.total < sms ? tl.total : sms;
+    kern<<<grid, kRsThreads, S::SMEM, s>>>(mx, mw, a, tl, err);
+    return cudaGetLastError();
+}
+
+// 32-channel outputs take the row-streaming kernel, wider ones the 9-tap kernel.
+template <int CIN, int COUT>
+static cudaError_t run_shape(int mode, const ConvArgs& a, int* err, cudaStream_t s) {
+    if constexpr (COUT == 32) {
+        if (mode == 0) return run_rs<CIN, 0>(a, err, s);
+        if (mode == 1) return run_rs<CIN, 1>(a, err, s);
+        return run_rs<CIN, 2>(a, err, s);
+    } else {
+        if (mode == 0) return run_tc<CIN, COUT, 0>(a, err, s);
+        if (mode == 1) return run_tc<CIN, COUT, 1>(a, err, s);
+        return run_tc<CIN, COUT, 2>(a, err, s);
+    }
+}
+
 cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err, cudaStream_t s) {
     // TMA: 16-byte aligned base addresses and strides; the input's channels contiguous (NHWC view)
     if (!err || !view_ok(a.x) || !view_ok(a.y) || a.x.grp != 8 || (((uintptr_t)a.w) & 15) || a.B < 1 || a.H < 1 ||
         a.W < 1)
         return cudaErrorInvalidValue;
 #define SGI_TC_CASE(CI, CO)                                                  \
-    if (cin == CI && cout == CO) {                                           \
-        if (mode == 0) return run_tc<CI, CO, 0>(a, err, s);                  \
-        if (mode == 1) return run_tc<CI, CO, 1>(a, err, s);                  \
-        return run_tc<CI, CO, 2>(a, err, s);                                 \
-    }
+    if (cin == CI && cout == CO) return run_shape<CI, CO>(mode, a, err, s);
     SGI_TC_CASE(16, 32)
     SGI_TC_CASE(32, 32)
     SGI_TC_CASE(32, 64)

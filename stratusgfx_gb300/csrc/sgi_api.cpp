@@ -76,6 +76,11 @@ struct sgi_ctx {
     bool timing = false;
     cudaEvent_t ev[SGI_NUM_PASS_TIMES + 1] = {};
     bool have_times = false;
+
+    // direct lighting runs on a side stream, concurrently with the VPL and tile
+    // culls and the GI gather, and joins before the final composite
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 namespace {
@@ -157,6 +162,9 @@ void free_all(sgi_ctx* c) {
     void* nnp[] = {c->nn_feat, c->nn_noisy, c->nn_prev, c->nn_den};
     for (void* p : nnp) if (p) cudaFree(p);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    if (c->fork) cudaEventDestroy(c->fork);
+    if (c->join) cudaEventDestroy(c->join);
+    if (c->side) cudaStreamDestroy(c->side);
 }
 
 inline void record(sgi_ctx* c, int k, cudaStream_t s) {
@@ -249,6 +257,9 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     if (cfg->debug_keep_passes)
         for (int k = 0; k < cfg->denoise_passes; ++k) chk(dalloc(&c->pass_bufs[k], P));
     for (auto& ev : c->ev) chk(cudaEventCreate(&ev));
+    chk(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    chk(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+    chk(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
     if (e == cudaSuccess) chk(cudaMemset(c->visible_index, 0, sizeof(int32_t) * (1 + (size_t)cfg->max_vpls)));
     if (e == cudaSuccess) chk(cudaMemset(c->gi_hist[0], 0, P * sizeof(uint2)));
     if (e == cudaSuccess) chk(cudaMemset(c->gi_hist[1], 0, P * sizeof(uint2)));
@@ -392,7 +403,7 @@ static sgi_status run_gather(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_cam
 
 static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer* prev, const sgi_camera* cam,
                          const void* hdr_in, void* hdr_out, const sgi_frame_params* params, cudaStream_t s,
-                         int ev_gather) {
+                         int ev_gather, cudaEvent_t hdr_ready = nullptr) {
     const sgi_config& cfg = ctx->cfg;
     const bool keep = cfg.debug_keep_passes != 0;
     sgi_status st = run_gather(ctx, cur, cam, params, s);
@@ -420,6 +431,7 @@ static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer
     d.guide = ctx->guide;
     d.res_in = in;
     d.res_out = keep ? ctx->pass_bufs[cfg.denoise_passes - 1] : nullptr;
+    if (hdr_ready) SGI_CUDA(ctx, cudaStreamWaitEvent(s, hdr_ready, 0), "join direct lighting");
     SGI_CUDA(ctx, sgi::launch_denoise_final(d, s), "denoise_final");
     ctx->launches += 1;
     ctx->hist_cur = 1 - ctx->hist_cur;
@@ -449,19 +461,32 @@ sgi_status sgi_render_frame(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuf
     if (!frame_args_ok(cur, prev, cam, params) || !hdr_out)
         return fail(ctx, SGI_ERR_ARG, "NULL frame argument or frames_per_second <= 0");
     cudaStream_t s = (cudaStream_t)stream;
+    // Without per-pass timing the direct lighting overlaps the culls and the gather
+    // on the context's side stream (fork after the caller's prior work, join before
+    // the composite); with timing the passes run in sequence so each can be timed.
+    const bool overlap = !ctx->timing;
+    if (overlap) {
+        SGI_CUDA(ctx, cudaEventRecord(ctx->fork, s), "fork");
+        SGI_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->fork, 0), "fork");
+        sgi_status st0 = sgi_direct_lighting(ctx, cur, cam, ctx->direct, ctx->side);
+        if (st0 != SGI_OK) return st0;
+        SGI_CUDA(ctx, cudaEventRecord(ctx->join, ctx->side), "join");
+    }
     record(ctx, 0, s);
     sgi_status st = sgi_cull_vpls(ctx, stream);
     if (st != SGI_OK) return st;
     record(ctx, 1, s);
-    st = sgi_direct_lighting(ctx, cur, cam, ctx->direct, stream);
-    if (st != SGI_OK) return st;
+    if (!overlap) {
+        st = sgi_direct_lighting(ctx, cur, cam, ctx->direct, stream);
+        if (st != SGI_OK) return st;
+    }
     record(ctx, 2, s);
     if (ctx->cfg.gi_mode == SGI_GI_TILED) {
         st = sgi_cull_tiles(ctx, cur, cam, stream);
         if (st != SGI_OK) return st;
     }
     record(ctx, 3, s);
-    st = run_gi(ctx, cur, prev, cam, ctx->direct, hdr_out, params, s, 3);
+    st = run_gi(ctx, cur, prev, cam, ctx->direct, hdr_out, params, s, 3, overlap ? ctx->join : nullptr);
     if (st != SGI_OK) return st;
     record(ctx, 5, s);
     ctx->have_times = ctx->timing;
@@ -599,12 +624,22 @@ sgi_status sgi_render_frame_neural(sgi_ctx* ctx, sgi_nn* net, const sgi_gbuffer*
     sgi_status st = nn_buffers(ctx);
     if (st != SGI_OK) return st;
     cudaStream_t s = (cudaStream_t)stream;
+    const bool overlap = !ctx->timing;   // as in sgi_render_frame
+    if (overlap) {
+        SGI_CUDA(ctx, cudaEventRecord(ctx->fork, s), "fork");
+        SGI_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->fork, 0), "fork");
+        st = sgi_direct_lighting(ctx, cur, cam, ctx->direct, ctx->side);
+        if (st != SGI_OK) return st;
+        SGI_CUDA(ctx, cudaEventRecord(ctx->join, ctx->side), "join");
+    }
     record(ctx, 0, s);
     st = sgi_cull_vpls(ctx, stream);
     if (st != SGI_OK) return st;
     record(ctx, 1, s);
-    st = sgi_direct_lighting(ctx, cur, cam, ctx->direct, stream);
-    if (st != SGI_OK) return st;
+    if (!overlap) {
+        st = sgi_direct_lighting(ctx, cur, cam, ctx->direct, stream);
+        if (st != SGI_OK) return st;
+    }
     record(ctx, 2, s);
     if (ctx->cfg.gi_mode == SGI_GI_TILED) {
         st = sgi_cull_tiles(ctx, cur, cam, stream);
@@ -619,6 +654,7 @@ sgi_status sgi_render_frame_neural(sgi_ctx* ctx, sgi_nn* net, const sgi_gbuffer*
     st = sgi_nn_forward(net, ctx->nn_feat, (const float*)ctx->nn_noisy, (const float*)ctx->nn_prev, 1, H, W,
                         (float*)ctx->nn_den, stream);
     if (st != SGI_OK) return fail(ctx, st, std::string("denoiser: ") + sgi_nn_last_error(net));
+    if (overlap) SGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->join, 0), "join direct lighting");
     SGI_CUDA(ctx, sgi::nn::composite(ctx->nn_den, ctx->direct, cur->albedo, (uint2*)hdr_out,
                                      ctx->gi_hist[1 - ctx->hist_cur], ctx->hist_depth[1 - ctx->hist_cur],
                                      pixels(ctx->cfg), s), "kpcn_composite");

@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: the same 1080p workload with a 2-frame path, "
                          "--warmup + --steps frames of sgi_render_frame only (no e2e or CPU legs)")
+    ap.add_argument("--neural", action="store_true",
+                    help="with --profile: frames of sgi_render_frame_neural (K = 2) instead")
     return ap.parse_args()
 
 
@@ -556,14 +558,29 @@ def run_profile(args):
     sc = S.make_scene(1234 + 2, w.width, w.height, w.num_boxes, w.num_vpls, 2, vpl_radius=w.vpl_radius,
                       num_points=w.num_points, csm_resolution=w.csm_resolution)
     ds = stage.DeviceScene(sc, w)
-    st = stage.GiStage(stage.workload_config(w))
+    st = stage.GiStage(stage.workload_config(w, samples_per_pixel=2) if args.neural else stage.workload_config(w))
     st.set_lights(ds.vpls, ds.entries, ds.points)
     out = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
+    net = None
+    if args.neural:
+        import ctypes as C
+
+        from stratusgfx_gb300 import abi, denoiser
+        net = denoiser.KpcnDenoiser(1, w.height, w.width)
+        net.load(denoiser.WEIGHTS)
     for s in range(args.warmup + args.steps):
         k = s % 2 + 1
         st.set_shadow_maps(ds.csms[k], ds.cubes)
-        st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * s, 60.0)
+        if net is None:
+            st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * s, 60.0)
+        else:
+            fp = abi.FrameParams(1000.0 + 16.0 * s, 60.0)
+            abi.check(st.lib.sgi_render_frame_neural(st.ctx, net.h, C.byref(ds.gbuffers[k].struct()),
+                                                     C.byref(ds.gbuffers[k - 1].struct()), C.byref(ds.camera(k)),
+                                                     C.byref(fp), C.c_void_p(out.data_ptr()), None), st.ctx)
     torch.cuda.synchronize()
+    if net is not None:
+        net.close()
     print(json.dumps({"profile_case": w.name, "frames": args.warmup + args.steps,
                       "launches_per_frame": st.launch_count() // (args.warmup + args.steps)}))
     st.close()

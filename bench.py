@@ -468,21 +468,22 @@ def neural_vs_plain(args, ds, sc, w, cfg, flush):
                                                  stage._stream_ptr(None)), st.ctx)
 
     out = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
-    for name, render, ks in (("plain", plain_render, (8, 16, 32, 64)), ("neural", neural_render, (8, 4, 2))):
-        for K in ks:
-            kcfg = stage.workload_config(w, samples_per_pixel=K)
-            st = stage.GiStage(kcfg)
-            st.set_lights(ds.vpls, ds.entries, ds.points)
+    runs = [("plain", plain_render, f"K{K}", dict(samples_per_pixel=K)) for K in (8, 16, 32, 64)]
+    runs += [("neural", neural_render, f"K{K}", dict(samples_per_pixel=K)) for K in (8, 4, 2, 1)]
+    for name, render, label, kw in runs:
+        kcfg = stage.workload_config(w, **kw)
+        st = stage.GiStage(kcfg)
+        st.set_lights(ds.vpls, ds.entries, ds.points)
 
-            def one(k, s, st=st, render=render):
-                st.set_shadow_maps(ds.csms[k], ds.cubes)
-                render(st, k, out)
+        def one(k, s, st=st, render=render):
+            st.set_shadow_maps(ds.csms[k], ds.cubes)
+            render(st, k, out)
 
-            ms = time_frames(one, ds, frames, max(8, args.steps // 2), 3, flush)
-            st.close()
-            p_full, p_gi = psnr_vs_converged(render, ds, sc, w, kcfg, targets)
-            res[name][f"K{K}"] = {"ms_per_frame": round(ms, 4), "mpix_s": round(W * H / ms / 1e3, 1),
-                                  "psnr_db": p_full, "psnr_gi_db": p_gi}
+        ms = time_frames(one, ds, frames, max(8, args.steps // 2), 3, flush)
+        st.close()
+        p_full, p_gi = psnr_vs_converged(render, ds, sc, w, kcfg, targets)
+        res[name][label] = {"ms_per_frame": round(ms, 4), "mpix_s": round(W * H / ms / 1e3, 1),
+                            "psnr_db": p_full, "psnr_gi_db": p_gi}
     net.close()
     # Equal PSNR. The plain path's quality saturates with K (the a-trous filter's bias, not
     # the sample count, bounds its error against the converged frame), so the comparison is:

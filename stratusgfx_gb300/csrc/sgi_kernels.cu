@@ -342,28 +342,43 @@ SGI_D void bitonic_stage(uint32_t& k0, int& i0, uint32_t& k1, int& i1, int size,
     }
 }
 
-// 2a. keys: one thread per (tile, VPL), fully parallel; keys[tile][k] in
-// global memory (L2-resident), kNoKey when the VPL is not a candidate.
+// 2a. keys: a block takes kKeyTiles tiles; its threads stride over the visible
+// VPLs (the count lives on the device, so the grid cannot be sized by it), read
+// each VPL's position and radius once and write its key for every tile of the
+// block: keys[tile][k] in global memory (L2-resident), kNoKey when the VPL is
+// not a candidate. Reading the VPL records once per block instead of once per
+// tile cuts the L2 traffic of this pass by kKeyTiles.
+constexpr int kKeyTiles = 16;
 __global__ void __launch_bounds__(256) tile_keys_kernel(int num_tiles, int key_stride,
                                                         const sgi_tile_stage1* __restrict__ s1,
                                                         const sgi_vpl* __restrict__ cv,
                                                         const int32_t* __restrict__ visible_index,
                                                         uint32_t* __restrict__ keys) {
+    __shared__ float4 tile_p[kKeyTiles], tile_n[kKeyTiles];
     const int count = __ldg(visible_index);
-    const int k = blockIdx.y * blockDim.x + threadIdx.x;
-    const int tile = blockIdx.x;
-    if (k >= count || tile >= num_tiles) return;
-    const float4 p4 = __ldg(reinterpret_cast<const float4*>(s1 + tile));
-    const float4 n4 = __ldg(reinterpret_cast<const float4*>(s1 + tile) + 1);
-    const float* rec = reinterpret_cast<const float*>(cv + k);
-    const V3 lmf = v3(__ldg(rec + 0), __ldg(rec + 1), __ldg(rec + 2)) - v3(p4.x, p4.y, p4.z);
-    const float side = dot(v3(n4.x, n4.y, n4.z), lmf);
-    uint32_t u = kNoKey;
-    if (!(side < 0.0f)) {
-        const float ratio = length(lmf) / __ldg(rec + 12);
-        if (!(ratio > 1.0f) && ratio < kFloatMax) u = order_key(ratio);
+    const int t0 = blockIdx.x * kKeyTiles;
+    const int nt = min(kKeyTiles, num_tiles - t0);
+    if (threadIdx.x < nt) {
+        tile_p[threadIdx.x] = __ldg(reinterpret_cast<const float4*>(s1 + t0 + threadIdx.x));
+        tile_n[threadIdx.x] = __ldg(reinterpret_cast<const float4*>(s1 + t0 + threadIdx.x) + 1);
     }
-    keys[(size_t)tile * key_stride + k] = u;
+    __syncthreads();
+    for (int k = threadIdx.x; k < count; k += blockDim.x) {
+        const float* rec = reinterpret_cast<const float*>(cv + k);
+        const V3 lp = v3(__ldg(rec + 0), __ldg(rec + 1), __ldg(rec + 2));
+        const float radius = __ldg(rec + 12);
+        for (int j = 0; j < nt; ++j) {
+            const float4 p4 = tile_p[j], n4 = tile_n[j];
+            const V3 lmf = lp - v3(p4.x, p4.y, p4.z);
+            const float side = dot(v3(n4.x, n4.y, n4.z), lmf);
+            uint32_t u = kNoKey;
+            if (!(side < 0.0f)) {
+                const float ratio = length(lmf) / radius;
+                if (!(ratio > 1.0f) && ratio < kFloatMax) u = order_key(ratio);
+            }
+            keys[(size_t)(t0 + j) * key_stride + k] = u;
+        }
+    }
 }
 
 // 2b. select: one warp per tile over its keys.
@@ -479,8 +494,7 @@ cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1,
     const int ts = cfg.tile_size;
     const int T = ((cfg.width + ts - 1) / ts) * ((cfg.height + ts - 1) / ts);
     const int key_stride = (cfg.max_visible + 31) & ~31;
-    dim3 kgrid(T, (cfg.max_visible + 255) / 256);
-    tile_keys_kernel<<<kgrid, 256, 0, s>>>(T, key_stride, s1, cv, visible_index, keys);
+    tile_keys_kernel<<<(T + kKeyTiles - 1) / kKeyTiles, 256, 0, s>>>(T, key_stride, s1, cv, visible_index, keys);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     tile_select_kernel<<<(T + 7) / 8, 256, 0, s>>>(T, cfg.max_vpls_per_tile, key_stride, keys, visible_index, lists);

@@ -455,7 +455,12 @@ def neural_vs_plain(args, ds, sc, w, cfg, flush):
     H, W = w.height, w.width
     net = denoiser.KpcnDenoiser(1, H, W)
     net.load(denoiser.WEIGHTS)
-    res = {"plain": {}, "neural": {}}
+    # FP8 scales calibrated on a frame of another room (seed 777), not on the measured frames
+    calib = denoiser.make_dataset(1, H=H, W=W, frames_per_room=2, seed=777, samples=(2,), batches=1,
+                                  log=lambda *a: None)
+    net.calibrate_fp8(calib.feat[:1])
+    del calib
+    res = {"plain": {}, "neural": {}, "neural_fp8": {}}
 
     def plain_render(st, k, out):
         st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * k, 60.0)
@@ -470,7 +475,9 @@ def neural_vs_plain(args, ds, sc, w, cfg, flush):
     out = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
     runs = [("plain", plain_render, f"K{K}", dict(samples_per_pixel=K)) for K in (8, 16, 32, 64)]
     runs += [("neural", neural_render, f"K{K}", dict(samples_per_pixel=K)) for K in (8, 4, 2, 1)]
+    runs += [("neural_fp8", neural_render, f"K{K}", dict(samples_per_pixel=K)) for K in (8, 4, 2, 1)]
     for name, render, label, kw in runs:
+        net.set_precision(abi.SGI_NN_FP8 if name == "neural_fp8" else abi.SGI_NN_BF16)
         kcfg = stage.workload_config(w, **kw)
         st = stage.GiStage(kcfg)
         st.set_lights(ds.vpls, ds.entries, ds.points)
@@ -493,11 +500,13 @@ def neural_vs_plain(args, ds, sc, w, cfg, flush):
     plain_ref = min(((v["ms_per_frame"], k) for k, v in res["plain"].items() if v["psnr_gi_db"] >= best_plain - 0.1))
     eq = {"plain_best_gi_psnr_db": best_plain, "plain_config": plain_ref[1], "plain_ms": plain_ref[0],
           "plain_K8_gi_psnr_db": res["plain"]["K8"]["psnr_gi_db"], "plain_K8_ms": res["plain"]["K8"]["ms_per_frame"]}
-    ok = [(v["ms_per_frame"], k) for k, v in res["neural"].items() if v["psnr_gi_db"] >= best_plain]
+    ok = [(v["ms_per_frame"], f"{n}_{k}") for n in ("neural", "neural_fp8") for k, v in res[n].items()
+          if v["psnr_gi_db"] >= best_plain]
     if ok:
         nk = min(ok)[1]
+        prec, kk = nk.rsplit("_", 1)
         eq.update({"neural_config": nk, "neural_ms": min(ok)[0],
-                   "neural_gain_gi_db": round(res["neural"][nk]["psnr_gi_db"] - best_plain, 2),
+                   "neural_gain_gi_db": round(res[prec][kk]["psnr_gi_db"] - best_plain, 2),
                    "speedup_at_equal_or_better_psnr": round(plain_ref[0] / min(ok)[0], 3)})
     else:
         eq["neural_config"] = None

@@ -72,6 +72,18 @@ sgi_status sgi_nn_features(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_camer
 enum { SGI_NN_CONV_WARP_MMA = 0, SGI_NN_CONV_TCGEN05 = 1 };
 sgi_status sgi_nn_set_conv_path(sgi_nn* net, int32_t path);
 
+/* Inference precision of the convolutions: BF16 (default) or FP8 E4M3 with
+ * per-channel scales and FP32 accumulation (tcgen05 path only). FP8 needs a
+ * calibration after the last change of the weights (set_params, training). */
+enum { SGI_NN_BF16 = 0, SGI_NN_FP8 = 1 };
+sgi_status sgi_nn_set_precision(sgi_nn* net, int32_t precision);
+/* Runs the BF16 network on `features` (as for sgi_nn_forward), takes per-channel
+ * maxima of every tensor a convolution reads (scale = max / 448, the largest
+ * finite E4M3) and quantizes the weights per output channel with the input
+ * scales folded in. Synchronises the stream. */
+sgi_status sgi_nn_calibrate_fp8(sgi_nn* net, const void* features, int32_t batch, int32_t height, int32_t width,
+                                void* stream);
+
 /* Synchronises the device and reads (and clears) the network's error flag:
  * SGI_ERR_TIMEOUT when a tensor-core convolution gave up a bounded wait. */
 sgi_status sgi_nn_device_status(sgi_nn* net);

@@ -108,6 +108,8 @@ assert C.sizeof(Vpl) == 64 and C.sizeof(PointLight) == 48 and C.sizeof(AtlasEntr
 
 SGI_NN_CONV_WARP_MMA = 0
 SGI_NN_CONV_TCGEN05 = 1
+SGI_NN_BF16 = 0
+SGI_NN_FP8 = 1
 
 EXPORTS = {
     "sgi_abi_version": (C.c_int32, []),
@@ -148,6 +150,8 @@ EXPORTS = {
     "sgi_cull_vpls_noalloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(Csm), C.c_int32, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p]),
     "sgi_nn_set_conv_path": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "sgi_nn_set_precision": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "sgi_nn_calibrate_fp8": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "sgi_nn_device_status": (C.c_int32, [C.c_void_p]),
     "sgi_nn_conv3x3": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,

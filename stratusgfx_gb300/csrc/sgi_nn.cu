@@ -13,6 +13,7 @@
 // with A/B fragments loaded by ldmatrix.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -589,6 +590,93 @@ cudaError_t adam(float* w, const float* g, float* m, float* v, bf16* wb, size_t 
 __global__ void to_bf16_kernel(const float* __restrict__ w, bf16* __restrict__ wb, size_t n) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) wb[i] = __float2bfloat16(w[i]);
+}
+
+// ------------------------------------------------------------- FP8 E4M3 --
+// Per-channel |x| maxima of a BF16 view (calibration): out[c] = max over images
+// and pixels (out must start at zero; non-negative floats order as their bits).
+__global__ void channel_absmax_kernel(View v, int C, int B, int HW, float* __restrict__ out) {
+    const int c = blockIdx.y * 32 + (threadIdx.x & 31);
+    float m = 0.0f;
+    if (c < C) {
+        const size_t pixels = (size_t)B * HW;
+        for (size_t p = (size_t)blockIdx.x * 8 + (threadIdx.x >> 5); p < pixels; p += (size_t)gridDim.x * 8) {
+            const int b = (int)(p / HW);
+            m = fmaxf(m, fabsf(__bfloat162float(v.p[v.at(b, p - (size_t)b * HW, c / 8) + c % 8])));
+        }
+        atomicMax(reinterpret_cast<unsigned int*>(out + c), __float_as_uint(m));
+    }
+}
+
+cudaError_t channel_absmax(const View& v, int C, int B, int H, int W, float* out, cudaStream_t s) {
+    if (!view_ok(v)) return cudaErrorInvalidValue;
+    dim3 grid(128, (C + 31) / 32);
+    channel_absmax_kernel<<<grid, 256, 0, s>>>(v, C, B, H * W, out);
+    return cudaGetLastError();
+}
+
+// Weight quantization of one layer, one block per output channel n:
+// w'[t][k] = w[n][t][k] * s_in[k]; scale[n] = max |w'| / 448; q = E4M3(w' / scale[n]).
+__global__ void quantize_weights_kernel(const float* __restrict__ w, const float* __restrict__ s_in, int cin,
+                                        uint8_t* __restrict__ q, float* __restrict__ scale) {
+    __shared__ float red[256];
+    const int n = blockIdx.x, K = 9 * cin;
+    const float* wn = w + (size_t)n * K;
+    float m = 0.0f;
+    for (int i = threadIdx.x; i < K; i += blockDim.x) m = fmaxf(m, fabsf(wn[i] * s_in[i % cin]));
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + st]);
+        __syncthreads();
+    }
+    const float sc = red[0] > 0.0f ? red[0] / 448.0f : 1.0f;
+    if (threadIdx.x == 0) scale[n] = sc;
+    const float inv = 1.0f / sc;
+    for (int i = threadIdx.x; i < K; i += blockDim.x)
+        q[(size_t)n * K + i] =
+            (uint8_t)__nv_cvt_float_to_fp8(wn[i] * s_in[i % cin] * inv, __NV_SATFINITE, __NV_E4M3);
+}
+
+cudaError_t quantize_weights(const float* w, const float* s_in, int cin, int cout, uint8_t* q, float* scale,
+                             cudaStream_t s) {
+    quantize_weights_kernel<<<cout, 256, 0, s>>>(w, s_in, cin, q, scale);
+    return cudaGetLastError();
+}
+
+// BF16 NHWC tensor (C channels, C % 16 == 0) -> E4M3 with per-channel inverse scales;
+// the output is described by a BF16-unit view (two channels per unit).
+__global__ void quantize_act_kernel(View in, View out, int C, int B, int HW, const float* __restrict__ inv) {
+    const unsigned n = (unsigned)B * HW * (C / 16);
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int g = (int)(i % (C / 16));
+    const unsigned q = i / (C / 16);
+    const int b = (int)(q / HW);
+    const size_t pix = q - (size_t)b * HW;
+    float f[16];
+    bf8_to_f(*reinterpret_cast<const uint4*>(in.p + in.at(b, pix, 2 * g)), f);
+    bf8_to_f(*reinterpret_cast<const uint4*>(in.p + in.at(b, pix, 2 * g + 1)), f + 8);
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int c = 16 * g + 4 * j;
+        const __nv_fp8x2_storage_t lo =
+            __nv_cvt_float2_to_fp8x2(make_float2(f[4 * j] * inv[c], f[4 * j + 1] * inv[c + 1]), __NV_SATFINITE, __NV_E4M3);
+        const __nv_fp8x2_storage_t hi = __nv_cvt_float2_to_fp8x2(
+            make_float2(f[4 * j + 2] * inv[c + 2], f[4 * j + 3] * inv[c + 3]), __NV_SATFINITE, __NV_E4M3);
+        w[j] = (uint32_t)lo | ((uint32_t)hi << 16);
+    }
+    *reinterpret_cast<uint4*>(out.p + out.at(b, pix, g)) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+cudaError_t quantize_act(const View& in, const View& out, int C, int B, int H, int W, const float* inv,
+                         cudaStream_t s) {
+    const size_t n = (size_t)B * H * W * (C / 16);
+    if (!view_ok(in) || !view_ok(out) || C % 16 || n > 0xffffff00u) return cudaErrorInvalidValue;
+    if (n == 0) return cudaSuccess;
+    quantize_act_kernel<<<blocks_for(n), 256, 0, s>>>(in, out, C, B, H * W, inv);
+    return cudaGetLastError();
 }
 
 cudaError_t to_bf16(const float* w, bf16* wb, size_t n, cudaStream_t s) {

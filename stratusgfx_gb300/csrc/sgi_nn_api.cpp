@@ -96,6 +96,19 @@ cudaError_t Net::init(const sgi_nn_config& c) {
     chk(alloc(&GQ3, P4 * 64));
     chk(alloc(&fwd_out, P));
     chk(alloc(&dev_err, 1));
+    size_t sc = 0, in = 0;
+    for (int l = 0; l < NUM_LAYERS; ++l) {
+        sc_off[l] = sc;
+        sc += kCout[l];
+        in_off[l] = in;
+        in += kCin[l];
+    }
+    chk(alloc(&wq, nparams));
+    chk(alloc(&f8_wscale, sc));
+    chk(alloc(&f8_oinv, sc));
+    chk(alloc(&f8_sin, in));
+    chk(alloc(&f8_finv, 16));
+    chk(alloc(&f8_absmax, 11 * 128));
     if (e != cudaSuccess) return e;
     e = cudaMemset(dev_err, 0, sizeof(int));
     if (e != cudaSuccess) return e;
@@ -116,6 +129,7 @@ cudaError_t Net::init(const sgi_nn_config& c) {
 }
 
 cudaError_t Net::set_params(const float* host, size_t n) {
+    fp8_ready = false;   // new weights need a new FP8 calibration
     cudaError_t e = cudaMemcpy(w32, host, n * sizeof(float), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return e;
     e = to_bf16(w32, wbf, nparams, 0);
@@ -135,10 +149,116 @@ cudaError_t Net::conv(int l, const View& x, const View& y, int B, int H, int W, 
 
 // Activations, gradients and the input features are NHWC; the decoder inputs
 // D1IN (96 channels) and D2IN (192) take the skip connections as channel slices.
-cudaError_t Net::forward(const bf16* feat, int B, int H, int W, cudaStream_t s) {
+#define NN_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
+
+cudaError_t Net::conv8(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s, bool out8,
+                       const View* pool) {
+    ConvArgs a{x, reinterpret_cast<const bf16*>(wq + w_off[l]), w32 + b_off[l], y, B, H, W};
+    if (pool) a.pool = *pool;
+    a.wscale = f8_wscale + sc_off[l];
+    a.oinv = out8 ? f8_oinv + sc_off[l] : nullptr;
+    return conv3x3_tc_fp8(kCin[l], kCout[l], l == HEAD ? 1 : 0, out8, a, dev_err, s);
+}
+
+// FP8 E4M3 forward: the features are quantized with per-channel scales, every
+// convolution but the head writes E4M3 with the per-channel scales of its output
+// (folded into the next layer's weights), pooling and upsampling move E4M3 bytes
+// unchanged, and the head writes BF16 logits. FP8 tensors are BF16-unit views
+// with half the channel count (two E4M3 channels per unit).
+cudaError_t Net::forward_fp8(const bf16* feat, int B, int H, int W, cudaStream_t s) {
     const int H2 = H / 2, W2 = W / 2, H4 = H / 4, W4 = W / 4;
     cudaError_t e;
-#define NN_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
+    const View fb = nhwc_view(feat, 16, H, W), fq = nhwc_view(GA, 8, H, W);
+    const View e1a = nhwc_view(E1A_, 16, H, W), d1in = nhwc_view(D1IN, 48, H, W);
+    const View p1 = nhwc_view(P1, 16, H2, W2), e2a = nhwc_view(E2A_, 32, H2, W2);
+    const View d2in = nhwc_view(D2IN, 96, H2, W2), p2 = nhwc_view(P2_, 32, H4, W4);
+    const View b1 = nhwc_view(B1_, 64, H4, W4), b2 = nhwc_view(B2_, 64, H4, W4);
+    const View d2a = nhwc_view(D2A_, 32, H2, W2), d2b = nhwc_view(D2B_, 32, H2, W2);
+    const View d1a = nhwc_view(D1A_, 16, H, W), d1b = nhwc_view(D1B_, 16, H, W);
+    const View lg = planar_view(LOG, 4, H, W);
+    NN_TRY(quantize_act(fb, fq, 16, B, H, W, f8_finv, s));
+    NN_TRY(conv8(E1A, fq, e1a, B, H, W, s, true));
+    NN_TRY(conv8(E1B, e1a, channel_slice(d1in, 32), B, H, W, s, true, &p1));
+    NN_TRY(conv8(E2A, p1, e2a, B, H2, W2, s, true));
+    NN_TRY(conv8(E2B, e2a, channel_slice(d2in, 64), B, H2, W2, s, true, &p2));
+    NN_TRY(conv8(B1, p2, b1, B, H4, W4, s, true));
+    NN_TRY(conv8(B2, b1, b2, B, H4, W4, s, true));
+    NN_TRY(up_fwd(b2, d2in, B, H2, W2, 64, s));
+    NN_TRY(conv8(D2A, d2in, d2a, B, H2, W2, s, true));
+    NN_TRY(conv8(D2B, d2a, d2b, B, H2, W2, s, true));
+    NN_TRY(up_fwd(d2b, d1in, B, H, W, 32, s));
+    NN_TRY(conv8(D1A, d1in, d1a, B, H, W, s, true));
+    NN_TRY(conv8(D1B, d1a, d1b, B, H, W, s, true));
+    NN_TRY(conv8(HEAD, d1b, lg, B, H, W, s, false));
+    launches += 14;
+    return cudaSuccess;
+}
+
+// Calibration: the BF16 forward on `feat`, per-channel |x| maxima of every tensor a
+// convolution reads, scales = max / 448 (the largest finite E4M3), then the weights
+// quantized with the input scales folded in.
+cudaError_t Net::calibrate_fp8(const bf16* feat, int B, int H, int W, cudaStream_t s) {
+    const int H2 = H / 2, W2 = W / 2, H4 = H / 4, W4 = W / 4;
+    cudaError_t e;
+    const int saved = conv_path;
+    conv_path = SGI_NN_CONV_TCGEN05;
+    e = forward(feat, B, H, W, s, false);
+    conv_path = saved;
+    if (e != cudaSuccess) return e;
+    NN_TRY(cudaMemsetAsync(f8_absmax, 0, 11 * 128 * sizeof(float), s));
+    struct T { View v; int c, h, w; };
+    const T ts[11] = {{nhwc_view(feat, 16, H, W), 16, H, W},
+                      {nhwc_view(E1A_, 32, H, W), 32, H, W},
+                      {channel_slice(nhwc_view(D1IN, 96, H, W), 64), 32, H, W},
+                      {nhwc_view(E2A_, 64, H2, W2), 64, H2, W2},
+                      {channel_slice(nhwc_view(D2IN, 192, H2, W2), 128), 64, H2, W2},
+                      {nhwc_view(B1_, 128, H4, W4), 128, H4, W4},
+                      {nhwc_view(B2_, 128, H4, W4), 128, H4, W4},
+                      {nhwc_view(D2A_, 64, H2, W2), 64, H2, W2},
+                      {nhwc_view(D2B_, 64, H2, W2), 64, H2, W2},
+                      {nhwc_view(D1A_, 32, H, W), 32, H, W},
+                      {nhwc_view(D1B_, 32, H, W), 32, H, W}};
+    for (int t = 0; t < 11; ++t) NN_TRY(channel_absmax(ts[t].v, ts[t].c, B, ts[t].h, ts[t].w, f8_absmax + 128 * t, s));
+    std::vector<float> mx(11 * 128);
+    NN_TRY(cudaMemcpyAsync(mx.data(), f8_absmax, mx.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+    NN_TRY(cudaStreamSynchronize(s));
+    auto scale = [&](int t, int c) { const float m = mx[128 * t + c]; return m > 0.0f ? m / 448.0f : 1.0f; };
+    // tensors feeding each layer (index, channels); decoder inputs concatenate two tensors
+    const int in_t[NUM_LAYERS][2] = {{0, -1}, {1, -1}, {2, -1}, {3, -1}, {4, -1}, {5, -1},
+                                     {6, 4}, {7, -1}, {8, 2}, {9, -1}, {10, -1}};
+    const int out_t[NUM_LAYERS] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, -1};
+    std::vector<float> sin_h(in_off[NUM_LAYERS - 1] + kCin[NUM_LAYERS - 1]);
+    std::vector<float> oinv_h(sc_off[NUM_LAYERS - 1] + kCout[NUM_LAYERS - 1], 1.0f);
+    for (int l = 0; l < NUM_LAYERS; ++l) {
+        int k = 0;
+        for (int part = 0; part < 2 && in_t[l][part] >= 0; ++part) {
+            const int t = in_t[l][part];
+            for (int c = 0; c < ts[t].c; ++c) sin_h[in_off[l] + k++] = scale(t, c);
+        }
+        if (k != kCin[l]) return cudaErrorInvalidValue;
+        if (out_t[l] >= 0)
+            for (int c = 0; c < kCout[l]; ++c) oinv_h[sc_off[l] + c] = 1.0f / scale(out_t[l], c);
+    }
+    float finv_h[16];
+    for (int c = 0; c < 16; ++c) finv_h[c] = 1.0f / scale(0, c);
+    NN_TRY(cudaMemcpyAsync(f8_sin, sin_h.data(), sin_h.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    NN_TRY(cudaMemcpyAsync(f8_oinv, oinv_h.data(), oinv_h.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    NN_TRY(cudaMemcpyAsync(f8_finv, finv_h, sizeof(finv_h), cudaMemcpyHostToDevice, s));
+    for (int l = 0; l < NUM_LAYERS; ++l)
+        NN_TRY(quantize_weights(w32 + w_off[l], f8_sin + in_off[l], kCin[l], kCout[l], wq + w_off[l],
+                                f8_wscale + sc_off[l], s));
+    NN_TRY(cudaStreamSynchronize(s));
+    fp8_ready = true;
+    return cudaSuccess;
+}
+
+cudaError_t Net::forward(const bf16* feat, int B, int H, int W, cudaStream_t s, bool allow_fp8) {
+    if (allow_fp8 && precision == SGI_NN_FP8) {
+        if (!fp8_ready || conv_path != SGI_NN_CONV_TCGEN05) return cudaErrorNotReady;
+        return forward_fp8(feat, B, H, W, s);
+    }
+    const int H2 = H / 2, W2 = W / 2, H4 = H / 4, W4 = W / 4;
+    cudaError_t e;
     const View f = nhwc_view(feat, 16, H, W);
     const View e1a = nhwc_view(E1A_, 32, H, W), d1in = nhwc_view(D1IN, 96, H, W);
     const View p1 = nhwc_view(P1, 32, H2, W2), e2a = nhwc_view(E2A_, 64, H2, W2);
@@ -318,6 +438,7 @@ sgi_status sgi_nn_forward(sgi_nn* n, const void* features, const float* noisy, c
     if (!shape_ok(n, B, H, W)) return nn_fail(n, SGI_ERR_CAP, "batch/size exceed the network's capacity or H, W % 4");
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = n->net.forward((const __nv_bfloat16*)features, B, H, W, s);
+    if (e == cudaErrorNotReady) return nn_fail(n, SGI_ERR_STATE, "FP8 precision needs sgi_nn_calibrate_fp8 after the last weight change");
     if (e != cudaSuccess) return nn_cuda(n, e, "forward");
     const sgi::nn::View none{nullptr, 8, 8, 8};
     sgi::nn::ApplyArgs a{sgi::nn::planar_view(n->net.LOG, 4, H, W), (const float4*)noisy, (const float4*)prev, nullptr,
@@ -334,7 +455,7 @@ sgi_status sgi_nn_train_step(sgi_nn* n, const void* features, const float* noisy
     if (!shape_ok(n, B, H, W)) return nn_fail(n, SGI_ERR_CAP, "batch/size exceed the network's capacity or H, W % 4");
     cudaStream_t s = (cudaStream_t)stream;
     Net& net = n->net;
-    cudaError_t e = net.forward((const __nv_bfloat16*)features, B, H, W, s);
+    cudaError_t e = net.forward((const __nv_bfloat16*)features, B, H, W, s, false);
     if (e != cudaSuccess) return nn_cuda(n, e, "forward");
     e = cudaMemsetAsync(net.loss_dev, 0, sizeof(float), s);
     if (e != cudaSuccess) return nn_cuda(n, e, "loss reset");
@@ -348,6 +469,7 @@ sgi_status sgi_nn_train_step(sgi_nn* n, const void* features, const float* noisy
     if (e != cudaSuccess) return nn_cuda(n, e, "backward");
     if (apply_update) {
         n->step += 1;
+        net.fp8_ready = false;
         e = sgi::nn::adam(net.w32, net.g32, net.m32, net.v32, net.wbf, net.nparams, lr, 0.9f, 0.999f, 1e-8f, n->step, s);
         if (e != cudaSuccess) return nn_cuda(n, e, "adam");
     }
@@ -362,6 +484,19 @@ sgi_status sgi_nn_train_step(sgi_nn* n, const void* features, const float* noisy
         if (flag) return nn_fail(n, SGI_ERR_TIMEOUT, "a tensor-core convolution wait ran out");
         *loss_host = l / (3.0f * (float)P);
     }
+    return SGI_OK;
+}
+
+sgi_status sgi_nn_calibrate_fp8(sgi_nn* n, const void* features, int32_t B, int32_t H, int32_t W, void* stream) {
+    if (!n || !features) return nn_fail(n, SGI_ERR_ARG, "NULL tensor");
+    if (!shape_ok(n, B, H, W)) return nn_fail(n, SGI_ERR_CAP, "batch/size exceed the network's capacity or H, W % 4");
+    cudaError_t e = n->net.calibrate_fp8((const __nv_bfloat16*)features, B, H, W, (cudaStream_t)stream);
+    return e == cudaSuccess ? SGI_OK : nn_cuda(n, e, "fp8 calibration");
+}
+
+sgi_status sgi_nn_set_precision(sgi_nn* n, int32_t precision) {
+    if (!n || (precision != SGI_NN_BF16 && precision != SGI_NN_FP8)) return SGI_ERR_ARG;
+    n->net.precision = precision;
     return SGI_OK;
 }
 

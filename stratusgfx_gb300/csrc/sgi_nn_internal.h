@@ -47,8 +47,13 @@ struct ConvArgs {
     View y;
     int B, H, W;
     // Optional extra output of the tensor-core path (p == nullptr: none): the 2x2
-    // mean of the BF16 y, an H/2 x W/2 view (COUT <= 64).
+    // mean of y, an H/2 x W/2 view (COUT <= 64).
     View pool;
+    // FP8 path (conv3x3_tc_fp8): per-output-channel weight scales (the accumulator
+    // is multiplied by them) and, for FP8 outputs, the inverse per-channel scales
+    // of the output tensor.
+    const float* wscale;
+    const float* oinv;
 };
 
 struct WgradArgs {
@@ -94,6 +99,9 @@ cudaError_t conv3x3(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t
 // The same convolution on the 5th-generation tensor cores (sgi_nn_tc.cu); *err is
 // set to 1 when a bounded wait of a block ran out.
 cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err, cudaStream_t s);
+// FP8 E4M3 operands (x, w: one byte per channel, described by BF16-unit views with
+// two channels per unit); the output is FP8 (out8) or BF16.
+cudaError_t conv3x3_tc_fp8(int cin, int cout, int mode, bool out8, const ConvArgs& a, int* err, cudaStream_t s);
 cudaError_t flip_weights(const __nv_bfloat16* w, __nv_bfloat16* wt, int cin, int cout, cudaStream_t s);
 cudaError_t wgrad(const WgradArgs& a, cudaStream_t s);
 cudaError_t bias_grad(const View& dz, int c, int B, int H, int W, float* db, cudaStream_t s);
@@ -111,6 +119,12 @@ cudaError_t kpcn_apply(const ApplyArgs& a, cudaStream_t s);
 cudaError_t adam(float* w, const float* g, float* m, float* v, __nv_bfloat16* wb, size_t n, float lr, float b1,
                  float b2, float eps, int step, cudaStream_t s);
 cudaError_t to_bf16(const float* w, __nv_bfloat16* wb, size_t n, cudaStream_t s);
+// FP8 E4M3 support: calibration maxima, weight and activation quantization.
+cudaError_t channel_absmax(const View& v, int C, int B, int H, int W, float* out, cudaStream_t s);
+cudaError_t quantize_weights(const float* w, const float* s_in, int cin, int cout, uint8_t* q, float* scale,
+                             cudaStream_t s);
+cudaError_t quantize_act(const View& in, const View& out, int C, int B, int H, int W, const float* inv,
+                         cudaStream_t s);
 
 }  // namespace nn
 }  // namespace sgi

@@ -34,6 +34,14 @@ struct Net {
     float4* fwd_out = nullptr;
     int* dev_err = nullptr;   // set by a tcgen05 convolution whose wait ran out
     int conv_path = SGI_NN_CONV_TCGEN05;
+    // FP8 E4M3 inference (after calibrate_fp8): quantized weights (offsets w_off),
+    // per-output-channel weight scales and inverse output scales (offsets sc_off),
+    // per-input-channel scales folded into the weights (offsets in_off)
+    int precision = SGI_NN_BF16;
+    bool fp8_ready = false;
+    uint8_t* wq = nullptr;
+    float *f8_wscale = nullptr, *f8_oinv = nullptr, *f8_sin = nullptr, *f8_finv = nullptr, *f8_absmax = nullptr;
+    size_t sc_off[11] = {}, in_off[11] = {};
 
     ~Net();
     void release();
@@ -43,7 +51,11 @@ struct Net {
     cudaError_t conv_any(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t s);
     cudaError_t conv(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s,
                      const View* pool = nullptr);
-    cudaError_t forward(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);
+    cudaError_t forward(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s, bool allow_fp8 = true);
+    cudaError_t forward_fp8(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);
+    cudaError_t conv8(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s, bool out8,
+                      const View* pool = nullptr);
+    cudaError_t calibrate_fp8(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);
     cudaError_t layer_backward(int l, const View& x, const View& y, const View& dy, __nv_bfloat16* dz_buf,
                                const View& dx, int B, int H, int W, cudaStream_t s);
     cudaError_t backward(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);

@@ -37,6 +37,7 @@
 // error in *err and raises a shared abort flag that ends the other roles' waits.
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 #include <stdint.h>
@@ -61,10 +62,13 @@ __host__ __device__ constexpr int pow2_cols(int c) {
     return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
 }
 
-template <int CIN, int COUT> struct TcShape {
-    static constexpr int KC = (COUT <= 64 && CIN % 32 == 0) ? 32 : 16;  // input channels per stage
-    static constexpr int ROWB = 2 * KC;                                   // bytes per pixel row
-    static constexpr uint32_t LAYOUT = KC == 32 ? 4u : 6u;               // descriptor: 64B / 32B swizzle
+// F8: FP8 E4M3 operands (one byte per channel, 32 channels per MMA step) instead
+// of BF16 (two bytes, 16 channels); either way an MMA step reads 32 bytes of a row.
+template <int CIN, int COUT, bool F8 = false> struct TcShape {
+    static constexpr int ROWB = (COUT <= 64 && CIN % (F8 ? 64 : 32) == 0) ? 64 : 32;   // bytes per pixel row
+    static constexpr int KC = F8 ? ROWB : ROWB / 2;                       // input channels per stage
+    static constexpr int NCH = (CIN + KC - 1) / KC;                       // stages per tile (the last zero-padded)
+    static constexpr uint32_t LAYOUT = ROWB == 64 ? 4u : 6u;             // descriptor: 64B / 32B swizzle
     static constexpr int R = COUT == 32 ? 4 : (COUT <= 128 ? 2 : 1);     // output rows per tile
     static constexpr int HALO_ROWS = R + 2;
     static constexpr int HALO = HALO_ROWS * kHaloPix * ROWB;
@@ -75,9 +79,9 @@ template <int CIN, int COUT> struct TcShape {
     static constexpr int TMEM_COLS = pow2_cols(2 * R * COUT);          // two accumulator buffers
     static constexpr int BUF_COLS = TMEM_COLS / 2;
     static constexpr uint32_t TX_BYTES = HALO + WBYTES;
-    static constexpr size_t SMEM =
-        (size_t)STAGES * STAGE + 1024 /* alignment slack */ + 256 /* barriers */ + COUT * 4 /* bias */;
-    static_assert(CIN % KC == 0 && STAGES >= 2, "stage ring");
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE + 1024 /* alignment slack */ + 256 /* barriers */ +
+                                   3 * COUT * 4 /* bias, weight scales, output scales */;
+    static_assert(STAGES >= 2, "stage ring");
     static_assert(R * COUT <= BUF_COLS, "accumulators");
 };
 
@@ -95,9 +99,30 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
-// Instruction descriptor of kind::f16: BF16 A and B (both K-major), FP32 D, M x N.
-__host__ __device__ constexpr uint32_t instr_desc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor, FP32 D, both operands K-major, M x N: kind::f16 with BF16
+// A and B, or kind::f8f6f4 with E4M3 A and B (format code 0).
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N, bool f8) {
+    return (1u << 4) | (f8 ? 0u : (1u << 7) | (1u << 10)) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// One MMA from descriptor low words a, b (shared high word hi): D (+)= A * B^T.
+template <bool F8>
+__device__ __forceinline__ void umma(uint32_t d, uint32_t a, uint32_t b, uint32_t hi, uint32_t idesc, uint32_t accum) {
+    if constexpr (F8) {
+        asm volatile(
+            "{\n .reg .pred p;\n .reg .b64 ad, bd;\n setp.ne.b32 p, %5, 0;\n"
+            " mov.b64 ad, {%1, %3};\n mov.b64 bd, {%2, %3};\n"
+            " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], ad, bd, %4, p;\n}\n" ::"r"(d),
+            "r"(a), "r"(b), "r"(hi), "r"(idesc), "r"(accum)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n .reg .pred p;\n .reg .b64 ad, bd;\n setp.ne.b32 p, %5, 0;\n"
+            " mov.b64 ad, {%1, %3};\n mov.b64 bd, {%2, %3};\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %4, p;\n}\n" ::"r"(d),
+            "r"(a), "r"(b), "r"(hi), "r"(idesc), "r"(accum)
+            : "memory");
+    }
 }
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
@@ -176,6 +201,16 @@ __device__ __forceinline__ uint4 shfl_down_u4(uint4 v, int d) {
     return v;
 }
 
+// 16 consecutive 32-bit TMEM columns of this warp's 32 lanes (one per thread).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+}
+
 // 32 consecutive 32-bit TMEM columns of this warp's 32 lanes (one per thread).
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v) {
     asm volatile(
@@ -188,16 +223,118 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v) {
         : "r"(taddr));
 }
 
+// Epilogue of NC (16 or 32) output channels n0 .. n0 + NC - 1 of one pixel: f holds
+// the FP32 accumulators; they are scaled (F8: by the weights' per-channel scale),
+// biased, passed through the ReLU (mode 0) and packed into NC / 16 vectors of 16
+// FP8 channels (OUT8, multiplied by the next layer's per-channel inverse scale) or
+// NC / 8 vectors of 8 BF16 channels.
+template <int NC, int MODE, bool F8, bool OUT8>
+__device__ __forceinline__ void epilogue_n(float* f, int n0, const float* bias_s, const float* ws_s,
+                                           const float* oinv_s, uint4* out) {
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        float x = f[j];
+        if (F8) x *= ws_s[n0 + j];
+        if (MODE != 2) x += bias_s[n0 + j];
+        if (MODE == 0) x = fmaxf(x, 0.0f);
+        f[j] = x;
+    }
+    if constexpr (OUT8) {
+#pragma unroll
+        for (int v = 0; v < NC / 16; ++v) {
+            uint32_t w[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = 16 * v + 4 * j;
+                const __nv_fp8x2_storage_t lo = __nv_cvt_float2_to_fp8x2(
+                    make_float2(f[c] * oinv_s[n0 + c], f[c + 1] * oinv_s[n0 + c + 1]), __NV_SATFINITE, __NV_E4M3);
+                const __nv_fp8x2_storage_t hi = __nv_cvt_float2_to_fp8x2(
+                    make_float2(f[c + 2] * oinv_s[n0 + c + 2], f[c + 3] * oinv_s[n0 + c + 3]), __NV_SATFINITE,
+                    __NV_E4M3);
+                w[j] = (uint32_t)lo | ((uint32_t)hi << 16);
+            }
+            out[v] = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < NC / 8; ++v) {
+            uint4 o;
+            __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) oh[j] = __floats2bfloat162_rn(f[8 * v + 2 * j], f[8 * v + 2 * j + 1]);
+            out[v] = o;
+        }
+    }
+}
+
+// FP8 E4M3 x 16 -> float
+__device__ __forceinline__ void fp8x16_unpack(const uint4& v, float* f) {
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const __half2_raw r = __nv_cvt_fp8x2_to_halfraw2((__nv_fp8x2_storage_t)(w[j] >> (16 * h)), __NV_E4M3);
+            __half2 hh;
+            hh = *reinterpret_cast<const __half2*>(&r);
+            const float2 t = __half22float2(hh);
+            f[4 * j + 2 * h] = t.x;
+            f[4 * j + 2 * h + 1] = t.y;
+        }
+    }
+}
+
+// 2x2 mean of four packed vectors, summed in the order given, re-packed in the same format
+// (an FP8 mean keeps the per-channel scale of its inputs).
+template <bool OUT8>
+__device__ __forceinline__ uint4 mean4(const uint4& a, const uint4& b, const uint4& c, const uint4& d) {
+    if constexpr (OUT8) {
+        float a0[16], a1[16], a2[16], a3[16];
+        fp8x16_unpack(a, a0);
+        fp8x16_unpack(b, a1);
+        fp8x16_unpack(c, a2);
+        fp8x16_unpack(d, a3);
+        uint32_t w[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float m[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int k = 4 * j + i;
+                m[i] = 0.25f * (((a0[k] + a1[k]) + a2[k]) + a3[k]);
+            }
+            const __nv_fp8x2_storage_t lo = __nv_cvt_float2_to_fp8x2(make_float2(m[0], m[1]), __NV_SATFINITE, __NV_E4M3);
+            const __nv_fp8x2_storage_t hi = __nv_cvt_float2_to_fp8x2(make_float2(m[2], m[3]), __NV_SATFINITE, __NV_E4M3);
+            w[j] = (uint32_t)lo | ((uint32_t)hi << 16);
+        }
+        return make_uint4(w[0], w[1], w[2], w[3]);
+    } else {
+        float a0[8], a1[8], a2[8], a3[8], pv[8];
+        bf8_unpack(a, a0);
+        bf8_unpack(b, a1);
+        bf8_unpack(c, a2);
+        bf8_unpack(d, a3);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) pv[j] = 0.25f * (((a0[j] + a1[j]) + a2[j]) + a3[j]);
+        uint4 po;
+        __nv_bfloat162* ph2 = reinterpret_cast<__nv_bfloat162*>(&po);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ph2[j] = __floats2bfloat162_rn(pv[2 * j], pv[2 * j + 1]);
+        return po;
+    }
+}
+
 struct TcTiles {
     int tiles_x, tiles_y, total;
 };
 
-template <int CIN, int COUT, int MODE>
+template <int CIN, int COUT, int MODE, bool F8, bool OUT8>
 __global__ void __launch_bounds__(kThreads, 1)
     conv3x3_tc_kernel(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_w,
                       ConvArgs a, TcTiles tl, int* err) {
-    using S = TcShape<CIN, COUT>;
-    constexpr int R = S::R, KC = S::KC, NCH = CIN / KC;
+    using S = TcShape<CIN, COUT, F8>;
+    constexpr int R = S::R, KC = S::KC, NCH = S::NCH;
+    constexpr int NV = OUT8 ? 2 : 4;   // output vectors per 32 channels
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT >= 16 && COUT <= 256, "shape");
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem =
@@ -211,6 +348,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     float* bias_s = reinterpret_cast<float*>(ctrl + 256);            // [COUT]
+    float* ws_s = bias_s + COUT;                                     // [COUT] weight scales (F8)
+    float* oinv_s = ws_s + COUT;                                     // [COUT] output inverse scales (OUT8)
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 1) {
@@ -267,7 +406,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
-            constexpr uint32_t IDESC = instr_desc_bf16(kTcM, COUT);
+            constexpr uint32_t IDESC = instr_desc(kTcM, COUT, F8);
             // Descriptors are split into a 32-bit low word (start address >> 4, leading
             // byte offset field 1) and a constant high word (stride byte offset =
             // 8 rows, version 1, swizzle mode). Every MMA of a chunk adds a
@@ -292,19 +431,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                         for (int tap = 0; tap < 9; ++tap) {
 #pragma unroll
-                            for (int ks = 0; ks < KC / 16; ++ks) {
+                            for (int ks = 0; ks < S::ROWB / 32; ++ks) {
                                 const int ky = tap / 3, kx = tap % 3;
                                 const uint32_t a =
                                     a_lo + (uint32_t)((((r + ky) * kHaloPix + kx) * S::ROWB + ks * 32) >> 4);
                                 const uint32_t b = b_lo + (uint32_t)((tap * COUT * S::ROWB + ks * 32) >> 4);
                                 const uint32_t accum = (tap > 0 || ks > 0) ? 1u : first;
-                                asm volatile(
-                                    "{\n .reg .pred p;\n .reg .b64 ad, bd;\n setp.ne.b32 p, %5, 0;\n"
-                                    " mov.b64 ad, {%1, %3};\n mov.b64 bd, {%2, %3};\n"
-                                    " tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %4, p;\n}\n" ::"r"(
-                                        d0 + (uint32_t)(r * COUT)),
-                                    "r"(a), "r"(b), "r"(HI), "r"(IDESC), "r"(accum)
-                                    : "memory");
+                                umma<F8>(d0 + (uint32_t)(r * COUT), a, b, HI, IDESC, accum);
                             }
                         }
                     }
@@ -331,13 +464,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ------------------------------------------------ epilogue (warps 2..5)
         const int q = warp & 3;   // TMEM lane quarter of this warp
         const int et = tid - 64;  // 0..127
-        if (MODE != 2)
-            for (int c = et; c < COUT; c += 128) bias_s[c] = a.bias[c];
+        for (int c = et; c < COUT; c += 128) {
+            if (MODE != 2) bias_s[c] = a.bias[c];
+            if (F8) ws_s[c] = a.wscale[c];
+            if (OUT8) oinv_s[c] = a.oinv[c];
+        }
         asm volatile("bar.sync 1, 128;\n" ::: "memory");   // epilogue warps only
         // the fused 2x2 mean pairs rows (r, r + 1) of one thread and pixels of lanes (2j, 2j + 1)
         constexpr bool CAN_POOL = (R % 2 == 0) && COUT <= 64;
         const bool pooling = CAN_POOL && a.pool.p != nullptr;
-        uint4 held[CAN_POOL ? COUT / 8 : 1];
+        uint4 held[CAN_POOL ? COUT / 32 * NV : 1];
         int acc = 0;
         uint32_t aph = 0;
         for (int t = blockIdx.x; t < tl.total; t += gridDim.x) {
@@ -364,61 +500,27 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                 for (int n0 = 0; n0 < COUT; n0 += 32) {
                     uint32_t v[32];
-                    const uint32_t taddr =
-                        tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * S::BUF_COLS + r * COUT + n0);
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-                        "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
-                        "%30, %31}, [%32];\n"
-                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-                          "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]),
-                          "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
-                          "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                        : "r"(taddr));
+                    tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * S::BUF_COLS + r * COUT + n0), v);
                     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    float f[32];
 #pragma unroll
-                    for (int g = 0; g < 4; ++g) {
-                        const int k = (n0 >> 3) + g;   // 8-channel group
-                        float f[8];
+                    for (int j = 0; j < 32; ++j) f[j] = __uint_as_float(v[j]);
+                    uint4 o[NV];
+                    epilogue_n<32, MODE, F8, OUT8>(f, n0, bias_s, ws_s, oinv_s, o);
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) f[j] = __uint_as_float(v[8 * g + j]);
-                        if (MODE != 2) {
-                            const float4 b0 = *reinterpret_cast<const float4*>(bias_s + n0 + 8 * g);
-                            const float4 b1 = *reinterpret_cast<const float4*>(bias_s + n0 + 8 * g + 4);
-                            f[0] += b0.x; f[1] += b0.y; f[2] += b0.z; f[3] += b0.w;
-                            f[4] += b1.x; f[5] += b1.y; f[6] += b1.z; f[7] += b1.w;
-                        }
-                        uint4 o;
-                        __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            float f0 = f[2 * j], f1 = f[2 * j + 1];
-                            if (MODE == 0) { f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); }
-                            oh[j] = __floats2bfloat162_rn(f0, f1);
-                        }
-                        if (valid) *reinterpret_cast<uint4*>(yp + (size_t)k * (size_t)a.y.grp) = o;
+                    for (int g = 0; g < NV; ++g) {
+                        const int k = n0 / (OUT8 ? 16 : 8) + g;   // 16-byte vector of the pixel
+                        if (valid) *reinterpret_cast<uint4*>(yp + (size_t)k * (size_t)a.y.grp) = o[g];
                         if (CAN_POOL && pooling) {
                             if ((r & 1) == 0) {
-                                held[CAN_POOL ? k : 0] = o;
+                                held[CAN_POOL ? k : 0] = o[g];
                             } else {
                                 // mean of (r - 1, px), (r - 1, px + 1), (r, px), (r, px + 1), summed in that order
-                                const uint4 nh = shfl_down_u4(held[CAN_POOL ? k : 0], 1), nc = shfl_down_u4(o, 1);
-                                if (valid && (lane & 1) == 0) {
-                                    float a0[8], a1[8], a2[8], a3[8], pv[8];
-                                    bf8_unpack(held[CAN_POOL ? k : 0], a0);
-                                    bf8_unpack(nh, a1);
-                                    bf8_unpack(o, a2);
-                                    bf8_unpack(nc, a3);
-#pragma unroll
-                                    for (int j = 0; j < 8; ++j) pv[j] = 0.25f * (((a0[j] + a1[j]) + a2[j]) + a3[j]);
-                                    uint4 po;
-                                    __nv_bfloat162* ph2 = reinterpret_cast<__nv_bfloat162*>(&po);
-#pragma unroll
-                                    for (int j = 0; j < 4; ++j) ph2[j] = __floats2bfloat162_rn(pv[2 * j], pv[2 * j + 1]);
+                                const uint4 nh = shfl_down_u4(held[CAN_POOL ? k : 0], 1), nc = shfl_down_u4(o[g], 1);
+                                if (valid && (lane & 1) == 0)
                                     *reinterpret_cast<uint4*>(
-                                        a.pool.p + a.pool.at(b, (size_t)(gy / 2) * (a.W / 2) + px / 2, k)) = po;
-                                }
+                                        a.pool.p + a.pool.at(b, (size_t)(gy / 2) * (a.W / 2) + px / 2, k)) =
+                                        mean4<OUT8>(held[CAN_POOL ? k : 0], nh, o[g], nc);
                             }
                         }
                     }
@@ -453,12 +555,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 // lives in a ring of five 96-column TMEM buffers, and output row y is written as
 // soon as E_{y+1} is complete. The weights of all taps and input channels
 // (at most 55 KB, [chunk][kx][ky][n][KC]) stay in shared memory.
-template <int CIN> struct RsShape {
+template <int CIN, bool F8 = false> struct RsShape {
     static constexpr int COUT = 32, NX = 96;
-    static constexpr int KC = CIN % 32 == 0 ? 32 : 16;
-    static constexpr int ROWB = 2 * KC;
-    static constexpr uint32_t LAYOUT = KC == 32 ? 4u : 6u;
-    static constexpr int NCH = CIN / KC;
+    static constexpr int ROWB = CIN % (F8 ? 64 : 32) == 0 ? 64 : 32;
+    static constexpr int KC = F8 ? ROWB : ROWB / 2;
+    static constexpr uint32_t LAYOUT = ROWB == 64 ? 4u : 6u;
+    static constexpr int NCH = (CIN + KC - 1) / KC;
     static constexpr int ROWS = 16;                                 // output rows per strip
     static constexpr uint32_t ROW_TX = kHaloPix * ROWB;             // one halo row of one chunk
     static constexpr int STAGE = round_up(kHaloPix * ROWB, 1024);
@@ -469,19 +571,20 @@ template <int CIN> struct RsShape {
     static constexpr int NE = 5;                                    // TMEM ring of E buffers
     static constexpr int TMEM_COLS = 512;
     // at least 120 KB, so that one CTA (which holds all 512 TMEM columns) runs per SM
-    static constexpr size_t SMEM_USED = (size_t)ST_OFF + (size_t)STAGES * STAGE + 1024 + 512 + COUT * 4;
+    static constexpr size_t SMEM_USED = (size_t)ST_OFF + (size_t)STAGES * STAGE + 1024 + 512 + 3 * COUT * 4;
     static constexpr size_t SMEM = SMEM_USED > 120 * 1024 ? SMEM_USED : 120 * 1024;
-    static_assert(CIN % KC == 0 && WCH % 1024 == 0 && STAGES >= 4, "shape");
+    static_assert(WCH % 1024 == 0 && STAGES >= 4, "shape");
     static_assert(NE * NX <= TMEM_COLS, "tmem");
 };
 
 constexpr int kRsThreads = 352;   // producer, MMA issuer, 8 epilogue warps, second MMA issuer
 
-template <int CIN, int MODE>
+template <int CIN, int MODE, bool F8, bool OUT8>
 __global__ void __launch_bounds__(kRsThreads, 1)
     conv3x3_rs_kernel(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_w,
                       ConvArgs a, TcTiles tl, int* err) {
-    using S = RsShape<CIN>;
+    using S = RsShape<CIN, F8>;
+    constexpr int NV = OUT8 ? 2 : 4;
     constexpr int COUT = 32, NX = S::NX, NE = S::NE, NCH = S::NCH, KC = S::KC;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem =
@@ -496,6 +599,8 @@ __global__ void __launch_bounds__(kRsThreads, 1)
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 2);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     float* bias_s = reinterpret_cast<float*>(ctrl + 512);           // [COUT]
+    float* ws_s = bias_s + 32;                                       // [COUT] weight scales (F8)
+    float* oinv_s = ws_s + 32;                                       // [COUT] output inverse scales (OUT8)
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 1) {
@@ -511,7 +616,7 @@ __global__ void __launch_bounds__(kRsThreads, 1)
         }
         for (int e = 0; e < NE; ++e) {
             mbar_init(s_addr(efull + e), 1);
-            mbar_init(s_addr(eempty + e), 12);  // three reads x four epilogue warps
+            mbar_init(s_addr(eempty + e), 8);   // one arrival per epilogue warp
         }
         mbar_init(s_addr(wbar), 1);
         mbar_init(s_addr(drain), 1);
@@ -567,7 +672,7 @@ __global__ void __launch_bounds__(kRsThreads, 1)
         // core busy). Each commits its own rows' stages and E buffers.
         if (lane == 0) {
             const unsigned who = warp == 1 ? 0u : 1u;
-            constexpr uint32_t IDESC = instr_desc_bf16(kTcM, NX);
+            constexpr uint32_t IDESC = instr_desc(kTcM, NX, F8);
             constexpr uint32_t HI = (uint32_t)((8 * S::ROWB) >> 4) | (1u << 14) | (S::LAYOUT << 29);
             // stage of this issuer's next chunk and E buffer of its next row, with their parities
             int s = (int)(who * NCH) % S::STAGES;
@@ -594,16 +699,11 @@ __global__ void __launch_bounds__(kRsThreads, 1)
 #pragma unroll
                         for (int kx = 0; kx < 3; ++kx) {
 #pragma unroll
-                            for (int ks = 0; ks < KC / 16; ++ks) {
+                            for (int ks = 0; ks < S::ROWB / 32; ++ks) {
                                 const uint32_t av = a_lo + (uint32_t)((kx * S::ROWB + ks * 32) >> 4);
                                 const uint32_t bv = b_lo + (uint32_t)((kx * NX * S::ROWB + ks * 32) >> 4);
                                 const uint32_t accum = (ch > 0 || kx > 0 || ks > 0) ? 1u : 0u;
-                                asm volatile(
-                                    "{\n .reg .pred p;\n .reg .b64 ad, bd;\n setp.ne.b32 p, %5, 0;\n"
-                                    " mov.b64 ad, {%1, %3};\n mov.b64 bd, {%2, %3};\n"
-                                    " tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %4, p;\n}\n" ::"r"(d),
-                                    "r"(av), "r"(bv), "r"(HI), "r"(IDESC), "r"(accum)
-                                    : "memory");
+                                umma<F8>(d, av, bv, HI, IDESC, accum);
                             }
                         }
                         issued = true;
@@ -631,21 +731,27 @@ __global__ void __launch_bounds__(kRsThreads, 1)
         }
     } else {
         // ------------------------------------------------ epilogue (warps 2..9)
-        // Two groups of four warps (one per TMEM lane quarter) take alternate pairs of
-        // output rows, so two rows are in flight per scheduler; a pair stays in one
-        // group because the fused pooling averages rows 2k and 2k + 1 in registers.
-        // E_h is read by output rows h - 1, h and h + 1; every E buffer collects
-        // 3 reads x 4 warps = 12 arrivals before the MMA reuses it (the strip's first
-        // and last rows add the arrivals of the missing neighbours).
+        // Two groups of four warps (one per TMEM lane quarter) split the 32 output
+        // channels (16 each). Halo row h's E is consumed as soon as it is complete:
+        // its ky 2 block completes output row h - 1, its ky 1 block is added to the
+        // partial sum of row h and its ky 0 block starts row h + 1. Each thread keeps
+        // those two partial rows in registers, so every E buffer is released right
+        // after it has been read (4 warps x 2 groups = 8 arrivals).
         const int q = warp & 3;
         const int grp = (warp - 2) >> 2;
+        const int c0 = 16 * grp;                // first output channel of this group
+        constexpr int NVG = OUT8 ? 1 : 2;       // 16-byte output vectors per 16 channels
         const int et = tid - 64;
-        if (MODE != 2)
-            for (int c = et; c < COUT; c += 256) bias_s[c] = a.bias[c];
+        for (int c = et; c < COUT; c += 256) {
+            if (MODE != 2) bias_s[c] = a.bias[c];
+            if (F8) ws_s[c] = a.wscale[c];
+            if (OUT8) oinv_s[c] = a.oinv[c];
+        }
         asm volatile("bar.sync 1, 256;\n" ::: "memory");
         const bool pooling = a.pool.p != nullptr;
-        uint4 held[4];
-        unsigned J0 = 0;
+        uint4 held[NVG];
+        float part1[16], part2[16];             // partial sums of output rows h and h + 1
+        unsigned J = 0;
         bool ok = true;
         for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
             const int sx = t % tl.tiles_x, rest = t / tl.tiles_x;
@@ -653,16 +759,10 @@ __global__ void __launch_bounds__(kRsThreads, 1)
             const int yb = sy * S::ROWS;
             const int nrows = min(S::ROWS, a.H - yb);
             const int px = sx * kTcM + q * 32 + lane;
-            for (int r = 2 * grp; r < nrows && ok; r += (r & 1) ? 3 : 1) {
-                // r runs over this group's pairs: 2g, 2g + 1, 2g + 4, 2g + 5, ...
-                const unsigned J = J0 + r;   // output row yb + r: E_J ky 0, E_{J+1} ky 1, E_{J+2} ky 2
+            const bool valid = px < a.W;
+            for (int i = 0; i < nrows + 2 && ok; ++i, ++J) {
                 int ready = 0;
-                if (lane == 0)
-                    ready = (mbar_wait(s_addr(efull + J % NE), (J / NE) & 1u, abort_flag) &&
-                             mbar_wait(s_addr(efull + (J + 1) % NE), ((J + 1) / NE) & 1u, abort_flag) &&
-                             mbar_wait(s_addr(efull + (J + 2) % NE), ((J + 2) / NE) & 1u, abort_flag))
-                                ? 1
-                                : 0;
+                if (lane == 0) ready = mbar_wait(s_addr(efull + J % NE), (J / NE) & 1u, abort_flag) ? 1 : 0;
                 ready = __shfl_sync(0xffffffffu, ready, 0);
                 if (!ready) {
                     if (lane == 0) give_up(abort_flag, err);
@@ -670,74 +770,49 @@ __global__ void __launch_bounds__(kRsThreads, 1)
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                const uint32_t lanes = (uint32_t)(q * 32) << 16;
-                uint32_t v0[32], v1[32], v2[32];
-                tmem_ld32(tmem + lanes + (uint32_t)((J % NE) * NX + 0), v0);
-                tmem_ld32(tmem + lanes + (uint32_t)(((J + 1) % NE) * NX + 32), v1);
-                tmem_ld32(tmem + lanes + (uint32_t)(((J + 2) % NE) * NX + 64), v2);
+                const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((J % NE) * NX + c0);
+                uint32_t k0v[16], k1v[16], k2v[16];
+                tmem_ld16(base + 0, k0v);
+                tmem_ld16(base + 32, k1v);
+                tmem_ld16(base + 64, k2v);
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
                 __syncwarp();
-                if (lane == 0) {
-                    const uint32_t b0 = s_addr(eempty + J % NE), b1 = s_addr(eempty + (J + 1) % NE),
-                                   b2 = s_addr(eempty + (J + 2) % NE);
-                    const int n0 = 1 + (r == 0 ? 2 : 0);
-                    const int n1 = 1 + (r == 0 ? 1 : 0) + (r == nrows - 1 ? 1 : 0);
-                    const int n2 = 1 + (r == nrows - 1 ? 2 : 0);
-                    for (int k = 0; k < n0; ++k) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(b0) : "memory");
-                    for (int k = 0; k < n1; ++k) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(b1) : "memory");
-                    for (int k = 0; k < n2; ++k) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(b2) : "memory");
-                }
-                const int y = yb + r;
-                const bool valid = px < a.W;
-                bf16* yp = a.y.p + a.y.at(b, valid ? (size_t)y * a.W + px : 0, 0);
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(s_addr(eempty + J % NE)) : "memory");
+                // halo row h = yb - 1 + i completes output row y = h - 1 = yb + i - 2
+                if (i >= 2) {
+                    const int y = yb + i - 2;
+                    float f[16];
 #pragma unroll
-                for (int g = 0; g < 4; ++g) {
-                    float f[8];
+                    for (int j = 0; j < 16; ++j) f[j] = part1[j] + __uint_as_float(k2v[j]);
+                    uint4 o[NVG];
+                    epilogue_n<16, MODE, F8, OUT8>(f, c0, bias_s, ws_s, oinv_s, o);
+                    bf16* yp = a.y.p + a.y.at(b, valid ? (size_t)y * a.W + px : 0, 0);
 #pragma unroll
-                    for (int j = 0; j < 8; ++j)
-                        f[j] = (__uint_as_float(v0[8 * g + j]) + __uint_as_float(v1[8 * g + j])) +
-                               __uint_as_float(v2[8 * g + j]);
-                    if (MODE != 2) {
-                        const float4 c0 = *reinterpret_cast<const float4*>(bias_s + 8 * g);
-                        const float4 c1 = *reinterpret_cast<const float4*>(bias_s + 8 * g + 4);
-                        f[0] += c0.x; f[1] += c0.y; f[2] += c0.z; f[3] += c0.w;
-                        f[4] += c1.x; f[5] += c1.y; f[6] += c1.z; f[7] += c1.w;
-                    }
-                    uint4 o;
-                    __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        float f0 = f[2 * j], f1 = f[2 * j + 1];
-                        if (MODE == 0) { f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); }
-                        oh[j] = __floats2bfloat162_rn(f0, f1);
-                    }
-                    if (valid) *reinterpret_cast<uint4*>(yp + (size_t)g * (size_t)a.y.grp) = o;
-                    if (pooling) {
-                        if ((y & 1) == 0) {
-                            held[g] = o;
-                        } else {
-                            const uint4 nh = shfl_down_u4(held[g], 1), nc = shfl_down_u4(o, 1);
-                            if (valid && (lane & 1) == 0) {
-                                float a0[8], a1[8], a2[8], a3[8], pv[8];
-                                bf8_unpack(held[g], a0);
-                                bf8_unpack(nh, a1);
-                                bf8_unpack(o, a2);
-                                bf8_unpack(nc, a3);
-#pragma unroll
-                                for (int j = 0; j < 8; ++j) pv[j] = 0.25f * (((a0[j] + a1[j]) + a2[j]) + a3[j]);
-                                uint4 po;
-                                __nv_bfloat162* ph2 = reinterpret_cast<__nv_bfloat162*>(&po);
-#pragma unroll
-                                for (int j = 0; j < 4; ++j) ph2[j] = __floats2bfloat162_rn(pv[2 * j], pv[2 * j + 1]);
-                                *reinterpret_cast<uint4*>(a.pool.p +
-                                                          a.pool.at(b, (size_t)(y / 2) * (a.W / 2) + px / 2, g)) = po;
+                    for (int g = 0; g < NVG; ++g) {
+                        const int k = c0 / (OUT8 ? 16 : 8) + g;   // 16-byte vector of the pixel
+                        if (valid) *reinterpret_cast<uint4*>(yp + (size_t)k * (size_t)a.y.grp) = o[g];
+                        if (pooling) {
+                            if ((y & 1) == 0) {
+                                held[g] = o[g];
+                            } else {
+                                const uint4 nh = shfl_down_u4(held[g], 1), nc = shfl_down_u4(o[g], 1);
+                                if (valid && (lane & 1) == 0)
+                                    *reinterpret_cast<uint4*>(
+                                        a.pool.p + a.pool.at(b, (size_t)(y / 2) * (a.W / 2) + px / 2, k)) =
+                                        mean4<OUT8>(held[g], nh, o[g], nc);
                             }
                         }
                     }
                 }
+                // (E_{h-1} ky 0 + E_h ky 1) for row h, E_h ky 0 starts row h + 1
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    part1[j] = part2[j] + __uint_as_float(k1v[j]);
+                    part2[j] = __uint_as_float(k0v[j]);
+                }
             }
-            J0 += nrows + 2;
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -771,28 +846,29 @@ static int sm_count() {
     return n;
 }
 
-template <int CIN, int COUT, int MODE>
+template <int CIN, int COUT, int MODE, bool F8, bool OUT8>
 static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
-    using S = TcShape<CIN, COUT>;
+    using S = TcShape<CIN, COUT, F8>;
+    constexpr cuuint64_t EB = F8 ? 1 : 2;   // bytes per element
+    const CUtensorMapDataType dt = F8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
     if (a.pool.p && (!view_ok(a.pool) || S::R % 2 != 0 || COUT > 64 || (a.H | a.W) & 1)) return cudaErrorInvalidValue;
     auto encode = encode_fn();
     if (!encode) return cudaErrorNotSupported;
-    const CUtensorMapSwizzle swz = S::KC == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+    const CUtensorMapSwizzle swz = S::ROWB == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
     CUtensorMap mx, mw;
     const cuuint32_t one[4] = {1, 1, 1, 1};
-    // NHWC input view: {CIN channels, W, H, B}, box {KC, 130, R + 2, 1}
+    // NHWC input view: {CIN channels, W, H, B}, box {KC, 130, R + 2, 1} (channels past CIN read as zero)
     const cuuint64_t xdim[4] = {(cuuint64_t)CIN, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.B};
     const cuuint64_t xstr[3] = {(cuuint64_t)a.x.pix * 2, (cuuint64_t)a.x.pix * a.W * 2, (cuuint64_t)a.x.img * 2};
     const cuuint32_t xbox[4] = {(cuuint32_t)S::KC, (cuuint32_t)kHaloPix, (cuuint32_t)S::HALO_ROWS, 1};
-    if (encode(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.x.p, xdim, xstr, xbox, one,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    if (encode(&mx, dt, 4, (void*)a.x.p, xdim, xstr, xbox, one, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
     // weights [COUT][9][CIN] viewed as {CIN channels, COUT, 9 taps}, box {KC, COUT, 9}
     const cuuint64_t wdim[3] = {(cuuint64_t)CIN, (cuuint64_t)COUT, 9};
-    const cuuint64_t wstr[2] = {(cuuint64_t)9 * CIN * 2, (cuuint64_t)CIN * 2};
+    const cuuint64_t wstr[2] = {(cuuint64_t)9 * CIN * EB, (cuuint64_t)CIN * EB};
     const cuuint32_t wbox[3] = {(cuuint32_t)S::KC, (cuuint32_t)COUT, 9};
-    if (encode(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)a.w, wdim, wstr, wbox, one,
+    if (encode(&mw, dt, 3, (void*)a.w, wdim, wstr, wbox, one,
                CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
@@ -804,7 +880,7 @@ static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
     tl.total = (int)total;
     const int sms = sm_count();
     if (sms <= 0) return cudaErrorInvalidDevice;
-    auto kern = conv3x3_tc_kernel<CIN, COUT, MODE>;
+    auto kern = conv3x3_tc_kernel<CIN, COUT, MODE, F8, OUT8>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
     if (e != cudaSuccess) return e;
     const int grid = tl.total < sms ? tl.total : sms;
@@ -812,28 +888,29 @@ static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <int CIN, int MODE>
+template <int CIN, int MODE, bool F8, bool OUT8>
 static cudaError_t run_rs(const ConvArgs& a, int* err, cudaStream_t s) {
-    using S = RsShape<CIN>;
+    using S = RsShape<CIN, F8>;
+    constexpr cuuint64_t EB = F8 ? 1 : 2;   // bytes per element
+    const CUtensorMapDataType dt = F8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
     if (a.pool.p && (!view_ok(a.pool) || (a.H | a.W) & 1)) return cudaErrorInvalidValue;
     auto encode = encode_fn();
     if (!encode) return cudaErrorNotSupported;
-    const CUtensorMapSwizzle swz = S::KC == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+    const CUtensorMapSwizzle swz = S::ROWB == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
     CUtensorMap mx, mw;
     const cuuint32_t one[4] = {1, 1, 1, 1};
-    // NHWC input view: {CIN channels, W, H, B}, box {KC, 130, 1 row, 1}
+    // NHWC input view: {CIN channels, W, H, B}, box {KC, 130, 1 row, 1} (channels past CIN read as zero)
     const cuuint64_t xdim[4] = {(cuuint64_t)CIN, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.B};
     const cuuint64_t xstr[3] = {(cuuint64_t)a.x.pix * 2, (cuuint64_t)a.x.pix * a.W * 2, (cuuint64_t)a.x.img * 2};
     const cuuint32_t xbox[4] = {(cuuint32_t)S::KC, (cuuint32_t)kHaloPix, 1, 1};
-    if (encode(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.x.p, xdim, xstr, xbox, one,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    if (encode(&mx, dt, 4, (void*)a.x.p, xdim, xstr, xbox, one, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
     // weights [32][ky][kx][CIN] viewed as {CIN channels, 32 n, 3 ky, 3 kx}, box {KC, 32, 3, 3} -> [kx][ky][n][KC]
     const cuuint64_t wdim[4] = {(cuuint64_t)CIN, 32, 3, 3};
-    const cuuint64_t wstr[3] = {(cuuint64_t)9 * CIN * 2, (cuuint64_t)3 * CIN * 2, (cuuint64_t)CIN * 2};
+    const cuuint64_t wstr[3] = {(cuuint64_t)9 * CIN * EB, (cuuint64_t)3 * CIN * EB, (cuuint64_t)CIN * EB};
     const cuuint32_t wbox[4] = {(cuuint32_t)S::KC, 32, 3, 3};
-    if (encode(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)a.w, wdim, wstr, wbox, one,
+    if (encode(&mw, dt, 4, (void*)a.w, wdim, wstr, wbox, one,
                CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
@@ -845,7 +922,7 @@ static cudaError_t run_rs(const ConvArgs& a, int* err, cudaStream_t s) {
     tl.total = (int)total;
     const int sms = sm_count();
     if (sms <= 0) return cudaErrorInvalidDevice;
-    auto kern = conv3x3_rs_kernel<CIN, MODE>;
+    auto kern = conv3x3_rs_kernel<CIN, MODE, F8, OUT8>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
     if (e != cudaSuccess) return e;
     const int grid = tl.total < sms ? tl.total : sms;
@@ -854,16 +931,16 @@ static cudaError_t run_rs(const ConvArgs& a, int* err, cudaStream_t s) {
 }
 
 // 32-channel outputs take the row-streaming kernel, wider ones the 9-tap kernel.
-template <int CIN, int COUT>
+template <int CIN, int COUT, bool F8, bool OUT8>
 static cudaError_t run_shape(int mode, const ConvArgs& a, int* err, cudaStream_t s) {
     if constexpr (COUT == 32) {
-        if (mode == 0) return run_rs<CIN, 0>(a, err, s);
-        if (mode == 1) return run_rs<CIN, 1>(a, err, s);
-        return run_rs<CIN, 2>(a, err, s);
+        if (mode == 0) return run_rs<CIN, 0, F8, OUT8>(a, err, s);
+        if (mode == 1) return run_rs<CIN, 1, F8, OUT8>(a, err, s);
+        return run_rs<CIN, 2, F8, OUT8>(a, err, s);
     } else {
-        if (mode == 0) return run_tc<CIN, COUT, 0>(a, err, s);
-        if (mode == 1) return run_tc<CIN, COUT, 1>(a, err, s);
-        return run_tc<CIN, COUT, 2>(a, err, s);
+        if (mode == 0) return run_tc<CIN, COUT, 0, F8, OUT8>(a, err, s);
+        if (mode == 1) return run_tc<CIN, COUT, 1, F8, OUT8>(a, err, s);
+        return run_tc<CIN, COUT, 2, F8, OUT8>(a, err, s);
     }
 }
 
@@ -873,7 +950,7 @@ cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err,
         a.W < 1)
         return cudaErrorInvalidValue;
 #define SGI_TC_CASE(CI, CO)                                                  \
-    if (cin == CI && cout == CO) return run_shape<CI, CO>(mode, a, err, s);
+    if (cin == CI && cout == CO) return run_shape<CI, CO, false, false>(mode, a, err, s);
     SGI_TC_CASE(16, 32)
     SGI_TC_CASE(32, 32)
     SGI_TC_CASE(32, 64)
@@ -887,6 +964,26 @@ cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err,
     SGI_TC_CASE(64, 192)
     SGI_TC_CASE(32, 96)
 #undef SGI_TC_CASE
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t conv3x3_tc_fp8(int cin, int cout, int mode, bool out8, const ConvArgs& a, int* err, cudaStream_t s) {
+    // FP8 tensors use BF16-unit views (two channels per unit): 16-byte vectors hold 16 channels
+    if (!err || !view_ok(a.x) || !view_ok(a.y) || a.x.grp != 8 || (((uintptr_t)a.w) & 15) || !a.wscale || a.B < 1 ||
+        a.H < 1 || a.W < 1 || (out8 && !a.oinv) || (mode != 2 && !a.bias))
+        return cudaErrorInvalidValue;
+#define SGI_TC8_CASE(CI, CO)                                                         \
+    if (cin == CI && cout == CO)                                                     \
+        return out8 ? run_shape<CI, CO, true, true>(mode, a, err, s) : run_shape<CI, CO, true, false>(mode, a, err, s);
+    SGI_TC8_CASE(16, 32)
+    SGI_TC8_CASE(32, 32)
+    SGI_TC8_CASE(32, 64)
+    SGI_TC8_CASE(64, 64)
+    SGI_TC8_CASE(64, 128)
+    SGI_TC8_CASE(128, 128)
+    SGI_TC8_CASE(192, 64)
+    SGI_TC8_CASE(96, 32)
+#undef SGI_TC8_CASE
     return cudaErrorInvalidValue;
 }
 

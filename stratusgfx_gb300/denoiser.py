@@ -82,6 +82,15 @@ class KpcnDenoiser:
         """abi.SGI_NN_CONV_TCGEN05 (tcgen05.mma, TMEM accumulators) or abi.SGI_NN_CONV_WARP_MMA."""
         self._chk(self.lib.sgi_nn_set_conv_path(self.h, path))
 
+    def set_precision(self, precision: int):
+        """abi.SGI_NN_BF16 or abi.SGI_NN_FP8 (after calibrate_fp8)."""
+        self._chk(self.lib.sgi_nn_set_precision(self.h, precision))
+
+    def calibrate_fp8(self, feat, stream=None):
+        """Per-channel FP8 scales from the BF16 network's activations on `feat` [B, H, W, 16]."""
+        B, H, W = feat.shape[:3]
+        self._chk(self.lib.sgi_nn_calibrate_fp8(self.h, _p(feat), B, H, W, stage._stream_ptr(stream)))
+
     def device_status(self):
         """Synchronises; raises SgiError(SGI_ERR_TIMEOUT) if a tensor-core wait ran out."""
         self._chk(self.lib.sgi_nn_device_status(self.h))

@@ -143,3 +143,40 @@ def test_neural_frame_runs_through_the_abi():
     assert np.isfinite(o).all() and (o[..., :3] > 0).mean() > 0.5
     st.close()
     net.close()
+
+
+def test_fp8_forward_tracks_bf16_on_rendered_frames():
+    """FP8 E4M3 inference (per-channel scales calibrated on one frame set, applied to
+    another) against the BF16 network with the trained weights, on frames the plain
+    path renders. Tolerance: the denoised GI differs from the BF16 result by at most
+    4 % of its peak in the mean and the FP8 loss against the converged target is
+    within 15 % of the BF16 loss (E4M3 keeps 3 mantissa bits)."""
+    import os
+
+    from stratusgfx_gb300 import denoiser
+    if not os.path.exists(denoiser.WEIGHTS):
+        pytest.skip("no trained weights")
+    calib = denoiser.make_dataset(2, H=64, W=128, frames_per_room=2, seed=500, samples=(2,), batches=2,
+                                  log=lambda *a: None)
+    ds = denoiser.make_dataset(3, H=64, W=128, frames_per_room=3, seed=900, samples=(2,), batches=8,
+                               log=lambda *a: None)
+    net = KpcnDenoiser(3, 64, 128, seed=1)
+    net.load(denoiser.WEIGHTS)
+    out_bf = torch.empty((3, 64, 128, 4), device="cuda")
+    out_f8 = torch.empty_like(out_bf)
+    net.forward(ds.feat[:3], ds.noisy[:3], ds.prev[:3], out_bf)
+    net.set_precision(abi.SGI_NN_FP8)
+    with pytest.raises(abi.SgiError):          # not calibrated yet
+        net.forward(ds.feat[:3], ds.noisy[:3], ds.prev[:3], out_f8)
+    net.calibrate_fp8(calib.feat[:2])
+    net.forward(ds.feat[:3], ds.noisy[:3], ds.prev[:3], out_f8)
+    net.device_status()
+    a, b = out_f8[..., :3], out_bf[..., :3]
+    assert torch.isfinite(a).all()
+    rel = float((a - b).abs().mean() / b.abs().max())
+    assert rel < 0.04, rel
+    t = ds.target[:3, ..., :3]
+    loss = lambda o: float((torch.log1p(o.clamp(min=0)) - torch.log1p(t.clamp(min=0))).abs().mean())  # noqa: E731
+    assert loss(a) <= 1.15 * loss(b) + 1e-3, (loss(a), loss(b))
+    net.set_precision(abi.SGI_NN_BF16)
+    net.close()

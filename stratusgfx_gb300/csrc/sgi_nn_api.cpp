@@ -151,46 +151,46 @@ cudaError_t Net::conv(int l, const View& x, const View& y, int B, int H, int W, 
 // D1IN (96 channels) and D2IN (192) take the skip connections as channel slices.
 #define NN_TRY(x) do { e = (x); if (e != cudaSuccess) return e; } while (0)
 
-cudaError_t Net::conv8(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s, bool out8,
+cudaError_t Net::conv8(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s, bool in8, bool out8,
                        const View* pool) {
-    ConvArgs a{x, reinterpret_cast<const bf16*>(wq + w_off[l]), w32 + b_off[l], y, B, H, W};
+    ConvArgs a{x, in8 ? reinterpret_cast<const bf16*>(wq + w_off[l]) : wbf + w_off[l], w32 + b_off[l], y, B, H, W};
     if (pool) a.pool = *pool;
-    a.wscale = f8_wscale + sc_off[l];
+    a.wscale = in8 ? f8_wscale + sc_off[l] : nullptr;
     a.oinv = out8 ? f8_oinv + sc_off[l] : nullptr;
-    return conv3x3_tc_fp8(kCin[l], kCout[l], l == HEAD ? 1 : 0, out8, a, dev_err, s);
+    return conv3x3_tc_fp8(kCin[l], kCout[l], l == HEAD ? 1 : 0, in8, out8, a, dev_err, s);
 }
 
-// FP8 E4M3 forward: the features are quantized with per-channel scales, every
-// convolution but the head writes E4M3 with the per-channel scales of its output
-// (folded into the next layer's weights), pooling and upsampling move E4M3 bytes
-// unchanged, and the head writes BF16 logits. FP8 tensors are BF16-unit views
-// with half the channel count (two E4M3 channels per unit).
+// FP8 E4M3 forward. The first and the last two layers keep BF16 where precision
+// matters most: e1a reads the BF16 features with BF16 weights and writes E4M3,
+// d1b reads E4M3 and writes BF16, and the head runs in BF16. The layers between
+// read and write E4M3 with per-channel scales (each output's scales are folded
+// into the next layer's weights); pooling and upsampling move E4M3 bytes
+// unchanged. FP8 tensors are BF16-unit views with half the channel count.
 cudaError_t Net::forward_fp8(const bf16* feat, int B, int H, int W, cudaStream_t s) {
     const int H2 = H / 2, W2 = W / 2, H4 = H / 4, W4 = W / 4;
     cudaError_t e;
-    const View fb = nhwc_view(feat, 16, H, W), fq = nhwc_view(GA, 8, H, W);
+    const View fb = nhwc_view(feat, 16, H, W);
     const View e1a = nhwc_view(E1A_, 16, H, W), d1in = nhwc_view(D1IN, 48, H, W);
     const View p1 = nhwc_view(P1, 16, H2, W2), e2a = nhwc_view(E2A_, 32, H2, W2);
     const View d2in = nhwc_view(D2IN, 96, H2, W2), p2 = nhwc_view(P2_, 32, H4, W4);
     const View b1 = nhwc_view(B1_, 64, H4, W4), b2 = nhwc_view(B2_, 64, H4, W4);
     const View d2a = nhwc_view(D2A_, 32, H2, W2), d2b = nhwc_view(D2B_, 32, H2, W2);
-    const View d1a = nhwc_view(D1A_, 16, H, W), d1b = nhwc_view(D1B_, 16, H, W);
+    const View d1a = nhwc_view(D1A_, 16, H, W), d1b = nhwc_view(D1B_, 32, H, W);   // d1b: BF16 output
     const View lg = planar_view(LOG, 4, H, W);
-    NN_TRY(quantize_act(fb, fq, 16, B, H, W, f8_finv, s));
-    NN_TRY(conv8(E1A, fq, e1a, B, H, W, s, true));
-    NN_TRY(conv8(E1B, e1a, channel_slice(d1in, 32), B, H, W, s, true, &p1));
-    NN_TRY(conv8(E2A, p1, e2a, B, H2, W2, s, true));
-    NN_TRY(conv8(E2B, e2a, channel_slice(d2in, 64), B, H2, W2, s, true, &p2));
-    NN_TRY(conv8(B1, p2, b1, B, H4, W4, s, true));
-    NN_TRY(conv8(B2, b1, b2, B, H4, W4, s, true));
+    NN_TRY(conv8(E1A, fb, e1a, B, H, W, s, false, true));
+    NN_TRY(conv8(E1B, e1a, channel_slice(d1in, 32), B, H, W, s, true, true, &p1));
+    NN_TRY(conv8(E2A, p1, e2a, B, H2, W2, s, true, true));
+    NN_TRY(conv8(E2B, e2a, channel_slice(d2in, 64), B, H2, W2, s, true, true, &p2));
+    NN_TRY(conv8(B1, p2, b1, B, H4, W4, s, true, true));
+    NN_TRY(conv8(B2, b1, b2, B, H4, W4, s, true, true));
     NN_TRY(up_fwd(b2, d2in, B, H2, W2, 64, s));
-    NN_TRY(conv8(D2A, d2in, d2a, B, H2, W2, s, true));
-    NN_TRY(conv8(D2B, d2a, d2b, B, H2, W2, s, true));
+    NN_TRY(conv8(D2A, d2in, d2a, B, H2, W2, s, true, true));
+    NN_TRY(conv8(D2B, d2a, d2b, B, H2, W2, s, true, true));
     NN_TRY(up_fwd(d2b, d1in, B, H, W, 32, s));
-    NN_TRY(conv8(D1A, d1in, d1a, B, H, W, s, true));
-    NN_TRY(conv8(D1B, d1a, d1b, B, H, W, s, true));
-    NN_TRY(conv8(HEAD, d1b, lg, B, H, W, s, false));
-    launches += 14;
+    NN_TRY(conv8(D1A, d1in, d1a, B, H, W, s, true, true));
+    NN_TRY(conv8(D1B, d1a, d1b, B, H, W, s, true, false));
+    NN_TRY(conv(HEAD, d1b, lg, B, H, W, s));
+    launches += 13;
     return cudaSuccess;
 }
 

@@ -99,9 +99,11 @@ cudaError_t conv3x3(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t
 // The same convolution on the 5th-generation tensor cores (sgi_nn_tc.cu); *err is
 // set to 1 when a bounded wait of a block ran out.
 cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err, cudaStream_t s);
-// FP8 E4M3 operands (x, w: one byte per channel, described by BF16-unit views with
-// two channels per unit); the output is FP8 (out8) or BF16.
-cudaError_t conv3x3_tc_fp8(int cin, int cout, int mode, bool out8, const ConvArgs& a, int* err, cudaStream_t s);
+// FP8 E4M3 operands (in8; x, w: one byte per channel, described by BF16-unit views
+// with two channels per unit) or BF16 operands (16 -> 32 only), the output E4M3
+// (out8) or BF16.
+cudaError_t conv3x3_tc_fp8(int cin, int cout, int mode, bool in8, bool out8, const ConvArgs& a, int* err,
+                           cudaStream_t s);
 cudaError_t flip_weights(const __nv_bfloat16* w, __nv_bfloat16* wt, int cin, int cout, cudaStream_t s);
 cudaError_t wgrad(const WgradArgs& a, cudaStream_t s);
 cudaError_t bias_grad(const View& dz, int c, int B, int H, int W, float* db, cudaStream_t s);

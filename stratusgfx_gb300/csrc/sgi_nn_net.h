@@ -53,7 +53,7 @@ struct Net {
                      const View* pool = nullptr);
     cudaError_t forward(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s, bool allow_fp8 = true);
     cudaError_t forward_fp8(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);
-    cudaError_t conv8(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s, bool out8,
+    cudaError_t conv8(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s, bool in8, bool out8,
                       const View* pool = nullptr);
     cudaError_t calibrate_fp8(const __nv_bfloat16* feat, int B, int H, int W, cudaStream_t s);
     cudaError_t layer_backward(int l, const View& x, const View& y, const View& dy, __nv_bfloat16* dz_buf,

@@ -967,11 +967,17 @@ cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err,
     return cudaErrorInvalidValue;
 }
 
-cudaError_t conv3x3_tc_fp8(int cin, int cout, int mode, bool out8, const ConvArgs& a, int* err, cudaStream_t s) {
+cudaError_t conv3x3_tc_fp8(int cin, int cout, int mode, bool in8, bool out8, const ConvArgs& a, int* err,
+                           cudaStream_t s) {
     // FP8 tensors use BF16-unit views (two channels per unit): 16-byte vectors hold 16 channels
-    if (!err || !view_ok(a.x) || !view_ok(a.y) || a.x.grp != 8 || (((uintptr_t)a.w) & 15) || !a.wscale || a.B < 1 ||
-        a.H < 1 || a.W < 1 || (out8 && !a.oinv) || (mode != 2 && !a.bias))
+    if (!err || !view_ok(a.x) || !view_ok(a.y) || a.x.grp != 8 || (((uintptr_t)a.w) & 15) || (in8 && !a.wscale) ||
+        a.B < 1 || a.H < 1 || a.W < 1 || (out8 && !a.oinv) || (mode != 2 && !a.bias) || (!in8 && !out8))
         return cudaErrorInvalidValue;
+    // BF16 operands with an E4M3 output: the first layer, whose input features keep BF16
+    if (!in8) {
+        if (cin == 16 && cout == 32) return run_shape<16, 32, false, true>(mode, a, err, s);
+        return cudaErrorInvalidValue;
+    }
 #define SGI_TC8_CASE(CI, CO)                                                         \
     if (cin == CI && cout == CO)                                                     \
         return out8 ? run_shape<CI, CO, true, true>(mode, a, err, s) : run_shape<CI, CO, true, false>(mode, a, err, s);

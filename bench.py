@@ -49,6 +49,8 @@ def parse():
                          "--warmup + --steps frames of sgi_render_frame only (no e2e or CPU legs)")
     ap.add_argument("--neural", action="store_true",
                     help="with --profile: frames of sgi_render_frame_neural (K = 2) instead")
+    ap.add_argument("--fp8", action="store_true",
+                    help="with --profile --neural: FP8 E4M3 convolutions (calibrated on another room) at K = 1")
     return ap.parse_args()
 
 
@@ -568,7 +570,8 @@ def run_profile(args):
     sc = S.make_scene(1234 + 2, w.width, w.height, w.num_boxes, w.num_vpls, 2, vpl_radius=w.vpl_radius,
                       num_points=w.num_points, csm_resolution=w.csm_resolution)
     ds = stage.DeviceScene(sc, w)
-    st = stage.GiStage(stage.workload_config(w, samples_per_pixel=2) if args.neural else stage.workload_config(w))
+    spp = (1 if args.fp8 else 2) if args.neural else None
+    st = stage.GiStage(stage.workload_config(w, samples_per_pixel=spp) if spp else stage.workload_config(w))
     st.set_lights(ds.vpls, ds.entries, ds.points)
     out = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
     net = None
@@ -578,6 +581,12 @@ def run_profile(args):
         from stratusgfx_gb300 import abi, denoiser
         net = denoiser.KpcnDenoiser(1, w.height, w.width)
         net.load(denoiser.WEIGHTS)
+        if args.fp8:
+            calib = denoiser.make_dataset(1, H=w.height, W=w.width, frames_per_room=2, seed=777, samples=(2,),
+                                          batches=1, log=lambda *a: None)
+            net.calibrate_fp8(calib.feat[:1])
+            net.set_precision(abi.SGI_NN_FP8)
+            del calib
     for s in range(args.warmup + args.steps):
         k = s % 2 + 1
         st.set_shadow_maps(ds.csms[k], ds.cubes)
@@ -591,7 +600,8 @@ def run_profile(args):
     torch.cuda.synchronize()
     if net is not None:
         net.close()
-    print(json.dumps({"profile_case": w.name, "frames": args.warmup + args.steps,
+    print(json.dumps({"profile_case": w.name + ("_neural_fp8_k1" if args.fp8 else "_neural_k2" if net else ""),
+                      "frames": args.warmup + args.steps,
                       "launches_per_frame": st.launch_count() // (args.warmup + args.steps)}))
     st.close()
 

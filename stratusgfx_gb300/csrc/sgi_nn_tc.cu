@@ -139,12 +139,24 @@ __device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
     return done != 0;
 }
 
+// try_wait that may suspend the thread for up to `hint_ns` (instead of the system's
+// default limit) while the phase is incomplete: a waiting warp then takes no issue slots.
+__device__ __forceinline__ bool mbar_test_sleep(uint32_t bar, uint32_t parity, uint32_t hint_ns) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity), "r"(hint_ns)
+        : "memory");
+    return done != 0;
+}
+
 // Bounded wait for the phase of `parity`; false on timeout or when another role aborted.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
     if (mbar_test(bar, parity)) return true;
     const unsigned long long deadline = global_ns() + kWaitNs;
     while (true) {
-        if (mbar_test(bar, parity)) return true;
+        if (mbar_test_sleep(bar, parity, 20000u)) return true;
         if (*abort_flag) return false;
         if (global_ns() > deadline) return false;
     }
@@ -541,66 +553,170 @@ __global__ void __launch_bounds__(kThreads, 1)
                      : "memory");
 }
 
-// ---------------------------------- 32 output channels: row streaming, ky in N
+// ---------------------------------- 32 output channels: row streaming, taps accumulated in TMEM
 //
 // With COUT = 32 an MMA of N = 32 costs about as much as one of N = 96 (both are
 // bounded by reading the 128-row A operand from shared memory), so the three
-// vertical taps share one MMA. For halo row h (an image row) the tensor core
-// accumulates
-//   E_h[m][ky * 32 + n] = sum over kx, k of X[h][x0 - 1 + m + kx][k] * W[n][ky][kx][k]
-// (A = halo row h from pixel kx, B = taps (0..2, kx) stacked along N = 96), and
-// output row y is E_{y-1}[ky 0] + E_y[ky 1] + E_{y+1}[ky 2]: the same TMEM lane
-// (pixel) in three buffers, so the epilogue only adds. A CTA walks strips of
-// 128 pixels x RS_ROWS rows from the top: each halo row is loaded once, its E
-// lives in a ring of five 96-column TMEM buffers, and output row y is written as
-// soon as E_{y+1} is complete. The weights of all taps and input channels
-// (at most 55 KB, [chunk][kx][ky][n][KC]) stay in shared memory.
-template <int CIN, bool F8 = false> struct RsShape {
+// vertical taps share one MMA. A CTA walks strips of 128 pixels x 16 rows from
+// the top. Output row j of a strip (image row y0 + j) owns the 32 TMEM columns
+// C(j) = 32 (15 - j). Halo row i (image row y0 - 1 + i) feeds row i - ky with
+// vertical tap ky, i.e. columns C(i) + 32 ky, so one MMA with B = taps
+// (0..2, kx) stacked along N = 96 and D at column C(i) adds halo row i into
+// rows i, i - 1 and i - 2:
+//   D[m][C(i) + 32 ky + n] += sum over kx, k of X[i][x0 - 1 + m + kx][k] * W[n][ky][kx][k].
+// At the strip's top and bottom only the taps that land on rows 0 .. nrows - 1
+// are issued (N = 32 or 64, with B and D advanced by 32 ky_lo). Row j is complete
+// after halo row j + 2: the epilogue reads its 32 columns, writes zeros back (the
+// MMAs only accumulate, so every row slot starts at zero) and hands the slot to
+// the next strip's row j. Each halo row is loaded once, two rows per TMA box (the
+// copy engine streams narrow pixel rows faster in larger boxes); the weights of all
+// taps and input channels (at most 55 KB, [chunk][kx][ky][n][KC]) stay in shared
+// memory. FP8 with 96 input channels takes one 128-byte chunk per pixel (three
+// 32-channel K steps, the fourth slice of the row is zero fill and skipped).
+// ROWS_ = 16: one CTA per SM holds all 512 TMEM columns; ROWS_ = 8: two CTAs per
+// SM (256 columns and at most 110 KB of shared memory each), two independent
+// pipelines per SM for the price of 10 / 8 instead of 18 / 16 halo rows per strip.
+template <int CIN, bool F8 = false, int ROWS_ = 16> struct RsShape {
     static constexpr int COUT = 32, NX = 96;
-    static constexpr int ROWB = CIN % (F8 ? 64 : 32) == 0 ? 64 : 32;
-    static constexpr int KC = F8 ? ROWB : ROWB / 2;
-    static constexpr uint32_t LAYOUT = ROWB == 64 ? 4u : 6u;
+    static constexpr int EB = F8 ? 1 : 2;                           // bytes per channel
+    static constexpr int ROWB = (F8 && CIN == 96) ? 128 : CIN % (F8 ? 64 : 32) == 0 ? 64 : 32;
+    static constexpr int KC = ROWB / EB;
+    static constexpr uint32_t LAYOUT = ROWB == 128 ? 2u : ROWB == 64 ? 4u : 6u;   // 128B / 64B / 32B swizzle
     static constexpr int NCH = (CIN + KC - 1) / KC;
-    static constexpr int ROWS = 16;                                 // output rows per strip
-    static constexpr uint32_t ROW_TX = kHaloPix * ROWB;             // one halo row of one chunk
-    static constexpr int STAGE = round_up(kHaloPix * ROWB, 1024);
+    static constexpr int KS = ROWB / 32;                            // 32-byte K steps of a full chunk
+    static constexpr int KS_LAST = ((CIN - (NCH - 1) * KC) * EB + 31) / 32;   // of the last chunk
+    static constexpr int ROWS = ROWS_;                              // output rows per strip = TMEM row slots
+    static constexpr int HPS = 2;                                   // halo rows per stage (one TMA box)
+    static constexpr int HROW = kHaloPix * ROWB;                    // bytes of one halo row of one chunk
+    static constexpr uint32_t STAGE_TX = HPS * HROW;
+    static constexpr int STAGE = round_up(HPS * HROW, 1024);
     static constexpr int WCH = 9 * COUT * ROWB;                     // weights of one chunk
     static constexpr int WBYTES = NCH * WCH;
     static constexpr int ST_OFF = round_up(WBYTES, 1024);
-    static constexpr int STAGES = (kSmemBudget - ST_OFF) / STAGE < 16 ? (kSmemBudget - ST_OFF) / STAGE : 16;
-    static constexpr int NE = 5;                                    // TMEM ring of E buffers
-    static constexpr int TMEM_COLS = 512;
-    // at least 120 KB, so that one CTA (which holds all 512 TMEM columns) runs per SM
-    static constexpr size_t SMEM_USED = (size_t)ST_OFF + (size_t)STAGES * STAGE + 1024 + 512 + 3 * COUT * 4;
-    static constexpr size_t SMEM = SMEM_USED > 120 * 1024 ? SMEM_USED : 120 * 1024;
-    static_assert(WCH % 1024 == 0 && STAGES >= 4, "shape");
-    static_assert(NE * NX <= TMEM_COLS, "tmem");
+    static constexpr int CTAS = 16 / ROWS;                           // CTAs per SM
+    static constexpr int BUDGET = ROWS == 16 ? kSmemBudget : 110 * 1024;
+    static constexpr int STAGES = (BUDGET - ST_OFF) / STAGE < 16 ? (BUDGET - ST_OFF) / STAGE : 16;
+    static constexpr int TMEM_COLS = ROWS * COUT;
+    static constexpr int CTRL = 640;                                // barriers, TMEM address, abort flag
+    // with 16 rows at least 120 KB, so that one CTA (which holds all 512 TMEM columns) runs per SM
+    static constexpr size_t SMEM_USED = (size_t)ST_OFF + (size_t)STAGES * STAGE + 1024 + CTRL + 2 * COUT * 4;
+    static constexpr size_t SMEM = (ROWS == 8 || SMEM_USED > 120 * 1024) ? SMEM_USED : 120 * 1024;
+    static_assert(WCH % 1024 == 0 && (ROWS == 8 || STAGES >= 2 * NCH), "shape");
+    static_assert(ROWS * COUT == TMEM_COLS && ROWS % HPS == 0, "tmem");
+    static_assert((2 * STAGES + ROWS + 2) * 8 + 8 <= CTRL, "control block");
 };
 
-constexpr int kRsThreads = 352;   // producer, MMA issuer, 8 epilogue warps, second MMA issuer
+constexpr int kRsThreads = 320;   // producer, MMA issuer, 8 epilogue warps
 
-template <int CIN, int MODE, bool F8, bool OUT8>
-__global__ void __launch_bounds__(kRsThreads, 1)
+__device__ __forceinline__ void tmem_st16_zero(uint32_t taddr) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+        "%1};\n" ::"r"(taddr),
+        "r"(0u)
+        : "memory");
+}
+
+// 16 FP32 accumulators -> y = act(acc * sc + bb) in FP32 (packed FMAs).
+template <int MODE>
+__device__ __forceinline__ void act16(const uint32_t* v, const float* sc, const float* bb, float* f) {
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        unsigned long long x, s, c, d;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "r"(v[2 * p]), "r"(v[2 * p + 1]));
+        asm("mov.b64 %0, {%1, %2};" : "=l"(s) : "f"(sc[2 * p]), "f"(sc[2 * p + 1]));
+        asm("mov.b64 %0, {%1, %2};" : "=l"(c) : "f"(bb[2 * p]), "f"(bb[2 * p + 1]));
+        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(x), "l"(s), "l"(c));
+        float lo, hi;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(d));
+        f[2 * p] = MODE == 0 ? fmaxf(lo, 0.0f) : lo;
+        f[2 * p + 1] = MODE == 0 ? fmaxf(hi, 0.0f) : hi;
+    }
+}
+
+// 16 floats -> 16 E4M3 channels (one 16-byte vector, OUT8) or 16 BF16 channels (two).
+template <bool OUT8>
+__device__ __forceinline__ void pack16(const float* f, uint4* out) {
+    uint32_t w[8];
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        if constexpr (OUT8) {
+            uint16_t r;
+            asm("cvt.rn.satfinite.e4m3x2.f32 %0, %1, %2;" : "=h"(r) : "f"(f[2 * p + 1]), "f"(f[2 * p]));
+            w[p] = r;
+        } else {
+            asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(w[p]) : "f"(f[2 * p + 1]), "f"(f[2 * p]));
+        }
+    }
+    if constexpr (OUT8) {
+        out[0] = make_uint4(w[0] | (w[1] << 16), w[2] | (w[3] << 16), w[4] | (w[5] << 16), w[6] | (w[7] << 16));
+    } else {
+        out[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        out[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+}
+
+// 16 FP32 accumulators -> y = act(acc * sc + bb) (packed FMAs), as 16 E4M3 channels
+// (one 16-byte vector, OUT8) or 16 BF16 channels (two vectors). ReLU (mode 0) is
+// applied by the conversion.
+template <int MODE, bool OUT8>
+__device__ __forceinline__ void epilogue16(const uint32_t* v, const float* sc, const float* bb, uint4* out) {
+    uint32_t w[8];
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        unsigned long long x, s, c, d;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "r"(v[2 * p]), "r"(v[2 * p + 1]));
+        asm("mov.b64 %0, {%1, %2};" : "=l"(s) : "f"(sc[2 * p]), "f"(sc[2 * p + 1]));
+        asm("mov.b64 %0, {%1, %2};" : "=l"(c) : "f"(bb[2 * p]), "f"(bb[2 * p + 1]));
+        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(x), "l"(s), "l"(c));
+        float lo, hi;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(d));
+        if constexpr (OUT8) {
+            uint16_t r;
+            if constexpr (MODE == 0)
+                asm("cvt.rn.satfinite.relu.e4m3x2.f32 %0, %1, %2;" : "=h"(r) : "f"(hi), "f"(lo));
+            else
+                asm("cvt.rn.satfinite.e4m3x2.f32 %0, %1, %2;" : "=h"(r) : "f"(hi), "f"(lo));
+            w[p] = r;
+        } else {
+            if constexpr (MODE == 0)
+                asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(w[p]) : "f"(hi), "f"(lo));
+            else
+                asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(w[p]) : "f"(hi), "f"(lo));
+        }
+    }
+    if constexpr (OUT8) {
+        out[0] = make_uint4(w[0] | (w[1] << 16), w[2] | (w[3] << 16), w[4] | (w[5] << 16), w[6] | (w[7] << 16));
+    } else {
+        out[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        out[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+}
+
+// Two CTAs per SM where the 8-row shape fits (at least two halo-row pairs of stages).
+template <int CIN, bool F8> constexpr int rs_rows() {
+    return RsShape<CIN, F8, 8>::STAGES >= 2 * RsShape<CIN, F8, 8>::NCH ? 8 : 16;
+}
+
+template <int CIN, int MODE, bool F8, bool OUT8, int ROWS_>
+__global__ void __launch_bounds__(kRsThreads, 16 / ROWS_)
     conv3x3_rs_kernel(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_w,
                       ConvArgs a, TcTiles tl, int* err) {
-    using S = RsShape<CIN, F8>;
-    constexpr int NV = OUT8 ? 2 : 4;
-    constexpr int COUT = 32, NX = S::NX, NE = S::NE, NCH = S::NCH, KC = S::KC;
+    using S = RsShape<CIN, F8, ROWS_>;
+    constexpr int COUT = 32, NX = S::NX, NCH = S::NCH, KC = S::KC, ROWS = S::ROWS, NP = ROWS / 2;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem =
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     unsigned char* ctrl = smem + (size_t)S::ST_OFF + (size_t)S::STAGES * S::STAGE;
     uint64_t* full = reinterpret_cast<uint64_t*>(ctrl);            // [STAGES]
     uint64_t* empty = full + S::STAGES;                            // [STAGES]
-    uint64_t* efull = empty + S::STAGES;                           // [NE]
-    uint64_t* eempty = efull + NE;                                 // [NE]
-    uint64_t* wbar = eempty + NE;                                  // [1]
-    uint64_t* drain = wbar + 1;                                    // [2], one per MMA issuer
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 2);
+    uint64_t* pairfull = empty + S::STAGES;                        // [NP] rows 2p, 2p + 1 accumulated
+    uint64_t* pairfree = pairfull + NP;                            // [NP] rows 2p, 2p + 1 read and zeroed
+    uint64_t* wbar = pairfree + NP;                                // [1]
+    uint64_t* drain = wbar + 1;                                    // [1]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-    float* bias_s = reinterpret_cast<float*>(ctrl + 512);           // [COUT]
-    float* ws_s = bias_s + 32;                                       // [COUT] weight scales (F8)
-    float* oinv_s = ws_s + 32;                                       // [COUT] output inverse scales (OUT8)
+    float* sc_s = reinterpret_cast<float*>(ctrl + S::CTRL);         // [COUT] accumulator scales
+    float* bb_s = sc_s + COUT;                                       // [COUT] biases (scaled)
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 1) {
@@ -614,13 +730,12 @@ __global__ void __launch_bounds__(kRsThreads, 1)
             mbar_init(s_addr(full + s), 1);
             mbar_init(s_addr(empty + s), 1);
         }
-        for (int e = 0; e < NE; ++e) {
-            mbar_init(s_addr(efull + e), 1);
-            mbar_init(s_addr(eempty + e), 8);   // one arrival per epilogue warp
+        for (int p = 0; p < NP; ++p) {
+            mbar_init(s_addr(pairfull + p), 1);
+            mbar_init(s_addr(pairfree + p), 8);   // one arrival per epilogue warp
         }
         mbar_init(s_addr(wbar), 1);
         mbar_init(s_addr(drain), 1);
-        mbar_init(s_addr(drain + 1), 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&map_x)) : "memory");
@@ -648,15 +763,16 @@ __global__ void __launch_bounds__(kRsThreads, 1)
             for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
                 const int sx = t % tl.tiles_x, rest = t / tl.tiles_x;
                 const int sy = rest % tl.tiles_y, b = rest / tl.tiles_y;
-                const int x0 = sx * kTcM, yb = sy * S::ROWS;
-                const int nrows = min(S::ROWS, a.H - yb);
-                for (int i = 0; i < nrows + 2 && ok; ++i) {
+                const int x0 = sx * kTcM, yb = sy * ROWS;
+                const int nrows = min(ROWS, a.H - yb);
+                for (int i = 0; i < nrows + 2 && ok; i += 2) {
                     for (int ch = 0; ch < NCH; ++ch) {
                         if (!mbar_wait(s_addr(empty + s), ph ^ 1u, abort_flag)) { ok = false; break; }
                         const uint32_t bar = s_addr(full + s);
                         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
-                                     "r"(S::ROW_TX)
+                                     "r"(S::STAGE_TX)
                                      : "memory");
+                        // halo rows i, i + 1 (a row past the strip's last is loaded and not used)
                         tma_load_4d(stage_base + s * S::STAGE, &map_x, ch * KC, x0 - 1, yb - 1 + i, b, bar);
                         if (++s == S::STAGES) { s = 0; ph ^= 1u; }
                     }
@@ -664,67 +780,83 @@ __global__ void __launch_bounds__(kRsThreads, 1)
             }
             if (!ok) give_up(abort_flag, err);
         }
-    } else if (warp == 1 || warp == 10) {
-        // ------------------------------------------------ MMA issuers
-        // Two threads on different schedulers issue the MMAs: warp 1 takes the even
-        // halo rows of the CTA's sequence, warp 10 the odd ones (an issuing thread
-        // spends more cycles on its control flow than a 6-MMA row keeps the tensor
-        // core busy). Each commits its own rows' stages and E buffers.
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        // Halo rows go in pairs (one stage per chunk). Pair k first touches output
+        // rows 2k, 2k + 1, whose columns must have been zeroed (pairfree[k]); the
+        // output pairs whose last tap it adds are committed to pairfull.
         if (lane == 0) {
-            const unsigned who = warp == 1 ? 0u : 1u;
-            constexpr uint32_t IDESC = instr_desc(kTcM, NX, F8);
+            constexpr uint32_t IDESC0 = instr_desc(kTcM, 0, F8);   // N added per MMA
             constexpr uint32_t HI = (uint32_t)((8 * S::ROWB) >> 4) | (1u << 14) | (S::LAYOUT << 29);
-            // stage of this issuer's next chunk and E buffer of its next row, with their parities
-            int s = (int)(who * NCH) % S::STAGES;
-            uint32_t ph = (who * NCH) / S::STAGES;
-            int e = (int)who;
-            uint32_t eph = 0;
-            unsigned J = 0;   // running halo-row index of this CTA
+            int s = 0;
+            uint32_t ph = 0;
+            uint32_t pf_ph = 0;   // bit p: parity of the next phase of pairfree[p]
             bool ok = mbar_wait(s_addr(wbar), 0, abort_flag), issued = false;
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const uint32_t w_lo = ((smem_base >> 4) & 0x3FFFu) | (1u << 16);
             for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
                 const int sy = (t / tl.tiles_x) % tl.tiles_y;
-                const int nh = min(S::ROWS, a.H - sy * S::ROWS) + 2;
-                for (int i = 0; i < nh && ok; ++i, ++J) {
-                    if ((J & 1u) != who) continue;
-                    if (!mbar_wait(s_addr(eempty + e), eph ^ 1u, abort_flag)) { ok = false; break; }
-                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    const uint32_t d = tmem + (uint32_t)(e * NX);
+                const int nrows = min(ROWS, a.H - sy * ROWS);
+                const int nh = nrows + 2;
+                int next_p = 0;   // next output pair to commit
+                for (int i0 = 0; i0 < nh && ok; i0 += 2) {
                     for (int ch = 0; ch < NCH; ++ch) {
-                        if (!mbar_wait(s_addr(full + s), ph, abort_flag)) { ok = false; break; }
-                        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                        const uint32_t a_lo = (((stage_base + s * S::STAGE) >> 4) & 0x3FFFu) | (1u << 16);
-                        const uint32_t b_lo = w_lo + (uint32_t)((ch * S::WCH) >> 4);
+                        const int sc = (s + ch) % S::STAGES;
+                        const uint32_t pc = ph ^ (uint32_t)((s + ch) / S::STAGES);
+                        if (!mbar_wait(s_addr(full + sc), pc, abort_flag)) { ok = false; break; }
+                    }
+                    const int k = i0 >> 1;
+                    if (ok && 2 * k < nrows) {   // rows 2k, 2k + 1 start here: wait until they are zero
+                        ok = mbar_wait(s_addr(pairfree + k), (pf_ph >> k) & 1u, abort_flag);
+                        pf_ph ^= 1u << k;
+                    }
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    for (int r = 0; r < 2; ++r) {
+                        const int i = i0 + r;
+                        if (i >= nh) break;
+                        // taps of halo row i that land on rows 0 .. nrows - 1
+                        const int ky_lo = max(0, i - nrows + 1), ky_hi = min(2, i);
+                        const uint32_t d = tmem + (uint32_t)(32 * (ROWS - 1 - i + ky_lo));
+                        const uint32_t idesc = IDESC0 | ((uint32_t)(4 * (ky_hi - ky_lo + 1)) << 17);
+                        const uint32_t b_ky = (uint32_t)((32 * ky_lo * S::ROWB) >> 4);
+                        for (int ch = 0; ch < NCH; ++ch) {
+                            const int sc = (s + ch) % S::STAGES;
+                            const uint32_t a_lo =
+                                (((stage_base + sc * S::STAGE + r * S::HROW) >> 4) & 0x3FFFu) | (1u << 16);
+                            const uint32_t b_lo = w_lo + (uint32_t)((ch * S::WCH) >> 4) + b_ky;
+                            const int kss = ch == NCH - 1 ? S::KS_LAST : S::KS;
 #pragma unroll
-                        for (int kx = 0; kx < 3; ++kx) {
+                            for (int kx = 0; kx < 3; ++kx) {
 #pragma unroll
-                            for (int ks = 0; ks < S::ROWB / 32; ++ks) {
-                                const uint32_t av = a_lo + (uint32_t)((kx * S::ROWB + ks * 32) >> 4);
-                                const uint32_t bv = b_lo + (uint32_t)((kx * NX * S::ROWB + ks * 32) >> 4);
-                                const uint32_t accum = (ch > 0 || kx > 0 || ks > 0) ? 1u : 0u;
-                                umma<F8>(d, av, bv, HI, IDESC, accum);
+                                for (int ks = 0; ks < S::KS; ++ks) {
+                                    if (ks >= kss) break;
+                                    const uint32_t av = a_lo + (uint32_t)((kx * S::ROWB + ks * 32) >> 4);
+                                    const uint32_t bv = b_lo + (uint32_t)((kx * NX * S::ROWB + ks * 32) >> 4);
+                                    umma<F8>(d, av, bv, HI, idesc, 1u);
+                                }
                             }
                         }
                         issued = true;
+                    }
+                    // output pair p is complete once halo row (its last row) + 2 is in
+                    const int last = min(i0 + 1, nh - 1);
+                    while (2 * next_p < nrows && min(2 * next_p + 1, nrows - 1) + 2 <= last) {
+                        mma_commit(s_addr(pairfull + next_p));
+                        ++next_p;
+                    }
+                    for (int ch = 0; ch < NCH; ++ch) {
                         mma_commit(s_addr(empty + s));
                         if (++s == S::STAGES) { s = 0; ph ^= 1u; }
                     }
-                    if (!ok) break;
-                    mma_commit(s_addr(efull + e));
-                    // skip the other issuer's row: its NCH stages and its E buffer
-                    s += NCH;
-                    if (s >= S::STAGES) { s -= S::STAGES; ph ^= 1u; }
-                    e += 2;
-                    if (e >= NE) { e -= NE; eph ^= 1u; }
                 }
             }
             if (!ok) {
                 give_up(abort_flag, err);
                 if (issued) {
-                    mma_commit(s_addr(drain + who));
+                    mma_commit(s_addr(drain));
                     const unsigned long long deadline = global_ns() + kWaitNs;
-                    while (!mbar_test(s_addr(drain + who), 0) && global_ns() < deadline) {
+                    while (!mbar_test(s_addr(drain), 0) && global_ns() < deadline) {
                     }
                 }
             }
@@ -732,85 +864,105 @@ __global__ void __launch_bounds__(kRsThreads, 1)
     } else {
         // ------------------------------------------------ epilogue (warps 2..9)
         // Two groups of four warps (one per TMEM lane quarter) split the 32 output
-        // channels (16 each). Halo row h's E is consumed as soon as it is complete:
-        // its ky 2 block completes output row h - 1, its ky 1 block is added to the
-        // partial sum of row h and its ky 0 block starts row h + 1. Each thread keeps
-        // those two partial rows in registers, so every E buffer is released right
-        // after it has been read (4 warps x 2 groups = 8 arrivals).
+        // channels (16 each); every thread owns one pixel of a row and handles the
+        // rows in pairs (the 2x2 mean of a pooled output needs both).
         const int q = warp & 3;
         const int grp = (warp - 2) >> 2;
         const int c0 = 16 * grp;                // first output channel of this group
         constexpr int NVG = OUT8 ? 1 : 2;       // 16-byte output vectors per 16 channels
         const int et = tid - 64;
         for (int c = et; c < COUT; c += 256) {
-            if (MODE != 2) bias_s[c] = a.bias[c];
-            if (F8) ws_s[c] = a.wscale[c];
-            if (OUT8) oinv_s[c] = a.oinv[c];
+            // y = act((acc * wscale + bias) * oinv) = act(acc * (wscale * oinv) + bias * oinv), oinv > 0
+            float sc = F8 ? a.wscale[c] : 1.0f, bb = MODE != 2 ? a.bias[c] : 0.0f;
+            if (OUT8) {
+                const float o = a.oinv[c];
+                sc *= o;
+                bb *= o;
+            }
+            sc_s[c] = sc;
+            bb_s[c] = bb;
         }
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+        // every row slot starts at zero: the MMAs only accumulate
+#pragma unroll
+        for (int j = 0; j < ROWS; ++j) tmem_st16_zero(lane_base + (uint32_t)(32 * j));
+        asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncwarp();
+        if (lane == 0)
+            for (int p = 0; p < NP; ++p)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(s_addr(pairfree + p)) : "memory");
         asm volatile("bar.sync 1, 256;\n" ::: "memory");
+        float sc[16], bb[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            sc[j] = sc_s[c0 + j];
+            bb[j] = bb_s[c0 + j];
+        }
         const bool pooling = a.pool.p != nullptr;
-        uint4 held[NVG];
-        float part1[16], part2[16];             // partial sums of output rows h and h + 1
-        unsigned J = 0;
+        uint32_t pf_ph = 0;   // bit p: parity of the next phase of pairfull[p]
         bool ok = true;
         for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
             const int sx = t % tl.tiles_x, rest = t / tl.tiles_x;
             const int sy = rest % tl.tiles_y, b = rest / tl.tiles_y;
-            const int yb = sy * S::ROWS;
-            const int nrows = min(S::ROWS, a.H - yb);
+            const int yb = sy * ROWS;
+            const int nrows = min(ROWS, a.H - yb);
             const int px = sx * kTcM + q * 32 + lane;
             const bool valid = px < a.W;
-            for (int i = 0; i < nrows + 2 && ok; ++i, ++J) {
+            for (int p = 0; 2 * p < nrows; ++p) {
                 int ready = 0;
-                if (lane == 0) ready = mbar_wait(s_addr(efull + J % NE), (J / NE) & 1u, abort_flag) ? 1 : 0;
+                if (lane == 0) ready = mbar_wait(s_addr(pairfull + p), (pf_ph >> p) & 1u, abort_flag) ? 1 : 0;
                 ready = __shfl_sync(0xffffffffu, ready, 0);
+                pf_ph ^= 1u << p;
                 if (!ready) {
                     if (lane == 0) give_up(abort_flag, err);
                     ok = false;
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((J % NE) * NX + c0);
-                uint32_t k0v[16], k1v[16], k2v[16];
-                tmem_ld16(base + 0, k0v);
-                tmem_ld16(base + 32, k1v);
-                tmem_ld16(base + 64, k2v);
+                const bool two = 2 * p + 1 < nrows;
+                const uint32_t ta0 = lane_base + (uint32_t)(32 * (ROWS - 1 - 2 * p));   // row 2p
+                const uint32_t ta1 = ta0 - 32u;                                          // row 2p + 1
+                uint32_t v0[16], v1[16];
+                tmem_ld16(ta0, v0);
+                tmem_ld16(ta1, v1);
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                tmem_st16_zero(ta0);
+                tmem_st16_zero(ta1);
+                uint4 o0[NVG], o1[NVG], om[NVG];
+                if (pooling) {
+                    // the 2x2 mean of the activations in FP32 (H is even when pooling, so the pair is whole)
+                    float f0[16], f1[16];
+                    act16<MODE>(v0, sc, bb, f0);
+                    act16<MODE>(v1, sc, bb, f1);
+                    pack16<OUT8>(f0, o0);
+                    pack16<OUT8>(f1, o1);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const float m = f0[j] + f1[j];
+                        f0[j] = (m + __shfl_down_sync(0xffffffffu, m, 1)) * 0.25f;
+                    }
+                    pack16<OUT8>(f0, om);
+                } else {
+                    epilogue16<MODE, OUT8>(v0, sc, bb, o0);
+                    epilogue16<MODE, OUT8>(v1, sc, bb, o1);
+                }
+                asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
                 __syncwarp();
                 if (lane == 0)
-                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(s_addr(eempty + J % NE)) : "memory");
-                // halo row h = yb - 1 + i completes output row y = h - 1 = yb + i - 2
-                if (i >= 2) {
-                    const int y = yb + i - 2;
-                    float f[16];
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(s_addr(pairfree + p)) : "memory");
+                const int y = yb + 2 * p;   // even: strips start on multiples of 8
+                bf16* yp0 = a.y.p + a.y.at(b, valid ? (size_t)y * a.W + px : 0, 0);
+                bf16* yp1 = a.y.p + a.y.at(b, valid && two ? (size_t)(y + 1) * a.W + px : 0, 0);
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) f[j] = part1[j] + __uint_as_float(k2v[j]);
-                    uint4 o[NVG];
-                    epilogue_n<16, MODE, F8, OUT8>(f, c0, bias_s, ws_s, oinv_s, o);
-                    bf16* yp = a.y.p + a.y.at(b, valid ? (size_t)y * a.W + px : 0, 0);
-#pragma unroll
-                    for (int g = 0; g < NVG; ++g) {
-                        const int k = c0 / (OUT8 ? 16 : 8) + g;   // 16-byte vector of the pixel
-                        if (valid) *reinterpret_cast<uint4*>(yp + (size_t)k * (size_t)a.y.grp) = o[g];
-                        if (pooling) {
-                            if ((y & 1) == 0) {
-                                held[g] = o[g];
-                            } else {
-                                const uint4 nh = shfl_down_u4(held[g], 1), nc = shfl_down_u4(o[g], 1);
-                                if (valid && (lane & 1) == 0)
-                                    *reinterpret_cast<uint4*>(
-                                        a.pool.p + a.pool.at(b, (size_t)(y / 2) * (a.W / 2) + px / 2, k)) =
-                                        mean4<OUT8>(held[g], nh, o[g], nc);
-                            }
-                        }
-                    }
-                }
-                // (E_{h-1} ky 0 + E_h ky 1) for row h, E_h ky 0 starts row h + 1
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    part1[j] = part2[j] + __uint_as_float(k1v[j]);
-                    part2[j] = __uint_as_float(k0v[j]);
+                for (int g = 0; g < NVG; ++g) {
+                    const int k = c0 / (OUT8 ? 16 : 8) + g;   // 16-byte vector of the pixel
+                    if (valid) *reinterpret_cast<uint4*>(yp0 + (size_t)k * (size_t)a.y.grp) = o0[g];
+                    if (valid && two) *reinterpret_cast<uint4*>(yp1 + (size_t)k * (size_t)a.y.grp) = o1[g];
+                    if (pooling && valid && (lane & 1) == 0)
+                        *reinterpret_cast<uint4*>(a.pool.p + a.pool.at(b, (size_t)(y / 2) * (a.W / 2) + px / 2, k)) =
+                            om[g];
                 }
             }
         }
@@ -890,19 +1042,21 @@ static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
 
 template <int CIN, int MODE, bool F8, bool OUT8>
 static cudaError_t run_rs(const ConvArgs& a, int* err, cudaStream_t s) {
-    using S = RsShape<CIN, F8>;
+    constexpr int ROWS_ = rs_rows<CIN, F8>();
+    using S = RsShape<CIN, F8, ROWS_>;
     constexpr cuuint64_t EB = F8 ? 1 : 2;   // bytes per element
     const CUtensorMapDataType dt = F8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
     if (a.pool.p && (!view_ok(a.pool) || (a.H | a.W) & 1)) return cudaErrorInvalidValue;
     auto encode = encode_fn();
     if (!encode) return cudaErrorNotSupported;
-    const CUtensorMapSwizzle swz = S::ROWB == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+    const CUtensorMapSwizzle swz = S::ROWB == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                   : S::ROWB == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
     CUtensorMap mx, mw;
     const cuuint32_t one[4] = {1, 1, 1, 1};
-    // NHWC input view: {CIN channels, W, H, B}, box {KC, 130, 1 row, 1} (channels past CIN read as zero)
+    // NHWC input view: {CIN channels, W, H, B}, box {KC, 130, 2 rows, 1} (channels past CIN read as zero)
     const cuuint64_t xdim[4] = {(cuuint64_t)CIN, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.B};
     const cuuint64_t xstr[3] = {(cuuint64_t)a.x.pix * 2, (cuuint64_t)a.x.pix * a.W * 2, (cuuint64_t)a.x.img * 2};
-    const cuuint32_t xbox[4] = {(cuuint32_t)S::KC, (cuuint32_t)kHaloPix, 1, 1};
+    const cuuint32_t xbox[4] = {(cuuint32_t)S::KC, (cuuint32_t)kHaloPix, (cuuint32_t)S::HPS, 1};
     if (encode(&mx, dt, 4, (void*)a.x.p, xdim, xstr, xbox, one, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
@@ -922,10 +1076,10 @@ static cudaError_t run_rs(const ConvArgs& a, int* err, cudaStream_t s) {
     tl.total = (int)total;
     const int sms = sm_count();
     if (sms <= 0) return cudaErrorInvalidDevice;
-    auto kern = conv3x3_rs_kernel<CIN, MODE, F8, OUT8>;
+    auto kern = conv3x3_rs_kernel<CIN, MODE, F8, OUT8, ROWS_>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
     if (e != cudaSuccess) return e;
-    const int grid = tl.total < sms ? tl.total : sms;
+    const int grid = tl.total < sms * S::CTAS ? tl.total : sms * S::CTAS;
     kern<<<grid, kRsThreads, S::SMEM, s>>>(mx, mw, a, tl, err);
     return cudaGetLastError();
 }

@@ -378,6 +378,8 @@ __global__ void pool_bwd_kernel(View dout, View din, int B, int H, int W, int g8
 // nearest 2x upsampling: out[b, y, x] = in[b, y/2, x/2]
 template <bool PIXFAST>
 __global__ void up_fwd_kernel(View in, View out, int B, int H, int W, int g8) {
+    pdl_wait();
+    pdl_trigger();
     const unsigned n = (unsigned)B * H * W * g8;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -440,9 +442,8 @@ cudaError_t up_fwd(const View& in, const View& out, int B, int H, int W, int c, 
     const size_t n = (size_t)B * H * W * (c / 8);
     if (!view_ok(in) || !view_ok(out) || !launch_ok(n, c)) return cudaErrorInvalidValue;
     if (n == 0) return cudaSuccess;
-    if (out.grp == 8) up_fwd_kernel<false><<<blocks_for(n), 256, 0, s>>>(in, out, B, H, W, c / 8);
-    else up_fwd_kernel<true><<<blocks_for(n), 256, 0, s>>>(in, out, B, H, W, c / 8);
-    return cudaGetLastError();
+    if (out.grp == 8) return launch_pdl(up_fwd_kernel<false>, dim3(blocks_for(n)), dim3(256), 0, s, in, out, B, H, W, c / 8);
+    return launch_pdl(up_fwd_kernel<true>, dim3(blocks_for(n)), dim3(256), 0, s, in, out, B, H, W, c / 8);
 }
 cudaError_t up_bwd(const View& dout, const View& din, int B, int Hi, int Wi, int c, cudaStream_t s) {
     const size_t n = (size_t)B * Hi * Wi * (c / 8);
@@ -464,6 +465,8 @@ __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
     // the block's 32 x 8 pixels of `noisy` with a 2-pixel edge-clamped border
     __shared__ float4 tile[kApplyTY + 4][kApplyTX + 4];
     __shared__ float red[8];
+    pdl_wait();
+    pdl_trigger();
     const int tx = threadIdx.x % kApplyTX, ty = threadIdx.x / kApplyTX;
     const int x0 = blockIdx.x * kApplyTX, y0 = blockIdx.y * kApplyTY, b = blockIdx.z;
     const int H = a.H, W = a.W;
@@ -556,12 +559,10 @@ cudaError_t kpcn_apply(const ApplyArgs& a, cudaStream_t s) {
     dim3 grid((a.W + kApplyTX - 1) / kApplyTX, (a.H + kApplyTY - 1) / kApplyTY, a.B);
     if (a.target) {
         if (!a.loss || !a.target) return cudaErrorInvalidValue;
-        kpcn_apply_kernel<true><<<grid, 256, 0, s>>>(a);
-    } else {
-        if (!a.out) return cudaErrorInvalidValue;
-        kpcn_apply_kernel<false><<<grid, 256, 0, s>>>(a);
+        return launch_pdl(kpcn_apply_kernel<true>, grid, dim3(256), 0, s, a);
     }
-    return cudaGetLastError();
+    if (!a.out) return cudaErrorInvalidValue;
+    return launch_pdl(kpcn_apply_kernel<false>, grid, dim3(256), 0, s, a);
 }
 
 // ------------------------------------------------------------------ Adam --

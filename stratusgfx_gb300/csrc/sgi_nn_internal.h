@@ -128,5 +128,30 @@ cudaError_t quantize_weights(const float* w, const float* s_in, int cin, int cou
 cudaError_t quantize_act(const View& in, const View& out, int C, int B, int H, int W, const float* inv,
                          cudaStream_t s);
 
+#ifdef __CUDACC__
+// Programmatic dependent launch: the kernel may be scheduled while the previous
+// kernel of the stream is still finishing. Every kernel launched this way calls
+// pdl_wait() before its first global-memory access (which returns once the
+// previous kernel has completed and its writes are visible) and pdl_trigger() to
+// let the next kernel be scheduled early in turn.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+#endif
+
 }  // namespace nn
 }  // namespace sgi

@@ -388,6 +388,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    pdl_wait();   // every global access below follows the previous kernel's completion
+    pdl_trigger();
     const uint32_t tmem = *tmem_slot;
     const uint32_t smem_base = s_addr(smem);
 
@@ -744,6 +746,8 @@ __global__ void __launch_bounds__(kRsThreads, 16 / ROWS_)
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    pdl_wait();   // every global access below follows the previous kernel's completion
+    pdl_trigger();
     const uint32_t tmem = *tmem_slot;
     const uint32_t smem_base = s_addr(smem);
     const uint32_t stage_base = smem_base + S::ST_OFF;
@@ -1036,8 +1040,7 @@ static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
     if (e != cudaSuccess) return e;
     const int grid = tl.total < sms ? tl.total : sms;
-    kern<<<grid, kThreads, S::SMEM, s>>>(mx, mw, a, tl, err);
-    return cudaGetLastError();
+    return launch_pdl(kern, dim3(grid), dim3(kThreads), S::SMEM, s, mx, mw, a, tl, err);
 }
 
 template <int CIN, int MODE, bool F8, bool OUT8>
@@ -1080,8 +1083,7 @@ static cudaError_t run_rs(const ConvArgs& a, int* err, cudaStream_t s) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
     if (e != cudaSuccess) return e;
     const int grid = tl.total < sms * S::CTAS ? tl.total : sms * S::CTAS;
-    kern<<<grid, kRsThreads, S::SMEM, s>>>(mx, mw, a, tl, err);
-    return cudaGetLastError();
+    return launch_pdl(kern, dim3(grid), dim3(kRsThreads), S::SMEM, s, mx, mw, a, tl, err);
 }
 
 // 32-channel outputs take the row-streaming kernel, wider ones the 9-tap kernel.

@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["hd", "small"], default="hd")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-uhd", action="store_true", help="skip the 3840x2160 neural/plain comparison")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: the same 1080p workload with a 2-frame path, "
                          "--warmup + --steps frames of sgi_render_frame only (no e2e or CPU legs)")
@@ -327,6 +328,9 @@ def run_ours(args, rank, world, local_rank):
         result.update(neural_vs_plain(args, ds, sc, w, cfg, flush))
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline_from_device(ds, sc, w, cfg)
+    if rank == 0 and not args.no_uhd and w.name == S.HD.name:
+        del ds
+        result.update(uhd_comparison(args, flush))
     st.close()
     st2.close()
     return result
@@ -442,27 +446,39 @@ def time_frames(render, ds, frames, steps, warmup, flush):
     return ms / steps
 
 
-def neural_vs_plain(args, ds, sc, w, cfg, flush):
-    """The metric's comparison: plain a-trous at K = 8..64 against the learned denoiser at K = 8, 4, 2;
-    ms/frame (device-resident) and PSNR against the converged frame (equal_psnr below)."""
-    import ctypes as C
-
+def measure_runs(runs, res, net, ds, sc, w, targets, flush, steps):
+    """For each (name, render, label, config overrides): ms/frame over `steps` frames (device-resident,
+    L2 flushed) and PSNR of the HDR frame and of its GI term against the converged frames;
+    res[name][label] receives the numbers. Names starting with "neural_fp8" run the U-Net in FP8."""
     import torch
 
-    from stratusgfx_gb300 import abi, denoiser, stage
-    if not os.path.exists(denoiser.WEIGHTS):
-        return {"neural": {"unavailable": f"no trained weights at {denoiser.WEIGHTS}"}}
-    targets, target_ms = converged_targets(ds, sc, w, cfg)
-    frames = len(sc.cameras) - 1
+    from stratusgfx_gb300 import abi, stage
     H, W = w.height, w.width
-    net = denoiser.KpcnDenoiser(1, H, W)
-    net.load(denoiser.WEIGHTS)
-    # FP8 scales calibrated on a frame of another room (seed 777), not on the measured frames
-    calib = denoiser.make_dataset(1, H=H, W=W, frames_per_room=2, seed=777, samples=(2,), batches=1,
-                                  log=lambda *a: None)
-    net.calibrate_fp8(calib.feat[:1])
-    del calib
-    res = {"plain": {}, "neural": {}, "neural_fp8": {}}
+    frames = len(sc.cameras) - 1
+    out = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+    for name, render, label, kw in runs:
+        if net is not None:
+            net.set_precision(abi.SGI_NN_FP8 if name.startswith("neural_fp8") else abi.SGI_NN_BF16)
+        kcfg = stage.workload_config(w, **kw)
+        st = stage.GiStage(kcfg)
+        st.set_lights(ds.vpls, ds.entries, ds.points)
+
+        def one(k, s, st=st, render=render):
+            st.set_shadow_maps(ds.csms[k], ds.cubes)
+            render(st, k, out)
+
+        ms = time_frames(one, ds, frames, steps, 3, flush)
+        st.close()
+        p_full, p_gi = psnr_vs_converged(render, ds, sc, w, kcfg, targets)
+        res.setdefault(name, {})[label] = {"ms_per_frame": round(ms, 4), "mpix_s": round(W * H / ms / 1e3, 1),
+                                           "psnr_db": p_full, "psnr_gi_db": p_gi}
+
+
+def render_fns(ds, net):
+    """The plain and the neural frame of frame k into `out`, on context `st`."""
+    import ctypes as C
+
+    from stratusgfx_gb300 import abi, stage
 
     def plain_render(st, k, out):
         st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * k, 60.0)
@@ -473,26 +489,65 @@ def neural_vs_plain(args, ds, sc, w, cfg, flush):
                                                  C.byref(ds.gbuffers[k - 1].struct()), C.byref(ds.camera(k)),
                                                  C.byref(fp), C.c_void_p(out.data_ptr()),
                                                  stage._stream_ptr(None)), st.ctx)
+    return plain_render, neural_render
 
-    out = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+
+def uhd_comparison(args, flush):
+    """3840x2160 with 4096 VPLs at K = 4: the plain a-trous frame, the BF16 U-Net frame and the FP8
+    U-Net frame (scales calibrated on a frame of another room); ms/frame and PSNR against the
+    converged (K = 512, FP64) frames."""
+    from stratusgfx_gb300 import denoiser, stage
+    from stratusgfx_gb300 import scene as S
+    if not os.path.exists(denoiser.WEIGHTS):
+        return {"uhd": {"unavailable": f"no trained weights at {denoiser.WEIGHTS}"}}
+    w = S.UHD
+    sc = S.workload_scene(w, 1234 + 4)
+    ds = stage.DeviceScene(sc, w)
+    cfg = stage.workload_config(w)
+    targets, target_ms = converged_targets(ds, sc, w, cfg)
+    net = denoiser.KpcnDenoiser(1, w.height, w.width)
+    net.load(denoiser.WEIGHTS)
+    calib = denoiser.make_dataset(1, H=w.height, W=w.width, frames_per_room=2, seed=778, samples=(2,), batches=1,
+                                  log=lambda *a: None)
+    net.calibrate_fp8(calib.feat[:1])
+    del calib
+    plain_render, neural_render = render_fns(ds, net)
+    K = w.samples
+    runs = [("plain", plain_render, f"K{K}", {}), ("neural_bf16", neural_render, f"K{K}", {}),
+            ("neural_fp8", neural_render, f"K{K}", {})]
+    res = {}
+    measure_runs(runs, res, net, ds, sc, w, targets, flush, max(6, args.steps // 4))
+    net.close()
+    out = {"workload": w.name, "resolution": f"{w.width}x{w.height}", "vpls": w.num_vpls,
+           "cube": f"6x{w.cube_size}^2 fp16", "samples_per_pixel": K, "frames": len(sc.cameras) - 1}
+    for name in ("plain", "neural_bf16", "neural_fp8"):
+        out[name] = res[name][f"K{K}"]
+    out["converged_target"] = {"samples_per_pixel": 512, "accumulation": "fp64", "ms_per_frame": round(target_ms, 2)}
+    return {"uhd": out}
+
+
+def neural_vs_plain(args, ds, sc, w, cfg, flush):
+    """The metric's comparison: plain a-trous at K = 8..64 against the learned denoiser at K = 8, 4, 2;
+    ms/frame (device-resident) and PSNR against the converged frame (equal_psnr below)."""
+    from stratusgfx_gb300 import denoiser
+    if not os.path.exists(denoiser.WEIGHTS):
+        return {"neural": {"unavailable": f"no trained weights at {denoiser.WEIGHTS}"}}
+    targets, target_ms = converged_targets(ds, sc, w, cfg)
+    H, W = w.height, w.width
+    net = denoiser.KpcnDenoiser(1, H, W)
+    net.load(denoiser.WEIGHTS)
+    # FP8 scales calibrated on a frame of another room (seed 777), not on the measured frames
+    calib = denoiser.make_dataset(1, H=H, W=W, frames_per_room=2, seed=777, samples=(2,), batches=1,
+                                  log=lambda *a: None)
+    net.calibrate_fp8(calib.feat[:1])
+    del calib
+    res = {"plain": {}, "neural": {}, "neural_fp8": {}}
+    plain_render, neural_render = render_fns(ds, net)
+
     runs = [("plain", plain_render, f"K{K}", dict(samples_per_pixel=K)) for K in (8, 16, 32, 64)]
     runs += [("neural", neural_render, f"K{K}", dict(samples_per_pixel=K)) for K in (8, 4, 2, 1)]
     runs += [("neural_fp8", neural_render, f"K{K}", dict(samples_per_pixel=K)) for K in (8, 4, 2, 1)]
-    for name, render, label, kw in runs:
-        net.set_precision(abi.SGI_NN_FP8 if name == "neural_fp8" else abi.SGI_NN_BF16)
-        kcfg = stage.workload_config(w, **kw)
-        st = stage.GiStage(kcfg)
-        st.set_lights(ds.vpls, ds.entries, ds.points)
-
-        def one(k, s, st=st, render=render):
-            st.set_shadow_maps(ds.csms[k], ds.cubes)
-            render(st, k, out)
-
-        ms = time_frames(one, ds, frames, max(8, args.steps // 2), 3, flush)
-        st.close()
-        p_full, p_gi = psnr_vs_converged(render, ds, sc, w, kcfg, targets)
-        res[name][label] = {"ms_per_frame": round(ms, 4), "mpix_s": round(W * H / ms / 1e3, 1),
-                            "psnr_db": p_full, "psnr_gi_db": p_gi}
+    measure_runs(runs, res, net, ds, sc, w, targets, flush, max(8, args.steps // 2))
     net.close()
     # Equal PSNR. The plain path's quality saturates with K (the a-trous filter's bias, not
     # the sample count, bounds its error against the converged frame), so the comparison is:

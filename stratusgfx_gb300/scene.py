@@ -330,6 +330,9 @@ SMALL = Workload("room12_320x180_vpl64_k8", 320, 180, 12, 64, 0, 1024, 64, 0, 8,
 # plain method, 1920x1080, 40 boxes, 4 point lights, 4x2048^2 CSM, 2048 VPLs with
 # 6x128^2 FP16 cubes, <= 64 VPLs per 16x16 tile, K = 8, 8 frames
 HD = Workload("room40_1920x1080_vpl2048_k8", 1920, 1080, 40, 2048, 4, 2048, 128, 1, 8, 5, 8)
+# 3840x2160, the same room generator, 4096 VPLs with 6x128^2 FP16 cubes, K = 4, 4-frame path
+# (the neural comparison at 4K: plain a-trous vs the BF16 and FP8 U-Net)
+UHD = Workload("room40_3840x2160_vpl4096_k4", 3840, 2160, 40, 4096, 4, 2048, 128, 1, 4, 5, 4)
 
 
 def workload_scene(w: Workload, seed: int) -> Scene:

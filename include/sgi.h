@@ -306,6 +306,17 @@ sgi_status sgi_get_pass_times(sgi_ctx* ctx, float* ms, int32_t n);
 /* Kernel launches the context issued since creation (all sgi_* calls). */
 int64_t sgi_launch_count(const sgi_ctx* ctx);
 
+/* Thread-block shape of a per-pixel pass (no counterpart in StratusGFX, whose
+ * fragment shaders have no block shape). Every shape computes the same pixels
+ * bit for bit; the fastest depends on the viewport, which is what
+ * sgi_batch_create's autotuner (sgi_batch.h) measures. bx * by must be 256 with
+ * bx a multiple of 8; (0, 0) restores the pass's default (gather 16x16, the
+ * others 32x8). */
+enum { SGI_BLOCK_GATHER = 0, SGI_BLOCK_ATROUS = 1, SGI_BLOCK_DENOISE_FINAL = 2, SGI_BLOCK_DIRECT = 3,
+       SGI_NUM_BLOCK_PASSES = 4 };
+sgi_status sgi_set_block_shape(sgi_ctx* ctx, int32_t pass, int32_t bx, int32_t by);
+sgi_status sgi_get_block_shape(const sgi_ctx* ctx, int32_t pass, int32_t* bx, int32_t* by);
+
 #ifdef __cplusplus
 }
 #endif

@@ -104,7 +104,14 @@ class SceneCamera(C.Structure):
                 ("prev_proj_view", C.c_float * 16), ("position", C.c_float * 4)]
 
 
+class View(C.Structure):          # sgi_view (sgi_batch.h)
+    _fields_ = [("ctx", C.c_void_p), ("cur", C.c_void_p), ("prev", C.c_void_p), ("cam", C.c_void_p),
+                ("params", FrameParams), ("hdr_out", C.c_void_p)]
+
+
 assert C.sizeof(Vpl) == 64 and C.sizeof(PointLight) == 48 and C.sizeof(AtlasEntry) == 8 and C.sizeof(Box) == 64
+
+SGI_BLOCK_GATHER, SGI_BLOCK_ATROUS, SGI_BLOCK_DENOISE_FINAL, SGI_BLOCK_DIRECT = 0, 1, 2, 3
 
 SGI_NN_CONV_WARP_MMA = 0
 SGI_NN_CONV_TCGEN05 = 1
@@ -163,6 +170,14 @@ EXPORTS = {
     "sgi_scene_csm": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(Csm), C.POINTER((C.c_float * 16) * 4), C.c_void_p]),
     "sgi_scene_cube_atlas": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                          C.POINTER(CubeAtlas), C.c_void_p]),
+    "sgi_set_block_shape": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "sgi_get_block_shape": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "sgi_batch_create": (C.c_int32, [C.POINTER(View), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
+                                     C.POINTER(C.c_void_p)]),
+    "sgi_batch_launch": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "sgi_batch_kernel_count": (C.c_int64, [C.c_void_p]),
+    "sgi_batch_destroy": (C.c_int32, [C.c_void_p]),
+    "sgi_batch_last_error": (C.c_char_p, [C.c_void_p]),
 }
 
 _lib = None

@@ -18,70 +18,11 @@
 #include "../../include/sgi.h"
 #include "../../include/sgi_nn.h"
 #include "../../include/sgi_scene.h"
+#include "sgi_ctx.h"
 #include "sgi_internal.h"
 #include "sgi_nn_internal.h"
 #include "sgi_nn_net.h"
 
-struct sgi_ctx {
-    sgi_config cfg;
-    sgi::ShadeConfig sc;
-    std::string err;
-    int64_t launches = 0;
-    int device = 0;
-
-    // lights
-    sgi_vpl* vpls = nullptr;
-    sgi_atlas_entry* entries = nullptr;
-    int32_t num_vpls = 0;
-    sgi_point_light* points = nullptr;
-    int32_t num_points = 0;
-    bool lights_set = false;
-    bool maps_set = false;
-    sgi_csm csm;
-    sgi_cube_atlas cubes;
-
-    // culling scratch
-    uint8_t* flags = nullptr;
-    sgi_vpl* cv = nullptr;
-    sgi_atlas_entry* ce = nullptr;
-    int32_t* visible_index = nullptr;
-    sgi_tile_stage1* stage1 = nullptr;
-    int32_t* lists = nullptr;
-    uint32_t* tile_keys = nullptr;
-    int32_t num_tiles = 0;
-    bool culled = false;
-
-    // GI scratch
-    uint2* reservoir = nullptr;
-    uint2* ping[2] = {nullptr, nullptr};
-    uint2* merged = nullptr;                // denoise pass-0 output (kept for the learned denoiser)
-    uint2* pass_bufs[SGI_MAX_DENOISE_PASSES] = {};
-    uint2* direct = nullptr;
-    float4* guide = nullptr;
-    uint2* gi_hist[2] = {nullptr, nullptr};
-    uint16_t* hist_depth[2] = {nullptr, nullptr};
-    int hist_cur = 0;
-    bool have_history = false;
-    const uint2* last_merged = nullptr;   // pass-0 output of the last gather
-    int feat_hist = 0;                    // history slot that was "previous" for the last gather
-    bool feat_have_history = false;
-
-    // learned-denoiser inputs/outputs (allocated on first use)
-    __nv_bfloat16* nn_feat = nullptr;
-    float4* nn_noisy = nullptr;
-    float4* nn_prev = nullptr;
-    float4* nn_den = nullptr;
-
-    // timing
-    bool timing = false;
-    cudaEvent_t ev[SGI_NUM_PASS_TIMES + 1] = {};
-    bool have_times = false;
-
-    // direct lighting runs on a side stream, concurrently with the VPL and tile
-    // culls and the GI gather, and joins before the final composite
-    cudaStream_t side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
-};
 
 namespace {
 
@@ -378,7 +319,8 @@ sgi_status sgi_direct_lighting(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_
     if (!gbuffer_ok(gbuf, true) || !cam || !hdr_out) return fail(ctx, SGI_ERR_ARG, "NULL G-buffer, camera or output");
     if (!ctx->lights_set || !ctx->maps_set) return fail(ctx, SGI_ERR_STATE, "set lights and shadow maps first");
     SGI_CUDA(ctx, sgi::launch_deferred(ctx->cfg, ctx->sc, *gbuf, *cam, ctx->points, ctx->num_points, ctx->csm,
-                                       (uint2*)hdr_out, (cudaStream_t)stream), "deferred_pbr_csm");
+                                       (uint2*)hdr_out, (cudaStream_t)stream, ctx->block_dim(SGI_BLOCK_DIRECT)),
+             "deferred_pbr_csm");
     ctx->launches += 1;
     return SGI_OK;
 }
@@ -393,7 +335,8 @@ static sgi_status run_gather(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_cam
     go.guide = ctx->guide;
     go.raw = keep ? ctx->reservoir : nullptr;
     SGI_CUDA(ctx, sgi::launch_gather(cfg, ctx->sc, *cur, *cam, ctx->cv, ctx->ce, ctx->visible_index, ctx->lists,
-                                     ctx->cubes, params->time, go, s), "vpl_gather");
+                                     ctx->cubes, params->time, go, s, ctx->block_dim(SGI_BLOCK_GATHER)),
+             "vpl_gather");
     ctx->launches += 1;
     ctx->last_merged = go.merged;
     ctx->feat_hist = ctx->hist_cur;
@@ -413,7 +356,9 @@ static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer
     const uint2* in = ctx->last_merged;
     for (int pass = 1; pass < cfg.denoise_passes - 1; ++pass) {
         uint2* out = keep ? ctx->pass_bufs[pass] : ctx->ping[pass & 1];
-        SGI_CUDA(ctx, sgi::launch_atrous(cfg.width, cfg.height, pass, ctx->guide, in, out, s), "atrous");
+        SGI_CUDA(ctx, sgi::launch_atrous(cfg.width, cfg.height, pass, ctx->guide, in, out, s,
+                                         ctx->block_dim(SGI_BLOCK_ATROUS)),
+                 "atrous");
         ctx->launches += 1;
         in = out;
     }
@@ -432,7 +377,7 @@ static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer
     d.res_in = in;
     d.res_out = keep ? ctx->pass_bufs[cfg.denoise_passes - 1] : nullptr;
     if (hdr_ready) SGI_CUDA(ctx, cudaStreamWaitEvent(s, hdr_ready, 0), "join direct lighting");
-    SGI_CUDA(ctx, sgi::launch_denoise_final(d, s), "denoise_final");
+    SGI_CUDA(ctx, sgi::launch_denoise_final(d, s, ctx->block_dim(SGI_BLOCK_DENOISE_FINAL)), "denoise_final");
     ctx->launches += 1;
     ctx->hist_cur = 1 - ctx->hist_cur;
     ctx->have_history = true;
@@ -550,6 +495,24 @@ sgi_status sgi_read_debug(sgi_ctx* ctx, int32_t which, void* host_dst, size_t by
     if (!host_dst) return SGI_OK;
     SGI_CUDA(ctx, cudaDeviceSynchronize(), "synchronize before debug read");
     SGI_CUDA(ctx, cudaMemcpy(host_dst, src, bytes < size ? bytes : size, cudaMemcpyDeviceToHost), "debug read");
+    return SGI_OK;
+}
+
+sgi_status sgi_set_block_shape(sgi_ctx* ctx, int32_t pass, int32_t bx, int32_t by) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (pass < 0 || pass >= SGI_NUM_BLOCK_PASSES) return fail(ctx, SGI_ERR_ARG, "unknown pass");
+    const bool dflt = bx == 0 && by == 0;
+    if (!dflt && (bx < 1 || by < 1 || bx * by != 256 || bx % 8 != 0))
+        return fail(ctx, SGI_ERR_ARG, "block shape must be 256 threads with a width that is a multiple of 8");
+    ctx->block[pass][0] = bx;
+    ctx->block[pass][1] = by;
+    return SGI_OK;
+}
+
+sgi_status sgi_get_block_shape(const sgi_ctx* ctx, int32_t pass, int32_t* bx, int32_t* by) {
+    if (!ctx || !bx || !by || pass < 0 || pass >= SGI_NUM_BLOCK_PASSES) return SGI_ERR_ARG;
+    *bx = ctx->block[pass][0];
+    *by = ctx->block[pass][1];
     return SGI_OK;
 }
 

@@ -65,7 +65,7 @@ cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1,
 cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam,
                           const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index,
                           const int32_t* lists, const sgi_cube_atlas& cubes, float time, const GatherOut& out,
-                          cudaStream_t s);
+                          cudaStream_t s, dim3 block = dim3(0, 0, 0));
 // converged target: `batches` runs of the sample loop, sums in FP64 -> float4 (rgb, 1)
 cudaError_t launch_gi_target(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
                              const sgi_camera& cam, const sgi_vpl* cv, const sgi_atlas_entry* ce,
@@ -73,12 +73,15 @@ cudaError_t launch_gi_target(const sgi_config& cfg, const ShadeConfig& sc, const
                              float time, int batches, float4* out, cudaStream_t s);
 // a-trous pass `pass` (1 .. passes-2): 5x5 taps at stride 2^pass
 cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in,
-                          uint2* res_out, cudaStream_t s);
+                          uint2* res_out, cudaStream_t s, dim3 block = dim3(0, 0, 0));
 // last pass: a-trous filter + temporal reprojection + composite
-cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s);
+cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s, dim3 block = dim3(0, 0, 0));
 cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
                             const sgi_camera& cam, const sgi_point_light* points, int32_t num_points,
-                            const sgi_csm& csm, uint2* hdr_out, cudaStream_t s);
+                            const sgi_csm& csm, uint2* hdr_out, cudaStream_t s, dim3 block = dim3(0, 0, 0));
+// Thread-block shapes of the per-pixel passes: any shape of 256 threads gives the
+// same results (every pixel is computed by one thread, independently); a zero
+// shape selects the pass's default.
 
 // scene generation (sgi_scene.cu)
 cudaError_t launch_scene_gbuffer(const sgi_box* boxes, int32_t nb, const sgi_scene_camera& cam, int32_t W,

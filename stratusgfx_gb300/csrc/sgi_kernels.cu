@@ -656,15 +656,15 @@ __global__ void __launch_bounds__(256, 4) vpl_gather_kernel(GatherParams p) {
 cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam,
                           const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index,
                           const int32_t* lists, const sgi_cube_atlas& cubes, float time, const GatherOut& out,
-                          cudaStream_t s) {
+                          cudaStream_t s, dim3 block) {
     GatherParams p;
     p.W = cfg.width; p.H = cfg.height; p.ts = cfg.tile_size;
     p.tiles_x = (cfg.width + cfg.tile_size - 1) / cfg.tile_size;
     p.L = cfg.max_vpls_per_tile; p.tiled = cfg.gi_mode == SGI_GI_TILED; p.spp = cfg.samples_per_pixel;
     p.sc = sc; p.g = g; p.cam = cam; p.cv = cv; p.ce = ce; p.visible_index = visible_index; p.lists = lists;
     p.cubes = cubes; p.time = time; p.out = out;
-    dim3 block(16, 16);
-    dim3 grid((cfg.width + 15) / 16, (cfg.height + 15) / 16);
+    if (block.x == 0) block = dim3(16, 16);
+    dim3 grid((cfg.width + block.x - 1) / block.x, (cfg.height + block.y - 1) / block.y);
     vpl_gather_kernel<<<grid, block, 0, s>>>(p);
     return cudaGetLastError();
 }
@@ -760,9 +760,9 @@ __global__ void __launch_bounds__(256) atrous_kernel(int W, int H, int step, con
 }
 
 cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in,
-                          uint2* res_out, cudaStream_t s) {
-    dim3 block(32, 8);
-    dim3 grid((W + 31) / 32, (H + 7) / 8);
+                          uint2* res_out, cudaStream_t s, dim3 block) {
+    if (block.x == 0) block = dim3(32, 8);
+    dim3 grid((W + block.x - 1) / block.x, (H + block.y - 1) / block.y);
     atrous_kernel<<<grid, block, 0, s>>>(W, H, 1 << pass, guide, res_in, res_out);
     return cudaGetLastError();
 }
@@ -828,9 +828,9 @@ __global__ void __launch_bounds__(256) denoise_final_kernel(DenoiseLaunch d) {
     d.hist_out[i] = f2h(historyAccum);
 }
 
-cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s) {
-    dim3 block(32, 8);
-    dim3 grid((d.width + 31) / 32, (d.height + 7) / 8);
+cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s, dim3 block) {
+    if (block.x == 0) block = dim3(32, 8);
+    dim3 grid((d.width + block.x - 1) / block.x, (d.height + block.y - 1) / block.y);
     denoise_final_kernel<<<grid, block, 0, s>>>(d);
     return cudaGetLastError();
 }
@@ -898,12 +898,12 @@ __global__ void __launch_bounds__(256, 4) deferred_pbr_csm_kernel(DeferredParams
 
 cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
                             const sgi_camera& cam, const sgi_point_light* points, int32_t num_points,
-                            const sgi_csm& csm, uint2* hdr_out, cudaStream_t s) {
+                            const sgi_csm& csm, uint2* hdr_out, cudaStream_t s, dim3 block) {
     DeferredParams p;
     p.W = cfg.width; p.H = cfg.height; p.sc = sc; p.g = g; p.cam = cam; p.points = points;
     p.num_points = num_points; p.csm = csm; p.out = hdr_out;
-    dim3 block(32, 8);
-    dim3 grid((cfg.width + 31) / 32, (cfg.height + 7) / 8);
+    if (block.x == 0) block = dim3(32, 8);
+    dim3 grid((cfg.width + block.x - 1) / block.x, (cfg.height + block.y - 1) / block.y);
     deferred_pbr_csm_kernel<<<grid, block, 0, s>>>(p);
     return cudaGetLastError();
 }

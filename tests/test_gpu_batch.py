@@ -1,0 +1,137 @@
+"""Block shapes of the per-pixel passes and the multi-view CUDA graph batch.
+
+Every thread-block shape computes each pixel with the same arithmetic, so frames
+rendered with any shape must be bit-identical; a batch replay must produce the
+same frames, bit for bit, as rendering each view in turn through the C ABI the
+same number of times (the captured launches are the same kernels with the same
+arguments), and its host state must stay in step with the history it wrote.
+"""
+import ctypes as C
+
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from stratusgfx_gb300 import abi, stage  # noqa: E402
+from stratusgfx_gb300 import scene as S  # noqa: E402
+from stratusgfx_gb300.denoiser import KpcnDenoiser  # noqa: E402
+
+SHAPES = [(32, 8), (16, 16), (64, 4), (128, 2), (8, 32)]
+
+
+def view_scene(W, H, seed, K=4):
+    w = S.Workload(f"room12_{W}x{H}", W, H, 12, 48, 2, 512, 32, abi.SGI_CUBE_F16, K, 5, 2)
+    return w, stage.DeviceScene(S.workload_scene(w, seed), w)
+
+
+class View:
+    """One view: a context with lights and maps set, frame 1 of its scene."""
+
+    def __init__(self, w, ds):
+        self.w, self.ds = w, ds
+        self.st = stage.GiStage(stage.workload_config(w))
+        self.st.set_lights(ds.vpls, ds.entries, ds.points)
+        self.st.set_shadow_maps(ds.csms[1], ds.cubes)
+        self.out = torch.zeros((w.height, w.width, 4), dtype=torch.float16, device="cuda")
+        self.cur, self.prev = ds.gbuffers[1].struct(), ds.gbuffers[0].struct()
+        self.cam = ds.camera(1)
+        self.params = abi.FrameParams(1016.0, 60.0)
+
+    def frame(self, net=None):
+        lib = self.st.lib
+        if net is None:
+            st = lib.sgi_render_frame(self.st.ctx, C.byref(self.cur), C.byref(self.prev), C.byref(self.cam),
+                                      C.byref(self.params), C.c_void_p(self.out.data_ptr()), None)
+        else:
+            st = lib.sgi_render_frame_neural(self.st.ctx, net.h, C.byref(self.cur), C.byref(self.prev),
+                                             C.byref(self.cam), C.byref(self.params),
+                                             C.c_void_p(self.out.data_ptr()), None)
+        abi.check(st, self.st.ctx)
+
+    def struct(self):
+        return abi.View(self.st.ctx.value, C.addressof(self.cur), C.addressof(self.prev), C.addressof(self.cam),
+                        self.params, self.out.data_ptr())
+
+
+def test_block_shapes_are_bit_identical():
+    w, ds = view_scene(200, 120, 71)
+    ref = View(w, ds)
+    for _ in range(3):
+        ref.frame()
+    torch.cuda.synchronize()
+    lib = abi.load()
+    for bx, by in SHAPES:
+        v = View(w, ds)
+        for p in range(4):
+            assert lib.sgi_set_block_shape(v.st.ctx, p, bx, by) == abi.SGI_OK
+        for _ in range(3):
+            v.frame()
+        torch.cuda.synchronize()
+        assert torch.equal(v.out.view(torch.int16), ref.out.view(torch.int16)), (bx, by)
+        v.st.close()
+    gx, gy = C.c_int32(), C.c_int32()
+    assert lib.sgi_get_block_shape(ref.st.ctx, abi.SGI_BLOCK_GATHER, C.byref(gx), C.byref(gy)) == abi.SGI_OK
+    assert (gx.value, gy.value) == (0, 0)
+    for bad in ((16, 8), (12, 21), (256, 2), (4, 64)):
+        assert lib.sgi_set_block_shape(ref.st.ctx, 0, *bad) == abi.SGI_ERR_ARG
+    assert lib.sgi_set_block_shape(ref.st.ctx, 4, 32, 8) == abi.SGI_ERR_ARG
+
+
+def run_batch(net, tune):
+    lib = abi.load()
+    sizes = [(96, 64, 11), (160, 96, 12), (64, 64, 13)]
+    scenes = [view_scene(W, H, seed) for W, H, seed in sizes]
+    seq = [View(w, ds) for w, ds in scenes]
+    bat = [View(w, ds) for w, ds in scenes]
+    for v in seq + bat:
+        v.frame(net)            # history and scratch exist before the capture
+    arr = (abi.View * len(bat))(*[v.struct() for v in bat])
+    h = C.c_void_p()
+    st = lib.sgi_batch_create(arr, len(bat), net.h if net else None, tune, None, C.byref(h))
+    assert st == abi.SGI_OK, lib.sgi_batch_last_error(h)
+    assert lib.sgi_batch_kernel_count(h) >= 3 * (20 if net else 10)
+    tuned_frames = 5 * (tune + 1) if tune else 0
+    for v in seq:
+        for _ in range(tuned_frames):
+            v.frame(net)
+    for _ in range(3):
+        assert lib.sgi_batch_launch(h, None) == abi.SGI_OK
+    for v in seq:
+        for _ in range(3):
+            v.frame(net)
+    torch.cuda.synchronize()
+    for a, b in zip(seq, bat):
+        assert torch.equal(a.out.view(torch.int16), b.out.view(torch.int16)), a.w.name
+    # an odd number of replays: destroy puts the host state on the history the replays wrote
+    assert lib.sgi_batch_destroy(h) == abi.SGI_OK
+    for v in seq + bat:
+        v.frame(net)
+    torch.cuda.synchronize()
+    for a, b in zip(seq, bat):
+        assert torch.equal(a.out.view(torch.int16), b.out.view(torch.int16)), a.w.name
+    for v in seq + bat:
+        v.st.close()
+
+
+def test_batch_replay_matches_per_view_frames_plain():
+    run_batch(None, tune=1)
+
+
+def test_batch_replay_matches_per_view_frames_neural():
+    net = KpcnDenoiser(1, 96, 160, seed=5)
+    try:
+        run_batch(net, tune=0)
+    finally:
+        net.close()
+
+
+def test_batch_create_rejects_views_without_a_first_frame():
+    lib = abi.load()
+    w, ds = view_scene(64, 64, 21)
+    v = View(w, ds)
+    arr = (abi.View * 1)(v.struct())
+    h = C.c_void_p()
+    assert lib.sgi_batch_create(arr, 1, None, 0, None, C.byref(h)) == abi.SGI_ERR_STATE
+    assert lib.sgi_batch_create(arr, 0, None, 0, None, C.byref(h)) == abi.SGI_ERR_ARG
+    v.st.close()

@@ -235,8 +235,10 @@ def fit_cascades(cam_world: np.ndarray, light_dir: np.ndarray, fovy_deg: float, 
 
 def make_scene(seed: int, width: int, height: int, num_boxes: int, num_vpls: int, num_frames: int,
                vpl_radius: float = 8.0, num_points: int = 0, csm_resolution: int = 1024,
-               vpl_color_scale: float = 50.0, fovy_deg: float = 60.0) -> Scene:
-    """Seeded room + lights + camera path. cameras[0] seeds the history; frames 1..num_frames are rendered."""
+               vpl_color_scale: float = 50.0, fovy_deg: float = 60.0, camera_seed: int | None = None) -> Scene:
+    """Seeded room + lights + camera path. cameras[0] seeds the history; frames 1..num_frames are rendered.
+    The room and its lights depend on `seed` only; with camera_seed the camera path comes from its own
+    generator (another view of the same room)."""
     rng = np.random.default_rng(seed)
     boxes = make_boxes(rng, num_boxes)
     el = math.radians(rng.uniform(30.0, 75.0))
@@ -277,6 +279,8 @@ def make_scene(seed: int, width: int, height: int, num_boxes: int, num_vpls: int
         points[k, 8], points[k, 9] = 15.0, 15.0
 
     # camera path: eye near one wall, looking across the room and slightly down
+    if camera_seed is not None:
+        rng = np.random.default_rng(camera_seed)
     aspect = width / height
     proj = perspective(math.radians(fovy_deg), aspect, 0.1, 30.0)
     for _ in range(100):

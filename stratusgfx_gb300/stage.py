@@ -188,6 +188,37 @@ class DeviceScene:
         return camera_struct(self.scene, k)
 
 
+class ViewScene:
+    """Another viewport of a room whose lights and shadow atlas a DeviceScene already holds: the
+    view's own G-buffers (every camera of `scene`) and the CSM of its last frame, generated on the GPU;
+    the VPLs, point lights and cube atlas are the room's."""
+
+    def __init__(self, room: DeviceScene, scene: Scene, w: Workload, device="cuda", stream=None):
+        lib = abi.load()
+        self.scene, self.w, self.device = scene, w, device
+        s = _stream_ptr(stream)
+        H, W = w.height, w.width
+        self.boxes, self.vpls, self.entries, self.points = room.boxes, room.vpls, room.entries, room.points
+        self.cubes = room.cubes
+        nb = scene.boxes.shape[0]
+        nframes = len(scene.cameras)
+        self.gbuffers = []
+        for k in range(nframes):
+            g = GBufferTensors(H, W, device)
+            abi.check(lib.sgi_scene_gbuffer(C.c_void_p(_ptr(self.boxes)), nb, C.byref(scene_camera_struct(scene, k)),
+                                            W, H, C.byref(g.struct()), s))
+            self.gbuffers.append(g)
+        R = w.csm_resolution
+        k = nframes - 1
+        self.csm_depth = {k: torch.empty((4, R, R), dtype=torch.float32, device=device)}
+        cs = csm_struct(scene, k, _ptr(self.csm_depth[k]), R)
+        abi.check(lib.sgi_scene_csm(C.c_void_p(_ptr(self.boxes)), nb, C.byref(cs), C.byref(inv_cascade_array(scene, k)), s))
+        self.csms = {k: cs}
+
+    def camera(self, k: int) -> abi.Camera:
+        return camera_struct(self.scene, k)
+
+
 class GiStage:
     def __init__(self, cfg: abi.Config):
         self.lib = abi.load()

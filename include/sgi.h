@@ -184,6 +184,18 @@ typedef struct sgi_cube_atlas {
     int32_t format;                      /* SGI_CUBE_* */
 } sgi_cube_atlas;
 
+/* Diffuse colour cubes of the VPLs: the RGB each VPL's shadow pass renders
+ * (shadowVpl.fs:34 into an RGB8 attachment with nearest filtering,
+ * StratusRendererBackend.cpp:2397-2430), stored as RGBA8 texels (A unused) with
+ * the addressing of sgi_cube_atlas: [layer][face][row][col]. */
+typedef struct sgi_diffuse_atlas {
+    const void* atlas[SGI_MAX_ATLASES];  /* DEVICE pointers */
+    int32_t num_atlases;
+    int32_t layers_per_atlas;
+    int32_t face_size;
+    int32_t reserved;
+} sgi_diffuse_atlas;
+
 typedef struct sgi_frame_params {
     float time;               /* RNG seed z (uniform float time), milliseconds */
     float frames_per_second;  /* uniform framesPerSecond = 1 / deltaSeconds */
@@ -305,6 +317,17 @@ sgi_status sgi_get_pass_times(sgi_ctx* ctx, float* ms, int32_t n);
 
 /* Kernel launches the context issued since creation (all sgi_* calls). */
 int64_t sgi_launch_count(const sgi_ctx* ctx);
+
+/* VPL colouring (vpl_light_color.cs:41-75, dispatched after the visibility cull
+ * by PerformVirtualPointLightCullingStage1_, StratusRendererBackend.cpp:1703-1731).
+ * Once set (NULL turns it off; the atlas must stay valid while set), every
+ * sgi_cull_vpls also recolours the visible VPLs of the compacted list in place:
+ *   color             = (diffuse(-L).rgb * sun colour) * intensity * 50000, w = 1
+ *   specularPosition  = position.xyz - (1.1 * radius * depth(-L)) * L, w = 1
+ * with L the CSM's light direction and sun colour its light colour, both cubes
+ * read at the nearest texel in direction -L (the distance cube of
+ * sgi_set_shadow_maps as a normalised depth). */
+sgi_status sgi_set_vpl_coloring(sgi_ctx* ctx, const sgi_diffuse_atlas* diffuse);
 
 /* Thread-block shape of a per-pixel pass (no counterpart in StratusGFX, whose
  * fragment shaders have no block shape). Every shape computes the same pixels

@@ -57,6 +57,13 @@ sgi_status sgi_scene_cube_atlas(const sgi_box* boxes, int32_t num_boxes, const s
                                 const sgi_atlas_entry* entries, int32_t count,
                                 const sgi_cube_atlas* atlas, void* stream);
 
+/* Diffuse colour cubes for the same VPLs and texel directions: the RGB8 albedo of
+ * the first box the texel's ray hits (A = 255), 0 where it hits none (the colour
+ * attachment shadowVpl.fs writes). */
+sgi_status sgi_scene_diffuse_atlas(const sgi_box* boxes, int32_t num_boxes, const sgi_vpl* vpls,
+                                   const sgi_atlas_entry* entries, int32_t count, const sgi_diffuse_atlas* atlas,
+                                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

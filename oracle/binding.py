@@ -58,6 +58,9 @@ def load() -> C.CDLL:
                                             P, P, P]),
             "oracle_scene_csm": (None, [P, C.c_int, C.POINTER(abi.Csm), P, P]),
             "oracle_scene_cube_atlas": (None, [P, C.c_int, P, P, C.c_int, C.POINTER(abi.CubeAtlas)]),
+            "oracle_scene_diffuse_atlas": (None, [P, C.c_int, P, P, C.c_int, C.POINTER(abi.DiffuseAtlas)]),
+            "oracle_color_vpls": (None, [C.c_int, P, P, C.c_int, C.POINTER(abi.CubeAtlas), C.POINTER(abi.DiffuseAtlas),
+                                         C.POINTER(abi.Csm)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -118,6 +121,35 @@ def scene_cubes(boxes, vpls, entries, face, fmt, layers=320):
         e = np.ascontiguousarray(entries, dtype=np.int32)
         load().oracle_scene_cube_atlas(_p(boxes), boxes.shape[0], _p(v), _p(e), n, C.byref(at))
     return storage, at
+
+
+def scene_diffuse(boxes, vpls, entries, face, layers=320):
+    """Diffuse colour cubes (RGBA8 texels as uint32) of the CPU ray caster, and their sgi_diffuse_atlas."""
+    n = vpls.shape[0]
+    na = max(1, (n + layers - 1) // layers)
+    storage = np.zeros((na, layers, 6, face, face), np.uint32)
+    at = diffuse_struct(storage, layers)
+    if n:
+        v = np.ascontiguousarray(vpls, dtype=np.float32)
+        e = np.ascontiguousarray(entries, dtype=np.int32)
+        load().oracle_scene_diffuse_atlas(_p(boxes), boxes.shape[0], _p(v), _p(e), n, C.byref(at))
+    return storage, at
+
+
+def diffuse_struct(storage: np.ndarray, layers: int = 320) -> abi.DiffuseAtlas:
+    at = abi.DiffuseAtlas()
+    for a in range(storage.shape[0]):
+        at.atlas[a] = storage[a].ctypes.data
+    at.num_atlases, at.layers_per_atlas, at.face_size = storage.shape[0], layers, storage.shape[-1]
+    return at
+
+
+def color_vpls(prec, cvpls, centries, count, cubes: abi.CubeAtlas, diffuse: abi.DiffuseAtlas, csm: abi.Csm):
+    """vpl_light_color.cs on the compacted VPLs (a recoloured copy)."""
+    out = np.array(cvpls, dtype=np.float32, copy=True, order="C")
+    e = np.ascontiguousarray(centries, dtype=np.int32)
+    load().oracle_color_vpls(prec, _p(out), _p(e), count, C.byref(cubes), C.byref(diffuse), C.byref(csm))
+    return out
 
 
 def cube_struct(storage: np.ndarray, fmt: int, layers: int = 320) -> abi.CubeAtlas:

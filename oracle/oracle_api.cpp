@@ -81,6 +81,13 @@ int oracle_vis_cull(int prec, const sgi_vpl* vpls, int n, const sgi_csm* csm, in
                       : vis_cull<double>(vpls, n, *csm, cap, visible_index);
 }
 
+// Recolours cv[0..count) in place (FP32 or FP64 arithmetic, stored as float).
+void oracle_color_vpls(int prec, sgi_vpl* cv, const sgi_atlas_entry* ce, int count, const sgi_cube_atlas* cubes,
+                       const sgi_diffuse_atlas* diffuse, const sgi_csm* csm) {
+    if (prec == 32) color_vpls<float>(cv, ce, count, *cubes, *diffuse, *csm);
+    else color_vpls<double>(cv, ce, count, *cubes, *diffuse, *csm);
+}
+
 void oracle_tile_stage1(int prec, const sgi_config* cfg, const sgi_gbuffer* g, const sgi_camera* cam, void* out) {
     if (prec == 32) tile_stage1<float>(*cfg, *g, *cam, (float*)out);
     else tile_stage1<double>(*cfg, *g, *cam, (double*)out);
@@ -284,6 +291,39 @@ void oracle_scene_cube_atlas(const sgi_box* boxes, int nb, const sgi_vpl* vpls, 
                     if (atlas->format == SGI_CUBE_F32) ((float*)atlas->atlas[e.index])[off] = val;
                     else if (atlas->format == SGI_CUBE_F16) ((uint16_t*)atlas->atlas[e.index])[off] = f32_to_f16(val);
                     else ((uint16_t*)atlas->atlas[e.index])[off] = (uint16_t)(val * 65535.0f + 0.5f);
+                }
+            }
+        }
+    }
+}
+
+void oracle_scene_diffuse_atlas(const sgi_box* boxes, int nb, const sgi_vpl* vpls, const sgi_atlas_entry* entries,
+                                int count, const sgi_diffuse_atlas* atlas) {
+    const int n = atlas->face_size;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int v = 0; v < count; ++v) {
+        const sgi_vpl& vp = vpls[v];
+        sgi_atlas_entry e = entries[v];
+        for (int f = 0; f < 6; ++f) {
+            for (int j = 0; j < n; ++j) {
+                for (int i = 0; i < n; ++i) {
+                    float sc = ((float(i) + 0.5f) / float(n)) * 2.0f - 1.0f;
+                    float tc = ((float(j) + 0.5f) / float(n)) * 2.0f - 1.0f;
+                    float d[3];
+                    cube_dir(f, sc, tc, d);
+                    float best = INFINITY;
+                    int bi = -1;
+                    for (int k = 0; k < nb; ++k) {
+                        float tn, tf; int ax;
+                        if (!ray_box(vp.position, d, boxes[k], tn, ax, tf)) continue;
+                        if (tn > 0.0f && tn < best) { best = tn; bi = k; }
+                    }
+                    uint32_t t = 0;
+                    if (bi >= 0)
+                        t = enc_unorm8(boxes[bi].albedo[0]) | (enc_unorm8(boxes[bi].albedo[1]) << 8) |
+                            (enc_unorm8(boxes[bi].albedo[2]) << 16) | 0xff000000u;
+                    size_t off = (((size_t)e.layer * 6 + f) * n + j) * n + i;
+                    ((uint32_t*)atlas->atlas[e.index])[off] = t;
                 }
             }
         }

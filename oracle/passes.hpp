@@ -130,6 +130,52 @@ template <class T> inline T cube_fetch(const sgi_cube_atlas& at, sgi_atlas_entry
     }
 }
 
+// Nearest-texel offset of direction d in a cube stack of face size n (cube_fetch's selection).
+template <class T> inline size_t cube_texel(int layer, int n, V3<T> d) {
+    T ax = gabs(d.x), ay = gabs(d.y), az = gabs(d.z);
+    int face; T sc, tc, ma;
+    if (ax >= ay && ax >= az) {
+        ma = ax;
+        if (d.x >= T(0)) { face = 0; sc = -d.z; tc = -d.y; } else { face = 1; sc = d.z; tc = -d.y; }
+    } else if (ay >= az) {
+        ma = ay;
+        if (d.y >= T(0)) { face = 2; sc = d.x; tc = d.z; } else { face = 3; sc = d.x; tc = -d.z; }
+    } else {
+        ma = az;
+        if (d.z >= T(0)) { face = 4; sc = d.x; tc = -d.y; } else { face = 5; sc = -d.x; tc = -d.y; }
+    }
+    T s = T(0.5) * (sc / ma + T(1));
+    T t = T(0.5) * (tc / ma + T(1));
+    int i = nearest_index(s, n), j = nearest_index(t, n);
+    return (((size_t)layer * 6 + face) * n + j) * n + i;
+}
+
+// vpl_light_color.cs:41-75 over the compacted list: colour from the diffuse cube
+// and the sun, specular position from the distance cube, both in direction -L.
+template <class T> void color_vpls(sgi_vpl* cv, const sgi_atlas_entry* ce, int count, const sgi_cube_atlas& cubes,
+                                   const sgi_diffuse_atlas& diffuse, const sgi_csm& csm) {
+    const V3<T> L(T(csm.light_direction[0]), T(csm.light_direction[1]), T(csm.light_direction[2]));
+    const V3<T> sun(T(csm.light_color[0]), T(csm.light_color[1]), T(csm.light_color[2]));
+    const V3<T> dir(-L.x, -L.y, -L.z);
+    for (int k = 0; k < count; ++k) {
+        const sgi_atlas_entry e = ce[k];
+        sgi_vpl& v = cv[k];
+        V3<T> diff(T(0), T(0), T(0));
+        if (e.index >= 0 && e.index < diffuse.num_atlases && e.layer >= 0 && e.layer < diffuse.layers_per_atlas) {
+            const uint32_t t = ((const uint32_t*)diffuse.atlas[e.index])[cube_texel(e.layer, diffuse.face_size, dir)];
+            diff = V3<T>(T(t & 0xffu) / T(255), T((t >> 8) & 0xffu) / T(255), T((t >> 16) & 0xffu) / T(255));
+        }
+        const V3<T> color = diff * sun;
+        const T magnitude = T(v.radius) * cube_fetch(cubes, e, dir);
+        const T m = T(1.1f) * magnitude;
+        const V3<T> spec = V3<T>(T(v.position[0]), T(v.position[1]), T(v.position[2])) - L * m;
+        const V3<T> c = ((color / T(1)) * T(v.intensity)) * T(50000);
+        v.color[0] = float(c.x); v.color[1] = float(c.y); v.color[2] = float(c.z); v.color[3] = 1.0f;
+        v.specular_position[0] = float(spec.x); v.specular_position[1] = float(spec.y);
+        v.specular_position[2] = float(spec.z); v.specular_position[3] = 1.0f;
+    }
+}
+
 // calculateShadowValue1Sample, pbr.glsl:116-136 (1 = occluded)
 template <class T> inline T shadow_1sample(const sgi_cube_atlas& at, sgi_atlas_entry e, T farPlane, V3<T> fragPos,
                                            V3<T> lightPos, T lightNormalDot, T minBias) {

@@ -86,6 +86,11 @@ class CubeAtlas(C.Structure):
                 ("layers_per_atlas", C.c_int32), ("face_size", C.c_int32), ("format", C.c_int32)]
 
 
+class DiffuseAtlas(C.Structure):  # sgi_diffuse_atlas
+    _fields_ = [("atlas", C.c_void_p * 14), ("num_atlases", C.c_int32), ("layers_per_atlas", C.c_int32),
+                ("face_size", C.c_int32), ("reserved", C.c_int32)]
+
+
 class FrameParams(C.Structure):
     _fields_ = [("time", C.c_float), ("frames_per_second", C.c_float)]
 
@@ -171,6 +176,9 @@ EXPORTS = {
     "sgi_scene_cube_atlas": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                          C.POINTER(CubeAtlas), C.c_void_p]),
     "sgi_set_block_shape": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "sgi_set_vpl_coloring": (C.c_int32, [C.c_void_p, C.POINTER(DiffuseAtlas)]),
+    "sgi_scene_diffuse_atlas": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                            C.POINTER(DiffuseAtlas), C.c_void_p]),
     "sgi_get_block_shape": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "sgi_batch_create": (C.c_int32, [C.POINTER(View), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                      C.POINTER(C.c_void_p)]),

@@ -274,6 +274,11 @@ sgi_status sgi_cull_vpls(sgi_ctx* ctx, void* stream) {
         SGI_CUDA(ctx, sgi::launch_compact(ctx->vpls, ctx->entries, ctx->flags, ctx->num_vpls, ctx->cfg.max_visible,
                                           ctx->cv, ctx->ce, ctx->visible_index, s), "vpl_compact");
         ctx->launches += 2;
+        if (ctx->coloring) {
+            SGI_CUDA(ctx, sgi::launch_vpl_color(ctx->cv, ctx->ce, ctx->visible_index, ctx->cfg.max_visible,
+                                                ctx->cubes, ctx->diffuse, ctx->csm, s), "vpl_color");
+            ctx->launches += 1;
+        }
     }
     ctx->culled = true;
     return SGI_OK;
@@ -498,6 +503,23 @@ sgi_status sgi_read_debug(sgi_ctx* ctx, int32_t which, void* host_dst, size_t by
     return SGI_OK;
 }
 
+sgi_status sgi_set_vpl_coloring(sgi_ctx* ctx, const sgi_diffuse_atlas* diffuse) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (!diffuse) {
+        ctx->coloring = false;
+        return SGI_OK;
+    }
+    if (diffuse->num_atlases < 1 || diffuse->num_atlases > SGI_MAX_ATLASES || diffuse->layers_per_atlas < 1 ||
+        diffuse->face_size < 1)
+        return fail(ctx, SGI_ERR_ARG, "diffuse atlas: bad dimensions");
+    for (int a = 0; a < diffuse->num_atlases; ++a)
+        if (!diffuse->atlas[a] || ((uintptr_t)diffuse->atlas[a] & 3))
+            return fail(ctx, SGI_ERR_ARG, "diffuse atlas: NULL or misaligned layer pointer");
+    ctx->diffuse = *diffuse;
+    ctx->coloring = true;
+    return SGI_OK;
+}
+
 sgi_status sgi_set_block_shape(sgi_ctx* ctx, int32_t pass, int32_t bx, int32_t by) {
     if (!ctx) return SGI_ERR_ARG;
     if (pass < 0 || pass >= SGI_NUM_BLOCK_PASSES) return fail(ctx, SGI_ERR_ARG, "unknown pass");
@@ -643,6 +665,16 @@ sgi_status sgi_scene_csm(const sgi_box* boxes, int32_t num_boxes, const sgi_csm*
         !inv_cascade_proj_view)
         return SGI_ERR_ARG;
     cudaError_t e = sgi::launch_scene_csm(boxes, num_boxes, *csm, inv_cascade_proj_view, (cudaStream_t)stream);
+    return e == cudaSuccess ? SGI_OK : (e == cudaErrorInvalidValue ? SGI_ERR_CAP : SGI_ERR_CUDA);
+}
+
+sgi_status sgi_scene_diffuse_atlas(const sgi_box* boxes, int32_t num_boxes, const sgi_vpl* vpls,
+                                   const sgi_atlas_entry* entries, int32_t count, const sgi_diffuse_atlas* atlas,
+                                   void* stream) {
+    if (!boxes || num_boxes < 1 || !vpls || !entries || count < 0 || !atlas || atlas->face_size < 1)
+        return SGI_ERR_ARG;
+    if (count == 0) return SGI_OK;
+    cudaError_t e = sgi::launch_scene_diffuse(boxes, num_boxes, vpls, entries, count, *atlas, (cudaStream_t)stream);
     return e == cudaSuccess ? SGI_OK : (e == cudaErrorInvalidValue ? SGI_ERR_CAP : SGI_ERR_CUDA);
 }
 

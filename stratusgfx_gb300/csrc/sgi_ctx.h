@@ -70,6 +70,10 @@ struct sgi_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
 
+    // VPL colouring after the cull (sgi_set_vpl_coloring)
+    bool coloring = false;
+    sgi_diffuse_atlas diffuse = {};
+
     // thread-block shapes of the per-pixel passes (SGI_BLOCK_*; {0, 0} = default)
     int32_t block[SGI_NUM_BLOCK_PASSES][2] = {};
     dim3 block_dim(int pass) const {

@@ -55,6 +55,10 @@ struct DenoiseLaunch {
 cudaError_t launch_vis_flags(const sgi_vpl* vpls, int32_t n, const sgi_csm& csm, uint8_t* flags, cudaStream_t s);
 // Device address of the fixed flag array of sgi_cull_vpls_noalloc on the current device.
 cudaError_t noalloc_cull_flags(uint8_t** flags);
+// vpl_light_color.cs over the compacted list (recolours cv in place)
+cudaError_t launch_vpl_color(sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index, int32_t cap,
+                             const sgi_cube_atlas& cubes, const sgi_diffuse_atlas& diffuse, const sgi_csm& csm,
+                             cudaStream_t s);
 cudaError_t launch_compact(const sgi_vpl* vpls, const sgi_atlas_entry* entries, const uint8_t* flags, int32_t n,
                            int32_t cap, sgi_vpl* cv, sgi_atlas_entry* ce, int32_t* visible_index, cudaStream_t s);
 cudaError_t launch_tile_stage1(const sgi_config& cfg, const sgi_gbuffer& g, const sgi_camera& cam,
@@ -88,6 +92,9 @@ cudaError_t launch_scene_gbuffer(const sgi_box* boxes, int32_t nb, const sgi_sce
                                  int32_t H, const sgi_gbuffer& out, cudaStream_t s);
 cudaError_t launch_scene_csm(const sgi_box* boxes, int32_t nb, const sgi_csm& csm, const float (*inv)[16],
                              cudaStream_t s);
+cudaError_t launch_scene_diffuse(const sgi_box* boxes, int32_t nb, const sgi_vpl* vpls,
+                                 const sgi_atlas_entry* entries, int32_t count, const sgi_diffuse_atlas& atlas,
+                                 cudaStream_t s);
 cudaError_t launch_scene_cubes(const sgi_box* boxes, int32_t nb, const sgi_vpl* vpls, const sgi_atlas_entry* entries,
                                int32_t count, const sgi_cube_atlas& atlas, cudaStream_t s);
 

@@ -96,6 +96,26 @@ SGI_D float infinite_shadow(const sgi_csm& csm, V3 fragPos, V3 normal, bool useD
 }
 
 // ------------------------------------------------------------- cube maps --
+// Nearest texel of a cube face_size n in direction d: returns its offset within the layer stack.
+SGI_D size_t cube_texel(int layer, int n, V3 d) {
+    float ax = gabs(d.x), ay = gabs(d.y), az = gabs(d.z);
+    int face; float sc, tc, ma;
+    if (ax >= ay && ax >= az) {
+        ma = ax;
+        if (d.x >= 0.0f) { face = 0; sc = -d.z; tc = -d.y; } else { face = 1; sc = d.z; tc = -d.y; }
+    } else if (ay >= az) {
+        ma = ay;
+        if (d.y >= 0.0f) { face = 2; sc = d.x; tc = d.z; } else { face = 3; sc = d.x; tc = -d.z; }
+    } else {
+        ma = az;
+        if (d.z >= 0.0f) { face = 4; sc = d.x; tc = -d.y; } else { face = 5; sc = -d.x; tc = -d.y; }
+    }
+    float s = 0.5f * (sc / ma + 1.0f);
+    float t = 0.5f * (tc / ma + 1.0f);
+    int i = nearest_index(s, n), j = nearest_index(t, n);
+    return (((size_t)layer * 6 + face) * n + j) * n + i;
+}
+
 SGI_D float cube_fetch(const sgi_cube_atlas& at, sgi_atlas_entry e, V3 d) {
     if (e.index < 0 || e.index >= at.num_atlases || e.layer < 0 || e.layer >= at.layers_per_atlas) return 1.0f;
     float ax = gabs(d.x), ay = gabs(d.y), az = gabs(d.z);
@@ -130,6 +150,43 @@ SGI_D float shadow_1sample(const sgi_cube_atlas& at, sgi_atlas_entry e, float fa
     float depth = cube_fetch(at, e, fragDir);
     depth = depth * farPlane;
     return (currentDepth - bias) > depth ? 1.0f : 0.0f;
+}
+
+// ========================================================= VPL colouring --
+// vpl_light_color.cs:41-75 over the compacted list (count = visible_index[0]).
+__global__ void vpl_color_kernel(sgi_vpl* __restrict__ cv, const sgi_atlas_entry* __restrict__ ce,
+                                 const int32_t* __restrict__ visible_index, int cap, sgi_cube_atlas cubes,
+                                 sgi_diffuse_atlas diffuse, sgi_csm csm) {
+    const int n = min(visible_index[0], cap);
+    const V3 L = v3(csm.light_direction[0], csm.light_direction[1], csm.light_direction[2]);
+    const V3 sun = v3(csm.light_color[0], csm.light_color[1], csm.light_color[2]);
+    const V3 dir = v3(-L.x, -L.y, -L.z);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const sgi_atlas_entry e = ce[k];
+        sgi_vpl v = cv[k];
+        V3 diff = v3s(0.0f);
+        if (e.index >= 0 && e.index < diffuse.num_atlases && e.layer >= 0 && e.layer < diffuse.layers_per_atlas) {
+            const uint32_t t = __ldg((const uint32_t*)diffuse.atlas[e.index] + cube_texel(e.layer, diffuse.face_size, dir));
+            diff = v3(unorm8(t, 0), unorm8(t, 1), unorm8(t, 2));
+        }
+        const V3 color = diff * sun;
+        const float magnitude = v.radius * cube_fetch(cubes, e, dir);
+        const float m = 1.1f * magnitude;
+        const V3 spec = v3(v.position[0], v.position[1], v.position[2]) - L * m;
+        const V3 c = ((color / 1.0f) * v.intensity) * 50000.0f;
+        v.color[0] = c.x; v.color[1] = c.y; v.color[2] = c.z; v.color[3] = 1.0f;
+        v.specular_position[0] = spec.x; v.specular_position[1] = spec.y; v.specular_position[2] = spec.z;
+        v.specular_position[3] = 1.0f;
+        cv[k] = v;
+    }
+}
+
+cudaError_t launch_vpl_color(sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index, int32_t cap,
+                             const sgi_cube_atlas& cubes, const sgi_diffuse_atlas& diffuse, const sgi_csm& csm,
+                             cudaStream_t s) {
+    const int blocks = (cap + 255) / 256 < 152 ? (cap + 255) / 256 : 152;
+    vpl_color_kernel<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(cv, ce, visible_index, cap, cubes, diffuse, csm);
+    return cudaGetLastError();
 }
 
 // =========================================================== VPL vis cull --

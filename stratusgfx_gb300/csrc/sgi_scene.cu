@@ -194,6 +194,39 @@ __global__ void scene_cube_kernel(const sgi_box* __restrict__ boxes, int nb, con
     else ((uint16_t*)base)[off] = (uint16_t)(val * 65535.0f + 0.5f);
 }
 
+// Diffuse colour cubes: RGB8 albedo of the first box hit (A = 255), 0 on a miss.
+__global__ void scene_diffuse_kernel(const sgi_box* __restrict__ boxes, int nb, const sgi_vpl* __restrict__ vpls,
+                                     const sgi_atlas_entry* __restrict__ entries, sgi_diffuse_atlas at) {
+    __shared__ sgi_box sb[kMaxSceneBoxes];
+    load_boxes(sb, boxes, nb);
+    const int n = at.face_size;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int v = blockIdx.z / 6, f = blockIdx.z % 6;
+    if (i >= n || j >= n) return;
+    const sgi_vpl& vp = vpls[v];
+    const sgi_atlas_entry e = entries[v];
+    if (e.index < 0 || e.index >= at.num_atlases || e.layer < 0 || e.layer >= at.layers_per_atlas) return;
+    const float sc = ((float(i) + 0.5f) / float(n)) * 2.0f - 1.0f;
+    const float tc = ((float(j) + 0.5f) / float(n)) * 2.0f - 1.0f;
+    float d[3];
+    cube_dir(f, sc, tc, d);
+    float o[3] = {vp.position[0], vp.position[1], vp.position[2]};
+    float best = __int_as_float(0x7f800000);
+    int bi = -1;
+    for (int k = 0; k < nb; ++k) {
+        float tn; int ax;
+        if (!ray_box(o, d, sb[k], tn, ax)) continue;
+        if (tn > 0.0f && tn < best) { best = tn; bi = k; }
+    }
+    uint32_t t = 0;
+    if (bi >= 0)
+        t = enc_unorm8(sb[bi].albedo[0]) | (enc_unorm8(sb[bi].albedo[1]) << 8) | (enc_unorm8(sb[bi].albedo[2]) << 16) |
+            0xff000000u;
+    const size_t off = (((size_t)e.layer * 6 + f) * n + j) * n + i;
+    ((uint32_t*)const_cast<void*>(at.atlas[e.index]))[off] = t;
+}
+
 cudaError_t launch_scene_gbuffer(const sgi_box* boxes, int32_t nb, const sgi_scene_camera& cam, int32_t W,
                                  int32_t H, const sgi_gbuffer& out, cudaStream_t s) {
     if (nb > kMaxSceneBoxes) return cudaErrorInvalidValue;
@@ -228,6 +261,21 @@ cudaError_t launch_scene_cubes(const sgi_box* boxes, int32_t nb, const sgi_vpl* 
         const int c = count - first < 10000 ? count - first : 10000;
         dim3 block(16, 16), grid((n + 15) / 16, (n + 15) / 16, c * 6);
         scene_cube_kernel<<<grid, block, 0, s>>>(boxes, nb, vpls + first, entries + first, atlas);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_scene_diffuse(const sgi_box* boxes, int32_t nb, const sgi_vpl* vpls,
+                                 const sgi_atlas_entry* entries, int32_t count, const sgi_diffuse_atlas& atlas,
+                                 cudaStream_t s) {
+    if (nb > kMaxSceneBoxes || atlas.face_size < 1) return cudaErrorInvalidValue;
+    const int n = atlas.face_size;
+    for (int first = 0; first < count; first += 10000) {
+        const int c = count - first < 10000 ? count - first : 10000;
+        dim3 block(16, 16), grid((n + 15) / 16, (n + 15) / 16, c * 6);
+        scene_diffuse_kernel<<<grid, block, 0, s>>>(boxes, nb, vpls + first, entries + first, atlas);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

@@ -168,3 +168,33 @@ def test_vpl_brdf_matches_independent_evaluation(case):
         out = np.zeros(3)
         O.load().oracle_vpl_brdf(prec, inp.ctypes.data_as(C.c_void_p), C.byref(cfg), out.ctypes.data_as(C.c_void_p))
         assert np.allclose(out, ref, rtol=tol, atol=1e-12), (prec, out, ref)
+
+
+def test_vpl_coloring_known_answer():
+    """vpl_light_color.cs on one VPL 0.25 m above a floor box, sun straight overhead:
+    the diffuse cube in direction -L sees the floor's albedo and the distance cube
+    the floor, so color = albedo * sun * intensity * 50000 and the specular position
+    lies 1.1 * radius * depth below the VPL."""
+    box = np.zeros((1, 16), np.float32)
+    box[0, 0:3], box[0, 4:7] = (-5.0, -1.0, -5.0), (5.0, 0.0, 5.0)
+    box[0, 8:12] = (0.5, 0.25, 1.0, 1.0)                  # albedo rgba
+    vpl = np.zeros((1, 16), np.float32)
+    vpl[0, 0:4] = (0.3, 0.25, -0.2, 1.0)
+    vpl[0, 12], vpl[0, 13], vpl[0, 14] = 2.0, 4.0, 0.001  # radius, far plane, intensity
+    entries = np.zeros((1, 2), np.int32)
+    storage, cubes = O.scene_cubes(box, vpl, entries, 8, abi.SGI_CUBE_F32)
+    dstore, diffuse = O.scene_diffuse(box, vpl, entries, 8)
+    csm = abi.Csm()
+    csm.light_direction[0:4] = [0.0, 1.0, 0.0, 0.0]
+    csm.light_color[0:4] = [3.0, 2.0, 1.0, 1.0]
+    out = O.color_vpls(64, vpl, entries, 1, cubes, diffuse, csm)
+    alb = np.array([round(0.5 * 255) / 255, round(0.25 * 255) / 255, 1.0])
+    np.testing.assert_allclose(out[0, 4:7], alb * [3.0, 2.0, 1.0] * 0.001 * 50000, rtol=1e-6)
+    assert out[0, 7] == 1.0
+    # the nearest texel to straight down (face -y, texel (4, 4) of 8) looks along (1/8, -1, -1/8)
+    depth = 0.25 * math.sqrt(1.0 + 2.0 / 64.0) / 4.0        # distance along that ray / far plane
+    np.testing.assert_allclose(out[0, 8:11], [0.3, 0.25 - 1.1 * 2.0 * depth, -0.2], rtol=1e-5, atol=1e-6)
+    assert out[0, 11] == 1.0
+    # the texel straight down holds the floor's colour; straight up sees nothing (0)
+    assert dstore[0, 0, 3].max() == (128 | (64 << 8) | (255 << 16) | (255 << 24))
+    assert dstore[0, 0, 2].max() == 0

@@ -226,6 +226,18 @@ sgi_status sgi_set_lights(sgi_ctx* ctx,
                           const sgi_point_light* points, int32_t num_points,
                           void* stream);
 
+/* Shadow-casting point lights of sgi_direct_lighting (the shadowCasters loop of
+ * pbr.fs:116-131): each light within its radius adds calculatePointLighting2
+ * with a shadow factor from its distance cube (slot entries[i] of `atlas`):
+ * calculateShadowValue8Samples (pbr.glsl:81-113, 8 taps at +-0.3 offsets of the
+ * direction) when the view distance is below 150, calculateShadowValue1Sample
+ * (:116-136) below 750, none beyond. Records and entries are copied (device or
+ * host pointers) on `stream`; the atlas (caller-owned device memory, any
+ * SGI_CUBE_* format, nearest texel) must stay valid while set. n = 0 removes
+ * them. At most 256. */
+sgi_status sgi_set_shadow_point_lights(sgi_ctx* ctx, const sgi_point_light* lights, const sgi_atlas_entry* entries,
+                                       int32_t n, const sgi_cube_atlas* atlas, void* stream);
+
 /* Binds the directional light's CSM and the VPL cube atlases (caller-owned
  * device memory; pointers and matrices are copied into the context). */
 sgi_status sgi_set_shadow_maps(sgi_ctx* ctx, const sgi_csm* csm, const sgi_cube_atlas* cubes);

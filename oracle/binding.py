@@ -53,7 +53,7 @@ def load() -> C.CDLL:
             "oracle_denoise": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.GBuffer),
                                       P, P, P, P, C.c_int, C.POINTER(abi.FrameParams), P, P, P, P]),
             "oracle_deferred": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.Camera),
-                                       P, C.c_int, C.POINTER(abi.Csm), P]),
+                                       P, C.c_int, C.POINTER(abi.Csm), P, P, P, C.c_int, C.POINTER(abi.CubeAtlas)]),
             "oracle_scene_gbuffer": (None, [P, C.c_int, C.POINTER(abi.SceneCamera), C.c_int, C.c_int, P, P, P, P, P,
                                             P, P, P]),
             "oracle_scene_csm": (None, [P, C.c_int, C.POINTER(abi.Csm), P, P]),
@@ -219,11 +219,19 @@ def denoise(prec, cfg, cur: HostGBuffer, prev: HostGBuffer, reservoir, hdr_in, g
     return comb, gi, hist, passes
 
 
-def deferred(prec, cfg, g: HostGBuffer, cam, points, csm: abi.Csm):
+def deferred(prec, cfg, g: HostGBuffer, cam, points, csm: abi.Csm, casters=None, caster_entries=None,
+             caster_atlas: abi.CubeAtlas | None = None):
+    """pbr.fs: point lights, optional shadow-casting point lights (records, atlas slots, host cube atlas)
+    and the directional light with its CSM."""
     out = np.zeros((cfg.height, cfg.width, 4), _dt(prec))
     npts = 0 if points is None else points.shape[0]
     pts = None if points is None else np.ascontiguousarray(points, dtype=np.float32)
-    load().oracle_deferred(prec, C.byref(cfg), C.byref(g.struct()), C.byref(cam), _p(pts), npts, C.byref(csm), _p(out))
+    nc = 0 if casters is None else casters.shape[0]
+    cs = None if casters is None else np.ascontiguousarray(casters, dtype=np.float32)
+    ce = None if caster_entries is None else np.ascontiguousarray(caster_entries, dtype=np.int32)
+    at = C.byref(caster_atlas) if caster_atlas is not None else None
+    load().oracle_deferred(prec, C.byref(cfg), C.byref(g.struct()), C.byref(cam), _p(pts), npts, C.byref(csm), _p(out),
+                           _p(cs), _p(ce), nc, at)
     return out
 
 

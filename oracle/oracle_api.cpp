@@ -131,9 +131,12 @@ void oracle_denoise(int prec, const sgi_config* cfg, const sgi_gbuffer* cur, con
     }
 }
 
+// casters / caster_entries / caster_atlas: shadow-casting point lights (num_casters may be 0).
 void oracle_deferred(int prec, const sgi_config* cfg, const sgi_gbuffer* g, const sgi_camera* cam,
-                     const sgi_point_light* points, int num_points, const sgi_csm* csm, void* out) {
-    DeferredArgs a{cfg, g, cam, points, num_points, csm};
+                     const sgi_point_light* points, int num_points, const sgi_csm* csm, void* out,
+                     const sgi_point_light* casters, const sgi_atlas_entry* caster_entries, int num_casters,
+                     const sgi_cube_atlas* caster_atlas) {
+    DeferredArgs a{cfg, g, cam, points, num_points, csm, casters, caster_entries, num_casters, caster_atlas};
     if (prec == 32) deferred<float>(a, (float*)out);
     else deferred<double>(a, (double*)out);
 }

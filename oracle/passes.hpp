@@ -187,6 +187,24 @@ template <class T> inline T shadow_1sample(const sgi_cube_atlas& at, sgi_atlas_e
     return (currentDepth - bias) > depth ? T(1) : T(0);
 }
 
+// calculateShadowValue8Samples, pbr.glsl:81-113 (fraction occluded)
+template <class T> inline T shadow_8samples(const sgi_cube_atlas& at, sgi_atlas_entry e, T farPlane, V3<T> fragPos,
+                                            V3<T> lightPos, T lightNormalDot, T minBias) {
+    V3<T> fragDir = fragPos - lightPos;
+    T currentDepth = length(fragDir);
+    T bias = currentDepth * gmax(minBias, saturate(lightNormalDot) * T(0.03f));
+    T shadow = T(0);
+    const T offs[2] = {T(-0.3f), T(0.3f)};
+    for (int x = 0; x < 2; ++x)
+        for (int y = 0; y < 2; ++y)
+            for (int z = 0; z < 2; ++z) {
+                T depth = cube_fetch(at, e, fragDir + V3<T>(offs[x], offs[y], offs[z]));
+                depth = depth * farPlane;
+                if ((currentDepth - bias) > depth) shadow = shadow + T(1);
+            }
+    return shadow / T(8);
+}
+
 // ------------------------------------------------------------------ passes --
 inline int tiles_x(const sgi_config& c) { return (c.width + c.tile_size - 1) / c.tile_size; }
 inline int tiles_y(const sgi_config& c) { return (c.height + c.tile_size - 1) / c.tile_size; }
@@ -619,6 +637,11 @@ struct DeferredArgs {
     const sgi_point_light* points;
     int num_points;
     const sgi_csm* csm;
+    // shadow-casting point lights (pbr.fs:116-131)
+    const sgi_point_light* casters = nullptr;
+    const sgi_atlas_entry* caster_entries = nullptr;
+    int num_casters = 0;
+    const sgi_cube_atlas* caster_atlas = nullptr;
 };
 
 // pbr.fs:82-145 (non-shadow-casting point lights + INFINITE_LIGHTING_ENABLED).
@@ -655,6 +678,25 @@ template <class T> void deferred_pixel(const DeferredArgs& a, int x, int y, T* o
         if (distance < T(pl.radius)) {
             color = color + point_lighting2<T>(fragPos, baseColor, normal, viewDir, lp, lc, viewDist, roughness,
                                                metallic, ambient, T(0), V3<T>(reflR),
+                                               T(cfg.point_light_ambient_intensity), bp, fog);
+        }
+    }
+    for (int l = 0; l < a.num_casters; ++l) {
+        const sgi_point_light& pl = a.casters[l];
+        V3<T> lp(T(pl.position[0]), T(pl.position[1]), T(pl.position[2]));
+        V3<T> lc(T(pl.color[0]), T(pl.color[1]), T(pl.color[2]));
+        T distance = length(lp - fragPos);
+        if (distance < T(pl.radius)) {
+            T sf = T(0);
+            const sgi_atlas_entry e = a.caster_entries[l];
+            if (viewDist < T(150))
+                sf = shadow_8samples<T>(*a.caster_atlas, e, T(pl.far_plane), fragPos, lp, dot(lp - fragPos, normal),
+                                        T(0.03f));
+            else if (viewDist < T(750))
+                sf = shadow_1sample<T>(*a.caster_atlas, e, T(pl.far_plane), fragPos, lp, dot(lp - fragPos, normal),
+                                       T(0.03f));
+            color = color + point_lighting2<T>(fragPos, baseColor, normal, viewDir, lp, lc, viewDist, roughness,
+                                               metallic, ambient, sf, V3<T>(reflR),
                                                T(cfg.point_light_ambient_intensity), bp, fog);
         }
     }

@@ -177,6 +177,8 @@ EXPORTS = {
                                          C.POINTER(CubeAtlas), C.c_void_p]),
     "sgi_set_block_shape": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "sgi_set_vpl_coloring": (C.c_int32, [C.c_void_p, C.POINTER(DiffuseAtlas)]),
+    "sgi_set_shadow_point_lights": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(CubeAtlas),
+                                                C.c_void_p]),
     "sgi_scene_diffuse_atlas": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                             C.POINTER(DiffuseAtlas), C.c_void_p]),
     "sgi_get_block_shape": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),

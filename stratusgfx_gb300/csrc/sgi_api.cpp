@@ -95,7 +95,7 @@ sgi::ShadeConfig make_shade(const sgi_config& c) {
 }
 
 void free_all(sgi_ctx* c) {
-    void* ptrs[] = {c->vpls, c->entries, c->points, c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
+    void* ptrs[] = {c->vpls, c->entries, c->points, c->shadow_points, c->shadow_entries, c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
                     c->tile_keys, c->reservoir, c->ping[0], c->ping[1], c->merged, c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
                     c->hist_depth[0], c->hist_depth[1]};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -178,6 +178,8 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     chk(dalloc(&c->vpls, cfg->max_vpls));
     chk(dalloc(&c->entries, cfg->max_vpls));
     chk(dalloc(&c->points, SGI_MAX_POINT_LIGHTS));
+    chk(dalloc(&c->shadow_points, SGI_MAX_POINT_LIGHTS));
+    chk(dalloc(&c->shadow_entries, SGI_MAX_POINT_LIGHTS));
     chk(dalloc(&c->flags, cfg->max_vpls));
     chk(dalloc(&c->cv, cfg->max_visible));
     chk(dalloc(&c->ce, cfg->max_visible));
@@ -323,7 +325,8 @@ sgi_status sgi_direct_lighting(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_
     if (!ctx) return SGI_ERR_ARG;
     if (!gbuffer_ok(gbuf, true) || !cam || !hdr_out) return fail(ctx, SGI_ERR_ARG, "NULL G-buffer, camera or output");
     if (!ctx->lights_set || !ctx->maps_set) return fail(ctx, SGI_ERR_STATE, "set lights and shadow maps first");
-    SGI_CUDA(ctx, sgi::launch_deferred(ctx->cfg, ctx->sc, *gbuf, *cam, ctx->points, ctx->num_points, ctx->csm,
+    sgi::ShadowCasters casters{ctx->shadow_points, ctx->shadow_entries, ctx->num_shadow_points, ctx->shadow_atlas};
+    SGI_CUDA(ctx, sgi::launch_deferred(ctx->cfg, ctx->sc, *gbuf, *cam, ctx->points, ctx->num_points, casters, ctx->csm,
                                        (uint2*)hdr_out, (cudaStream_t)stream, ctx->block_dim(SGI_BLOCK_DIRECT)),
              "deferred_pbr_csm");
     ctx->launches += 1;
@@ -500,6 +503,29 @@ sgi_status sgi_read_debug(sgi_ctx* ctx, int32_t which, void* host_dst, size_t by
     if (!host_dst) return SGI_OK;
     SGI_CUDA(ctx, cudaDeviceSynchronize(), "synchronize before debug read");
     SGI_CUDA(ctx, cudaMemcpy(host_dst, src, bytes < size ? bytes : size, cudaMemcpyDeviceToHost), "debug read");
+    return SGI_OK;
+}
+
+sgi_status sgi_set_shadow_point_lights(sgi_ctx* ctx, const sgi_point_light* lights, const sgi_atlas_entry* entries,
+                                       int32_t n, const sgi_cube_atlas* atlas, void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (n < 0) return fail(ctx, SGI_ERR_ARG, "negative light count");
+    if (n > SGI_MAX_POINT_LIGHTS) return fail(ctx, SGI_ERR_CAP, "more than 256 shadow-casting point lights");
+    if (n == 0) {
+        ctx->num_shadow_points = 0;
+        return SGI_OK;
+    }
+    if (!lights || !entries || !atlas) return fail(ctx, SGI_ERR_ARG, "NULL lights, entries or atlas");
+    if (atlas->num_atlases < 1 || atlas->num_atlases > SGI_MAX_ATLASES || atlas->layers_per_atlas < 1 ||
+        atlas->face_size < 1 || atlas->format < SGI_CUBE_F32 || atlas->format > SGI_CUBE_UNORM16)
+        return fail(ctx, SGI_ERR_ARG, "shadow atlas: bad dimensions or format");
+    cudaStream_t s = (cudaStream_t)stream;
+    SGI_CUDA(ctx, cudaMemcpyAsync(ctx->shadow_points, lights, sizeof(sgi_point_light) * n, cudaMemcpyDefault, s),
+             "copy shadow-casting lights");
+    SGI_CUDA(ctx, cudaMemcpyAsync(ctx->shadow_entries, entries, sizeof(sgi_atlas_entry) * n, cudaMemcpyDefault, s),
+             "copy shadow atlas entries");
+    ctx->num_shadow_points = n;
+    ctx->shadow_atlas = *atlas;
     return SGI_OK;
 }
 

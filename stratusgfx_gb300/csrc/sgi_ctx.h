@@ -70,6 +70,12 @@ struct sgi_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
 
+    // shadow-casting point lights of the direct lighting (sgi_set_shadow_point_lights)
+    sgi_point_light* shadow_points = nullptr;
+    sgi_atlas_entry* shadow_entries = nullptr;
+    int32_t num_shadow_points = 0;
+    sgi_cube_atlas shadow_atlas = {};
+
     // VPL colouring after the cull (sgi_set_vpl_coloring)
     bool coloring = false;
     sgi_diffuse_atlas diffuse = {};

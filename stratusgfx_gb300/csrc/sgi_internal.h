@@ -80,9 +80,17 @@ cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guid
                           uint2* res_out, cudaStream_t s, dim3 block = dim3(0, 0, 0));
 // last pass: a-trous filter + temporal reprojection + composite
 cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s, dim3 block = dim3(0, 0, 0));
+// shadow-casting point lights of the deferred pass (pbr.fs:116-131)
+struct ShadowCasters {
+    const sgi_point_light* lights;
+    const sgi_atlas_entry* entries;
+    int32_t count;
+    sgi_cube_atlas atlas;
+};
 cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
                             const sgi_camera& cam, const sgi_point_light* points, int32_t num_points,
-                            const sgi_csm& csm, uint2* hdr_out, cudaStream_t s, dim3 block = dim3(0, 0, 0));
+                            const ShadowCasters& casters, const sgi_csm& csm, uint2* hdr_out, cudaStream_t s,
+                            dim3 block = dim3(0, 0, 0));
 // Thread-block shapes of the per-pixel passes: any shape of 256 threads gives the
 // same results (every pixel is computed by one thread, independently); a zero
 // shape selects the pass's default.

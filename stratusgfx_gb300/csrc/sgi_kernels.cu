@@ -152,6 +152,28 @@ SGI_D float shadow_1sample(const sgi_cube_atlas& at, sgi_atlas_entry e, float fa
     return (currentDepth - bias) > depth ? 1.0f : 0.0f;
 }
 
+// calculateShadowValue8Samples, pbr.glsl:81-113 (fraction occluded): eight taps at
+// the direction offset by (+-0.3, +-0.3, +-0.3), x outermost.
+SGI_D float shadow_8samples(const sgi_cube_atlas& at, sgi_atlas_entry e, float farPlane, V3 fragPos, V3 lightPos,
+                            float lightNormalDot, float minBias) {
+    V3 fragDir = fragPos - lightPos;
+    float currentDepth = length(fragDir);
+    float bias = currentDepth * gmax(minBias, saturate(lightNormalDot) * 0.03f);
+    float shadow = 0.0f;
+    const float offs[2] = {-0.3f, 0.3f};
+#pragma unroll
+    for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y)
+#pragma unroll
+            for (int z = 0; z < 2; ++z) {
+                float depth = cube_fetch(at, e, fragDir + v3(offs[x], offs[y], offs[z]));
+                depth = depth * farPlane;
+                if ((currentDepth - bias) > depth) shadow = shadow + 1.0f;
+            }
+    return shadow / 8.0f;
+}
+
 // ========================================================= VPL colouring --
 // vpl_light_color.cs:41-75 over the compacted list (count = visible_index[0]).
 __global__ void vpl_color_kernel(sgi_vpl* __restrict__ cv, const sgi_atlas_entry* __restrict__ ce,
@@ -900,6 +922,7 @@ struct DeferredParams {
     sgi_camera cam;
     const sgi_point_light* points;
     int num_points;
+    ShadowCasters casters;
     sgi_csm csm;
     uint2* out;
 };
@@ -943,6 +966,25 @@ __global__ void __launch_bounds__(256, 4) deferred_pbr_csm_kernel(DeferredParams
                                             quadratic_atten(lightDir), sp.point_ambient, sp);
         }
     }
+    // shadowCasters, pbr.fs:116-131
+    for (int l = 0; l < p.casters.count; ++l) {
+        const float4* rec = reinterpret_cast<const float4*>(p.casters.lights + l);
+        const float4 lp4 = __ldg(rec), lc4 = __ldg(rec + 1), m4 = __ldg(rec + 2);
+        const V3 lp = v3(lp4.x, lp4.y, lp4.z), lc = v3(lc4.x, lc4.y, lc4.z);
+        const float distance = length(lp - fragPos);
+        if (distance < m4.x) {
+            float shadowFactor = 0.0f;
+            const sgi_atlas_entry entry = p.casters.entries[l];
+            if (viewDist < 150.0f)
+                shadowFactor = shadow_8samples(p.casters.atlas, entry, m4.y, fragPos, lp, dot(lp - fragPos, normal), 0.03f);
+            else if (viewDist < 750.0f)
+                shadowFactor = shadow_1sample(p.casters.atlas, entry, m4.y, fragPos, lp, dot(lp - fragPos, normal), 0.03f);
+            const V3 lightDir = lp - fragPos;
+            color = color + lighting_burley(lc, lightDir, viewDir, normal, baseColor, viewDist, length(lc) / 12.0f,
+                                            roughness, metallic, ambient, 1.0f - shadowFactor, v3s(reflR),
+                                            quadratic_atten(lightDir), sp.point_ambient, sp);
+        }
+    }
     const V3 lightDir = v3(p.csm.light_direction[0], p.csm.light_direction[1], p.csm.light_direction[2]);
     const V3 lightColor = v3(p.csm.light_color[0], p.csm.light_color[1], p.csm.light_color[2]);
     const float shadowFactor = infinite_shadow(p.csm, fragPos, normal, true);
@@ -955,10 +997,11 @@ __global__ void __launch_bounds__(256, 4) deferred_pbr_csm_kernel(DeferredParams
 
 cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
                             const sgi_camera& cam, const sgi_point_light* points, int32_t num_points,
-                            const sgi_csm& csm, uint2* hdr_out, cudaStream_t s, dim3 block) {
+                            const ShadowCasters& casters, const sgi_csm& csm, uint2* hdr_out, cudaStream_t s,
+                            dim3 block) {
     DeferredParams p;
     p.W = cfg.width; p.H = cfg.height; p.sc = sc; p.g = g; p.cam = cam; p.points = points;
-    p.num_points = num_points; p.csm = csm; p.out = hdr_out;
+    p.num_points = num_points; p.casters = casters; p.csm = csm; p.out = hdr_out;
     if (block.x == 0) block = dim3(32, 8);
     dim3 grid((cfg.width + block.x - 1) / block.x, (cfg.height + block.y - 1) / block.y);
     deferred_pbr_csm_kernel<<<grid, block, 0, s>>>(p);

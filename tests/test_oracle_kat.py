@@ -198,3 +198,32 @@ def test_vpl_coloring_known_answer():
     # the texel straight down holds the floor's colour; straight up sees nothing (0)
     assert dstore[0, 0, 3].max() == (128 | (64 << 8) | (255 << 16) | (255 << 24))
     assert dstore[0, 0, 2].max() == 0
+
+
+def _kat_scene():
+    from stratusgfx_gb300 import scene as S
+    from stratusgfx_gb300 import stage
+    w = S.Workload("room12_48x32_kat", 48, 32, 12, 8, 2, 256, 8, abi.SGI_CUBE_F32, 4, 3, 1)
+    sc = S.workload_scene(w, 77)
+    hs = O.HostScene(sc, w)
+    return w, sc, hs, stage.workload_config(w)
+
+
+def test_shadow_caster_with_empty_cube_equals_plain_point_light():
+    """A shadow-casting point light whose distance cube is all 1.0 (nothing within its
+    far plane) gets shadow factor 0 from both the 8-sample and the 1-sample filter, so
+    pbr.fs adds exactly what the same light adds as a non-shadow caster."""
+    w, sc, hs, cfg = _kat_scene()
+    lights = sc.points.copy()
+    empty = np.ones((1, 320, 6, 8, 8), np.float32)
+    atlas = O.cube_struct(empty, abi.SGI_CUBE_F32)
+    entries = np.array([[0, k] for k in range(lights.shape[0])], np.int32)
+    ref = O.deferred(32, cfg, hs.gbuffers[1], hs.camera(1), lights, hs.csms[1])
+    got = O.deferred(32, cfg, hs.gbuffers[1], hs.camera(1), None, hs.csms[1], lights, entries, atlas)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    # a cube at depth 0 everywhere occludes every tap: the lights then add less
+    full = O.cube_struct(np.zeros((1, 320, 6, 8, 8), np.float32), abi.SGI_CUBE_F32)
+    dark = O.deferred(32, cfg, hs.gbuffers[1], hs.camera(1), None, hs.csms[1], lights, entries, full)
+    none = O.deferred(32, cfg, hs.gbuffers[1], hs.camera(1), None, hs.csms[1])
+    lit = ref[..., :3].sum()
+    assert none[..., :3].sum() <= dark[..., :3].sum() < lit

@@ -318,6 +318,7 @@ sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream);
 #define SGI_DEBUG_GI_HISTORY      6  /* RGB16F [W*H]: this frame's denoised GI (giColor) */
 #define SGI_DEBUG_HISTORY_DEPTH   7  /* R16F [W*H]: accumulated history length */
 #define SGI_DEBUG_DIRECT          8  /* RGB16F [W*H]: direct lighting of sgi_render_frame */
+#define SGI_DEBUG_TAA_HISTORY     9  /* RGBA16F [W*H]: the last TAA output of sgi_post_fx */
 #define SGI_DEBUG_PASS_BASE      16  /* + k: RGBA16F [W*H] reservoir output of denoise pass k */
 sgi_status sgi_read_debug(sgi_ctx* ctx, int32_t which, void* host_dst, size_t bytes, size_t* needed);
 
@@ -329,6 +330,20 @@ sgi_status sgi_get_pass_times(sgi_ctx* ctx, float* ms, int32_t n);
 
 /* Kernel launches the context issued since creation (all sgi_* calls). */
 int64_t sgi_launch_count(const sgi_ctx* ctx);
+
+/* Post-processing consumers of the HDR frame (no part of the GI stage in
+ * StratusGFX, which runs them later in the frame: PerformTaaPostFx_ and
+ * PerformGammaTonemapPostFx_, StratusRendererBackend.cpp:2323-2360):
+ *   taa != 0: taa.fs - the previous TAA output, bilinearly reprojected by the
+ *     G-buffer velocity, clamped in Reinhard space to the min/max of the pixel
+ *     and its 4 neighbours, blended 90 % with the current colour; the result
+ *     (RGBA16F, alpha 0.0625) becomes the context's TAA history (the first
+ *     frame after creation or sgi_reset_history uses the current colour);
+ *   then gammaTonemap.fs: ACES film curve (2.51, 0.03, 2.43, 0.59, 0.14),
+ *     gamma 1/2.2, written as RGBA8 (A = 255) to ldr_out [height][width].
+ * hdr_in: RGBA16F [height][width] (sgi_render_frame's output). */
+sgi_status sgi_post_fx(sgi_ctx* ctx, const void* hdr_in, const sgi_gbuffer* cur, int32_t taa, void* ldr_out,
+                       void* stream);
 
 /* VPL colouring (vpl_light_color.cs:41-75, dispatched after the visibility cull
  * by PerformVirtualPointLightCullingStage1_, StratusRendererBackend.cpp:1703-1731).

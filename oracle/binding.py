@@ -59,6 +59,7 @@ def load() -> C.CDLL:
             "oracle_scene_csm": (None, [P, C.c_int, C.POINTER(abi.Csm), P, P]),
             "oracle_scene_cube_atlas": (None, [P, C.c_int, P, P, C.c_int, C.POINTER(abi.CubeAtlas)]),
             "oracle_scene_diffuse_atlas": (None, [P, C.c_int, P, P, C.c_int, C.POINTER(abi.DiffuseAtlas)]),
+            "oracle_post_fx": (None, [C.c_int, C.c_int, C.c_int, P, P, P, P, P, C.c_int]),
             "oracle_color_vpls": (None, [C.c_int, P, P, C.c_int, C.POINTER(abi.CubeAtlas), C.POINTER(abi.DiffuseAtlas),
                                          C.POINTER(abi.Csm)]),
         }
@@ -150,6 +151,19 @@ def color_vpls(prec, cvpls, centries, count, cubes: abi.CubeAtlas, diffuse: abi.
     e = np.ascontiguousarray(centries, dtype=np.int32)
     load().oracle_color_vpls(prec, _p(out), _p(e), count, C.byref(cubes), C.byref(diffuse), C.byref(csm))
     return out
+
+
+def post_fx(prec, hdr, velocity, hist_in, taa=True):
+    """taa.fs + gammaTonemap.fs on an RGBA16F frame (float16 [H, W, 4]): (ldr uint32 [H, W], TAA output float32
+    [H, W, 4] holding binary16 values, or None)."""
+    H, W = hdr.shape[:2]
+    h = np.ascontiguousarray(hdr, dtype=np.float32)
+    hi = None if hist_in is None else np.ascontiguousarray(hist_in, dtype=np.float32)
+    ho = np.zeros((H, W, 4), np.float32)
+    ldr = np.zeros((H, W), np.uint32)
+    vel = np.ascontiguousarray(velocity, dtype=np.uint32)
+    load().oracle_post_fx(prec, W, H, _p(h), _p(vel), _p(hi), _p(ho), _p(ldr), 1 if taa else 0)
+    return ldr, (ho if taa else None)
 
 
 def cube_struct(storage: np.ndarray, fmt: int, layers: int = 320) -> abi.CubeAtlas:

@@ -88,6 +88,13 @@ void oracle_color_vpls(int prec, sgi_vpl* cv, const sgi_atlas_entry* ce, int cou
     else color_vpls<double>(cv, ce, count, *cubes, *diffuse, *csm);
 }
 
+// taa.fs + gammaTonemap.fs (sgi_post_fx); float buffers hold binary16 values.
+void oracle_post_fx(int prec, int W, int H, const float* hdr, const uint32_t* velocity, const float* hist_in,
+                    float* hist_out, uint32_t* ldr, int taa) {
+    if (prec == 32) post_fx<float>(W, H, hdr, velocity, hist_in, hist_out, ldr, taa);
+    else post_fx<double>(W, H, hdr, velocity, hist_in, hist_out, ldr, taa);
+}
+
 void oracle_tile_stage1(int prec, const sgi_config* cfg, const sgi_gbuffer* g, const sgi_camera* cam, void* out) {
     if (prec == 32) tile_stage1<float>(*cfg, *g, *cam, (float*)out);
     else tile_stage1<double>(*cfg, *g, *cam, (double*)out);

@@ -720,4 +720,64 @@ template <class T> void deferred(const DeferredArgs& a, T* out) {
         for (int x = 0; x < W; ++x) deferred_pixel<T>(a, x, y, out + ((size_t)y * W + x) * 4);
 }
 
+// ----------------------------------------------------------------- post FX --
+// taa.fs (aa_common.glsl Reinhard tonemap) + gammaTonemap.fs, as sgi_post_fx.
+// hdr, hist_in, hist_out: [P][4] holding binary16 values; hist_in NULL on the
+// first TAA frame; ldr: RGBA8.
+template <class T> inline V3<T> reinhard(V3<T> c) { return c / (c + V3<T>(T(1))); }
+template <class T> inline V3<T> inverse_reinhard(V3<T> c) { return c / (V3<T>(T(1)) - c); }
+template <class T> inline V3<T> vmin3(V3<T> a, V3<T> b) { return {gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z)}; }
+template <class T> inline V3<T> vmax3(V3<T> a, V3<T> b) { return {gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z)}; }
+template <class T> inline T aces_film(T x) {
+    return saturate((x * (T(2.51f) * x + T(0.03f))) / (x * (T(2.43f) * x + T(0.59f)) + T(0.14f)));
+}
+
+template <class T> void post_fx(int W, int H, const float* hdr, const uint32_t* velocity, const float* hist_in,
+                                float* hist_out, uint32_t* ldr, int taa) {
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            const size_t i = (size_t)y * W + x;
+            auto at = [&](int xx, int yy) {
+                xx = xx < 0 ? 0 : (xx >= W ? W - 1 : xx);
+                yy = yy < 0 ? 0 : (yy >= H ? H - 1 : yy);
+                const float* p = hdr + ((size_t)yy * W + xx) * 4;
+                return V3<T>(T(p[0]), T(p[1]), T(p[2]));
+            };
+            V3<T> outc = at(x, y);
+            if (taa) {
+                const uint32_t vel = velocity[i];
+                T u = (T(x) + T(0.5)) / T(W), v = (T(y) + T(0.5)) / T(H);
+                T pu = u - T(f16_to_f32(uint16_t(vel & 0xffffu))), pv = v - T(f16_to_f32(uint16_t(vel >> 16)));
+                V3<T> currentColor = at(x, y);
+                V3<T> prevColor = currentColor;
+                if (hist_in) {
+                    auto ch = [&](int c) {
+                        return [&, c](int ii, int jj) -> T { return T(hist_in[((size_t)jj * W + ii) * 4 + c]); };
+                    };
+                    prevColor = V3<T>(bilinear<T>(ch(0), W, H, pu, pv), bilinear<T>(ch(1), W, H, pu, pv),
+                                      bilinear<T>(ch(2), W, H, pu, pv));
+                }
+                prevColor = reinhard(prevColor);
+                V3<T> c1 = at(x, y + 1), c2 = at(x, y - 1), c3 = at(x + 1, y), c4 = at(x - 1, y);
+                V3<T> minColor = reinhard(vmin3(currentColor, vmin3(c1, vmin3(c2, vmin3(c3, c4)))));
+                V3<T> maxColor = reinhard(vmax3(currentColor, vmax3(c1, vmax3(c2, vmax3(c3, c4)))));
+                currentColor = reinhard(currentColor);
+                prevColor = vmin3(vmax3(prevColor, minColor), maxColor);
+                currentColor = inverse_reinhard(currentColor);
+                prevColor = inverse_reinhard(prevColor);
+                V3<T> m(mix(currentColor.x, prevColor.x, T(0.9f)), mix(currentColor.y, prevColor.y, T(0.9f)),
+                        mix(currentColor.z, prevColor.z, T(0.9f)));
+                float* ho = hist_out + i * 4;
+                ho[0] = Prec<T>::store16(m.x); ho[1] = Prec<T>::store16(m.y); ho[2] = Prec<T>::store16(m.z);
+                ho[3] = Prec<T>::store16(T(0.0625f));
+                outc = V3<T>(T(ho[0]), T(ho[1]), T(ho[2]));
+            }
+            const T inv_gamma = T(1.0f / 2.2f);
+            auto q = [&](T c) { return (uint32_t)(saturate(std::pow(aces_film(c), inv_gamma)) * T(255) + T(0.5)); };
+            ldr[i] = q(outc.x) | (q(outc.y) << 8) | (q(outc.z) << 16) | 0xff000000u;
+        }
+    }
+}
+
 }  // namespace oracle

@@ -37,6 +37,7 @@ SGI_DEBUG_RESERVOIR = 5
 SGI_DEBUG_GI_HISTORY = 6
 SGI_DEBUG_HISTORY_DEPTH = 7
 SGI_DEBUG_DIRECT = 8
+SGI_DEBUG_TAA_HISTORY = 9
 SGI_DEBUG_PASS_BASE = 16
 
 
@@ -177,6 +178,7 @@ EXPORTS = {
                                          C.POINTER(CubeAtlas), C.c_void_p]),
     "sgi_set_block_shape": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "sgi_set_vpl_coloring": (C.c_int32, [C.c_void_p, C.POINTER(DiffuseAtlas)]),
+    "sgi_post_fx": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(GBuffer), C.c_int32, C.c_void_p, C.c_void_p]),
     "sgi_set_shadow_point_lights": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(CubeAtlas),
                                                 C.c_void_p]),
     "sgi_scene_diffuse_atlas": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,

@@ -95,7 +95,8 @@ sgi::ShadeConfig make_shade(const sgi_config& c) {
 }
 
 void free_all(sgi_ctx* c) {
-    void* ptrs[] = {c->vpls, c->entries, c->points, c->shadow_points, c->shadow_entries, c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
+    void* ptrs[] = {c->vpls, c->entries, c->points, c->shadow_points, c->shadow_entries, c->taa_hist[0],
+                    c->taa_hist[1], c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
                     c->tile_keys, c->reservoir, c->ping[0], c->ping[1], c->merged, c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
                     c->hist_depth[0], c->hist_depth[1]};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -469,6 +470,30 @@ sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream) {
     }
     ctx->hist_cur = 0;
     ctx->have_history = false;
+    ctx->have_taa = false;
+    return SGI_OK;
+}
+
+sgi_status sgi_post_fx(sgi_ctx* ctx, const void* hdr_in, const sgi_gbuffer* cur, int32_t taa, void* ldr_out,
+                       void* stream) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (!hdr_in || !ldr_out || (taa && (!cur || !cur->velocity)))
+        return fail(ctx, SGI_ERR_ARG, "NULL frame, output or velocity");
+    const size_t P = pixels(ctx->cfg);
+    if (taa && !ctx->taa_hist[0]) {
+        SGI_CUDA(ctx, dalloc(&ctx->taa_hist[0], P), "alloc TAA history");
+        SGI_CUDA(ctx, dalloc(&ctx->taa_hist[1], P), "alloc TAA history");
+    }
+    const uint2* hin = taa && ctx->have_taa ? ctx->taa_hist[ctx->taa_cur] : nullptr;
+    uint2* hout = taa ? ctx->taa_hist[1 - ctx->taa_cur] : nullptr;
+    SGI_CUDA(ctx, sgi::launch_post_fx(ctx->cfg.width, ctx->cfg.height, (const uint2*)hdr_in,
+                                      taa ? cur->velocity : nullptr, hin, hout, (uint32_t*)ldr_out, taa ? 1 : 0,
+                                      (cudaStream_t)stream), "post_fx");
+    ctx->launches += 1;
+    if (taa) {
+        ctx->taa_cur = 1 - ctx->taa_cur;
+        ctx->have_taa = true;
+    }
     return SGI_OK;
 }
 
@@ -490,6 +515,9 @@ sgi_status sgi_read_debug(sgi_ctx* ctx, int32_t which, void* host_dst, size_t by
         case SGI_DEBUG_GI_HISTORY: src = ctx->gi_hist[ctx->hist_cur]; size = P * sizeof(uint2); break;
         case SGI_DEBUG_HISTORY_DEPTH: src = ctx->hist_depth[ctx->hist_cur]; size = P * sizeof(uint16_t); break;
         case SGI_DEBUG_DIRECT: src = ctx->direct; size = P * sizeof(uint2); break;
+        case SGI_DEBUG_TAA_HISTORY:
+            if (!ctx->have_taa) return fail(ctx, SGI_ERR_STATE, "no TAA frame yet");
+            src = ctx->taa_hist[ctx->taa_cur]; size = P * sizeof(uint2); break;
         default:
             if (which >= SGI_DEBUG_PASS_BASE && which < SGI_DEBUG_PASS_BASE + ctx->cfg.denoise_passes &&
                 ctx->pass_bufs[which - SGI_DEBUG_PASS_BASE]) {

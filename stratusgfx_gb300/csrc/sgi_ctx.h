@@ -76,6 +76,11 @@ struct sgi_ctx {
     int32_t num_shadow_points = 0;
     sgi_cube_atlas shadow_atlas = {};
 
+    // TAA history of sgi_post_fx (RGBA16F ping-pong, allocated on first use)
+    uint2* taa_hist[2] = {nullptr, nullptr};
+    int taa_cur = 0;
+    bool have_taa = false;
+
     // VPL colouring after the cull (sgi_set_vpl_coloring)
     bool coloring = false;
     sgi_diffuse_atlas diffuse = {};

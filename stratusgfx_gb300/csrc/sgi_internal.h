@@ -55,6 +55,9 @@ struct DenoiseLaunch {
 cudaError_t launch_vis_flags(const sgi_vpl* vpls, int32_t n, const sgi_csm& csm, uint8_t* flags, cudaStream_t s);
 // Device address of the fixed flag array of sgi_cull_vpls_noalloc on the current device.
 cudaError_t noalloc_cull_flags(uint8_t** flags);
+// taa.fs + gammaTonemap.fs: hist_in NULL on the first TAA frame; taa = 0 tonemaps hdr directly
+cudaError_t launch_post_fx(int32_t W, int32_t H, const uint2* hdr, const uint32_t* velocity, const uint2* hist_in,
+                           uint2* hist_out, uint32_t* ldr, int32_t taa, cudaStream_t s);
 // vpl_light_color.cs over the compacted list (recolours cv in place)
 cudaError_t launch_vpl_color(sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index, int32_t cap,
                              const sgi_cube_atlas& cubes, const sgi_diffuse_atlas& diffuse, const sgi_csm& csm,

@@ -174,6 +174,90 @@ SGI_D float shadow_8samples(const sgi_cube_atlas& at, sgi_atlas_entry e, float f
     return shadow / 8.0f;
 }
 
+// ============================================================== post FX --
+// taa.fs with aa_common.glsl's Reinhard tonemap, then gammaTonemap.fs (ACES film
+// curve and gamma 2.2): the consumers of the stage's HDR frame
+// (PerformTaaPostFx_ / PerformGammaTonemapPostFx_, StratusRendererBackend.cpp:2323-2360).
+struct PostFxParams {
+    int W, H;
+    const uint2* hdr;            // RGBA16F frame
+    const uint32_t* velocity;    // RG16F G-buffer velocity
+    const uint2* hist_in;        // previous TAA output (RGBA16F), NULL on the first frame
+    uint2* hist_out;             // this TAA output (RGBA16F)
+    uint32_t* ldr;               // RGBA8 gamma-corrected output
+    int taa;
+};
+
+SGI_D V3 h4rgb(uint2 t) {
+    return v3(h2f((uint16_t)(t.x & 0xffffu)), h2f((uint16_t)(t.x >> 16)), h2f((uint16_t)(t.y & 0xffffu)));
+}
+SGI_D V3 reinhard(V3 c) { return c / (c + v3s(1.0f)); }
+SGI_D V3 inverse_reinhard(V3 c) { return c / (v3s(1.0f) - c); }
+SGI_D V3 vmin3(V3 a, V3 b) { return v3(gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z)); }
+SGI_D V3 vmax3(V3 a, V3 b) { return v3(gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z)); }
+SGI_D float aces_film(float x) {
+    return saturate((x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f));
+}
+
+__global__ void __launch_bounds__(256) post_fx_kernel(PostFxParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= p.W || y >= p.H) return;
+    const int W = p.W, H = p.H;
+    const size_t i = (size_t)y * W + x;
+    auto at = [&](int xx, int yy) {
+        xx = xx < 0 ? 0 : (xx >= W ? W - 1 : xx);
+        yy = yy < 0 ? 0 : (yy >= H ? H - 1 : yy);
+        return h4rgb(__ldg(p.hdr + (size_t)yy * W + xx));
+    };
+    V3 outc = at(x, y);
+    if (p.taa) {
+        const uint32_t vel = __ldg(p.velocity + i);
+        const float u = (float(x) + 0.5f) / float(W), v = (float(y) + 0.5f) / float(H);
+        const float pu = u - h2f((uint16_t)(vel & 0xffffu)), pv = v - h2f((uint16_t)(vel >> 16));
+        V3 currentColor = at(x, y);
+        V3 prevColor = currentColor;
+        if (p.hist_in) {
+            const uint2* hp = p.hist_in;
+            auto ch = [&](int ii, int jj, int c) {
+                const uint2 t = __ldg(hp + (size_t)jj * W + ii);
+                const uint32_t w = c < 2 ? t.x : t.y;
+                return h2f((uint16_t)((c & 1) ? (w >> 16) : (w & 0xffffu)));
+            };
+            prevColor = v3(bilinear([&](int ii, int jj) { return ch(ii, jj, 0); }, W, H, pu, pv),
+                           bilinear([&](int ii, int jj) { return ch(ii, jj, 1); }, W, H, pu, pv),
+                           bilinear([&](int ii, int jj) { return ch(ii, jj, 2); }, W, H, pu, pv));
+        }
+        prevColor = reinhard(prevColor);
+        const V3 c1 = at(x, y + 1), c2 = at(x, y - 1), c3 = at(x + 1, y), c4 = at(x - 1, y);
+        const V3 minColor = reinhard(vmin3(currentColor, vmin3(c1, vmin3(c2, vmin3(c3, c4)))));
+        const V3 maxColor = reinhard(vmax3(currentColor, vmax3(c1, vmax3(c2, vmax3(c3, c4)))));
+        currentColor = reinhard(currentColor);
+        prevColor = vmin3(vmax3(prevColor, minColor), maxColor);
+        currentColor = inverse_reinhard(currentColor);
+        prevColor = inverse_reinhard(prevColor);
+        const V3 m = v3(mixf(currentColor.x, prevColor.x, 0.9f), mixf(currentColor.y, prevColor.y, 0.9f),
+                        mixf(currentColor.z, prevColor.z, 0.9f));
+        const uint2 h = pack_h4(m.x, m.y, m.z, 0.0625f);
+        p.hist_out[i] = h;
+        outc = h4rgb(h);   // the RGB16F TAA target is what the tonemap pass reads
+    }
+    const float inv_gamma = 1.0f / 2.2f;
+    const float r = powf(aces_film(outc.x), inv_gamma);
+    const float g = powf(aces_film(outc.y), inv_gamma);
+    const float b = powf(aces_film(outc.z), inv_gamma);
+    auto q = [](float c) { return (uint32_t)(saturate(c) * 255.0f + 0.5f); };
+    p.ldr[i] = q(r) | (q(g) << 8) | (q(b) << 16) | 0xff000000u;
+}
+
+cudaError_t launch_post_fx(int32_t W, int32_t H, const uint2* hdr, const uint32_t* velocity, const uint2* hist_in,
+                           uint2* hist_out, uint32_t* ldr, int32_t taa, cudaStream_t s) {
+    PostFxParams p{W, H, hdr, velocity, hist_in, hist_out, ldr, taa};
+    dim3 block(32, 8), grid((W + 31) / 32, (H + 7) / 8);
+    post_fx_kernel<<<grid, block, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
 // ========================================================= VPL colouring --
 // vpl_light_color.cs:41-75 over the compacted list (count = visible_index[0]).
 __global__ void vpl_color_kernel(sgi_vpl* __restrict__ cv, const sgi_atlas_entry* __restrict__ ce,

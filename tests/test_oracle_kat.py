@@ -227,3 +227,25 @@ def test_shadow_caster_with_empty_cube_equals_plain_point_light():
     none = O.deferred(32, cfg, hs.gbuffers[1], hs.camera(1), None, hs.csms[1])
     lit = ref[..., :3].sum()
     assert none[..., :3].sum() <= dark[..., :3].sum() < lit
+
+
+def test_post_fx_known_answers():
+    """gammaTonemap.fs: ACES film then gamma 1/2.2 to RGBA8 (0 -> 0, 1 -> 231, saturating
+    colours -> 255); taa.fs: a history far outside the current pixel's neighbourhood is
+    clamped to it, so on a flat image the TAA output is the image itself."""
+    H, W = 6, 8
+    vel = np.zeros((H, W), np.uint32)
+    for val, want in ((0.0, 0), (1.0, 231), (500.0, 255)):
+        hdr = np.full((H, W, 4), val, np.float16)
+        ldr, _ = O.post_fx(64, hdr, vel, None, taa=False)
+        assert (ldr & 0xff).max() == want and (ldr & 0xff).min() == want, (val, ldr & 0xff)
+        assert ((ldr >> 24) == 255).all()
+    aces1 = 2.54 / 3.16
+    assert round(aces1 ** (1 / 2.2) * 255) == 231
+    hdr = np.full((H, W, 4), 0.75, np.float16)
+    hist = np.full((H, W, 4), 40.0, np.float32)
+    ldr, taa = O.post_fx(64, hdr, vel, hist, taa=True)
+    np.testing.assert_allclose(taa[..., :3], 0.75, rtol=1e-3)
+    assert (taa[..., 3] == 0.0625).all()
+    ref, _ = O.post_fx(64, hdr, vel, None, taa=False)
+    assert np.array_equal(ldr, ref)

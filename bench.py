@@ -518,6 +518,8 @@ def uhd_comparison(args, flush):
     K = w.samples
     runs = [("plain", plain_render, f"K{K}", {}), ("neural_bf16", neural_render, f"K{K}", {}),
             ("neural_fp8", neural_render, f"K{K}", {})]
+    # the FP8 network at fewer samples, for the equal-PSNR point at 4K
+    runs += [("neural_fp8_low", neural_render, f"K{k}", dict(samples_per_pixel=k)) for k in (2, 1)]
     res = {}
     measure_runs(runs, res, net, ds, sc, w, targets, flush, max(6, args.steps // 4))
     net.close()
@@ -525,6 +527,17 @@ def uhd_comparison(args, flush):
            "cube": f"6x{w.cube_size}^2 fp16", "samples_per_pixel": K, "frames": len(sc.cameras) - 1}
     for name in ("plain", "neural_bf16", "neural_fp8"):
         out[name] = res[name][f"K{K}"]
+    for k, v in res["neural_fp8_low"].items():
+        out[f"neural_fp8_{k}"] = v
+    plain = out["plain"]
+    ok = [(v["ms_per_frame"], n) for n, v in out.items()
+          if n.startswith("neural") and isinstance(v, dict) and v["psnr_gi_db"] >= plain["psnr_gi_db"]]
+    if ok:
+        best = min(ok)
+        out["equal_psnr"] = {"plain_ms": plain["ms_per_frame"], "plain_gi_psnr_db": plain["psnr_gi_db"],
+                             "neural_config": best[1], "neural_ms": best[0],
+                             "neural_gain_gi_db": round(out[best[1]]["psnr_gi_db"] - plain["psnr_gi_db"], 2),
+                             "speedup_at_equal_or_better_psnr": round(plain["ms_per_frame"] / best[0], 3)}
     out["converged_target"] = {"samples_per_pixel": 512, "accumulation": "fp64", "ms_per_frame": round(target_ms, 2)}
     return {"uhd": out}
 
@@ -677,6 +690,55 @@ def batched_views(args, flush):
     return {"batched": res}
 
 
+# U-Net multiply-adds per pixel: 3x3 convolutions at full, half and quarter resolution
+UNET_MACS_PER_PIXEL = 9 * (16 * 32 + 32 * 32 + 96 * 32 + 32 * 32 + 32 * 32) + \
+    9 * (32 * 64 + 64 * 64 + 192 * 64 + 64 * 64) / 4 + 9 * (64 * 128 + 128 * 128) / 16
+
+
+def unet_roofline(net, H, W, flush, iters=10):
+    """The learned denoiser's forward pass (11 convolutions, upsampling, kernel apply) at H x W in BF16 and
+    FP8: ms (CUDA events, L2 flushed before each), achieved dense TFLOP/s (2 x multiply-adds of the 3x3
+    convolutions) and its fraction of the measured BF16 tensor peak (FP8: of twice that, the E4M3 rate)."""
+    import torch
+
+    from stratusgfx_gb300 import abi
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    bf16 = peaks.get("bf16_tflops") or 1900.0
+    src = "measured" if peaks.get("bf16_tflops") else "fallback"
+    g = torch.Generator(device="cpu").manual_seed(5)
+    feat = torch.randn((1, H, W, 16), generator=g).clamp(-3, 3).to("cuda", torch.bfloat16)
+    noisy = torch.rand((1, H, W, 4), generator=g).cuda()
+    prev = torch.rand((1, H, W, 4), generator=g).cuda()
+    out = torch.empty((1, H, W, 4), device="cuda")
+    flops = 2.0 * UNET_MACS_PER_PIXEL * H * W
+    res = {"flops_per_forward": flops, "peak_source": src}
+    for name, prec, peak in (("bf16", abi.SGI_NN_BF16, bf16), ("fp8", abi.SGI_NN_FP8, 2.0 * bf16)):
+        net.set_precision(prec)
+        for _ in range(3):
+            net.forward(feat, noisy, prev, out)
+        torch.cuda.synchronize()
+        ms = 0.0
+        for i in range(iters):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            net.forward(feat, noisy, prev, out)
+            e1.record()
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+        ms /= iters
+        tf = flops / (ms / 1e3) / 1e12
+        res[name] = {"ms": round(ms, 4), "tflops": round(tf, 1), "peak_tflops": round(peak, 1),
+                     "frac": round(tf / peak, 4)}
+    net.set_precision(abi.SGI_NN_BF16)
+    return res
+
+
 def neural_vs_plain(args, ds, sc, w, cfg, flush):
     """The metric's comparison: plain a-trous at K = 8..64 against the learned denoiser at K = 8, 4, 2;
     ms/frame (device-resident) and PSNR against the converged frame (equal_psnr below)."""
@@ -699,6 +761,7 @@ def neural_vs_plain(args, ds, sc, w, cfg, flush):
     runs += [("neural", neural_render, f"K{K}", dict(samples_per_pixel=K)) for K in (8, 4, 2, 1)]
     runs += [("neural_fp8", neural_render, f"K{K}", dict(samples_per_pixel=K)) for K in (8, 4, 2, 1)]
     measure_runs(runs, res, net, ds, sc, w, targets, flush, max(8, args.steps // 2))
+    res["unet"] = unet_roofline(net, H, W, flush)
     net.close()
     # Equal PSNR. The plain path's quality saturates with K (the a-trous filter's bias, not
     # the sample count, bounds its error against the converged frame), so the comparison is:

@@ -575,11 +575,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 // taps and input channels (at most 55 KB, [chunk][kx][ky][n][KC]) stay in shared
 // memory. FP8 with 96 input channels takes one 128-byte chunk per pixel (three
 // 32-channel K steps, the fourth slice of the row is zero fill and skipped).
-// ROWS_ = 16: one CTA per SM holds all 512 TMEM columns; ROWS_ = 8: two CTAs per
-// SM (256 columns and at most 110 KB of shared memory each), two independent
-// pipelines per SM for the price of 10 / 8 instead of 18 / 16 halo rows per strip.
-template <int CIN, bool F8 = false, int ROWS_ = 16> struct RsShape {
-    static constexpr int COUT = 32, NX = 96;
+// COUT_ = 32 or 64 output channels (row slots of COUT_ TMEM columns, N = 3 COUT_).
+// ROWS_ x COUT_ = 512: one CTA per SM holds all TMEM columns; = 256: two CTAs per
+// SM (at most 110 KB of shared memory each), two independent pipelines per SM for
+// the price of more halo rows per strip (10 / 8 instead of 18 / 16 for COUT_ = 32).
+template <int CIN, bool F8 = false, int ROWS_ = 16, int COUT_ = 32> struct RsShape {
+    static constexpr int COUT = COUT_, NX = 3 * COUT_;
     static constexpr int EB = F8 ? 1 : 2;                           // bytes per channel
     static constexpr int ROWB = (F8 && CIN == 96) ? 128 : CIN % (F8 ? 64 : 32) == 0 ? 64 : 32;
     static constexpr int KC = ROWB / EB;
@@ -595,16 +596,17 @@ template <int CIN, bool F8 = false, int ROWS_ = 16> struct RsShape {
     static constexpr int WCH = 9 * COUT * ROWB;                     // weights of one chunk
     static constexpr int WBYTES = NCH * WCH;
     static constexpr int ST_OFF = round_up(WBYTES, 1024);
-    static constexpr int CTAS = 16 / ROWS;                           // CTAs per SM
-    static constexpr int BUDGET = ROWS == 16 ? kSmemBudget : 110 * 1024;
-    static constexpr int STAGES = (BUDGET - ST_OFF) / STAGE < 16 ? (BUDGET - ST_OFF) / STAGE : 16;
     static constexpr int TMEM_COLS = ROWS * COUT;
+    static constexpr int CTAS = 512 / TMEM_COLS;                     // CTAs per SM
+    static constexpr int BUDGET = CTAS == 1 ? kSmemBudget : 110 * 1024;
+    static constexpr int STAGES = (BUDGET - ST_OFF) / STAGE < 16 ? (BUDGET - ST_OFF) / STAGE : 16;
     static constexpr int CTRL = 640;                                // barriers, TMEM address, abort flag
-    // with 16 rows at least 120 KB, so that one CTA (which holds all 512 TMEM columns) runs per SM
+    // one CTA per SM (all 512 TMEM columns): at least 120 KB, so that no second CTA waits for TMEM
     static constexpr size_t SMEM_USED = (size_t)ST_OFF + (size_t)STAGES * STAGE + 1024 + CTRL + 2 * COUT * 4;
-    static constexpr size_t SMEM = (ROWS == 8 || SMEM_USED > 120 * 1024) ? SMEM_USED : 120 * 1024;
-    static_assert(WCH % 1024 == 0 && (ROWS == 8 || STAGES >= 2 * NCH), "shape");
-    static_assert(ROWS * COUT == TMEM_COLS && ROWS % HPS == 0, "tmem");
+    static constexpr size_t SMEM = (CTAS == 2 || SMEM_USED > 120 * 1024) ? SMEM_USED : 120 * 1024;
+    static constexpr bool FITS = STAGES >= 2 * NCH && SMEM_USED <= (size_t)(CTAS == 1 ? 227 * 1024 : 113 * 1024);
+    static_assert(WCH % 1024 == 0, "shape");
+    static_assert((TMEM_COLS == 256 || TMEM_COLS == 512) && ROWS % HPS == 0, "tmem");
     static_assert((2 * STAGES + ROWS + 2) * 8 + 8 <= CTRL, "control block");
 };
 
@@ -694,17 +696,24 @@ __device__ __forceinline__ void epilogue16(const uint32_t* v, const float* sc, c
     }
 }
 
-// Two CTAs per SM where the 8-row shape fits (at least two halo-row pairs of stages).
-template <int CIN, bool F8> constexpr int rs_rows() {
-    return RsShape<CIN, F8, 8>::STAGES >= 2 * RsShape<CIN, F8, 8>::NCH ? 8 : 16;
+// Two CTAs per SM (256 TMEM columns each) where that shape fits (at least two
+// halo-row pairs of stages), else one; 0 when neither fits (the 9-tap kernel runs).
+template <int CIN, bool F8, int COUT> constexpr int rs_rows() {
+    return RsShape<CIN, F8, 256 / COUT, COUT>::FITS ? 256 / COUT : RsShape<CIN, F8, 512 / COUT, COUT>::FITS ? 512 / COUT : 0;
 }
 
-template <int CIN, int MODE, bool F8, bool OUT8, int ROWS_>
-__global__ void __launch_bounds__(kRsThreads, 16 / ROWS_)
+template <int CIN, bool F8, int COUT> constexpr int rs_rows_any() {
+    if constexpr (COUT == 32 || COUT == 64) return rs_rows<CIN, F8, COUT>();
+    else return 0;
+}
+
+template <int CIN, int MODE, bool F8, bool OUT8, int ROWS_, int COUT_>
+__global__ void __launch_bounds__(kRsThreads, 512 / (ROWS_ * COUT_))
     conv3x3_rs_kernel(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_w,
                       ConvArgs a, TcTiles tl, int* err) {
-    using S = RsShape<CIN, F8, ROWS_>;
-    constexpr int COUT = 32, NX = S::NX, NCH = S::NCH, KC = S::KC, ROWS = S::ROWS, NP = ROWS / 2;
+    using S = RsShape<CIN, F8, ROWS_, COUT_>;
+    constexpr int COUT = COUT_, NX = S::NX, NCH = S::NCH, KC = S::KC, ROWS = S::ROWS, NP = ROWS / 2;
+    constexpr int CPT = COUT / 2;             // output channels of each epilogue group
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem =
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -755,7 +764,7 @@ __global__ void __launch_bounds__(kRsThreads, 16 / ROWS_)
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
         if (lane == 0) {
-            // resident weights: one box {KC, 32 n, 3 ky, 3 kx} per chunk
+            // resident weights: one box {KC, COUT n, 3 ky, 3 kx} per chunk
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(s_addr(wbar)),
                          "r"((uint32_t)S::WBYTES)
                          : "memory");
@@ -821,9 +830,9 @@ __global__ void __launch_bounds__(kRsThreads, 16 / ROWS_)
                         if (i >= nh) break;
                         // taps of halo row i that land on rows 0 .. nrows - 1
                         const int ky_lo = max(0, i - nrows + 1), ky_hi = min(2, i);
-                        const uint32_t d = tmem + (uint32_t)(32 * (ROWS - 1 - i + ky_lo));
-                        const uint32_t idesc = IDESC0 | ((uint32_t)(4 * (ky_hi - ky_lo + 1)) << 17);
-                        const uint32_t b_ky = (uint32_t)((32 * ky_lo * S::ROWB) >> 4);
+                        const uint32_t d = tmem + (uint32_t)(COUT * (ROWS - 1 - i + ky_lo));
+                        const uint32_t idesc = IDESC0 | ((uint32_t)((COUT / 8) * (ky_hi - ky_lo + 1)) << 17);
+                        const uint32_t b_ky = (uint32_t)((COUT * ky_lo * S::ROWB) >> 4);
                         for (int ch = 0; ch < NCH; ++ch) {
                             const int sc = (s + ch) % S::STAGES;
                             const uint32_t a_lo =
@@ -867,12 +876,12 @@ __global__ void __launch_bounds__(kRsThreads, 16 / ROWS_)
         }
     } else {
         // ------------------------------------------------ epilogue (warps 2..9)
-        // Two groups of four warps (one per TMEM lane quarter) split the 32 output
-        // channels (16 each); every thread owns one pixel of a row and handles the
-        // rows in pairs (the 2x2 mean of a pooled output needs both).
+        // Two groups of four warps (one per TMEM lane quarter) split the COUT output
+        // channels (CPT each, in 16-channel pieces); every thread owns one pixel of a
+        // row and handles the rows in pairs (the 2x2 mean of a pooled output needs both).
         const int q = warp & 3;
         const int grp = (warp - 2) >> 2;
-        const int c0 = 16 * grp;                // first output channel of this group
+        const int c0 = CPT * grp;               // first output channel of this group
         constexpr int NVG = OUT8 ? 1 : 2;       // 16-byte output vectors per 16 channels
         const int et = tid - 64;
         for (int c = et; c < COUT; c += 256) {
@@ -889,7 +898,9 @@ __global__ void __launch_bounds__(kRsThreads, 16 / ROWS_)
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
         // every row slot starts at zero: the MMAs only accumulate
 #pragma unroll
-        for (int j = 0; j < ROWS; ++j) tmem_st16_zero(lane_base + (uint32_t)(32 * j));
+        for (int j = 0; j < ROWS; ++j)
+#pragma unroll
+            for (int u = 0; u < CPT / 16; ++u) tmem_st16_zero(lane_base + (uint32_t)(COUT * j + 16 * u));
         asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncwarp();
@@ -897,11 +908,11 @@ __global__ void __launch_bounds__(kRsThreads, 16 / ROWS_)
             for (int p = 0; p < NP; ++p)
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(s_addr(pairfree + p)) : "memory");
         asm volatile("bar.sync 1, 256;\n" ::: "memory");
-        float sc[16], bb[16];
+        float sc_r[16], bb_r[16];               // the piece's scales and biases (kept when CPT = 16)
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-            sc[j] = sc_s[c0 + j];
-            bb[j] = bb_s[c0 + j];
+            sc_r[j] = sc_s[c0 + j];
+            bb_r[j] = bb_s[c0 + j];
         }
         const bool pooling = a.pool.p != nullptr;
         uint32_t pf_ph = 0;   // bit p: parity of the next phase of pairfull[p]
@@ -925,49 +936,60 @@ __global__ void __launch_bounds__(kRsThreads, 16 / ROWS_)
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                 const bool two = 2 * p + 1 < nrows;
-                const uint32_t ta0 = lane_base + (uint32_t)(32 * (ROWS - 1 - 2 * p));   // row 2p
-                const uint32_t ta1 = ta0 - 32u;                                          // row 2p + 1
-                uint32_t v0[16], v1[16];
-                tmem_ld16(ta0, v0);
-                tmem_ld16(ta1, v1);
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                tmem_st16_zero(ta0);
-                tmem_st16_zero(ta1);
-                uint4 o0[NVG], o1[NVG], om[NVG];
-                if (pooling) {
-                    // the 2x2 mean of the activations in FP32 (H is even when pooling, so the pair is whole)
-                    float f0[16], f1[16];
-                    act16<MODE>(v0, sc, bb, f0);
-                    act16<MODE>(v1, sc, bb, f1);
-                    pack16<OUT8>(f0, o0);
-                    pack16<OUT8>(f1, o1);
+                const int y = yb + 2 * p;   // even: strips start on multiples of 4
+                bf16* yp0 = a.y.p + a.y.at(b, valid ? (size_t)y * a.W + px : 0, 0);
+                bf16* yp1 = a.y.p + a.y.at(b, valid && two ? (size_t)(y + 1) * a.W + px : 0, 0);
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        const float m = f0[j] + f1[j];
-                        f0[j] = (m + __shfl_down_sync(0xffffffffu, m, 1)) * 0.25f;
+                for (int u = 0; u < CPT / 16; ++u) {
+                    const int cb = c0 + 16 * u;   // first channel of this piece
+                    if (CPT > 16) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            sc_r[j] = sc_s[cb + j];
+                            bb_r[j] = bb_s[cb + j];
+                        }
                     }
-                    pack16<OUT8>(f0, om);
-                } else {
-                    epilogue16<MODE, OUT8>(v0, sc, bb, o0);
-                    epilogue16<MODE, OUT8>(v1, sc, bb, o1);
+                    const uint32_t ta0 = lane_base + (uint32_t)(COUT * (ROWS - 1 - 2 * p) + 16 * u);   // row 2p
+                    const uint32_t ta1 = ta0 - (uint32_t)COUT;                                         // row 2p + 1
+                    uint32_t v0[16], v1[16];
+                    tmem_ld16(ta0, v0);
+                    tmem_ld16(ta1, v1);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    tmem_st16_zero(ta0);
+                    tmem_st16_zero(ta1);
+                    uint4 o0[NVG], o1[NVG], om[NVG];
+                    if (pooling) {
+                        // the 2x2 mean of the activations in FP32 (H is even when pooling, so the pair is whole)
+                        float f0[16], f1[16];
+                        act16<MODE>(v0, sc_r, bb_r, f0);
+                        act16<MODE>(v1, sc_r, bb_r, f1);
+                        pack16<OUT8>(f0, o0);
+                        pack16<OUT8>(f1, o1);
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const float m = f0[j] + f1[j];
+                            f0[j] = (m + __shfl_down_sync(0xffffffffu, m, 1)) * 0.25f;
+                        }
+                        pack16<OUT8>(f0, om);
+                    } else {
+                        epilogue16<MODE, OUT8>(v0, sc_r, bb_r, o0);
+                        epilogue16<MODE, OUT8>(v1, sc_r, bb_r, o1);
+                    }
+#pragma unroll
+                    for (int g = 0; g < NVG; ++g) {
+                        const int k = cb / (OUT8 ? 16 : 8) + g;   // 16-byte vector of the pixel
+                        if (valid) *reinterpret_cast<uint4*>(yp0 + (size_t)k * (size_t)a.y.grp) = o0[g];
+                        if (valid && two) *reinterpret_cast<uint4*>(yp1 + (size_t)k * (size_t)a.y.grp) = o1[g];
+                        if (pooling && valid && (lane & 1) == 0)
+                            *reinterpret_cast<uint4*>(a.pool.p +
+                                                      a.pool.at(b, (size_t)(y / 2) * (a.W / 2) + px / 2, k)) = om[g];
+                    }
                 }
                 asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
                 __syncwarp();
                 if (lane == 0)
                     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(s_addr(pairfree + p)) : "memory");
-                const int y = yb + 2 * p;   // even: strips start on multiples of 8
-                bf16* yp0 = a.y.p + a.y.at(b, valid ? (size_t)y * a.W + px : 0, 0);
-                bf16* yp1 = a.y.p + a.y.at(b, valid && two ? (size_t)(y + 1) * a.W + px : 0, 0);
-#pragma unroll
-                for (int g = 0; g < NVG; ++g) {
-                    const int k = c0 / (OUT8 ? 16 : 8) + g;   // 16-byte vector of the pixel
-                    if (valid) *reinterpret_cast<uint4*>(yp0 + (size_t)k * (size_t)a.y.grp) = o0[g];
-                    if (valid && two) *reinterpret_cast<uint4*>(yp1 + (size_t)k * (size_t)a.y.grp) = o1[g];
-                    if (pooling && valid && (lane & 1) == 0)
-                        *reinterpret_cast<uint4*>(a.pool.p + a.pool.at(b, (size_t)(y / 2) * (a.W / 2) + px / 2, k)) =
-                            om[g];
-                }
             }
         }
     }
@@ -1043,10 +1065,11 @@ static cudaError_t run_tc(const ConvArgs& a, int* err, cudaStream_t s) {
     return launch_pdl(kern, dim3(grid), dim3(kThreads), S::SMEM, s, mx, mw, a, tl, err);
 }
 
-template <int CIN, int MODE, bool F8, bool OUT8>
+template <int CIN, int COUT, int MODE, bool F8, bool OUT8>
 static cudaError_t run_rs(const ConvArgs& a, int* err, cudaStream_t s) {
-    constexpr int ROWS_ = rs_rows<CIN, F8>();
-    using S = RsShape<CIN, F8, ROWS_>;
+    constexpr int ROWS_ = rs_rows<CIN, F8, COUT>();
+    static_assert(ROWS_ > 0, "row-streaming shape does not fit");
+    using S = RsShape<CIN, F8, ROWS_, COUT>;
     constexpr cuuint64_t EB = F8 ? 1 : 2;   // bytes per element
     const CUtensorMapDataType dt = F8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
     if (a.pool.p && (!view_ok(a.pool) || (a.H | a.W) & 1)) return cudaErrorInvalidValue;
@@ -1063,10 +1086,10 @@ static cudaError_t run_rs(const ConvArgs& a, int* err, cudaStream_t s) {
     if (encode(&mx, dt, 4, (void*)a.x.p, xdim, xstr, xbox, one, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    // weights [32][ky][kx][CIN] viewed as {CIN channels, 32 n, 3 ky, 3 kx}, box {KC, 32, 3, 3} -> [kx][ky][n][KC]
-    const cuuint64_t wdim[4] = {(cuuint64_t)CIN, 32, 3, 3};
+    // weights [COUT][ky][kx][CIN] viewed as {CIN channels, COUT n, 3 ky, 3 kx}, box {KC, COUT, 3, 3} -> [kx][ky][n][KC]
+    const cuuint64_t wdim[4] = {(cuuint64_t)CIN, (cuuint64_t)COUT, 3, 3};
     const cuuint64_t wstr[3] = {(cuuint64_t)9 * CIN * EB, (cuuint64_t)3 * CIN * EB, (cuuint64_t)CIN * EB};
-    const cuuint32_t wbox[4] = {(cuuint32_t)S::KC, 32, 3, 3};
+    const cuuint32_t wbox[4] = {(cuuint32_t)S::KC, (cuuint32_t)COUT, 3, 3};
     if (encode(&mw, dt, 4, (void*)a.w, wdim, wstr, wbox, one,
                CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
@@ -1079,20 +1102,21 @@ static cudaError_t run_rs(const ConvArgs& a, int* err, cudaStream_t s) {
     tl.total = (int)total;
     const int sms = sm_count();
     if (sms <= 0) return cudaErrorInvalidDevice;
-    auto kern = conv3x3_rs_kernel<CIN, MODE, F8, OUT8, ROWS_>;
+    auto kern = conv3x3_rs_kernel<CIN, MODE, F8, OUT8, ROWS_, COUT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
     if (e != cudaSuccess) return e;
     const int grid = tl.total < sms * S::CTAS ? tl.total : sms * S::CTAS;
     return launch_pdl(kern, dim3(grid), dim3(kRsThreads), S::SMEM, s, mx, mw, a, tl, err);
 }
 
-// 32-channel outputs take the row-streaming kernel, wider ones the 9-tap kernel.
+// 32- and 64-channel outputs take the row-streaming kernel where its resident
+// weights fit in shared memory, the others the 9-tap kernel.
 template <int CIN, int COUT, bool F8, bool OUT8>
 static cudaError_t run_shape(int mode, const ConvArgs& a, int* err, cudaStream_t s) {
-    if constexpr (COUT == 32) {
-        if (mode == 0) return run_rs<CIN, 0, F8, OUT8>(a, err, s);
-        if (mode == 1) return run_rs<CIN, 1, F8, OUT8>(a, err, s);
-        return run_rs<CIN, 2, F8, OUT8>(a, err, s);
+    if constexpr (rs_rows_any<CIN, F8, COUT>() > 0) {
+        if (mode == 0) return run_rs<CIN, COUT, 0, F8, OUT8>(a, err, s);
+        if (mode == 1) return run_rs<CIN, COUT, 1, F8, OUT8>(a, err, s);
+        return run_rs<CIN, COUT, 2, F8, OUT8>(a, err, s);
     } else {
         if (mode == 0) return run_tc<CIN, COUT, 0, F8, OUT8>(a, err, s);
         if (mode == 1) return run_tc<CIN, COUT, 1, F8, OUT8>(a, err, s);

@@ -145,9 +145,8 @@ def traffic_from_profiles(kernel: str):
 # --------------------------------------------------------- our arm ----
 def run_ours(args, rank, world, local_rank):
     import torch
-    import torch.distributed as dist
 
-    from stratusgfx_gb300 import abi, stage
+    from stratusgfx_gb300 import abi, replicas, stage
     from stratusgfx_gb300 import scene as S
 
     torch.cuda.set_device(local_rank)
@@ -173,8 +172,7 @@ def run_ours(args, rank, world, local_rank):
     for s in range(args.warmup):
         frame(s)
     torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     clocks = ClockSampler(local_rank)
@@ -198,13 +196,9 @@ def run_ours(args, rank, world, local_rank):
         pass_ms += np.array(st.pass_times())     # synchronises on the frame's last event
     st.set_timing(False)
     torch.cuda.synchronize()
-    total_ms = float(sum(ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = replicas.max_over_ranks(float(sum(ms)), device="cuda")
     ms_per_step = total_ms / args.steps
-    value = world * P * args.steps / (total_ms / 1e3) / 1e6
+    value = replicas.job_throughput(P * args.steps, world, total_ms) / 1e6
 
     # ---- e2e: host buffers through the public API (ABI), copies inside the timed region.
     # Three G-buffer slots and two output buffers: the host->device copy of frame s+1 and the
@@ -272,20 +266,15 @@ def run_ours(args, rank, world, local_rank):
     slots[2].copy_from(host_g[0])              # the frame before the first one
     e2e_run(0, args.warmup)
     torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(comp)
     e2e_run(args.warmup, args.steps, e0)
     e1.record(copy)                            # after the last device->host copy
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * P * args.steps / (e2e_ms / 1e3) / 1e6
+    e2e_ms = replicas.max_over_ranks(e0.elapsed_time(e1), device="cuda")
+    e2e_value = replicas.job_throughput(P * args.steps, world, e2e_ms) / 1e6
 
     # ---- roofline of the dominant pass
     peaks = {}

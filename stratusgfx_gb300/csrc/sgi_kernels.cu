@@ -29,6 +29,28 @@ SGI_D uint2 pack_h4(float a, float b, float c, float d) {
     return make_uint2((uint32_t)f2h(a) | ((uint32_t)f2h(b) << 16), (uint32_t)f2h(c) | ((uint32_t)f2h(d) << 16));
 }
 
+// The texels and weights of one bilinear sample: several channels sampled at
+// the same uv share them (each channel then evaluates exactly the sum that
+// bilinear() below forms).
+struct Bilinear {
+    size_t o00, o10, o01, o11;
+    float w00, w10, w01, w11;
+};
+SGI_D Bilinear bilinear_at(int W, int H, float s, float t) {
+    const float u = s * float(W) - 0.5f, v = t * float(H) - 0.5f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float a = u - fu, b = v - fv;
+    const int i0 = tex_index(fu, W), i1 = tex_index(fu + 1.0f, W);
+    const size_t r0 = (size_t)tex_index(fv, H) * W, r1 = (size_t)tex_index(fv + 1.0f, H) * W;
+    Bilinear q;
+    q.o00 = r0 + i0; q.o10 = r0 + i1; q.o01 = r1 + i0; q.o11 = r1 + i1;
+    q.w00 = (1.0f - a) * (1.0f - b); q.w10 = a * (1.0f - b); q.w01 = (1.0f - a) * b; q.w11 = a * b;
+    return q;
+}
+SGI_D float bilinear_sum(const Bilinear& q, float f00, float f10, float f01, float f11) {
+    return __fmaf_rn(f11, q.w11, __fmaf_rn(f01, q.w01, __fmaf_rn(f10, q.w10, f00 * q.w00)));
+}
+
 // Bilinear sample (LINEAR, CLAMP_TO_EDGE) at uv of a scalar image.
 template <class F> SGI_D float bilinear(F fetch, int W, int H, float s, float t) {
     float u = s * float(W) - 0.5f, v = t * float(H) - 0.5f;
@@ -877,36 +899,51 @@ cudaError_t launch_gi_target(const sgi_config& cfg, const ShadeConfig& sc, const
 // exp(-|z_c - z_q|) / sigmaZ, centre weight 1, taps at stride 2^pass, clamped
 // to the edge. Normals and depths come from the gather's guide (the same
 // decoded values the shader computes per tap).
+//
+// The 24 off-centre taps run in pairs on the packed FP32 pipe (expf_ieee2,
+// pow128x2, packed dot and accumulation): each lane performs the scalar
+// operations of its tap with the same roundings, and the taps still
+// accumulate one after another in the order dx = -2..2 (outer), dy = -2..2
+// (inner), so the sums are those of the one-tap-at-a-time loop bit for bit.
+// |z_c - z_q| is taken as |z_q - z_c|, which is the same value (the two
+// differences are exact negations of each other under round-to-nearest).
 SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __restrict__ guide,
                          const uint2* __restrict__ res_in, V3 cn, float cd, float& rf0, float& rf1, float& rf2,
                          float& rf3) {
-    rf0 = rf1 = rf2 = rf3 = 0.0f;
-    for (int dx = -2; dx <= 2; ++dx) {
-        int xx = x + dx * step;
-        xx = xx < 0 ? 0 : (xx > W - 1 ? W - 1 : xx);
+    int xs[5];
+    size_t rows[5];
 #pragma unroll
-        for (int dy = -2; dy <= 2; ++dy) {
-            int yy = y + dy * step;
-            yy = yy < 0 ? 0 : (yy > H - 1 ? H - 1 : yy);
-            const size_t j = (size_t)yy * W + xx;
-            float a, b, c, e;
-            unpack_h4(ld_u2(res_in, j), a, b, c, e);
-            float filtered;
-            if (dx == 0 && dy == 0) {
-                filtered = 1.0f;
-            } else {
-                const float4 gq = __ldg(guide + j);
-                const float wz = expf_ieee(-gabs(cd - gq.w)) / 1.0f;
-                float wn = gmax(0.0f, dot(cn, v3(gq.x, gq.y, gq.z)));
-                wn = pow128(wn);
-                filtered = wn * wz * 1.0f;
-            }
-            rf0 = __fmaf_rn(filtered, a, rf0);
-            rf1 = __fmaf_rn(filtered, b, rf1);
-            rf2 = __fmaf_rn(filtered, c, rf2);
-            rf3 = __fmaf_rn(filtered, e, rf3);
-        }
+    for (int d = 0; d < 5; ++d) {
+        const int xx = x + (d - 2) * step, yy = y + (d - 2) * step;
+        xs[d] = xx < 0 ? 0 : (xx > W - 1 ? W - 1 : xx);
+        rows[d] = (size_t)(yy < 0 ? 0 : (yy > H - 1 ? H - 1 : yy)) * W;
     }
+    float2 acc01 = make_float2(0.0f, 0.0f), acc23 = make_float2(0.0f, 0.0f);
+    auto accumulate = [&](float f, uint2 t) {
+        float a, b, c, e;
+        unpack_h4(t, a, b, c, e);
+        acc01 = __ffma2_rn(f2s(f), make_float2(a, b), acc01);
+        acc23 = __ffma2_rn(f2s(f), make_float2(c, e), acc23);
+    };
+    const float ncd = -cd;
+    const float2 cx = f2s(cn.x), cy = f2s(cn.y), cz = f2s(cn.z);
+#pragma unroll
+    for (int p = 0; p < 12; ++p) {   // taps t = 5 * (dx + 2) + (dy + 2); pairs (0,1) .. (10,11), (13,14) .. (23,24)
+        if (p == 6) accumulate(1.0f, ld_u2(res_in, rows[2] + xs[2]));   // the centre tap, weight 1
+        const int t = p < 6 ? 2 * p : 2 * p + 1;
+        const size_t j0 = rows[t % 5] + xs[t / 5], j1 = rows[(t + 1) % 5] + xs[(t + 1) / 5];
+        const float4 g0 = __ldg(guide + j0), g1 = __ldg(guide + j1);
+        const uint2 r0 = ld_u2(res_in, j0), r1 = ld_u2(res_in, j1);
+        const float2 dz = __fadd2_rn(make_float2(g0.w, g1.w), f2s(ncd));
+        const float2 wz = expf_ieee2(make_float2(dz.x < 0.0f ? dz.x : -dz.x, dz.y < 0.0f ? dz.y : -dz.y));
+        const float2 dn = __ffma2_rn(cz, make_float2(g0.z, g1.z),
+                                     __ffma2_rn(cy, make_float2(g0.y, g1.y), __fmul2_rn(cx, make_float2(g0.x, g1.x))));
+        const float2 wn = pow128x2(make_float2(gmax(0.0f, dn.x), gmax(0.0f, dn.y)));
+        const float2 f = __fmul2_rn(wn, wz);
+        accumulate(f.x, r0);
+        accumulate(f.y, r1);
+    }
+    rf0 = acc01.x; rf1 = acc01.y; rf2 = acc23.x; rf3 = acc23.y;
 }
 
 __global__ void __launch_bounds__(256) atrous_kernel(int W, int H, int step, const float4* __restrict__ guide,
@@ -959,22 +996,26 @@ __global__ void __launch_bounds__(256) denoise_final_kernel(DenoiseLaunch d) {
     float historyAccum = h2f(__ldg(d.hist_prev + i));
     float accumMultiplier = 1.0f;
     const V3 currGi = shadowFactor;
+    // previous depth, normal and GI bilinearly at the reprojected uv: one set of
+    // texels and weights, each texel read once
+    const Bilinear q = bilinear_at(W, H, pu, pv);
     const float* pd = d.prev_depth;
-    const uint32_t* pn = d.prev_normal;
-    const float prevCenterDepth = bilinear([&](int ii, int jj) { return __ldg(pd + (size_t)jj * W + ii); }, W, H, pu, pv);
-    const V3 pnv = v3(bilinear([&](int ii, int jj) { return unorm8(__ldg(pn + (size_t)jj * W + ii), 0); }, W, H, pu, pv),
-                      bilinear([&](int ii, int jj) { return unorm8(__ldg(pn + (size_t)jj * W + ii), 1); }, W, H, pu, pv),
-                      bilinear([&](int ii, int jj) { return unorm8(__ldg(pn + (size_t)jj * W + ii), 2); }, W, H, pu, pv));
+    const float prevCenterDepth = bilinear_sum(q, __ldg(pd + q.o00), __ldg(pd + q.o10), __ldg(pd + q.o01),
+                                               __ldg(pd + q.o11));
+    const uint32_t n00 = __ldg(d.prev_normal + q.o00), n10 = __ldg(d.prev_normal + q.o10),
+                   n01 = __ldg(d.prev_normal + q.o01), n11 = __ldg(d.prev_normal + q.o11);
+    V3 pnv;
+    pnv.x = bilinear_sum(q, unorm8(n00, 0), unorm8(n10, 0), unorm8(n01, 0), unorm8(n11, 0));
+    pnv.y = bilinear_sum(q, unorm8(n00, 1), unorm8(n10, 1), unorm8(n01, 1), unorm8(n11, 1));
+    pnv.z = bilinear_sum(q, unorm8(n00, 2), unorm8(n10, 2), unorm8(n01, 2), unorm8(n11, 2));
     const V3 prevCenterNormal = normalize(pnv * 2.0f - v3s(1.0f));
-    const uint2* gp = d.gi_prev;
-    auto gch = [&](int ii, int jj, int ch) {
-        float a, b, c, e;
-        unpack_h4(ld_u2(gp, (size_t)jj * W + ii), a, b, c, e);
-        return ch == 0 ? a : (ch == 1 ? b : c);
-    };
-    const V3 prevGi = v3(bilinear([&](int ii, int jj) { return gch(ii, jj, 0); }, W, H, pu, pv),
-                         bilinear([&](int ii, int jj) { return gch(ii, jj, 1); }, W, H, pu, pv),
-                         bilinear([&](int ii, int jj) { return gch(ii, jj, 2); }, W, H, pu, pv));
+    float g00[4], g10[4], g01[4], g11[4];
+    unpack_h4(ld_u2(d.gi_prev, q.o00), g00[0], g00[1], g00[2], g00[3]);
+    unpack_h4(ld_u2(d.gi_prev, q.o10), g10[0], g10[1], g10[2], g10[3]);
+    unpack_h4(ld_u2(d.gi_prev, q.o01), g01[0], g01[1], g01[2], g01[3]);
+    unpack_h4(ld_u2(d.gi_prev, q.o11), g11[0], g11[1], g11[2], g11[3]);
+    const V3 prevGi = v3(bilinear_sum(q, g00[0], g10[0], g01[0], g11[0]), bilinear_sum(q, g00[1], g10[1], g01[1], g11[1]),
+                         bilinear_sum(q, g00[2], g10[2], g01[2], g11[2]));
     const float currId = __ldg(d.cur.id + i);
     const float prevId = __ldg(d.prev_id + (size_t)nearest_index(pv, H) * W + nearest_index(pu, W));
     const float wn = gmax(0.0f, dot(centerNormal, prevCenterNormal));

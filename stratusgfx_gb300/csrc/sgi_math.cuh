@@ -67,6 +67,49 @@ SGI_D float pow128(float x) {
     float y = x * x; y = y * y; y = y * y; y = y * y; y = y * y; y = y * y; y = y * y; return y;
 }
 
+// Two lanes of the same functions on the packed FP32 pipe (sm_100+): every
+// __fmul2_rn / __fadd2_rn / __ffma2_rn component rounds exactly like the
+// scalar operation it stands for, so each lane returns the scalar result bit
+// for bit. x - a*b is written x + a*(-b) (round-to-nearest is symmetric, so
+// the product is the negated scalar product and the sum the scalar
+// difference); expf_ieee's early returns become selects at the end.
+SGI_D float2 f2s(float s) { return make_float2(s, s); }
+// expf_ieee's exact scaling by 2^k, split into a factor s (2^127, 2^-126 or 1)
+// and 2^k' with k' in the normal exponent range; k is updated to k'.
+SGI_D float exp_scale(int& k) {
+    const float s = k > 127 ? 1.7014118346046923e+38f : (k < -126 ? 1.1754943508222875e-38f : 1.0f);
+    k = k > 127 ? k - 127 : (k < -126 ? k + 126 : k);
+    return s;
+}
+SGI_D float exp_special(float x, float v) {
+    return x != x ? x : (x > 88.72283935546875f ? __int_as_float(0x7f800000) : (x < -103.97283935546875f ? 0.0f : v));
+}
+SGI_D float2 expf_ieee2(float2 x) {
+    const float2 t = __fadd2_rn(__fmul2_rn(x, f2s(1.44269502162933349609375f)), f2s(0.5f));
+    const float2 kf = make_float2(floorf(t.x), floorf(t.y));
+    const float2 r = __fadd2_rn(__fadd2_rn(x, __fmul2_rn(kf, f2s(-0.693145751953125f))),
+                                __fmul2_rn(kf, f2s(-1.428606765330187045037746429443359375e-06f)));
+    float2 p = __ffma2_rn(r, f2s(1.0f / 5040.0f), f2s(1.0f / 720.0f));
+    p = __ffma2_rn(p, r, f2s(1.0f / 120.0f));
+    p = __ffma2_rn(p, r, f2s(1.0f / 24.0f));
+    p = __ffma2_rn(p, r, f2s(1.0f / 6.0f));
+    p = __ffma2_rn(p, r, f2s(0.5f));
+    p = __ffma2_rn(p, r, f2s(1.0f));
+    p = __ffma2_rn(p, r, f2s(1.0f));
+    // __float2int_rz is defined for NaN and infinities (those lanes are selected away)
+    int k0 = __float2int_rz(kf.x), k1 = __float2int_rz(kf.y);
+    const float2 s = make_float2(exp_scale(k0), exp_scale(k1));   // p * 1 = p exactly
+    p = __fmul2_rn(__fmul2_rn(p, s), make_float2(__uint_as_float((uint32_t)(k0 + 127) << 23),
+                                                 __uint_as_float((uint32_t)(k1 + 127) << 23)));
+    return make_float2(exp_special(x.x, p.x), exp_special(x.y, p.y));
+}
+SGI_D float2 pow128x2(float2 x) {
+    float2 y = __fmul2_rn(x, x);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) y = __fmul2_rn(y, y);
+    return y;
+}
+
 // ---------------------------------------------------------------- vectors --
 struct V3 { float x, y, z; };
 SGI_D V3 v3(float x, float y, float z) { return V3{x, y, z}; }
@@ -122,7 +165,16 @@ SGI_D float random3(float sx, float sy, float sz) {
     return __uint_as_float((h & 0x007FFFFFu) | 0x3F800000u) - 1.0f;
 }
 
-SGI_D float unorm8(uint32_t t, int ch) { return float((t >> (8 * ch)) & 0xffu) / 255.0f; }
+// b / 255 for a UNORM8 byte b: the product with the rounded reciprocal plus one
+// fused correction step returns the correctly rounded quotient for every one
+// of the 256 bytes (checked exhaustively in exact rational arithmetic), so it
+// equals the IEEE division without the division's instruction sequence.
+SGI_D float unorm8(uint32_t t, int ch) {
+    const float b = float((t >> (8 * ch)) & 0xffu);
+    const float r = 1.0f / 255.0f;
+    const float q = b * r;
+    return __fmaf_rn(__fmaf_rn(-q, 255.0f, b), r, q);
+}
 SGI_D V3 decode_normal(uint32_t t) {   // normalize(rgb * 2 - 1), common.glsl:216-220
     V3 c = v3(unorm8(t, 0), unorm8(t, 1), unorm8(t, 2));
     return normalize(c * 2.0f - v3s(1.0f));

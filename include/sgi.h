@@ -331,6 +331,19 @@ sgi_status sgi_get_pass_times(sgi_ctx* ctx, float* ms, int32_t n);
 /* Kernel launches the context issued since creation (all sgi_* calls). */
 int64_t sgi_launch_count(const sgi_ctx* ctx);
 
+/* Self-check of the packed FP32 arithmetic (no StratusGFX counterpart). The
+ * a-trous passes evaluate two filter taps per instruction on the packed FP32
+ * pipe; each lane must equal the scalar arithmetic bit for bit. Runs n
+ * threads, each evaluating SGI_LANE_CHECKS checks both ways on hashed
+ * operands: 0-2 packed add, multiply, multiply-add; 3-5 the same on exact
+ * rounding ties; 6 exp over its whole range; 7 x^128; 8 a pair of a-trous tap
+ * weights; 9 their accumulation into the channel sums. counts[k] = threads
+ * whose check k differed; `first` (optional, SGI_LANE_CHECKS * 16 floats)
+ * receives for each failing check the packed results, the scalar results and
+ * the operands of one failing thread. Synchronous; uses the current device. */
+#define SGI_LANE_CHECKS 12
+sgi_status sgi_lane_selftest(int32_t n, uint32_t* counts, float* first);
+
 /* Post-processing consumers of the HDR frame (no part of the GI stage in
  * StratusGFX, which runs them later in the frame: PerformTaaPostFx_ and
  * PerformGammaTonemapPostFx_, StratusRendererBackend.cpp:2323-2360):

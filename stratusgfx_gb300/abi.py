@@ -27,6 +27,7 @@ SGI_MAX_ATLASES = 14
 SGI_MAX_VPLS_BEFORE_CULL = 10000
 SGI_MAX_VPLS_PER_FRAME = 4480
 SGI_NUM_PASS_TIMES = 5
+SGI_LANE_CHECKS = 12
 
 SGI_DEBUG_VISIBLE_INDEX = 0
 SGI_DEBUG_COMPACT_VPLS = 1
@@ -147,6 +148,7 @@ EXPORTS = {
     "sgi_set_timing": (C.c_int32, [C.c_void_p, C.c_int32]),
     "sgi_get_pass_times": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "sgi_launch_count": (C.c_int64, [C.c_void_p]),
+    "sgi_lane_selftest": (C.c_int32, [C.c_int32, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
     "sgi_nn_create": (C.c_int32, [C.POINTER(NnConfig), C.POINTER(C.c_void_p)]),
     "sgi_nn_destroy": (C.c_int32, [C.c_void_p]),
     "sgi_nn_last_error": (C.c_char_p, [C.c_void_p]),

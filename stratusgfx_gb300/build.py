@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # results are bit-reproducible against the CPU restatement of the shaders.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-Xcompiler", "-fPIC", "-I" + os.path.join(REPO, "include")]
-CUDA_SOURCES = ["sgi_kernels.cu", "sgi_scene.cu", "sgi_nn.cu", "sgi_nn_tc.cu"]
+CUDA_SOURCES = ["sgi_kernels.cu", "sgi_scene.cu", "sgi_nn.cu", "sgi_nn_tc.cu", "sgi_selftest.cu"]
 HOST_SOURCES = ["sgi_api.cpp", "sgi_nn_api.cpp", "sgi_batch.cpp"]
 # The learned denoiser is checked against the oracle within a tolerance, not bit
 # for bit, so its kernels keep the compiler's default multiply-add contraction.

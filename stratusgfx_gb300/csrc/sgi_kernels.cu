@@ -900,13 +900,12 @@ cudaError_t launch_gi_target(const sgi_config& cfg, const ShadeConfig& sc, const
 // to the edge. Normals and depths come from the gather's guide (the same
 // decoded values the shader computes per tap).
 //
-// The 24 off-centre taps run in pairs on the packed FP32 pipe (expf_ieee2,
-// pow128x2, packed dot and accumulation): each lane performs the scalar
-// operations of its tap with the same roundings, and the taps still
-// accumulate one after another in the order dx = -2..2 (outer), dy = -2..2
-// (inner), so the sums are those of the one-tap-at-a-time loop bit for bit.
-// |z_c - z_q| is taken as |z_q - z_c|, which is the same value (the two
-// differences are exact negations of each other under round-to-nearest).
+// The 24 off-centre taps run in pairs on the packed FP32 pipe
+// (atrous_weight2, packed accumulation of the four channels): each lane
+// performs the scalar operations of its tap with the same roundings, and the
+// taps still accumulate one after another in the order dx = -2..2 (outer),
+// dy = -2..2 (inner), so the sums are those of the one-tap-at-a-time loop
+// (atrous_weight) bit for bit.
 SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __restrict__ guide,
                          const uint2* __restrict__ res_in, V3 cn, float cd, float& rf0, float& rf1, float& rf2,
                          float& rf3) {
@@ -918,12 +917,13 @@ SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __r
         xs[d] = xx < 0 ? 0 : (xx > W - 1 ? W - 1 : xx);
         rows[d] = (size_t)(yy < 0 ? 0 : (yy > H - 1 ? H - 1 : yy)) * W;
     }
+    // the four channel sums, two per packed register
     float2 acc01 = make_float2(0.0f, 0.0f), acc23 = make_float2(0.0f, 0.0f);
     auto accumulate = [&](float f, uint2 t) {
         float a, b, c, e;
         unpack_h4(t, a, b, c, e);
-        acc01 = __ffma2_rn(f2s(f), make_float2(a, b), acc01);
-        acc23 = __ffma2_rn(f2s(f), make_float2(c, e), acc23);
+        acc01 = fma2(f2s(f), make_float2(a, b), acc01);
+        acc23 = fma2(f2s(f), make_float2(c, e), acc23);
     };
     const float ncd = -cd;
     const float2 cx = f2s(cn.x), cy = f2s(cn.y), cz = f2s(cn.z);
@@ -934,12 +934,7 @@ SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __r
         const size_t j0 = rows[t % 5] + xs[t / 5], j1 = rows[(t + 1) % 5] + xs[(t + 1) / 5];
         const float4 g0 = __ldg(guide + j0), g1 = __ldg(guide + j1);
         const uint2 r0 = ld_u2(res_in, j0), r1 = ld_u2(res_in, j1);
-        const float2 dz = __fadd2_rn(make_float2(g0.w, g1.w), f2s(ncd));
-        const float2 wz = expf_ieee2(make_float2(dz.x < 0.0f ? dz.x : -dz.x, dz.y < 0.0f ? dz.y : -dz.y));
-        const float2 dn = __ffma2_rn(cz, make_float2(g0.z, g1.z),
-                                     __ffma2_rn(cy, make_float2(g0.y, g1.y), __fmul2_rn(cx, make_float2(g0.x, g1.x))));
-        const float2 wn = pow128x2(make_float2(gmax(0.0f, dn.x), gmax(0.0f, dn.y)));
-        const float2 f = __fmul2_rn(wn, wz);
+        const float2 f = atrous_weight2(cx, cy, cz, ncd, g0, g1);
         accumulate(f.x, r0);
         accumulate(f.y, r1);
     }

@@ -67,47 +67,75 @@ SGI_D float pow128(float x) {
     float y = x * x; y = y * y; y = y * y; y = y * y; y = y * y; y = y * y; y = y * y; return y;
 }
 
-// Two lanes of the same functions on the packed FP32 pipe (sm_100+): every
-// __fmul2_rn / __fadd2_rn / __ffma2_rn component rounds exactly like the
-// scalar operation it stands for, so each lane returns the scalar result bit
-// for bit. x - a*b is written x + a*(-b) (round-to-nearest is symmetric, so
-// the product is the negated scalar product and the sum the scalar
-// difference); expf_ieee's early returns become selects at the end.
+// Two lanes of the same functions on the packed FP32 pipe (sm_100+). Each
+// packed component rounds like the scalar operation it stands for, with one
+// exception the lane self-check in sgi_selftest.cu found: a packed multiply
+// whose result feeds a packed add can be contracted into a packed fused
+// multiply-add despite -fmad=false and an explicit .rn (the scalar operations
+// are not). So no packed add below takes a packed product as an operand; a
+// product that is then added is formed per lane.
 SGI_D float2 f2s(float s) { return make_float2(s, s); }
-// expf_ieee's exact scaling by 2^k, split into a factor s (2^127, 2^-126 or 1)
-// and 2^k' with k' in the normal exponent range; k is updated to k'.
-SGI_D float exp_scale(int& k) {
-    const float s = k > 127 ? 1.7014118346046923e+38f : (k < -126 ? 1.1754943508222875e-38f : 1.0f);
-    k = k > 127 ? k - 127 : (k < -126 ? k + 126 : k);
-    return s;
+SGI_D unsigned long long pk2(float2 a) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
 }
-SGI_D float exp_special(float x, float v) {
-    return x != x ? x : (x > 88.72283935546875f ? __int_as_float(0x7f800000) : (x < -103.97283935546875f ? 0.0f : v));
+SGI_D float2 upk2(unsigned long long r) {
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+SGI_D float2 add2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(d);
+}
+SGI_D float2 mul2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(d);
+}
+SGI_D float2 fma2(float2 a, float2 b, float2 c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)), "l"(pk2(c)));
+    return upk2(d);
+}
+// x in [-87, 88] with |x| >= 2^-100, or 0: the reduced argument, the
+// polynomial, 2^k and the result are all normal numbers (or exact), and
+// expf_ieee's extra scaling steps do not apply; other lanes (underflow,
+// overflow, tiny and special arguments) take the scalar code.
+SGI_D bool exp_packable(float x) {
+    const float a = fabsf(x);
+    return a == 0.0f || (a >= 0x1p-100f && x >= -87.0f && x <= 88.0f);
+}
+// expf_ieee's range reduction, per lane (its products feed sums).
+SGI_D float exp_reduce(float x, float& kf) {
+    kf = floorf(x * 1.44269502162933349609375f + 0.5f);
+    return (x - kf * 0.693145751953125f) - kf * 1.428606765330187045037746429443359375e-06f;
 }
 SGI_D float2 expf_ieee2(float2 x) {
-    const float2 t = __fadd2_rn(__fmul2_rn(x, f2s(1.44269502162933349609375f)), f2s(0.5f));
-    const float2 kf = make_float2(floorf(t.x), floorf(t.y));
-    const float2 r = __fadd2_rn(__fadd2_rn(x, __fmul2_rn(kf, f2s(-0.693145751953125f))),
-                                __fmul2_rn(kf, f2s(-1.428606765330187045037746429443359375e-06f)));
-    float2 p = __ffma2_rn(r, f2s(1.0f / 5040.0f), f2s(1.0f / 720.0f));
-    p = __ffma2_rn(p, r, f2s(1.0f / 120.0f));
-    p = __ffma2_rn(p, r, f2s(1.0f / 24.0f));
-    p = __ffma2_rn(p, r, f2s(1.0f / 6.0f));
-    p = __ffma2_rn(p, r, f2s(0.5f));
-    p = __ffma2_rn(p, r, f2s(1.0f));
-    p = __ffma2_rn(p, r, f2s(1.0f));
-    // __float2int_rz is defined for NaN and infinities (those lanes are selected away)
-    int k0 = __float2int_rz(kf.x), k1 = __float2int_rz(kf.y);
-    const float2 s = make_float2(exp_scale(k0), exp_scale(k1));   // p * 1 = p exactly
-    p = __fmul2_rn(__fmul2_rn(p, s), make_float2(__uint_as_float((uint32_t)(k0 + 127) << 23),
-                                                 __uint_as_float((uint32_t)(k1 + 127) << 23)));
-    return make_float2(exp_special(x.x, p.x), exp_special(x.y, p.y));
+    if (!(exp_packable(x.x) && exp_packable(x.y))) return make_float2(expf_ieee(x.x), expf_ieee(x.y));
+    float2 kf;
+    const float2 r = make_float2(exp_reduce(x.x, kf.x), exp_reduce(x.y, kf.y));
+    float2 p = fma2(r, f2s(1.0f / 5040.0f), f2s(1.0f / 720.0f));
+    p = fma2(p, r, f2s(1.0f / 120.0f));
+    p = fma2(p, r, f2s(1.0f / 24.0f));
+    p = fma2(p, r, f2s(1.0f / 6.0f));
+    p = fma2(p, r, f2s(0.5f));
+    p = fma2(p, r, f2s(1.0f));
+    p = fma2(p, r, f2s(1.0f));
+    const int k0 = (int)kf.x, k1 = (int)kf.y;   // in [-126, 127]
+    return mul2(p, make_float2(__int_as_float((k0 + 127) << 23), __int_as_float((k1 + 127) << 23)));
 }
+// x^128 by seven squarings, the first six packed and the last one per lane:
+// for 0 <= x <= 1 the squares decrease, so if x^64 >= 2^-126 every packed
+// square was a normal number, and otherwise x^64 < 2^-126 in both forms and
+// the last square is 0 in both (for x >= 1 the squares grow).
 SGI_D float2 pow128x2(float2 x) {
-    float2 y = __fmul2_rn(x, x);
+    float2 y = mul2(x, x);
 #pragma unroll
-    for (int i = 0; i < 6; ++i) y = __fmul2_rn(y, y);
-    return y;
+    for (int i = 0; i < 5; ++i) y = mul2(y, y);
+    return make_float2(y.x * y.x, y.y * y.y);
 }
 
 // ---------------------------------------------------------------- vectors --
@@ -153,6 +181,25 @@ SGI_D V3 world_from_depth(float u, float v, float depth, const float* inv_pv) {
     float z = depth * 2.0f - 1.0f;
     V4 w = mat4_mul(inv_pv, u * 2.0f - 1.0f, v * 2.0f - 1.0f, z, 1.0f);
     return V3{w.x, w.y, w.z} / w.w;
+}
+
+// Edge-stopping weight of one a-trous tap q for the centre (cn, cd)
+// (filterInput, vpl_pbr_gi_denoise.fs:142-190, sigmaZ = 1):
+// pow(max(0, cn . nq), 128) * exp(-|cd - zq|).
+SGI_D float atrous_weight(V3 cn, float cd, float4 gq) {
+    const float wz = expf_ieee(-gabs(cd - gq.w));
+    const float wn = pow128(gmax(0.0f, dot(cn, v3(gq.x, gq.y, gq.z))));
+    return wn * wz;
+}
+// The weights of two taps at once, each lane equal to atrous_weight. The
+// depth term uses zq - cd (ncd = -cd): |zq - cd| and |cd - zq| are the same
+// value. The final product is taken per lane (it may be subnormal).
+SGI_D float2 atrous_weight2(float2 cx, float2 cy, float2 cz, float ncd, float4 g0, float4 g1) {
+    const float2 dz = add2(make_float2(g0.w, g1.w), f2s(ncd));
+    const float2 wz = expf_ieee2(make_float2(dz.x < 0.0f ? dz.x : -dz.x, dz.y < 0.0f ? dz.y : -dz.y));
+    const float2 dn = fma2(cz, make_float2(g0.z, g1.z), fma2(cy, make_float2(g0.y, g1.y), mul2(cx, make_float2(g0.x, g1.x))));
+    const float2 wn = pow128x2(make_float2(gmax(0.0f, dn.x), gmax(0.0f, dn.y)));
+    return make_float2(wn.x * wz.x, wn.y * wz.y);
 }
 
 // hash / floatConstruct / random(vec3), common.glsl:183-214

@@ -756,6 +756,8 @@ SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX,
     if (candidates <= 0) return;
     const float minGi = p.sc.min_gi_occlusion;
     const V3 fragPos = px.fragPos, normal = px.normal;
+    const VplPixel vp = vpl_pixel(fragPos, px.baseColor, normal, px.viewDir, px.distToCamera, px.roughness,
+                                  px.metallic, px.ambient, px.baseRefl, sp);
     for (int s = 0, resamples = 0; s < px.sampleCount; ++s) {
         const float rnd = random3(seedX, seedY, seedZ);
         seedZ += 10000.0f;
@@ -791,9 +793,8 @@ SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX,
         float reweight = 1.0f;
         if (shadowFactor > 0.0f) reweight = (1.0f - distAttenuation) * minGi + distAttenuation;
         validSamples += reweight;
-        const V3 tmp = px.ao * vpl_lighting2(fragPos, px.baseColor, normal, px.viewDir, v3(spec.x, spec.y, spec.z),
-                                             lightPosition, lightColor, px.distToCamera, lightRadius, px.roughness,
-                                             px.metallic, px.ambient, px.baseRefl, sp);
+        const V3 tmp = px.ao * vpl_lighting2_sample(vp, v3(spec.x, spec.y, spec.z), lightPosition, lightColor,
+                                                    lightRadius);
         vplColor = vplColor + (1.0f - shadowFactor) * tmp;
     }
 }

@@ -335,30 +335,52 @@ SGI_D float vpl_atten(V3 lightDir, float radius) {
     float minDist = mixf(10.0f, 1.0f, expf_ieee(-3.0f * ratio)) * radius;
     return 1.0f / (minDist + 1.0f * d * d);
 }
-// calculateVirtualPointLighting2 (shadowFactor argument 0, fog intensity 0,
-// ambient intensity 0) -> calculateLighting_Lambert_SeparateDiffuseSpecular ->
-// BRDF_Lambert_SeparateDiffuseSpecular; pbr2.glsl:613-657, :541-574, :382-452.
-SGI_D V3 vpl_lighting2(V3 fragPos, V3 baseColor, V3 N, V3 V, V3 specPos, V3 diffPos, V3 lightColor, float viewDist,
-                       float radius, float roughness, float metallic, float ao, V3 baseRefl, const ShadeParams& sp) {
-    V3 specDir = specPos - fragPos;
-    V3 diffDir = diffPos - fragPos;
-    float adjusted = 1.0f - 0.0f;
+// The per-pixel part of vpl_lighting2: everything that does not depend on the
+// VPL (BRDF_Base's remapped roughness, diffuse colour and F0, and the fog
+// factor of the view distance), computed once per pixel instead of once per
+// sample; vpl_lighting2_sample then evaluates exactly the remaining operations.
+struct VplPixel {
+    V3 fragPos, N, V, dc, f0, fogAdd;
+    float rr, fogF, ao;
+};
+SGI_D VplPixel vpl_pixel(V3 fragPos, V3 baseColor, V3 N, V3 V, float viewDist, float roughness, float metallic,
+                         float ao, V3 baseRefl, const ShadeParams& sp) {
+    VplPixel q;
+    q.fragPos = fragPos; q.N = N; q.V = V; q.ao = ao;
+    const V3 specMult = 1.0f / (baseColor + kEps);
+    brdf_base(baseColor, baseRefl, roughness, metallic, baseColor, specMult, sp, q.rr, q.dc, q.f0);
+    // applyFog(color, viewDist, 0) = color * f + fc * (1 - f), fc = fogColor * 0
+    q.fogF = expf_ieee(-sp.fog_density * viewDist);
+    const V3 fc = v3(sp.fog_color[0], sp.fog_color[1], sp.fog_color[2]) * 0.0f;
+    q.fogAdd = fc * (1.0f - q.fogF);
+    return q;
+}
+SGI_D V3 vpl_lighting2_sample(const VplPixel& q, V3 specPos, V3 diffPos, V3 lightColor, float radius) {
+    V3 specDir = specPos - q.fragPos;
+    V3 diffDir = diffPos - q.fragPos;
     float specAtten = vpl_atten(specDir, radius);
     float diffAtten = vpl_atten(diffDir, radius);
-    V3 specMult = 1.0f / (baseColor + kEps);
-    float rr; V3 dc, f0;
-    brdf_base(baseColor, baseRefl, roughness, metallic, baseColor, specMult, sp, rr, dc, f0);
     float NdotV, NdotL, NdotH, LdotH;
-    brdf_dots(V, specDir, N, NdotV, NdotL, NdotH, LdotH);
-    V3 Fr = spec_brdf(NdotV, NdotL, NdotH, LdotH, rr, f0) * NdotL;
-    brdf_dots(V, diffDir, N, NdotV, NdotL, NdotH, LdotH);
-    V3 Fd = (dc * (1.0f / kPi)) * NdotL;
+    brdf_dots(q.V, specDir, q.N, NdotV, NdotL, NdotH, LdotH);
+    V3 Fr = spec_brdf(NdotV, NdotL, NdotH, LdotH, q.rr, q.f0) * NdotL;
+    brdf_dots(q.V, diffDir, q.N, NdotV, NdotL, NdotH, LdotH);
+    V3 Fd = (q.dc * (1.0f / kPi)) * NdotL;
     V3 bs = specAtten * Fr;
     V3 bd = diffAtten * Fd;
     V3 brdf = bs + bd;
-    V3 ambient = brdf * ao * lightColor * 0.0f;
+    V3 ambient = brdf * q.ao * lightColor * 0.0f;
     V3 finalB = brdf * lightColor;
-    return ambient + adjusted * apply_fog(finalB, viewDist, 0.0f, sp);
+    // the shader scales the fogged term by 1.0 - 0.0, which is exactly 1
+    return ambient + (finalB * q.fogF + q.fogAdd);
+}
+// calculateVirtualPointLighting2 (shadowFactor argument 0, fog intensity 0,
+// ambient intensity 0) -> calculateLighting_Lambert_SeparateDiffuseSpecular ->
+// BRDF_Lambert_SeparateDiffuseSpecular; pbr2.glsl:613-657, :541-574, :382-452:
+// the two parts above in sequence.
+SGI_D V3 vpl_lighting2(V3 fragPos, V3 baseColor, V3 N, V3 V, V3 specPos, V3 diffPos, V3 lightColor, float viewDist,
+                       float radius, float roughness, float metallic, float ao, V3 baseRefl, const ShadeParams& sp) {
+    return vpl_lighting2_sample(vpl_pixel(fragPos, baseColor, N, V, viewDist, roughness, metallic, ao, baseRefl, sp),
+                                specPos, diffPos, lightColor, radius);
 }
 
 }  // namespace sgi

@@ -101,7 +101,7 @@ void free_all(sgi_ctx* c) {
                     c->hist_depth[0], c->hist_depth[1]};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto* p : c->pass_bufs) if (p) cudaFree(p);
-    void* nnp[] = {c->nn_feat, c->nn_noisy, c->nn_prev, c->nn_den};
+    void* nnp[] = {c->nn_feat, c->nn_prev};
     for (void* p : nnp) if (p) cudaFree(p);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     if (c->fork) cudaEventDestroy(c->fork);
@@ -618,9 +618,7 @@ static sgi_status nn_buffers(sgi_ctx* ctx) {
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t r) { if (e == cudaSuccess && r != cudaSuccess) e = r; };
     chk(dalloc(&ctx->nn_feat, P * 16));
-    chk(dalloc(&ctx->nn_noisy, P));
     chk(dalloc(&ctx->nn_prev, P));
-    chk(dalloc(&ctx->nn_den, P));
     if (e != cudaSuccess) return cuda_fail(ctx, e, "allocate denoiser buffers");
     return SGI_OK;
 }
@@ -688,16 +686,17 @@ sgi_status sgi_render_frame_neural(sgi_ctx* ctx, sgi_nn* net, const sgi_gbuffer*
     st = run_gather(ctx, cur, cam, params, s);
     if (st != SGI_OK) return st;
     record(ctx, 4, s);
-    st = run_features(ctx, cur, cam, ctx->nn_feat, ctx->nn_noisy, ctx->nn_prev, s);
+    st = run_features(ctx, cur, cam, ctx->nn_feat, nullptr, ctx->nn_prev, s);
     if (st != SGI_OK) return st;
-    st = sgi_nn_forward(net, ctx->nn_feat, (const float*)ctx->nn_noisy, (const float*)ctx->nn_prev, 1, H, W,
-                        (float*)ctx->nn_den, stream);
+    st = nn_forward_net(net, ctx->nn_feat, H, W, s);
     if (st != SGI_OK) return fail(ctx, st, std::string("denoiser: ") + sgi_nn_last_error(net));
     if (overlap) SGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->join, 0), "join direct lighting");
-    SGI_CUDA(ctx, sgi::nn::composite(ctx->nn_den, ctx->direct, cur->albedo, (uint2*)hdr_out,
-                                     ctx->gi_hist[1 - ctx->hist_cur], ctx->hist_depth[1 - ctx->hist_cur],
-                                     pixels(ctx->cfg), s), "kpcn_composite");
-    ctx->launches += 17;
+    // the kernel apply writes the composite (HDR frame, GI history) directly
+    st = nn_apply_composite(net, ctx->last_merged, (const float*)ctx->nn_prev, H, W, ctx->direct,
+                            cur->albedo, (uint2*)hdr_out, ctx->gi_hist[1 - ctx->hist_cur],
+                            ctx->hist_depth[1 - ctx->hist_cur], s);
+    if (st != SGI_OK) return fail(ctx, st, std::string("denoiser: ") + sgi_nn_last_error(net));
+    ctx->launches += 16;
     ctx->hist_cur = 1 - ctx->hist_cur;
     ctx->have_history = true;
     record(ctx, 5, s);

@@ -56,9 +56,7 @@ struct sgi_ctx {
 
     // learned-denoiser inputs/outputs (allocated on first use)
     __nv_bfloat16* nn_feat = nullptr;
-    float4* nn_noisy = nullptr;
     float4* nn_prev = nullptr;
-    float4* nn_den = nullptr;
 
     // timing
     bool timing = false;

@@ -390,6 +390,27 @@ __global__ void up_fwd_kernel(View in, View out, int B, int H, int W, int g8) {
     vec8(out, b, (size_t)y * W + x, g) = vec8(in, b, (size_t)(y / 2) * (W / 2) + x / 2, g);
 }
 
+// The same for even H and W, one thread per input pixel and channel group:
+// one 16-byte load, four 16-byte stores (the 2x2 block it is copied to).
+template <bool PIXFAST>
+__global__ void up2x2_fwd_kernel(View in, View out, int B, int Hi, int Wi, int g8) {
+    pdl_wait();
+    pdl_trigger();
+    const unsigned n = (unsigned)B * Hi * Wi * g8;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned q;
+    int g, b;
+    split_index<PIXFAST>(i, (unsigned)Hi * Wi, g8, q, g, b);
+    const int x = (int)(q % Wi), y = (int)(q / Wi);
+    const uint4 v = vec8(in, b, q, g);
+    const size_t W = 2 * (size_t)Wi, o = (size_t)(2 * y) * W + 2 * x;
+    vec8(out, b, o, g) = v;
+    vec8(out, b, o + 1, g) = v;
+    vec8(out, b, o + W, g) = v;
+    vec8(out, b, o + W + 1, g) = v;
+}
+
 // din[b, y, x] = sum of dout over the 2x2 block it was copied to
 template <bool PIXFAST>
 __global__ void up_bwd_kernel(View dout, View din, int B, int Hi, int Wi, int g8) {
@@ -442,6 +463,12 @@ cudaError_t up_fwd(const View& in, const View& out, int B, int H, int W, int c, 
     const size_t n = (size_t)B * H * W * (c / 8);
     if (!view_ok(in) || !view_ok(out) || !launch_ok(n, c)) return cudaErrorInvalidValue;
     if (n == 0) return cudaSuccess;
+    if (H % 2 == 0 && W % 2 == 0) {
+        const size_t ni = n / 4;
+        if (out.grp == 8)
+            return launch_pdl(up2x2_fwd_kernel<false>, dim3(blocks_for(ni)), dim3(256), 0, s, in, out, B, H / 2, W / 2, c / 8);
+        return launch_pdl(up2x2_fwd_kernel<true>, dim3(blocks_for(ni)), dim3(256), 0, s, in, out, B, H / 2, W / 2, c / 8);
+    }
     if (out.grp == 8) return launch_pdl(up_fwd_kernel<false>, dim3(blocks_for(n)), dim3(256), 0, s, in, out, B, H, W, c / 8);
     return launch_pdl(up_fwd_kernel<true>, dim3(blocks_for(n)), dim3(256), 0, s, in, out, B, H, W, c / 8);
 }
@@ -459,6 +486,31 @@ cudaError_t up_bwd(const View& dout, const View& din, int B, int Hi, int Wi, int
 // [B, H, W, 4] float (rgb used). out = a * sum_k softmax(l)_k noisy(p + o_k) + (1 - a) * prev,
 // a = sigmoid(l25); neighbours clamped to the image. With a target, also the
 // loss sum of |log1p(out) - log1p(target)| and dlogits = d(mean loss)/dlogits.
+// The composite of one pixel's denoised GI (d0, d1, d2): the direct lighting
+// plus the GI times the gather's colour output (albedo + 1e-5 stored as FP16),
+// the GI history and a history length of 1.
+__device__ __forceinline__ void composite_px(float d0, float d1, float d2, const uint2* __restrict__ screen,
+                                             const uint32_t* __restrict__ albedo, uint2* __restrict__ hdr,
+                                             uint2* __restrict__ gi_out, uint16_t* __restrict__ hist_out, size_t i) {
+    const uint2 st = screen[i];
+    const float sc0 = __half2float(__ushort_as_half((uint16_t)(st.x & 0xffffu)));
+    const float sc1 = __half2float(__ushort_as_half((uint16_t)(st.x >> 16)));
+    const float sc2 = __half2float(__ushort_as_half((uint16_t)(st.y & 0xffffu)));
+    const uint32_t alb = albedo[i];
+    const float g0 = __half2float(__float2half_rn(fmaxf((alb & 0xffu) / 255.0f, 0.01f) + 0.00001f));
+    const float g1 = __half2float(__float2half_rn(fmaxf(((alb >> 8) & 0xffu) / 255.0f, 0.01f) + 0.00001f));
+    const float g2 = __half2float(__float2half_rn(fmaxf(((alb >> 16) & 0xffu) / 255.0f, 0.01f) + 0.00001f));
+    auto pack = [](float a0, float a1, float a2, float a3) {
+        return make_uint2((uint32_t)__half_as_ushort(__float2half_rn(a0)) |
+                              ((uint32_t)__half_as_ushort(__float2half_rn(a1)) << 16),
+                          (uint32_t)__half_as_ushort(__float2half_rn(a2)) |
+                              ((uint32_t)__half_as_ushort(__float2half_rn(a3)) << 16));
+    };
+    hdr[i] = pack(sc0 + g0 * d0, sc1 + g1 * d1, sc2 + g2 * d2, 1.0f);
+    gi_out[i] = pack(d0, d1, d2, 1.0f);
+    hist_out[i] = __half_as_ushort(__float2half_rn(1.0f));
+}
+
 constexpr int kApplyTX = 32, kApplyTY = 8;
 template <bool TRAIN>
 __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
@@ -474,7 +526,15 @@ __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
     for (int v = threadIdx.x; v < (kApplyTY + 4) * (kApplyTX + 4); v += 256) {
         const int hy = v / (kApplyTX + 4), hx = v % (kApplyTX + 4);
         const int yy = min(max(y0 + hy - 2, 0), H - 1), xx = min(max(x0 + hx - 2, 0), W - 1);
-        tile[hy][hx] = nz[(size_t)yy * W + xx];
+        const size_t t = (size_t)yy * W + xx;
+        if (a.noisy_h) {   // the same values as the float4 copy the feature pass can write
+            const uint2 h = a.noisy_h[(size_t)b * H * W + t];
+            tile[hy][hx] = make_float4(__half2float(__ushort_as_half((uint16_t)(h.x & 0xffffu))),
+                                       __half2float(__ushort_as_half((uint16_t)(h.x >> 16))),
+                                       __half2float(__ushort_as_half((uint16_t)(h.y & 0xffffu))), 1.0f);
+        } else {
+            tile[hy][hx] = nz[t];
+        }
     }
     __syncthreads();
     const int x = x0 + tx, y = y0 + ty;
@@ -505,7 +565,10 @@ __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
         float o[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) o[c] = alpha * sp[c] + (1.0f - alpha) * pr[c];
-        if (!TRAIN) a.out[i] = make_float4(o[0], o[1], o[2], 1.0f);
+        if (!TRAIN) {
+            if (a.hdr) composite_px(o[0], o[1], o[2], a.screen, a.albedo, a.hdr, a.gi_out, a.hist_out, i);
+            else a.out[i] = make_float4(o[0], o[1], o[2], 1.0f);
+        }
         if (TRAIN) {
             const float4 tv = a.target[i];
             const float t[3] = {tv.x, tv.y, tv.z};
@@ -556,12 +619,14 @@ __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
 cudaError_t kpcn_apply(const ApplyArgs& a, cudaStream_t s) {
     if (!view_ok(a.logits) || (a.target && !view_ok(a.dlogits))) return cudaErrorInvalidValue;
     if (a.B < 1 || a.H < 1 || a.W < 1 || a.B > 65535) return cudaErrorInvalidValue;
+    if ((!a.noisy && !a.noisy_h) || !a.prev || (a.target && a.noisy_h)) return cudaErrorInvalidValue;
     dim3 grid((a.W + kApplyTX - 1) / kApplyTX, (a.H + kApplyTY - 1) / kApplyTY, a.B);
     if (a.target) {
         if (!a.loss || !a.target) return cudaErrorInvalidValue;
         return launch_pdl(kpcn_apply_kernel<true>, grid, dim3(256), 0, s, a);
     }
-    if (!a.out) return cudaErrorInvalidValue;
+    const bool composite = a.hdr && a.screen && a.albedo && a.gi_out && a.hist_out && a.B == 1;
+    if (!a.out && !composite) return cudaErrorInvalidValue;
     return launch_pdl(kpcn_apply_kernel<false>, grid, dim3(256), 0, s, a);
 }
 
@@ -737,7 +802,7 @@ __global__ void __launch_bounds__(256) features_kernel(FeatureArgs a) {
     pr.z = p00.z * w00 + p10.z * w10 + p01.z * w01 + p11.z * w11;
     pr.w = 1.0f;
     if (!a.have_history) pr = make_float4(nz.x, nz.y, nz.z, 1.0f);
-    a.noisy[i] = make_float4(nz.x, nz.y, nz.z, 1.0f);
+    if (a.noisy) a.noisy[i] = make_float4(nz.x, nz.y, nz.z, 1.0f);
     a.prev[i] = pr;
     float f[16];
     f[0] = log1pf(fmaxf(nz.x, 0.0f)); f[1] = log1pf(fmaxf(nz.y, 0.0f)); f[2] = log1pf(fmaxf(nz.z, 0.0f));
@@ -767,20 +832,7 @@ __global__ void composite_kernel(const float4* __restrict__ den, const uint2* __
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
     const float4 d = den[i];
-    const float4 sc = unpack4(screen[i]);
-    const uint32_t alb = albedo[i];
-    const float g0 = __half2float(__float2half_rn(fmaxf((alb & 0xffu) / 255.0f, 0.01f) + 0.00001f));
-    const float g1 = __half2float(__float2half_rn(fmaxf(((alb >> 8) & 0xffu) / 255.0f, 0.01f) + 0.00001f));
-    const float g2 = __half2float(__float2half_rn(fmaxf(((alb >> 16) & 0xffu) / 255.0f, 0.01f) + 0.00001f));
-    auto pack = [](float a0, float a1, float a2, float a3) {
-        return make_uint2((uint32_t)__half_as_ushort(__float2half_rn(a0)) |
-                              ((uint32_t)__half_as_ushort(__float2half_rn(a1)) << 16),
-                          (uint32_t)__half_as_ushort(__float2half_rn(a2)) |
-                              ((uint32_t)__half_as_ushort(__float2half_rn(a3)) << 16));
-    };
-    hdr[i] = pack(sc.x + g0 * d.x, sc.y + g1 * d.y, sc.z + g2 * d.z, 1.0f);
-    gi_out[i] = pack(d.x, d.y, d.z, 1.0f);
-    hist_out[i] = __half_as_ushort(__float2half_rn(1.0f));
+    composite_px(d.x, d.y, d.z, screen, albedo, hdr, gi_out, hist_out, i);
 }
 
 cudaError_t composite(const float4* den, const uint2* screen, const uint32_t* albedo, uint2* hdr, uint2* gi_out,

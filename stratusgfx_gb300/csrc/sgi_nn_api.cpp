@@ -432,6 +432,33 @@ sgi_status sgi_nn_get_grads(sgi_nn* n, float* host, int64_t count) {
     return e == cudaSuccess ? SGI_OK : nn_cuda(n, e, "get grads");
 }
 
+}  // extern "C"
+
+sgi_status nn_forward_net(sgi_nn* n, const void* features, int H, int W, cudaStream_t s) {
+    if (!n || !features) return nn_fail(n, SGI_ERR_ARG, "NULL tensor");
+    if (!shape_ok(n, 1, H, W)) return nn_fail(n, SGI_ERR_CAP, "batch/size exceed the network's capacity or H, W % 4");
+    cudaError_t e = n->net.forward((const __nv_bfloat16*)features, 1, H, W, s);
+    if (e == cudaErrorNotReady) return nn_fail(n, SGI_ERR_STATE, "FP8 precision needs sgi_nn_calibrate_fp8 after the last weight change");
+    return e == cudaSuccess ? SGI_OK : nn_cuda(n, e, "forward");
+}
+
+sgi_status nn_apply_composite(sgi_nn* n, const uint2* noisy, const float* prev, int H, int W, const uint2* screen,
+                              const uint32_t* albedo, uint2* hdr, uint2* gi_out, uint16_t* hist_out, cudaStream_t s) {
+    if (!n || !noisy || !prev || !screen || !albedo || !hdr || !gi_out || !hist_out)
+        return nn_fail(n, SGI_ERR_ARG, "NULL tensor");
+    if (!shape_ok(n, 1, H, W)) return nn_fail(n, SGI_ERR_CAP, "batch/size exceed the network's capacity or H, W % 4");
+    const sgi::nn::View none{nullptr, 8, 8, 8};
+    sgi::nn::ApplyArgs a{sgi::nn::planar_view(n->net.LOG, 4, H, W), nullptr, (const float4*)prev, nullptr,
+                         nullptr, none, nullptr, 0.0f, 1, H, W};
+    a.noisy_h = noisy;
+    a.screen = screen; a.albedo = albedo; a.hdr = hdr; a.gi_out = gi_out; a.hist_out = hist_out;
+    const cudaError_t e = sgi::nn::kpcn_apply(a, s);
+    n->net.launches += 1;
+    return e == cudaSuccess ? SGI_OK : nn_cuda(n, e, "apply");
+}
+
+extern "C" {
+
 sgi_status sgi_nn_forward(sgi_nn* n, const void* features, const float* noisy, const float* prev, int32_t B,
                           int32_t H, int32_t W, float* out, void* stream) {
     if (!n || !features || !noisy || !prev || !out) return nn_fail(n, SGI_ERR_ARG, "NULL tensor");

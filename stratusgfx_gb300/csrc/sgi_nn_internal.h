@@ -74,6 +74,15 @@ struct ApplyArgs {
     float* loss;                  // sum of |log1p(out) - log1p(target)| (device scalar) or null
     float grad_scale;             // 1 / (3 * pixels)
     int B, H, W;
+    // inference only: with hdr set, the composite of the GI frame is written
+    // instead of `out` (hdr = screen + albedo' * gi, gi_out = gi, hist_out = 1;
+    // see composite) - B must be 1
+    const uint2* noisy_h = nullptr;   // if set, noisy is read from this RGBA16F image instead
+    const uint2* screen = nullptr;
+    const uint32_t* albedo = nullptr;
+    uint2* hdr = nullptr;
+    uint2* gi_out = nullptr;
+    uint16_t* hist_out = nullptr;
 };
 
 struct FeatureArgs {
@@ -88,7 +97,7 @@ struct FeatureArgs {
     float inv_pv[16];
     float cam_pos[3];
     __nv_bfloat16* features;      // [P][16]
-    float4* noisy;
+    float4* noisy;                // or null (not written)
     float4* prev;
 };
 

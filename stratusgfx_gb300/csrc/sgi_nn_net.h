@@ -69,3 +69,12 @@ struct sgi_nn {
     std::string err;
     int step = 0;
 };
+
+// The two halves of sgi_nn_forward for one image (B = 1), for the frame path:
+// the U-Net, then the kernel apply with the frame's composite fused into it
+// (the HDR frame, the GI history and the history length are written instead
+// of the denoised GI; see sgi::nn::composite). The noisy GI is read from the
+// RGBA16F pass-0 output the features were built from.
+sgi_status nn_forward_net(sgi_nn* n, const void* features, int H, int W, cudaStream_t s);
+sgi_status nn_apply_composite(sgi_nn* n, const uint2* noisy, const float* prev, int H, int W, const uint2* screen,
+                              const uint32_t* albedo, uint2* hdr, uint2* gi_out, uint16_t* hist_out, cudaStream_t s);

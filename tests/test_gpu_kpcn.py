@@ -141,6 +141,16 @@ def test_neural_frame_runs_through_the_abi():
     torch.cuda.synchronize()
     o = out.float().cpu().numpy()
     assert np.isfinite(o).all() and (o[..., :3] > 0).mean() > 0.5
+    # the kernel apply writes the composite: HDR = direct + (albedo + 1e-5 as FP16) * GI,
+    # with the GI history holding the same GI rounded to FP16
+    H, W = w.height, w.width
+    direct = st.read_debug(abi.SGI_DEBUG_DIRECT, np.uint16).view(np.float16).reshape(H, W, 4).astype(np.float32)
+    gi = st.read_debug(abi.SGI_DEBUG_GI_HISTORY, np.uint16).view(np.float16).reshape(H, W, 4).astype(np.float32)
+    alb = ds.gbuffers[2].albedo.cpu().numpy()[..., :3].astype(np.float32) / 255.0
+    g = (np.maximum(alb, 0.01) + 1e-5).astype(np.float16).astype(np.float32)
+    want = direct[..., :3] + g * gi[..., :3]
+    assert np.allclose(o[..., :3], want, rtol=4e-3, atol=1e-4), np.abs(o[..., :3] - want).max()
+    assert (gi[..., 3] == 1.0).all() and (o[..., 3] == 1.0).all()
     st.close()
     net.close()
 

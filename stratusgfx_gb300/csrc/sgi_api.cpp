@@ -627,6 +627,7 @@ static sgi_status run_features(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_c
                                float4* noisy, float4* prevw, cudaStream_t s) {
     sgi::nn::FeatureArgs a;
     a.W = ctx->cfg.width; a.H = ctx->cfg.height;
+    a.inv_w = 1.0f / (float)a.W; a.inv_h = 1.0f / (float)a.H;
     a.merged = ctx->last_merged; a.guide = ctx->guide;
     a.albedo = cur->albedo; a.rma = cur->roughness_metallic_ambient; a.velocity = cur->velocity;
     a.gi_prev = ctx->gi_hist[ctx->feat_hist];

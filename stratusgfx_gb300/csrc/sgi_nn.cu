@@ -757,6 +757,11 @@ __device__ __forceinline__ float4 unpack4(uint2 t) {
 }
 __device__ __forceinline__ float lum(float4 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
 
+// log(1 + max(x, 0)) to the precision of a BF16 feature: the fast natural
+// logarithm of 1 + x (the features are stored in BF16, 8 significant bits).
+__device__ __forceinline__ float log1p_bf(float x) { return __logf(1.0f + fmaxf(x, 0.0f)); }
+constexpr float k255 = 1.0f / 255.0f;
+
 __global__ void __launch_bounds__(256) features_kernel(FeatureArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -772,19 +777,20 @@ __global__ void __launch_bounds__(256) features_kernel(FeatureArgs a) {
             const float l = lum(unpack4(a.merged[(size_t)yy * W + xx]));
             s1 += l; s2 += l * l;
         }
-    const float mean = s1 / 9.0f;
-    const float var = fmaxf(s2 / 9.0f - mean * mean, 0.0f);
+    const float mean = s1 * (1.0f / 9.0f);
+    const float var = fmaxf(s2 * (1.0f / 9.0f) - mean * mean, 0.0f);
     const float4 g = a.guide[i];
     const uint32_t alb = a.albedo[i], rma = a.rma[i];
     // view distance from the unprojected depth
-    const float u = (x + 0.5f) / W, v = (y + 0.5f) / H;
+    const float u = (x + 0.5f) * a.inv_w, v = (y + 0.5f) * a.inv_h;
     const float* m = a.inv_pv;
     const float nx = u * 2.0f - 1.0f, ny = v * 2.0f - 1.0f, nzc = g.w * 2.0f - 1.0f;
     const float wx = m[0] * nx + m[4] * ny + m[8] * nzc + m[12];
     const float wy = m[1] * nx + m[5] * ny + m[9] * nzc + m[13];
     const float wz = m[2] * nx + m[6] * ny + m[10] * nzc + m[14];
     const float ww = m[3] * nx + m[7] * ny + m[11] * nzc + m[15];
-    const float px = wx / ww - a.cam_pos[0], py = wy / ww - a.cam_pos[1], pz = wz / ww - a.cam_pos[2];
+    const float rw = __frcp_rn(ww);
+    const float px = wx * rw - a.cam_pos[0], py = wy * rw - a.cam_pos[1], pz = wz * rw - a.cam_pos[2];
     const float dist = sqrtf(px * px + py * py + pz * pz);
     // previous output warped by the velocity (bilinear, clamped)
     const uint32_t vel = a.velocity[i];
@@ -805,15 +811,15 @@ __global__ void __launch_bounds__(256) features_kernel(FeatureArgs a) {
     if (a.noisy) a.noisy[i] = make_float4(nz.x, nz.y, nz.z, 1.0f);
     a.prev[i] = pr;
     float f[16];
-    f[0] = log1pf(fmaxf(nz.x, 0.0f)); f[1] = log1pf(fmaxf(nz.y, 0.0f)); f[2] = log1pf(fmaxf(nz.z, 0.0f));
-    f[3] = fmaxf((alb & 0xffu) / 255.0f, 0.01f); f[4] = fmaxf(((alb >> 8) & 0xffu) / 255.0f, 0.01f);
-    f[5] = fmaxf(((alb >> 16) & 0xffu) / 255.0f, 0.01f);
+    f[0] = log1p_bf(nz.x); f[1] = log1p_bf(nz.y); f[2] = log1p_bf(nz.z);
+    f[3] = fmaxf((alb & 0xffu) * k255, 0.01f); f[4] = fmaxf(((alb >> 8) & 0xffu) * k255, 0.01f);
+    f[5] = fmaxf(((alb >> 16) & 0xffu) * k255, 0.01f);
     f[6] = g.x; f[7] = g.y; f[8] = g.z;
     f[9] = dist * 0.1f;
-    f[10] = (rma & 0xffu) / 255.0f;
-    f[11] = log1pf(var);
-    f[12] = log1pf(fmaxf(pr.x, 0.0f)); f[13] = log1pf(fmaxf(pr.y, 0.0f)); f[14] = log1pf(fmaxf(pr.z, 0.0f));
-    f[15] = ((rma >> 8) & 0xffu) / 255.0f;
+    f[10] = (rma & 0xffu) * k255;
+    f[11] = log1p_bf(var);
+    f[12] = log1p_bf(pr.x); f[13] = log1p_bf(pr.y); f[14] = log1p_bf(pr.z);
+    f[15] = ((rma >> 8) & 0xffu) * k255;
     __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(a.features + i * 16);
 #pragma unroll
     for (int k = 0; k < 8; ++k) o[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);

@@ -87,6 +87,7 @@ struct ApplyArgs {
 
 struct FeatureArgs {
     int W, H;
+    float inv_w, inv_h;           // 1 / W, 1 / H
     const uint2* merged;          // denoise pass-0 output (RGBA16F)
     const float4* guide;          // normal xyz, depth
     const uint32_t* albedo;

@@ -18,6 +18,7 @@ oracle, all host threads) on the same workload.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -39,7 +40,7 @@ UNIT = "Mpix/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["hd", "small"], default="hd")
@@ -63,7 +64,11 @@ def workload(name):
 
 # ------------------------------------------------------------- clocks ----
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clock and throttle-reason samples every 50 ms. start() returns
+    once the first sample is in, so the samples cover the timed region;
+    window() marks that region and stop() keeps the samples taken inside it
+    (all samples if none fell inside, which the result says)."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -71,43 +76,60 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-i", str(self.gpu), "-lms", "200"], stdout=open(self.path, "w"),
+                                          "-i", str(self.gpu), "-lms", "50"], stdout=open(self.path, "w"),
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        deadline = time.time() + 5.0
+        while time.time() < deadline and os.path.getsize(self.path) == 0 and self.proc.poll() is None:
+            time.sleep(0.01)
+
+    def window(self, begin: bool):
+        if begin:
+            self.t0 = datetime.datetime.now()
+        else:
+            self.t1 = datetime.datetime.now()
 
     def stop(self) -> dict:
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.06)   # one more sample after the timed region
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, mx, reasons = [], None, set()
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         with open(self.path) as f:
             for line in f:
                 parts = [p.strip() for p in line.split(",")]
-                if len(parts) < 9:
+                if len(parts) < 10:
                     continue
                 try:
-                    sm.append(float(parts[1]))
-                    mx = float(parts[2])
+                    ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+                    rows.append((ts, float(parts[2]), float(parts[3]),
+                                 {n for n, v in zip(names, parts[6:10]) if v.lower().startswith("active")}))
                 except ValueError:
                     continue
-                for n, v in zip(names, parts[5:9]):
-                    if v.lower().startswith("active"):
-                        reasons.add(n)
         os.unlink(self.path)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        inside = [r for r in rows if self.t0 and self.t1 and
+                  self.t0 - datetime.timedelta(milliseconds=50) <= r[0] <= self.t1 + datetime.timedelta(milliseconds=50)]
+        use = inside or rows
+        reasons = set().union(*[r[3] for r in use]) if use else set()
+        out = {"sm_mhz": statistics.median([r[1] for r in use]) if use else None,
+               "sm_max_mhz": use[-1][2] if use else None, "reasons": sorted(reasons), "samples": len(use)}
+        if rows and not inside:
+            out["note"] = "no sample fell inside the timed region; all samples of the run reported"
+        return out
 
 
 # ------------------------------------------------- algorithmic bytes ----
@@ -178,12 +200,15 @@ def run_ours(args, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     clocks.start()
     launches_before = st.launch_count()
+    torch.cuda.synchronize()
+    clocks.window(True)
     for s in range(args.steps):
         flush.fill_(float(s))                    # evict L2 (256 MB > 129 MB), outside the events
         starts[s].record()
         frame(args.warmup + s)                   # direct lighting overlaps the culls and the gather
         ends[s].record()
     torch.cuda.synchronize()
+    clocks.window(False)
     launches_timed = st.launch_count() - launches_before
     clock = clocks.stop()
     ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]

@@ -337,7 +337,8 @@ int64_t sgi_launch_count(const sgi_ctx* ctx);
  * threads, each evaluating SGI_LANE_CHECKS checks both ways on hashed
  * operands: 0-2 packed add, multiply, multiply-add; 3-5 the same on exact
  * rounding ties; 6 exp over its whole range; 7 x^128; 8 a pair of a-trous tap
- * weights; 9 their accumulation into the channel sums. counts[k] = threads
+ * weights; 9 their accumulation into the channel sums; 10-11 multiply-add
+ * with a subnormal multiplicand onto zero and onto normal sums. counts[k] = threads
  * whose check k differed; `first` (optional, SGI_LANE_CHECKS * 16 floats)
  * receives for each failing check the packed results, the scalar results and
  * the operands of one failing thread. Synchronous; uses the current device. */

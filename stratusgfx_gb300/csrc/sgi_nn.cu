@@ -832,20 +832,5 @@ cudaError_t features(const FeatureArgs& a, cudaStream_t s) {
 }
 
 // hdr = screen + gi * denoised, gi = RGB16F(max(albedo, 0.01) + 1e-5); history <- denoised
-__global__ void composite_kernel(const float4* __restrict__ den, const uint2* __restrict__ screen,
-                                 const uint32_t* __restrict__ albedo, uint2* __restrict__ hdr,
-                                 uint2* __restrict__ gi_out, uint16_t* __restrict__ hist_out, size_t P) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P) return;
-    const float4 d = den[i];
-    composite_px(d.x, d.y, d.z, screen, albedo, hdr, gi_out, hist_out, i);
-}
-
-cudaError_t composite(const float4* den, const uint2* screen, const uint32_t* albedo, uint2* hdr, uint2* gi_out,
-                      uint16_t* hist_out, size_t P, cudaStream_t s) {
-    composite_kernel<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(den, screen, albedo, hdr, gi_out, hist_out, P);
-    return cudaGetLastError();
-}
-
 }  // namespace nn
 }  // namespace sgi

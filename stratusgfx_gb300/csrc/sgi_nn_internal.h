@@ -103,8 +103,6 @@ struct FeatureArgs {
 };
 
 cudaError_t features(const FeatureArgs& a, cudaStream_t s);
-cudaError_t composite(const float4* den, const uint2* screen, const uint32_t* albedo, uint2* hdr, uint2* gi_out,
-                      uint16_t* hist_out, size_t P, cudaStream_t s);
 cudaError_t conv3x3(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t s);
 // The same convolution on the 5th-generation tensor cores (sgi_nn_tc.cu); *err is
 // set to 1 when a bounded wait of a block ran out.

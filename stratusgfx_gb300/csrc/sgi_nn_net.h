@@ -73,7 +73,7 @@ struct sgi_nn {
 // The two halves of sgi_nn_forward for one image (B = 1), for the frame path:
 // the U-Net, then the kernel apply with the frame's composite fused into it
 // (the HDR frame, the GI history and the history length are written instead
-// of the denoised GI; see sgi::nn::composite). The noisy GI is read from the
+// of the denoised GI; see composite_px in sgi_nn.cu). The noisy GI is read from the
 // RGBA16F pass-0 output the features were built from.
 sgi_status nn_forward_net(sgi_nn* n, const void* features, int H, int W, cudaStream_t s);
 sgi_status nn_apply_composite(sgi_nn* n, const uint2* noisy, const float* prev, int H, int W, const uint2* screen,

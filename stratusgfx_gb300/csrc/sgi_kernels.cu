@@ -942,7 +942,7 @@ SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __r
     rf0 = acc01.x; rf1 = acc01.y; rf2 = acc23.x; rf3 = acc23.y;
 }
 
-__global__ void __launch_bounds__(256) atrous_kernel(int W, int H, int step, const float4* __restrict__ guide,
+__global__ void __launch_bounds__(256, 5) atrous_kernel(int W, int H, int step, const float4* __restrict__ guide,
                                                      const uint2* __restrict__ res_in, uint2* __restrict__ res_out) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -965,7 +965,7 @@ cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guid
 
 // Final pass (final = true): the filter above, then temporal reprojection
 // (vpl_pbr_gi_denoise.fs:336-429) and the composite screen + gi * illumAvg (:431).
-__global__ void __launch_bounds__(256) denoise_final_kernel(DenoiseLaunch d) {
+__global__ void __launch_bounds__(256, 5) denoise_final_kernel(DenoiseLaunch d) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int W = d.width, H = d.height;

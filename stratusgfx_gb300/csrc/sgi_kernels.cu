@@ -533,7 +533,7 @@ SGI_D void bitonic_stage(uint32_t& k0, int& i0, uint32_t& k1, int& i1, int size,
 // block: keys[tile][k] in global memory (L2-resident), kNoKey when the VPL is
 // not a candidate. Reading the VPL records once per block instead of once per
 // tile cuts the L2 traffic of this pass by kKeyTiles.
-constexpr int kKeyTiles = 16;
+constexpr int kKeyTiles = 8;
 __global__ void __launch_bounds__(256) tile_keys_kernel(int num_tiles, int key_stride,
                                                         const sgi_tile_stage1* __restrict__ s1,
                                                         const sgi_vpl* __restrict__ cv,

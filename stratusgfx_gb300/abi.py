@@ -28,6 +28,7 @@ SGI_MAX_VPLS_BEFORE_CULL = 10000
 SGI_MAX_VPLS_PER_FRAME = 4480
 SGI_NUM_PASS_TIMES = 5
 SGI_LANE_CHECKS = 12
+SGI_NO_LIGHT = 0xFFFFFFFFFFFFFFFF
 
 SGI_DEBUG_VISIBLE_INDEX = 0
 SGI_DEBUG_COMPACT_VPLS = 1
@@ -149,6 +150,15 @@ EXPORTS = {
     "sgi_get_pass_times": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "sgi_launch_count": (C.c_int64, [C.c_void_p]),
     "sgi_lane_selftest": (C.c_int32, [C.c_int32, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
+    "sgi_slot_cache_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "sgi_slot_cache_destroy": (C.c_int32, [C.c_void_p]),
+    "sgi_slot_cache_get": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(AtlasEntry), C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_uint64)]),
+    "sgi_slot_cache_remove": (C.c_int32, [C.c_void_p, C.c_uint64]),
+    "sgi_slot_cache_find": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(AtlasEntry)]),
+    "sgi_slot_cache_capacity": (C.c_int32, [C.c_void_p]),
+    "sgi_slot_cache_free": (C.c_int32, [C.c_void_p]),
+    "sgi_slot_cache_used": (C.c_int32, [C.c_void_p]),
     "sgi_nn_create": (C.c_int32, [C.POINTER(NnConfig), C.POINTER(C.c_void_p)]),
     "sgi_nn_destroy": (C.c_int32, [C.c_void_p]),
     "sgi_nn_last_error": (C.c_char_p, [C.c_void_p]),

@@ -159,6 +159,8 @@ EXPORTS = {
     "sgi_slot_cache_capacity": (C.c_int32, [C.c_void_p]),
     "sgi_slot_cache_free": (C.c_int32, [C.c_void_p]),
     "sgi_slot_cache_used": (C.c_int32, [C.c_void_p]),
+    "sgi_prepare_vpls": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                     C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),
     "sgi_nn_create": (C.c_int32, [C.POINTER(NnConfig), C.POINTER(C.c_void_p)]),
     "sgi_nn_destroy": (C.c_int32, [C.c_void_p]),
     "sgi_nn_last_error": (C.c_char_p, [C.c_void_p]),

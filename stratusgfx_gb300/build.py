@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-Xcompiler", "-fPIC", "-I" + os.path.join(REPO, "include")]
 CUDA_SOURCES = ["sgi_kernels.cu", "sgi_scene.cu", "sgi_nn.cu", "sgi_nn_tc.cu", "sgi_selftest.cu"]
-HOST_SOURCES = ["sgi_api.cpp", "sgi_nn_api.cpp", "sgi_batch.cpp", "sgi_slots.cpp"]
+HOST_SOURCES = ["sgi_api.cpp", "sgi_nn_api.cpp", "sgi_batch.cpp", "sgi_slots.cpp", "sgi_host.cpp"]
 # The learned denoiser is checked against the oracle within a tolerance, not bit
 # for bit, so its kernels keep the compiler's default multiply-add contraction.
 FAST_MATH_OK = {"sgi_nn.cu", "sgi_nn_tc.cu"}
@@ -74,7 +74,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         o = os.path.join(OUT, src.replace(".cpp", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + _cuda_include(),
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off", "-I" + _cuda_include(),
                          "-I" + os.path.join(REPO, "include"), "-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         logs = list(ex.map(_run, jobs))

@@ -342,7 +342,7 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0:
         result.update(neural_vs_plain(args, ds, sc, w, cfg, flush))
     if rank == 0 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline_from_device(ds, sc, w, cfg)
+        result["parity"], result["cpu_baseline"] = parity_and_cpu_baseline(ds, sc, w, cfg)
     if rank == 0 and not args.no_uhd and w.name == S.HD.name:
         del ds
         result.update(uhd_comparison(args, flush))
@@ -413,36 +413,80 @@ def psnr_vs_converged(render, ds, sc, w, cfg, targets):
     return round(sum(full) / len(full), 2), round(sum(gi_only) / len(gi_only), 2)
 
 
-def cpu_baseline_from_device(ds, sc, w, cfg):
-    """FP32 oracle (CPU restatement of the reference shaders) on one full frame of the same workload,
-    on the inputs the GPU generated (copied to host); all host threads."""
+def _host_scene(ds, sc, w, frames):
+    """The oracle's view of the device-generated inputs (copied to host) for the listed frames."""
     from oracle import binding as O
-    hg = [O.HostGBuffer(w.height, w.width, g.numpy()) for g in ds.gbuffers[:3]]
-    hs = O.HostScene.__new__(O.HostScene)
-    hs.scene, hs.w = sc, w
-    hs.gbuffers = hg
-    hs.csm_depth = [ds.csm_depth[k].cpu().numpy() for k in range(3)]
-    from stratusgfx_gb300 import stage
-    hs.csms = [stage.csm_struct(sc, k, hs.csm_depth[k].ctypes.data, w.csm_resolution) for k in range(3)]
-    storage = ds.cube_storage.cpu().numpy()
-    if storage.dtype == np.int16:
-        storage = storage.view(np.uint16)
-    hs.cube_storage = storage
-    hs.cubes = O.cube_struct(storage, w.cube_format, sc.layers_per_atlas)
+    g = [None] * len(ds.gbuffers)
+    for k in frames:
+        g[k] = ds.gbuffers[k].numpy()
+    csm = {k: ds.csm_depth[k].cpu().numpy() for k in frames}
+    return O.HostScene.from_arrays(sc, w, g, csm, ds.cube_storage.cpu().numpy())
+
+
+def parity_and_cpu_baseline(ds, sc, w, cfg):
+    """Frames 1 and 2 of the workload (the second reading the first's history) through the FP32 oracle,
+    timed with all host threads (the CPU baseline), and through sgi_render_frame on a fresh context with
+    the same inputs and frame parameters: the visible list, every per-tile list and the HDR output are
+    compared, then frame 1 is compared with the FP64 oracle (PSNR)."""
+    import torch
+
+    from oracle import binding as O
+    from stratusgfx_gb300 import abi, stage
+    hs = _host_scene(ds, sc, w, (0, 1, 2))
     H, W = w.height, w.width
     gi = np.zeros((H, W, 4), np.float32)
     hist = np.zeros((H, W), np.float32)
+    refs = []
     t0 = time.perf_counter()
-    nf = 0
     for k in (1, 2):
         r = O.frame(32, cfg, hs, k, gi, hist, 1000.0 + 16.0 * k, 60.0)
         gi, hist = r["gi"], r["hist"]
-        nf += 1
+        refs.append(r)
     dt = time.perf_counter() - t0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": round(nf * W * H / dt / 1e6, 4), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{nf} full {W}x{H} frames of the same workload through the FP32 oracle (OpenMP), "
-                      f"{dt:.1f} s"}
+    cpu = {"value": round(len(refs) * W * H / dt / 1e6, 4), "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{len(refs)} full {W}x{H} frames of the same workload through the FP32 oracle (OpenMP), "
+                     f"{dt:.1f} s"}
+    st = stage.GiStage(cfg)
+    st.set_lights(ds.vpls, ds.entries, ds.points)
+    out = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+    L = cfg.max_vpls_per_tile
+    lists_ok = vis_ok = True
+    differ = 0
+    max_rel = 0.0
+    frame1 = None
+    for k, ref in zip((1, 2), refs):
+        st.set_shadow_maps(ds.csms[k], ds.cubes)
+        st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * k, 60.0)
+        torch.cuda.synchronize()
+        idx = st.read_debug(abi.SGI_DEBUG_VISIBLE_INDEX, np.int32)
+        cnt = ref["count"]
+        vis_ok &= bool(idx[0] == cnt and np.array_equal(idx[1:1 + cnt], ref["visible_index"][1:1 + cnt]))
+        lists = st.read_debug(abi.SGI_DEBUG_TILE_LISTS, np.int32).reshape(-1, 1 + L)
+        lists_ok &= bool(np.array_equal(lists, ref["lists"]))
+        got = out.cpu().numpy().astype(np.float32)[..., :3]
+        exp = ref["combined"][..., :3].astype(np.float32)
+        same = (got == exp) | (np.isnan(got) & np.isnan(exp))
+        differ += int((~same).sum())
+        ok = np.isfinite(got) & np.isfinite(exp)
+        rel = np.abs(got[ok].astype(np.float64) - exp[ok]) / np.maximum(np.abs(exp[ok]), 1e-6)
+        max_rel = max(max_rel, float(rel.max()) if rel.size else 0.0)
+        if k == 1:
+            frame1 = got.astype(np.float64)
+    st.close()
+    t1 = time.perf_counter()
+    r64 = O.frame(64, cfg, hs, 1, np.zeros((H, W, 4)), np.zeros((H, W)), 1016.0, 60.0)
+    t64 = time.perf_counter() - t1
+    ref64 = r64["combined"][..., :3]
+    mse = float(np.mean((frame1 - ref64) ** 2))
+    peak = float(np.max(np.abs(ref64)))
+    parity = {"workload": w.name, "frames": 2, "visible_lists_equal": vis_ok, "tile_lists_equal": lists_ok,
+              "tiles_per_frame": int(refs[0]["lists"].shape[0]), "hdr_bit_exact": differ == 0,
+              "hdr_values_differing": differ, "max_rel_err_vs_fp32_oracle": max_rel,
+              "psnr_vs_fp64_oracle_db": round(10.0 * np.log10(peak * peak / mse), 2) if mse > 0 else None,
+              "fp64_oracle_frame_s": round(t64, 2),
+              "oracle": "CPU restatement of the reference shaders (parity unpinned by the reference)"}
+    return parity, cpu
 
 
 def time_frames(render, ds, frames, steps, warmup, flush):
@@ -801,9 +845,25 @@ def neural_vs_plain(args, ds, sc, w, cfg, flush):
 
 
 # ---------------------------------------------------- reference arm ----
+def _mapped_libraries() -> list[str]:
+    """Shared objects of this repository mapped into the process (from /proc/self/maps)."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if len(line.split()) >= 6 else ""
+                if path.startswith(ROOT) and path.endswith(".so"):
+                    out.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(out)
+
+
 def run_reference(args):
     """The reference's path restated on the CPU (its GLSL needs an OpenGL driver, unavailable on this machine):
-    FP32 oracle with all host threads; inputs from the oracle's CPU ray caster."""
+    FP32 oracle with all host threads, inputs from the oracle's CPU ray caster, one full frame per step
+    and the same --steps / --warmup as the GPU arm. Nothing of the GPU library is loaded: the config
+    comes from abi.config_defaults (Python), and the arm checks its own mappings before printing."""
     from oracle import binding as O
     from stratusgfx_gb300 import stage
     from stratusgfx_gb300 import scene as S
@@ -817,8 +877,8 @@ def run_reference(args):
     frames = len(sc.cameras) - 1
     gi = np.zeros((H, W, 4), np.float32)
     hist = np.zeros((H, W), np.float32)
-    steps = max(1, min(args.steps, 6))
-    warm = max(0, min(args.warmup, 1))
+    steps = max(1, args.steps)
+    warm = max(0, args.warmup)
     for s in range(warm):
         k = s % frames + 1
         r = O.frame(32, cfg, hs, k, gi, hist, 1000.0 + 16.0 * s, 60.0)
@@ -831,15 +891,20 @@ def run_reference(args):
     dt = time.perf_counter() - t0
     value = steps * W * H / dt / 1e6
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    libs = _mapped_libraries()
+    if any("libsgi" in p for p in libs):
+        raise RuntimeError(f"the reference arm mapped the GPU library: {libs}")
     return {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warm,
             "ms_per_step": round(dt / steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
             "config": {"workload": w.name, "resolution": f"{W}x{H}", "gi_mode": "tiled",
-                       "samples_per_pixel": w.samples, "denoise_passes": w.denoise_passes},
+                       "samples_per_pixel": w.samples, "denoise_passes": w.denoise_passes,
+                       "vpls": w.num_vpls, "point_lights": w.num_points, "frames": frames},
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{steps} full frames (of --steps {args.steps}) through the FP32 CPU "
+                             "sample": f"{steps} full {W}x{H} frames (one per step) through the FP32 CPU "
                                        f"restatement of the reference shaders; input generation {gen_s:.1f} s "
                                        f"untimed"},
+            "native_libraries": libs,
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -899,6 +964,17 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: relaunch under torch.distributed.run with N local ranks
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+        sys.exit(subprocess.call(cmd))
+    if world != args.gpus:
+        sys.exit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE is {world}")
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)))

@@ -261,7 +261,10 @@ sgi_status sgi_cull_vpls(sgi_ctx* ctx, void* stream);
  * start at zero. Calls that overlap on one device (two streams, or two host
  * threads, with work in flight at the same time) share that array and race:
  * order them on one stream or with events. The first call on each device looks
- * up the array's address; make that call before any stream capture begins. */
+ * up the array's address (cudaGetSymbolAddress, no allocation) and keeps it for
+ * the life of the process; make that call before any stream capture begins. A
+ * cudaDeviceReset destroys the array with the context, so the kept address is
+ * stale after one: do not call this entry point again in that process. */
 #define SGI_NOALLOC_CULL_MAX_VPLS 16384
 sgi_status sgi_cull_vpls_noalloc(const sgi_vpl* vpls, const sgi_atlas_entry* entries, int32_t num_vpls,
                                  const sgi_csm* csm, int32_t max_visible, sgi_vpl* visible_vpls,

@@ -13,9 +13,13 @@
  * (sgi_set_vpl_coloring).
  *
  * Arithmetic, in binary32 with each operation rounded on its own:
- *   distance = sqrt(dx*dx + dy*dy + dz*dz), d = position - camera
+ *   distance = sqrt((dx*dx + dy*dy) + dz*dz), d = position - camera
  *   (glm::distance), and a sphere is outside when for some plane
- *   a*x + b*y + c*z + d*1 < -radius, the terms added left to right (glm::dot).
+ *   (a*x + b*y) + (c*z + d*1) < -radius: the four products added in pairs,
+ *   as glm::dot of two vec4 adds them (glm/detail/func_geometric.inl:64-70).
+ *
+ * Non-finite planes, camera, positions or radii return SGI_ERR_ARG (a NaN
+ * distance has no place in the distance order).
  */
 #ifndef SGI_HOST_H_
 #define SGI_HOST_H_

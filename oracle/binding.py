@@ -272,6 +272,28 @@ class HostScene:
         from stratusgfx_gb300 import stage
         return stage.camera_struct(self.scene, k)
 
+    @classmethod
+    def from_arrays(cls, scene, w, gbuffers, csm_depth, cube_storage):
+        """A HostScene over inputs made elsewhere (e.g. copied back from the device generator, which is
+        bit-identical to the CPU ray caster): gbuffers = dicts of G-buffer planes per frame, csm_depth =
+        {frame: float32 [4, R, R]}, cube_storage = the cube atlas array (uint16 or float32)."""
+        from stratusgfx_gb300 import stage
+        hs = cls.__new__(cls)
+        hs.scene, hs.w = scene, w
+        hs.gbuffers = [None if g is None else HostGBuffer(w.height, w.width, g) for g in gbuffers]
+        hs.csm_depth, hs.csms = {}, {}
+        for k, d in csm_depth.items():
+            hs.csm_depth[k] = np.ascontiguousarray(d, dtype=np.float32)
+            hs.csms[k] = stage.csm_struct(scene, k, hs.csm_depth[k].ctypes.data, w.csm_resolution)
+        hs.cube_storage = hs.cubes = None
+        if cube_storage is not None:     # not needed by the culls
+            storage = np.ascontiguousarray(cube_storage)
+            if storage.dtype == np.int16:
+                storage = storage.view(np.uint16)
+            hs.cube_storage = storage
+            hs.cubes = cube_struct(storage, w.cube_format, scene.layers_per_atlas)
+        return hs
+
 
 def frame(prec, cfg, hs: HostScene, k: int, gi_prev, hist_prev, time, fps, keep=False):
     """The whole stage for camera k (k >= 1; k - 1 is the previous frame), like sgi_render_frame.

@@ -5,7 +5,9 @@ checked against it.
 - UpdatePointLights_, VPL branch (Source/Engine/StratusRendererBackend.cpp:1357-1389):
   distance = glm::distance(camera, light) taken as a double key; a VPL is kept
   when IsSphereInFrustum (Source/Engine/StratusMath.h:401-412) holds, i.e. no
-  plane gives dot(plane, vec4(center, 1)) < -radius; keys go into a
+  plane gives dot(plane, vec4(center, 1)) < -radius, where glm's vec4 dot adds
+  the products in pairs, (x + y) + (z + w) (glm/detail/func_geometric.inl:64-70)
+  and its vec3 dot left to right, (x + y) + z (:54-60); keys go into a
   std::multiset ordered by distance (equal keys after the earlier ones), and
   the first MAX_TOTAL_VPLS_BEFORE_CULLING are taken.
 - InitVplFrameData_ (:1281-1292): position (x, y, z, 1), far plane, radius,
@@ -28,8 +30,7 @@ def prepare_vpls(pos, radii, far, inten, planes, cam, cap):
         c = pos[i]
         inside = True
         for g in planes:
-            d = f32(f32(f32(g[0] * c[0]) + f32(g[1] * c[1])) + f32(g[2] * c[2]))
-            d = f32(d + f32(g[3] * f32(1.0)))
+            d = f32(f32(f32(g[0] * c[0]) + f32(g[1] * c[1])) + f32(f32(g[2] * c[2]) + f32(g[3] * f32(1.0))))
             if d < -f32(radii[i]):
                 inside = False
                 break

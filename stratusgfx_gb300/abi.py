@@ -67,6 +67,32 @@ class Config(C.Structure):
                 ("point_light_ambient_intensity", C.c_float)]
 
 
+def config_defaults(width: int, height: int) -> Config:
+    """The values sgi_config_defaults writes (the reference's RendererSettings and
+    shader constants), stated in Python so that code which must not load libsgi.so
+    (the CPU reference arm of the benchmark) builds the same config; a test keeps
+    the two equal field by field."""
+    cfg = Config()
+    cfg.width, cfg.height = width, height
+    cfg.max_vpls = SGI_MAX_VPLS_BEFORE_CULL
+    cfg.max_visible = SGI_MAX_VPLS_PER_FRAME
+    cfg.tile_size = 16
+    cfg.max_vpls_per_tile = 12
+    cfg.gi_mode = SGI_GI_REFERENCE
+    cfg.samples_per_pixel = 0
+    cfg.denoise_passes = 4
+    cfg.debug_keep_passes = 0
+    cfg.min_roughness = 0.08
+    cfg.use_perceptual_roughness = 1
+    cfg.min_gi_occlusion_factor = 0.95
+    cfg.emission_strength = 0.0
+    cfg.fog_density = 0.0
+    for i in range(3):
+        cfg.fog_color[i] = 0.5
+    cfg.point_light_ambient_intensity = 0.003
+    return cfg
+
+
 class GBuffer(C.Structure):
     _fields_ = [("depth", C.c_void_p), ("normal", C.c_void_p), ("albedo", C.c_void_p),
                 ("base_reflectivity", C.c_void_p), ("roughness_metallic_ambient", C.c_void_p),

@@ -12,15 +12,24 @@
 
 namespace {
 
+// glm::dot of two vec4 forms the four products and adds them pairwise,
+// (x + y) + (z + w) (glm/detail/func_geometric.inl:64-70, compute_dot<tvec4>).
 bool sphere_in_frustum(const float* c, float radius, const float* planes) {
     for (int i = 0; i < 6; ++i) {
         const float* g = planes + 4 * i;
-        const float distance = g[0] * c[0] + g[1] * c[1] + g[2] * c[2] + g[3] * 1.0f;
+        const float distance = (g[0] * c[0] + g[1] * c[1]) + (g[2] * c[2] + g[3] * 1.0f);
         if (distance < -radius) return false;
     }
     return true;
 }
 
+bool all_finite(const float* v, size_t n) {
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+// glm::distance of two vec3: sqrt((x + y) + z) of the squared differences.
 float distance_to(const float* p, const float* cam) {
     const float dx = p[0] - cam[0], dy = p[1] - cam[1], dz = p[2] - cam[2];
     return std::sqrt(dx * dx + dy * dy + dz * dz);
@@ -36,6 +45,10 @@ extern "C" sgi_status sgi_prepare_vpls(const float* positions, const float* radi
     if (n > 0 && (!positions || !radii || !far_planes || !intensities)) return SGI_ERR_ARG;
     if (cap > 0 && !out) return SGI_ERR_ARG;
     *count = 0;
+    // A NaN distance would break the strict weak order the sort needs, and a NaN
+    // plane or radius makes the frustum test meaningless: such input is rejected.
+    if (!all_finite(planes, 24) || !all_finite(camera, 3)) return SGI_ERR_ARG;
+    if (n > 0 && (!all_finite(positions, 3 * (size_t)n) || !all_finite(radii, (size_t)n))) return SGI_ERR_ARG;
     struct Key {
         double distance;
         int32_t index;

@@ -33,9 +33,8 @@ def _stream_ptr(stream) -> C.c_void_p:
 
 
 def default_config(width: int, height: int, **kw) -> abi.Config:
-    lib = abi.load()
-    cfg = abi.Config()
-    lib.sgi_config_defaults(C.byref(cfg), width, height)
+    """sgi_config_defaults (as abi.config_defaults states it) with overrides."""
+    cfg = abi.config_defaults(width, height)
     for k, v in kw.items():
         if k == "fog_color":
             for i in range(3):

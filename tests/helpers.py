@@ -69,3 +69,15 @@ def upload_cubes(storage: np.ndarray, fmt: int, layers: int = 320, device="cuda"
 
 def half4_to_f32(buf: np.ndarray, H: int, W: int) -> np.ndarray:
     return buf.view(np.float16).reshape(H, W, 4).astype(np.float32)
+
+
+def host_scene_from_device(ds, frames, cubes=True):
+    """oracle HostScene over the device generator's inputs (bit-identical to the CPU ray caster) for
+    the listed frames: their G-buffers and CSMs, and the cube atlas unless cubes=False."""
+    from oracle import binding as O
+    g = [None] * len(ds.gbuffers)
+    for k in frames:
+        g[k] = ds.gbuffers[k].numpy()
+    csm = {k: ds.csm_depth[k].cpu().numpy() for k in frames}
+    storage = ds.cube_storage.cpu().numpy() if cubes else None
+    return O.HostScene.from_arrays(ds.scene, ds.w, g, csm, storage)

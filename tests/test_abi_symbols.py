@@ -47,6 +47,15 @@ def test_config_defaults_are_the_reference_settings():
     assert lib.sgi_abi_version() == 1
 
 
+def test_python_config_defaults_equal_the_library_defaults():
+    """abi.config_defaults (used where libsgi.so must not be loaded) writes the same bytes."""
+    lib = abi.load(build_if_missing=True)
+    for W, H in ((1920, 1080), (17, 9)):
+        cfg = abi.Config()
+        lib.sgi_config_defaults(C.byref(cfg), W, H)
+        assert bytes(cfg) == bytes(abi.config_defaults(W, H))
+
+
 def test_create_rejects_bad_configs_before_touching_the_device():
     lib = abi.load(build_if_missing=True)
     h = C.c_void_p()

@@ -81,3 +81,45 @@ def test_empty_and_bad_arguments():
     assert cnt.value == 0
     assert lib.sgi_prepare_vpls(None, None, None, None, 3, p(planes), p(cam), 4, None, None, C.byref(cnt)) == \
         abi.SGI_ERR_ARG
+
+
+def test_plane_products_are_added_in_pairs():
+    """A sphere on a plane boundary where the two addition orders disagree: the
+    products are -2, 0, -2^-23 and -2^-23. Added left to right they give -2 (the
+    last two additions round back to -2), added in pairs as glm's vec4 dot does,
+    (-2 + 0) + (-2^-23 - 2^-23) = -2 - 2^-22, which is below -radius = -2: the
+    reference culls this VPL."""
+    tiny = np.float32(2.0 ** -23)
+    planes = np.zeros((6, 4), np.float32)
+    planes[:, 3] = 1.0e6                       # five planes far away on the inner side
+    planes[0] = [1.0, 0.0, 1.0, -tiny]
+    pos = np.array([[-2.0, 0.0, -tiny], [-1.0, 0.0, 0.0]], np.float32)
+    radii = np.array([2.0, 2.0], np.float32)
+    far = np.ones(2, np.float32)
+    inten = np.ones(2, np.float32)
+    cam = np.zeros(3, np.float32)
+    seq = np.float32(np.float32(np.float32(-2.0) + np.float32(0.0)) + -tiny) + -tiny
+    assert seq == np.float32(-2.0)             # the left-to-right sum would keep it
+    got, src = run(pos, radii, far, inten, planes, cam, 8)
+    want, wsrc = prepare_vpls(pos, radii, far, inten, planes, cam, 8)
+    assert list(src) == [1] and list(wsrc) == [1]
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("what", ["position", "radius", "camera", "plane"])
+def test_non_finite_input_is_rejected(what):
+    lib = abi.load()
+    pos = np.zeros((3, 3), np.float32)
+    radii = np.ones(3, np.float32)
+    far = np.ones(3, np.float32)
+    inten = np.ones(3, np.float32)
+    planes = np.zeros((6, 4), np.float32)
+    planes[:, 3] = 1.0
+    cam = np.zeros(3, np.float32)
+    {"position": pos, "radius": radii, "camera": cam, "plane": planes}[what].flat[1] = np.nan
+    out = np.zeros((3, 16), np.float32)
+    cnt = C.c_int32(0)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)   # noqa: E731
+    assert lib.sgi_prepare_vpls(p(pos), p(radii), p(far), p(inten), 3, p(planes), p(cam), 3, p(out), None,
+                                C.byref(cnt)) == abi.SGI_ERR_ARG
+    assert cnt.value == 0

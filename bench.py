@@ -52,6 +52,8 @@ def parse():
                          "--warmup + --steps frames of sgi_render_frame only (no e2e or CPU legs)")
     ap.add_argument("--neural", action="store_true",
                     help="with --profile: frames of sgi_render_frame_neural (K = 2) instead")
+    ap.add_argument("--fast", action="store_true",
+                    help="with --profile: the shading kernels in their tolerance mode (SGI_SHADING_FAST)")
     ap.add_argument("--fp8", action="store_true",
                     help="with --profile --neural: FP8 E4M3 convolutions (calibrated on another room) at K = 1")
     return ap.parse_args()
@@ -133,29 +135,54 @@ class ClockSampler:
 
 
 # ------------------------------------------------- algorithmic bytes ----
-def pass_bytes(w, num_points: int) -> dict:
-    """Bytes each pass must move per launch (each input read once, each output written once)."""
+def kernel_bytes(w) -> dict:
+    """Bytes each kernel (group) must move per frame: each input read once, each output written once, in the
+    layouts these kernels use (the gather writes the per-pixel guide the later passes read)."""
     P = w.width * w.height
     cube = 2 if w.cube_format == 1 else 4
     # gather: depth, normal, albedo, rma (4 B each), reflectivity, ssao (2 B each), K cube texels;
     # writes the pass-0 reservoir (8 B) and the guide (16 B)
     gather = P * (4 + 4 + 4 + 4 + 2 + 2 + w.samples * cube + 8 + 16)
-    atrous = P * (8 + 16 + 8)
+    atrous = P * (8 + 16 + 8) * (w.denoise_passes - 2)
     # final: reservoir, guide, albedo, screen, velocity, id, prev depth/normal/id, prev GI, history in;
     # HDR, GI, history out
     final = P * (8 + 16 + 4 + 8 + 4 + 4 + 4 + 4 + 4 + 8 + 2 + 8 + 8 + 2)
-    denoise = atrous * (w.denoise_passes - 2) + final
     deferred = P * (4 + 4 + 4 + 4 + 2 + 2 + 8) + 4 * w.csm_resolution ** 2 * 4
     tiles = P * (4 + 4)
     vis = w.num_vpls * (64 + 8 + 4 + 1)
-    return {"vpl_cull": vis, "direct": deferred, "tile_cull": tiles, "gather": gather, "denoise": denoise}
+    return {"vpl_cull": vis, "deferred_pbr_csm": deferred, "tile_cull": tiles, "vpl_gather": gather,
+            "atrous": atrous, "denoise_final": final}
 
 
-PASS_NAMES = ["vpl_cull", "direct", "tile_cull", "gather", "denoise"]
+# kernel (group) -> index into sgi_get_pass_times with the denoise split, and the CUDA kernels it holds
+KERNELS = {"vpl_cull": (0, "vpl_vis_flags_kernel + vpl_compact_kernel"),
+           "deferred_pbr_csm": (1, "deferred_pbr_csm_kernel"),
+           "tile_cull": (2, "tile_stage1_kernel + tile_keys_kernel + tile_select_kernel"),
+           "vpl_gather": (3, "vpl_gather_kernel (gather + denoise pass 0 merge + guide)"),
+           "atrous": (5, "atrous_kernel x (denoise passes - 2)"),
+           "denoise_final": (6, "denoise_final_kernel")}
+
+
+def kernel_flops(fl: dict) -> dict:
+    """Algorithmic FLOPs per frame of each kernel (group) from the oracle's counting instantiation."""
+    return {"vpl_cull": fl["vpl_cull"][0], "deferred_pbr_csm": fl["direct"][0],
+            "tile_cull": fl["tile_stage1"][0] + fl["tile_stage2"][0],
+            "vpl_gather": fl["gather"][0] + fl["denoise_pass0"][0], "atrous": fl["atrous"][0],
+            "denoise_final": fl["denoise_final"][0]}
+
+
+def fp32_peak_tflops(sm_mhz) -> tuple[float, str]:
+    """FP32 rate of the GPU at the sampled SM clock: SMs x 128 FP32 lanes x 2 FLOP (FMA) per cycle."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = sm_mhz or 2070.0
+    return sms * 128 * 2 * mhz * 1e6 / 1e12, (f"nominal FP32 rate at the sampled SM clock: {sms} SMs x 128 lanes "
+                                               f"x 2 FLOP x {mhz:.0f} MHz")
 
 
 def traffic_from_profiles(kernel: str):
-    """dram bytes per launch recorded from an ncu capture in profiles/ (None if absent)."""
+    """DRAM bytes per frame of a kernel group (ncu dram__bytes_read.sum + dram__bytes_write.sum summed over its
+    launches in one frame) recorded in profiles/traffic.json (None if absent)."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
@@ -213,14 +240,44 @@ def run_ours(args, rank, world, local_rank):
     clock = clocks.stop()
     ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     # per-pass breakdown: the same frames with per-pass events (the passes then run in sequence)
-    st.set_timing(True)
-    pass_ms = np.zeros(len(PASS_NAMES))
+    def per_pass(stage_obj, render):
+        stage_obj.set_timing(True)
+        acc = np.zeros(7)
+        for s in range(args.steps):
+            flush.fill_(float(s))
+            render(args.warmup + s)
+            acc += np.array(stage_obj.pass_times(split=True))   # synchronises on the frame's last event
+        stage_obj.set_timing(False)
+        torch.cuda.synchronize()
+        return acc
+
+    pass_ms = per_pass(st, frame)
+
+    # ---- the same frames in the tolerance mode of the shading kernels (SGI_SHADING_FAST)
+    stf = stage.GiStage(cfg)
+    abi.check(stf.lib.sgi_set_shading_precision(stf.ctx, abi.SGI_SHADING_FAST), stf.ctx)
+    stf.set_lights(ds.vpls, ds.entries, ds.points)
+
+    def frame_fast(step):
+        k = step % frames + 1
+        stf.set_shadow_maps(ds.csms[k], ds.cubes)
+        stf.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * step, fps)
+
+    for s in range(args.warmup):
+        frame_fast(s)
+    torch.cuda.synchronize()
+    fast_ms = 0.0
     for s in range(args.steps):
         flush.fill_(float(s))
-        frame(args.warmup + s)
-        pass_ms += np.array(st.pass_times())     # synchronises on the frame's last event
-    st.set_timing(False)
-    torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        frame_fast(args.warmup + s)
+        e1.record()
+        torch.cuda.synchronize()
+        fast_ms += e0.elapsed_time(e1)
+    fast_ms /= args.steps
+    fast_pass_ms = per_pass(stf, frame_fast)
+    stf.close()
     total_ms = replicas.max_over_ranks(float(sum(ms)), device="cuda")
     ms_per_step = total_ms / args.steps
     value = replicas.job_throughput(P * args.steps, world, total_ms) / 1e6
@@ -301,7 +358,12 @@ def run_ours(args, rank, world, local_rank):
     e2e_ms = replicas.max_over_ranks(e0.elapsed_time(e1), device="cuda")
     e2e_value = replicas.job_throughput(P * args.steps, world, e2e_ms) / 1e6
 
-    # ---- roofline of the dominant pass
+    # ---- per-kernel roofline: algorithmic bytes against HBM, algorithmic FLOPs against the FP32 rate
+    parity = cpu = None
+    flops = None
+    if rank == 0 and not args.no_cpu_baseline:
+        parity, cpu, fl = parity_and_cpu_baseline(ds, sc, w, cfg)
+        flops = kernel_flops(fl)
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -310,16 +372,44 @@ def run_ours(args, rank, world, local_rank):
         pass
     hbm_peak = peaks.get("hbm_gbs") or 6800.0
     peak_src = "measured" if peaks.get("hbm_gbs") else "fallback"
-    pb = pass_bytes(w, len(sc.points))
-    per_pass = {}
-    for i, name in enumerate(PASS_NAMES):
-        avg = pass_ms[i] / args.steps
-        gbs = pb[name] / (avg / 1e3) / 1e9 if avg > 0 else 0.0
-        per_pass[name] = {"ms": round(avg, 4), "alg_bytes": pb[name], "gbs": round(gbs, 1),
-                          "frac_hbm": round(gbs / hbm_peak, 4)}
-    dom = max(PASS_NAMES, key=lambda n: per_pass[n]["ms"])
-    roof = {"bound": "hbm", "kernel": dom, "achieved": per_pass[dom]["gbs"], "peak": hbm_peak, "unit": "GB/s",
-            "frac": per_pass[dom]["frac_hbm"], "traffic": traffic_from_profiles(dom), "peak_source": peak_src}
+    fp32_peak, fp32_src = fp32_peak_tflops(clock.get("sm_mhz"))
+    kb = kernel_bytes(w)
+
+    def kernel_table(pms):
+        table = {}
+        for name, (idx, what) in KERNELS.items():
+            avg = pms[idx] / args.steps
+            gbs = kb[name] / (avg / 1e3) / 1e9 if avg > 0 else 0.0
+            k = {"kernels": what, "ms": round(avg, 4), "alg_bytes": kb[name], "gbs": round(gbs, 1),
+                 "frac_hbm": round(gbs / hbm_peak, 4)}
+            if flops is not None:
+                tf = flops[name] / (avg / 1e3) / 1e12 if avg > 0 else 0.0
+                k.update({"alg_flops": int(flops[name]), "tflops": round(tf, 2),
+                          "frac_fp32": round(tf / fp32_peak, 4)})
+                k["bound"] = "fp32" if k["frac_fp32"] > k["frac_hbm"] else "hbm"
+            else:
+                k["bound"] = "hbm"
+            table[name] = k
+        return table
+
+    kernels = kernel_table(pass_ms)
+    fast = {"shading": "SGI_SHADING_FAST (approximate division, square root and exponential, contraction; "
+                       "decisions and texel choices correctly rounded)",
+            "ms_per_frame": round(fast_ms, 4), "mpix_s": round(P / fast_ms / 1e3, 1),
+            "speedup_vs_exact": round(ms_per_step / fast_ms, 3), "kernels": kernel_table(fast_pass_ms)}
+    dom = max(kernels, key=lambda n: kernels[n]["ms"])
+    dk = kernels[dom]
+    if dk["bound"] == "fp32":
+        roof = {"bound": "fp32", "kernel": dom, "achieved": dk["tflops"], "peak": round(fp32_peak, 1),
+                "unit": "TFLOP/s", "frac": dk["frac_fp32"], "peak_source": fp32_src,
+                "alg_flops_per_launch": dk["alg_flops"], "frac_hbm": dk["frac_hbm"]}
+    else:
+        roof = {"bound": "hbm", "kernel": dom, "achieved": dk["gbs"], "peak": hbm_peak, "unit": "GB/s",
+                "frac": dk["frac_hbm"], "peak_source": peak_src}
+    roof["alg_bytes_per_launch"] = dk["alg_bytes"]
+    roof["traffic"] = traffic_from_profiles(dom)
+    roof["hbm_peak_gbs"] = hbm_peak
+    roof["hbm_peak_source"] = peak_src
 
     result = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -336,13 +426,14 @@ def run_ours(args, rank, world, local_rank):
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms / args.steps, 4)},
         "gpu_launches": int(launches_timed),
         "roofline": roof,
-        "passes": per_pass,
+        "kernels": kernels,
+        "fast": fast,
         "clocks": clock,
     }
     if rank == 0:
         result.update(neural_vs_plain(args, ds, sc, w, cfg, flush))
-    if rank == 0 and not args.no_cpu_baseline:
-        result["parity"], result["cpu_baseline"] = parity_and_cpu_baseline(ds, sc, w, cfg)
+    if parity is not None:
+        result["parity"], result["cpu_baseline"] = parity, cpu
     if rank == 0 and not args.no_uhd and w.name == S.HD.name:
         del ds
         result.update(uhd_comparison(args, flush))
@@ -427,7 +518,8 @@ def parity_and_cpu_baseline(ds, sc, w, cfg):
     """Frames 1 and 2 of the workload (the second reading the first's history) through the FP32 oracle,
     timed with all host threads (the CPU baseline), and through sgi_render_frame on a fresh context with
     the same inputs and frame parameters: the visible list, every per-tile list and the HDR output are
-    compared, then frame 1 is compared with the FP64 oracle (PSNR)."""
+    compared, then frame 1 is compared with the FP64 oracle (PSNR). Frame 1 also runs through the oracle's
+    operation-counting instantiation for the algorithmic FLOPs of each kernel."""
     import torch
 
     from oracle import binding as O
@@ -474,19 +566,52 @@ def parity_and_cpu_baseline(ds, sc, w, cfg):
         if k == 1:
             frame1 = got.astype(np.float64)
     st.close()
+    # the tolerance mode on the same two frames: identical lists, radiance within tolerance of the oracle
+    stf = stage.GiStage(cfg)
+    abi.check(stf.lib.sgi_set_shading_precision(stf.ctx, abi.SGI_SHADING_FAST), stf.ctx)
+    stf.set_lights(ds.vpls, ds.entries, ds.points)
+    f_lists_ok = True
+    f_max_rel = 0.0
+    f_over = 0
+    fast1 = None
+    for k, ref in zip((1, 2), refs):
+        stf.set_shadow_maps(ds.csms[k], ds.cubes)
+        stf.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * k, 60.0)
+        torch.cuda.synchronize()
+        lists = stf.read_debug(abi.SGI_DEBUG_TILE_LISTS, np.int32).reshape(-1, 1 + L)
+        f_lists_ok &= bool(np.array_equal(lists, ref["lists"]))
+        got = out.cpu().numpy().astype(np.float64)[..., :3]
+        exp = ref["combined"][..., :3].astype(np.float64)
+        rel = np.abs(got - exp) / np.maximum(np.abs(exp), 2.0 ** -14)
+        rel[np.isnan(got) & np.isnan(exp)] = 0.0
+        f_max_rel = max(f_max_rel, float(np.nanmax(rel)))
+        f_over += int((rel.max(axis=2) > 1e-3).sum())
+        if k == 1:
+            fast1 = got
+    stf.close()
     t1 = time.perf_counter()
     r64 = O.frame(64, cfg, hs, 1, np.zeros((H, W, 4)), np.zeros((H, W)), 1016.0, 60.0)
     t64 = time.perf_counter() - t1
     ref64 = r64["combined"][..., :3]
     mse = float(np.mean((frame1 - ref64) ** 2))
     peak = float(np.max(np.abs(ref64)))
+    t2 = time.perf_counter()
+    fl = O.frame_flops(cfg, hs, 1, np.zeros((H, W, 4), np.float32), np.zeros((H, W), np.float32), 1016.0, 60.0)
+    t_count = time.perf_counter() - t2
     parity = {"workload": w.name, "frames": 2, "visible_lists_equal": vis_ok, "tile_lists_equal": lists_ok,
               "tiles_per_frame": int(refs[0]["lists"].shape[0]), "hdr_bit_exact": differ == 0,
               "hdr_values_differing": differ, "max_rel_err_vs_fp32_oracle": max_rel,
               "psnr_vs_fp64_oracle_db": round(10.0 * np.log10(peak * peak / mse), 2) if mse > 0 else None,
               "fp64_oracle_frame_s": round(t64, 2),
-              "oracle": "CPU restatement of the reference shaders (parity unpinned by the reference)"}
-    return parity, cpu
+              "oracle": "CPU restatement of the reference shaders (parity unpinned by the reference)",
+              "fast": {"tile_lists_equal": f_lists_ok,
+                       "max_rel_err_vs_fp32_oracle": f_max_rel,
+                       "pixels_over_1e-3": f_over, "pixels": 2 * H * W,
+                       "rel_err": "|gpu - oracle| / max(|oracle|, 2^-14) over the HDR frame after all passes",
+                       "psnr_vs_fp64_oracle_db": round(10.0 * np.log10(peak * peak /
+                                                                       float(np.mean((fast1 - ref64) ** 2))), 2)},
+              "flop_count_s": round(t_count, 2)}
+    return parity, cpu, fl
 
 
 def time_frames(render, ds, frames, steps, warmup, flush):
@@ -920,6 +1045,9 @@ def run_profile(args):
     ds = stage.DeviceScene(sc, w)
     spp = (1 if args.fp8 else 2) if args.neural else None
     st = stage.GiStage(stage.workload_config(w, samples_per_pixel=spp) if spp else stage.workload_config(w))
+    if args.fast:
+        from stratusgfx_gb300 import abi
+        abi.check(st.lib.sgi_set_shading_precision(st.ctx, abi.SGI_SHADING_FAST), st.ctx)
     st.set_lights(ds.vpls, ds.entries, ds.points)
     out = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
     net = None
@@ -948,7 +1076,8 @@ def run_profile(args):
     torch.cuda.synchronize()
     if net is not None:
         net.close()
-    print(json.dumps({"profile_case": w.name + ("_neural_fp8_k1" if args.fp8 else "_neural_k2" if net else ""),
+    print(json.dumps({"profile_case": w.name + ("_neural_fp8_k1" if args.fp8 else "_neural_k2" if net else "") +
+                      ("_fast" if args.fast else ""),
                       "frames": args.warmup + args.steps,
                       "launches_per_frame": st.launch_count() // (args.warmup + args.steps)}))
     st.close()

@@ -325,9 +325,28 @@ sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream);
 #define SGI_DEBUG_PASS_BASE      16  /* + k: RGBA16F [W*H] reservoir output of denoise pass k */
 sgi_status sgi_read_debug(sgi_ctx* ctx, int32_t which, void* host_dst, size_t bytes, size_t* needed);
 
+/* Arithmetic of the shading kernels (gather, denoise, deferred lighting) of a
+ * context; no counterpart in StratusGFX, whose GLSL leaves the precision of
+ * division, sqrt, exp and multiply-add fusion to the driver.
+ *   SGI_SHADING_EXACT (default): correctly rounded operations in a fixed order,
+ *     bit-identical to the CPU restatement of the shaders.
+ *   SGI_SHADING_FAST: the same expressions with approximate division and square
+ *     root, hardware reciprocal square root and exponential and multiply-add
+ *     contraction. Each pass stays within 1e-3 relative error of the exact one
+ *     (denominator at least 2^-14, the smallest normal binary16) wherever no
+ *     branch decision of the pass lies within its decision margin; the VPL and
+ *     tile culls are exact in both modes, so the per-tile lists are identical. */
+#define SGI_SHADING_EXACT 0
+#define SGI_SHADING_FAST  1
+sgi_status sgi_set_shading_precision(sgi_ctx* ctx, int32_t mode);
+int32_t    sgi_get_shading_precision(const sgi_ctx* ctx);
+
 /* Per-pass GPU times (ms) of the last sgi_render_frame when timing is on:
- * [0] vpl cull, [1] direct lighting, [2] tile cull, [3] gather, [4] denoise. */
+ * [0] vpl cull, [1] direct lighting, [2] tile cull, [3] gather, [4] denoise;
+ * with n >= 7 also the denoise pass split into [5] its a-trous passes and
+ * [6] its final pass (temporal reprojection and composite). */
 #define SGI_NUM_PASS_TIMES 5
+#define SGI_NUM_PASS_TIMES_SPLIT 7
 sgi_status sgi_set_timing(sgi_ctx* ctx, int32_t enabled);
 sgi_status sgi_get_pass_times(sgi_ctx* ctx, float* ms, int32_t n);
 

@@ -51,7 +51,13 @@ def load() -> C.CDLL:
             "oracle_gi_target": (None, [C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.Camera), P, P,
                                         C.c_int, P, C.POINTER(abi.CubeAtlas), C.c_float, C.c_int, P]),
             "oracle_denoise": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.GBuffer),
-                                      P, P, P, P, C.c_int, C.POINTER(abi.FrameParams), P, P, P, P]),
+                                      P, P, P, P, C.c_int, C.POINTER(abi.FrameParams), P, P, P, P, P]),
+            "oracle_count_reset": (None, []),
+            "oracle_set_margin_output": (None, [P]),
+            "oracle_denoise_pass": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer),
+                                           C.POINTER(abi.GBuffer), C.c_int, P, P, P, P, C.c_int,
+                                           C.POINTER(abi.FrameParams), P, P, P, P]),
+            "oracle_count_read": (None, [P]),
             "oracle_deferred": (None, [C.c_int, C.POINTER(abi.Config), C.POINTER(abi.GBuffer), C.POINTER(abi.Camera),
                                        P, C.c_int, C.POINTER(abi.Csm), P, P, P, C.c_int, C.POINTER(abi.CubeAtlas)]),
             "oracle_scene_gbuffer": (None, [P, C.c_int, C.POINTER(abi.SceneCamera), C.c_int, C.c_int, P, P, P, P, P,
@@ -72,7 +78,43 @@ def load() -> C.CDLL:
 
 
 def _dt(prec):
-    return np.float32 if prec == 32 else np.float64
+    """Buffer dtype of an instantiation: 32 float, 64 double, 0 the counting float instantiation,
+    1 the margin-tracking double instantiation."""
+    return np.float64 if prec in (64, 1) else np.float32
+
+
+class margins:
+    """Context manager: prec = 1 passes run inside it write each pixel's smallest decision margins
+    (see oracle/counted.hpp, Tracked) into self.m ([H, W, 2] float64: comparisons, texel choices)."""
+
+    def __init__(self, H, W):
+        self.m = np.full((H, W, 2), np.inf)
+
+    def __enter__(self):
+        load().oracle_set_margin_output(_p(self.m))
+        return self
+
+    def __exit__(self, *exc):
+        load().oracle_set_margin_output(None)
+        return False
+
+
+def denoise_pass(prec, cfg, cur: HostGBuffer, prev: HostGBuffer, pass_index, res_in, hdr_in, gi_prev, hist_prev,
+                 num_visible, time, fps):
+    """One denoise pass from res_in: returns (res_out, combined, gi, hist) (the last three only filled on
+    the final pass)."""
+    H, W = cfg.height, cfg.width
+    dt = _dt(prec)
+    keep = [np.ascontiguousarray(a, dtype=dt) for a in (res_in, hdr_in, gi_prev, hist_prev)]
+    res_out = np.zeros((H, W, 4), dt)
+    comb = np.zeros((H, W, 4), dt)
+    gi = np.zeros((H, W, 4), dt)
+    hist = np.zeros((H, W), dt)
+    fp = abi.FrameParams(time, fps)
+    load().oracle_denoise_pass(prec, C.byref(cfg), C.byref(cur.struct()), C.byref(prev.struct()), pass_index,
+                               *[_p(a) for a in keep], num_visible, C.byref(fp), _p(res_out), _p(comb), _p(gi),
+                               _p(hist))
+    return res_out, comb, gi, hist
 
 
 class HostGBuffer:
@@ -219,7 +261,7 @@ def gi_target(cfg, g: HostGBuffer, cam, cvpls, centries, count, lists, cubes: ab
 
 
 def denoise(prec, cfg, cur: HostGBuffer, prev: HostGBuffer, reservoir, hdr_in, gi_prev, hist_prev, num_visible,
-            time, fps, keep_passes=False):
+            time, fps, keep_passes=False, pass_flops=None):
     H, W = cfg.height, cfg.width
     dt = _dt(prec)
     comb = np.zeros((H, W, 4), dt)
@@ -229,8 +271,60 @@ def denoise(prec, cfg, cur: HostGBuffer, prev: HostGBuffer, reservoir, hdr_in, g
     keep = [np.ascontiguousarray(a, dtype=dt) for a in (reservoir, hdr_in, gi_prev, hist_prev)]
     fp = abi.FrameParams(time, fps)
     load().oracle_denoise(prec, C.byref(cfg), C.byref(cur.struct()), C.byref(prev.struct()),
-                          *[_p(a) for a in keep], num_visible, C.byref(fp), _p(comb), _p(gi), _p(hist), _p(passes))
+                          *[_p(a) for a in keep], num_visible, C.byref(fp), _p(comb), _p(gi), _p(hist), _p(passes),
+                          _p(pass_flops))
     return comb, gi, hist, passes
+
+
+def count_reset():
+    load().oracle_count_reset()
+
+
+def count_read():
+    """(flops, cmps) tallied by prec = 0 calls since the last count_reset."""
+    out = np.zeros(2, np.uint64)
+    load().oracle_count_read(_p(out))
+    return int(out[0]), int(out[1])
+
+
+def frame_flops(cfg, hs: "HostScene", k: int, gi_prev, hist_prev, time, fps):
+    """Algorithmic FLOPs (and comparisons) of each pass of frame k, from the counting instantiation
+    (the same values as the FP32 oracle). Keys follow the CUDA kernels: vpl_cull, tile_stage1,
+    tile_stage2, gather (the sample loop), denoise_pass0 (the merge, fused into the gather kernel),
+    atrous (passes 1 .. n-2 together), denoise_final, direct. Each entry is (flops, cmps)."""
+    sc = hs.scene
+    cam = hs.camera(k)
+    csm = hs.csms[k]
+    out = {}
+
+    def run(name, fn):
+        count_reset()
+        r = fn()
+        out[name] = count_read()
+        return r
+
+    idx = run("vpl_cull", lambda: vis_cull(0, sc.vpls, csm, cfg.max_visible))
+    count = int(idx[0])
+    order = idx[1:1 + count]
+    cv = np.ascontiguousarray(sc.vpls[order])
+    ce = np.ascontiguousarray(sc.entries[order])
+    direct = run("direct", lambda: deferred(0, cfg, hs.gbuffers[k], cam, sc.points if len(sc.points) else None, csm))
+    lists = None
+    if cfg.gi_mode == abi.SGI_GI_TILED:
+        s1 = run("tile_stage1", lambda: tile_stage1(0, cfg, hs.gbuffers[k], cam))
+        lists = run("tile_stage2", lambda: tile_stage2(0, cfg, s1, cv, count))
+    res = run("gather", lambda: gather(0, cfg, hs.gbuffers[k], cam, cv, ce, count, lists, hs.cubes, time))
+    n = cfg.denoise_passes
+    pf = np.zeros(n, np.uint64)
+    count_reset()
+    denoise(0, cfg, hs.gbuffers[k], hs.gbuffers[k - 1], res, direct, gi_prev, hist_prev, count, time, fps,
+            pass_flops=pf)
+    cum = [0] + [int(v) for v in pf]
+    per = [cum[i + 1] - cum[i] for i in range(n)]
+    out["denoise_pass0"] = (per[0], None)
+    out["atrous"] = (sum(per[1:n - 1]), None)
+    out["denoise_final"] = (per[n - 1], None)
+    return out
 
 
 def deferred(prec, cfg, g: HostGBuffer, cam, points, csm: abi.Csm, casters=None, caster_entries=None,

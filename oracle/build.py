@@ -14,8 +14,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liboracle.so")
 SOURCES = ["oracle_api.cpp"]
-DEPS = SOURCES + ["glsl.hpp", "passes.hpp", "../include/sgi.h", "../include/sgi_scene.h"]
-FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-Wall"]
+DEPS = SOURCES + ["glsl.hpp", "counted.hpp", "passes.hpp", "../include/sgi.h", "../include/sgi_scene.h"]
+# -fno-strict-aliasing: the operation-counting instantiation reads and writes float32
+# buffers through its one-float wrapper type.
+FLAGS = ["-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fno-strict-aliasing", "-fPIC",
+         "-shared", "-Wall"]
 
 
 def build(force: bool = False) -> str:

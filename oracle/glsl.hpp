@@ -47,6 +47,7 @@ template <class T> inline T gclamp(T x, T lo, T hi) { return gmin(gmax(x, lo), h
 template <class T> inline T saturate(T x) { return gclamp(x, T(0), T(1)); }   // common.glsl:99-101
 template <class T> inline T mix(T x, T y, T a) { return gfma(y, a, x * (T(1) - a)); }
 template <class T> inline T gabs(T x) { return x < T(0) ? -x : x; }
+template <class T> inline T gfloor(T x) { return std::floor(x); }
 
 // exp for binary32 (see header comment). Returns exactly 1 for +-0.
 inline float exp_f32(float x) {

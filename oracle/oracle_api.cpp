@@ -9,7 +9,11 @@
 // StratusGFX, and its GLSL cannot run without an OpenGL driver).
 //
 // prec selects the instantiation: 32 -> float (buffers are float32),
-// 64 -> double (buffers are float64).
+// 64 -> double (buffers are float64), 0 -> Counted (float32 buffers; the same
+// values as 32, with the operations tallied, see counted.hpp) for the passes
+// that report algorithmic FLOPs, 1 -> Tracked (float64 buffers; the values of
+// 64, plus each pixel's smallest decision margin written to the buffer given
+// to oracle_set_margin_output) for the gather, denoise and deferred passes.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -17,6 +21,7 @@
 #include "../include/sgi.h"
 #include "../include/sgi_scene.h"
 #include "glsl.hpp"
+#include "counted.hpp"
 #include "passes.hpp"
 
 using namespace oracle;
@@ -24,6 +29,14 @@ using namespace oracle;
 extern "C" {
 
 int oracle_version(void) { return 1; }
+
+// ---- operation tallies of the prec = 0 instantiation -----------------------
+void oracle_count_reset(void) { tally_reset(); }
+void oracle_count_read(uint64_t* out2) { tally_read(&out2[0], &out2[1]); }
+
+// ---- decision margins of the prec = 1 instantiation ---------------------------
+// margins: [H][W][2] float64 (comparison, texel-choice margins), or NULL to stop recording.
+void oracle_set_margin_output(double* margins) { set_margin_output(margins); }
 
 // ---- known-answer helpers ---------------------------------------------------
 float oracle_random3(float x, float y, float z) { return random3(x, y, z); }
@@ -77,6 +90,7 @@ void oracle_infinite_shadow(int prec, const sgi_csm* csm, const double* pts, con
 
 // ---- passes ------------------------------------------------------------------
 int oracle_vis_cull(int prec, const sgi_vpl* vpls, int n, const sgi_csm* csm, int cap, int32_t* visible_index) {
+    if (prec == 0) return vis_cull<Counted>(vpls, n, *csm, cap, visible_index);
     return prec == 32 ? vis_cull<float>(vpls, n, *csm, cap, visible_index)
                       : vis_cull<double>(vpls, n, *csm, cap, visible_index);
 }
@@ -96,13 +110,15 @@ void oracle_post_fx(int prec, int W, int H, const float* hdr, const uint32_t* ve
 }
 
 void oracle_tile_stage1(int prec, const sgi_config* cfg, const sgi_gbuffer* g, const sgi_camera* cam, void* out) {
-    if (prec == 32) tile_stage1<float>(*cfg, *g, *cam, (float*)out);
+    if (prec == 0) tile_stage1<Counted>(*cfg, *g, *cam, (Counted*)out);
+    else if (prec == 32) tile_stage1<float>(*cfg, *g, *cam, (float*)out);
     else tile_stage1<double>(*cfg, *g, *cam, (double*)out);
 }
 
 void oracle_tile_stage2(int prec, const sgi_config* cfg, const void* stage1, const sgi_vpl* cv, int count,
                         int32_t* lists) {
-    if (prec == 32) tile_stage2<float>(*cfg, (const float*)stage1, cv, count, lists);
+    if (prec == 0) tile_stage2<Counted>(*cfg, (const Counted*)stage1, cv, count, lists);
+    else if (prec == 32) tile_stage2<float>(*cfg, (const float*)stage1, cv, count, lists);
     else tile_stage2<double>(*cfg, (const double*)stage1, cv, count, lists);
 }
 
@@ -110,7 +126,9 @@ void oracle_gather(int prec, const sgi_config* cfg, const sgi_gbuffer* g, const 
                    const sgi_atlas_entry* ce, int count, const int32_t* lists, const sgi_cube_atlas* cubes, float time,
                    void* reservoir) {
     GatherArgs a{cfg, g, cam, cv, ce, count, lists, cubes, time};
-    if (prec == 32) gather<float>(a, (float*)reservoir);
+    if (prec == 0) gather<Counted>(a, (Counted*)reservoir);
+    else if (prec == 1) gather<Tracked>(a, (Tracked*)reservoir);
+    else if (prec == 32) gather<float>(a, (float*)reservoir);
     else gather<double>(a, (double*)reservoir);
 }
 
@@ -121,12 +139,27 @@ void oracle_gi_target(const sgi_config* cfg, const sgi_gbuffer* g, const sgi_cam
     gi_target(a, batches, out);
 }
 
+// Cumulative tallied FLOPs after each denoise pass of a prec = 0 run.
+static uint64_t* g_pass_flops = nullptr;
+static void record_pass_flops(int pass) {
+    uint64_t f, c;
+    tally_read(&f, &c);
+    g_pass_flops[pass] = f;
+}
+
 // hdr_in, gi_prev: [P][4]; hist_prev: [P]; all buffers of the precision's type.
+// pass_flops (prec = 0 only, may be NULL): [denoise_passes] tallied FLOPs after each pass.
 void oracle_denoise(int prec, const sgi_config* cfg, const sgi_gbuffer* cur, const sgi_gbuffer* prev,
                     const void* reservoir, const void* hdr_in, const void* gi_prev, const void* hist_prev,
                     int num_visible, const sgi_frame_params* params, void* combined, void* gi_out, void* hist_out,
-                    void* pass_out) {
-    if (prec == 32) {
+                    void* pass_out, uint64_t* pass_flops) {
+    g_pass_flops = pass_flops;
+    if (prec == 0) {
+        DenoiseArgs<Counted> a{cfg, cur, prev, (const Counted*)hdr_in, (const Counted*)gi_prev,
+                               (const Counted*)hist_prev, num_visible, params->time, params->frames_per_second};
+        denoise<Counted>(a, (const Counted*)reservoir, (Counted*)combined, (Counted*)gi_out, (Counted*)hist_out,
+                         (Counted*)pass_out, pass_flops ? record_pass_flops : nullptr);
+    } else if (prec == 32) {
         DenoiseArgs<float> a{cfg, cur, prev, (const float*)hdr_in, (const float*)gi_prev, (const float*)hist_prev,
                              num_visible, params->time, params->frames_per_second};
         denoise<float>(a, (const float*)reservoir, (float*)combined, (float*)gi_out, (float*)hist_out, (float*)pass_out);
@@ -138,13 +171,32 @@ void oracle_denoise(int prec, const sgi_config* cfg, const sgi_gbuffer* cur, con
     }
 }
 
+// One denoise pass `pass` from the reservoir res_in (prec 32, 64 or 1); the final
+// pass also writes combined, gi_out and hist_out. Buffers as for oracle_denoise.
+void oracle_denoise_pass(int prec, const sgi_config* cfg, const sgi_gbuffer* cur, const sgi_gbuffer* prev, int pass,
+                         const void* res_in, const void* hdr_in, const void* gi_prev, const void* hist_prev,
+                         int num_visible, const sgi_frame_params* params, void* res_out, void* combined,
+                         void* gi_out, void* hist_out) {
+    auto run = [&](auto zero) {
+        using T = decltype(zero);
+        DenoiseArgs<T> a{cfg, cur, prev, (const T*)hdr_in, (const T*)gi_prev, (const T*)hist_prev, num_visible,
+                         params->time, params->frames_per_second};
+        denoise_one_pass<T>(a, pass, (const T*)res_in, (T*)res_out, (T*)combined, (T*)gi_out, (T*)hist_out);
+    };
+    if (prec == 32) run(float());
+    else if (prec == 1) run(Tracked());
+    else run(double());
+}
+
 // casters / caster_entries / caster_atlas: shadow-casting point lights (num_casters may be 0).
 void oracle_deferred(int prec, const sgi_config* cfg, const sgi_gbuffer* g, const sgi_camera* cam,
                      const sgi_point_light* points, int num_points, const sgi_csm* csm, void* out,
                      const sgi_point_light* casters, const sgi_atlas_entry* caster_entries, int num_casters,
                      const sgi_cube_atlas* caster_atlas) {
     DeferredArgs a{cfg, g, cam, points, num_points, csm, casters, caster_entries, num_casters, caster_atlas};
-    if (prec == 32) deferred<float>(a, (float*)out);
+    if (prec == 0) deferred<Counted>(a, (Counted*)out);
+    else if (prec == 1) deferred<Tracked>(a, (Tracked*)out);
+    else if (prec == 32) deferred<float>(a, (float*)out);
     else deferred<double>(a, (double*)out);
 }
 

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "../include/sgi.h"
+#include "counted.hpp"
 #include "glsl.hpp"
 
 namespace oracle {
@@ -38,14 +39,21 @@ template <class T> inline T half_texel(const uint16_t* p, size_t i) { return T(f
 // Bilinear sample of a single-channel float image at uv (see header).
 template <class T, class Fetch> inline T bilinear(Fetch fetch, int W, int H, T s, T t) {
     T u = s * T(W) - T(0.5), v = t * T(H) - T(0.5);
-    T fu = std::floor(u), fv = std::floor(v);
+    T fu = gfloor(u), fv = gfloor(v);
     T a = u - fu, b = v - fv;
     int i0 = tex_index(double(fu), W), i1 = tex_index(double(fu + T(1)), W);
     int j0 = tex_index(double(fv), H), j1 = tex_index(double(fv + T(1)), H);
     T w00 = (T(1) - a) * (T(1) - b), w10 = a * (T(1) - b), w01 = (T(1) - a) * b, w11 = a * b;
     return gfma(fetch(i1, j1), w11, gfma(fetch(i0, j1), w01, gfma(fetch(i1, j0), w10, fetch(i0, j0) * w00)));
 }
-template <class T> inline int nearest_index(T s, int n) { return tex_index(double(std::floor(s * T(n))), n); }
+template <class T> inline int nearest_index(T s, int n) { return tex_index(double(gfloor(s * T(n))), n); }
+// the margin-tracking instantiation also records how far the coordinate is from a texel boundary
+inline int nearest_index(Tracked s, int n) {
+    const double x = s.v * double(n);
+    const double f = std::floor(x);
+    record_margin(1, std::fmin(x - f, f + 1.0 - x) / std::fmax(std::fabs(x), 1.0));
+    return tex_index(f, n);
+}
 
 // ------------------------------------------------------------------- CSM --
 // texture(sampler2DArrayShadow, vec4(s, t, layer, ref)) with LINEAR + LEQUAL.
@@ -446,7 +454,11 @@ template <class T> void gather(const GatherArgs& a, T* reservoir) {
     const int W = a.cfg->width, H = a.cfg->height;
 #pragma omp parallel for schedule(dynamic, 1)
     for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x) gather_pixel<T>(a, x, y, reservoir + ((size_t)y * W + x) * 4);
+        for (int x = 0; x < W; ++x) {
+            margin_begin<T>();
+            gather_pixel<T>(a, x, y, reservoir + ((size_t)y * W + x) * 4);
+            margin_end<T>((size_t)y * W + x);
+        }
 }
 
 // Converged target: `batches` runs of the sample loop, batch b seeded at
@@ -615,7 +627,7 @@ template <class T> void denoise_pixel(const DenoiseArgs<T>& a, int pass, const T
 // StratusRendererBackend.cpp:1912-1940: pass i uses multiplier 2^i - 1; pass 0
 // merges reservoirs; the last pass is final.
 template <class T> void denoise(const DenoiseArgs<T>& a, const T* reservoir, T* combined, T* gi_out, T* hist_out,
-                                T* pass_out /* nullable [n][P][4] */) {
+                                T* pass_out /* nullable [n][P][4] */, void (*after_pass)(int) = nullptr) {
     const int W = a.cfg->width, H = a.cfg->height, n = a.cfg->denoise_passes;
     const size_t P = (size_t)W * H;
     std::vector<T> bufA(P * 4), bufB(P * 4);
@@ -624,10 +636,30 @@ template <class T> void denoise(const DenoiseArgs<T>& a, const T* reservoir, T* 
         T* out = (pass % 2 == 0) ? bufA.data() : bufB.data();
 #pragma omp parallel for schedule(dynamic, 1)
         for (int y = 0; y < H; ++y)
-            for (int x = 0; x < W; ++x) denoise_pixel<T>(a, pass, in, out, combined, gi_out, hist_out, x, y);
+            for (int x = 0; x < W; ++x) {
+                margin_begin<T>();
+                denoise_pixel<T>(a, pass, in, out, combined, gi_out, hist_out, x, y);
+                margin_end<T>((size_t)y * W + x);
+            }
         if (pass_out) std::copy(out, out + P * 4, pass_out + (size_t)pass * P * 4);
+        if (after_pass) after_pass(pass);
         in = out;
     }
+}
+
+// One denoise pass over the whole image (pass 0 merges, the last is final), from
+// an arbitrary input reservoir: lets a pass of another implementation be
+// checked on exactly the input it was given.
+template <class T> void denoise_one_pass(const DenoiseArgs<T>& a, int pass, const T* res_in, T* res_out, T* combined,
+                                         T* gi_out, T* hist_out) {
+    const int W = a.cfg->width, H = a.cfg->height;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            margin_begin<T>();
+            denoise_pixel<T>(a, pass, res_in, res_out, combined, gi_out, hist_out, x, y);
+            margin_end<T>((size_t)y * W + x);
+        }
 }
 
 struct DeferredArgs {
@@ -717,7 +749,11 @@ template <class T> void deferred(const DeferredArgs& a, T* out) {
     const int W = a.cfg->width, H = a.cfg->height;
 #pragma omp parallel for schedule(dynamic, 1)
     for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x) deferred_pixel<T>(a, x, y, out + ((size_t)y * W + x) * 4);
+        for (int x = 0; x < W; ++x) {
+            margin_begin<T>();
+            deferred_pixel<T>(a, x, y, out + ((size_t)y * W + x) * 4);
+            margin_end<T>((size_t)y * W + x);
+        }
 }
 
 // ----------------------------------------------------------------- post FX --

@@ -27,6 +27,9 @@ SGI_MAX_ATLASES = 14
 SGI_MAX_VPLS_BEFORE_CULL = 10000
 SGI_MAX_VPLS_PER_FRAME = 4480
 SGI_NUM_PASS_TIMES = 5
+SGI_NUM_PASS_TIMES_SPLIT = 7
+SGI_SHADING_EXACT = 0
+SGI_SHADING_FAST = 1
 SGI_LANE_CHECKS = 12
 SGI_NO_LIGHT = 0xFFFFFFFFFFFFFFFF
 
@@ -175,6 +178,8 @@ EXPORTS = {
     "sgi_set_timing": (C.c_int32, [C.c_void_p, C.c_int32]),
     "sgi_get_pass_times": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "sgi_launch_count": (C.c_int64, [C.c_void_p]),
+    "sgi_set_shading_precision": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "sgi_get_shading_precision": (C.c_int32, [C.c_void_p]),
     "sgi_lane_selftest": (C.c_int32, [C.c_int32, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
     "sgi_slot_cache_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "sgi_slot_cache_destroy": (C.c_int32, [C.c_void_p]),

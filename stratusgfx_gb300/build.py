@@ -23,11 +23,17 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # results are bit-reproducible against the CPU restatement of the shaders.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-Xcompiler", "-fPIC", "-I" + os.path.join(REPO, "include")]
-CUDA_SOURCES = ["sgi_kernels.cu", "sgi_scene.cu", "sgi_nn.cu", "sgi_nn_tc.cu", "sgi_selftest.cu"]
+CUDA_SOURCES = ["sgi_kernels.cu", "sgi_shade.cu", "sgi_shade_fast.cu", "sgi_scene.cu", "sgi_nn.cu", "sgi_nn_tc.cu",
+                "sgi_selftest.cu"]
 HOST_SOURCES = ["sgi_api.cpp", "sgi_nn_api.cpp", "sgi_batch.cpp", "sgi_slots.cpp", "sgi_host.cpp"]
 # The learned denoiser is checked against the oracle within a tolerance, not bit
 # for bit, so its kernels keep the compiler's default multiply-add contraction.
 FAST_MATH_OK = {"sgi_nn.cu", "sgi_nn_tc.cu"}
+# The tolerance-mode shading kernels: contraction, approximate division and square
+# root (subnormals are kept: the decision-side arithmetic must round as in the
+# exact build).
+FAST_SHADING = {"sgi_shade_fast.cu"}
+FAST_SHADING_FLAGS = ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"]
 
 
 def _nvcc() -> str:
@@ -59,6 +65,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers.append(os.path.join(CSRC, "sgi_shade.cu"))   # included by sgi_shade_fast.cu
     headers += [os.path.join(REPO, "include", f) for f in os.listdir(os.path.join(REPO, "include"))]
     jobs = []
     objs = []
@@ -68,6 +75,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, [s] + headers):
             flags = [f for f in NVCC_FLAGS if not (src in FAST_MATH_OK and f == "-fmad=false")]
+            if src in FAST_SHADING:
+                flags = [f for f in flags if f not in ("-fmad=false", "-prec-div=true", "-prec-sqrt=true")]
+                flags += FAST_SHADING_FLAGS
             jobs.append([nvcc] + flags + ["-Xptxas", "-v", "-c", s, "-o", o])
     for src in HOST_SOURCES:
         s = os.path.join(CSRC, src)

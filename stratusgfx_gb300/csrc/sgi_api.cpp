@@ -104,6 +104,7 @@ void free_all(sgi_ctx* c) {
     void* nnp[] = {c->nn_feat, c->nn_prev};
     for (void* p : nnp) if (p) cudaFree(p);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    if (c->ev_atrous_end) cudaEventDestroy(c->ev_atrous_end);
     if (c->fork) cudaEventDestroy(c->fork);
     if (c->join) cudaEventDestroy(c->join);
     if (c->side) cudaStreamDestroy(c->side);
@@ -112,6 +113,10 @@ void free_all(sgi_ctx* c) {
 inline void record(sgi_ctx* c, int k, cudaStream_t s) {
     if (c->timing) cudaEventRecord(c->ev[k], s);
 }
+
+// The context's build of a shading kernel: exact (bit-identical to the CPU
+// restatement) or the tolerance mode (sgi_set_shading_precision).
+#define SGI_SHADE(c, fn) ((c)->fast_shading ? sgi::fast::fn : sgi::exact::fn)
 
 }  // namespace
 
@@ -201,6 +206,7 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     if (cfg->debug_keep_passes)
         for (int k = 0; k < cfg->denoise_passes; ++k) chk(dalloc(&c->pass_bufs[k], P));
     for (auto& ev : c->ev) chk(cudaEventCreate(&ev));
+    chk(cudaEventCreate(&c->ev_atrous_end));
     chk(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
     chk(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
     chk(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
@@ -327,7 +333,7 @@ sgi_status sgi_direct_lighting(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_
     if (!gbuffer_ok(gbuf, true) || !cam || !hdr_out) return fail(ctx, SGI_ERR_ARG, "NULL G-buffer, camera or output");
     if (!ctx->lights_set || !ctx->maps_set) return fail(ctx, SGI_ERR_STATE, "set lights and shadow maps first");
     sgi::ShadowCasters casters{ctx->shadow_points, ctx->shadow_entries, ctx->num_shadow_points, ctx->shadow_atlas};
-    SGI_CUDA(ctx, sgi::launch_deferred(ctx->cfg, ctx->sc, *gbuf, *cam, ctx->points, ctx->num_points, casters, ctx->csm,
+    SGI_CUDA(ctx, SGI_SHADE(ctx, launch_deferred)(ctx->cfg, ctx->sc, *gbuf, *cam, ctx->points, ctx->num_points, casters, ctx->csm,
                                        (uint2*)hdr_out, (cudaStream_t)stream, ctx->block_dim(SGI_BLOCK_DIRECT)),
              "deferred_pbr_csm");
     ctx->launches += 1;
@@ -343,7 +349,7 @@ static sgi_status run_gather(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_cam
     go.merged = keep ? ctx->pass_bufs[0] : ctx->merged;
     go.guide = ctx->guide;
     go.raw = keep ? ctx->reservoir : nullptr;
-    SGI_CUDA(ctx, sgi::launch_gather(cfg, ctx->sc, *cur, *cam, ctx->cv, ctx->ce, ctx->visible_index, ctx->lists,
+    SGI_CUDA(ctx, SGI_SHADE(ctx, launch_gather)(cfg, ctx->sc, *cur, *cam, ctx->cv, ctx->ce, ctx->visible_index, ctx->lists,
                                      ctx->cubes, params->time, go, s, ctx->block_dim(SGI_BLOCK_GATHER)),
              "vpl_gather");
     ctx->launches += 1;
@@ -365,12 +371,14 @@ static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer
     const uint2* in = ctx->last_merged;
     for (int pass = 1; pass < cfg.denoise_passes - 1; ++pass) {
         uint2* out = keep ? ctx->pass_bufs[pass] : ctx->ping[pass & 1];
-        SGI_CUDA(ctx, sgi::launch_atrous(cfg.width, cfg.height, pass, ctx->guide, in, out, s,
+        SGI_CUDA(ctx, SGI_SHADE(ctx, launch_atrous)(cfg.width, cfg.height, pass, ctx->guide, in, out, s,
                                          ctx->block_dim(SGI_BLOCK_ATROUS)),
                  "atrous");
         ctx->launches += 1;
         in = out;
     }
+    if (ctx->timing) cudaEventRecord(ctx->ev_atrous_end, s);
+    ctx->have_split = ctx->timing;
     // pass n-1: a-trous + temporal reprojection + composite
     sgi::DenoiseLaunch d;
     std::memset(&d, 0, sizeof(d));
@@ -386,7 +394,7 @@ static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer
     d.res_in = in;
     d.res_out = keep ? ctx->pass_bufs[cfg.denoise_passes - 1] : nullptr;
     if (hdr_ready) SGI_CUDA(ctx, cudaStreamWaitEvent(s, hdr_ready, 0), "join direct lighting");
-    SGI_CUDA(ctx, sgi::launch_denoise_final(d, s, ctx->block_dim(SGI_BLOCK_DENOISE_FINAL)), "denoise_final");
+    SGI_CUDA(ctx, SGI_SHADE(ctx, launch_denoise_final)(d, s, ctx->block_dim(SGI_BLOCK_DENOISE_FINAL)), "denoise_final");
     ctx->launches += 1;
     ctx->hist_cur = 1 - ctx->hist_cur;
     ctx->have_history = true;
@@ -453,7 +461,7 @@ sgi_status sgi_gi_target(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera
     if (!gbuffer_ok(gbuf, true) || !cam || !target) return fail(ctx, SGI_ERR_ARG, "NULL G-buffer, camera or target");
     if (batches < 1 || batches > 65536) return fail(ctx, SGI_ERR_ARG, "batches must be in [1, 65536]");
     if (!ctx->culled || !ctx->maps_set) return fail(ctx, SGI_ERR_STATE, "cull VPLs (and tiles) first");
-    SGI_CUDA(ctx, sgi::launch_gi_target(ctx->cfg, ctx->sc, *gbuf, *cam, ctx->cv, ctx->ce, ctx->visible_index,
+    SGI_CUDA(ctx, sgi::exact::launch_gi_target(ctx->cfg, ctx->sc, *gbuf, *cam, ctx->cv, ctx->ce, ctx->visible_index,
                                         ctx->lists, ctx->cubes, time, batches, (float4*)target, (cudaStream_t)stream),
              "gi_target");
     ctx->launches += 1;
@@ -592,6 +600,18 @@ sgi_status sgi_get_block_shape(const sgi_ctx* ctx, int32_t pass, int32_t* bx, in
     return SGI_OK;
 }
 
+sgi_status sgi_set_shading_precision(sgi_ctx* ctx, int32_t mode) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (mode != SGI_SHADING_EXACT && mode != SGI_SHADING_FAST)
+        return fail(ctx, SGI_ERR_ARG, "shading precision must be SGI_SHADING_EXACT or SGI_SHADING_FAST");
+    ctx->fast_shading = mode == SGI_SHADING_FAST;
+    return SGI_OK;
+}
+
+int32_t sgi_get_shading_precision(const sgi_ctx* ctx) {
+    return ctx && ctx->fast_shading ? SGI_SHADING_FAST : SGI_SHADING_EXACT;
+}
+
 sgi_status sgi_set_timing(sgi_ctx* ctx, int32_t enabled) {
     if (!ctx) return SGI_ERR_ARG;
     ctx->timing = enabled != 0;
@@ -607,6 +627,15 @@ sgi_status sgi_get_pass_times(sgi_ctx* ctx, float* ms, int32_t n) {
         float t = 0.0f;
         SGI_CUDA(ctx, cudaEventElapsedTime(&t, ctx->ev[k], ctx->ev[k + 1]), "event elapsed");
         ms[k] = t;
+    }
+    // the denoise pass split at its last a-trous pass (0 when the last timed frame had none)
+    if (n > SGI_NUM_PASS_TIMES) {
+        ms[5] = 0.0f;
+        if (ctx->have_split) SGI_CUDA(ctx, cudaEventElapsedTime(&ms[5], ctx->ev[4], ctx->ev_atrous_end), "event elapsed");
+    }
+    if (n > SGI_NUM_PASS_TIMES + 1) {
+        ms[6] = 0.0f;
+        if (ctx->have_split) SGI_CUDA(ctx, cudaEventElapsedTime(&ms[6], ctx->ev_atrous_end, ctx->ev[5]), "event elapsed");
     }
     return SGI_OK;
 }
@@ -701,6 +730,7 @@ sgi_status sgi_render_frame_neural(sgi_ctx* ctx, sgi_nn* net, const sgi_gbuffer*
     ctx->hist_cur = 1 - ctx->hist_cur;
     ctx->have_history = true;
     record(ctx, 5, s);
+    ctx->have_split = false;
     ctx->have_times = ctx->timing;
     return SGI_OK;
 }

@@ -58,9 +58,14 @@ struct sgi_ctx {
     __nv_bfloat16* nn_feat = nullptr;
     float4* nn_prev = nullptr;
 
+    // shading kernels: exact (false) or the tolerance mode (true)
+    bool fast_shading = false;
+
     // timing
     bool timing = false;
     cudaEvent_t ev[SGI_NUM_PASS_TIMES + 1] = {};
+    cudaEvent_t ev_atrous_end = nullptr;   // between the last a-trous pass and the final denoise pass
+    bool have_split = false;               // the last timed frame recorded ev_atrous_end
     bool have_times = false;
 
     // direct lighting runs on a side stream, concurrently with the VPL and tile

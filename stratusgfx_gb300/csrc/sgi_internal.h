@@ -69,20 +69,6 @@ cudaError_t launch_tile_stage1(const sgi_config& cfg, const sgi_gbuffer& g, cons
 // keys: scratch of tiles x round_up(max_visible, 32) uint32
 cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1, const sgi_vpl* cv,
                                const int32_t* visible_index, uint32_t* keys, int32_t* lists, cudaStream_t s);
-cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam,
-                          const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index,
-                          const int32_t* lists, const sgi_cube_atlas& cubes, float time, const GatherOut& out,
-                          cudaStream_t s, dim3 block = dim3(0, 0, 0));
-// converged target: `batches` runs of the sample loop, sums in FP64 -> float4 (rgb, 1)
-cudaError_t launch_gi_target(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
-                             const sgi_camera& cam, const sgi_vpl* cv, const sgi_atlas_entry* ce,
-                             const int32_t* visible_index, const int32_t* lists, const sgi_cube_atlas& cubes,
-                             float time, int batches, float4* out, cudaStream_t s);
-// a-trous pass `pass` (1 .. passes-2): 5x5 taps at stride 2^pass
-cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in,
-                          uint2* res_out, cudaStream_t s, dim3 block = dim3(0, 0, 0));
-// last pass: a-trous filter + temporal reprojection + composite
-cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s, dim3 block = dim3(0, 0, 0));
 // shadow-casting point lights of the deferred pass (pbr.fs:116-131)
 struct ShadowCasters {
     const sgi_point_light* lights;
@@ -90,10 +76,38 @@ struct ShadowCasters {
     int32_t count;
     sgi_cube_atlas atlas;
 };
-cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
-                            const sgi_camera& cam, const sgi_point_light* points, int32_t num_points,
-                            const ShadowCasters& casters, const sgi_csm& csm, uint2* hdr_out, cudaStream_t s,
-                            dim3 block = dim3(0, 0, 0));
+
+// The shading kernels (sgi_shade.cu) exist twice: sgi::exact is bit-identical to
+// the CPU restatement of the shaders, sgi::fast is the tolerance mode (fast
+// division, square root, exponential and contraction; see sgi_shade.cu).
+#define SGI_SHADE_LAUNCHERS \
+    cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam, \
+                              const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index, \
+                              const int32_t* lists, const sgi_cube_atlas& cubes, float time, const GatherOut& out, \
+                              cudaStream_t s, dim3 block = dim3(0, 0, 0)); \
+    /* a-trous pass `pass` (1 .. passes-2): 5x5 taps at stride 2^pass */ \
+    cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in, \
+                              uint2* res_out, cudaStream_t s, dim3 block = dim3(0, 0, 0)); \
+    /* last pass: a-trous filter + temporal reprojection + composite */ \
+    cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s, dim3 block = dim3(0, 0, 0)); \
+    cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, \
+                                const sgi_camera& cam, const sgi_point_light* points, int32_t num_points, \
+                                const ShadowCasters& casters, const sgi_csm& csm, uint2* hdr_out, cudaStream_t s, \
+                                dim3 block = dim3(0, 0, 0));
+
+namespace exact {
+SGI_SHADE_LAUNCHERS
+// converged target: `batches` runs of the sample loop, sums in FP64 -> float4 (rgb, 1)
+cudaError_t launch_gi_target(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
+                             const sgi_camera& cam, const sgi_vpl* cv, const sgi_atlas_entry* ce,
+                             const int32_t* visible_index, const int32_t* lists, const sgi_cube_atlas& cubes,
+                             float time, int batches, float4* out, cudaStream_t s);
+}  // namespace exact
+namespace fast {
+SGI_SHADE_LAUNCHERS
+}  // namespace fast
+#undef SGI_SHADE_LAUNCHERS
+
 // Thread-block shapes of the per-pixel passes: any shape of 256 threads gives the
 // same results (every pixel is computed by one thread, independently); a zero
 // shape selects the pass's default.

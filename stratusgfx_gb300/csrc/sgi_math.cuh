@@ -1,15 +1,23 @@
 // sgi_math.cuh - device-side shading math of the GI/lighting stage.
 //
-// Every translation unit that includes this header is compiled with
-// -fmad=false, -prec-div=true and -prec-sqrt=true: each +, -, *, / and sqrtf
-// below is one correctly rounded binary32 operation, and multiply-adds are
-// fused only where __fmaf_rn is written, evaluated in the order the
-// expression tree gives. That makes the results reproducible on any IEEE-754
-// machine, which is how the per-pixel results are checked bit for bit against
-// a CPU restatement of the StratusGFX shaders. No CUDA math-library
-// transcendental is called: exp is computed by Cody-Waite range reduction
-// plus a degree-7 Taylor polynomial, and pow only appears with the integer
-// exponents 5 and 128.
+// The exact build of the kernels is compiled with -fmad=false, -prec-div=true
+// and -prec-sqrt=true: each +, -, *, / and sqrtf below is one correctly rounded
+// binary32 operation, and multiply-adds are fused only where __fmaf_rn is
+// written, evaluated in the order the expression tree gives. That makes the
+// results reproducible on any IEEE-754 machine, which is how the per-pixel
+// results are checked bit for bit against a CPU restatement of the StratusGFX
+// shaders. No CUDA math-library transcendental is called there: exp is
+// computed by Cody-Waite range reduction plus a degree-7 Taylor polynomial, and
+// pow only appears with the integer exponents 5 and 128.
+//
+// The tolerance build of the shading kernels (SGI_FAST_MATH = 1, compiled with
+// contraction and approximate division and square root) evaluates the same
+// expressions faster, except for everything a branch decision or a texel
+// choice depends on: those are written with the x* functions below
+// (__fadd_rn, __fmul_rn, __fdiv_rn, __fsqrt_rn, __fmaf_rn), which no compiler
+// flag contracts or approximates, so both builds take the same branches, read
+// the same texels and keep the same per-tile lists; only continuous values
+// differ between them.
 //
 // Implementation-defined GLSL arithmetic, fixed here: dot products, matrix
 // rows, polynomial steps and weighted sums are fused multiply-add chains;
@@ -41,16 +49,27 @@ SGI_D float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 SGI_D float mixf(float x, float y, float a) { return __fmaf_rn(y, a, x * (1.0f - a)); }
 SGI_D float gabs(float x) { return x < 0.0f ? -x : x; }
 
-// exp(x): Cody & Waite (1980) reduction x = k*ln2 + r with ln2 split into a
-// 15-bit head (exact products for |k| < 512) and a tail, exp(r) by its Taylor
-// series to r^7 in Horner form, then exact scaling by 2^k.
-SGI_D float expf_ieee(float x) {
+#ifndef SGI_FAST_MATH
+#define SGI_FAST_MATH 0
+#endif
+
+// Correctly rounded binary32 operations in every build (see the header comment).
+SGI_D float xadd(float a, float b) { return __fadd_rn(a, b); }
+SGI_D float xsub(float a, float b) { return __fsub_rn(a, b); }
+SGI_D float xmul(float a, float b) { return __fmul_rn(a, b); }
+SGI_D float xdiv(float a, float b) { return __fdiv_rn(a, b); }
+SGI_D float xsqrt(float a) { return __fsqrt_rn(a); }
+SGI_D float xmixf(float x, float y, float a) { return __fmaf_rn(y, a, xmul(x, xsub(1.0f, a))); }
+
+// expf_ieee's arithmetic (below) with every operation explicitly rounded: the
+// same value in every build.
+SGI_D float expf_exact(float x) {
     if (x != x) return x;
     if (x > 88.72283935546875f) return __int_as_float(0x7f800000);
     if (x < -103.97283935546875f) return 0.0f;
-    float kf = floorf(x * 1.44269502162933349609375f + 0.5f);
+    float kf = floorf(xadd(xmul(x, 1.44269502162933349609375f), 0.5f));
     int k = (int)kf;
-    float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187045037746429443359375e-06f;
+    float r = xsub(xsub(x, xmul(kf, 0.693145751953125f)), xmul(kf, 1.428606765330187045037746429443359375e-06f));
     float p = __fmaf_rn(r, 1.0f / 5040.0f, 1.0f / 720.0f);
     p = __fmaf_rn(p, r, 1.0f / 120.0f);
     p = __fmaf_rn(p, r, 1.0f / 24.0f);
@@ -58,10 +77,20 @@ SGI_D float expf_ieee(float x) {
     p = __fmaf_rn(p, r, 0.5f);
     p = __fmaf_rn(p, r, 1.0f);
     p = __fmaf_rn(p, r, 1.0f);
-    if (k > 127) { p = p * 1.7014118346046923e+38f; k -= 127; }
-    if (k < -126) { p = p * 1.1754943508222875e-38f; k += 126; }
-    return p * __int_as_float((k + 127) << 23);
+    if (k > 127) { p = xmul(p, 1.7014118346046923e+38f); k -= 127; }
+    if (k < -126) { p = xmul(p, 1.1754943508222875e-38f); k += 126; }
+    return xmul(p, __int_as_float((k + 127) << 23));
 }
+
+// exp(x): Cody & Waite (1980) reduction x = k*ln2 + r with ln2 split into a
+// 15-bit head (exact products for |k| < 512) and a tail, exp(r) by its Taylor
+// series to r^7 in Horner form, then exact scaling by 2^k. In the tolerance
+// build of the shading kernels (SGI_FAST_MATH) it is the hardware exponential.
+#if SGI_FAST_MATH
+SGI_D float expf_ieee(float x) { return __expf(x); }
+#else
+SGI_D float expf_ieee(float x) { return expf_exact(x); }
+#endif
 SGI_D float pow5(float x) { float x2 = x * x; float x4 = x2 * x2; return x4 * x; }
 SGI_D float pow128(float x) {
     float y = x * x; y = y * y; y = y * y; y = y * y; y = y * y; y = y * y; y = y * y; return y;
@@ -114,6 +143,9 @@ SGI_D float exp_reduce(float x, float& kf) {
     return (x - kf * 0.693145751953125f) - kf * 1.428606765330187045037746429443359375e-06f;
 }
 SGI_D float2 expf_ieee2(float2 x) {
+#if SGI_FAST_MATH
+    return make_float2(__expf(x.x), __expf(x.y));
+#endif
     if (!(exp_packable(x.x) && exp_packable(x.y))) return make_float2(expf_ieee(x.x), expf_ieee(x.y));
     float2 kf;
     const float2 r = make_float2(exp_reduce(x.x, kf.x), exp_reduce(x.y, kf.y));
@@ -155,32 +187,45 @@ SGI_D V3 operator-(float s, V3 a) { return V3{s - a.x, s - a.y, s - a.z}; }
 SGI_D V3 operator/(float s, V3 a) { return V3{s / a.x, s / a.y, s / a.z}; }
 SGI_D float dot(V3 a, V3 b) { return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, a.x * b.x)); }
 SGI_D float length(V3 a) { return sqrtf(dot(a, a)); }
+#if SGI_FAST_MATH
+SGI_D V3 normalize(V3 a) { const float r = rsqrtf(dot(a, a)); return a * r; }
+#else
 SGI_D V3 normalize(V3 a) { const float r = 1.0f / sqrtf(dot(a, a)); return a * r; }
+#endif
 SGI_D V3 vmin(V3 a, float s) { return V3{gmin(a.x, s), gmin(a.y, s), gmin(a.z, s)}; }
 SGI_D V3 vmix(V3 x, V3 y, float a) {
     const float b = 1.0f - a;
     return V3{__fmaf_rn(y.x, a, x.x * b), __fmaf_rn(y.y, a, x.y * b), __fmaf_rn(y.z, a, x.z * b)};
 }
+// the decision-side vector operations (correctly rounded in every build)
+SGI_D V3 xadd3(V3 a, V3 b) { return V3{xadd(a.x, b.x), xadd(a.y, b.y), xadd(a.z, b.z)}; }
+SGI_D V3 xsub3(V3 a, V3 b) { return V3{xsub(a.x, b.x), xsub(a.y, b.y), xsub(a.z, b.z)}; }
+SGI_D V3 xmul3(V3 a, float s) { return V3{xmul(a.x, s), xmul(a.y, s), xmul(a.z, s)}; }
+SGI_D V3 xdiv3(V3 a, float s) { const float r = xdiv(1.0f, s); return xmul3(a, r); }
+SGI_D float xdot(V3 a, V3 b) { return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, xmul(a.x, b.x))); }
+SGI_D float xlength(V3 a) { return xsqrt(xdot(a, a)); }
+SGI_D V3 xnormalize(V3 a) { const float r = xdiv(1.0f, xsqrt(xdot(a, a))); return xmul3(a, r); }
 
 struct V4 { float x, y, z, w; };
 // column-major mat4 times (x, y, z, w), column-wise accumulation
+// (exact in every build: positions feed the culls' and the shadow tests' decisions)
 SGI_D V4 mat4_mul(const float* m, float x, float y, float z, float w) {
     V4 r;
-    r.x = __fmaf_rn(m[12], w, __fmaf_rn(m[8], z, __fmaf_rn(m[4], y, m[0] * x)));
-    r.y = __fmaf_rn(m[13], w, __fmaf_rn(m[9], z, __fmaf_rn(m[5], y, m[1] * x)));
-    r.z = __fmaf_rn(m[14], w, __fmaf_rn(m[10], z, __fmaf_rn(m[6], y, m[2] * x)));
-    r.w = __fmaf_rn(m[15], w, __fmaf_rn(m[11], z, __fmaf_rn(m[7], y, m[3] * x)));
+    r.x = __fmaf_rn(m[12], w, __fmaf_rn(m[8], z, __fmaf_rn(m[4], y, xmul(m[0], x))));
+    r.y = __fmaf_rn(m[13], w, __fmaf_rn(m[9], z, __fmaf_rn(m[5], y, xmul(m[1], x))));
+    r.z = __fmaf_rn(m[14], w, __fmaf_rn(m[10], z, __fmaf_rn(m[6], y, xmul(m[2], x))));
+    r.w = __fmaf_rn(m[15], w, __fmaf_rn(m[11], z, __fmaf_rn(m[7], y, xmul(m[3], x))));
     return r;
 }
 SGI_D float dot4(const float* pl, V3 p) {
-    return __fmaf_rn(pl[3], 1.0f, __fmaf_rn(pl[2], p.z, __fmaf_rn(pl[1], p.y, pl[0] * p.x)));
+    return __fmaf_rn(pl[3], 1.0f, __fmaf_rn(pl[2], p.z, __fmaf_rn(pl[1], p.y, xmul(pl[0], p.x))));
 }
 
-// worldPositionFromDepth, common.glsl:143-155
+// worldPositionFromDepth, common.glsl:143-155 (exact in every build)
 SGI_D V3 world_from_depth(float u, float v, float depth, const float* inv_pv) {
-    float z = depth * 2.0f - 1.0f;
-    V4 w = mat4_mul(inv_pv, u * 2.0f - 1.0f, v * 2.0f - 1.0f, z, 1.0f);
-    return V3{w.x, w.y, w.z} / w.w;
+    float z = xsub(xmul(depth, 2.0f), 1.0f);
+    V4 w = mat4_mul(inv_pv, xsub(xmul(u, 2.0f), 1.0f), xsub(xmul(v, 2.0f), 1.0f), z, 1.0f);
+    return xdiv3(V3{w.x, w.y, w.z}, w.w);
 }
 
 // Edge-stopping weight of one a-trous tap q for the centre (cn, cd)
@@ -219,12 +264,12 @@ SGI_D float random3(float sx, float sy, float sz) {
 SGI_D float unorm8(uint32_t t, int ch) {
     const float b = float((t >> (8 * ch)) & 0xffu);
     const float r = 1.0f / 255.0f;
-    const float q = b * r;
+    const float q = xmul(b, r);
     return __fmaf_rn(__fmaf_rn(-q, 255.0f, b), r, q);
 }
-SGI_D V3 decode_normal(uint32_t t) {   // normalize(rgb * 2 - 1), common.glsl:216-220
+SGI_D V3 decode_normal(uint32_t t) {   // normalize(rgb * 2 - 1), common.glsl:216-220 (exact in every build)
     V3 c = v3(unorm8(t, 0), unorm8(t, 1), unorm8(t, 2));
-    return normalize(c * 2.0f - v3s(1.0f));
+    return xnormalize(V3{xsub(xmul(c.x, 2.0f), 1.0f), xsub(xmul(c.y, 2.0f), 1.0f), xsub(xmul(c.z, 2.0f), 1.0f)});
 }
 SGI_D float h2f(uint16_t h) { return __half2float(__ushort_as_half(h)); }
 SGI_D uint16_t f2h(float f) { return __half_as_ushort(__float2half_rn(f)); }
@@ -235,7 +280,7 @@ SGI_D int tex_index(float f, int n) {
     if (f >= 0.0f) return (int)f;
     return 0;
 }
-SGI_D int nearest_index(float s, int n) { return tex_index(floorf(s * float(n)), n); }
+SGI_D int nearest_index(float s, int n) { return tex_index(floorf(xmul(s, float(n))), n); }
 
 // ------------------------------------------------------- shading library --
 struct ShadeParams {

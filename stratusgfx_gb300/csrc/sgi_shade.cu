@@ -1,0 +1,483 @@
+// sgi_shade.cu - the shading kernels of the GI/lighting hot path on sm_103a:
+//   vpl_gather        vpl_pbr_gi.fs:81-207 (+ denoise pass 0, the reservoir merge)
+//   gi_target         the converged K-sample target (no reference counterpart)
+//   atrous            vpl_pbr_gi_denoise.fs:142-327 (passes 1 .. n-2)
+//   denoise_final     vpl_pbr_gi_denoise.fs:275-435 (last pass: filter, temporal, composite)
+//   deferred_pbr_csm  pbr.fs:82-145 (+ pbr.glsl:158-227)
+//
+// This file is compiled twice into the library:
+//   * as sgi_shade.cu with -fmad=false -prec-div=true -prec-sqrt=true: every
+//     operation rounds as the CPU restatement of the shaders rounds, so the
+//     results are bit-identical to it (namespace sgi::exact);
+//   * through sgi_shade_fast.cu with SGI_FAST_MATH = 1 and contraction,
+//     approximate division and square root, hardware reciprocal square root and
+//     exponential (namespace sgi::fast): the tolerance mode, within 1e-3
+//     relative error of the restatement outside the decision margins.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sgi_internal.h"
+#include "sgi_math.cuh"
+#include "sgi_shade_common.cuh"
+
+#ifndef SGI_FAST_MATH
+#define SGI_FAST_MATH 0
+#endif
+#if SGI_FAST_MATH
+#define SGI_SHADE_NS fast
+#else
+#define SGI_SHADE_NS exact
+#endif
+
+namespace sgi {
+namespace SGI_SHADE_NS {
+
+// ================================================================ gather --
+struct GatherParams {
+    int W, H, ts, tiles_x, L, tiled, spp;
+    ShadeConfig sc;
+    sgi_gbuffer g;
+    sgi_camera cam;
+    const sgi_vpl* cv;
+    const sgi_atlas_entry* ce;
+    const int32_t* visible_index;
+    const int32_t* lists;
+    sgi_cube_atlas cubes;
+    float time;
+    GatherOut out;
+};
+
+// Per-pixel inputs of the gather (vpl_pbr_gi.fs:99-145).
+struct PixelShade {
+    V3 fragPos, viewDir, baseColor, normal, baseRefl;
+    float distToCamera, roughness, metallic, ao, ambient;
+    int sampleCount, candidates;
+    const int32_t* list;
+};
+
+SGI_D PixelShade load_pixel(const GatherParams& p, int x, int y, size_t i) {
+    PixelShade px;
+    const float u = xdiv(float(x) + 0.5f, float(p.W)), v = xdiv(float(y) + 0.5f, float(p.H));
+    px.fragPos = world_from_depth(u, v, __ldg(p.g.depth + i), p.cam.inv_proj_view);
+    const V3 viewPos = v3(p.cam.view_position[0], p.cam.view_position[1], p.cam.view_position[2]);
+    px.viewDir = normalize(viewPos - px.fragPos);
+    px.distToCamera = xlength(xsub3(viewPos, px.fragPos));   // decides the shadow test and the sample count
+    const uint32_t alb = __ldg(p.g.albedo + i);
+    px.baseColor = v3(gmax(unorm8(alb, 0), 0.01f), gmax(unorm8(alb, 1), 0.01f), gmax(unorm8(alb, 2), 0.01f));
+    px.normal = decode_normal(__ldg(p.g.normal + i));
+    const uint32_t rma = __ldg(p.g.roughness_metallic_ambient + i);
+    px.roughness = gmax(0.5f, unorm8(rma, 0));
+    px.metallic = unorm8(rma, 1);
+    px.ao = gclamp(h2f(__ldg(p.g.ssao + i)), 0.35f, 1.0f);
+    px.ambient = unorm8(rma, 2);
+    px.baseRefl = v3s(float(__ldg(p.g.base_reflectivity + i) & 0xffu) / 255.0f);
+    const float roughnessWeight = xsub(1.0f, px.roughness);
+    const float distRatio = gmin(xsub(1.0f, xdiv(px.distToCamera, 1000.0f)), 1.0f);
+    if (p.spp > 0) {
+        px.sampleCount = p.spp;
+    } else {
+        int maxSamplesPerPixel = (int)xmixf(2.0f, 10.0f, roughnessWeight);
+        int samplesMax = (int)xmul(float(maxSamplesPerPixel), distRatio);
+        px.sampleCount = samplesMax > 1 ? samplesMax : 1;
+    }
+    px.list = nullptr;
+    if (p.tiled) {
+        const int tile = (y / p.ts) * p.tiles_x + (x / p.ts);
+        px.list = p.lists + (size_t)tile * (1 + p.L);
+        px.candidates = __ldg(px.list);
+    } else {
+        px.candidates = __ldg(p.visible_index);
+    }
+    return px;
+}
+
+// The sample loop of vpl_pbr_gi.fs:148-200 with the seed z starting at seedZ.
+SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX, float seedY, float seedZ,
+                       V3& vplColor, float& validSamples) {
+    ShadeParams sp{p.sc.min_roughness, p.sc.perceptual, p.sc.fog_density,
+                   {p.sc.fog_color[0], p.sc.fog_color[1], p.sc.fog_color[2]}, p.sc.point_ambient};
+    vplColor = v3s(0.0f);
+    validSamples = 0.0f;
+    const int candidates = px.candidates;
+    if (candidates <= 0) return;
+    const float minGi = p.sc.min_gi_occlusion;
+    const V3 fragPos = px.fragPos, normal = px.normal;
+    const VplPixel vp = vpl_pixel(fragPos, px.baseColor, normal, px.viewDir, px.distToCamera, px.roughness,
+                                  px.metallic, px.ambient, px.baseRefl, sp);
+    for (int s = 0, resamples = 0; s < px.sampleCount; ++s) {
+        const float rnd = random3(seedX, seedY, seedZ);
+        seedZ += 10000.0f;
+        int lightIndex;
+        if (px.list) {
+            int r = (int)xmul(float(candidates), rnd);
+            lightIndex = __ldg(px.list + 1 + (r < candidates - 1 ? r : candidates - 1));
+        } else {
+            lightIndex = (int)xmul(float(candidates - 1), rnd);
+        }
+        const float4* rec = reinterpret_cast<const float4*>(p.cv + lightIndex);
+        const float4 pos = __ldg(rec);
+        const float4 spec = __ldg(rec + 2);
+        const float4 misc = __ldg(rec + 3);   // radius, farPlane, intensity
+        const sgi_atlas_entry entry = p.ce[lightIndex];
+        const V3 lightPosition = v3(pos.x, pos.y, pos.z);
+        const V3 lmf = xsub3(lightPosition, fragPos);
+        const float lightRadius = misc.x;
+        const float distance = xlength(lmf);
+        if (resamples < 5) {
+            float sideCheck = xdot(normal, xnormalize(lmf));
+            if (sideCheck < 0.0f || distance > lightRadius) { ++resamples; --s; continue; }
+        }
+        const float distanceRatio = gclamp((2.0f * distance) / lightRadius, 0.0f, 1.0f);
+        const float distAttenuation = distanceRatio;
+        const float4 col = __ldg(rec + 1);
+        const V3 lightColor = v3(col.x, col.y, col.z);
+        float shadowFactor = px.distToCamera < 500.0f
+                                 ? shadow_1sample(p.cubes, entry, misc.y, fragPos, lightPosition,
+                                                  xdot(lmf, normal), 0.1f)
+                                 : 0.0f;
+        shadowFactor = gmin(shadowFactor, mixf(minGi, 1.0f, distanceRatio));
+        float reweight = 1.0f;
+        if (shadowFactor > 0.0f) reweight = (1.0f - distAttenuation) * minGi + distAttenuation;
+        validSamples += reweight;
+        const V3 tmp = px.ao * vpl_lighting2_sample(vp, v3(spec.x, spec.y, spec.z), lightPosition, lightColor,
+                                                    lightRadius);
+        vplColor = vplColor + (1.0f - shadowFactor) * tmp;
+    }
+}
+
+// vpl_pbr_gi.fs:81-207, one thread per pixel.
+__global__ void __launch_bounds__(256, 4) vpl_gather_kernel(GatherParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= p.W || y >= p.H) return;
+    const size_t i = (size_t)y * p.W + x;
+    const PixelShade px = load_pixel(p, x, y, i);
+    const V3 normal = px.normal;
+    const float seedX = float(x) + 0.5f, seedY = float(y) + 0.5f;
+    V3 vplColor;
+    float validSamples;
+    sample_vpls(p, px, seedX, seedY, p.time, vplColor, validSamples);
+    validSamples = gmax(validSamples, 1.0f);
+    const V3 b = vmin(vplColor, kHalfMax);
+    // The reservoir as stored in its RGBA16F target (vpl_pbr_gi.fs:205).
+    const float r0 = h2f(f2h(b.x)), r1 = h2f(f2h(b.y)), r2 = h2f(f2h(b.z)), r3 = h2f(f2h(validSamples));
+    if (p.out.raw) p.out.raw[i] = pack_h4(r0, r1, r2, r3);
+    // Denoise pass 0 for this pixel: computeMergedReservoir with minmaxNearest = 0
+    // (vpl_pbr_gi_denoise.fs:192-273) reads only the centre texel, which is this one.
+    const float depth = __ldg(p.g.depth + i);
+    float cr0 = 0.0f, cr1 = 0.0f, cr2 = 0.0f, cr3 = 0.0f;
+    float runningSum = 0.0f;
+    const float probabilisticWeight = 1.0f / float(__ldg(p.visible_index));
+    if (!(xdot(normal, normal) < 0.906f)) {
+        if (!(gabs(xsub(depth, depth)) > xmul(0.1f, depth))) {
+            const float randUpdate = random3(seedX, seedY, p.time);
+            const float probability = r3 * probabilisticWeight;
+            cr3 = xadd(cr3, probability);
+            if (randUpdate < xdiv(probability, cr3)) {
+                cr0 += r0; cr1 += r1; cr2 += r2;
+                runningSum += r3;
+            }
+        }
+    }
+    const float den = gmax(kEps, runningSum);
+    p.out.merged[i] = pack_h4(cr0 / den, cr1 / den, cr2 / den, 1.0f);
+    p.out.guide[i] = make_float4(normal.x, normal.y, normal.z, depth);
+}
+
+cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam,
+                          const sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index,
+                          const int32_t* lists, const sgi_cube_atlas& cubes, float time, const GatherOut& out,
+                          cudaStream_t s, dim3 block) {
+    GatherParams p;
+    p.W = cfg.width; p.H = cfg.height; p.ts = cfg.tile_size;
+    p.tiles_x = (cfg.width + cfg.tile_size - 1) / cfg.tile_size;
+    p.L = cfg.max_vpls_per_tile; p.tiled = cfg.gi_mode == SGI_GI_TILED; p.spp = cfg.samples_per_pixel;
+    p.sc = sc; p.g = g; p.cam = cam; p.cv = cv; p.ce = ce; p.visible_index = visible_index; p.lists = lists;
+    p.cubes = cubes; p.time = time; p.out = out;
+    if (block.x == 0) block = dim3(16, 16);
+    dim3 grid((cfg.width + block.x - 1) / block.x, (cfg.height + block.y - 1) / block.y);
+    vpl_gather_kernel<<<grid, block, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+#if !SGI_FAST_MATH
+// Converged GI target: `batches` independent runs of the gather's sample loop
+// per pixel (batch b seeds z at time + b * 2e5, far past the previous batch's
+// draws), with sum(vplColor) and sum(validSamples) accumulated in FP64. Its
+// ratio is the limit of the per-pixel estimate the K-sample path denoises;
+// out = (sum vplColor / max(sum validSamples, 1), 1) as FP32.
+__global__ void __launch_bounds__(256, 4) gi_target_kernel(GatherParams p, int batches, float4* __restrict__ out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= p.W || y >= p.H) return;
+    const size_t i = (size_t)y * p.W + x;
+    const PixelShade px = load_pixel(p, x, y, i);
+    const float seedX = float(x) + 0.5f, seedY = float(y) + 0.5f;
+    double c0 = 0.0, c1 = 0.0, c2 = 0.0, w = 0.0;
+    for (int b = 0; b < batches; ++b) {
+        V3 col;
+        float valid;
+        sample_vpls(p, px, seedX, seedY, p.time + float(b) * 200000.0f, col, valid);
+        c0 += (double)col.x; c1 += (double)col.y; c2 += (double)col.z; w += (double)valid;
+    }
+    const double den = w < 1.0 ? 1.0 : w;
+    out[i] = make_float4((float)(c0 / den), (float)(c1 / den), (float)(c2 / den), 1.0f);
+}
+
+cudaError_t launch_gi_target(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
+                             const sgi_camera& cam, const sgi_vpl* cv, const sgi_atlas_entry* ce,
+                             const int32_t* visible_index, const int32_t* lists, const sgi_cube_atlas& cubes,
+                             float time, int batches, float4* out, cudaStream_t s) {
+    GatherParams p;
+    p.W = cfg.width; p.H = cfg.height; p.ts = cfg.tile_size;
+    p.tiles_x = (cfg.width + cfg.tile_size - 1) / cfg.tile_size;
+    p.L = cfg.max_vpls_per_tile; p.tiled = cfg.gi_mode == SGI_GI_TILED; p.spp = cfg.samples_per_pixel;
+    p.sc = sc; p.g = g; p.cam = cam; p.cv = cv; p.ce = ce; p.visible_index = visible_index; p.lists = lists;
+    p.cubes = cubes; p.time = time;
+    dim3 block(16, 16);
+    dim3 grid((cfg.width + 15) / 16, (cfg.height + 15) / 16);
+    gi_target_kernel<<<grid, block, 0, s>>>(p, batches, out);
+    return cudaGetLastError();
+}
+#endif  // !SGI_FAST_MATH
+
+// =============================================================== denoise --
+// The 5x5 edge-stopping filter of vpl_pbr_gi_denoise.fs:307-327 with the
+// weights of filterInput (:142-190): w = pow(max(0, n_c . n_q), 128) *
+// exp(-|z_c - z_q|) / sigmaZ, centre weight 1, taps at stride 2^pass, clamped
+// to the edge. Normals and depths come from the gather's guide (the same
+// decoded values the shader computes per tap).
+//
+// The 24 off-centre taps run in pairs on the packed FP32 pipe
+// (atrous_weight2, packed accumulation of the four channels): each lane
+// performs the scalar operations of its tap with the same roundings, and the
+// taps still accumulate one after another in the order dx = -2..2 (outer),
+// dy = -2..2 (inner), so the sums are those of the one-tap-at-a-time loop
+// (atrous_weight) bit for bit.
+SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __restrict__ guide,
+                         const uint2* __restrict__ res_in, V3 cn, float cd, float& rf0, float& rf1, float& rf2,
+                         float& rf3) {
+    int xs[5];
+    size_t rows[5];
+#pragma unroll
+    for (int d = 0; d < 5; ++d) {
+        const int xx = x + (d - 2) * step, yy = y + (d - 2) * step;
+        xs[d] = xx < 0 ? 0 : (xx > W - 1 ? W - 1 : xx);
+        rows[d] = (size_t)(yy < 0 ? 0 : (yy > H - 1 ? H - 1 : yy)) * W;
+    }
+    // the four channel sums, two per packed register
+    float2 acc01 = make_float2(0.0f, 0.0f), acc23 = make_float2(0.0f, 0.0f);
+    auto accumulate = [&](float f, uint2 t) {
+        float a, b, c, e;
+        unpack_h4(t, a, b, c, e);
+        acc01 = fma2(f2s(f), make_float2(a, b), acc01);
+        acc23 = fma2(f2s(f), make_float2(c, e), acc23);
+    };
+    const float ncd = -cd;
+    const float2 cx = f2s(cn.x), cy = f2s(cn.y), cz = f2s(cn.z);
+#pragma unroll
+    for (int p = 0; p < 12; ++p) {   // taps t = 5 * (dx + 2) + (dy + 2); pairs (0,1) .. (10,11), (13,14) .. (23,24)
+        if (p == 6) accumulate(1.0f, ld_u2(res_in, rows[2] + xs[2]));   // the centre tap, weight 1
+        const int t = p < 6 ? 2 * p : 2 * p + 1;
+        const size_t j0 = rows[t % 5] + xs[t / 5], j1 = rows[(t + 1) % 5] + xs[(t + 1) / 5];
+        const float4 g0 = __ldg(guide + j0), g1 = __ldg(guide + j1);
+        const uint2 r0 = ld_u2(res_in, j0), r1 = ld_u2(res_in, j1);
+        const float2 f = atrous_weight2(cx, cy, cz, ncd, g0, g1);
+        accumulate(f.x, r0);
+        accumulate(f.y, r1);
+    }
+    rf0 = acc01.x; rf1 = acc01.y; rf2 = acc23.x; rf3 = acc23.y;
+}
+
+__global__ void __launch_bounds__(256, 5) atrous_kernel(int W, int H, int step, const float4* __restrict__ guide,
+                                                     const uint2* __restrict__ res_in, uint2* __restrict__ res_out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * W + x;
+    const float4 gc = __ldg(guide + i);
+    float rf0, rf1, rf2, rf3;
+    atrous_filter(x, y, W, H, step, guide, res_in, v3(gc.x, gc.y, gc.z), gc.w, rf0, rf1, rf2, rf3);
+    const float den = gmax(kEps, rf3);
+    res_out[i] = pack_h4(rf0 / den, rf1 / den, rf2 / den, 1.0f);
+}
+
+cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in,
+                          uint2* res_out, cudaStream_t s, dim3 block) {
+    if (block.x == 0) block = dim3(32, 8);
+    dim3 grid((W + block.x - 1) / block.x, (H + block.y - 1) / block.y);
+    atrous_kernel<<<grid, block, 0, s>>>(W, H, 1 << pass, guide, res_in, res_out);
+    return cudaGetLastError();
+}
+
+// Final pass (final = true): the filter above, then temporal reprojection
+// (vpl_pbr_gi_denoise.fs:336-429) and the composite screen + gi * illumAvg (:431).
+__global__ void __launch_bounds__(256, 5) denoise_final_kernel(DenoiseLaunch d) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = d.width, H = d.height;
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * W + x;
+    const float u = xdiv(float(x) + 0.5f, float(W)), v = xdiv(float(y) + 0.5f, float(H));
+    const float4 gc = __ldg(d.guide + i);
+    const V3 centerNormal = v3(gc.x, gc.y, gc.z);
+    const float centerDepth = gc.w;
+    float rf0, rf1, rf2, rf3;
+    atrous_filter(x, y, W, H, 1 << d.pass, d.guide, d.res_in, centerNormal, centerDepth, rf0, rf1, rf2, rf3);
+    const float den = gmax(kEps, rf3);
+    const V3 shadowFactor = v3(rf0 / den, rf1 / den, rf2 / den);
+    if (d.res_out) d.res_out[i] = pack_h4(shadowFactor.x, shadowFactor.y, shadowFactor.z, 1.0f);
+    // indirectIllumination: the gather colour output baseColor + 1e-5 as RGB16F
+    const uint32_t alb = __ldg(d.cur.albedo + i);
+    const V3 gi = v3(h2f(f2h(gmax(unorm8(alb, 0), 0.01f) + kEps)), h2f(f2h(gmax(unorm8(alb, 1), 0.01f) + kEps)),
+                     h2f(f2h(gmax(unorm8(alb, 2), 0.01f) + kEps)));
+    float s0, s1, s2, s3;
+    unpack_h4(ld_u2(d.hdr_in, i), s0, s1, s2, s3);
+    const V3 screen = v3(s0, s1, s2);
+    const uint32_t vel = __ldg(d.cur.velocity + i);
+    const float pu = xsub(u, h2f((uint16_t)(vel & 0xffffu))), pv = xsub(v, h2f((uint16_t)(vel >> 16)));
+    float historyAccum = h2f(__ldg(d.hist_prev + i));
+    float accumMultiplier = 1.0f;
+    const V3 currGi = shadowFactor;
+    // previous depth, normal and GI bilinearly at the reprojected uv: one set of
+    // texels and weights, each texel read once
+    const Bilinear q = bilinear_at(W, H, pu, pv);
+    const float* pd = d.prev_depth;
+    const float prevCenterDepth = bilinear_sum(q, __ldg(pd + q.o00), __ldg(pd + q.o10), __ldg(pd + q.o01),
+                                               __ldg(pd + q.o11));
+    const uint32_t n00 = __ldg(d.prev_normal + q.o00), n10 = __ldg(d.prev_normal + q.o10),
+                   n01 = __ldg(d.prev_normal + q.o01), n11 = __ldg(d.prev_normal + q.o11);
+    V3 pnv;
+    pnv.x = bilinear_sum(q, unorm8(n00, 0), unorm8(n10, 0), unorm8(n01, 0), unorm8(n11, 0));
+    pnv.y = bilinear_sum(q, unorm8(n00, 1), unorm8(n10, 1), unorm8(n01, 1), unorm8(n11, 1));
+    pnv.z = bilinear_sum(q, unorm8(n00, 2), unorm8(n10, 2), unorm8(n01, 2), unorm8(n11, 2));
+    const V3 prevCenterNormal = xnormalize(xsub3(xmul3(pnv, 2.0f), v3s(1.0f)));
+    float g00[4], g10[4], g01[4], g11[4];
+    unpack_h4(ld_u2(d.gi_prev, q.o00), g00[0], g00[1], g00[2], g00[3]);
+    unpack_h4(ld_u2(d.gi_prev, q.o10), g10[0], g10[1], g10[2], g10[3]);
+    unpack_h4(ld_u2(d.gi_prev, q.o01), g01[0], g01[1], g01[2], g01[3]);
+    unpack_h4(ld_u2(d.gi_prev, q.o11), g11[0], g11[1], g11[2], g11[3]);
+    const V3 prevGi = v3(bilinear_sum(q, g00[0], g10[0], g01[0], g11[0]), bilinear_sum(q, g00[1], g10[1], g01[1], g11[1]),
+                         bilinear_sum(q, g00[2], g10[2], g01[2], g11[2]));
+    const float currId = __ldg(d.cur.id + i);
+    const float prevId = __ldg(d.prev_id + (size_t)nearest_index(pv, H) * W + nearest_index(pu, W));
+    // the temporal decision: similarity against 0.99, exact in both builds
+    const float wn = gmax(0.0f, xdot(centerNormal, prevCenterNormal));
+    const float wz = expf_exact(-gabs(xsub(centerDepth, prevCenterDepth)));
+    const float wid = currId != prevId ? 0.0f : 1.0f;
+    float similarity = xmul(xmul(wn, wz), wid);
+    if (similarity < 0.99f) { similarity = 0.0f; accumMultiplier = 0.0f; }
+    historyAccum = gmin(xadd(1.0f, xmul(historyAccum, accumMultiplier)), d.fps);
+    const float maxAccumulationFactor = 1.0f / historyAccum;
+    const V3 illumAvg = vmix(prevGi, currGi, maxAccumulationFactor);
+    const V3 comb = screen + gi * illumAvg;
+    d.hdr_out[i] = pack_h4(comb.x, comb.y, comb.z, 1.0f);
+    d.gi_out[i] = pack_h4(illumAvg.x, illumAvg.y, illumAvg.z, 1.0f);
+    d.hist_out[i] = f2h(historyAccum);
+}
+
+cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s, dim3 block) {
+    if (block.x == 0) block = dim3(32, 8);
+    dim3 grid((d.width + block.x - 1) / block.x, (d.height + block.y - 1) / block.y);
+    denoise_final_kernel<<<grid, block, 0, s>>>(d);
+    return cudaGetLastError();
+}
+
+// ============================================================== deferred --
+struct DeferredParams {
+    int W, H;
+    ShadeConfig sc;
+    sgi_gbuffer g;
+    sgi_camera cam;
+    const sgi_point_light* points;
+    int num_points;
+    ShadowCasters casters;
+    sgi_csm csm;
+    uint2* out;
+};
+
+// pbr.fs:82-145: non-shadow-casting point lights + the directional light
+// with its CSM (INFINITE_LIGHTING_ENABLED).
+__global__ void __launch_bounds__(256, 4) deferred_pbr_csm_kernel(DeferredParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= p.W || y >= p.H) return;
+    const size_t i = (size_t)y * p.W + x;
+    ShadeParams sp{p.sc.min_roughness, p.sc.perceptual, p.sc.fog_density,
+                   {p.sc.fog_color[0], p.sc.fog_color[1], p.sc.fog_color[2]}, p.sc.point_ambient};
+    const float u = xdiv(float(x) + 0.5f, float(p.W)), v = xdiv(float(y) + 0.5f, float(p.H));
+    const V3 fragPos = world_from_depth(u, v, __ldg(p.g.depth + i), p.cam.inv_proj_view);
+    const V3 viewPos = v3(p.cam.view_position[0], p.cam.view_position[1], p.cam.view_position[2]);
+    const V3 viewMinusFrag = xsub3(viewPos, fragPos);
+    const V3 viewDir = normalize(viewMinusFrag);
+    const float viewDist = xlength(viewMinusFrag);   // decides the caster shadow quality
+    const uint32_t alb = __ldg(p.g.albedo + i);
+    const V3 baseColor = v3(unorm8(alb, 0), unorm8(alb, 1), unorm8(alb, 2));
+    const float albedoA = unorm8(alb, 3);
+    const V3 normal = decode_normal(__ldg(p.g.normal + i));
+    const uint32_t rma = __ldg(p.g.roughness_metallic_ambient + i);
+    const float roughness = unorm8(rma, 0), metallic = unorm8(rma, 1), rmeB = unorm8(rma, 2);
+    const float ambient = h2f(__ldg(p.g.ssao + i));
+    const uint32_t br = __ldg(p.g.base_reflectivity + i);
+    const float reflR = float(br & 0xffu) / 255.0f, reflG = float(br >> 8) / 255.0f;
+    const V3 emissive = v3(albedoA, reflG, rmeB);
+    V3 color = v3s(0.0f);
+    for (int l = 0; l < p.num_points; ++l) {
+        const float4* rec = reinterpret_cast<const float4*>(p.points + l);
+        const float4 lp4 = __ldg(rec), lc4 = __ldg(rec + 1), m4 = __ldg(rec + 2);
+        const V3 lp = v3(lp4.x, lp4.y, lp4.z), lc = v3(lc4.x, lc4.y, lc4.z);
+        const float distance = xlength(xsub3(lp, fragPos));
+        if (distance < m4.x) {
+            // calculatePointLighting2, pbr2.glsl:593-611
+            const V3 lightDir = lp - fragPos;
+            color = color + lighting_burley(lc, lightDir, viewDir, normal, baseColor, viewDist, length(lc) / 12.0f,
+                                            roughness, metallic, ambient, 1.0f - 0.0f, v3s(reflR),
+                                            quadratic_atten(lightDir), sp.point_ambient, sp);
+        }
+    }
+    // shadowCasters, pbr.fs:116-131
+    for (int l = 0; l < p.casters.count; ++l) {
+        const float4* rec = reinterpret_cast<const float4*>(p.casters.lights + l);
+        const float4 lp4 = __ldg(rec), lc4 = __ldg(rec + 1), m4 = __ldg(rec + 2);
+        const V3 lp = v3(lp4.x, lp4.y, lp4.z), lc = v3(lc4.x, lc4.y, lc4.z);
+        const float distance = xlength(xsub3(lp, fragPos));
+        if (distance < m4.x) {
+            float shadowFactor = 0.0f;
+            const sgi_atlas_entry entry = p.casters.entries[l];
+            if (viewDist < 150.0f)
+                shadowFactor = shadow_8samples(p.casters.atlas, entry, m4.y, fragPos, lp, xdot(xsub3(lp, fragPos), normal),
+                                               0.03f);
+            else if (viewDist < 750.0f)
+                shadowFactor = shadow_1sample(p.casters.atlas, entry, m4.y, fragPos, lp, xdot(xsub3(lp, fragPos), normal),
+                                              0.03f);
+            const V3 lightDir = lp - fragPos;
+            color = color + lighting_burley(lc, lightDir, viewDir, normal, baseColor, viewDist, length(lc) / 12.0f,
+                                            roughness, metallic, ambient, 1.0f - shadowFactor, v3s(reflR),
+                                            quadratic_atten(lightDir), sp.point_ambient, sp);
+        }
+    }
+    const V3 lightDir = v3(p.csm.light_direction[0], p.csm.light_direction[1], p.csm.light_direction[2]);
+    const V3 lightColor = v3(p.csm.light_color[0], p.csm.light_color[1], p.csm.light_color[2]);
+    const float shadowFactor = infinite_shadow(p.csm, fragPos, normal, true);
+    // calculateDirectionalLighting, pbr2.glsl:576-591, called with 1 - shadowFactor
+    color = color + lighting_burley(lightColor, lightDir, viewDir, normal, baseColor, viewDist, 0.0f, roughness,
+                                    metallic, ambient, 1.0f - (1.0f - shadowFactor), v3s(reflR), 1.0f, 0.0f, sp);
+    const V3 o = vmin(color + emissive * p.sc.emission_strength, kHalfMax);
+    p.out[i] = pack_h4(o.x, o.y, o.z, 1.0f);
+}
+
+cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
+                            const sgi_camera& cam, const sgi_point_light* points, int32_t num_points,
+                            const ShadowCasters& casters, const sgi_csm& csm, uint2* hdr_out, cudaStream_t s,
+                            dim3 block) {
+    DeferredParams p;
+    p.W = cfg.width; p.H = cfg.height; p.sc = sc; p.g = g; p.cam = cam; p.points = points;
+    p.num_points = num_points; p.casters = casters; p.csm = csm; p.out = hdr_out;
+    if (block.x == 0) block = dim3(32, 8);
+    dim3 grid((cfg.width + block.x - 1) / block.x, (cfg.height + block.y - 1) / block.y);
+    deferred_pbr_csm_kernel<<<grid, block, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace SGI_SHADE_NS
+}  // namespace sgi

@@ -292,9 +292,12 @@ class GiStage:
     def set_timing(self, on: bool):
         self._chk(self.lib.sgi_set_timing(self.ctx, 1 if on else 0))
 
-    def pass_times(self) -> list[float]:
-        arr = (C.c_float * abi.SGI_NUM_PASS_TIMES)()
-        self._chk(self.lib.sgi_get_pass_times(self.ctx, arr, abi.SGI_NUM_PASS_TIMES))
+    def pass_times(self, split: bool = False) -> list[float]:
+        """[vpl cull, direct, tile cull, gather, denoise] ms of the last timed frame; with split, also the
+        denoise pass's a-trous passes and its final pass."""
+        n = abi.SGI_NUM_PASS_TIMES_SPLIT if split else abi.SGI_NUM_PASS_TIMES
+        arr = (C.c_float * n)()
+        self._chk(self.lib.sgi_get_pass_times(self.ctx, arr, n))
         return list(arr)
 
     def launch_count(self) -> int:

@@ -81,3 +81,35 @@ def host_scene_from_device(ds, frames, cubes=True):
     csm = {k: ds.csm_depth[k].cpu().numpy() for k in frames}
     storage = ds.cube_storage.cpu().numpy() if cubes else None
     return O.HostScene.from_arrays(ds.scene, ds.w, g, csm, storage)
+
+
+class GpuSetup:
+    """A workload's inputs from the oracle's CPU ray caster, uploaded: G-buffers, CSMs, cube atlas, lights."""
+
+    def __init__(self, w, seed: int, **cfgkw):
+        import torch
+
+        from oracle import binding as O
+        from stratusgfx_gb300 import scene as S
+        from stratusgfx_gb300 import stage
+        self.w = w
+        self.sc = S.workload_scene(w, seed)
+        self.hs = O.HostScene(self.sc, w)
+        self.cfg = stage.workload_config(w, **cfgkw)
+        self.g = [upload_gbuffer(g) for g in self.hs.gbuffers]
+        self.csm_t = [torch.from_numpy(d).cuda() for d in self.hs.csm_depth]
+        self.csm = [stage.csm_struct(self.sc, k, self.csm_t[k].data_ptr(), w.csm_resolution)
+                    for k in range(len(self.sc.cameras))]
+        self.cube_t, self.cubes = upload_cubes(self.hs.cube_storage, w.cube_format, self.sc.layers_per_atlas)
+        self.vpls = torch.from_numpy(self.sc.vpls).cuda()
+        self.entries = torch.from_numpy(self.sc.entries).cuda()
+        self.points = torch.from_numpy(self.sc.points).cuda() if len(self.sc.points) else None
+
+    def stage(self, k=1, **cfgkw):
+        from stratusgfx_gb300 import stage
+        cfgkw.setdefault("debug_keep_passes", 1)
+        cfg = stage.workload_config(self.w, **cfgkw)
+        st = stage.GiStage(cfg)
+        st.set_lights(self.vpls, self.entries, self.points)
+        st.set_shadow_maps(self.csm[k], self.cubes)
+        return st, cfg

@@ -11,7 +11,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from helpers import assert_bit_exact, half4_to_f32, half_bits_equal, psnr, upload_cubes, upload_gbuffer
+from helpers import GpuSetup, assert_bit_exact, half4_to_f32, half_bits_equal, psnr
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -24,28 +24,7 @@ TIME = 1000.0
 FPS = 60.0
 
 
-class Setup:
-    def __init__(self, w: S.Workload, seed: int, **cfgkw):
-        self.w = w
-        self.sc = S.workload_scene(w, seed)
-        self.hs = O.HostScene(self.sc, w)
-        self.cfg = stage.workload_config(w, **cfgkw)
-        self.g = [upload_gbuffer(g) for g in self.hs.gbuffers]
-        self.csm_t = [torch.from_numpy(d).cuda() for d in self.hs.csm_depth]
-        self.csm = [stage.csm_struct(self.sc, k, self.csm_t[k].data_ptr(), w.csm_resolution)
-                    for k in range(len(self.sc.cameras))]
-        self.cube_t, self.cubes = upload_cubes(self.hs.cube_storage, w.cube_format, self.sc.layers_per_atlas)
-        self.vpls = torch.from_numpy(self.sc.vpls).cuda()
-        self.entries = torch.from_numpy(self.sc.entries).cuda()
-        self.points = torch.from_numpy(self.sc.points).cuda() if len(self.sc.points) else None
-
-    def stage(self, k=1, **cfgkw):
-        cfgkw.setdefault("debug_keep_passes", 1)
-        cfg = stage.workload_config(self.w, **cfgkw)
-        st = stage.GiStage(cfg)
-        st.set_lights(self.vpls, self.entries, self.points)
-        st.set_shadow_maps(self.csm[k], self.cubes)
-        return st, cfg
+Setup = GpuSetup
 
 
 @pytest.fixture(scope="module")

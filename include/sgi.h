@@ -115,7 +115,7 @@ typedef struct sgi_config {
     int32_t height;                /* viewport height in pixels */
     int32_t max_vpls;              /* capacity of sgi_set_lights (<= 10000) */
     int32_t max_visible;           /* cap of the compacted list (reference 4480) */
-    int32_t tile_size;             /* tile edge in pixels, 8..32 (reference 5, configs 16) */
+    int32_t tile_size;             /* tile edge in pixels, 4..32 (reference and default 5, configs 16) */
     int32_t max_vpls_per_tile;     /* L, 1..64 (reference 12) */
     int32_t gi_mode;               /* SGI_GI_REFERENCE or SGI_GI_TILED */
     int32_t samples_per_pixel;     /* 0 = reference adaptive 2..10 (vpl_pbr_gi.fs:138-143), else fixed K */

@@ -250,8 +250,17 @@ template <class T> inline T butterfly_sum(T* a, int n) {
     }
     return a[0];
 }
-template <class T> inline T block_sum(std::vector<T>& vals) {   // vals.size() = tile_size^2 (64, 256 or 1024)
+// tile_size^2 = 32 x (a power of two) (tile sizes 8, 16, 32): the butterfly
+// order above; otherwise (e.g. the reference's 5x5 tiles) the sequential sum of
+// vpl_tiled_deferred_culling_stage1.cs:73-81, from 0 in the order of the pixels.
+inline bool butterfly_tile(int n) { return n % 32 == 0 && ((n / 32) & (n / 32 - 1)) == 0; }
+template <class T> inline T block_sum(std::vector<T>& vals) {
     int n = (int)vals.size();
+    if (!butterfly_tile(n)) {
+        T acc = T(0);
+        for (int i = 0; i < n; ++i) acc = acc + vals[i];
+        return acc;
+    }
     int nw = n / 32;
     std::vector<T> w(nw);
     for (int k = 0; k < nw; ++k) w[k] = butterfly_sum(&vals[k * 32], 32);

@@ -79,7 +79,7 @@ def config_defaults(width: int, height: int) -> Config:
     cfg.width, cfg.height = width, height
     cfg.max_vpls = SGI_MAX_VPLS_BEFORE_CULL
     cfg.max_visible = SGI_MAX_VPLS_PER_FRAME
-    cfg.tile_size = 16
+    cfg.tile_size = 5
     cfg.max_vpls_per_tile = 12
     cfg.gi_mode = SGI_GI_REFERENCE
     cfg.samples_per_pixel = 0

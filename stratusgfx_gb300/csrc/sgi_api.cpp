@@ -60,8 +60,8 @@ sgi_status validate_config(const sgi_config* cfg, std::string& why) {
     if (cfg->max_visible < 1 || cfg->max_visible > SGI_MAX_VPLS_BEFORE_CULL) {
         why = "max_visible must be in [1, 10000]"; return SGI_ERR_ARG;
     }
-    if (cfg->tile_size != 8 && cfg->tile_size != 16 && cfg->tile_size != 32) {
-        why = "tile_size must be 8, 16 or 32"; return SGI_ERR_ARG;
+    if (cfg->tile_size < 4 || cfg->tile_size > 32) {
+        why = "tile_size must be in [4, 32]"; return SGI_ERR_ARG;
     }
     if (cfg->max_vpls_per_tile < 1 || cfg->max_vpls_per_tile > SGI_MAX_TILE_LIST) {
         why = "max_vpls_per_tile must be in [1, 64]"; return SGI_ERR_ARG;
@@ -97,7 +97,7 @@ sgi::ShadeConfig make_shade(const sgi_config& c) {
 void free_all(sgi_ctx* c) {
     void* ptrs[] = {c->vpls, c->entries, c->points, c->shadow_points, c->shadow_entries, c->taa_hist[0],
                     c->taa_hist[1], c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
-                    c->tile_keys, c->reservoir, c->ping[0], c->ping[1], c->merged, c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
+                    c->vpr, c->reservoir, c->ping[0], c->ping[1], c->merged, c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
                     c->hist_depth[0], c->hist_depth[1]};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto* p : c->pass_bufs) if (p) cudaFree(p);
@@ -144,8 +144,8 @@ void sgi_config_defaults(sgi_config* cfg, int32_t width, int32_t height) {
     cfg->height = height;
     cfg->max_vpls = SGI_MAX_VPLS_BEFORE_CULL;
     cfg->max_visible = SGI_MAX_VPLS_PER_FRAME;
-    cfg->tile_size = 16;
-    cfg->max_vpls_per_tile = 12;
+    cfg->tile_size = 5;                 // VirtualPointLightData::tileXDivisor, StratusRendererBackend.h:346-347
+    cfg->max_vpls_per_tile = 12;        // MAX_VPLS_PER_TILE, vpl_common.glsl:9
     cfg->gi_mode = SGI_GI_REFERENCE;
     cfg->samples_per_pixel = 0;
     cfg->denoise_passes = 4;
@@ -192,7 +192,7 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     chk(dalloc(&c->visible_index, 1 + (size_t)cfg->max_vpls));
     chk(dalloc(&c->stage1, c->num_tiles));
     chk(dalloc(&c->lists, (size_t)c->num_tiles * (1 + cfg->max_vpls_per_tile)));
-    chk(dalloc(&c->tile_keys, (size_t)c->num_tiles * (size_t)((cfg->max_visible + 31) & ~31)));
+    chk(dalloc(&c->vpr, (size_t)cfg->max_visible));
     chk(dalloc(&c->reservoir, cfg->debug_keep_passes ? P : 1));
     chk(dalloc(&c->guide, P));
     chk(dalloc(&c->ping[0], P));
@@ -320,10 +320,11 @@ sgi_status sgi_cull_tiles(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camer
     if (!gbuffer_ok(gbuf, false) || !cam) return fail(ctx, SGI_ERR_ARG, "NULL G-buffer depth/normal or camera");
     if (!ctx->culled) return fail(ctx, SGI_ERR_STATE, "sgi_cull_vpls must run before sgi_cull_tiles");
     cudaStream_t s = (cudaStream_t)stream;
-    SGI_CUDA(ctx, sgi::launch_tile_stage1(ctx->cfg, *gbuf, *cam, ctx->stage1, s), "tile_stage1");
-    SGI_CUDA(ctx, sgi::launch_tile_stage2(ctx->cfg, ctx->stage1, ctx->cv, ctx->visible_index, ctx->tile_keys,
-                                          ctx->lists, s), "tile_stage2");
-    ctx->launches += 3;
+    SGI_CUDA(ctx, sgi::launch_tile_stage1(ctx->cfg, *gbuf, *cam, ctx->stage1, ctx->cv, ctx->visible_index, ctx->vpr,
+                                          s), "tile_stage1");
+    SGI_CUDA(ctx, sgi::launch_tile_stage2(ctx->cfg, ctx->stage1, ctx->vpr, ctx->visible_index, ctx->lists, s),
+             "tile_stage2");
+    ctx->launches += 2;
     return SGI_OK;
 }
 

@@ -35,7 +35,7 @@ struct sgi_ctx {
     int32_t* visible_index = nullptr;
     sgi_tile_stage1* stage1 = nullptr;
     int32_t* lists = nullptr;
-    uint32_t* tile_keys = nullptr;
+    float4* vpr = nullptr;            // (position, radius) of the compacted VPLs, for the tile cull
     int32_t num_tiles = 0;
     bool culled = false;
 

@@ -242,20 +242,36 @@ cudaError_t launch_compact(const sgi_vpl* vpls, const sgi_atlas_entry* entries, 
 
 // ============================================================ tile cull --
 // Stage 1: one block per tile (tile_size^2 threads). Per-tile mean world
-// position and normalised mean normal; the sums use the warp butterfly order
-// (xor 16, 8, 4, 2, 1, then xor nw/2 .. 1 over the warp totals).
+// position and normalised mean normal. For tile sizes 8, 16 and 32 (a power of
+// two number of warps) the sums use the warp butterfly order (xor 16, 8, 4, 2,
+// 1, then xor nw/2 .. 1 over the warp totals); otherwise (e.g. the reference's
+// 5x5 tiles) thread 0 adds the pixels in their order in the tile, as
+// vpl_tiled_deferred_culling_stage1.cs:73-81 does. Pixels outside the image add 0 and are left out of the count.
+// The kernel also packs (position, radius) of the compacted VPLs into `vpr`
+// (16 bytes per VPL) for stage 2, which reads them once per tile.
 SGI_D float butterfly(float v) {
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, off);
     return v;
 }
 
-__global__ void tile_stage1_kernel(int W, int H, int ts, int tiles_x, sgi_gbuffer g, sgi_camera cam,
-                                   sgi_tile_stage1* __restrict__ out) {
+__global__ void tile_stage1_kernel(int W, int H, int ts, int tiles_x, int num_tiles, sgi_gbuffer g, sgi_camera cam,
+                                   sgi_tile_stage1* __restrict__ out, const sgi_vpl* __restrict__ cv,
+                                   const int32_t* __restrict__ visible_index, float4* __restrict__ vpr) {
     __shared__ float wsum[32][6];
+    extern __shared__ float seq[];   // [tile_size^2][6], only for the sequential sum
     const int tile = blockIdx.x;
     const int tx = tile % tiles_x, ty = tile / tiles_x;
     const int l = threadIdx.x;
+    const int nthreads = ts * ts;
+    {   // (position, radius) of the compacted VPLs, strided over all blocks
+        const int count = __ldg(visible_index);
+        for (int k = tile * nthreads + l; k < count; k += num_tiles * nthreads) {
+            const float4 pos = __ldg(reinterpret_cast<const float4*>(cv + k));
+            const float radius = __ldg(reinterpret_cast<const float*>(cv + k) + 12);
+            vpr[k] = make_float4(pos.x, pos.y, pos.z, radius);
+        }
+    }
     const int x = tx * ts + l % ts, y = ty * ts + l / ts;
     float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (x < W && y < H) {
@@ -265,59 +281,84 @@ __global__ void tile_stage1_kernel(int W, int H, int ts, int tiles_x, sgi_gbuffe
         V3 n = decode_normal(__ldg(g.normal + i));
         v[0] = p.x; v[1] = p.y; v[2] = p.z; v[3] = n.x; v[4] = n.y; v[5] = n.z;
     }
-    const int lane = l & 31, warp = l >> 5, nw = (ts * ts) >> 5;
+    float w[6];
+    bool have = false;
+    const bool butterfly_order = (nthreads & 31) == 0 && (((nthreads >> 5) & ((nthreads >> 5) - 1)) == 0);
+    if (butterfly_order) {
+        const int lane = l & 31, warp = l >> 5, nw = nthreads >> 5;
 #pragma unroll
-    for (int c = 0; c < 6; ++c) v[c] = butterfly(v[c]);
-    if (lane == 0) {
-#pragma unroll
-        for (int c = 0; c < 6; ++c) wsum[warp][c] = v[c];
-    }
-    __syncthreads();
-    if (warp == 0) {
-        float w[6];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) w[c] = lane < nw ? wsum[lane][c] : 0.0f;
-        for (int off = nw >> 1; off >= 1; off >>= 1) {
-#pragma unroll
-            for (int c = 0; c < 6; ++c) w[c] = w[c] + __shfl_xor_sync(0xffffffffu, w[c], off);
-        }
+        for (int c = 0; c < 6; ++c) v[c] = butterfly(v[c]);
         if (lane == 0) {
-            int cx = W - tx * ts < ts ? W - tx * ts : ts;
-            int cy = H - ty * ts < ts ? H - ty * ts : ts;
-            float cnt = float(cx * cy);
-            V3 ap = v3(w[0], w[1], w[2]) / cnt;
-            V3 an = v3(w[3], w[4], w[5]) / cnt;
-            an = normalize(an);
-            sgi_tile_stage1 o;
-            o.average_position[0] = ap.x; o.average_position[1] = ap.y; o.average_position[2] = ap.z;
-            o.average_position[3] = 1.0f;
-            o.average_normal[0] = an.x; o.average_normal[1] = an.y; o.average_normal[2] = an.z;
-            o.average_normal[3] = 1.0f;
-            out[tile] = o;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) wsum[warp][c] = v[c];
         }
+        __syncthreads();
+        if (warp == 0) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) w[c] = lane < nw ? wsum[lane][c] : 0.0f;
+            for (int off = nw >> 1; off >= 1; off >>= 1) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) w[c] = w[c] + __shfl_xor_sync(0xffffffffu, w[c], off);
+            }
+            have = lane == 0;
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) seq[l * 6 + c] = v[c];
+        __syncthreads();
+        if (l == 0) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) w[c] = 0.0f;
+            for (int j = 0; j < nthreads; ++j) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) w[c] = w[c] + seq[j * 6 + c];
+            }
+            have = true;
+        }
+    }
+    if (have) {
+        int cx = W - tx * ts < ts ? W - tx * ts : ts;
+        int cy = H - ty * ts < ts ? H - ty * ts : ts;
+        float cnt = float(cx * cy);
+        V3 ap = v3(w[0], w[1], w[2]) / cnt;
+        V3 an = v3(w[3], w[4], w[5]) / cnt;
+        an = normalize(an);
+        sgi_tile_stage1 o;
+        o.average_position[0] = ap.x; o.average_position[1] = ap.y; o.average_position[2] = ap.z;
+        o.average_position[3] = 1.0f;
+        o.average_normal[0] = an.x; o.average_normal[1] = an.y; o.average_normal[2] = an.z;
+        o.average_normal[3] = 1.0f;
+        out[tile] = o;
     }
 }
 
 cudaError_t launch_tile_stage1(const sgi_config& cfg, const sgi_gbuffer& g, const sgi_camera& cam,
-                               sgi_tile_stage1* out, cudaStream_t s) {
+                               sgi_tile_stage1* out, const sgi_vpl* cv, const int32_t* visible_index, float4* vpr,
+                               cudaStream_t s) {
     const int ts = cfg.tile_size;
     const int tx = (cfg.width + ts - 1) / ts, ty = (cfg.height + ts - 1) / ts;
-    tile_stage1_kernel<<<tx * ty, ts * ts, 0, s>>>(cfg.width, cfg.height, ts, tx, g, cam, out);
+    const int nw = (ts * ts) >> 5;
+    const bool butterfly_order = ((ts * ts) & 31) == 0 && (nw & (nw - 1)) == 0;
+    const size_t seq_bytes = butterfly_order ? 0 : sizeof(float) * 6 * ts * ts;
+    tile_stage1_kernel<<<tx * ty, ts * ts, seq_bytes, s>>>(cfg.width, cfg.height, ts, tx, tx * ty, g, cam, out, cv,
+                                                          visible_index, vpr);
     return cudaGetLastError();
 }
 
-// Stage 2: one warp per tile. vpl_tiled_deferred_culling_stage2.cs:61-129
-// inserts the visible VPLs, in order, into a list sorted by key =
+// Stage 2, vpl_tiled_deferred_culling_stage2.cs:61-129: for each tile the
+// shader inserts the visible VPLs, in order, into a list sorted by key =
 // distance / radius with a strict '<' (ties keep the earlier VPL) and keeps
-// the first L: the result is the first L entries of the stable sort of the
-// candidates by key. This kernel computes that set without the sequential
-// insertions, whose number depends on the VPL order:
-//   1. every candidate's key (as an order-preserving uint) goes to shared memory;
-//   2. if there are more than L candidates, a 4-round radix select (8 bits per
-//      round) finds the L-th smallest key tau and how many keys equal to tau
-//      are still needed;
-//   3. keys < tau, then the needed keys == tau in index order, are compacted;
-//   4. a 64-element warp bitonic sort orders them by (key, index).
+// the first L. The result is the L smallest candidates by (key, index), in
+// that order. One 256-thread block per tile computes that set with the keys
+// in shared memory (nothing per (tile, VPL) reaches global memory):
+//   1. every visible VPL's key (kNoKey when it is not a candidate) goes to
+//      shared memory, and each candidate counts into a 256-bin histogram of
+//      floor(ratio * 256) (ratio <= 1; the bins are ordered like the keys);
+//   2. with more than L candidates, a block scan of the histogram finds the
+//      bin b where the count reaches L: every candidate of a lower bin is
+//      kept, and from bin b the need = L - (candidates below b) smallest by
+//      (key, index), found by ranking bin b's members against each other;
+//   3. the kept (key, index) pairs, at most 64, are sorted by one warp.
 constexpr uint32_t kNoKey = 0xffffffffu;
 
 SGI_D uint32_t order_key(float k) {     // float order -> uint order (-0 == +0)
@@ -325,189 +366,156 @@ SGI_D uint32_t order_key(float k) {     // float order -> uint order (-0 == +0)
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
-SGI_D bool key_less(uint32_t ka, int ia, uint32_t kb, int ib) { return ka < kb || (ka == kb && ia < ib); }
+// the histogram bin of a candidate's ratio (<= 1): non-decreasing in the ratio
+SGI_D int ratio_bin(float ratio) {
+    if (!(ratio > 0.0f)) return 0;
+    const int b = (int)(ratio * 256.0f);
+    return b > 255 ? 255 : b;
+}
+
+SGI_D unsigned long long pair_key(uint32_t key, int index) {
+    return ((unsigned long long)key << 32) | (uint32_t)index;
+}
 
 // One compare-exchange stage of a bitonic network over 64 elements held as
-// (k0, i0) at position lane and (k1, i1) at position lane + 32.
-SGI_D void bitonic_stage(uint32_t& k0, int& i0, uint32_t& k1, int& i1, int size, int j, int lane) {
+// k0 at position lane and k1 at position lane + 32.
+SGI_D void bitonic_stage64(unsigned long long& k0, unsigned long long& k1, int size, int j, int lane) {
     const unsigned FULL = 0xffffffffu;
-    if (j == 32) {
-        // partners are the two registers of this lane; size == 64 -> ascending
-        if (key_less(k1, i1, k0, i0)) { uint32_t tk = k0; int ti = i0; k0 = k1; i0 = i1; k1 = tk; i1 = ti; }
+    if (j == 32) {   // partners are the two registers of this lane; size == 64 -> ascending
+        if (k1 < k0) { const unsigned long long t = k0; k0 = k1; k1 = t; }
         return;
     }
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
-        uint32_t& k = r ? k1 : k0;
-        int& id = r ? i1 : i0;
+        unsigned long long& k = r ? k1 : k0;
         const int pos = lane + 32 * r;
-        const uint32_t ok = __shfl_xor_sync(FULL, k, j);
-        const int oi = __shfl_xor_sync(FULL, id, j);
+        const unsigned long long o = __shfl_xor_sync(FULL, k, j);
         const bool ascending = (pos & size) == 0;
         const bool lower = (pos & j) == 0;
-        const bool other_less = key_less(ok, oi, k, id);
         // the lower position keeps the min when ascending, the max otherwise
-        const bool take_other = (lower == ascending) ? other_less : !other_less;
-        if (take_other) { k = ok; id = oi; }
+        if ((lower == ascending) ? (o < k) : (k < o)) k = o;
     }
 }
 
-// 2a. keys: a block takes kKeyTiles tiles; its threads stride over the visible
-// VPLs (the count lives on the device, so the grid cannot be sized by it), read
-// each VPL's position and radius once and write its key for every tile of the
-// block: keys[tile][k] in global memory (L2-resident), kNoKey when the VPL is
-// not a candidate. Reading the VPL records once per block instead of once per
-// tile cuts the L2 traffic of this pass by kKeyTiles.
-constexpr int kKeyTiles = 8;
-__global__ void __launch_bounds__(256) tile_keys_kernel(int num_tiles, int key_stride,
-                                                        const sgi_tile_stage1* __restrict__ s1,
-                                                        const sgi_vpl* __restrict__ cv,
-                                                        const int32_t* __restrict__ visible_index,
-                                                        uint32_t* __restrict__ keys) {
-    __shared__ float4 tile_p[kKeyTiles], tile_n[kKeyTiles];
+constexpr int kCullThreads = 256;
+
+__global__ void __launch_bounds__(kCullThreads) tile_cull_kernel(int L, const sgi_tile_stage1* __restrict__ s1,
+                                                                 const float4* __restrict__ vpr,
+                                                                 const int32_t* __restrict__ visible_index,
+                                                                 int32_t* __restrict__ lists) {
+    extern __shared__ uint32_t cull_smem[];   // keys[count], then bin-b member indices[count]
+    __shared__ uint32_t hist[256];
+    __shared__ unsigned long long kept[64];
+    __shared__ int warp_sum[kCullThreads / 32];
+    __shared__ int s_bin, s_need, s_nkept, s_nb, s_mc;
+    const int tile = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int count = __ldg(visible_index);
-    const int t0 = blockIdx.x * kKeyTiles;
-    const int nt = min(kKeyTiles, num_tiles - t0);
-    if (threadIdx.x < nt) {
-        tile_p[threadIdx.x] = __ldg(reinterpret_cast<const float4*>(s1 + t0 + threadIdx.x));
-        tile_n[threadIdx.x] = __ldg(reinterpret_cast<const float4*>(s1 + t0 + threadIdx.x) + 1);
+    uint32_t* keys = cull_smem;
+    uint32_t* members = cull_smem + count;
+    hist[tid] = 0u;
+    if (tid == 0) { s_nkept = 0; s_nb = 0; }
+    const float4 p4 = __ldg(reinterpret_cast<const float4*>(s1 + tile));
+    const float4 n4 = __ldg(reinterpret_cast<const float4*>(s1 + tile) + 1);
+    const V3 tp = v3(p4.x, p4.y, p4.z), tn = v3(n4.x, n4.y, n4.z);
+    __syncthreads();
+    int mine = 0;
+    for (int k = tid; k < count; k += kCullThreads) {
+        const float4 v = __ldg(vpr + k);
+        const V3 lmf = v3(v.x, v.y, v.z) - tp;
+        const float side = dot(tn, lmf);
+        uint32_t u = kNoKey;
+        if (!(side < 0.0f)) {
+            const float ratio = length(lmf) / v.w;
+            if (!(ratio > 1.0f) && ratio < kFloatMax) {
+                u = order_key(ratio);
+                ++mine;
+                atomicAdd(&hist[ratio_bin(ratio)], 1u);
+            }
+        }
+        keys[k] = u;
+    }
+    // candidates in the tile
+    for (int off = 16; off >= 1; off >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, off);
+    if (lane == 0) warp_sum[warp] = mine;
+    __syncthreads();
+    if (tid == 0) {
+        int mc = 0;
+        for (int w = 0; w < kCullThreads / 32; ++w) mc += warp_sum[w];
+        s_mc = mc;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < count; k += blockDim.x) {
-        const float* rec = reinterpret_cast<const float*>(cv + k);
-        const V3 lp = v3(__ldg(rec + 0), __ldg(rec + 1), __ldg(rec + 2));
-        const float radius = __ldg(rec + 12);
-        for (int j = 0; j < nt; ++j) {
-            const float4 p4 = tile_p[j], n4 = tile_n[j];
-            const V3 lmf = lp - v3(p4.x, p4.y, p4.z);
-            const float side = dot(v3(n4.x, n4.y, n4.z), lmf);
-            uint32_t u = kNoKey;
-            if (!(side < 0.0f)) {
-                const float ratio = length(lmf) / radius;
-                if (!(ratio > 1.0f) && ratio < kFloatMax) u = order_key(ratio);
-            }
-            keys[(size_t)(t0 + j) * key_stride + k] = u;
-        }
-    }
-}
-
-// 2b. select: one warp per tile over its keys.
-__global__ void __launch_bounds__(256) tile_select_kernel(int num_tiles, int L, int key_stride,
-                                                          const uint32_t* __restrict__ all_keys,
-                                                          const int32_t* __restrict__ visible_index,
-                                                          int32_t* __restrict__ lists) {
-    __shared__ uint32_t hist_all[8][256];
-    __shared__ uint32_t sel_all[8][128];
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tile = blockIdx.x * 8 + warp;
-    if (tile >= num_tiles) return;     // warps are independent: no block-wide barrier below
-    uint32_t* hist = hist_all[warp];
-    uint32_t* sel_k = sel_all[warp];
-    int* sel_i = reinterpret_cast<int*>(sel_k + 64);
-    const uint32_t* keys = all_keys + (size_t)tile * key_stride;
-    const unsigned lt_mask = (1u << lane) - 1u;
-    const int count = __ldg(visible_index);
-
-    int mc = 0;
-    for (int base = 0; base < count; base += 32) {
-        const int k = base + lane;
-        const uint32_t u = k < count ? __ldg(keys + k) : kNoKey;
-        mc += __popc(__ballot_sync(FULL, u != kNoKey));
-    }
+    const int mc = s_mc;
     const int take = mc < L ? mc : L;
-
-    // radix select of the take-th smallest key
-    uint32_t tau = kNoKey;
-    int need_eq = 0;
     if (mc > L) {
-        uint32_t prefix = 0u, mask = 0u;
-        int remaining = L;
-        for (int shift = 24; shift >= 0; shift -= 8) {
-            for (int b = lane; b < 256; b += 32) hist[b] = 0u;
-            __syncwarp();
-            for (int k = lane; k < count; k += 32) {
-                const uint32_t u = __ldg(keys + k);
-                if (u != kNoKey && (u & mask) == prefix) atomicAdd(&hist[(u >> shift) & 0xffu], 1u);
-            }
-            __syncwarp();
-            uint32_t hv[8];
-            uint32_t sum = 0u;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) { hv[j] = hist[lane * 8 + j]; sum += hv[j]; }
-            uint32_t incl = sum;
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const uint32_t t = __shfl_up_sync(FULL, incl, off);
-                if (lane >= off) incl += t;
-            }
-            const unsigned found = __ballot_sync(FULL, incl >= (uint32_t)remaining);
-            const int src = __ffs(found) - 1;
-            int bin = 0;
-            uint32_t below = 0u;
-            if (lane == src) {
-                uint32_t c = incl - sum;
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    if (c + hv[j] >= (uint32_t)remaining) { bin = lane * 8 + j; below = c; break; }
-                    c += hv[j];
-                }
-            }
-            bin = __shfl_sync(FULL, bin, src);
-            below = __shfl_sync(FULL, below, src);
-            remaining -= (int)below;
-            prefix |= (uint32_t)bin << shift;
-            mask |= 0xffu << shift;
-            __syncwarp();
+        // inclusive scan of the histogram: bin b holds the L-th candidate
+        const uint32_t h = hist[tid];
+        uint32_t incl = h;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += t;
         }
-        tau = prefix;
-        need_eq = remaining;
+        if (lane == 31) warp_sum[warp] = (int)incl;
+        __syncthreads();
+        uint32_t before = 0;
+        for (int w = 0; w < warp; ++w) before += (uint32_t)warp_sum[w];
+        incl += before;
+        if (incl >= (uint32_t)L && incl - h < (uint32_t)L) { s_bin = tid; s_need = L - (int)(incl - h); }
+        __syncthreads();
+    } else if (tid == 0) {
+        s_bin = 256;   // every candidate is kept
+        s_need = 0;
     }
-
-    // compaction in index order: keys < tau, then the first need_eq keys == tau
-    int pos = 0, eq_seen = 0;
-    for (int base = 0; base < count && pos < take; base += 32) {
-        const int k = base + lane;
-        const uint32_t u = k < count ? __ldg(keys + k) : kNoKey;
-        const bool eq = u == tau && u != kNoKey;
-        const unsigned meq = __ballot_sync(FULL, eq);
-        const int eq_rank = eq_seen + __popc(meq & lt_mask);
-        const bool sel = (u < tau) || (eq && eq_rank < need_eq);
-        const unsigned ms = __ballot_sync(FULL, sel);
-        if (sel) {
-            const int p = pos + __popc(ms & lt_mask);
-            sel_k[p] = u;
-            sel_i[p] = k;
+    __syncthreads();
+    const int bin = s_bin;
+    // kept: candidates of lower bins; bin b's members are ranked below
+    for (int k = tid; k < count; k += kCullThreads) {
+        const uint32_t u = keys[k];
+        if (u == kNoKey) continue;
+        const int b = ratio_bin(__uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u));
+        if (b < bin) kept[atomicAdd(&s_nkept, 1)] = pair_key(u, k);
+        else if (b == bin) members[atomicAdd(&s_nb, 1)] = (uint32_t)k;
+    }
+    __syncthreads();
+    if (mc > L) {
+        const int nb = s_nb, need = s_need;
+        for (int m = tid; m < nb; m += kCullThreads) {
+            const uint32_t k = members[m];
+            const unsigned long long mk = pair_key(keys[k], (int)k);
+            int rank = 0;
+            for (int j = 0; j < nb; ++j) {
+                const uint32_t kj = members[j];
+                rank += pair_key(keys[kj], (int)kj) < mk ? 1 : 0;
+            }
+            if (rank < need) kept[atomicAdd(&s_nkept, 1)] = mk;
         }
-        pos += __popc(ms);
-        eq_seen += __popc(meq);
+        __syncthreads();
     }
-    __syncwarp();
-
-    // sort (key, index) ascending
-    uint32_t k0 = lane < take ? sel_k[lane] : kNoKey;
-    int i0 = lane < take ? sel_i[lane] : 0x7fffffff;
-    uint32_t k1 = lane + 32 < take ? sel_k[lane + 32] : kNoKey;
-    int i1 = lane + 32 < take ? sel_i[lane + 32] : 0x7fffffff;
-    if (take > 1) {
-        for (int size = 2; size <= 64; size <<= 1)
-            for (int j = size >> 1; j >= 1; j >>= 1) bitonic_stage(k0, i0, k1, i1, size, j, lane);
+    if (warp == 0) {
+        unsigned long long k0 = lane < take ? kept[lane] : ~0ull;
+        unsigned long long k1 = lane + 32 < take ? kept[lane + 32] : ~0ull;
+        if (take > 1) {
+            for (int size = 2; size <= 64; size <<= 1)
+                for (int j = size >> 1; j >= 1; j >>= 1) bitonic_stage64(k0, k1, size, j, lane);
+        }
+        int32_t* o = lists + (size_t)tile * (1 + L);
+        if (lane == 0) o[0] = take;
+        if (lane < L) o[1 + lane] = lane < take ? (int32_t)(uint32_t)k0 : -1;
+        if (lane + 32 < L) o[33 + lane] = lane + 32 < take ? (int32_t)(uint32_t)k1 : -1;
     }
-    int32_t* o = lists + (size_t)tile * (1 + L);
-    if (lane == 0) o[0] = take;
-    if (lane < L) o[1 + lane] = lane < take ? i0 : -1;
-    if (lane + 32 < L) o[33 + lane] = lane + 32 < take ? i1 : -1;
 }
 
-cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1, const sgi_vpl* cv,
-                               const int32_t* visible_index, uint32_t* keys, int32_t* lists, cudaStream_t s) {
+size_t tile_cull_smem(const sgi_config& cfg) { return (size_t)2 * sizeof(uint32_t) * (size_t)cfg.max_visible; }
+
+cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1, const float4* vpr,
+                               const int32_t* visible_index, int32_t* lists, cudaStream_t s) {
     const int ts = cfg.tile_size;
     const int T = ((cfg.width + ts - 1) / ts) * ((cfg.height + ts - 1) / ts);
-    const int key_stride = (cfg.max_visible + 31) & ~31;
-    tile_keys_kernel<<<(T + kKeyTiles - 1) / kKeyTiles, 256, 0, s>>>(T, key_stride, s1, cv, visible_index, keys);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    tile_select_kernel<<<(T + 7) / 8, 256, 0, s>>>(T, cfg.max_vpls_per_tile, key_stride, keys, visible_index, lists);
+    const size_t smem = tile_cull_smem(cfg);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(tile_cull_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    tile_cull_kernel<<<T, kCullThreads, smem, s>>>(cfg.max_vpls_per_tile, s1, vpr, visible_index, lists);
     return cudaGetLastError();
 }
 

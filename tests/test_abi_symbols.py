@@ -44,6 +44,7 @@ def test_config_defaults_are_the_reference_settings():
     assert cfg.use_perceptual_roughness == 1               # :194
     assert cfg.denoise_passes == 4                         # StratusRendererBackend.cpp:1914
     assert cfg.max_visible == 4480 and cfg.max_vpls == 10000
+    assert cfg.tile_size == 5 and cfg.max_vpls_per_tile == 12   # StratusRendererBackend.h:346-347, vpl_common.glsl:9
     assert lib.sgi_abi_version() == 1
 
 
@@ -59,7 +60,7 @@ def test_python_config_defaults_equal_the_library_defaults():
 def test_create_rejects_bad_configs_before_touching_the_device():
     lib = abi.load(build_if_missing=True)
     h = C.c_void_p()
-    for field, val in [("tile_size", 5), ("max_vpls_per_tile", 65), ("denoise_passes", 1), ("width", 0),
+    for field, val in [("tile_size", 3), ("tile_size", 33), ("max_vpls_per_tile", 65), ("denoise_passes", 1), ("width", 0),
                        ("gi_mode", 3), ("max_vpls", 10001)]:
         cfg = abi.Config()
         lib.sgi_config_defaults(C.byref(cfg), 64, 48)

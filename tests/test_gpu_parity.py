@@ -123,7 +123,7 @@ def test_tile_cull_bit_exact(small):
     assert np.array_equal(lists, ref2), "tile stage 2 lists"
 
 
-@pytest.mark.parametrize("L,ts", [(1, 16), (12, 8), (33, 32), (64, 16)])
+@pytest.mark.parametrize("L,ts", [(1, 16), (12, 8), (33, 32), (64, 16), (12, 5), (64, 4), (20, 24)])
 def test_tile_lists_variants(small, L, ts):
     st, cfg = small.stage(1, max_vpls_per_tile=L, tile_size=ts)
     st.cull_vpls()
@@ -135,6 +135,44 @@ def test_tile_lists_variants(small, L, ts):
     ref2 = O.tile_stage2(32, cfg, ref1, small.sc.vpls[idx[1:1 + cnt]], cnt)
     lists = st.read_debug(abi.SGI_DEBUG_TILE_LISTS, np.int32).reshape(-1, 1 + L)
     assert np.array_equal(lists, ref2)
+    st.close()
+
+
+def test_tile_lists_with_tied_keys():
+    """Groups of VPLs at the same position with the same radius: equal keys, which the
+    reference's strict '<' insertion keeps in index order; with L = 12 the cut falls
+    inside a group of ties."""
+    w = S.Workload("room12_128x96_vpl600", 128, 96, 12, 600, 0, 512, 16, abi.SGI_CUBE_F32, 4, 3, 1)
+    s = Setup(w, 91)
+    v = s.sc.vpls.copy()
+    v[1::3, :3] = v[0::3, :3][: len(v[1::3])]    # every group of three shares one position
+    v[2::3, :3] = v[0::3, :3][: len(v[2::3])]
+    s.vpls = torch.from_numpy(v).cuda()
+    for L, ts in ((12, 16), (7, 5)):
+        st, cfg = s.stage(1, max_vpls_per_tile=L, tile_size=ts)
+        st.cull_vpls()
+        st.cull_tiles(s.g[1], s.hs.camera(1))
+        torch.cuda.synchronize()
+        idx = st.read_debug(abi.SGI_DEBUG_VISIBLE_INDEX, np.int32)
+        cnt = int(idx[0])
+        ref1 = O.tile_stage1(32, cfg, s.hs.gbuffers[1], s.hs.camera(1))
+        ref2 = O.tile_stage2(32, cfg, ref1, v[idx[1:1 + cnt]], cnt)
+        lists = st.read_debug(abi.SGI_DEBUG_TILE_LISTS, np.int32).reshape(-1, 1 + L)
+        assert (ref2[:, 0] == L).mean() > 0.5
+        assert np.array_equal(lists, ref2)
+        st.close()
+
+
+def test_reference_tile_preset_frame_bit_exact(small):
+    """The reference's tile constants: 5x5 tiles (StratusRendererBackend.h:346-347), 12 VPLs per tile
+    (vpl_common.glsl:9), the per-tile mean by the sequential sum of stage 1; tiled gather, whole frame."""
+    st, cfg, out = _run_frame(small, tile_size=5, max_vpls_per_tile=12)
+    H, W = cfg.height, cfg.width
+    ref = O.frame(32, cfg, small.hs, 1, np.zeros((H, W, 4), np.float32), np.zeros((H, W), np.float32), TIME, FPS)
+    lists = st.read_debug(abi.SGI_DEBUG_TILE_LISTS, np.int32).reshape(-1, 1 + 12)
+    assert lists.shape[0] == 64 * 36
+    assert np.array_equal(lists, ref["lists"])
+    assert_bit_exact(out.cpu().numpy().astype(np.float32)[..., :3], ref["combined"][..., :3], "5x5-tile frame HDR")
     st.close()
 
 
@@ -254,7 +292,7 @@ def test_abi_rejects_bad_arguments():
     lib = abi.load()
     cfg = stage.default_config(64, 48)
     h = C.c_void_p()
-    bad = stage.default_config(64, 48, tile_size=12)
+    bad = stage.default_config(64, 48, tile_size=40)
     assert lib.sgi_create(C.byref(bad), C.byref(h)) == abi.SGI_ERR_ARG
     abi.check(lib.sgi_create(C.byref(cfg), C.byref(h)))
     try:

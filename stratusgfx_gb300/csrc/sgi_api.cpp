@@ -281,7 +281,7 @@ sgi_status sgi_cull_vpls(sgi_ctx* ctx, void* stream) {
     } else {
         SGI_CUDA(ctx, sgi::launch_vis_flags(ctx->vpls, ctx->num_vpls, ctx->csm, ctx->flags, s), "vpl_vis_flags");
         SGI_CUDA(ctx, sgi::launch_compact(ctx->vpls, ctx->entries, ctx->flags, ctx->num_vpls, ctx->cfg.max_visible,
-                                          ctx->cv, ctx->ce, ctx->visible_index, s), "vpl_compact");
+                                          ctx->cv, ctx->ce, ctx->visible_index, ctx->vpr, s), "vpl_compact");
         ctx->launches += 2;
         if (ctx->coloring) {
             SGI_CUDA(ctx, sgi::launch_vpl_color(ctx->cv, ctx->ce, ctx->visible_index, ctx->cfg.max_visible,
@@ -310,7 +310,7 @@ sgi_status sgi_cull_vpls_noalloc(const sgi_vpl* vpls, const sgi_atlas_entry* ent
     if (sgi::noalloc_cull_flags(&flags) != cudaSuccess) return SGI_ERR_CUDA;
     if (sgi::launch_vis_flags(vpls, num_vpls, *csm, flags, s) != cudaSuccess) return SGI_ERR_CUDA;
     if (sgi::launch_compact(vpls, entries, flags, num_vpls, max_visible, visible_vpls, visible_entries, visible_index,
-                            s) != cudaSuccess)
+                            nullptr, s) != cudaSuccess)
         return SGI_ERR_CUDA;
     return SGI_OK;
 }
@@ -320,8 +320,7 @@ sgi_status sgi_cull_tiles(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camer
     if (!gbuffer_ok(gbuf, false) || !cam) return fail(ctx, SGI_ERR_ARG, "NULL G-buffer depth/normal or camera");
     if (!ctx->culled) return fail(ctx, SGI_ERR_STATE, "sgi_cull_vpls must run before sgi_cull_tiles");
     cudaStream_t s = (cudaStream_t)stream;
-    SGI_CUDA(ctx, sgi::launch_tile_stage1(ctx->cfg, *gbuf, *cam, ctx->stage1, ctx->cv, ctx->visible_index, ctx->vpr,
-                                          s), "tile_stage1");
+    SGI_CUDA(ctx, sgi::launch_tile_stage1(ctx->cfg, *gbuf, *cam, ctx->stage1, s), "tile_stage1");
     SGI_CUDA(ctx, sgi::launch_tile_stage2(ctx->cfg, ctx->stage1, ctx->vpr, ctx->visible_index, ctx->lists, s),
              "tile_stage2");
     ctx->launches += 2;

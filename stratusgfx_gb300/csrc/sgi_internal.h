@@ -62,12 +62,12 @@ cudaError_t launch_post_fx(int32_t W, int32_t H, const uint2* hdr, const uint32_
 cudaError_t launch_vpl_color(sgi_vpl* cv, const sgi_atlas_entry* ce, const int32_t* visible_index, int32_t cap,
                              const sgi_cube_atlas& cubes, const sgi_diffuse_atlas& diffuse, const sgi_csm& csm,
                              cudaStream_t s);
+// vpr (may be null): (position, radius) of the kept VPLs for the tile cull
 cudaError_t launch_compact(const sgi_vpl* vpls, const sgi_atlas_entry* entries, const uint8_t* flags, int32_t n,
-                           int32_t cap, sgi_vpl* cv, sgi_atlas_entry* ce, int32_t* visible_index, cudaStream_t s);
-// stage 1 also packs (position, radius) of the compacted VPLs into vpr [max_visible]
+                           int32_t cap, sgi_vpl* cv, sgi_atlas_entry* ce, int32_t* visible_index, float4* vpr,
+                           cudaStream_t s);
 cudaError_t launch_tile_stage1(const sgi_config& cfg, const sgi_gbuffer& g, const sgi_camera& cam,
-                               sgi_tile_stage1* out, const sgi_vpl* cv, const int32_t* visible_index, float4* vpr,
-                               cudaStream_t s);
+                               sgi_tile_stage1* out, cudaStream_t s);
 // stage 2: one block per tile, keys in shared memory (tile_cull_smem bytes)
 cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1, const float4* vpr,
                                const int32_t* visible_index, int32_t* lists, cudaStream_t s);

@@ -91,9 +91,20 @@ SGI_D PixelShade load_pixel(const GatherParams& p, int x, int y, size_t i) {
     return px;
 }
 
+// A tile's VPL list staged in shared memory: the records and atlas slots of its
+// L nearest VPLs, in list order. Used when a gather block covers exactly one
+// tile (block = tile_size x tile_size), so that every sample of the block reads
+// its VPL from shared memory instead of the compacted buffers in L2.
+struct StagedList {
+    float4 rec[SGI_MAX_TILE_LIST][4];   // position, colour, specular position, (radius, far, intensity, -)
+    sgi_atlas_entry ent[SGI_MAX_TILE_LIST];
+};
+
 // The sample loop of vpl_pbr_gi.fs:148-200 with the seed z starting at seedZ.
+// kStaged: the list of the pixel's tile is in `staged` (list slot = array index).
+template <bool kStaged>
 SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX, float seedY, float seedZ,
-                       V3& vplColor, float& validSamples) {
+                       V3& vplColor, float& validSamples, const StagedList* staged = nullptr) {
     ShadeParams sp{p.sc.min_roughness, p.sc.perceptual, p.sc.fog_density,
                    {p.sc.fog_color[0], p.sc.fog_color[1], p.sc.fog_color[2]}, p.sc.point_ambient};
     vplColor = v3s(0.0f);
@@ -107,18 +118,31 @@ SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX,
     for (int s = 0, resamples = 0; s < px.sampleCount; ++s) {
         const float rnd = random3(seedX, seedY, seedZ);
         seedZ += 10000.0f;
-        int lightIndex;
-        if (px.list) {
-            int r = (int)xmul(float(candidates), rnd);
-            lightIndex = __ldg(px.list + 1 + (r < candidates - 1 ? r : candidates - 1));
+        float4 pos, col, spec, misc;
+        sgi_atlas_entry entry;
+        if (kStaged) {
+            const int r = (int)xmul(float(candidates), rnd);
+            const int slot = r < candidates - 1 ? r : candidates - 1;
+            pos = staged->rec[slot][0];
+            col = staged->rec[slot][1];
+            spec = staged->rec[slot][2];
+            misc = staged->rec[slot][3];
+            entry = staged->ent[slot];
         } else {
-            lightIndex = (int)xmul(float(candidates - 1), rnd);
+            int lightIndex;
+            if (px.list) {
+                int r = (int)xmul(float(candidates), rnd);
+                lightIndex = __ldg(px.list + 1 + (r < candidates - 1 ? r : candidates - 1));
+            } else {
+                lightIndex = (int)xmul(float(candidates - 1), rnd);
+            }
+            const float4* rec = reinterpret_cast<const float4*>(p.cv + lightIndex);
+            pos = __ldg(rec);
+            col = __ldg(rec + 1);
+            spec = __ldg(rec + 2);
+            misc = __ldg(rec + 3);   // radius, farPlane, intensity
+            entry = p.ce[lightIndex];
         }
-        const float4* rec = reinterpret_cast<const float4*>(p.cv + lightIndex);
-        const float4 pos = __ldg(rec);
-        const float4 spec = __ldg(rec + 2);
-        const float4 misc = __ldg(rec + 3);   // radius, farPlane, intensity
-        const sgi_atlas_entry entry = p.ce[lightIndex];
         const V3 lightPosition = v3(pos.x, pos.y, pos.z);
         const V3 lmf = xsub3(lightPosition, fragPos);
         const float lightRadius = misc.x;
@@ -129,7 +153,6 @@ SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX,
         }
         const float distanceRatio = gclamp((2.0f * distance) / lightRadius, 0.0f, 1.0f);
         const float distAttenuation = distanceRatio;
-        const float4 col = __ldg(rec + 1);
         const V3 lightColor = v3(col.x, col.y, col.z);
         float shadowFactor = px.distToCamera < 500.0f
                                  ? shadow_1sample(p.cubes, entry, misc.y, fragPos, lightPosition,
@@ -145,10 +168,25 @@ SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX,
     }
 }
 
-// vpl_pbr_gi.fs:81-207, one thread per pixel.
+// vpl_pbr_gi.fs:81-207, one thread per pixel. kStaged: the block is one tile
+// and first stages the tile's list (StagedList, dynamic shared memory).
+template <bool kStaged>
 __global__ void __launch_bounds__(256, 4) vpl_gather_kernel(GatherParams p) {
+    extern __shared__ float4 gather_smem[];
+    StagedList* staged = reinterpret_cast<StagedList*>(gather_smem);
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (kStaged) {
+        const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
+        const int32_t* list = p.lists + (size_t)(blockIdx.y * p.tiles_x + blockIdx.x) * (1 + p.L);
+        const int count = __ldg(list);
+        for (int j = tid; j < count * 4; j += nthreads) {
+            const int idx = __ldg(list + 1 + (j >> 2));
+            staged->rec[j >> 2][j & 3] = __ldg(reinterpret_cast<const float4*>(p.cv + idx) + (j & 3));
+        }
+        for (int j = tid; j < count; j += nthreads) staged->ent[j] = p.ce[__ldg(list + 1 + j)];
+        __syncthreads();
+    }
     if (x >= p.W || y >= p.H) return;
     const size_t i = (size_t)y * p.W + x;
     const PixelShade px = load_pixel(p, x, y, i);
@@ -156,7 +194,7 @@ __global__ void __launch_bounds__(256, 4) vpl_gather_kernel(GatherParams p) {
     const float seedX = float(x) + 0.5f, seedY = float(y) + 0.5f;
     V3 vplColor;
     float validSamples;
-    sample_vpls(p, px, seedX, seedY, p.time, vplColor, validSamples);
+    sample_vpls<kStaged>(p, px, seedX, seedY, p.time, vplColor, validSamples, staged);
     validSamples = gmax(validSamples, 1.0f);
     const V3 b = vmin(vplColor, kHalfMax);
     // The reservoir as stored in its RGBA16F target (vpl_pbr_gi.fs:205).
@@ -196,7 +234,12 @@ cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sg
     p.cubes = cubes; p.time = time; p.out = out;
     if (block.x == 0) block = dim3(16, 16);
     dim3 grid((cfg.width + block.x - 1) / block.x, (cfg.height + block.y - 1) / block.y);
-    vpl_gather_kernel<<<grid, block, 0, s>>>(p);
+    // a block that is exactly one tile stages the tile's list in shared memory
+    const bool staged = p.tiled && (int)block.x == cfg.tile_size && (int)block.y == cfg.tile_size;
+    if (staged)
+        vpl_gather_kernel<true><<<grid, block, sizeof(StagedList), s>>>(p);
+    else
+        vpl_gather_kernel<false><<<grid, block, 0, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -217,7 +260,7 @@ __global__ void __launch_bounds__(256, 4) gi_target_kernel(GatherParams p, int b
     for (int b = 0; b < batches; ++b) {
         V3 col;
         float valid;
-        sample_vpls(p, px, seedX, seedY, p.time + float(b) * 200000.0f, col, valid);
+        sample_vpls<false>(p, px, seedX, seedY, p.time + float(b) * 200000.0f, col, valid);
         c0 += (double)col.x; c1 += (double)col.y; c2 += (double)col.z; w += (double)valid;
     }
     const double den = w < 1.0 ? 1.0 : w;

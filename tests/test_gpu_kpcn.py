@@ -190,3 +190,42 @@ def test_fp8_forward_tracks_bf16_on_rendered_frames():
     assert loss(a) <= 1.15 * loss(b) + 1e-3, (loss(a), loss(b))
     net.set_precision(abi.SGI_NN_BF16)
     net.close()
+
+
+def test_fp8_and_bf16_forward_against_the_float64_oracle_on_rendered_frames():
+    """The trained network in FP8 E4M3 (scales calibrated on other frames) and in BF16, each against the
+    float64 network oracle (oracle/kpcn.py) with the same BF16 weights and BF16-rounded features, on
+    frames the plain path renders. Stated error: mean |gpu - oracle| over the denoised GI, relative to
+    the oracle's peak; bounds 2 % (BF16: 8 mantissa bits between layers) and 5 % (E4M3: 3 bits)."""
+    import os
+
+    from stratusgfx_gb300 import denoiser
+    if not os.path.exists(denoiser.WEIGHTS):
+        pytest.skip("no trained weights")
+    calib = denoiser.make_dataset(2, H=64, W=128, frames_per_room=2, seed=501, samples=(2,), batches=2,
+                                  log=lambda *a: None)
+    ds = denoiser.make_dataset(2, H=64, W=128, frames_per_room=2, seed=901, samples=(2,), batches=2,
+                               log=lambda *a: None)
+    net = KpcnDenoiser(2, 64, 128, seed=1)
+    net.load(denoiser.WEIGHTS)
+    p64 = kpcn.unpack(bf16_round(net.params()).astype(np.float64))
+    out_bf = torch.empty((2, 64, 128, 4), device="cuda")
+    out_f8 = torch.empty_like(out_bf)
+    net.forward(ds.feat[:2], ds.noisy[:2], ds.prev[:2], out_bf)
+    net.calibrate_fp8(calib.feat[:2])
+    net.set_precision(abi.SGI_NN_FP8)
+    net.forward(ds.feat[:2], ds.noisy[:2], ds.prev[:2], out_f8)
+    net.set_precision(abi.SGI_NN_BF16)
+    torch.cuda.synchronize()
+    feat = ds.feat[:2].float().cpu().numpy().astype(np.float64)
+    a = kpcn.forward(p64, feat)
+    ref = kpcn.apply(a["head"], ds.noisy[:2, ..., :3].cpu().numpy().astype(np.float64),
+                     ds.prev[:2, ..., :3].cpu().numpy().astype(np.float64))
+    peak = np.abs(ref).max()
+    err_bf = float(np.abs(out_bf[..., :3].cpu().numpy() - ref).mean() / peak)
+    err_f8 = float(np.abs(out_f8[..., :3].cpu().numpy() - ref).mean() / peak)
+    max_f8 = float(np.abs(out_f8[..., :3].cpu().numpy() - ref).max() / peak)
+    print(f"vs float64 oracle: BF16 mean rel {err_bf:.2e}; FP8 mean rel {err_f8:.2e}, max rel {max_f8:.2e}")
+    assert err_bf < 0.02, err_bf
+    assert err_f8 < 0.05, err_f8
+    net.close()

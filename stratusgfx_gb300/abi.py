@@ -232,6 +232,11 @@ EXPORTS = {
     "sgi_batch_create": (C.c_int32, [C.POINTER(View), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                      C.POINTER(C.c_void_p)]),
     "sgi_batch_launch": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "sgi_batch_create_persistent": (C.c_int32, [C.POINTER(View), C.c_int32, C.c_int32, C.c_void_p,
+                                                C.POINTER(C.c_void_p)]),
+    "sgi_batch_status": (C.c_int32, [C.c_void_p]),
+    "sgi_batch_set_wait_limit": (C.c_int32, [C.c_void_p, C.c_int64]),
+    "sgi_batch_skip_pass": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "sgi_batch_kernel_count": (C.c_int64, [C.c_void_p]),
     "sgi_batch_destroy": (C.c_int32, [C.c_void_p]),
     "sgi_batch_last_error": (C.c_char_p, [C.c_void_p]),

@@ -10,6 +10,12 @@
 
 namespace sgi {
 
+#ifdef __CUDACC__
+#define SGI_HD_INLINE __host__ __device__ __forceinline__
+#else
+#define SGI_HD_INLINE inline
+#endif
+
 // Device-side constants of the shading passes (RendererSettings subset).
 struct ShadeConfig {
     float min_roughness;
@@ -80,6 +86,66 @@ struct ShadowCasters {
     sgi_cube_atlas atlas;
 };
 
+// ------------------------------------------------ persistent multi-view frame --
+// One launch renders a plain frame of many views: persistent CTAs take work
+// items (view, level, index) from a queue in dependency order and wait, with a
+// time limit, until the levels an item depends on are complete for its view.
+enum PLevel : int {
+    kPVis = 0,        // VPL visibility flags, 256 VPLs per item
+    kPCompact = 1,    // stable compaction of the visible VPLs, one item
+    kPDirect = 2,     // deferred lighting, one 16x16 pixel block per item
+    kPTile = 3,       // tile mean + tile cull, one 16x16 tile per item
+    kPGather = 4,     // gather + denoise pass 0, one tile per item
+    kPAtrous = 5,     // + (pass - 1): a-trous pass 1 .. n-2; the final pass follows the last one
+};
+constexpr int kPMaxLevels = kPAtrous + SGI_MAX_DENOISE_PASSES - 1;
+constexpr int kPMaxViews = 256;
+SGI_HD_INLINE uint32_t pitem(int view, int level, int index) {
+    return (uint32_t)view | ((uint32_t)level << 8) | ((uint32_t)index << 13);
+}
+
+// Work-queue state in device memory: zero before the first launch; the last
+// CTA of every launch returns it to zero.
+struct PQueue {
+    unsigned int next;        // items taken
+    unsigned int finished;    // CTAs that left the loop
+    int done[kPMaxViews][kPMaxLevels];
+};
+
+// What a view's passes need, gathered from its context (host side).
+struct PViewDesc {
+    sgi_config cfg;
+    ShadeConfig sc;
+    const sgi_vpl* vpls; const sgi_atlas_entry* entries; int32_t num_vpls;
+    sgi_csm csm;
+    sgi_cube_atlas cubes;
+    const sgi_point_light* points; int32_t num_points;
+    const sgi_point_light* casters; const sgi_atlas_entry* caster_entries; int32_t num_casters;
+    sgi_cube_atlas caster_atlas;
+    uint8_t* flags; sgi_vpl* cv; sgi_atlas_entry* ce; int32_t* visible_index; float4* vpr;
+    sgi_tile_stage1* stage1; int32_t* lists;
+    sgi_gbuffer cur; sgi_camera cam; const sgi_gbuffer* prev_ptr; sgi_gbuffer prev;
+    sgi_frame_params params;
+    float4* guide; uint2* raw;
+    uint2* pass_buf[SGI_MAX_DENOISE_PASSES];   // output of every denoise pass
+    uint2* direct;
+    const uint2* gi_prev; uint2* gi_out; const uint16_t* hist_prev; uint16_t* hist_out;
+    void* hdr_out;
+};
+
+struct PPlan {
+    const uint32_t* items;     // dispatch order
+    int32_t num_items;
+    int32_t num_views;
+    const int32_t* counts;     // [num_views][kPMaxLevels] items per level
+    PQueue* q;
+    int32_t* status;           // SGI_OK, or SGI_ERR_TIMEOUT after a wait gave up (the host clears it)
+    const int32_t* skip;       // [num_views][kPMaxLevels]: nonzero = the level's items do nothing (test switch)
+    const long long* wait_ns;  // limit of every wait (device memory, so that a captured launch sees changes)
+    const unsigned char* views;  // per-view parameter blocks of view_bytes each
+    int32_t view_bytes;
+};
+
 // The shading kernels (sgi_shade.cu) exist twice: sgi::exact is bit-identical to
 // the CPU restatement of the shaders, sgi::fast is the tolerance mode (fast
 // division, square root, exponential and contraction; see sgi_shade.cu).
@@ -96,7 +162,13 @@ struct ShadowCasters {
     cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, \
                                 const sgi_camera& cam, const sgi_point_light* points, int32_t num_points, \
                                 const ShadowCasters& casters, const sgi_csm& csm, uint2* hdr_out, cudaStream_t s, \
-                                dim3 block = dim3(0, 0, 0));
+                                dim3 block = dim3(0, 0, 0)); \
+    /* persistent multi-view frame: bytes of one view's parameter block, filling it, the launch */ \
+    int32_t persistent_view_bytes(); \
+    void persistent_fill_view(const PViewDesc& d, unsigned char* out); \
+    size_t persistent_smem(int32_t max_visible); \
+    cudaError_t persistent_occupancy(size_t smem, int* blocks_per_sm); \
+    cudaError_t launch_persistent(const PPlan& plan, int grid, size_t smem, cudaStream_t s);
 
 namespace exact {
 SGI_SHADE_LAUNCHERS

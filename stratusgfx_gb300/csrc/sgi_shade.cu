@@ -16,6 +16,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstring>
+
+#include "sgi_cull.cuh"
 #include "sgi_internal.h"
 #include "sgi_math.cuh"
 #include "sgi_shade_common.cuh"
@@ -168,26 +171,21 @@ SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX,
     }
 }
 
-// vpl_pbr_gi.fs:81-207, one thread per pixel. kStaged: the block is one tile
-// and first stages the tile's list (StagedList, dynamic shared memory).
-template <bool kStaged>
-__global__ void __launch_bounds__(256, 4) vpl_gather_kernel(GatherParams p) {
-    extern __shared__ float4 gather_smem[];
-    StagedList* staged = reinterpret_cast<StagedList*>(gather_smem);
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (kStaged) {
-        const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
-        const int32_t* list = p.lists + (size_t)(blockIdx.y * p.tiles_x + blockIdx.x) * (1 + p.L);
-        const int count = __ldg(list);
-        for (int j = tid; j < count * 4; j += nthreads) {
-            const int idx = __ldg(list + 1 + (j >> 2));
-            staged->rec[j >> 2][j & 3] = __ldg(reinterpret_cast<const float4*>(p.cv + idx) + (j & 3));
-        }
-        for (int j = tid; j < count; j += nthreads) staged->ent[j] = p.ce[__ldg(list + 1 + j)];
-        __syncthreads();
+// The block's tile list into shared memory (the block is tile `tile`).
+SGI_D void stage_tile_list(const GatherParams& p, int tile, StagedList* staged, int tid, int nthreads) {
+    const int32_t* list = p.lists + (size_t)tile * (1 + p.L);
+    const int count = __ldg(list);
+    for (int j = tid; j < count * 4; j += nthreads) {
+        const int idx = __ldg(list + 1 + (j >> 2));
+        staged->rec[j >> 2][j & 3] = __ldg(reinterpret_cast<const float4*>(p.cv + idx) + (j & 3));
     }
-    if (x >= p.W || y >= p.H) return;
+    for (int j = tid; j < count; j += nthreads) staged->ent[j] = p.ce[__ldg(list + 1 + j)];
+}
+
+// vpl_pbr_gi.fs:81-207 for pixel (x, y) inside the image, with denoise pass 0
+// and the guide in its epilogue.
+template <bool kStaged>
+SGI_D void gather_pixel(const GatherParams& p, int x, int y, const StagedList* staged) {
     const size_t i = (size_t)y * p.W + x;
     const PixelShade px = load_pixel(p, x, y, i);
     const V3 normal = px.normal;
@@ -220,6 +218,23 @@ __global__ void __launch_bounds__(256, 4) vpl_gather_kernel(GatherParams p) {
     const float den = gmax(kEps, runningSum);
     p.out.merged[i] = pack_h4(cr0 / den, cr1 / den, cr2 / den, 1.0f);
     p.out.guide[i] = make_float4(normal.x, normal.y, normal.z, depth);
+}
+
+// one thread per pixel; kStaged: the block is one tile and first stages the
+// tile's list (StagedList, dynamic shared memory)
+template <bool kStaged>
+__global__ void __launch_bounds__(256, 4) vpl_gather_kernel(GatherParams p) {
+    extern __shared__ float4 gather_smem[];
+    StagedList* staged = reinterpret_cast<StagedList*>(gather_smem);
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (kStaged) {
+        stage_tile_list(p, blockIdx.y * p.tiles_x + blockIdx.x, staged, threadIdx.y * blockDim.x + threadIdx.x,
+                        blockDim.x * blockDim.y);
+        __syncthreads();
+    }
+    if (x >= p.W || y >= p.H) return;
+    gather_pixel<kStaged>(p, x, y, staged);
 }
 
 cudaError_t launch_gather(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, const sgi_camera& cam,
@@ -332,17 +347,21 @@ SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __r
     rf0 = acc01.x; rf1 = acc01.y; rf2 = acc23.x; rf3 = acc23.y;
 }
 
-__global__ void __launch_bounds__(256, 5) atrous_kernel(int W, int H, int step, const float4* __restrict__ guide,
-                                                     const uint2* __restrict__ res_in, uint2* __restrict__ res_out) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= W || y >= H) return;
+SGI_D void atrous_pixel(int W, int H, int step, const float4* __restrict__ guide, const uint2* __restrict__ res_in,
+                        uint2* __restrict__ res_out, int x, int y) {
     const size_t i = (size_t)y * W + x;
     const float4 gc = __ldg(guide + i);
     float rf0, rf1, rf2, rf3;
     atrous_filter(x, y, W, H, step, guide, res_in, v3(gc.x, gc.y, gc.z), gc.w, rf0, rf1, rf2, rf3);
     const float den = gmax(kEps, rf3);
     res_out[i] = pack_h4(rf0 / den, rf1 / den, rf2 / den, 1.0f);
+}
+
+__global__ void __launch_bounds__(256, 5) atrous_kernel(int W, int H, int step, const float4* __restrict__ guide,
+                                                     const uint2* __restrict__ res_in, uint2* __restrict__ res_out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x < W && y < H) atrous_pixel(W, H, step, guide, res_in, res_out, x, y);
 }
 
 cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in,
@@ -355,11 +374,8 @@ cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guid
 
 // Final pass (final = true): the filter above, then temporal reprojection
 // (vpl_pbr_gi_denoise.fs:336-429) and the composite screen + gi * illumAvg (:431).
-__global__ void __launch_bounds__(256, 5) denoise_final_kernel(DenoiseLaunch d) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+SGI_D void denoise_final_pixel(const DenoiseLaunch& d, int x, int y) {
     const int W = d.width, H = d.height;
-    if (x >= W || y >= H) return;
     const size_t i = (size_t)y * W + x;
     const float u = xdiv(float(x) + 0.5f, float(W)), v = xdiv(float(y) + 0.5f, float(H));
     const float4 gc = __ldg(d.guide + i);
@@ -419,6 +435,12 @@ __global__ void __launch_bounds__(256, 5) denoise_final_kernel(DenoiseLaunch d) 
     d.hist_out[i] = f2h(historyAccum);
 }
 
+__global__ void __launch_bounds__(256, 5) denoise_final_kernel(DenoiseLaunch d) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x < d.width && y < d.height) denoise_final_pixel(d, x, y);
+}
+
 cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s, dim3 block) {
     if (block.x == 0) block = dim3(32, 8);
     dim3 grid((d.width + block.x - 1) / block.x, (d.height + block.y - 1) / block.y);
@@ -441,10 +463,7 @@ struct DeferredParams {
 
 // pbr.fs:82-145: non-shadow-casting point lights + the directional light
 // with its CSM (INFINITE_LIGHTING_ENABLED).
-__global__ void __launch_bounds__(256, 4) deferred_pbr_csm_kernel(DeferredParams p) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= p.W || y >= p.H) return;
+SGI_D void deferred_pixel(const DeferredParams& p, int x, int y) {
     const size_t i = (size_t)y * p.W + x;
     ShadeParams sp{p.sc.min_roughness, p.sc.perceptual, p.sc.fog_density,
                    {p.sc.fog_color[0], p.sc.fog_color[1], p.sc.fog_color[2]}, p.sc.point_ambient};
@@ -509,6 +528,12 @@ __global__ void __launch_bounds__(256, 4) deferred_pbr_csm_kernel(DeferredParams
     p.out[i] = pack_h4(o.x, o.y, o.z, 1.0f);
 }
 
+__global__ void __launch_bounds__(256, 4) deferred_pbr_csm_kernel(DeferredParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x < p.W && y < p.H) deferred_pixel(p, x, y);
+}
+
 cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,
                             const sgi_camera& cam, const sgi_point_light* points, int32_t num_points,
                             const ShadowCasters& casters, const sgi_csm& csm, uint2* hdr_out, cudaStream_t s,
@@ -521,6 +546,9 @@ cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const 
     deferred_pbr_csm_kernel<<<grid, block, 0, s>>>(p);
     return cudaGetLastError();
 }
+
+// the persistent multi-view frame over the passes above
+#include "sgi_persistent.cuh"
 
 }  // namespace SGI_SHADE_NS
 }  // namespace sgi

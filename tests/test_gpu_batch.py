@@ -135,3 +135,104 @@ def test_batch_create_rejects_views_without_a_first_frame():
     assert lib.sgi_batch_create(arr, 1, None, 0, None, C.byref(h)) == abi.SGI_ERR_STATE
     assert lib.sgi_batch_create(arr, 0, None, 0, None, C.byref(h)) == abi.SGI_ERR_ARG
     v.st.close()
+
+
+def run_persistent(fast=False):
+    """The persistent batch (one kernel per frame over all views' passes) against each view rendered in turn:
+    bit for bit in the exact precision; in the tolerance precision within its 1e-3 relative error (the two
+    kernels may fuse multiply-adds differently)."""
+    lib = abi.load()
+    sizes = [(96, 64, 11), (160, 96, 12), (64, 64, 13), (200, 120, 14)]
+    scenes = [view_scene(W, H, seed) for W, H, seed in sizes]
+    seq = [View(w, ds) for w, ds in scenes]
+    bat = [View(w, ds) for w, ds in scenes]
+    for v in seq + bat:
+        if fast:
+            assert lib.sgi_set_shading_precision(v.st.ctx, abi.SGI_SHADING_FAST) == abi.SGI_OK
+        v.frame()
+    arr = (abi.View * len(bat))(*[v.struct() for v in bat])
+    h = C.c_void_p()
+    st = lib.sgi_batch_create_persistent(arr, len(bat), 0, None, C.byref(h))
+    assert st == abi.SGI_OK, lib.sgi_batch_last_error(h)
+    assert lib.sgi_batch_kernel_count(h) == 1
+
+    def compare():
+        for a, b in zip(seq, bat):
+            if fast:
+                x, y = a.out.float(), b.out.float()
+                rel = ((x - y).abs() / y.abs().clamp(min=2.0 ** -14)).max().item()
+                assert rel <= 1e-3, (a.w.name, rel)
+            else:
+                assert torch.equal(a.out.view(torch.int16), b.out.view(torch.int16)), a.w.name
+
+    for _ in range(3):
+        assert lib.sgi_batch_launch(h, None) == abi.SGI_OK
+    for v in seq:
+        for _ in range(3):
+            v.frame()
+    torch.cuda.synchronize()
+    assert lib.sgi_batch_status(h) == abi.SGI_OK
+    compare()
+    assert lib.sgi_batch_destroy(h) == abi.SGI_OK
+    for v in seq + bat:
+        v.frame()
+    torch.cuda.synchronize()
+    compare()
+    for v in seq + bat:
+        v.st.close()
+
+
+def test_persistent_batch_matches_per_view_frames():
+    run_persistent(fast=False)
+
+
+def test_persistent_batch_in_the_tolerance_precision():
+    run_persistent(fast=True)
+
+
+def test_persistent_batch_wait_gives_up_and_the_next_launch_succeeds():
+    """The test switch holds back view 0's VPL compaction: the tile passes that wait for it give up after the
+    batch's 20 ms limit, the launch ends with SGI_ERR_TIMEOUT, and with the switch cleared the next launch
+    completes (status OK, every view's output finite)."""
+    lib = abi.load()
+    views = [View(*view_scene(W, H, seed)) for W, H, seed in ((96, 64, 31), (128, 96, 32))]
+    for v in views:
+        v.frame()
+    arr = (abi.View * 2)(*[v.struct() for v in views])
+    h = C.c_void_p()
+    assert lib.sgi_batch_create_persistent(arr, 2, 2, None, C.byref(h)) == abi.SGI_OK   # tuned CTA count
+    assert lib.sgi_batch_set_wait_limit(h, 20_000_000) == abi.SGI_OK
+    assert lib.sgi_batch_skip_pass(h, 0, 1, 1) == abi.SGI_OK
+    assert lib.sgi_batch_launch(h, None) == abi.SGI_OK
+    torch.cuda.synchronize()
+    assert lib.sgi_batch_status(h) == abi.SGI_ERR_TIMEOUT
+    assert b"gave up" in lib.sgi_batch_last_error(h)
+    assert lib.sgi_batch_skip_pass(h, 0, 1, 0) == abi.SGI_OK
+    for _ in range(2):
+        assert lib.sgi_batch_launch(h, None) == abi.SGI_OK
+    torch.cuda.synchronize()
+    assert lib.sgi_batch_status(h) == abi.SGI_OK
+    for v in views:
+        assert torch.isfinite(v.out.float()).all()
+    assert lib.sgi_batch_skip_pass(h, 2, 1, 1) == abi.SGI_ERR_ARG
+    assert lib.sgi_batch_destroy(h) == abi.SGI_OK
+    for v in views:
+        v.st.close()
+
+
+def test_persistent_batch_rejects_unsupported_views():
+    lib = abi.load()
+    w, ds = view_scene(64, 64, 41)
+    v = View(w, ds)
+    arr = (abi.View * 1)(v.struct())
+    h = C.c_void_p()
+    assert lib.sgi_batch_create_persistent(arr, 1, 0, None, C.byref(h)) == abi.SGI_ERR_STATE   # no first frame
+    v.frame()
+    assert lib.sgi_batch_create_persistent(arr, 257, 0, None, C.byref(h)) == abi.SGI_ERR_ARG
+    w8 = S.Workload("room12_64x64_t8", 64, 64, 12, 48, 2, 512, 32, abi.SGI_CUBE_F16, 4, 5, 2, tile_size=8)
+    v8 = View(w8, stage.DeviceScene(S.workload_scene(w8, 42), w8))
+    v8.frame()
+    arr8 = (abi.View * 1)(v8.struct())
+    assert lib.sgi_batch_create_persistent(arr8, 1, 0, None, C.byref(h)) == abi.SGI_ERR_ARG   # 8x8 tiles
+    v.st.close()
+    v8.st.close()

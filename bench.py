@@ -850,6 +850,11 @@ def batched_views(args, flush):
         ms_graph /= steps
         abi.check(lib.sgi_batch_status(h))
         kernels = int(lib.sgi_batch_kernel_count(h))
+        pshape = None
+        if persistent:
+            regs, ctas = C.c_int32(), C.c_int32()
+            abi.check(lib.sgi_batch_persistent_shape(h, C.byref(regs), C.byref(ctas)))
+            pshape = {"registers_per_thread": regs.value, "ctas": ctas.value}
         shapes = {}
         bx, by = C.c_int32(), C.c_int32()
         for o in objs:
@@ -863,7 +868,8 @@ def batched_views(args, flush):
                              "mpix_s": round(total_px / ms_graph / 1e3, 1),
                              "view_by_view_ms": round(ms_seq, 3), "graph_speedup": round(ms_seq / ms_graph, 3),
                              "mean_gi_psnr_db": round(sum(psnr) / len(psnr), 2),
-                             "kernels_per_launch": kernels, "tuned_gather_blocks": shapes,
+                             "kernels_per_launch": kernels,
+                             "tuned": pshape if persistent else {"gather_blocks": shapes},
                              "tune_and_capture_s": round(build_s, 2)}
     net.close()
     plain = res["runs"]["plain_K8"]

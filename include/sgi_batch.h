@@ -68,6 +68,9 @@ sgi_status sgi_batch_create(const sgi_view* views, int32_t num_views, sgi_nn* ne
  * gets its own denoise pass buffers (width x height x 8 bytes per pass). */
 sgi_status sgi_batch_create_persistent(const sgi_view* views, int32_t num_views, int32_t tune_frames, void* stream,
                                        sgi_batch** out);
+/* The shape the persistent batch launches with: registers per thread the
+ * kernel is built for (64 or 128) and the number of CTAs. */
+sgi_status sgi_batch_persistent_shape(const sgi_batch* batch, int32_t* registers, int32_t* ctas);
 /* SGI_OK, or the status a persistent launch set (SGI_ERR_TIMEOUT when a wait
  * gave up); reading it clears it. Synchronous. SGI_OK for graph batches. */
 sgi_status sgi_batch_status(sgi_batch* batch);

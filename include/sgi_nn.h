@@ -88,6 +88,15 @@ sgi_status sgi_nn_calibrate_fp8(sgi_nn* net, const void* features, int32_t batch
  * SGI_ERR_TIMEOUT when a tensor-core convolution gave up a bounded wait. */
 sgi_status sgi_nn_device_status(sgi_nn* net);
 
+/* The bounded waits of the tensor-core convolutions (no counterpart in
+ * StratusGFX): every wait of a role (TMA producer, MMA issuer, epilogue) on
+ * another gives up after wait_ns nanoseconds (0: the default 200 ms), raises
+ * the CTA's abort flag, lets MMAs already issued finish, frees its tensor
+ * memory and returns; sgi_nn_device_status then reports SGI_ERR_TIMEOUT.
+ * skip_producer != 0 is a test switch: the TMA producers issue no copy, so the
+ * first wait of the MMA role runs out with no copy or MMA in flight. */
+sgi_status sgi_nn_set_wait_test(sgi_nn* net, int64_t wait_ns, int32_t skip_producer);
+
 /* One 3x3 convolution layer (zero padding) as the network runs it:
  * y[b][h][w][o] = act(bias[o] + sum_{ky,kx,c} w[o][ky*3+kx][c] * x[b][h+ky-1][w+kx-1][c])
  * with act = ReLU (mode 0), identity (mode 1) or no bias and identity (mode 2).

@@ -211,6 +211,7 @@ EXPORTS = {
     "sgi_nn_set_precision": (C.c_int32, [C.c_void_p, C.c_int32]),
     "sgi_nn_calibrate_fp8": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "sgi_nn_device_status": (C.c_int32, [C.c_void_p]),
+    "sgi_nn_set_wait_test": (C.c_int32, [C.c_void_p, C.c_int64, C.c_int32]),
     "sgi_nn_conv3x3": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                    C.c_void_p]),
@@ -235,6 +236,7 @@ EXPORTS = {
     "sgi_batch_create_persistent": (C.c_int32, [C.POINTER(View), C.c_int32, C.c_int32, C.c_void_p,
                                                 C.POINTER(C.c_void_p)]),
     "sgi_batch_status": (C.c_int32, [C.c_void_p]),
+    "sgi_batch_persistent_shape": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "sgi_batch_set_wait_limit": (C.c_int32, [C.c_void_p, C.c_int64]),
     "sgi_batch_skip_pass": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "sgi_batch_kernel_count": (C.c_int64, [C.c_void_p]),

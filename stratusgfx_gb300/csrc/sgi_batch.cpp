@@ -29,6 +29,7 @@ struct sgi_batch {
     long long* d_wait = nullptr;
     std::vector<void*> scratch;           // per-view denoise pass buffers
     sgi::PPlan plan[2] = {};
+    int variant = 0;                      // register budget of the persistent kernel (tuned)
     int grid = 0;
     size_t smem = 0;
 };
@@ -137,9 +138,9 @@ sgi_status pcheck(sgi_batch* b, cudaError_t e, const char* what) {
 }
 
 // One persistent launch of plan p on s.
-cudaError_t persistent_launch(sgi_batch* b, int p, int grid, cudaStream_t s) {
-    return b->fast ? sgi::fast::launch_persistent(b->plan[p], grid, b->smem, s)
-                   : sgi::exact::launch_persistent(b->plan[p], grid, b->smem, s);
+cudaError_t persistent_launch(sgi_batch* b, int p, int variant, int grid, cudaStream_t s) {
+    return b->fast ? sgi::fast::launch_persistent(b->plan[p], variant, grid, b->smem, s)
+                   : sgi::exact::launch_persistent(b->plan[p], variant, grid, b->smem, s);
 }
 
 // The view's passes as the persistent kernel reads them, for history parity `parity`
@@ -241,37 +242,43 @@ sgi_status build_persistent(sgi_batch* b, int32_t tune_frames, cudaStream_t s) {
         pl.view_bytes = vb;
     }
     b->smem = b->fast ? sgi::fast::persistent_smem(max_visible) : sgi::exact::persistent_smem(max_visible);
-    int per_sm = 0;
-    cudaError_t e = b->fast ? sgi::fast::persistent_occupancy(b->smem, &per_sm)
-                            : sgi::exact::persistent_occupancy(b->smem, &per_sm);
-    if ((st = pcheck(b, e, "occupancy")) != SGI_OK) return st;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (per_sm < 1) return bfail(b, SGI_ERR_CUDA, "the persistent kernel does not fit on an SM");
-    // CTAs per SM: every count that fits is timed over tune_frames launches (all of them co-resident,
-    // which the waits need); without tuning, the most that fit
-    b->grid = per_sm * sms;
-    if (tune_frames > 0 && per_sm > 1) {
+    int per_sm[2] = {0, 0};
+    for (int var = 0; var < 2; ++var) {
+        cudaError_t e = b->fast ? sgi::fast::persistent_occupancy(var, b->smem, &per_sm[var])
+                                : sgi::exact::persistent_occupancy(var, b->smem, &per_sm[var]);
+        if ((st = pcheck(b, e, "occupancy")) != SGI_OK) return st;
+    }
+    if (per_sm[0] < 1) return bfail(b, SGI_ERR_CUDA, "the persistent kernel does not fit on an SM");
+    // register budget (64 or 128 per thread) and CTAs per SM: without tuning, 64 registers and the most CTAs
+    // that fit; with tuning, every pair is timed over tune_frames launches and the fastest is kept
+    b->variant = 0;
+    b->grid = per_sm[0] * sms;
+    cudaError_t e = cudaSuccess;
+    if (tune_frames > 0) {
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         float best = 1e30f;
-        for (int c = 1; c <= per_sm; ++c) {
-            float total = 0.0f;
-            for (int f = 0; f < tune_frames + 1; ++f) {
-                cudaEventRecord(e0, s);
-                e = persistent_launch(b, b->next, c * sms, s);
-                cudaEventRecord(e1, s);
-                b->next ^= 1;
-                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                if (e != cudaSuccess) break;
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                if (f > 0) total += ms;
+        for (int var = 0; var < 2 && st == SGI_OK; ++var) {
+            for (int c = 1; c <= per_sm[var]; ++c) {
+                float total = 0.0f;
+                for (int f = 0; f < tune_frames + 1; ++f) {
+                    cudaEventRecord(e0, s);
+                    e = persistent_launch(b, b->next, var, c * sms, s);
+                    cudaEventRecord(e1, s);
+                    b->next ^= 1;
+                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                    if (e != cudaSuccess) break;
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (f > 0) total += ms;
+                }
+                if ((st = pcheck(b, e, "tuning launch")) != SGI_OK) break;
+                if (total < best) { best = total; b->variant = var; b->grid = c * sms; }
             }
-            if ((st = pcheck(b, e, "tuning launch")) != SGI_OK) break;
-            if (total < best) { best = total; b->grid = c * sms; }
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -286,7 +293,7 @@ sgi_status build_persistent(sgi_batch* b, int32_t tune_frames, cudaStream_t s) {
         const int par = (b->next + p) & 1;
         e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
         if (e == cudaSuccess) {
-            cudaError_t le = persistent_launch(b, par, b->grid, s);
+            cudaError_t le = persistent_launch(b, par, b->variant, b->grid, s);
             cudaGraph_t g = nullptr;
             e = cudaStreamEndCapture(s, &g);
             if (e == cudaSuccess) e = le;
@@ -383,6 +390,13 @@ sgi_status sgi_batch_create_persistent(const sgi_view* views, int32_t num_views,
         return st;
     }
     *out = b;
+    return SGI_OK;
+}
+
+sgi_status sgi_batch_persistent_shape(const sgi_batch* b, int32_t* registers, int32_t* ctas) {
+    if (!b || !b->persistent || !registers || !ctas) return SGI_ERR_ARG;
+    *registers = b->variant == 0 ? 64 : 128;
+    *ctas = b->grid;
     return SGI_OK;
 }
 

@@ -167,8 +167,9 @@ struct PPlan {
     int32_t persistent_view_bytes(); \
     void persistent_fill_view(const PViewDesc& d, unsigned char* out); \
     size_t persistent_smem(int32_t max_visible); \
-    cudaError_t persistent_occupancy(size_t smem, int* blocks_per_sm); \
-    cudaError_t launch_persistent(const PPlan& plan, int grid, size_t smem, cudaStream_t s);
+    /* variant 0: registers for 4 CTAs per SM, 1: for 2 */ \
+    cudaError_t persistent_occupancy(int variant, size_t smem, int* blocks_per_sm); \
+    cudaError_t launch_persistent(const PPlan& plan, int variant, int grid, size_t smem, cudaStream_t s);
 
 namespace exact {
 SGI_SHADE_LAUNCHERS

@@ -138,7 +138,11 @@ cudaError_t Net::set_params(const float* host, size_t n) {
 }
 
 cudaError_t Net::conv_any(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t s) {
-    return conv_path == SGI_NN_CONV_TCGEN05 ? conv3x3_tc(cin, cout, mode, a, dev_err, s) : conv3x3(cin, cout, mode, a, s);
+    if (conv_path != SGI_NN_CONV_TCGEN05) return conv3x3(cin, cout, mode, a, s);
+    ConvArgs b = a;
+    b.wait_ns = wait_ns;
+    b.skip_producer = skip_producer;
+    return conv3x3_tc(cin, cout, mode, b, dev_err, s);
 }
 
 cudaError_t Net::conv(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s, const View* pool) {
@@ -157,6 +161,8 @@ cudaError_t Net::conv8(int l, const View& x, const View& y, int B, int H, int W,
     if (pool) a.pool = *pool;
     a.wscale = in8 ? f8_wscale + sc_off[l] : nullptr;
     a.oinv = out8 ? f8_oinv + sc_off[l] : nullptr;
+    a.wait_ns = wait_ns;
+    a.skip_producer = skip_producer;
     return conv3x3_tc_fp8(kCin[l], kCout[l], l == HEAD ? 1 : 0, in8, out8, a, dev_err, s);
 }
 
@@ -530,6 +536,13 @@ sgi_status sgi_nn_set_precision(sgi_nn* n, int32_t precision) {
 sgi_status sgi_nn_set_conv_path(sgi_nn* n, int32_t path) {
     if (!n || (path != SGI_NN_CONV_WARP_MMA && path != SGI_NN_CONV_TCGEN05)) return SGI_ERR_ARG;
     n->net.conv_path = path;
+    return SGI_OK;
+}
+
+sgi_status sgi_nn_set_wait_test(sgi_nn* n, int64_t wait_ns, int32_t skip_producer) {
+    if (!n || wait_ns < 0 || wait_ns > 60000000000ll) return SGI_ERR_ARG;
+    n->net.wait_ns = (unsigned long long)wait_ns;
+    n->net.skip_producer = skip_producer ? 1 : 0;
     return SGI_OK;
 }
 

@@ -54,6 +54,11 @@ struct ConvArgs {
     // of the output tensor.
     const float* wscale;
     const float* oinv;
+    // Bounded waits of the tensor-core path: the limit of every wait (0 = the
+    // default 200 ms) and a test switch that keeps the TMA producer from issuing
+    // any copy, so the MMA role's first wait runs out with nothing in flight.
+    unsigned long long wait_ns;
+    int skip_producer;
 };
 
 struct WgradArgs {

@@ -33,6 +33,8 @@ struct Net {
                   *GH3 = nullptr, *GQ1 = nullptr, *GQ2 = nullptr, *GQ3 = nullptr;
     float4* fwd_out = nullptr;
     int* dev_err = nullptr;   // set by a tcgen05 convolution whose wait ran out
+    unsigned long long wait_ns = 0;   // limit of the tcgen05 waits (0: the kernels' default)
+    int skip_producer = 0;            // test switch: the convolutions' TMA producers issue nothing
     int conv_path = SGI_NN_CONV_TCGEN05;
     // FP8 E4M3 inference (after calibrate_fp8): quantized weights (offsets w_off),
     // per-output-channel weight scales and inverse output scales (offsets sc_off),

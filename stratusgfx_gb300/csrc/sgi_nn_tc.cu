@@ -54,7 +54,7 @@ typedef __nv_bfloat16 bf16;
 constexpr int kTcM = 128;                    // pixels per tile row (MMA M)
 constexpr int kHaloPix = kTcM + 2;           // 130
 constexpr int kThreads = 192;
-constexpr unsigned long long kWaitNs = 200ull * 1000ull * 1000ull;   // bound on every wait
+constexpr unsigned long long kWaitNs = 200ull * 1000ull * 1000ull;   // default bound on every wait
 constexpr int kSmemBudget = 220 * 1024;
 
 __host__ __device__ constexpr int round_up(int v, int m) { return (v + m - 1) / m * m; }
@@ -152,9 +152,10 @@ __device__ __forceinline__ bool mbar_test_sleep(uint32_t bar, uint32_t parity, u
 }
 
 // Bounded wait for the phase of `parity`; false on timeout or when another role aborted.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                          unsigned long long limit_ns) {
     if (mbar_test(bar, parity)) return true;
-    const unsigned long long deadline = global_ns() + kWaitNs;
+    const unsigned long long deadline = global_ns() + limit_ns;
     while (true) {
         if (mbar_test_sleep(bar, parity, 20000u)) return true;
         if (*abort_flag) return false;
@@ -390,12 +391,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     pdl_wait();   // every global access below follows the previous kernel's completion
     pdl_trigger();
+    const unsigned long long wait_ns = a.wait_ns ? a.wait_ns : kWaitNs;
     const uint32_t tmem = *tmem_slot;
     const uint32_t smem_base = s_addr(smem);
 
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
-        if (lane == 0) {
+        if (lane == 0 && !a.skip_producer) {
             int s = 0;
             uint32_t ph = 0;
             bool ok = true;
@@ -404,7 +406,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int ty = rest % tl.tiles_y, b = rest / tl.tiles_y;
                 const int x0 = tx * kTcM, y0 = ty * R;
                 for (int ch = 0; ch < NCH; ++ch) {
-                    if (!mbar_wait(s_addr(empty + s), ph ^ 1u, abort_flag)) { ok = false; break; }
+                    if (!mbar_wait(s_addr(empty + s), ph ^ 1u, abort_flag, wait_ns)) { ok = false; break; }
                     const uint32_t bar = s_addr(full + s);
                     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
                                  "r"(S::TX_BYTES)
@@ -430,11 +432,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             uint32_t ph = 0, aph = 0;
             bool ok = true, issued = false;
             for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
-                if (!mbar_wait(s_addr(tempty + acc), aph ^ 1u, abort_flag)) { ok = false; break; }
+                if (!mbar_wait(s_addr(tempty + acc), aph ^ 1u, abort_flag, wait_ns)) { ok = false; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                 const uint32_t d0 = tmem + (uint32_t)(acc * S::BUF_COLS);
                 for (int ch = 0; ch < NCH; ++ch) {
-                    if (!mbar_wait(s_addr(full + s), ph, abort_flag)) { ok = false; break; }
+                    if (!mbar_wait(s_addr(full + s), ph, abort_flag, wait_ns)) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                     const uint32_t st = smem_base + s * S::STAGE;
                     const uint32_t a_lo = ((st >> 4) & 0x3FFFu) | (1u << 16);
@@ -468,7 +470,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (issued) {
                     // let the MMAs already issued finish before the TMEM is released
                     mma_commit(s_addr(drain));
-                    const unsigned long long deadline = global_ns() + kWaitNs;
+                    const unsigned long long deadline = global_ns() + wait_ns;
                     while (!mbar_test(s_addr(drain), 0) && global_ns() < deadline) {
                     }
                 }
@@ -495,7 +497,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // operand reads in shared memory); the warp then leaves or proceeds together,
             // as tcgen05.ld below is a warp-wide (.sync.aligned) instruction
             int ready = 0;
-            if (lane == 0) ready = mbar_wait(s_addr(tfull + acc), aph, abort_flag) ? 1 : 0;
+            if (lane == 0) ready = mbar_wait(s_addr(tfull + acc), aph, abort_flag, wait_ns) ? 1 : 0;
             ready = __shfl_sync(0xffffffffu, ready, 0);
             if (!ready) {
                 if (lane == 0) give_up(abort_flag, err);
@@ -757,13 +759,14 @@ __global__ void __launch_bounds__(kRsThreads, 512 / (ROWS_ * COUT_))
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     pdl_wait();   // every global access below follows the previous kernel's completion
     pdl_trigger();
+    const unsigned long long wait_ns = a.wait_ns ? a.wait_ns : kWaitNs;
     const uint32_t tmem = *tmem_slot;
     const uint32_t smem_base = s_addr(smem);
     const uint32_t stage_base = smem_base + S::ST_OFF;
 
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
-        if (lane == 0) {
+        if (lane == 0 && !a.skip_producer) {
             // resident weights: one box {KC, COUT n, 3 ky, 3 kx} per chunk
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(s_addr(wbar)),
                          "r"((uint32_t)S::WBYTES)
@@ -780,7 +783,7 @@ __global__ void __launch_bounds__(kRsThreads, 512 / (ROWS_ * COUT_))
                 const int nrows = min(ROWS, a.H - yb);
                 for (int i = 0; i < nrows + 2 && ok; i += 2) {
                     for (int ch = 0; ch < NCH; ++ch) {
-                        if (!mbar_wait(s_addr(empty + s), ph ^ 1u, abort_flag)) { ok = false; break; }
+                        if (!mbar_wait(s_addr(empty + s), ph ^ 1u, abort_flag, wait_ns)) { ok = false; break; }
                         const uint32_t bar = s_addr(full + s);
                         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
                                      "r"(S::STAGE_TX)
@@ -804,7 +807,7 @@ __global__ void __launch_bounds__(kRsThreads, 512 / (ROWS_ * COUT_))
             int s = 0;
             uint32_t ph = 0;
             uint32_t pf_ph = 0;   // bit p: parity of the next phase of pairfree[p]
-            bool ok = mbar_wait(s_addr(wbar), 0, abort_flag), issued = false;
+            bool ok = mbar_wait(s_addr(wbar), 0, abort_flag, wait_ns), issued = false;
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const uint32_t w_lo = ((smem_base >> 4) & 0x3FFFu) | (1u << 16);
             for (int t = blockIdx.x; t < tl.total && ok; t += gridDim.x) {
@@ -816,11 +819,11 @@ __global__ void __launch_bounds__(kRsThreads, 512 / (ROWS_ * COUT_))
                     for (int ch = 0; ch < NCH; ++ch) {
                         const int sc = (s + ch) % S::STAGES;
                         const uint32_t pc = ph ^ (uint32_t)((s + ch) / S::STAGES);
-                        if (!mbar_wait(s_addr(full + sc), pc, abort_flag)) { ok = false; break; }
+                        if (!mbar_wait(s_addr(full + sc), pc, abort_flag, wait_ns)) { ok = false; break; }
                     }
                     const int k = i0 >> 1;
                     if (ok && 2 * k < nrows) {   // rows 2k, 2k + 1 start here: wait until they are zero
-                        ok = mbar_wait(s_addr(pairfree + k), (pf_ph >> k) & 1u, abort_flag);
+                        ok = mbar_wait(s_addr(pairfree + k), (pf_ph >> k) & 1u, abort_flag, wait_ns);
                         pf_ph ^= 1u << k;
                     }
                     if (!ok) break;
@@ -868,7 +871,7 @@ __global__ void __launch_bounds__(kRsThreads, 512 / (ROWS_ * COUT_))
                 give_up(abort_flag, err);
                 if (issued) {
                     mma_commit(s_addr(drain));
-                    const unsigned long long deadline = global_ns() + kWaitNs;
+                    const unsigned long long deadline = global_ns() + wait_ns;
                     while (!mbar_test(s_addr(drain), 0) && global_ns() < deadline) {
                     }
                 }
@@ -926,7 +929,7 @@ __global__ void __launch_bounds__(kRsThreads, 512 / (ROWS_ * COUT_))
             const bool valid = px < a.W;
             for (int p = 0; 2 * p < nrows; ++p) {
                 int ready = 0;
-                if (lane == 0) ready = mbar_wait(s_addr(pairfull + p), (pf_ph >> p) & 1u, abort_flag) ? 1 : 0;
+                if (lane == 0) ready = mbar_wait(s_addr(pairfull + p), (pf_ph >> p) & 1u, abort_flag, wait_ns) ? 1 : 0;
                 ready = __shfl_sync(0xffffffffu, ready, 0);
                 pf_ph ^= 1u << p;
                 if (!ready) {

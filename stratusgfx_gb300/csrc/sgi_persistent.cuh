@@ -139,7 +139,10 @@ SGI_D bool wait_deps(const PPlan& plan, const PView& pv, int v, int level) {
     }
 }
 
-__global__ void __launch_bounds__(256, 4) persistent_frame_kernel(PPlan plan) {
+// kMinBlocks: the CTAs per SM the registers are budgeted for (4: 64 registers a
+// thread, 2: 128); the batch's tuner times both.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) persistent_frame_kernel(PPlan plan) {
     extern __shared__ float4 persistent_smem_buf[];
     __shared__ uint32_t s_item;
     __shared__ int s_go;
@@ -221,16 +224,23 @@ __global__ void __launch_bounds__(256, 4) persistent_frame_kernel(PPlan plan) {
     }
 }
 
-cudaError_t persistent_occupancy(size_t smem, int* blocks_per_sm) {
+template <int kMinBlocks> cudaError_t persistent_occupancy_of(size_t smem, int* blocks_per_sm) {
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(persistent_frame_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(persistent_frame_kernel<kMinBlocks>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, persistent_frame_kernel, 256, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, persistent_frame_kernel<kMinBlocks>, 256, smem);
 }
 
-cudaError_t launch_persistent(const PPlan& plan, int grid, size_t smem, cudaStream_t s) {
-    persistent_frame_kernel<<<grid, 256, smem, s>>>(plan);
+cudaError_t persistent_occupancy(int variant, size_t smem, int* blocks_per_sm) {
+    return variant == 0 ? persistent_occupancy_of<4>(smem, blocks_per_sm) : persistent_occupancy_of<2>(smem, blocks_per_sm);
+}
+
+cudaError_t launch_persistent(const PPlan& plan, int variant, int grid, size_t smem, cudaStream_t s) {
+    if (variant == 0)
+        persistent_frame_kernel<4><<<grid, 256, smem, s>>>(plan);
+    else
+        persistent_frame_kernel<2><<<grid, 256, smem, s>>>(plan);
     return cudaGetLastError();
 }

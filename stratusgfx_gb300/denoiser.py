@@ -91,6 +91,10 @@ class KpcnDenoiser:
         B, H, W = feat.shape[:3]
         self._chk(self.lib.sgi_nn_calibrate_fp8(self.h, _p(feat), B, H, W, stage._stream_ptr(stream)))
 
+    def set_wait_test(self, wait_ns: int = 0, skip_producer: bool = False):
+        """Limit of the tensor-core convolutions' waits (0: default) and the producer test switch."""
+        self._chk(self.lib.sgi_nn_set_wait_test(self.h, int(wait_ns), 1 if skip_producer else 0))
+
     def device_status(self):
         """Synchronises; raises SgiError(SGI_ERR_TIMEOUT) if a tensor-core wait ran out."""
         self._chk(self.lib.sgi_nn_device_status(self.h))

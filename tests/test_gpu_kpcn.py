@@ -229,3 +229,32 @@ def test_fp8_and_bf16_forward_against_the_float64_oracle_on_rendered_frames():
     assert err_bf < 0.02, err_bf
     assert err_f8 < 0.05, err_f8
     net.close()
+
+
+@pytest.mark.parametrize("precision", [abi.SGI_NN_BF16, abi.SGI_NN_FP8])
+def test_tensor_core_wait_runs_out_and_the_next_forward_succeeds(precision):
+    """The producer test switch keeps every convolution's TMA producer from issuing a copy: the MMA role's
+    first wait runs out after the 2 ms limit with nothing in flight, every role leaves, and the network
+    reports SGI_ERR_TIMEOUT; with the switch off the next forward completes and equals the one before."""
+    B, H, W = 1, 64, 128
+    net = KpcnDenoiser(B, H, W, seed=2)
+    feat, noisy, prev, _ = random_problem(B, H, W, 6)
+    f, n, pv, _ = to_dev(feat, noisy, prev, noisy)
+    if precision == abi.SGI_NN_FP8:
+        net.calibrate_fp8(f)
+    net.set_precision(precision)
+    out = torch.empty((B, H, W, 4), dtype=torch.float32, device="cuda")
+    net.forward(f, n, pv, out)
+    net.device_status()
+    ref = out.clone()
+    net.set_wait_test(2_000_000, skip_producer=True)
+    net.forward(f, n, pv, out)
+    with pytest.raises(abi.SgiError) as err:
+        net.device_status()
+    assert err.value.status == abi.SGI_ERR_TIMEOUT
+    net.set_wait_test(0, skip_producer=False)
+    net.forward(f, n, pv, out)
+    net.device_status()
+    assert torch.equal(out, ref)
+    net.set_precision(abi.SGI_NN_BF16)
+    net.close()

@@ -309,6 +309,27 @@ sgi_status sgi_gi_target(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera
 /* Clears the denoiser history (vplGIDenoisedPrevFrameFbo). */
 sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream);
 
+/* Snapshot and restore of the denoiser history (no counterpart in StratusGFX,
+ * whose history lives only in its FBOs): the GI the next frame reprojects
+ * (RGBA16F, width x height x 8 bytes) and the accumulated history length
+ * (R16F, width x height x 2 bytes), device buffers, copied on `stream`;
+ * *valid / valid say whether a frame has written them (before the first frame
+ * the final pass starts from zero history). A restored context renders its next
+ * frame exactly as the context the snapshot came from would have. */
+sgi_status sgi_get_history(sgi_ctx* ctx, void* gi, void* history_length, int32_t* valid, void* stream);
+sgi_status sgi_set_history(sgi_ctx* ctx, const void* gi, const void* history_length, int32_t valid, void* stream);
+
+/* Log callback (the counterpart of STRATUS_LOG / STRATUS_ERROR, StratusLog.h:8-10):
+ * every failure a call returns is also reported with its message, level
+ * SGI_LOG_ERROR; NULL removes the callback. The callback may run on any thread
+ * that calls the library and must not call back into it. */
+#define SGI_LOG_INFO  0
+#define SGI_LOG_ERROR 1
+typedef void (*sgi_log_fn)(int32_t level, const char* message, void* user);
+void sgi_set_log_callback(sgi_log_fn fn, void* user);
+/* Sends one message through the callback (used by the library's own modules). */
+void sgi_log_message(int32_t level, const char* message);
+
 /* Synchronous copies of context scratch for parity tests.
  * which: SGI_DEBUG_*; writes at most `bytes` to host_dst; *needed (if not
  * NULL) receives the full size. */

@@ -46,6 +46,11 @@ const char* sgi_nn_last_error(const sgi_nn* net);
 int64_t sgi_nn_num_params(const sgi_nn* net);
 sgi_status sgi_nn_get_params(sgi_nn* net, float* host, int64_t n);
 sgi_status sgi_nn_set_params(sgi_nn* net, const float* host, int64_t n);
+/* The Adam state (first and second moments, same layout as the parameters, and
+ * the number of updates taken) for training checkpoints; restoring it with the
+ * parameters resumes training where it stopped. */
+sgi_status sgi_nn_get_optimizer_state(sgi_nn* net, float* m, float* v, int64_t n, int64_t* step);
+sgi_status sgi_nn_set_optimizer_state(sgi_nn* net, const float* m, const float* v, int64_t n, int64_t step);
 /* Gradients of the last sgi_nn_train_step (same layout as the parameters). */
 sgi_status sgi_nn_get_grads(sgi_nn* net, float* host, int64_t n);
 

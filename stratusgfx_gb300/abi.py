@@ -28,6 +28,9 @@ SGI_MAX_VPLS_BEFORE_CULL = 10000
 SGI_MAX_VPLS_PER_FRAME = 4480
 SGI_NUM_PASS_TIMES = 5
 SGI_NUM_PASS_TIMES_SPLIT = 7
+SGI_LOG_INFO = 0
+SGI_LOG_ERROR = 1
+LOG_FN = C.CFUNCTYPE(None, C.c_int32, C.c_char_p, C.c_void_p)
 SGI_SHADING_EXACT = 0
 SGI_SHADING_FAST = 1
 SGI_LANE_CHECKS = 12
@@ -179,6 +182,10 @@ EXPORTS = {
     "sgi_get_pass_times": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "sgi_launch_count": (C.c_int64, [C.c_void_p]),
     "sgi_set_shading_precision": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "sgi_get_history": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
+    "sgi_set_history": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "sgi_set_log_callback": (None, [C.c_void_p, C.c_void_p]),
+    "sgi_log_message": (None, [C.c_int32, C.c_char_p]),
     "sgi_get_shading_precision": (C.c_int32, [C.c_void_p]),
     "sgi_lane_selftest": (C.c_int32, [C.c_int32, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
     "sgi_slot_cache_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
@@ -199,6 +206,9 @@ EXPORTS = {
     "sgi_nn_get_params": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64]),
     "sgi_nn_set_params": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64]),
     "sgi_nn_get_grads": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "sgi_nn_get_optimizer_state": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                               C.POINTER(C.c_int64)]),
+    "sgi_nn_set_optimizer_state": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64]),
     "sgi_nn_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                    C.c_void_p, C.c_void_p]),
     "sgi_nn_train_step": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,

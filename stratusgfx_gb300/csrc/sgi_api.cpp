@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <mutex>
 #include <string>
 
 #include "../../include/sgi.h"
@@ -26,8 +27,14 @@
 
 namespace {
 
+// the log callback (sgi_set_log_callback); every failure of a context is reported through it
+std::mutex g_log_lock;
+sgi_log_fn g_log_fn = nullptr;
+void* g_log_user = nullptr;
+
 sgi_status fail(sgi_ctx* c, sgi_status s, const std::string& msg) {
     if (c) c->err = msg;
+    sgi_log_message(SGI_LOG_ERROR, msg.c_str());
     return s;
 }
 
@@ -122,6 +129,23 @@ inline void record(sgi_ctx* c, int k, cudaStream_t s) {
 
 extern "C" {
 
+void sgi_set_log_callback(sgi_log_fn fn, void* user) {
+    std::lock_guard<std::mutex> g(g_log_lock);
+    g_log_fn = fn;
+    g_log_user = user;
+}
+
+void sgi_log_message(int32_t level, const char* msg) {
+    sgi_log_fn fn;
+    void* user;
+    {
+        std::lock_guard<std::mutex> g(g_log_lock);
+        fn = g_log_fn;
+        user = g_log_user;
+    }
+    if (fn && msg) fn(level, msg, user);
+}
+
 int32_t sgi_abi_version(void) { return SGI_ABI_VERSION; }
 
 const char* sgi_status_string(sgi_status s) {
@@ -168,6 +192,7 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     *out = nullptr;
     std::string why;
     sgi_status st = validate_config(cfg, why);
+    if (st != SGI_OK) sgi_log_message(SGI_LOG_ERROR, ("sgi_create: " + why).c_str());
     if (st != SGI_OK) return st;
     sgi_ctx* c = new (std::nothrow) sgi_ctx();
     if (!c) return SGI_ERR_OOM;
@@ -479,6 +504,30 @@ sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream) {
     ctx->hist_cur = 0;
     ctx->have_history = false;
     ctx->have_taa = false;
+    return SGI_OK;
+}
+
+sgi_status sgi_get_history(sgi_ctx* ctx, void* gi, void* history_length, int32_t* valid, void* stream) {
+    if (!ctx || !gi || !history_length || !valid) return fail(ctx, SGI_ERR_ARG, "NULL history output");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t P = pixels(ctx->cfg);
+    SGI_CUDA(ctx, cudaMemcpyAsync(gi, ctx->gi_hist[ctx->hist_cur], P * sizeof(uint2), cudaMemcpyDeviceToDevice, s),
+             "copy gi history");
+    SGI_CUDA(ctx, cudaMemcpyAsync(history_length, ctx->hist_depth[ctx->hist_cur], P * sizeof(uint16_t),
+                                  cudaMemcpyDeviceToDevice, s), "copy history length");
+    *valid = ctx->have_history ? 1 : 0;
+    return SGI_OK;
+}
+
+sgi_status sgi_set_history(sgi_ctx* ctx, const void* gi, const void* history_length, int32_t valid, void* stream) {
+    if (!ctx || !gi || !history_length) return fail(ctx, SGI_ERR_ARG, "NULL history input");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t P = pixels(ctx->cfg);
+    SGI_CUDA(ctx, cudaMemcpyAsync(ctx->gi_hist[ctx->hist_cur], gi, P * sizeof(uint2), cudaMemcpyDeviceToDevice, s),
+             "restore gi history");
+    SGI_CUDA(ctx, cudaMemcpyAsync(ctx->hist_depth[ctx->hist_cur], history_length, P * sizeof(uint16_t),
+                                  cudaMemcpyDeviceToDevice, s), "restore history length");
+    ctx->have_history = valid != 0;
     return SGI_OK;
 }
 

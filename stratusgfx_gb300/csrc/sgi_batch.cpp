@@ -40,6 +40,7 @@ constexpr int kShapes[5][2] = {{32, 8}, {16, 16}, {64, 4}, {128, 2}, {8, 32}};
 
 sgi_status bfail(sgi_batch* b, sgi_status s, const std::string& msg) {
     if (b) b->err = msg;
+    sgi_log_message(SGI_LOG_ERROR, msg.c_str());
     return s;
 }
 
@@ -196,13 +197,14 @@ sgi_status build_persistent(sgi_batch* b, int32_t tune_frames, cudaStream_t s) {
             else sgi::exact::persistent_fill_view(d, out);
         }
         const int blocks = ((cfg.width + 15) / 16) * ((cfg.height + 15) / 16);
+        const int chunks = (blocks + sgi::kPBlocksPerItem - 1) / sgi::kPBlocksPerItem;
         int32_t* c = counts.data() + (size_t)i * sgi::kPMaxLevels;
         c[sgi::kPVis] = (v.ctx->num_vpls + 255) / 256;
         c[sgi::kPCompact] = 1;
-        c[sgi::kPDirect] = blocks;
-        c[sgi::kPTile] = blocks;
-        c[sgi::kPGather] = blocks;
-        for (int pass = 1; pass < cfg.denoise_passes; ++pass) c[sgi::kPAtrous + pass - 1] = blocks;
+        c[sgi::kPDirect] = chunks;
+        c[sgi::kPTile] = chunks;
+        c[sgi::kPGather] = chunks;
+        for (int pass = 1; pass < cfg.denoise_passes; ++pass) c[sgi::kPAtrous + pass - 1] = chunks;
         if (cfg.max_visible > max_visible) max_visible = cfg.max_visible;
     }
     // dispatch order: pass by pass, every view's items of a pass before the next pass

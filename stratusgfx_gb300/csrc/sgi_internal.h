@@ -93,12 +93,13 @@ struct ShadowCasters {
 enum PLevel : int {
     kPVis = 0,        // VPL visibility flags, 256 VPLs per item
     kPCompact = 1,    // stable compaction of the visible VPLs, one item
-    kPDirect = 2,     // deferred lighting, one 16x16 pixel block per item
-    kPTile = 3,       // tile mean + tile cull, one 16x16 tile per item
-    kPGather = 4,     // gather + denoise pass 0, one tile per item
+    kPDirect = 2,     // deferred lighting, kPBlocksPerItem 16x16 pixel blocks per item
+    kPTile = 3,       // tile mean + tile cull, kPBlocksPerItem 16x16 tiles per item
+    kPGather = 4,     // gather + denoise pass 0, kPBlocksPerItem tiles per item
     kPAtrous = 5,     // + (pass - 1): a-trous pass 1 .. n-2; the final pass follows the last one
 };
 constexpr int kPMaxLevels = kPAtrous + SGI_MAX_DENOISE_PASSES - 1;
+constexpr int kPBlocksPerItem = 4;   // 16x16 pixel blocks of one item of the pixel passes
 constexpr int kPMaxViews = 256;
 SGI_HD_INLINE uint32_t pitem(int view, int level, int index) {
     return (uint32_t)view | ((uint32_t)level << 8) | ((uint32_t)index << 13);

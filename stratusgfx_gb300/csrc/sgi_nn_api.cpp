@@ -377,6 +377,7 @@ using sgi::nn::Net;
 
 static sgi_status nn_fail(sgi_nn* n, sgi_status s, const std::string& m) {
     if (n) n->err = m;
+    sgi_log_message(SGI_LOG_ERROR, m.c_str());
     return s;
 }
 static sgi_status nn_cuda(sgi_nn* n, cudaError_t e, const char* what) {
@@ -423,6 +424,24 @@ sgi_status sgi_nn_get_params(sgi_nn* n, float* host, int64_t count) {
     cudaError_t e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaMemcpy(host, n->net.w32, n->net.nparams * sizeof(float), cudaMemcpyDeviceToHost);
     return e == cudaSuccess ? SGI_OK : nn_cuda(n, e, "get params");
+}
+
+sgi_status sgi_nn_get_optimizer_state(sgi_nn* n, float* m, float* v, int64_t count, int64_t* step) {
+    if (!n || !m || !v || !step || count < (int64_t)n->net.nparams) return SGI_ERR_ARG;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(m, n->net.m32, n->net.nparams * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(v, n->net.v32, n->net.nparams * sizeof(float), cudaMemcpyDeviceToHost);
+    *step = n->step;
+    return e == cudaSuccess ? SGI_OK : nn_cuda(n, e, "get optimizer state");
+}
+
+sgi_status sgi_nn_set_optimizer_state(sgi_nn* n, const float* m, const float* v, int64_t count, int64_t step) {
+    if (!n || !m || !v || count < (int64_t)n->net.nparams || step < 0 || step > 0x7fffffff) return SGI_ERR_ARG;
+    cudaError_t e = cudaMemcpy(n->net.m32, m, n->net.nparams * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(n->net.v32, v, n->net.nparams * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return nn_cuda(n, e, "set optimizer state");
+    n->step = (int)step;
+    return SGI_OK;
 }
 
 sgi_status sgi_nn_set_params(sgi_nn* n, const float* host, int64_t count) {

@@ -37,7 +37,7 @@ struct PView {
     const sgi_vpl* vpls;
     const sgi_atlas_entry* entries;
     int32_t num_vpls, max_visible, L;
-    int32_t width, height, tiles_x, passes;
+    int32_t width, height, tiles_x, blocks, passes;
     uint8_t* flags;
     sgi_vpl* cv;
     sgi_atlas_entry* ce;
@@ -65,6 +65,7 @@ void persistent_fill_view(const PViewDesc& d, unsigned char* out) {
     v.vpls = d.vpls; v.entries = d.entries; v.num_vpls = d.num_vpls; v.max_visible = cfg.max_visible;
     v.L = cfg.max_vpls_per_tile;
     v.width = cfg.width; v.height = cfg.height; v.tiles_x = (cfg.width + 15) / 16; v.passes = cfg.denoise_passes;
+    v.blocks = v.tiles_x * ((cfg.height + 15) / 16);
     v.flags = d.flags; v.cv = d.cv; v.ce = d.ce; v.visible_index = d.visible_index; v.vpr = d.vpr;
     v.stage1 = d.stage1; v.lists = d.lists; v.csm = d.csm; v.g = d.cur; v.cam = d.cam;
     GatherParams& p = v.gp;
@@ -148,18 +149,18 @@ __global__ void __launch_bounds__(256, kMinBlocks) persistent_frame_kernel(PPlan
     __shared__ int s_go;
     __shared__ sgi_tile_stage1 s_tile;
     const int tid = threadIdx.x;
+    // thread 0 takes the next queue position while the CTA works on the current item
+    unsigned next = tid == 0 ? atomicAdd(&plan.q->next, 1u) : 0u;
     for (;;) {
         if (tid == 0) {
             uint32_t it = 0xffffffffu;
             int go = 0;
-            if (*(volatile int*)plan.status == SGI_OK) {
-                const unsigned i = atomicAdd(&plan.q->next, 1u);
-                if (i < (unsigned)plan.num_items) {
-                    it = plan.items[i];
-                    const int v = (int)(it & 0xffu), level = (int)((it >> 8) & 0x1fu);
-                    const PView& pv = *reinterpret_cast<const PView*>(plan.views + (size_t)v * plan.view_bytes);
-                    go = wait_deps(plan, pv, v, level) ? 1 : 0;
-                }
+            if (*(volatile int*)plan.status == SGI_OK && next < (unsigned)plan.num_items) {
+                it = plan.items[next];
+                const int v = (int)(it & 0xffu), level = (int)((it >> 8) & 0x1fu);
+                const PView& pv = *reinterpret_cast<const PView*>(plan.views + (size_t)v * plan.view_bytes);
+                go = wait_deps(plan, pv, v, level) ? 1 : 0;
+                if (go) next = atomicAdd(&plan.q->next, 1u);
             }
             s_item = it;
             s_go = go;
@@ -170,38 +171,46 @@ __global__ void __launch_bounds__(256, kMinBlocks) persistent_frame_kernel(PPlan
         const int v = (int)(it & 0xffu), level = (int)((it >> 8) & 0x1fu), index = (int)(it >> 13);
         const PView& pv = *reinterpret_cast<const PView*>(plan.views + (size_t)v * plan.view_bytes);
         if (!plan.skip[v * kPMaxLevels + level]) {
-            const int bx = index % pv.tiles_x, by = index / pv.tiles_x;
-            const int x = bx * 16 + (tid & 15), y = by * 16 + (tid >> 4);
-            const bool inside = x < pv.width && y < pv.height;
             if (level == kPVis) {
                 const int i = index * 256 + tid;
                 if (i < pv.num_vpls) pv.flags[i] = vpl_visible(pv.vpls, i, pv.csm);
             } else if (level == kPCompact) {
                 compact_vpls<256>(pv.vpls, pv.entries, pv.flags, pv.num_vpls, pv.max_visible, pv.cv, pv.ce,
                                   pv.visible_index, pv.vpr, tid);
-            } else if (level == kPDirect) {
-                if (inside) deferred_pixel(pv.dp, x, y);
-            } else if (level == kPTile) {
-                tile_mean(pv.width, pv.height, 16, bx, by, tid, pv.g, pv.cam, nullptr, &s_tile);
-                __syncthreads();
-                if (tid == 0) pv.stage1[index] = s_tile;
-                const V3 tp = v3(s_tile.average_position[0], s_tile.average_position[1], s_tile.average_position[2]);
-                const V3 tn = v3(s_tile.average_normal[0], s_tile.average_normal[1], s_tile.average_normal[2]);
-                tile_cull(pv.L, tp, tn, pv.vpr, __ldg(pv.visible_index),
-                          reinterpret_cast<uint32_t*>(persistent_smem_buf), pv.lists + (size_t)index * (1 + pv.L),
-                          tid);
-            } else if (level == kPGather) {
-                StagedList* staged = reinterpret_cast<StagedList*>(persistent_smem_buf);
-                stage_tile_list(pv.gp, index, staged, tid, 256);
-                __syncthreads();
-                if (inside) gather_pixel<true>(pv.gp, x, y, staged);
-            } else if (level < kPAtrous + pv.passes - 2) {
-                const int pass = level - kPAtrous + 1;
-                if (inside)
-                    atrous_pixel(pv.width, pv.height, 1 << pass, pv.guide, pv.pass_buf[pass - 1], pv.pass_buf[pass],
-                                 x, y);
             } else {
-                if (inside) denoise_final_pixel(pv.dl, x, y);
+                // the pixel passes: kPBlocksPerItem consecutive 16x16 blocks (tiles) an item
+                const int b1 = min((index + 1) * kPBlocksPerItem, pv.blocks);
+                for (int b = index * kPBlocksPerItem; b < b1; ++b) {
+                    const int bx = b % pv.tiles_x, by = b / pv.tiles_x;
+                    const int x = bx * 16 + (tid & 15), y = by * 16 + (tid >> 4);
+                    const bool inside = x < pv.width && y < pv.height;
+                    if (level == kPDirect) {
+                        if (inside) deferred_pixel(pv.dp, x, y);
+                    } else if (level == kPTile) {
+                        tile_mean(pv.width, pv.height, 16, bx, by, tid, pv.g, pv.cam, nullptr, &s_tile);
+                        __syncthreads();
+                        if (tid == 0) pv.stage1[b] = s_tile;
+                        const V3 tp = v3(s_tile.average_position[0], s_tile.average_position[1],
+                                         s_tile.average_position[2]);
+                        const V3 tn = v3(s_tile.average_normal[0], s_tile.average_normal[1], s_tile.average_normal[2]);
+                        tile_cull(pv.L, tp, tn, pv.vpr, __ldg(pv.visible_index),
+                                  reinterpret_cast<uint32_t*>(persistent_smem_buf), pv.lists + (size_t)b * (1 + pv.L),
+                                  tid);
+                    } else if (level == kPGather) {
+                        StagedList* staged = reinterpret_cast<StagedList*>(persistent_smem_buf);
+                        stage_tile_list(pv.gp, b, staged, tid, 256);
+                        __syncthreads();
+                        if (inside) gather_pixel<true>(pv.gp, x, y, staged);
+                        __syncthreads();   // the staged list is rewritten by the next block
+                    } else if (level < kPAtrous + pv.passes - 2) {
+                        const int pass = level - kPAtrous + 1;
+                        if (inside)
+                            atrous_pixel(pv.width, pv.height, 1 << pass, pv.guide, pv.pass_buf[pass - 1],
+                                         pv.pass_buf[pass], x, y);
+                    } else {
+                        if (inside) denoise_final_pixel(pv.dl, x, y);
+                    }
+                }
             }
         }
         __syncthreads();

@@ -21,6 +21,7 @@ import torch
 from . import abi, stage
 from . import scene as S
 
+CKPT_MAGIC = b"SGICKPT1"
 MAGIC = b"SGIKPCN1"
 LAYERS = [(16, 32), (32, 32), (32, 64), (64, 64), (64, 128), (128, 128), (192, 64), (64, 64), (96, 32), (32, 32),
           (32, 32)]
@@ -114,6 +115,46 @@ class KpcnDenoiser:
         with open(path, "wb") as f:
             f.write(blob + struct.pack("<I", zlib.crc32(blob) & 0xFFFFFFFF))
 
+    def optimizer_state(self):
+        """(m, v, step): the Adam moments and the number of updates taken."""
+        m = np.empty(self.n, np.float32)
+        v = np.empty(self.n, np.float32)
+        step = C.c_int64()
+        self._chk(self.lib.sgi_nn_get_optimizer_state(self.h, m.ctypes.data_as(C.c_void_p), v.ctypes.data_as(C.c_void_p),
+                                                      self.n, C.byref(step)))
+        return m, v, step.value
+
+    def set_optimizer_state(self, m, v, step: int):
+        m = np.ascontiguousarray(m, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        self._chk(self.lib.sgi_nn_set_optimizer_state(self.h, m.ctypes.data_as(C.c_void_p),
+                                                      v.ctypes.data_as(C.c_void_p), self.n, int(step)))
+
+    def save_checkpoint(self, path: str):
+        """Training checkpoint: parameters, Adam moments and step (magic, version 1, layer shapes, CRC32)."""
+        m, v, step = self.optimizer_state()
+        shapes = b"".join(struct.pack("<ii", ci, co) for ci, co in LAYERS)
+        header = CKPT_MAGIC + struct.pack("<IIqq", 1, len(LAYERS), self.n, step) + shapes
+        blob = header + self.params().tobytes() + m.tobytes() + v.tobytes()
+        os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+        with open(path, "wb") as f:
+            f.write(blob + struct.pack("<I", zlib.crc32(blob) & 0xFFFFFFFF))
+
+    def load_checkpoint(self, path: str):
+        with open(path, "rb") as f:
+            blob = f.read()
+        data, crc = blob[:-4], struct.unpack("<I", blob[-4:])[0]
+        if data[:8] != CKPT_MAGIC or zlib.crc32(data) & 0xFFFFFFFF != crc:
+            raise ValueError(f"{path}: bad magic or CRC")
+        version, nlayers, n, step = struct.unpack("<IIqq", data[8:32])
+        shapes = [struct.unpack("<ii", data[32 + 8 * i:40 + 8 * i]) for i in range(nlayers)]
+        if version != 1 or n != self.n or shapes != LAYERS:
+            raise ValueError(f"{path}: incompatible checkpoint ({version}, {shapes})")
+        off = 32 + 8 * nlayers
+        arr = np.frombuffer(data[off:off + 12 * n], dtype=np.float32)
+        self.set_params(arr[:n])
+        self.set_optimizer_state(arr[n:2 * n], arr[2 * n:], step)
+
     def load(self, path: str):
         with open(path, "rb") as f:
             blob = f.read()
@@ -188,8 +229,11 @@ def make_dataset(num_frames: int, H: int = 256, W: int = 256, frames_per_room: i
 
 
 def train(net: KpcnDenoiser, ds: Dataset, steps: int = 3000, batch: int = 16, crop: int = 128, lr: float = 2e-3,
-          seed: int = 0, log=print, log_every: int = 250) -> list:
-    """Adam on random crops; cosine learning-rate decay. Returns the logged losses."""
+          seed: int = 0, log=print, log_every: int = 250, checkpoint: str | None = None, checkpoint_every: int = 500,
+          start: int = 0) -> list:
+    """Adam on random crops; cosine learning-rate decay. Returns the logged losses. With `checkpoint`, the
+    parameters, Adam moments and step are written there every checkpoint_every steps; `start` resumes a run
+    at that step (after load_checkpoint): the crop sampler and the learning-rate schedule continue from it."""
     g = torch.Generator(device="cpu").manual_seed(seed)
     H, W = ds.feat.shape[1:3]
     fb = torch.empty((batch, crop, crop, 16), dtype=torch.bfloat16, device="cuda")
@@ -202,6 +246,8 @@ def train(net: KpcnDenoiser, ds: Dataset, steps: int = 3000, batch: int = 16, cr
         idx = torch.randint(0, ds.n, (batch,), generator=g)
         ys = torch.randint(0, (H - crop) // 4 + 1, (batch,), generator=g) * 4
         xs = torch.randint(0, (W - crop) // 4 + 1, (batch,), generator=g) * 4
+        if it < start:
+            continue
         for b in range(batch):
             i, y, x = int(idx[b]), int(ys[b]), int(xs[b])
             fb[b].copy_(ds.feat[i, y:y + crop, x:x + crop])
@@ -214,5 +260,7 @@ def train(net: KpcnDenoiser, ds: Dataset, steps: int = 3000, batch: int = 16, cr
         if want:
             losses.append((it, loss))
             log(f"step {it:5d} loss {loss:.5f} lr {cur_lr:.2e} ({time.time() - t0:.1f} s)")
+        if checkpoint and (it + 1) % checkpoint_every == 0:
+            net.save_checkpoint(checkpoint)
     torch.cuda.synchronize()
     return losses

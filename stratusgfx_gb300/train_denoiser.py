@@ -30,6 +30,8 @@ def main():
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=100)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--checkpoint", default=None, help="write parameters + Adam state here every 500 steps")
+    ap.add_argument("--resume", action="store_true", help="continue from --checkpoint")
     args = ap.parse_args()
     import torch
 
@@ -40,8 +42,13 @@ def main():
     ds = denoiser.make_dataset(args.frames, args.size, args.size, seed=args.seed)
     t_data = time.time() - t0
     net = denoiser.KpcnDenoiser(args.batch, args.crop, args.crop, seed=args.seed)
+    start = 0
+    if args.resume and args.checkpoint and os.path.exists(args.checkpoint):
+        net.load_checkpoint(args.checkpoint)
+        start = net.optimizer_state()[2]
     t0 = time.time()
-    losses = denoiser.train(net, ds, steps=args.steps, batch=args.batch, crop=args.crop, lr=args.lr, seed=args.seed)
+    losses = denoiser.train(net, ds, steps=args.steps, batch=args.batch, crop=args.crop, lr=args.lr, seed=args.seed,
+                            checkpoint=args.checkpoint, start=start)
     t_train = time.time() - t0
     out = args.out or denoiser.WEIGHTS
     net.save(out)

@@ -68,3 +68,23 @@ def test_create_rejects_bad_configs_before_touching_the_device():
         assert lib.sgi_create(C.byref(cfg), C.byref(h)) == abi.SGI_ERR_ARG, field
     assert lib.sgi_create(None, C.byref(h)) == abi.SGI_ERR_ARG
     assert lib.sgi_status_string(abi.SGI_ERR_CAP) == b"capacity exceeded"
+
+
+def test_log_callback_receives_failures():
+    """sgi_set_log_callback: a rejected configuration is reported through the callback with its reason."""
+    lib = abi.load(build_if_missing=True)
+    got = []
+    cb = abi.LOG_FN(lambda level, msg, user: got.append((level, msg.decode())))
+    lib.sgi_set_log_callback(C.cast(cb, C.c_void_p), None)
+    try:
+        cfg = abi.config_defaults(64, 48)
+        cfg.tile_size = 40
+        h = C.c_void_p()
+        assert lib.sgi_create(C.byref(cfg), C.byref(h)) == abi.SGI_ERR_ARG
+        lib.sgi_log_message(abi.SGI_LOG_INFO, b"hello")
+    finally:
+        lib.sgi_set_log_callback(None, None)
+    assert got[0][0] == abi.SGI_LOG_ERROR and "tile_size" in got[0][1]
+    assert got[1] == (abi.SGI_LOG_INFO, "hello")
+    lib.sgi_log_message(abi.SGI_LOG_INFO, b"nobody listens")   # no callback: nothing happens
+    assert len(got) == 2

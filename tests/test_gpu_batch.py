@@ -236,3 +236,34 @@ def test_persistent_batch_rejects_unsupported_views():
     assert lib.sgi_batch_create_persistent(arr8, 1, 0, None, C.byref(h)) == abi.SGI_ERR_ARG   # 8x8 tiles
     v.st.close()
     v8.st.close()
+
+
+def test_tuner_choices_are_cached_per_viewport(tmp_path):
+    """stratusgfx_gb300.tuning: the first batch tunes and records every view's block shapes by viewport; a
+    second batch of views with those viewports applies them and builds without tuning."""
+    from stratusgfx_gb300 import tuning
+    lib = abi.load()
+    cache = str(tmp_path / "shapes.json")
+    sizes = [(96, 64, 51), (160, 96, 52)]
+    runs = []
+    for _ in range(2):
+        views = [View(*view_scene(W, H, seed)) for W, H, seed in sizes]
+        for v in views:
+            v.frame()
+        arr = (abi.View * len(views))(*[v.struct() for v in views])
+        h, tuned = tuning.create_batch(arr, [(v.w.width, v.w.height) for v in views], cache=cache, tune_frames=1)
+        assert lib.sgi_batch_launch(h, None) == abi.SGI_OK
+        torch.cuda.synchronize()
+        runs.append((tuned, views, h))
+    assert runs[0][0] and not runs[1][0]
+    import json
+    entries = json.load(open(cache))
+    assert set(entries) == {"96x64:plain", "160x96:plain"}
+    gx, gy = C.c_int32(), C.c_int32()
+    for v in runs[1][1]:
+        lib.sgi_get_block_shape(v.st.ctx, abi.SGI_BLOCK_GATHER, C.byref(gx), C.byref(gy))
+        assert [gx.value, gy.value] == entries[f"{v.w.width}x{v.w.height}:plain"]["gather"]
+    for _, views, h in runs:
+        assert lib.sgi_batch_destroy(h) == abi.SGI_OK
+        for v in views:
+            v.st.close()

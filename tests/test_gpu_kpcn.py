@@ -258,3 +258,40 @@ def test_tensor_core_wait_runs_out_and_the_next_forward_succeeds(precision):
     assert torch.equal(out, ref)
     net.set_precision(abi.SGI_NN_BF16)
     net.close()
+
+
+def test_training_checkpoint_resumes_where_it_stopped(tmp_path):
+    """A checkpoint (parameters, Adam moments, step count) round-trips exactly, and training resumed from it
+    continues like the uninterrupted run (the weight gradients are summed with atomics, so the comparison is
+    within a tolerance, not bit for bit)."""
+    from stratusgfx_gb300 import denoiser
+    B, H, W = 4, 32, 32
+    rng = np.random.default_rng(8)
+    noisy = rng.uniform(0.0, 2.0, (B, H, W, 4)).astype(np.float32)
+    target = np.repeat(noisy.mean(axis=(1, 2), keepdims=True), H, 1).repeat(W, 2).astype(np.float32)
+    feat = np.zeros((B, H, W, 16), np.float32)
+    feat[..., :3] = np.log1p(noisy[..., :3])
+    f, n, pv, t = to_dev(feat, noisy, noisy.copy(), target)
+    a = KpcnDenoiser(B, H, W, seed=11)
+    for _ in range(10):
+        a.train_step(f, n, pv, t, 1e-3)
+    path = str(tmp_path / "ckpt.bin")
+    a.save_checkpoint(path)
+    b = KpcnDenoiser(B, H, W, seed=99)
+    b.load_checkpoint(path)
+    pa, (ma, va, sa) = a.params(), a.optimizer_state()
+    pb, (mb, vb, sb) = b.params(), b.optimizer_state()
+    assert sa == sb == 10
+    assert np.array_equal(pa, pb) and np.array_equal(ma, mb) and np.array_equal(va, vb)
+    la = [a.train_step(f, n, pv, t, 1e-3) for _ in range(10)]
+    lb = [b.train_step(f, n, pv, t, 1e-3) for _ in range(10)]
+    assert abs(la[-1] - lb[-1]) <= 0.05 * abs(la[-1]) + 1e-4, (la[-1], lb[-1])
+    with open(path, "r+b") as fh:
+        fh.seek(64)
+        c = fh.read(1)
+        fh.seek(64)
+        fh.write(bytes([c[0] ^ 0x55]))
+    with pytest.raises(ValueError):
+        b.load_checkpoint(path)
+    a.close()
+    b.close()

@@ -325,3 +325,30 @@ def test_converged_target_bit_exact(small, mode):
                       small.sc.entries[idx[1:1 + cnt]], cnt, lists, small.hs.cubes, TIME, 6)
     assert_bit_exact(out.cpu().numpy(), ref, f"converged target mode={mode}")
     st.close()
+
+
+def test_history_snapshot_restores_the_next_frame(small):
+    """sgi_get_history after frame 1 on one context, sgi_set_history on a fresh one: frame 2 of both is
+    bit-identical (the temporal pass reads only the history and the inputs)."""
+    lib = abi.load()
+    H, W = small.w.height, small.w.width
+    a, _ = small.stage(1)
+    b, _ = small.stage(1)
+    out_a = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+    out_b = torch.empty_like(out_a)
+    a.render_frame(small.g[1], small.g[0], small.hs.camera(1), out_a, TIME + 16.0, FPS)
+    gi = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+    hl = torch.empty((H, W), dtype=torch.float16, device="cuda")
+    valid = C.c_int32(-1)
+    abi.check(lib.sgi_get_history(a.ctx, C.c_void_p(gi.data_ptr()), C.c_void_p(hl.data_ptr()), C.byref(valid),
+                                  None), a.ctx)
+    assert valid.value == 1
+    abi.check(lib.sgi_set_history(b.ctx, C.c_void_p(gi.data_ptr()), C.c_void_p(hl.data_ptr()), 1, None), b.ctx)
+    for st, out in ((a, out_a), (b, out_b)):
+        st.set_shadow_maps(small.csm[2], small.cubes)
+        st.render_frame(small.g[2], small.g[1], small.hs.camera(2), out, TIME + 32.0, FPS)
+    torch.cuda.synchronize()
+    assert torch.equal(out_a.view(torch.int16), out_b.view(torch.int16))
+    assert lib.sgi_get_history(a.ctx, None, None, C.byref(valid), None) == abi.SGI_ERR_ARG
+    a.close()
+    b.close()

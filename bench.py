@@ -52,6 +52,8 @@ def parse():
                          "--warmup + --steps frames of sgi_render_frame only (no e2e or CPU legs)")
     ap.add_argument("--neural", action="store_true",
                     help="with --profile: frames of sgi_render_frame_neural (K = 2) instead")
+    ap.add_argument("--persistent", action="store_true",
+                    help="with --profile: 8 views of 960x540 of one room rendered by the persistent batch kernel")
     ap.add_argument("--fast", action="store_true",
                     help="with --profile: the shading kernels in their tolerance mode (SGI_SHADING_FAST)")
     ap.add_argument("--fp8", action="store_true",
@@ -157,7 +159,7 @@ def kernel_bytes(w) -> dict:
 # kernel (group) -> index into sgi_get_pass_times with the denoise split, and the CUDA kernels it holds
 KERNELS = {"vpl_cull": (0, "vpl_vis_flags_kernel + vpl_compact_kernel"),
            "deferred_pbr_csm": (1, "deferred_pbr_csm_kernel"),
-           "tile_cull": (2, "tile_stage1_kernel + tile_keys_kernel + tile_select_kernel"),
+           "tile_cull": (2, "tile_stage1_kernel + tile_cull_kernel"),
            "vpl_gather": (3, "vpl_gather_kernel (gather + denoise pass 0 merge + guide)"),
            "atrous": (5, "atrous_kernel x (denoise passes - 2)"),
            "denoise_final": (6, "denoise_final_kernel")}
@@ -1045,12 +1047,60 @@ def run_reference(args):
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_profile_persistent(args):
+    """Frames of 8 views (960x540, one 40-box room with 2048 VPLs, K = 8) through the persistent batch kernel
+    (untuned shape), for kernel captures (about 1 GB on the device)."""
+    import ctypes as C
+
+    import torch
+
+    from stratusgfx_gb300 import abi, stage
+    from stratusgfx_gb300 import scene as S
+    lib = abi.load()
+    views = []
+    room = None
+    for i in range(8):
+        w = S.Workload(f"view{i}_960x540", 960, 540, 40, 2048, 4, 2048, 128, abi.SGI_CUBE_F16, 8, 5, 1)
+        sc = S.make_scene(1234 + 2, w.width, w.height, w.num_boxes, w.num_vpls, 1, num_points=w.num_points,
+                          csm_resolution=w.csm_resolution, camera_seed=300 + i)
+        vs = stage.DeviceScene(sc, w) if room is None else stage.ViewScene(room, sc, w)
+        room = room or vs
+        st = stage.GiStage(stage.workload_config(w))
+        if args.fast:
+            abi.check(lib.sgi_set_shading_precision(st.ctx, abi.SGI_SHADING_FAST), st.ctx)
+        st.set_lights(vs.vpls, vs.entries, vs.points)
+        st.set_shadow_maps(vs.csms[1], vs.cubes)
+        out = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
+        st.render_frame(vs.gbuffers[1], vs.gbuffers[0], vs.camera(1), out, 1016.0, 60.0)
+        o = dict(st=st, out=out, cur=vs.gbuffers[1].struct(), prev=vs.gbuffers[0].struct(), cam=vs.camera(1), vs=vs)
+        views.append(o)
+    arr = (abi.View * len(views))(*[abi.View(o["st"].ctx.value, C.addressof(o["cur"]), C.addressof(o["prev"]),
+                                             C.addressof(o["cam"]), abi.FrameParams(1032.0, 60.0),
+                                             o["out"].data_ptr()) for o in views])
+    h = C.c_void_p()
+    abi.check(lib.sgi_batch_create_persistent(arr, len(views), 0, None, C.byref(h)))
+    for _ in range(args.warmup + args.steps):
+        abi.check(lib.sgi_batch_launch(h, None))
+    torch.cuda.synchronize()
+    abi.check(lib.sgi_batch_status(h))
+    regs, ctas = C.c_int32(), C.c_int32()
+    abi.check(lib.sgi_batch_persistent_shape(h, C.byref(regs), C.byref(ctas)))
+    abi.check(lib.sgi_batch_destroy(h))
+    print(json.dumps({"profile_case": "8 views 960x540 persistent" + (" fast" if args.fast else ""),
+                      "launches": args.warmup + args.steps, "registers": regs.value, "ctas": ctas.value}))
+    for o in views:
+        o["st"].close()
+
+
 def run_profile(args):
     """Frames of the workload only, for kernel captures (about 0.7 GB on the device)."""
     import torch
 
     from stratusgfx_gb300 import stage
     from stratusgfx_gb300 import scene as S
+    if args.persistent:
+        run_profile_persistent(args)
+        return
     w = workload(args.workload)
     sc = S.make_scene(1234 + 2, w.width, w.height, w.num_boxes, w.num_vpls, 2, vpl_radius=w.vpl_radius,
                       num_points=w.num_points, csm_resolution=w.csm_resolution)

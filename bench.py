@@ -54,6 +54,8 @@ def parse():
                     help="with --profile: frames of sgi_render_frame_neural (K = 2) instead")
     ap.add_argument("--persistent", action="store_true",
                     help="with --profile: 8 views of 960x540 of one room rendered by the persistent batch kernel")
+    ap.add_argument("--atrous", choices=["direct", "staged"], default=None,
+                    help="with --profile: the a-trous tap staging (default: the library's default)")
     ap.add_argument("--fast", action="store_true",
                     help="with --profile: the shading kernels in their tolerance mode (SGI_SHADING_FAST)")
     ap.add_argument("--fp8", action="store_true",
@@ -161,7 +163,7 @@ KERNELS = {"vpl_cull": (0, "vpl_vis_flags_kernel + vpl_compact_kernel"),
            "deferred_pbr_csm": (1, "deferred_pbr_csm_kernel"),
            "tile_cull": (2, "tile_stage1_kernel + tile_cull_kernel"),
            "vpl_gather": (3, "vpl_gather_kernel (gather + denoise pass 0 merge + guide)"),
-           "atrous": (5, "atrous_kernel x (denoise passes - 2)"),
+           "atrous": (5, "atrous_staged_kernel x (denoise passes - 2) (strides 2, 4, 8; atrous_kernel beyond)"),
            "denoise_final": (6, "denoise_final_kernel")}
 
 
@@ -280,6 +282,40 @@ def run_ours(args, rank, world, local_rank):
     fast_ms /= args.steps
     fast_pass_ms = per_pass(stf, frame_fast)
     stf.close()
+
+    # ---- a-trous passes with the other tap staging (SGI_ATROUS_DIRECT / _STAGED), per-pass times
+    def staging_leg(fast_mode, staged):
+        sx = stage.GiStage(cfg)
+        if fast_mode:
+            abi.check(sx.lib.sgi_set_shading_precision(sx.ctx, abi.SGI_SHADING_FAST), sx.ctx)
+        abi.check(sx.lib.sgi_set_atrous_staging(sx.ctx, abi.SGI_ATROUS_STAGED if staged else abi.SGI_ATROUS_DIRECT),
+                  sx.ctx)
+        sx.set_lights(ds.vpls, ds.entries, ds.points)
+
+        def frame_x(step):
+            k = step % frames + 1
+            sx.set_shadow_maps(ds.csms[k], ds.cubes)
+            sx.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, 1000.0 + 16.0 * step, fps)
+
+        for s in range(args.warmup):
+            frame_x(s)
+        acc = per_pass(sx, frame_x)
+        abi.check(sx.lib.sgi_device_status(sx.ctx), sx.ctx)
+        sx.close()
+        return acc
+
+    default_staged = st.lib.sgi_get_atrous_staging(st.ctx) == abi.SGI_ATROUS_STAGED
+    other_ms = staging_leg(False, not default_staged)
+    other_fast_ms = staging_leg(True, not default_staged)
+    atrous_ms = {False: (pass_ms[5], fast_pass_ms[5]), True: (other_ms[5], other_fast_ms[5])}
+    if default_staged:
+        atrous_ms = {True: atrous_ms[False], False: atrous_ms[True]}
+    staging = {"default": "staged" if default_staged else "direct",
+               "passes": "a-trous passes 1 .. n-2 (strides 2, 4, 8), ms per frame from per-pass events",
+               "exact": {"direct_ms": round(atrous_ms[False][0] / args.steps, 4),
+                         "staged_ms": round(atrous_ms[True][0] / args.steps, 4)},
+               "fast": {"direct_ms": round(atrous_ms[False][1] / args.steps, 4),
+                        "staged_ms": round(atrous_ms[True][1] / args.steps, 4)}}
     total_ms = replicas.max_over_ranks(float(sum(ms)), device="cuda")
     ms_per_step = total_ms / args.steps
     value = replicas.job_throughput(P * args.steps, world, total_ms) / 1e6
@@ -430,6 +466,7 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roof,
         "kernels": kernels,
         "fast": fast,
+        "atrous_staging": staging,
         "clocks": clock,
     }
     if rank == 0:
@@ -1107,9 +1144,12 @@ def run_profile(args):
     ds = stage.DeviceScene(sc, w)
     spp = (1 if args.fp8 else 2) if args.neural else None
     st = stage.GiStage(stage.workload_config(w, samples_per_pixel=spp) if spp else stage.workload_config(w))
+    from stratusgfx_gb300 import abi
     if args.fast:
-        from stratusgfx_gb300 import abi
         abi.check(st.lib.sgi_set_shading_precision(st.ctx, abi.SGI_SHADING_FAST), st.ctx)
+    if args.atrous is not None:
+        abi.check(st.lib.sgi_set_atrous_staging(st.ctx, {"direct": abi.SGI_ATROUS_DIRECT,
+                                                         "staged": abi.SGI_ATROUS_STAGED}[args.atrous]), st.ctx)
     st.set_lights(ds.vpls, ds.entries, ds.points)
     out = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
     net = None

@@ -362,6 +362,27 @@ sgi_status sgi_read_debug(sgi_ctx* ctx, int32_t which, void* host_dst, size_t by
 sgi_status sgi_set_shading_precision(sgi_ctx* ctx, int32_t mode);
 int32_t    sgi_get_shading_precision(const sgi_ctx* ctx);
 
+/* Where the a-trous passes 1 .. n-2 (vpl_pbr_gi_denoise.fs:307-327 at stride
+ * 2^pass) take their taps; no counterpart in StratusGFX (a fragment shader
+ * samples textures). Both modes give bit-identical results.
+ *   SGI_ATROUS_DIRECT: every tap is a clamped load from global memory.
+ *   SGI_ATROUS_STAGED (default): a CTA stages the lattice of pixels its taps
+ *     reach in shared memory with strided TMA copies (strides 2, 4 and 8 on
+ *     even widths; other passes run direct). */
+#define SGI_ATROUS_DIRECT 0
+#define SGI_ATROUS_STAGED 1
+sgi_status sgi_set_atrous_staging(sgi_ctx* ctx, int32_t mode);
+int32_t    sgi_get_atrous_staging(const sgi_ctx* ctx);
+
+/* Bounded device waits of a context's kernels (the staged a-trous pass waits
+ * for its copies): wait_ns limits each wait (0 = the default, 200 ms);
+ * skip_copies != 0 is a test switch under which no copy is issued, so that
+ * every wait runs out with nothing in flight. A wait that runs out leaves its
+ * pixels unwritten and sets SGI_ERR_TIMEOUT in the context's device status,
+ * which sgi_device_status returns (after synchronising the device) and clears. */
+sgi_status sgi_set_wait_test(sgi_ctx* ctx, int64_t wait_ns, int32_t skip_copies);
+sgi_status sgi_device_status(sgi_ctx* ctx);
+
 /* Per-pass GPU times (ms) of the last sgi_render_frame when timing is on:
  * [0] vpl cull, [1] direct lighting, [2] tile cull, [3] gather, [4] denoise;
  * with n >= 7 also the denoise pass split into [5] its a-trous passes and

@@ -33,6 +33,8 @@ SGI_LOG_ERROR = 1
 LOG_FN = C.CFUNCTYPE(None, C.c_int32, C.c_char_p, C.c_void_p)
 SGI_SHADING_EXACT = 0
 SGI_SHADING_FAST = 1
+SGI_ATROUS_DIRECT = 0
+SGI_ATROUS_STAGED = 1
 SGI_LANE_CHECKS = 12
 SGI_NO_LIGHT = 0xFFFFFFFFFFFFFFFF
 
@@ -187,6 +189,10 @@ EXPORTS = {
     "sgi_set_log_callback": (None, [C.c_void_p, C.c_void_p]),
     "sgi_log_message": (None, [C.c_int32, C.c_char_p]),
     "sgi_get_shading_precision": (C.c_int32, [C.c_void_p]),
+    "sgi_set_atrous_staging": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "sgi_get_atrous_staging": (C.c_int32, [C.c_void_p]),
+    "sgi_set_wait_test": (C.c_int32, [C.c_void_p, C.c_int64, C.c_int32]),
+    "sgi_device_status": (C.c_int32, [C.c_void_p]),
     "sgi_lane_selftest": (C.c_int32, [C.c_int32, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
     "sgi_slot_cache_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "sgi_slot_cache_destroy": (C.c_int32, [C.c_void_p]),

@@ -105,7 +105,7 @@ void free_all(sgi_ctx* c) {
     void* ptrs[] = {c->vpls, c->entries, c->points, c->shadow_points, c->shadow_entries, c->taa_hist[0],
                     c->taa_hist[1], c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
                     c->vpr, c->reservoir, c->ping[0], c->ping[1], c->merged, c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
-                    c->hist_depth[0], c->hist_depth[1]};
+                    c->hist_depth[0], c->hist_depth[1], c->dev_status};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto* p : c->pass_bufs) if (p) cudaFree(p);
     void* nnp[] = {c->nn_feat, c->nn_prev};
@@ -228,6 +228,7 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     chk(dalloc(&c->gi_hist[1], P));
     chk(dalloc(&c->hist_depth[0], P));
     chk(dalloc(&c->hist_depth[1], P));
+    chk(dalloc(&c->dev_status, 1));
     if (cfg->debug_keep_passes)
         for (int k = 0; k < cfg->denoise_passes; ++k) chk(dalloc(&c->pass_bufs[k], P));
     for (auto& ev : c->ev) chk(cudaEventCreate(&ev));
@@ -236,6 +237,7 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     chk(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
     chk(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
     if (e == cudaSuccess) chk(cudaMemset(c->visible_index, 0, sizeof(int32_t) * (1 + (size_t)cfg->max_vpls)));
+    if (e == cudaSuccess) chk(cudaMemset(c->dev_status, 0, sizeof(int32_t)));
     if (e == cudaSuccess) chk(cudaMemset(c->gi_hist[0], 0, P * sizeof(uint2)));
     if (e == cudaSuccess) chk(cudaMemset(c->gi_hist[1], 0, P * sizeof(uint2)));
     if (e == cudaSuccess) chk(cudaMemset(c->hist_depth[0], 0, P * sizeof(uint16_t)));
@@ -396,9 +398,14 @@ static sgi_status run_gi(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuffer
     const uint2* in = ctx->last_merged;
     for (int pass = 1; pass < cfg.denoise_passes - 1; ++pass) {
         uint2* out = keep ? ctx->pass_bufs[pass] : ctx->ping[pass & 1];
-        SGI_CUDA(ctx, SGI_SHADE(ctx, launch_atrous)(cfg.width, cfg.height, pass, ctx->guide, in, out, s,
-                                         ctx->block_dim(SGI_BLOCK_ATROUS)),
-                 "atrous");
+        cudaError_t e = cudaErrorNotSupported;
+        if (ctx->atrous_staged)
+            e = SGI_SHADE(ctx, launch_atrous_staged)(cfg.width, cfg.height, pass, ctx->guide, in, out, ctx->wait_ns,
+                                                     ctx->skip_copies, ctx->dev_status, s);
+        if (e == cudaErrorNotSupported)   // strides above 8, odd widths: the direct kernel
+            e = SGI_SHADE(ctx, launch_atrous)(cfg.width, cfg.height, pass, ctx->guide, in, out, s,
+                                              ctx->block_dim(SGI_BLOCK_ATROUS));
+        SGI_CUDA(ctx, e, "atrous");
         ctx->launches += 1;
         in = out;
     }
@@ -659,6 +666,35 @@ sgi_status sgi_set_shading_precision(sgi_ctx* ctx, int32_t mode) {
 
 int32_t sgi_get_shading_precision(const sgi_ctx* ctx) {
     return ctx && ctx->fast_shading ? SGI_SHADING_FAST : SGI_SHADING_EXACT;
+}
+
+sgi_status sgi_set_atrous_staging(sgi_ctx* ctx, int32_t mode) {
+    if (!ctx) return SGI_ERR_ARG;
+    if (mode != SGI_ATROUS_DIRECT && mode != SGI_ATROUS_STAGED)
+        return fail(ctx, SGI_ERR_ARG, "a-trous staging must be SGI_ATROUS_DIRECT or SGI_ATROUS_STAGED");
+    ctx->atrous_staged = mode == SGI_ATROUS_STAGED;
+    return SGI_OK;
+}
+
+int32_t sgi_get_atrous_staging(const sgi_ctx* ctx) {
+    return ctx && ctx->atrous_staged ? SGI_ATROUS_STAGED : SGI_ATROUS_DIRECT;
+}
+
+sgi_status sgi_set_wait_test(sgi_ctx* ctx, int64_t wait_ns, int32_t skip_copies) {
+    if (!ctx || wait_ns < 0) return SGI_ERR_ARG;
+    ctx->wait_ns = wait_ns;
+    ctx->skip_copies = skip_copies != 0;
+    return SGI_OK;
+}
+
+sgi_status sgi_device_status(sgi_ctx* ctx) {
+    if (!ctx) return SGI_ERR_ARG;
+    int32_t st = SGI_OK;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&st, ctx->dev_status, sizeof(st), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && st != SGI_OK) e = cudaMemset(ctx->dev_status, 0, sizeof(st));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "device status");
+    return st == SGI_OK ? SGI_OK : fail(ctx, st, "a bounded device wait ran out (its pass wrote nothing)");
 }
 
 sgi_status sgi_set_timing(sgi_ctx* ctx, int32_t enabled) {

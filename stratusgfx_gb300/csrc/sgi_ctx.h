@@ -60,6 +60,13 @@ struct sgi_ctx {
 
     // shading kernels: exact (false) or the tolerance mode (true)
     bool fast_shading = false;
+    // a-trous passes from the TMA-staged lattice (true, the default: 9-11 % faster at
+    // 1080p) or with direct tap loads
+    bool atrous_staged = true;
+    // bounded device waits: limit (0 = the kernels' default), test switch, status word
+    long long wait_ns = 0;
+    int32_t skip_copies = 0;
+    int32_t* dev_status = nullptr;
 
     // timing
     bool timing = false;

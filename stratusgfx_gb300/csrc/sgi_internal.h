@@ -158,6 +158,11 @@ struct PPlan {
     /* a-trous pass `pass` (1 .. passes-2): 5x5 taps at stride 2^pass */ \
     cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in, \
                               uint2* res_out, cudaStream_t s, dim3 block = dim3(0, 0, 0)); \
+    /* the same pass from a TMA-staged shared-memory lattice (strides 2, 4, 8; even width; */ \
+    /* cudaErrorNotSupported otherwise); a wait that runs out sets SGI_ERR_TIMEOUT in *status */ \
+    cudaError_t launch_atrous_staged(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in, \
+                                     uint2* res_out, long long wait_ns, int32_t skip_copies, int32_t* status, \
+                                     cudaStream_t s); \
     /* last pass: a-trous filter + temporal reprojection + composite */ \
     cudaError_t launch_denoise_final(const DenoiseLaunch& d, cudaStream_t s, dim3 block = dim3(0, 0, 0)); \
     cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g, \

@@ -41,6 +41,13 @@ constexpr float kEps = 0.00001f;               // PREVENT_DIV_BY_ZERO, common.gl
 constexpr float kHalfMax = 65504.0f;           // HALF_FLOAT_MAX, common.glsl:6
 constexpr float kFloatMax = 3.402823466e+38f;  // FLOAT_MAX, common.glsl:7
 
+// the global nanosecond timer (bounded waits)
+SGI_D long long global_ns() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 SGI_D float gmin(float x, float y) { return y < x ? y : x; }
 SGI_D float gmax(float x, float y) { return x < y ? y : x; }
 SGI_D float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }

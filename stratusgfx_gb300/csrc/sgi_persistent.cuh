@@ -25,12 +25,6 @@
 // write.
 #pragma once
 
-SGI_D long long global_ns() {
-    long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 // One view's parameters in device memory.
 struct PView {
     // culls

@@ -13,10 +13,13 @@
 //     approximate division and square root, hardware reciprocal square root and
 //     exponential (namespace sgi::fast): the tolerance mode, within 1e-3
 //     relative error of the restatement outside the decision margins.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <stdint.h>
 
 #include <cstring>
+#include <mutex>
 
 #include "sgi_cull.cuh"
 #include "sgi_internal.h"
@@ -312,17 +315,14 @@ cudaError_t launch_gi_target(const sgi_config& cfg, const ShadeConfig& sc, const
 // taps still accumulate one after another in the order dx = -2..2 (outer),
 // dy = -2..2 (inner), so the sums are those of the one-tap-at-a-time loop
 // (atrous_weight) bit for bit.
-SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __restrict__ guide,
-                         const uint2* __restrict__ res_in, V3 cn, float cd, float& rf0, float& rf1, float& rf2,
-                         float& rf3) {
-    int xs[5];
-    size_t rows[5];
-#pragma unroll
-    for (int d = 0; d < 5; ++d) {
-        const int xx = x + (d - 2) * step, yy = y + (d - 2) * step;
-        xs[d] = xx < 0 ? 0 : (xx > W - 1 ? W - 1 : xx);
-        rows[d] = (size_t)(yy < 0 ? 0 : (yy > H - 1 ? H - 1 : yy)) * W;
-    }
+//
+// The arithmetic takes its taps from two functors, guide_at(t) and res_at(t)
+// for tap t = 5 * (dx + 2) + (dy + 2), so that the direct kernel (taps read
+// from global memory, coordinates clamped per tap) and the staged kernel (taps
+// read from a shared-memory lattice) run the same operations in the same order.
+template <class GuideAt, class ResAt>
+SGI_D void atrous_taps(GuideAt guide_at, ResAt res_at, V3 cn, float cd, float& rf0, float& rf1, float& rf2,
+                       float& rf3) {
     // the four channel sums, two per packed register
     float2 acc01 = make_float2(0.0f, 0.0f), acc23 = make_float2(0.0f, 0.0f);
     auto accumulate = [&](float f, uint2 t) {
@@ -335,16 +335,30 @@ SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __r
     const float2 cx = f2s(cn.x), cy = f2s(cn.y), cz = f2s(cn.z);
 #pragma unroll
     for (int p = 0; p < 12; ++p) {   // taps t = 5 * (dx + 2) + (dy + 2); pairs (0,1) .. (10,11), (13,14) .. (23,24)
-        if (p == 6) accumulate(1.0f, ld_u2(res_in, rows[2] + xs[2]));   // the centre tap, weight 1
+        if (p == 6) accumulate(1.0f, res_at(12));   // the centre tap, weight 1
         const int t = p < 6 ? 2 * p : 2 * p + 1;
-        const size_t j0 = rows[t % 5] + xs[t / 5], j1 = rows[(t + 1) % 5] + xs[(t + 1) / 5];
-        const float4 g0 = __ldg(guide + j0), g1 = __ldg(guide + j1);
-        const uint2 r0 = ld_u2(res_in, j0), r1 = ld_u2(res_in, j1);
+        const float4 g0 = guide_at(t), g1 = guide_at(t + 1);
+        const uint2 r0 = res_at(t), r1 = res_at(t + 1);
         const float2 f = atrous_weight2(cx, cy, cz, ncd, g0, g1);
         accumulate(f.x, r0);
         accumulate(f.y, r1);
     }
     rf0 = acc01.x; rf1 = acc01.y; rf2 = acc23.x; rf3 = acc23.y;
+}
+
+SGI_D void atrous_filter(int x, int y, int W, int H, int step, const float4* __restrict__ guide,
+                         const uint2* __restrict__ res_in, V3 cn, float cd, float& rf0, float& rf1, float& rf2,
+                         float& rf3) {
+    int xs[5];
+    size_t rows[5];
+#pragma unroll
+    for (int d = 0; d < 5; ++d) {
+        const int xx = x + (d - 2) * step, yy = y + (d - 2) * step;
+        xs[d] = xx < 0 ? 0 : (xx > W - 1 ? W - 1 : xx);
+        rows[d] = (size_t)(yy < 0 ? 0 : (yy > H - 1 ? H - 1 : yy)) * W;
+    }
+    atrous_taps([&](int t) { return __ldg(guide + rows[t % 5] + xs[t / 5]); },
+                [&](int t) { return ld_u2(res_in, rows[t % 5] + xs[t / 5]); }, cn, cd, rf0, rf1, rf2, rf3);
 }
 
 SGI_D void atrous_pixel(int W, int H, int step, const float4* __restrict__ guide, const uint2* __restrict__ res_in,
@@ -369,6 +383,163 @@ cudaError_t launch_atrous(int32_t W, int32_t H, int32_t pass, const float4* guid
     if (block.x == 0) block = dim3(32, 8);
     dim3 grid((W + block.x - 1) / block.x, (H + block.y - 1) / block.y);
     atrous_kernel<<<grid, block, 0, s>>>(W, H, 1 << pass, guide, res_in, res_out);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------- staged a-trous pass --
+// At stride s the taps of pixel (x, y) are the pixels (x + i s, y + j s): the
+// pixels whose coordinates leave the remainders (x mod s, y mod s) form a
+// lattice on which the pass is a plain 5x5 stencil. A CTA of the staged kernel
+// takes a 16 x 8 patch of two neighbouring lattices (x remainders 2k and
+// 2k + 1, one lane each of a lane pair, so that a warp's shared-memory reads
+// are contiguous) and stages the 20 x 12 lattice points its taps reach, as
+// pixel pairs, with two TMA loads (guide and reservoir) whose traversal
+// strides are s / 2 pixel pairs in x and s rows in y. Lattice points outside
+// the image are filled by the copy with zeros and then replaced with the
+// clamped pixel's values (plain loads, only in CTAs at the image border), so
+// every tap reads what the direct kernel's clamped tap reads, and the
+// arithmetic (atrous_taps) is the same: the results are bit-identical.
+//
+// Conditions (otherwise the caller runs the direct kernel): s = 2, 4 or 8
+// (the copy's traversal stride is at most 8), an even width (pixel pairs; the
+// reservoir's rows are then multiples of 16 bytes) and 16-byte aligned
+// buffers. The wait for the copies is bounded: after `wait_ns` the CTA sets
+// SGI_ERR_TIMEOUT in `status` and returns without writing. `skip_copies` (a test switch) issues no copy, so a
+// wait runs out with nothing in flight.
+constexpr int kLatX = 16, kLatY = 8, kLatHX = kLatX + 4, kLatHY = kLatY + 4;
+
+struct AtrousStageWait {
+    long long wait_ns;
+    int32_t skip_copies;
+    int32_t* status;
+};
+
+SGI_D uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+SGI_D bool stage_wait(uint32_t bar, const AtrousStageWait& w) {
+    uint32_t done = 0;
+    const long long t0 = global_ns();
+    for (;;) {
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0, 20000;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar)
+            : "memory");
+        if (done) return true;
+        if (global_ns() - t0 > w.wait_ns) {
+            atomicCAS(w.status, SGI_OK, SGI_ERR_TIMEOUT);
+            return false;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256, 5) atrous_staged_kernel(const __grid_constant__ CUtensorMap gmap,
+                                                             const __grid_constant__ CUtensorMap rmap, int W,
+                                                             int H, int s, int ntx, int nty,
+                                                             const float4* __restrict__ guide,
+                                                             const uint2* __restrict__ res_in,
+                                                             uint2* __restrict__ res_out, AtrousStageWait wt) {
+    __shared__ __align__(128) float4 sg[kLatHY][kLatHX][2];
+    __shared__ __align__(128) uint2 sr[kLatHY][kLatHX][2];
+    __shared__ __align__(8) unsigned long long bar;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tqx = blockIdx.x % ntx, rp = blockIdx.x / ntx;
+    const int tqy = blockIdx.y % nty, ry = blockIdx.y / nty;
+    const int qx0 = tqx * kLatX, qy0 = tqy * kLatY, rx = 2 * rp;
+    const uint32_t b = smem_u32(&bar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0 && !wt.skip_copies) {
+        constexpr uint32_t kBytes = sizeof(sg) + sizeof(sr);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b), "r"(kBytes) : "memory");
+        const int c1 = rp + (s >> 1) * (qx0 - 2), c2 = ry + s * (qy0 - 2);
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+            "[%5];\n" ::"r"(smem_u32(sg)),
+            "l"(reinterpret_cast<uint64_t>(&gmap)), "r"(0), "r"(c1), "r"(c2), "r"(b)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+            "[%5];\n" ::"r"(smem_u32(sr)),
+            "l"(reinterpret_cast<uint64_t>(&rmap)), "r"(0), "r"(c1), "r"(c2), "r"(b)
+            : "memory");
+    }
+    const bool ok = __syncthreads_and(stage_wait(b, wt));
+    if (!ok) return;
+    // lattice points outside the image: the clamped pixel's values (CTA-uniform test)
+    if (qx0 < 2 || qy0 < 2 || rx + s * (qx0 + kLatHX - 3) >= W || ry + s * (qy0 + kLatHY - 3) >= H) {
+        for (int e = tid; e < kLatHX * kLatHY; e += blockDim.x) {
+            const int ex = e % kLatHX, ey = e / kLatHX;
+            const int x0 = rx + s * (qx0 - 2 + ex), y = ry + s * (qy0 - 2 + ey);
+            if (x0 >= 0 && x0 < W && y >= 0 && y < H) continue;   // x0 even, W even: x0 + 1 < W too
+            const size_t row = (size_t)(y < 0 ? 0 : (y > H - 1 ? H - 1 : y)) * W;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int xx = x0 + h, cx = xx < 0 ? 0 : (xx > W - 1 ? W - 1 : xx);
+                sg[ey][ex][h] = __ldg(guide + row + cx);
+                sr[ey][ex][h] = ld_u2(res_in, row + cx);
+            }
+        }
+        __syncthreads();
+    }
+    const int lx = lane >> 1, h = lane & 1, ly = warp;
+    const int x = rx + h + s * (qx0 + lx), y = ry + s * (qy0 + ly);
+    if (x >= W || y >= H) return;
+    const float4 gc = sg[ly + 2][lx + 2][h];
+    float rf0, rf1, rf2, rf3;
+    atrous_taps([&](int t) { return sg[ly + t % 5][lx + t / 5][h]; },
+                [&](int t) { return sr[ly + t % 5][lx + t / 5][h]; }, v3(gc.x, gc.y, gc.z), gc.w, rf0, rf1, rf2,
+                rf3);
+    const float den = gmax(kEps, rf3);
+    res_out[(size_t)y * W + x] = pack_h4(rf0 / den, rf1 / den, rf2 / den, 1.0f);
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+cudaError_t launch_atrous_staged(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in,
+                                 uint2* res_out, long long wait_ns, int32_t skip_copies, int32_t* status,
+                                 cudaStream_t s) {
+    const int st = pass >= 1 && pass <= 3 ? 1 << pass : 0;
+    if (!st || W < 2 || (W & 1) || H < 1 || ((uintptr_t)guide & 15) || ((uintptr_t)res_in & 15) || !status)
+        return cudaErrorNotSupported;
+    auto encode = tensor_map_encoder();
+    if (!encode) return cudaErrorNotSupported;
+    // pixel-pair views {8 values, W / 2 pairs, H rows}; boxes {8, 20 pairs at stride s / 2, 12 rows at stride s}
+    const cuuint64_t dim[3] = {8, (cuuint64_t)W / 2, (cuuint64_t)H};
+    const cuuint32_t box[3] = {8, (cuuint32_t)(kLatHX * st / 2), (cuuint32_t)(kLatHY * st)};
+    const cuuint32_t stride[3] = {1, (cuuint32_t)(st / 2), (cuuint32_t)st};
+    const cuuint64_t gstr[2] = {32, (cuuint64_t)W * 16};
+    const cuuint64_t rstr[2] = {16, (cuuint64_t)W * 8};
+    CUtensorMap gm, rm;
+    if (encode(&gm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)guide, dim, gstr, box, stride,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    if (encode(&rm, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, (void*)res_in, dim, rstr, box, stride,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    const int ntx = ((W + st - 1) / st + kLatX - 1) / kLatX;
+    const int nty = ((H + st - 1) / st + kLatY - 1) / kLatY;
+    const AtrousStageWait wt{wait_ns > 0 ? wait_ns : 200000000LL, skip_copies, status};
+    atrous_staged_kernel<<<dim3(ntx * (st / 2), nty * st), 256, 0, s>>>(gm, rm, W, H, st, ntx, nty, guide, res_in,
+                                                                        res_out, wt);
     return cudaGetLastError();
 }
 

@@ -378,6 +378,33 @@ SGI_D V3 lighting_burley(V3 lightColor, V3 lightDir, V3 V, V3 N, V3 baseColor, f
     V3 finalB = brdf * lightColor;
     return atten * (ambient + shadowFactor * apply_fog(finalB, viewDist, fogIntensity, sp));
 }
+// lighting_burley split like vpl_pixel / vpl_lighting2_sample: the part that
+// depends only on the pixel (BRDF_Base with unit divisors, and the fog factor
+// of the view distance) once per pixel, the rest per light; the operations and
+// their order per light are those of lighting_burley.
+struct BurleyPixel {
+    V3 dc, f0;
+    float rr, fogF;
+};
+SGI_D BurleyPixel burley_pixel(V3 baseColor, V3 baseRefl, float roughness, float metallic, float viewDist,
+                               const ShadeParams& sp) {
+    BurleyPixel b;
+    brdf_base(baseColor, baseRefl, roughness, metallic, v3s(1.0f), v3s(1.0f), sp, b.rr, b.dc, b.f0);
+    b.fogF = expf_ieee(-sp.fog_density * viewDist);
+    return b;
+}
+SGI_D V3 lighting_burley_px(const BurleyPixel& b, V3 lightColor, V3 lightDir, V3 V, V3 N, float fogIntensity,
+                            float ao, float shadowFactor, float atten, float ambientIntensity, const ShadeParams& sp) {
+    float NdotV, NdotL, NdotH, LdotH;
+    brdf_dots(V, lightDir, N, NdotV, NdotL, NdotH, LdotH);
+    V3 Fr = spec_brdf(NdotV, NdotL, NdotH, LdotH, b.rr, b.f0);
+    V3 Fd = b.dc * fd_burley(NdotV, NdotL, LdotH, b.rr);
+    V3 brdf = (Fd + Fr) * NdotL;
+    V3 ambient = brdf * ao * lightColor * ambientIntensity;
+    V3 finalB = brdf * lightColor;
+    V3 fc = v3(sp.fog_color[0], sp.fog_color[1], sp.fog_color[2]) * fogIntensity;
+    return atten * (ambient + shadowFactor * (finalB * b.fogF + fc * (1.0f - b.fogF)));
+}
 // quadraticAttenuation, pbr.glsl:255-258
 SGI_D float quadratic_atten(V3 lightDir) { float d = length(lightDir); return 1.0f / (1.0f + d * d); }
 // vplDiffuseAttenuation / vplSpecularAttenuation, pbr.glsl:260-271

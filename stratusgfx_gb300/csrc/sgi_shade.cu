@@ -106,6 +106,23 @@ struct StagedList {
     sgi_atlas_entry ent[SGI_MAX_TILE_LIST];
 };
 
+// dot(normal, normalize(lmf)) < 0 (vpl_pbr_gi.fs:171-172), evaluated as the
+// shader evaluates it, but decided from the unnormalised product when its sign
+// is certain: the dot product of the normalised vector is r * dot(N, lmf) with
+// r = 1 / length(lmf) > 0 plus rounding errors below 4u r B (u = 2^-24,
+// B = sum |N_i lmf_i|), and the rounded unnormalised product differs from the
+// exact one by less than 3u B, so |dot(N, lmf)| > 2^-16 B fixes the sign of
+// both. The guards keep every quantity normal and finite (no overflow of the
+// length, no subnormal products); otherwise the full evaluation decides.
+SGI_D bool side_negative(V3 N, V3 lmf) {
+    const float d2 = xdot(lmf, lmf);
+    const float du = xdot(N, lmf);
+    const float b = __fmaf_rn(gabs(N.z), gabs(lmf.z), __fmaf_rn(gabs(N.y), gabs(lmf.y), xmul(gabs(N.x), gabs(lmf.x))));
+    if (d2 >= 0x1p-100f && d2 <= 0x1p100f && b >= 0x1p-40f && b <= 0x1p100f && gabs(du) > xmul(b, 0x1p-16f))
+        return du < 0.0f;
+    return xdot(N, xnormalize(lmf)) < 0.0f;
+}
+
 // The sample loop of vpl_pbr_gi.fs:148-200 with the seed z starting at seedZ.
 // kStaged: the list of the pixel's tile is in `staged` (list slot = array index).
 template <bool kStaged>
@@ -154,15 +171,16 @@ SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX,
         const float lightRadius = misc.x;
         const float distance = xlength(lmf);
         if (resamples < 5) {
-            float sideCheck = xdot(normal, xnormalize(lmf));
-            if (sideCheck < 0.0f || distance > lightRadius) { ++resamples; --s; continue; }
+            if (side_negative(normal, lmf) || distance > lightRadius) { ++resamples; --s; continue; }
         }
         const float distanceRatio = gclamp((2.0f * distance) / lightRadius, 0.0f, 1.0f);
         const float distAttenuation = distanceRatio;
         const V3 lightColor = v3(col.x, col.y, col.z);
+        // fragPos - lightPosition is -lmf exactly (a rounded difference changes sign with its operands),
+        // so its length is `distance`
         float shadowFactor = px.distToCamera < 500.0f
-                                 ? shadow_1sample(p.cubes, entry, misc.y, fragPos, lightPosition,
-                                                  xdot(lmf, normal), 0.1f)
+                                 ? shadow_1sample_dir(p.cubes, entry, misc.y, v3(-lmf.x, -lmf.y, -lmf.z), distance,
+                                                      xdot(lmf, normal), 0.1f)
                                  : 0.0f;
         shadowFactor = gmin(shadowFactor, mixf(minGi, 1.0f, distanceRatio));
         float reweight = 1.0f;
@@ -654,6 +672,7 @@ SGI_D void deferred_pixel(const DeferredParams& p, int x, int y) {
     const uint32_t br = __ldg(p.g.base_reflectivity + i);
     const float reflR = float(br & 0xffu) / 255.0f, reflG = float(br >> 8) / 255.0f;
     const V3 emissive = v3(albedoA, reflG, rmeB);
+    const BurleyPixel bp = burley_pixel(baseColor, v3s(reflR), roughness, metallic, viewDist, sp);
     V3 color = v3s(0.0f);
     for (int l = 0; l < p.num_points; ++l) {
         const float4* rec = reinterpret_cast<const float4*>(p.points + l);
@@ -663,9 +682,8 @@ SGI_D void deferred_pixel(const DeferredParams& p, int x, int y) {
         if (distance < m4.x) {
             // calculatePointLighting2, pbr2.glsl:593-611
             const V3 lightDir = lp - fragPos;
-            color = color + lighting_burley(lc, lightDir, viewDir, normal, baseColor, viewDist, length(lc) / 12.0f,
-                                            roughness, metallic, ambient, 1.0f - 0.0f, v3s(reflR),
-                                            quadratic_atten(lightDir), sp.point_ambient, sp);
+            color = color + lighting_burley_px(bp, lc, lightDir, viewDir, normal, length(lc) / 12.0f, ambient,
+                                               1.0f - 0.0f, quadratic_atten(lightDir), sp.point_ambient, sp);
         }
     }
     // shadowCasters, pbr.fs:116-131
@@ -684,17 +702,16 @@ SGI_D void deferred_pixel(const DeferredParams& p, int x, int y) {
                 shadowFactor = shadow_1sample(p.casters.atlas, entry, m4.y, fragPos, lp, xdot(xsub3(lp, fragPos), normal),
                                               0.03f);
             const V3 lightDir = lp - fragPos;
-            color = color + lighting_burley(lc, lightDir, viewDir, normal, baseColor, viewDist, length(lc) / 12.0f,
-                                            roughness, metallic, ambient, 1.0f - shadowFactor, v3s(reflR),
-                                            quadratic_atten(lightDir), sp.point_ambient, sp);
+            color = color + lighting_burley_px(bp, lc, lightDir, viewDir, normal, length(lc) / 12.0f, ambient,
+                                               1.0f - shadowFactor, quadratic_atten(lightDir), sp.point_ambient, sp);
         }
     }
     const V3 lightDir = v3(p.csm.light_direction[0], p.csm.light_direction[1], p.csm.light_direction[2]);
     const V3 lightColor = v3(p.csm.light_color[0], p.csm.light_color[1], p.csm.light_color[2]);
     const float shadowFactor = infinite_shadow(p.csm, fragPos, normal, true);
     // calculateDirectionalLighting, pbr2.glsl:576-591, called with 1 - shadowFactor
-    color = color + lighting_burley(lightColor, lightDir, viewDir, normal, baseColor, viewDist, 0.0f, roughness,
-                                    metallic, ambient, 1.0f - (1.0f - shadowFactor), v3s(reflR), 1.0f, 0.0f, sp);
+    color = color + lighting_burley_px(bp, lightColor, lightDir, viewDir, normal, 0.0f, ambient,
+                                       1.0f - (1.0f - shadowFactor), 1.0f, 0.0f, sp);
     const V3 o = vmin(color + emissive * p.sc.emission_strength, kHalfMax);
     p.out[i] = pack_h4(o.x, o.y, o.z, 1.0f);
 }

@@ -151,7 +151,15 @@ SGI_D float cube_fetch(const sgi_cube_atlas& at, sgi_atlas_entry e, V3 d) {
     return xdiv(float(__ldg((const unsigned short*)base + off)), 65535.0f);
 }
 
-// calculateShadowValue1Sample, pbr.glsl:116-136 (1 = occluded)
+// calculateShadowValue1Sample, pbr.glsl:116-136 (1 = occluded), given the
+// direction fragPos - lightPos and its length
+SGI_D float shadow_1sample_dir(const sgi_cube_atlas& at, sgi_atlas_entry e, float farPlane, V3 fragDir,
+                               float currentDepth, float lightNormalDot, float minBias) {
+    float bias = xmul(currentDepth, gmax(minBias, xmul(saturate(lightNormalDot), 0.03f)));
+    float depth = cube_fetch(at, e, fragDir);
+    depth = xmul(depth, farPlane);
+    return xsub(currentDepth, bias) > depth ? 1.0f : 0.0f;
+}
 SGI_D float shadow_1sample(const sgi_cube_atlas& at, sgi_atlas_entry e, float farPlane, V3 fragPos, V3 lightPos,
                            float lightNormalDot, float minBias) {
     V3 fragDir = xsub3(fragPos, lightPos);

@@ -176,98 +176,6 @@ cudaError_t flip_weights(const bf16* w, bf16* wt, int cin, int cout, cudaStream_
     return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------- wgrad --
-// dw[co][tap][ci] += sum_{b, p} dz[b, p, co] * x[b, p + off(tap), ci] (FP32, CUDA cores)
-// A block takes one 8 x 16 pixel tile and a 32 (co) x 32 (ci) slab for all 9 taps;
-// thread t owns co = t / 8 and ci = (t % 8) * 4 .. + 3 for the 9 taps (36 sums).
-__global__ void __launch_bounds__(256) wgrad_kernel(WgradArgs a) {
-    __shared__ float sdz[kTileH * kTileW][33];
-    __shared__ float sx[kHaloH * kHaloW][33];
-    const int tid = threadIdx.x;
-    const int tiles_x = (a.W + kTileW - 1) / kTileW, tiles_y = (a.H + kTileH - 1) / kTileH;
-    const int tile = blockIdx.x % (tiles_x * tiles_y), b = blockIdx.x / (tiles_x * tiles_y);
-    const int x0 = (tile % tiles_x) * kTileW, y0 = (tile / tiles_x) * kTileH;
-    const int co0 = blockIdx.y * 32, ci0 = blockIdx.z * 32;
-    const int H = a.H, W = a.W;
-    for (int v = tid; v < kTileH * kTileW * 32; v += 256) {
-        const int p = v / 32, c = v % 32;
-        const int gy = y0 + p / kTileW, gx = x0 + p % kTileW;
-        float val = 0.0f;
-        if (gy < H && gx < W && co0 + c < a.cout)
-            val = __bfloat162float(a.dz.p[a.dz.at(b, (size_t)gy * W + gx, (co0 + c) / 8) + (co0 + c) % 8]);
-        sdz[p][c] = val;
-    }
-    for (int v = tid; v < kHaloH * kHaloW * 32; v += 256) {
-        const int p = v / 32, c = v % 32;
-        const int gy = y0 + p / kHaloW - 1, gx = x0 + p % kHaloW - 1;
-        float val = 0.0f;
-        if (gy >= 0 && gy < H && gx >= 0 && gx < W && ci0 + c < a.cin)
-            val = __bfloat162float(a.x.p[a.x.at(b, (size_t)gy * W + gx, (ci0 + c) / 8) + (ci0 + c) % 8]);
-        sx[p][c] = val;
-    }
-    __syncthreads();
-    const int co = tid >> 3, cib = (tid & 7) * 4;
-    float acc[9][4];
-#pragma unroll
-    for (int t = 0; t < 9; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
-    for (int py = 0; py < kTileH; ++py) {
-        for (int px = 0; px < kTileW; ++px) {
-            const float g = sdz[py * kTileW + px][co];
-#pragma unroll
-            for (int t = 0; t < 9; ++t) {
-                const float* xr = sx[(py + t / 3) * kHaloW + px + t % 3];
-                acc[t][0] = fmaf(g, xr[cib + 0], acc[t][0]);
-                acc[t][1] = fmaf(g, xr[cib + 1], acc[t][1]);
-                acc[t][2] = fmaf(g, xr[cib + 2], acc[t][2]);
-                acc[t][3] = fmaf(g, xr[cib + 3], acc[t][3]);
-            }
-        }
-    }
-    if (co0 + co >= a.cout) return;
-#pragma unroll
-    for (int t = 0; t < 9; ++t)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (ci0 + cib + j < a.cin)
-                atomicAdd(a.dw + ((size_t)(co0 + co) * 9 + t) * a.cin + ci0 + cib + j, acc[t][j]);
-}
-
-cudaError_t wgrad(const WgradArgs& a, cudaStream_t s) {
-    if (!view_ok(a.x) || !view_ok(a.dz)) return cudaErrorInvalidValue;
-    const int tiles = ((a.W + kTileW - 1) / kTileW) * ((a.H + kTileH - 1) / kTileH);
-    dim3 grid(tiles * a.B, (a.cout + 31) / 32, (a.cin + 31) / 32);
-    wgrad_kernel<<<grid, 256, 0, s>>>(a);
-    return cudaGetLastError();
-}
-
-// db[c] += sum over pixels of dz[., c]
-__global__ void bias_grad_kernel(View dz, int c, int B, int HW, float* __restrict__ db) {
-    const int ch = threadIdx.x % 32 + blockIdx.y * 32;
-    const int row = threadIdx.x / 32;
-    float acc = 0.0f;
-    const size_t pixels = (size_t)B * HW;
-    if (ch < c)
-        for (size_t p = (size_t)blockIdx.x * 8 + row; p < pixels; p += (size_t)gridDim.x * 8) {
-            const int b = (int)(p / HW);
-            acc += __bfloat162float(dz.p[dz.at(b, p - (size_t)b * HW, ch / 8) + ch % 8]);
-        }
-    __shared__ float red[8][32];
-    red[row][threadIdx.x % 32] = acc;
-    __syncthreads();
-    if (row == 0 && ch < c) {
-        float s = 0.0f;
-        for (int r = 0; r < 8; ++r) s += red[r][threadIdx.x];
-        atomicAdd(db + ch, s);
-    }
-}
-
-cudaError_t bias_grad(const View& dz, int c, int B, int H, int W, float* db, cudaStream_t s) {
-    if (!view_ok(dz)) return cudaErrorInvalidValue;
-    dim3 grid(256, (c + 31) / 32);
-    bias_grad_kernel<<<grid, 256, 0, s>>>(dz, c, B, H * W, db);
-    return cudaGetLastError();
-}
-
 // ---------------------------------------------------- elementwise / resampling --
 // These kernels move 8 channels (one 16-byte vector) per thread. The thread
 // index runs over (image, pixel, channel group) with the group fastest for NHWC
@@ -611,9 +519,28 @@ __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
         if (threadIdx.x == 0) {
             float t = 0.0f;
             for (int w = 0; w < 8; ++w) t += red[w];
-            atomicAdd(a.loss, t);
+            a.loss_part[blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z)] = t;
         }
     }
+}
+
+// *out = the n values of part summed in a fixed order (one block: strided
+// partial sums per thread, then a tree over the 256 threads)
+__global__ void sum_ordered_kernel(const float* __restrict__ part, size_t n, float* __restrict__ out) {
+    __shared__ float red[256];
+    float s = 0.0f;
+    for (size_t i = threadIdx.x; i < n; i += 256) s += part[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+size_t apply_loss_blocks(int B, int H, int W) {
+    return (size_t)((W + kApplyTX - 1) / kApplyTX) * ((H + kApplyTY - 1) / kApplyTY) * B;
 }
 
 cudaError_t kpcn_apply(const ApplyArgs& a, cudaStream_t s) {
@@ -622,8 +549,11 @@ cudaError_t kpcn_apply(const ApplyArgs& a, cudaStream_t s) {
     if ((!a.noisy && !a.noisy_h) || !a.prev || (a.target && a.noisy_h)) return cudaErrorInvalidValue;
     dim3 grid((a.W + kApplyTX - 1) / kApplyTX, (a.H + kApplyTY - 1) / kApplyTY, a.B);
     if (a.target) {
-        if (!a.loss || !a.target) return cudaErrorInvalidValue;
-        return launch_pdl(kpcn_apply_kernel<true>, grid, dim3(256), 0, s, a);
+        if (!a.loss || !a.loss_part || !a.target) return cudaErrorInvalidValue;
+        cudaError_t e = launch_pdl(kpcn_apply_kernel<true>, grid, dim3(256), 0, s, a);
+        if (e != cudaSuccess) return e;
+        sum_ordered_kernel<<<1, 256, 0, s>>>(a.loss_part, apply_loss_blocks(a.B, a.H, a.W), a.loss);
+        return cudaGetLastError();
     }
     const bool composite = a.hdr && a.screen && a.albedo && a.gi_out && a.hist_out && a.B == 1;
     if (!a.out && !composite) return cudaErrorInvalidValue;

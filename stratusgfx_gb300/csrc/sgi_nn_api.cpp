@@ -13,6 +13,7 @@
 // the head. Backward runs the same schedule in reverse: ReLU masks, weight
 // gradients (FP32), bias gradients, and input gradients through the forward
 // kernel with flipped weights.
+#include <algorithm>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -95,6 +96,10 @@ cudaError_t Net::init(const sgi_nn_config& c) {
     chk(alloc(&GQ2, P4 * 128));
     chk(alloc(&GQ3, P4 * 64));
     chk(alloc(&fwd_out, P));
+    for (int l = 0; l < NUM_LAYERS; ++l)
+        wgrad_part_n = std::max(wgrad_part_n, wgrad_part_floats(kCin[l], kCout[l]));
+    chk(alloc(&wgrad_part, wgrad_part_n));
+    chk(alloc(&loss_part, apply_loss_blocks(c.max_batch, c.max_height, c.max_width)));
     chk(alloc(&dev_err, 1));
     size_t sc = 0, in = 0;
     for (int l = 0; l < NUM_LAYERS; ++l) {
@@ -323,9 +328,9 @@ cudaError_t Net::layer_backward(int l, const View& x, const View& y, const View&
         g = dz;
         launches += 1;
     }
-    WgradArgs wa{x, g, g32 + w_off[l], kCin[l], kCout[l], B, H, W};
-    NN_TRY(wgrad(wa, s));
-    NN_TRY(bias_grad(g, kCout[l], B, H, W, g32 + b_off[l], s));
+    WgradArgs wa{x, g, g32 + w_off[l], kCin[l], kCout[l], B, H, W, wgrad_part, wgrad_part_n, dev_err, wait_ns,
+                 skip_producer};
+    NN_TRY(wgrad(wa, s));   // weights and bias (b_off[l] follows the layer's weights)
     launches += 2;
     if (dx.p) {
         NN_TRY(flip_weights(wbf + w_off[l], wflip + w_off[l], kCin[l], kCout[l], s));
@@ -474,7 +479,7 @@ sgi_status nn_apply_composite(sgi_nn* n, const uint2* noisy, const float* prev, 
     if (!shape_ok(n, 1, H, W)) return nn_fail(n, SGI_ERR_CAP, "batch/size exceed the network's capacity or H, W % 4");
     const sgi::nn::View none{nullptr, 8, 8, 8};
     sgi::nn::ApplyArgs a{sgi::nn::planar_view(n->net.LOG, 4, H, W), nullptr, (const float4*)prev, nullptr,
-                         nullptr, none, nullptr, 0.0f, 1, H, W};
+                         nullptr, none, nullptr, nullptr, 0.0f, 1, H, W};
     a.noisy_h = noisy;
     a.screen = screen; a.albedo = albedo; a.hdr = hdr; a.gi_out = gi_out; a.hist_out = hist_out;
     const cudaError_t e = sgi::nn::kpcn_apply(a, s);
@@ -494,7 +499,7 @@ sgi_status sgi_nn_forward(sgi_nn* n, const void* features, const float* noisy, c
     if (e != cudaSuccess) return nn_cuda(n, e, "forward");
     const sgi::nn::View none{nullptr, 8, 8, 8};
     sgi::nn::ApplyArgs a{sgi::nn::planar_view(n->net.LOG, 4, H, W), (const float4*)noisy, (const float4*)prev, nullptr,
-                         (float4*)out, none, nullptr, 0.0f, B, H, W};
+                         (float4*)out, none, nullptr, nullptr, 0.0f, B, H, W};
     e = sgi::nn::kpcn_apply(a, s);
     n->net.launches += 1;
     return e == cudaSuccess ? SGI_OK : nn_cuda(n, e, "apply");
@@ -509,12 +514,10 @@ sgi_status sgi_nn_train_step(sgi_nn* n, const void* features, const float* noisy
     Net& net = n->net;
     cudaError_t e = net.forward((const __nv_bfloat16*)features, B, H, W, s, false);
     if (e != cudaSuccess) return nn_cuda(n, e, "forward");
-    e = cudaMemsetAsync(net.loss_dev, 0, sizeof(float), s);
-    if (e != cudaSuccess) return nn_cuda(n, e, "loss reset");
     const size_t P = (size_t)B * H * W;
     sgi::nn::ApplyArgs a{sgi::nn::planar_view(net.LOG, 4, H, W), (const float4*)noisy, (const float4*)prev,
                          (const float4*)target, nullptr, sgi::nn::nhwc_view(net.GA, 32, H, W), net.loss_dev,
-                         1.0f / (3.0f * (float)P), B, H, W};
+                         net.loss_part, 1.0f / (3.0f * (float)P), B, H, W};
     e = sgi::nn::kpcn_apply(a, s);
     if (e != cudaSuccess) return nn_cuda(n, e, "apply/loss");
     e = net.backward((const __nv_bfloat16*)features, B, H, W, s);

@@ -64,10 +64,17 @@ struct ConvArgs {
 struct WgradArgs {
     View x;
     View dz;
-    float* dw;                // [cout][9][cin], accumulated
+    float* dw;                // [cout][9][cin] followed by the bias [cout], accumulated
     int cin, cout;
     int B, H, W;
+    float* part;              // split-K partial sums, part_floats floats
+    size_t part_floats;
+    int* err;                 // set when a bounded wait ran out
+    unsigned long long wait_ns;
+    int skip_producer;        // test switch: the producers stage nothing
 };
+// floats of the partial-sum buffer wgrad needs for cin x cout
+size_t wgrad_part_floats(int cin, int cout);
 
 struct ApplyArgs {
     View logits;                  // 32 channels
@@ -77,6 +84,7 @@ struct ApplyArgs {
     float4* out;                  // [P] or null
     View dlogits;                 // 32 channels, when target
     float* loss;                  // sum of |log1p(out) - log1p(target)| (device scalar) or null
+    float* loss_part;             // per-block sums of the loss, summed into *loss in block order
     float grad_scale;             // 1 / (3 * pixels)
     int B, H, W;
     // inference only: with hdr set, the composite of the GI frame is written
@@ -119,7 +127,8 @@ cudaError_t conv3x3_tc_fp8(int cin, int cout, int mode, bool in8, bool out8, con
                            cudaStream_t s);
 cudaError_t flip_weights(const __nv_bfloat16* w, __nv_bfloat16* wt, int cin, int cout, cudaStream_t s);
 cudaError_t wgrad(const WgradArgs& a, cudaStream_t s);
-cudaError_t bias_grad(const View& dz, int c, int B, int H, int W, float* db, cudaStream_t s);
+// floats of kpcn_apply's loss_part for B x H x W
+size_t apply_loss_blocks(int B, int H, int W);
 // dz = dy * (y > 0)
 cudaError_t relu_bwd(const View& dy, const View& y, const View& dz, int c, int B, int H, int W, cudaStream_t s);
 // 2x2 mean pooling of an H x W input

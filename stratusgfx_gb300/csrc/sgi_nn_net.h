@@ -32,7 +32,10 @@ struct Net {
     __nv_bfloat16 *GA = nullptr, *GB = nullptr, *GC = nullptr, *GD = nullptr, *GH1 = nullptr, *GH2 = nullptr,
                   *GH3 = nullptr, *GQ1 = nullptr, *GQ2 = nullptr, *GQ3 = nullptr;
     float4* fwd_out = nullptr;
-    int* dev_err = nullptr;   // set by a tcgen05 convolution whose wait ran out
+    float* wgrad_part = nullptr;   // split-K partial sums of the weight and bias gradients
+    size_t wgrad_part_n = 0;
+    float* loss_part = nullptr;    // per-block loss sums of kpcn_apply
+    int* dev_err = nullptr;   // set by a tcgen05 kernel whose wait ran out
     unsigned long long wait_ns = 0;   // limit of the tcgen05 waits (0: the kernels' default)
     int skip_producer = 0;            // test switch: the convolutions' TMA producers issue nothing
     int conv_path = SGI_NN_CONV_TCGEN05;

@@ -1176,5 +1176,309 @@ cudaError_t conv3x3_tc_fp8(int cin, int cout, int mode, bool in8, bool out8, con
     return cudaErrorInvalidValue;
 }
 
+// ------------------------------------------------------- weight gradients
+//
+// dw[co][t][ci] = sum over pixels p of dz[p][co] * x[p + off(t)][ci], a GEMM
+// with the pixels as its reduction dimension. One tcgen05.mma accumulator per
+// tap: D_t[m][n] (M = 128 rows for the output channels, zero past COUT; N = CC
+// input channels of the CTA's group) += A[m][k] * B_t[n][k] over 16-pixel K
+// steps, both operands K-major with the 64-byte swizzle (a row is 32 pixels of
+// one channel, 64 bytes). The operands are transposes of the NHWC tensors, so
+// the producers build them: a stage is 32 pixels of one image row (pixels past
+// the row end are zero); each producer thread loads 8 pixels x 8 channels
+// (eight 16-byte loads, zero outside the image for the shifted taps),
+// transposes them in registers and stores 8 channel rows of 16 bytes at the
+// swizzled chunk (the tensor core reads the swizzle from absolute addresses;
+// each operand block starts on a 512-byte boundary). Roles (288 threads):
+// warps 0..7 produce the stages (4-stage ring) and afterwards read the
+// accumulators; warp 8 issues the MMAs and commits each stage back.
+//
+// A CTA owns one group of CC input channels and one contiguous slice of the
+// image-row segments; it writes its sums to part[slice][co][t][ci], and a
+// second kernel adds the slices in a fixed order to dw. The bias gradient
+// (the per-channel sums of dz) comes from the producers of the A operand, which
+// load every dz value of the slice anyway: part[slice][COUT * 9 * CIN + co],
+// added by the same kernel into the bias that follows the weights. No atomics:
+// the gradients are the same on every run.
+constexpr int kWgSeg = 32;          // pixels per stage (one 64-byte K-major row)
+constexpr int kWgStages = 4;
+constexpr int kWgThreads = 288;
+constexpr int kWgMaxSlices = 152;
+
+template <int CC> struct WgShape {
+    static constexpr int A_BYTES = 128 * 64;
+    static constexpr int B_BYTES = 9 * CC * 64;
+    static constexpr int STAGE = round_up(A_BYTES + B_BYTES, 1024);
+    static constexpr int TMEM_COLS = pow2_cols(9 * CC);
+    // CTAs that together would ask for more than the 512 TMEM columns of an SM do not share one
+    static constexpr int SMEM_NEED = kWgStages * STAGE + 1024 /* alignment */ + 256 /* barriers */;
+    static constexpr int SMEM = TMEM_COLS > 256 && SMEM_NEED < 120 * 1024 ? 120 * 1024 : SMEM_NEED;
+};
+
+__device__ __forceinline__ uint32_t perm(uint32_t a, uint32_t b, uint32_t sel) { return __byte_perm(a, b, sel); }
+
+// r[i] = 8 channels of pixel i (16 bytes) -> o[c] = channel c of the 8 pixels
+__device__ __forceinline__ void transpose8x8(const uint4* r, uint4* o) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t w0 = (&r[0].x)[j], w1 = (&r[1].x)[j], w2 = (&r[2].x)[j], w3 = (&r[3].x)[j];
+        const uint32_t w4 = (&r[4].x)[j], w5 = (&r[5].x)[j], w6 = (&r[6].x)[j], w7 = (&r[7].x)[j];
+        o[2 * j] = make_uint4(perm(w0, w1, 0x5410), perm(w2, w3, 0x5410), perm(w4, w5, 0x5410), perm(w6, w7, 0x5410));
+        o[2 * j + 1] =
+            make_uint4(perm(w0, w1, 0x7632), perm(w2, w3, 0x7632), perm(w4, w5, 0x7632), perm(w6, w7, 0x7632));
+    }
+}
+
+// row `row` (64 bytes, 32 pixels) of a K-major 64-byte-swizzled operand block, 16-byte chunk `chunk`
+__device__ __forceinline__ uint4* sw64(unsigned char* block, int row, int chunk) {
+    return reinterpret_cast<uint4*>(block + row * 64 + ((chunk ^ ((row >> 1) & 3)) << 4));
+}
+
+template <int CC>
+__global__ void __launch_bounds__(kWgThreads, 1) wgrad_tc_kernel(WgradArgs a, int slices, int segs_per_row) {
+    using S = WgShape<CC>;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    unsigned char* ctrl = smem + (size_t)kWgStages * S::STAGE;
+    uint64_t* full = reinterpret_cast<uint64_t*>(ctrl);     // [stages], one arrival per producer warp
+    uint64_t* empty = full + kWgStages;                      // [stages], tcgen05.commit
+    uint64_t* done = empty + kWgStages;                      // accumulators complete
+    uint64_t* drain = done + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int group = blockIdx.x % (a.cin / CC), slice = blockIdx.x / (a.cin / CC);
+    const int ci0 = group * CC;
+    const long long nseg = (long long)a.B * a.H * segs_per_row;
+    const long long seg0 = nseg * slice / slices, seg1 = nseg * (slice + 1) / slices;
+    const int nst = (int)(seg1 - seg0);
+    const unsigned long long wait_ns = a.wait_ns ? a.wait_ns : kWaitNs;
+
+    if (warp == 8) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s_addr(tmem_slot)),
+                     "r"(S::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kWgStages; ++s) {
+            mbar_init(s_addr(full + s), 8);
+            mbar_init(s_addr(empty + s), 1);
+        }
+        mbar_init(s_addr(done), 1);
+        mbar_init(s_addr(drain), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    // rows COUT..127 of every stage's A block stay zero
+    for (int s = 0; s < kWgStages; ++s)
+        for (int i = a.cout * 4 + tid; i < 128 * 4; i += kWgThreads)
+            reinterpret_cast<uint4*>(smem + (size_t)s * S::STAGE)[i] = make_uint4(0u, 0u, 0u, 0u);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t smem_base = s_addr(smem);
+
+    if (warp < 8) {
+        // ------------------------------------------------ producers
+        // item it < 9 * CC / 2: B block of tap it / (CC / 2), channels ((it / 4) % (CC / 8)) * 8, pixels (it % 4) * 8;
+        // then A: output channels ((it - nb) / 4) * 8, pixels (it % 4) * 8
+        constexpr int NB = 9 * (CC / 8) * 4;
+        const int na = a.cout / 2;
+        const int it = tid;
+        int s = 0;
+        uint32_t ph = 0;
+        bool ok = true;
+        float bsum[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};   // A items: this thread's pixels of dz
+        for (int st = 0; st < nst && !a.skip_producer; ++st) {
+            int free_ = 0;
+            if (lane == 0) free_ = mbar_wait(s_addr(empty + s), ph ^ 1u, abort_flag, wait_ns) ? 1 : 0;
+            free_ = __shfl_sync(0xffffffffu, free_, 0);
+            if (!free_) { ok = false; break; }
+            const long long sg = seg0 + st;
+            const int xs = (int)(sg % segs_per_row) * kWgSeg;
+            const long long rowi = sg / segs_per_row;
+            const int y = (int)(rowi % a.H), b = (int)(rowi / a.H);
+            unsigned char* stage = smem + (size_t)s * S::STAGE;
+            if (it < NB + na) {
+                uint4 r[8], o[8];
+                const int p8 = it & 3;
+                if (it < NB) {
+                    const int tap = it / (4 * (CC / 8)), c8 = (it / 4) % (CC / 8);
+                    const int yy = y + tap / 3 - 1, dx = tap % 3 - 1;
+                    const bool row_ok = yy >= 0 && yy < a.H;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int x = xs + p8 * 8 + i, xx = x + dx;
+                        r[i] = make_uint4(0u, 0u, 0u, 0u);
+                        if (row_ok && x < a.W && xx >= 0 && xx < a.W)
+                            r[i] = __ldg(reinterpret_cast<const uint4*>(
+                                a.x.p + a.x.at(b, (size_t)yy * a.W + xx, 0) + ci0 + c8 * 8));
+                    }
+                    transpose8x8(r, o);
+                    unsigned char* blk = stage + S::A_BYTES + tap * CC * 64;
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) *sw64(blk, c8 * 8 + c, p8) = o[c];
+                } else {
+                    const int o8 = (it - NB) / 4;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int x = xs + p8 * 8 + i;
+                        r[i] = make_uint4(0u, 0u, 0u, 0u);
+                        if (x < a.W)
+                            r[i] = __ldg(reinterpret_cast<const uint4*>(
+                                a.dz.p + a.dz.at(b, (size_t)y * a.W + x, 0) + o8 * 8));
+                    }
+                    transpose8x8(r, o);
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) *sw64(stage, o8 * 8 + c, p8) = o[c];
+                    // the bias gradient: the same dz values summed per channel, pixel by pixel
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        float f[8];
+                        bf8_unpack(r[i], f);
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) bsum[c] += f[c];
+                    }
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(s_addr(full + s)) : "memory");
+            if (++s == kWgStages) { s = 0; ph ^= 1u; }
+        }
+        if (!ok && lane == 0) give_up(abort_flag, a.err);
+        // bias partial sums of the slice: the four threads of an output-channel octet (lanes 4j .. 4j + 3,
+        // pixels p8 = 0..3 of every stage) combine theirs in a fixed order; the group-0 CTA writes them
+        // after the slice's weight sums
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            bsum[c] += __shfl_xor_sync(0xffffffffu, bsum[c], 1);
+            bsum[c] += __shfl_xor_sync(0xffffffffu, bsum[c], 2);
+        }
+        if (group == 0 && it >= NB && it < NB + na && (it & 3) == 0) {
+            float* pb = a.part + ((size_t)slice * (a.cout * 9 * a.cin + a.cout)) + (size_t)a.cout * 9 * a.cin +
+                        (it - NB) / 4 * 8;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) pb[c] = bsum[c];
+        }
+        // ------------------------------------------------ accumulators -> partial sums
+        int ready = 0;
+        if (lane == 0) ready = mbar_wait(s_addr(done), 0, abort_flag, wait_ns) ? 1 : 0;
+        ready = __shfl_sync(0xffffffffu, ready, 0);
+        if (ready) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int q = warp & 3, co = q * 32 + lane;
+            constexpr int NCOL = (9 * CC + 31) / 32;   // 32-column chunks (CC = 16: the last one half used)
+            float* prow = a.part + (size_t)slice * (a.cout * 9 * a.cin + a.cout) + (size_t)(co < a.cout ? co : 0) * 9 * a.cin;
+            for (int cchunk = warp >> 2; cchunk < NCOL; cchunk += 2) {
+                uint32_t v[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cchunk * 32), v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (co < a.cout) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int col = cchunk * 32 + j;
+                        if (col < 9 * CC) prow[(size_t)(col / CC) * a.cin + ci0 + col % CC] = __uint_as_float(v[j]);
+                    }
+                }
+            }
+        } else if (lane == 0) {
+            give_up(abort_flag, a.err);
+        }
+    } else if (lane == 0) {
+        // ------------------------------------------------ MMA issuer
+        constexpr uint32_t IDESC = instr_desc(128, CC, false);
+        constexpr uint32_t HI = (uint32_t)((8 * 64) >> 4) | (1u << 14) | (4u << 29);   // SBO 512 B, 64B swizzle
+        int s = 0;
+        uint32_t ph = 0;
+        bool ok = true, issued = false;
+        for (int st = 0; st < nst; ++st) {
+            if (!mbar_wait(s_addr(full + s), ph, abort_flag, wait_ns)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t base = smem_base + s * S::STAGE;
+            const uint32_t a_lo = ((base >> 4) & 0x3FFFu) | (1u << 16);
+            const uint32_t b_lo = (((base + S::A_BYTES) >> 4) & 0x3FFFu) | (1u << 16);
+#pragma unroll
+            for (int tap = 0; tap < 9; ++tap) {
+#pragma unroll
+                for (int ks = 0; ks < 2; ++ks) {
+                    const uint32_t av = a_lo + (uint32_t)((ks * 32) >> 4);
+                    const uint32_t bv = b_lo + (uint32_t)((tap * CC * 64 + ks * 32) >> 4);
+                    umma<false>(tmem + (uint32_t)(tap * CC), av, bv, HI, IDESC, (st > 0 || ks > 0) ? 1u : 0u);
+                }
+            }
+            issued = true;
+            mma_commit(s_addr(empty + s));
+            if (++s == kWgStages) { s = 0; ph ^= 1u; }
+        }
+        if (ok) mma_commit(s_addr(done));   // every slice has at least one stage
+        if (!ok) {
+            give_up(abort_flag, a.err);
+            if (issued) {
+                mma_commit(s_addr(drain));
+                const unsigned long long deadline = global_ns() + wait_ns;
+                while (!mbar_test(s_addr(drain), 0) && global_ns() < deadline) {
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 8)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::TMEM_COLS)
+                     : "memory");
+}
+
+// dw[e] += sum over slices j = 0 .. slices-1 of part[j][e], in that order
+__global__ void wgrad_reduce_kernel(const float* __restrict__ part, int slices, size_t n, float* __restrict__ dw) {
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        float acc = 0.0f;
+#pragma unroll 8
+        for (int j = 0; j < slices; ++j) acc += __ldg(part + (size_t)j * n + e);
+        dw[e] += acc;
+    }
+}
+
+static int wgrad_slices(int cin, int cout) {
+    const int groups = cin / (cin % 32 == 0 ? 32 : 16);
+    const int sl = kWgMaxSlices / groups;
+    (void)cout;
+    return sl < 1 ? 1 : sl;
+}
+
+size_t wgrad_part_floats(int cin, int cout) { return (size_t)wgrad_slices(cin, cout) * (cout * 9 * cin + cout); }
+
+template <int CC>
+static cudaError_t run_wgrad(const WgradArgs& a, cudaStream_t s) {
+    using S = WgShape<CC>;
+    const int segs_per_row = (a.W + kWgSeg - 1) / kWgSeg;
+    const long long nseg = (long long)a.B * a.H * segs_per_row;
+    int slices = wgrad_slices(a.cin, a.cout);
+    if (slices > nseg) slices = (int)nseg;
+    const size_t n = (size_t)a.cout * 9 * a.cin + a.cout;   // weights, then the bias
+    if ((size_t)slices * n > a.part_floats) return cudaErrorInvalidValue;
+    auto kern = wgrad_tc_kernel<CC>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM);
+    if (e != cudaSuccess) return e;
+    kern<<<(a.cin / CC) * slices, kWgThreads, S::SMEM, s>>>(a, slices, segs_per_row);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    wgrad_reduce_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(a.part, slices, n, a.dw);
+    return cudaGetLastError();
+}
+
+cudaError_t wgrad(const WgradArgs& a, cudaStream_t s) {
+    // 16-byte loads of 8 channels: NHWC views (channels contiguous), 16-channel groups
+    if (!view_ok(a.x) || !view_ok(a.dz) || a.x.grp != 8 || a.dz.grp != 8 || !a.part || !a.err || a.cin % 16 ||
+        a.cout % 8 || a.cout > 128 || a.B < 1 || a.H < 1 || a.W < 1)
+        return cudaErrorInvalidValue;
+    return a.cin % 32 == 0 ? run_wgrad<32>(a, s) : run_wgrad<16>(a, s);
+}
+
 }  // namespace nn
 }  // namespace sgi

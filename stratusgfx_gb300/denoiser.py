@@ -93,7 +93,8 @@ class KpcnDenoiser:
         self._chk(self.lib.sgi_nn_calibrate_fp8(self.h, _p(feat), B, H, W, stage._stream_ptr(stream)))
 
     def set_wait_test(self, wait_ns: int = 0, skip_producer: bool = False):
-        """Limit of the tensor-core convolutions' waits (0: default) and the producer test switch."""
+        """Limit of the tensor-core kernels' waits (convolutions, weight gradients; 0: default) and the producer
+        test switch."""
         self._chk(self.lib.sgi_nn_set_wait_test(self.h, int(wait_ns), 1 if skip_producer else 0))
 
     def device_status(self):

@@ -515,7 +515,7 @@ def converged_targets(ds, sc, w, cfg, batches=64):
 def psnr_vs_converged(render, ds, sc, w, cfg, targets):
     """Renders frames 1..8 in order with render(st, k, out) on a fresh context and returns the mean
     PSNR (dB) of the HDR frame against the converged frame screen + gi * target, and of the GI term
-    alone; FP64 reductions on the GPU."""
+    alone (sgi_gi_error_stats: FP64 reductions on the device)."""
     import torch
 
     from stratusgfx_gb300 import stage
@@ -529,16 +529,9 @@ def psnr_vs_converged(render, ds, sc, w, cfg, targets):
         st.set_shadow_maps(ds.csms[k], ds.cubes)
         render(st, k, out)
         st.direct_lighting(ds.gbuffers[k], ds.camera(k), direct)
-        torch.cuda.synchronize()
-        alb = ds.gbuffers[k].albedo[..., :3].double() / 255.0
-        gi = (torch.clamp(alb, min=0.01) + 1e-5).half().double()
-        ref_gi = gi * targets[k - 1][..., :3].double()
-        ref = direct[..., :3].double() + ref_gi
-        got = out[..., :3].double()
-        for lst, a, r in ((full, got, ref), (gi_only, got - direct[..., :3].double(), ref_gi)):
-            mse = torch.mean((a - r) ** 2)
-            peak = torch.max(torch.abs(r))
-            lst.append(float(10.0 * torch.log10(peak * peak / mse)))
+        es = stage.gi_error_stats(ds.gbuffers[k], out, direct, targets[k - 1])   # FP64 on the device
+        full.append(es["psnr_frame"])
+        gi_only.append(es["psnr_gi"])
     st.close()
     return round(sum(full) / len(full), 2), round(sum(gi_only) / len(gi_only), 2)
 
@@ -842,12 +835,7 @@ def batched_views(args, flush):
             w = o["w"]
             direct = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
             o["st"].direct_lighting(o["vs"].gbuffers[1], o["cam"], direct)
-            torch.cuda.synchronize()
-            alb = o["vs"].gbuffers[1].albedo[..., :3].double() / 255.0
-            ref = (torch.clamp(alb, min=0.01) + 1e-5).half().double() * o["tgt"][..., :3].double()
-            got = o["out"][..., :3].double() - direct[..., :3].double()
-            mse = torch.mean((got - ref) ** 2)
-            psnr.append(float(10.0 * torch.log10(torch.max(torch.abs(ref)) ** 2 / mse)))
+            psnr.append(stage.gi_error_stats(o["vs"].gbuffers[1], o["out"], direct, o["tgt"])["psnr_gi"])
         # the same frames issued view by view
         ms_seq = 0.0
         for s in range(steps + 2):

@@ -306,6 +306,25 @@ sgi_status sgi_render_frame(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_gbuf
 sgi_status sgi_gi_target(sgi_ctx* ctx, const sgi_gbuffer* gbuf, const sgi_camera* cam, float time,
                          int32_t batches, float* target, void* stream);
 
+/* FP64 error statistics of a rendered frame against the converged target
+ * (no counterpart in the reference; the reductions behind the reported PSNRs).
+ * With w = binary16(max(albedo / 255, 0.01) + 1e-5) per colour channel (the GI
+ * weight the final denoise pass composites with), the converged GI term is
+ * r_gi = w * target and the converged frame r = direct + r_gi; the statistics
+ * cover the errors hdr - r (frame) and (hdr - direct) - r_gi (GI term) over the
+ * three colour channels of every pixel, computed and reduced in binary64 on the
+ * device in a fixed order. hdr, direct: RGBA16F (8 bytes a pixel), target: the
+ * float4 output of sgi_gi_target; all device memory. Synchronises `stream`.
+ * PSNR = 10 log10(peak^2 / (sse / values)). */
+typedef struct sgi_error_stats {
+    double sse_frame, sse_gi;         /* sums of squared errors */
+    double peak_frame, peak_gi;       /* max |r|, max |r_gi| */
+    double max_abs_frame, max_abs_gi; /* largest absolute errors */
+    int64_t values;                   /* 3 * width * height */
+} sgi_error_stats;
+sgi_status sgi_gi_error_stats(const sgi_gbuffer* gbuf, const void* hdr, const void* direct, const float* target,
+                              int32_t width, int32_t height, sgi_error_stats* out, void* stream);
+
 /* Clears the denoiser history (vplGIDenoisedPrevFrameFbo). */
 sgi_status sgi_reset_history(sgi_ctx* ctx, void* stream);
 

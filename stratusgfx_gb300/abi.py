@@ -132,6 +132,12 @@ class FrameParams(C.Structure):
     _fields_ = [("time", C.c_float), ("frames_per_second", C.c_float)]
 
 
+class ErrorStats(C.Structure):    # sgi_error_stats
+    _fields_ = [("sse_frame", C.c_double), ("sse_gi", C.c_double), ("peak_frame", C.c_double),
+                ("peak_gi", C.c_double), ("max_abs_frame", C.c_double), ("max_abs_gi", C.c_double),
+                ("values", C.c_int64)]
+
+
 class Box(C.Structure):           # sgi_box, 64 B
     _fields_ = [("min", C.c_float * 4), ("max", C.c_float * 4), ("albedo", C.c_float * 4), ("roughness", C.c_float),
                 ("metallic", C.c_float), ("reflectance", C.c_float), ("id", C.c_float)]
@@ -177,6 +183,8 @@ EXPORTS = {
     "sgi_render_frame": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(GBuffer), C.POINTER(Camera),
                                      C.POINTER(FrameParams), C.c_void_p, C.c_void_p]),
     "sgi_reset_history": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "sgi_gi_error_stats": (C.c_int32, [C.POINTER(GBuffer), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                       C.POINTER(ErrorStats), C.c_void_p]),
     "sgi_gi_target": (C.c_int32, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(Camera), C.c_float, C.c_int32,
                                   C.c_void_p, C.c_void_p]),
     "sgi_read_debug": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),

@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-Xcompiler", "-fPIC", "-I" + os.path.join(REPO, "include")]
 CUDA_SOURCES = ["sgi_kernels.cu", "sgi_shade.cu", "sgi_shade_fast.cu", "sgi_scene.cu", "sgi_nn.cu", "sgi_nn_tc.cu",
-                "sgi_selftest.cu"]
+                "sgi_selftest.cu", "sgi_stats.cu"]
 HOST_SOURCES = ["sgi_api.cpp", "sgi_nn_api.cpp", "sgi_batch.cpp", "sgi_slots.cpp", "sgi_host.cpp"]
 # The learned denoiser is checked against the oracle within a tolerance, not bit
 # for bit, so its kernels keep the compiler's default multiply-add contraction.

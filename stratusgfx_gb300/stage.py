@@ -52,6 +52,26 @@ def workload_config(w: Workload, **kw) -> abi.Config:
     return default_config(w.width, w.height, **args)
 
 
+def gi_error_stats(g: "GBufferTensors", hdr: torch.Tensor, direct: torch.Tensor, target: torch.Tensor,
+                   stream=None) -> dict:
+    """sgi_gi_error_stats: FP64 error statistics (on the device) of the RGBA16F frame `hdr` against the
+    converged frame direct + w * target, w = binary16(max(albedo, 0.01) + 1e-5); returns the PSNRs of the
+    frame and of its GI term and the raw statistics."""
+    import math
+    H, W = hdr.shape[0], hdr.shape[1]
+    st = abi.ErrorStats()
+    lib = abi.load()
+    gs = g.struct()
+    abi.check(lib.sgi_gi_error_stats(C.byref(gs), hdr.data_ptr(), direct.data_ptr(), target.data_ptr(), W, H,
+                                     C.byref(st), _stream_ptr(stream)))
+
+    def psnr(peak, sse):
+        return math.inf if sse == 0 else 10.0 * math.log10(peak * peak / (sse / st.values))
+    return {"psnr_frame": psnr(st.peak_frame, st.sse_frame), "psnr_gi": psnr(st.peak_gi, st.sse_gi),
+            "sse_frame": st.sse_frame, "sse_gi": st.sse_gi, "peak_frame": st.peak_frame, "peak_gi": st.peak_gi,
+            "max_abs_frame": st.max_abs_frame, "max_abs_gi": st.max_abs_gi, "values": st.values}
+
+
 class GBufferTensors:
     """One frame's G-buffer in the reference formats (row 0 = bottom)."""
 

@@ -77,6 +77,12 @@ sgi_status sgi_nn_features(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_camer
 enum { SGI_NN_CONV_WARP_MMA = 0, SGI_NN_CONV_TCGEN05 = 1 };
 sgi_status sgi_nn_set_conv_path(sgi_nn* net, int32_t path);
 
+/* The neural frame (sgi_render_frame_neural) on the tcgen05 path applies the
+ * predicted kernels and writes the composite in the head convolution's
+ * epilogue (default, enabled != 0), or writes the logits and runs the separate
+ * kernel-apply pass (0); both give the same frame. */
+sgi_status sgi_nn_set_head_fusion(sgi_nn* net, int32_t enabled);
+
 /* Inference precision of the convolutions: BF16 (default) or FP8 E4M3 with
  * per-channel scales and FP32 accumulation (tcgen05 path only). FP8 needs a
  * calibration after the last change of the weights (set_params, training). */

@@ -232,6 +232,7 @@ EXPORTS = {
     "sgi_cull_vpls_noalloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(Csm), C.c_int32, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p]),
     "sgi_nn_set_conv_path": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "sgi_nn_set_head_fusion": (C.c_int32, [C.c_void_p, C.c_int32]),
     "sgi_nn_set_precision": (C.c_int32, [C.c_void_p, C.c_int32]),
     "sgi_nn_calibrate_fp8": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "sgi_nn_device_status": (C.c_int32, [C.c_void_p]),

@@ -803,15 +803,15 @@ sgi_status sgi_render_frame_neural(sgi_ctx* ctx, sgi_nn* net, const sgi_gbuffer*
     record(ctx, 4, s);
     st = run_features(ctx, cur, cam, ctx->nn_feat, nullptr, ctx->nn_prev, s);
     if (st != SGI_OK) return st;
-    st = nn_forward_net(net, ctx->nn_feat, H, W, s);
+    // the network's head applies the predicted kernels and writes the composite (HDR frame, GI history)
+    // directly; it reads the direct lighting, so it waits for the side stream first
+    st = nn_forward_composite(net, ctx->nn_feat, H, W, ctx->last_merged, (const float*)ctx->nn_prev, ctx->direct,
+                              cur->albedo, (uint2*)hdr_out, ctx->gi_hist[1 - ctx->hist_cur],
+                              ctx->hist_depth[1 - ctx->hist_cur], overlap ? ctx->join : nullptr, s);
     if (st != SGI_OK) return fail(ctx, st, std::string("denoiser: ") + sgi_nn_last_error(net));
-    if (overlap) SGI_CUDA(ctx, cudaStreamWaitEvent(s, ctx->join, 0), "join direct lighting");
-    // the kernel apply writes the composite (HDR frame, GI history) directly
-    st = nn_apply_composite(net, ctx->last_merged, (const float*)ctx->nn_prev, H, W, ctx->direct,
-                            cur->albedo, (uint2*)hdr_out, ctx->gi_hist[1 - ctx->hist_cur],
-                            ctx->hist_depth[1 - ctx->hist_cur], s);
-    if (st != SGI_OK) return fail(ctx, st, std::string("denoiser: ") + sgi_nn_last_error(net));
-    ctx->launches += 16;
+    // the network: 11 convolutions (the head with the kernel apply) and 2 upsamplings on the tcgen05 path;
+    // off it also 2 pooling launches and the separate kernel apply (the features kernel counts itself)
+    ctx->launches += net->net.conv_path != SGI_NN_CONV_TCGEN05 ? 16 : net->net.head_fusion ? 13 : 14;
     ctx->hist_cur = 1 - ctx->hist_cur;
     ctx->have_history = true;
     record(ctx, 5, s);

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "sgi_nn_apply.cuh"
 #include "sgi_nn_internal.h"
 
 namespace sgi {
@@ -394,31 +395,6 @@ cudaError_t up_bwd(const View& dout, const View& din, int B, int Hi, int Wi, int
 // [B, H, W, 4] float (rgb used). out = a * sum_k softmax(l)_k noisy(p + o_k) + (1 - a) * prev,
 // a = sigmoid(l25); neighbours clamped to the image. With a target, also the
 // loss sum of |log1p(out) - log1p(target)| and dlogits = d(mean loss)/dlogits.
-// The composite of one pixel's denoised GI (d0, d1, d2): the direct lighting
-// plus the GI times the gather's colour output (albedo + 1e-5 stored as FP16),
-// the GI history and a history length of 1.
-__device__ __forceinline__ void composite_px(float d0, float d1, float d2, const uint2* __restrict__ screen,
-                                             const uint32_t* __restrict__ albedo, uint2* __restrict__ hdr,
-                                             uint2* __restrict__ gi_out, uint16_t* __restrict__ hist_out, size_t i) {
-    const uint2 st = screen[i];
-    const float sc0 = __half2float(__ushort_as_half((uint16_t)(st.x & 0xffffu)));
-    const float sc1 = __half2float(__ushort_as_half((uint16_t)(st.x >> 16)));
-    const float sc2 = __half2float(__ushort_as_half((uint16_t)(st.y & 0xffffu)));
-    const uint32_t alb = albedo[i];
-    const float g0 = __half2float(__float2half_rn(fmaxf((alb & 0xffu) / 255.0f, 0.01f) + 0.00001f));
-    const float g1 = __half2float(__float2half_rn(fmaxf(((alb >> 8) & 0xffu) / 255.0f, 0.01f) + 0.00001f));
-    const float g2 = __half2float(__float2half_rn(fmaxf(((alb >> 16) & 0xffu) / 255.0f, 0.01f) + 0.00001f));
-    auto pack = [](float a0, float a1, float a2, float a3) {
-        return make_uint2((uint32_t)__half_as_ushort(__float2half_rn(a0)) |
-                              ((uint32_t)__half_as_ushort(__float2half_rn(a1)) << 16),
-                          (uint32_t)__half_as_ushort(__float2half_rn(a2)) |
-                              ((uint32_t)__half_as_ushort(__float2half_rn(a3)) << 16));
-    };
-    hdr[i] = pack(sc0 + g0 * d0, sc1 + g1 * d1, sc2 + g2 * d2, 1.0f);
-    gi_out[i] = pack(d0, d1, d2, 1.0f);
-    hist_out[i] = __half_as_ushort(__float2half_rn(1.0f));
-}
-
 constexpr int kApplyTX = 32, kApplyTY = 8;
 template <bool TRAIN>
 __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
@@ -436,10 +412,7 @@ __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
         const int yy = min(max(y0 + hy - 2, 0), H - 1), xx = min(max(x0 + hx - 2, 0), W - 1);
         const size_t t = (size_t)yy * W + xx;
         if (a.noisy_h) {   // the same values as the float4 copy the feature pass can write
-            const uint2 h = a.noisy_h[(size_t)b * H * W + t];
-            tile[hy][hx] = make_float4(__half2float(__ushort_as_half((uint16_t)(h.x & 0xffffu))),
-                                       __half2float(__ushort_as_half((uint16_t)(h.x >> 16))),
-                                       __half2float(__ushort_as_half((uint16_t)(h.y & 0xffffu))), 1.0f);
+            tile[hy][hx] = rgba16_to_f4(a.noisy_h[(size_t)b * H * W + t]);
         } else {
             tile[hy][hx] = nz[t];
         }
@@ -452,27 +425,10 @@ __global__ void __launch_bounds__(256) kpcn_apply_kernel(ApplyArgs a) {
         float lf[32];
 #pragma unroll
         for (int g = 0; g < 4; ++g) bf8_to_f(vec8(a.logits, b, q, g), lf + 8 * g);
-        float l[25];
-        float mx = -3.0e38f;
-#pragma unroll
-        for (int k = 0; k < 25; ++k) { l[k] = lf[k]; mx = fmaxf(mx, l[k]); }
-        float den = 0.0f;
-#pragma unroll
-        for (int k = 0; k < 25; ++k) { l[k] = __expf(l[k] - mx); den += l[k]; }
-        const float inv = 1.0f / den;
-        float sp[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-        for (int k = 0; k < 25; ++k) {
-            l[k] *= inv;
-            const float4 nv = tile[ty + k / 5][tx + k % 5];
-            sp[0] = fmaf(l[k], nv.x, sp[0]); sp[1] = fmaf(l[k], nv.y, sp[1]); sp[2] = fmaf(l[k], nv.z, sp[2]);
-        }
-        const float alpha = 1.0f / (1.0f + __expf(-lf[25]));
+        float l[25], sp[3], alpha, o[3];
         const float4 pv = a.prev[i];
         const float pr[3] = {pv.x, pv.y, pv.z};
-        float o[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) o[c] = alpha * sp[c] + (1.0f - alpha) * pr[c];
+        kpcn_apply_px(lf, [&](int k) { return tile[ty + k / 5][tx + k % 5]; }, pr, l, sp, alpha, o);
         if (!TRAIN) {
             if (a.hdr) composite_px(o[0], o[1], o[2], a.screen, a.albedo, a.hdr, a.gi_out, a.hist_out, i);
             else a.out[i] = make_float4(o[0], o[1], o[2], 1.0f);

@@ -153,6 +153,16 @@ cudaError_t Net::conv_any(int cin, int cout, int mode, const ConvArgs& a, cudaSt
 cudaError_t Net::conv(int l, const View& x, const View& y, int B, int H, int W, cudaStream_t s, const View* pool) {
     ConvArgs a{x, wbf + w_off[l], w32 + b_off[l], y, B, H, W};
     if (pool) a.pool = *pool;
+    if (l == HEAD && head_fuse && conv_path == SGI_NN_CONV_TCGEN05) {
+        if (head_wait) {
+            const cudaError_t e = cudaStreamWaitEvent(s, head_wait, 0);
+            if (e != cudaSuccess) return e;
+        }
+        a.fuse = *head_fuse;
+        a.wait_ns = wait_ns;
+        a.skip_producer = skip_producer;
+        return conv3x3_head_apply(a, dev_err, s);
+    }
     return conv_any(kCin[l], kCout[l], l == HEAD ? 1 : 0, a, s);
 }
 
@@ -472,6 +482,27 @@ sgi_status nn_forward_net(sgi_nn* n, const void* features, int H, int W, cudaStr
     return e == cudaSuccess ? SGI_OK : nn_cuda(n, e, "forward");
 }
 
+sgi_status nn_forward_composite(sgi_nn* n, const void* features, int H, int W, const uint2* noisy, const float* prev,
+                                const uint2* screen, const uint32_t* albedo, uint2* hdr, uint2* gi_out,
+                                uint16_t* hist_out, cudaEvent_t before_head, cudaStream_t s) {
+    if (!n || !features || !noisy || !prev || !screen || !albedo || !hdr || !gi_out || !hist_out)
+        return nn_fail(n, SGI_ERR_ARG, "NULL tensor");
+    if (n->net.conv_path != SGI_NN_CONV_TCGEN05 || !n->net.head_fusion) {
+        sgi_status st = nn_forward_net(n, features, H, W, s);
+        if (st != SGI_OK) return st;
+        if (before_head && cudaStreamWaitEvent(s, before_head, 0) != cudaSuccess)
+            return nn_fail(n, SGI_ERR_CUDA, "wait for the direct lighting");
+        return nn_apply_composite(n, noisy, prev, H, W, screen, albedo, hdr, gi_out, hist_out, s);
+    }
+    const sgi::nn::ConvArgs::ApplyFuse fuse{noisy, (const float4*)prev, screen, albedo, hdr, gi_out, hist_out};
+    n->net.head_fuse = &fuse;
+    n->net.head_wait = before_head;
+    const sgi_status st = nn_forward_net(n, features, H, W, s);
+    n->net.head_fuse = nullptr;
+    n->net.head_wait = nullptr;
+    return st;
+}
+
 sgi_status nn_apply_composite(sgi_nn* n, const uint2* noisy, const float* prev, int H, int W, const uint2* screen,
                               const uint32_t* albedo, uint2* hdr, uint2* gi_out, uint16_t* hist_out, cudaStream_t s) {
     if (!n || !noisy || !prev || !screen || !albedo || !hdr || !gi_out || !hist_out)
@@ -558,6 +589,12 @@ sgi_status sgi_nn_set_precision(sgi_nn* n, int32_t precision) {
 sgi_status sgi_nn_set_conv_path(sgi_nn* n, int32_t path) {
     if (!n || (path != SGI_NN_CONV_WARP_MMA && path != SGI_NN_CONV_TCGEN05)) return SGI_ERR_ARG;
     n->net.conv_path = path;
+    return SGI_OK;
+}
+
+sgi_status sgi_nn_set_head_fusion(sgi_nn* n, int32_t enabled) {
+    if (!n) return SGI_ERR_ARG;
+    n->net.head_fusion = enabled != 0;
     return SGI_OK;
 }
 

@@ -59,6 +59,17 @@ struct ConvArgs {
     // any copy, so the MMA role's first wait runs out with nothing in flight.
     unsigned long long wait_ns;
     int skip_producer;
+    // The head (conv3x3_head_apply): the kernel apply and the composite in the
+    // epilogue instead of writing the logits (see ApplyArgs for the buffers).
+    struct ApplyFuse {
+        const uint2* noisy;       // RGBA16F
+        const float4* prev;
+        const uint2* screen;      // RGBA16F
+        const uint32_t* albedo;   // RGBA8
+        uint2* hdr;               // RGBA16F
+        uint2* gi_out;            // RGBA16F
+        uint16_t* hist_out;       // R16F
+    } fuse;
 };
 
 struct WgradArgs {
@@ -120,6 +131,9 @@ cudaError_t conv3x3(int cin, int cout, int mode, const ConvArgs& a, cudaStream_t
 // The same convolution on the 5th-generation tensor cores (sgi_nn_tc.cu); *err is
 // set to 1 when a bounded wait of a block ran out.
 cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err, cudaStream_t s);
+// the 32 -> 32 head in BF16 with the kernel apply and composite of a.fuse in its epilogue (B = 1): the HDR
+// frame, GI and history length are written, the logits are not
+cudaError_t conv3x3_head_apply(const ConvArgs& a, int* err, cudaStream_t s);
 // FP8 E4M3 operands (in8; x, w: one byte per channel, described by BF16-unit views
 // with two channels per unit) or BF16 operands (16 -> 32 only), the output E4M3
 // (out8) or BF16.

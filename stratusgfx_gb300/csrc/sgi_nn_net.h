@@ -39,6 +39,10 @@ struct Net {
     unsigned long long wait_ns = 0;   // limit of the tcgen05 waits (0: the kernels' default)
     int skip_producer = 0;            // test switch: the convolutions' TMA producers issue nothing
     int conv_path = SGI_NN_CONV_TCGEN05;
+    // set while a neural frame runs: the head applies the kernels and writes the composite itself
+    const ConvArgs::ApplyFuse* head_fuse = nullptr;
+    bool head_fusion = true;           // sgi_nn_set_head_fusion
+    cudaEvent_t head_wait = nullptr;   // waited for before the head (the direct lighting it composites)
     // FP8 E4M3 inference (after calibrate_fp8): quantized weights (offsets w_off),
     // per-output-channel weight scales and inverse output scales (offsets sc_off),
     // per-input-channel scales folded into the weights (offsets in_off)
@@ -81,5 +85,11 @@ struct sgi_nn {
 // of the denoised GI; see composite_px in sgi_nn.cu). The noisy GI is read from the
 // RGBA16F pass-0 output the features were built from.
 sgi_status nn_forward_net(sgi_nn* n, const void* features, int H, int W, cudaStream_t s);
+// The network's forward with the kernel apply and composite fused into the head (tcgen05 path), or the
+// forward followed by the apply kernel (other paths); `before_head` (nullable) is waited for before the
+// first kernel that reads `screen`.
+sgi_status nn_forward_composite(sgi_nn* n, const void* features, int H, int W, const uint2* noisy, const float* prev,
+                                const uint2* screen, const uint32_t* albedo, uint2* hdr, uint2* gi_out,
+                                uint16_t* hist_out, cudaEvent_t before_head, cudaStream_t s);
 sgi_status nn_apply_composite(sgi_nn* n, const uint2* noisy, const float* prev, int H, int W, const uint2* screen,
                               const uint32_t* albedo, uint2* hdr, uint2* gi_out, uint16_t* hist_out, cudaStream_t s);

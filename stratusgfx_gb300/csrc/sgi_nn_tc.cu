@@ -44,6 +44,7 @@
 
 #include <mutex>
 
+#include "sgi_nn_apply.cuh"
 #include "sgi_nn_internal.h"
 
 namespace sgi {
@@ -709,6 +710,34 @@ template <int CIN, bool F8, int COUT> constexpr int rs_rows_any() {
     else return 0;
 }
 
+// The head's epilogue with the kernel apply (mode 3): the pixel's 32 logits
+// as the plain head stores them (accumulator + bias, rounded to BF16), then the
+// kernel apply and composite of kpcn_apply_kernel (sgi_nn_apply.cuh) with the
+// 5x5 neighbours of the noisy estimate read from global memory (clamped; a
+// warp's 32 consecutive pixels share them in L1). Exchanging one load per lane
+// and row by shuffles instead measured the same.
+__device__ __forceinline__ void head_apply_px(const ConvArgs& a, const uint32_t* v, const float* sc, const float* bb,
+                                              int y, int x) {
+    float lf[32];
+    act16<1>(v, sc, bb, lf);
+    act16<1>(v + 16, sc + 16, bb + 16, lf + 16);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) lf[j] = __bfloat162float(__float2bfloat16_rn(lf[j]));
+    const int W = a.W, H = a.H;
+    const size_t i = (size_t)y * W + x;
+    const ConvArgs::ApplyFuse& f = a.fuse;
+    const float4 pv = f.prev[i];
+    const float pr[3] = {pv.x, pv.y, pv.z};
+    float l[25], sp[3], alpha, o[3];
+    kpcn_apply_px(lf,
+                  [&](int k) {
+                      const int yy = min(max(y + k / 5 - 2, 0), H - 1), xx = min(max(x + k % 5 - 2, 0), W - 1);
+                      return rgba16_to_f4(__ldg(f.noisy + (size_t)yy * W + xx));
+                  },
+                  pr, l, sp, alpha, o);
+    composite_px(o[0], o[1], o[2], f.screen, f.albedo, f.hdr, f.gi_out, f.hist_out, i);
+}
+
 template <int CIN, int MODE, bool F8, bool OUT8, int ROWS_, int COUT_>
 __global__ void __launch_bounds__(kRsThreads, 512 / (ROWS_ * COUT_))
     conv3x3_rs_kernel(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_w,
@@ -942,6 +971,18 @@ __global__ void __launch_bounds__(kRsThreads, 512 / (ROWS_ * COUT_))
                 const int y = yb + 2 * p;   // even: strips start on multiples of 4
                 bf16* yp0 = a.y.p + a.y.at(b, valid ? (size_t)y * a.W + px : 0, 0);
                 bf16* yp1 = a.y.p + a.y.at(b, valid && two ? (size_t)(y + 1) * a.W + px : 0, 0);
+                if constexpr (MODE == 3) {
+                    // the head with the kernel apply: group g takes row 2p + g with all 32 logits
+                    const int r = 2 * p + grp;
+                    const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(COUT * (ROWS - 1 - r));
+                    uint32_t v[32];
+                    tmem_ld16(ta, v);
+                    tmem_ld16(ta + 16, v + 16);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    tmem_st16_zero(ta);
+                    tmem_st16_zero(ta + 16);
+                    if (r < nrows && valid) head_apply_px(a, v, sc_s, bb_s, yb + r, px);
+                } else {
 #pragma unroll
                 for (int u = 0; u < CPT / 16; ++u) {
                     const int cb = c0 + 16 * u;   // first channel of this piece
@@ -987,6 +1028,7 @@ __global__ void __launch_bounds__(kRsThreads, 512 / (ROWS_ * COUT_))
                             *reinterpret_cast<uint4*>(a.pool.p +
                                                       a.pool.at(b, (size_t)(y / 2) * (a.W / 2) + px / 2, k)) = om[g];
                     }
+                }
                 }
                 asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -1148,6 +1190,14 @@ cudaError_t conv3x3_tc(int cin, int cout, int mode, const ConvArgs& a, int* err,
     SGI_TC_CASE(32, 96)
 #undef SGI_TC_CASE
     return cudaErrorInvalidValue;
+}
+
+cudaError_t conv3x3_head_apply(const ConvArgs& a, int* err, cudaStream_t s) {
+    const ConvArgs::ApplyFuse& f = a.fuse;
+    if (!err || !view_ok(a.x) || a.x.grp != 8 || (((uintptr_t)a.w) & 15) || !a.bias || a.B != 1 || a.H < 1 ||
+        a.W < 1 || !f.noisy || !f.prev || !f.screen || !f.albedo || !f.hdr || !f.gi_out || !f.hist_out)
+        return cudaErrorInvalidValue;
+    return run_rs<32, 32, 3, false, false>(a, err, s);
 }
 
 cudaError_t conv3x3_tc_fp8(int cin, int cout, int mode, bool in8, bool out8, const ConvArgs& a, int* err,

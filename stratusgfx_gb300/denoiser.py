@@ -83,6 +83,10 @@ class KpcnDenoiser:
         """abi.SGI_NN_CONV_TCGEN05 (tcgen05.mma, TMEM accumulators) or abi.SGI_NN_CONV_WARP_MMA."""
         self._chk(self.lib.sgi_nn_set_conv_path(self.h, path))
 
+    def set_head_fusion(self, enabled: bool):
+        """The neural frame's kernel apply in the head convolution's epilogue (default) or as a separate pass."""
+        self._chk(self.lib.sgi_nn_set_head_fusion(self.h, 1 if enabled else 0))
+
     def set_precision(self, precision: int):
         """abi.SGI_NN_BF16 or abi.SGI_NN_FP8 (after calibrate_fp8)."""
         self._chk(self.lib.sgi_nn_set_precision(self.h, precision))

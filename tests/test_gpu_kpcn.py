@@ -184,6 +184,51 @@ def test_neural_frame_runs_through_the_abi():
     net.close()
 
 
+@pytest.mark.parametrize("precision", [abi.SGI_NN_BF16, abi.SGI_NN_FP8])
+def test_head_with_fused_kernel_apply_equals_the_separate_pass(precision):
+    """The neural frame with the kernel apply and composite in the head convolution's epilogue equals the
+    frame whose head writes BF16 logits for the separate kernel-apply pass (same logits, same expressions)."""
+    import ctypes as C
+
+    from stratusgfx_gb300 import denoiser
+    w = S.Workload("room12_200x96_vpl64", 200, 96, 12, 64, 2, 512, 16, abi.SGI_CUBE_F16, 2, 5, 2)
+    sc = S.workload_scene(w, 33)
+    ds = stage.DeviceScene(sc, w)
+    net = KpcnDenoiser(1, w.height, w.width, seed=1)
+    net.load(denoiser.WEIGHTS)
+    outs = {}
+    for fused in (True, False):
+        st = stage.GiStage(stage.workload_config(w))
+        st.set_lights(ds.vpls, ds.entries, ds.points)
+        if precision == abi.SGI_NN_FP8 and fused:
+            feat = torch.zeros((1, w.height, w.width, 16), dtype=torch.bfloat16, device="cuda")
+            feat.normal_()
+            net.calibrate_fp8(feat)
+        net.set_precision(precision)
+        net.set_head_fusion(fused)
+        frames = []
+        for k in (1, 2):
+            st.set_shadow_maps(ds.csms[k], ds.cubes)
+            out = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
+            fp = abi.FrameParams(1000.0 + 16 * k, 60.0)
+            abi.check(st.lib.sgi_render_frame_neural(st.ctx, net.h, C.byref(ds.gbuffers[k].struct()),
+                                                     C.byref(ds.gbuffers[k - 1].struct()), C.byref(ds.camera(k)),
+                                                     C.byref(fp), C.c_void_p(out.data_ptr()), C.c_void_p(0)),
+                      st.ctx)
+            frames.append(out.cpu().numpy())
+        net.device_status()
+        gi = st.read_debug(abi.SGI_DEBUG_GI_HISTORY, np.uint16)
+        hist = st.read_debug(abi.SGI_DEBUG_HISTORY_DEPTH, np.uint16)
+        outs[fused] = (frames, gi, hist)
+        st.close()
+    net.set_precision(abi.SGI_NN_BF16)
+    net.close()
+    (fa, ga, ha), (fb, gb, hb) = outs[True], outs[False]
+    for k in range(2):
+        assert np.array_equal(fa[k].view(np.uint16), fb[k].view(np.uint16)), f"frame {k + 1}"
+    assert np.array_equal(ga, gb) and np.array_equal(ha, hb)
+
+
 def test_fp8_forward_tracks_bf16_on_rendered_frames():
     """FP8 E4M3 inference (per-channel scales calibrated on one frame set, applied to
     another) against the BF16 network with the trained weights, on frames the plain

@@ -221,22 +221,26 @@ SGI_D void bitonic_stage64(unsigned long long& k0, unsigned long long& k1, int s
     }
 }
 
-// The list of one tile (mean position tp, mean normal tn) by a block of
-// kCullThreads threads; cull_smem holds 2 x count uint32 (keys, bin members).
+// The list of one tile (mean position tp, mean normal tn) by a block of NT
+// threads (128 or 256); cull_smem holds 2 x count uint32 (keys, bin members).
+template <int NT = kCullThreads>
 SGI_D void tile_cull(int L, V3 tp, V3 tn, const float4* __restrict__ vpr, int count, uint32_t* cull_smem,
                      int32_t* __restrict__ out, int tid) {
+    static_assert(NT == 128 || NT == 256, "block size");
+    constexpr int BPT = 256 / NT;   // histogram bins per thread
     __shared__ uint32_t hist[256];
     __shared__ unsigned long long kept[64];
-    __shared__ int warp_sum[kCullThreads / 32];
+    __shared__ int warp_sum[NT / 32];
     __shared__ int s_bin, s_need, s_nkept, s_nb, s_mc;
     const int lane = tid & 31, warp = tid >> 5;
     uint32_t* keys = cull_smem;
     uint32_t* members = cull_smem + count;
-    hist[tid] = 0u;
+#pragma unroll
+    for (int j = 0; j < BPT; ++j) hist[tid * BPT + j] = 0u;
     if (tid == 0) { s_nkept = 0; s_nb = 0; }
     __syncthreads();
     int mine = 0;
-    for (int k = tid; k < count; k += kCullThreads) {
+    for (int k = tid; k < count; k += NT) {
         const float4 v = __ldg(vpr + k);
         const V3 lmf = xsub3(v3(v.x, v.y, v.z), tp);
         const float side = xdot(tn, lmf);
@@ -257,26 +261,32 @@ SGI_D void tile_cull(int L, V3 tp, V3 tn, const float4* __restrict__ vpr, int co
     __syncthreads();
     if (tid == 0) {
         int mc = 0;
-        for (int w = 0; w < kCullThreads / 32; ++w) mc += warp_sum[w];
+        for (int w = 0; w < NT / 32; ++w) mc += warp_sum[w];
         s_mc = mc;
     }
     __syncthreads();
     const int mc = s_mc;
     const int take = mc < L ? mc : L;
     if (mc > L) {
-        // inclusive scan of the histogram: bin b holds the L-th candidate
-        const uint32_t h = hist[tid];
-        uint32_t incl = h;
+        // inclusive scan of the histogram: bin b holds the L-th candidate (thread tid owns bins
+        // tid * BPT .. + BPT - 1)
+        uint32_t h[BPT], tot = 0;
+#pragma unroll
+        for (int j = 0; j < BPT; ++j) { h[j] = hist[tid * BPT + j]; tot += h[j]; }
+        uint32_t incl = tot;
         for (int off = 1; off < 32; off <<= 1) {
             const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
             if (lane >= off) incl += t;
         }
         if (lane == 31) warp_sum[warp] = (int)incl;
         __syncthreads();
-        uint32_t before = 0;
-        for (int w = 0; w < warp; ++w) before += (uint32_t)warp_sum[w];
-        incl += before;
-        if (incl >= (uint32_t)L && incl - h < (uint32_t)L) { s_bin = tid; s_need = L - (int)(incl - h); }
+        uint32_t run = incl - tot;   // candidates below this thread's first bin
+        for (int w = 0; w < warp; ++w) run += (uint32_t)warp_sum[w];
+#pragma unroll
+        for (int j = 0; j < BPT; ++j) {
+            if (run + h[j] >= (uint32_t)L && run < (uint32_t)L) { s_bin = tid * BPT + j; s_need = L - (int)run; }
+            run += h[j];
+        }
         __syncthreads();
     } else if (tid == 0) {
         s_bin = 256;   // every candidate is kept
@@ -285,7 +295,7 @@ SGI_D void tile_cull(int L, V3 tp, V3 tn, const float4* __restrict__ vpr, int co
     __syncthreads();
     const int bin = s_bin;
     // kept: candidates of lower bins; bin b's members are ranked below
-    for (int k = tid; k < count; k += kCullThreads) {
+    for (int k = tid; k < count; k += NT) {
         const uint32_t u = keys[k];
         if (u == kNoKey) continue;
         const int b = ratio_bin(key_value(u));
@@ -295,7 +305,7 @@ SGI_D void tile_cull(int L, V3 tp, V3 tn, const float4* __restrict__ vpr, int co
     __syncthreads();
     if (mc > L) {
         const int nb = s_nb, need = s_need;
-        for (int m = tid; m < nb; m += kCullThreads) {
+        for (int m = tid; m < nb; m += NT) {
             const uint32_t k = members[m];
             const unsigned long long mk = pair_key(keys[k], (int)k);
             int rank = 0;

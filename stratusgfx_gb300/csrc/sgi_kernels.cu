@@ -216,17 +216,18 @@ cudaError_t launch_tile_stage1(const sgi_config& cfg, const sgi_gbuffer& g, cons
     return cudaGetLastError();
 }
 
-// Stage 2: one 256-thread block per tile, tile_cull of sgi_cull.cuh.
-__global__ void __launch_bounds__(kCullThreads) tile_cull_kernel(int L, const sgi_tile_stage1* __restrict__ s1,
-                                                                 const float4* __restrict__ vpr,
-                                                                 const int32_t* __restrict__ visible_index,
-                                                                 int32_t* __restrict__ lists) {
+// Stage 2: one block of kTileCullThreads threads per tile, tile_cull of sgi_cull.cuh.
+constexpr int kTileCullThreads = 128;
+__global__ void __launch_bounds__(kTileCullThreads) tile_cull_kernel(int L, const sgi_tile_stage1* __restrict__ s1,
+                                                                     const float4* __restrict__ vpr,
+                                                                     const int32_t* __restrict__ visible_index,
+                                                                     int32_t* __restrict__ lists) {
     extern __shared__ uint32_t cull_smem[];   // keys[count], then bin-b member indices[count]
     const int tile = blockIdx.x;
     const float4 p4 = __ldg(reinterpret_cast<const float4*>(s1 + tile));
     const float4 n4 = __ldg(reinterpret_cast<const float4*>(s1 + tile) + 1);
-    tile_cull(L, v3(p4.x, p4.y, p4.z), v3(n4.x, n4.y, n4.z), vpr, __ldg(visible_index), cull_smem,
-              lists + (size_t)tile * (1 + L), threadIdx.x);
+    tile_cull<kTileCullThreads>(L, v3(p4.x, p4.y, p4.z), v3(n4.x, n4.y, n4.z), vpr, __ldg(visible_index), cull_smem,
+                                lists + (size_t)tile * (1 + L), threadIdx.x);
 }
 
 size_t tile_cull_smem(const sgi_config& cfg) { return (size_t)2 * sizeof(uint32_t) * (size_t)cfg.max_visible; }
@@ -240,7 +241,7 @@ cudaError_t launch_tile_stage2(const sgi_config& cfg, const sgi_tile_stage1* s1,
         cudaError_t e = cudaFuncSetAttribute(tile_cull_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    tile_cull_kernel<<<T, kCullThreads, smem, s>>>(cfg.max_vpls_per_tile, s1, vpr, visible_index, lists);
+    tile_cull_kernel<<<T, kTileCullThreads, smem, s>>>(cfg.max_vpls_per_tile, s1, vpr, visible_index, lists);
     return cudaGetLastError();
 }
 

@@ -405,6 +405,27 @@ SGI_D V3 lighting_burley_px(const BurleyPixel& b, V3 lightColor, V3 lightDir, V3
     V3 fc = v3(sp.fog_color[0], sp.fog_color[1], sp.fog_color[2]) * fogIntensity;
     return atten * (ambient + shadowFactor * (finalB * b.fogF + fc * (1.0f - b.fogF)));
 }
+// lighting_burley_px for a light direction whose length len is already known
+// (the light's distance, computed for the range test): normalize(lightDir) is
+// lightDir * (1 / len), and in the exact build len is the square root that
+// normalize would take, so the result is the same.
+SGI_D V3 lighting_burley_pxl(const BurleyPixel& b, V3 lightColor, V3 lightDir, float len, V3 V, V3 N,
+                             float fogIntensity, float ao, float shadowFactor, float atten, float ambientIntensity,
+                             const ShadeParams& sp) {
+    const V3 L = lightDir * (1.0f / len);
+    const V3 H = normalize(V + L);
+    const float NdotV = saturate(dot(N, V)), NdotL = saturate(dot(N, L));
+    const float NdotH = saturate(dot(N, H)), LdotH = saturate(dot(L, H));
+    V3 Fr = spec_brdf(NdotV, NdotL, NdotH, LdotH, b.rr, b.f0);
+    V3 Fd = b.dc * fd_burley(NdotV, NdotL, LdotH, b.rr);
+    V3 brdf = (Fd + Fr) * NdotL;
+    V3 ambient = brdf * ao * lightColor * ambientIntensity;
+    V3 finalB = brdf * lightColor;
+    V3 fc = v3(sp.fog_color[0], sp.fog_color[1], sp.fog_color[2]) * fogIntensity;
+    return atten * (ambient + shadowFactor * (finalB * b.fogF + fc * (1.0f - b.fogF)));
+}
+// quadraticAttenuation, pbr.glsl:255-258, with |lightDir| given
+SGI_D float quadratic_atten_len(float d) { return 1.0f / (1.0f + d * d); }
 // quadraticAttenuation, pbr.glsl:255-258
 SGI_D float quadratic_atten(V3 lightDir) { float d = length(lightDir); return 1.0f / (1.0f + d * d); }
 // vplDiffuseAttenuation / vplSpecularAttenuation, pbr.glsl:260-271

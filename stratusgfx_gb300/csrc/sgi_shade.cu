@@ -652,7 +652,28 @@ struct DeferredParams {
 
 // pbr.fs:82-145: non-shadow-casting point lights + the directional light
 // with its CSM (INFINITE_LIGHTING_ENABLED).
-SGI_D void deferred_pixel(const DeferredParams& p, int x, int y) {
+// Per-light constants of a block: the fog intensity length(colour) / 12 of
+// the first kLightConst point lights and shadow casters (the same operations
+// as per pixel, once per block).
+constexpr int kLightConst = 32;
+struct LightConst {
+    float point_fog[kLightConst], caster_fog[kLightConst];
+    int points, casters;   // how many of each are held
+};
+SGI_D void light_const_fill(const DeferredParams& p, LightConst& lc, int tid, int nthreads) {
+    const int np = p.num_points < kLightConst ? p.num_points : kLightConst;
+    const int nc = p.casters.count < kLightConst ? p.casters.count : kLightConst;
+    for (int l = tid; l < np + nc; l += nthreads) {
+        const bool caster = l >= np;
+        const float4 c4 = __ldg(reinterpret_cast<const float4*>(caster ? p.casters.lights + (l - np) : p.points + l) + 1);
+        const float f = length(v3(c4.x, c4.y, c4.z)) / 12.0f;
+        if (caster) lc.caster_fog[l - np] = f;
+        else lc.point_fog[l] = f;
+    }
+    if (tid == 0) { lc.points = np; lc.casters = nc; }
+}
+
+SGI_D void deferred_pixel(const DeferredParams& p, int x, int y, const LightConst* lcs = nullptr) {
     const size_t i = (size_t)y * p.W + x;
     ShadeParams sp{p.sc.min_roughness, p.sc.perceptual, p.sc.fog_density,
                    {p.sc.fog_color[0], p.sc.fog_color[1], p.sc.fog_color[2]}, p.sc.point_ambient};
@@ -680,10 +701,11 @@ SGI_D void deferred_pixel(const DeferredParams& p, int x, int y) {
         const V3 lp = v3(lp4.x, lp4.y, lp4.z), lc = v3(lc4.x, lc4.y, lc4.z);
         const float distance = xlength(xsub3(lp, fragPos));
         if (distance < m4.x) {
-            // calculatePointLighting2, pbr2.glsl:593-611
+            // calculatePointLighting2, pbr2.glsl:593-611; |lightDir| is `distance`
             const V3 lightDir = lp - fragPos;
-            color = color + lighting_burley_px(bp, lc, lightDir, viewDir, normal, length(lc) / 12.0f, ambient,
-                                               1.0f - 0.0f, quadratic_atten(lightDir), sp.point_ambient, sp);
+            const float fog = lcs && l < lcs->points ? lcs->point_fog[l] : length(lc) / 12.0f;
+            color = color + lighting_burley_pxl(bp, lc, lightDir, distance, viewDir, normal, fog, ambient,
+                                                1.0f - 0.0f, quadratic_atten_len(distance), sp.point_ambient, sp);
         }
     }
     // shadowCasters, pbr.fs:116-131
@@ -702,8 +724,10 @@ SGI_D void deferred_pixel(const DeferredParams& p, int x, int y) {
                 shadowFactor = shadow_1sample(p.casters.atlas, entry, m4.y, fragPos, lp, xdot(xsub3(lp, fragPos), normal),
                                               0.03f);
             const V3 lightDir = lp - fragPos;
-            color = color + lighting_burley_px(bp, lc, lightDir, viewDir, normal, length(lc) / 12.0f, ambient,
-                                               1.0f - shadowFactor, quadratic_atten(lightDir), sp.point_ambient, sp);
+            const float fog = lcs && l < lcs->casters ? lcs->caster_fog[l] : length(lc) / 12.0f;
+            color = color + lighting_burley_pxl(bp, lc, lightDir, distance, viewDir, normal, fog, ambient,
+                                                1.0f - shadowFactor, quadratic_atten_len(distance), sp.point_ambient,
+                                                sp);
         }
     }
     const V3 lightDir = v3(p.csm.light_direction[0], p.csm.light_direction[1], p.csm.light_direction[2]);
@@ -717,9 +741,12 @@ SGI_D void deferred_pixel(const DeferredParams& p, int x, int y) {
 }
 
 __global__ void __launch_bounds__(256, 4) deferred_pbr_csm_kernel(DeferredParams p) {
+    __shared__ LightConst lcs;
+    light_const_fill(p, lcs, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y);
+    __syncthreads();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x < p.W && y < p.H) deferred_pixel(p, x, y);
+    if (x < p.W && y < p.H) deferred_pixel(p, x, y, &lcs);
 }
 
 cudaError_t launch_deferred(const sgi_config& cfg, const ShadeConfig& sc, const sgi_gbuffer& g,

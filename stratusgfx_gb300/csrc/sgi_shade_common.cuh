@@ -67,6 +67,68 @@ SGI_D float csm_pcf(const float* __restrict__ base, int R, float s, float t, flo
     return bilinear_sum(q, c00, c10, c01, c11);
 }
 
+// The 3x3 filtered samples of one cascade (pbr.glsl:206-215): the sum over
+// yi (outer), xi (inner) in -1..1 of csm_pcf at (s + xi wh, t + yi wh), added
+// in that order. The samples share their coordinates per axis (u depends on
+// xi only, v on yi only), so the texel columns, rows and fractions are formed
+// once per axis value. Where the columns of the three xi form the run
+// c - 1 .. c + 2 (and the rows likewise) -- away from the map's edges, where
+// the clamp repeats a texel -- the 16 texels of that window are read and
+// compared once; otherwise each sample reads its own four. Either way every
+// sample's weights and compare results are those csm_pcf forms.
+SGI_D float csm_pcf9(const float* __restrict__ base, int R, float s, float t, float wh, float ref) {
+    float a[3], b[3];
+    int c0[3], c1[3];
+    size_t r0[3], r1[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float o = xmul(float(k - 1), wh);
+        const float u = xsub(xmul(xadd(s, o), float(R)), 0.5f), v = xsub(xmul(xadd(t, o), float(R)), 0.5f);
+        const float fu = floorf(u), fv = floorf(v);
+        a[k] = xsub(u, fu);
+        b[k] = xsub(v, fv);
+        c0[k] = tex_index(fu, R);
+        c1[k] = tex_index(xadd(fu, 1.0f), R);
+        r0[k] = (size_t)tex_index(fv, R) * R;
+        r1[k] = (size_t)tex_index(xadd(fv, 1.0f), R) * R;
+    }
+    const bool run = c0[0] + 1 == c0[1] && c0[1] + 1 == c0[2] && c1[0] == c0[0] + 1 && c1[2] == c0[2] + 1 &&
+                     r0[0] + R == r0[1] && r0[1] + R == r0[2] && r1[0] == r0[0] + R && r1[2] == r0[2] + R;
+    float light = 0.0f;
+    if (run) {
+        float cmp[4][4];   // [row r0[0] + i R][column c0[0] + j]
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) cmp[i][j] = ref <= __ldg(base + r0[0] + (size_t)i * R + c0[0] + j) ? 1.0f : 0.0f;
+#pragma unroll
+        for (int yi = 0; yi < 3; ++yi)
+#pragma unroll
+            for (int xi = 0; xi < 3; ++xi) {
+                const float w00 = xmul(xsub(1.0f, a[xi]), xsub(1.0f, b[yi])), w10 = xmul(a[xi], xsub(1.0f, b[yi]));
+                const float w01 = xmul(xsub(1.0f, a[xi]), b[yi]), w11 = xmul(a[xi], b[yi]);
+                const float f = __fmaf_rn(cmp[yi + 1][xi + 1], w11,
+                                          __fmaf_rn(cmp[yi + 1][xi], w01, __fmaf_rn(cmp[yi][xi + 1], w10,
+                                                                                    xmul(cmp[yi][xi], w00))));
+                light = xadd(light, f);
+            }
+    } else {
+#pragma unroll
+        for (int yi = 0; yi < 3; ++yi)
+#pragma unroll
+            for (int xi = 0; xi < 3; ++xi) {
+                const float w00 = xmul(xsub(1.0f, a[xi]), xsub(1.0f, b[yi])), w10 = xmul(a[xi], xsub(1.0f, b[yi]));
+                const float w01 = xmul(xsub(1.0f, a[xi]), b[yi]), w11 = xmul(a[xi], b[yi]);
+                const float d00 = ref <= __ldg(base + r0[yi] + c0[xi]) ? 1.0f : 0.0f;
+                const float d10 = ref <= __ldg(base + r0[yi] + c1[xi]) ? 1.0f : 0.0f;
+                const float d01 = ref <= __ldg(base + r1[yi] + c0[xi]) ? 1.0f : 0.0f;
+                const float d11 = ref <= __ldg(base + r1[yi] + c1[xi]) ? 1.0f : 0.0f;
+                light = xadd(light, __fmaf_rn(d11, w11, __fmaf_rn(d01, w01, __fmaf_rn(d10, w10, xmul(d00, w00)))));
+            }
+    }
+    return light;
+}
+
 // calculateInfiniteShadowValue, pbr.glsl:158-227: lit fraction.
 SGI_D float infinite_shadow(const sgi_csm& csm, V3 fragPos, V3 normal, bool useDepthBias) {
     V3 blends = v3(dot4(csm.cascade_planes[0], fragPos), dot4(csm.cascade_planes[1], fragPos),
@@ -91,17 +153,9 @@ SGI_D float infinite_shadow(const sgi_csm& csm, V3 fragPos, V3 normal, bool useD
     const float* b1 = csm.depth + (size_t)index1 * R * R;
     const float* b2 = csm.depth + (size_t)index2 * R * R;
     float ref1 = xsub(depth1, bias), ref2 = xsub(depth2, bias);
-    float light1 = 0.0f, light2 = 0.0f, samples = 0.0f;
-#pragma unroll
-    for (int yi = -1; yi <= 1; ++yi) {
-#pragma unroll
-        for (int xi = -1; xi <= 1; ++xi) {
-            float ox = xmul(float(xi), wh), oy = xmul(float(yi), wh);
-            light1 = xadd(light1, csm_pcf(b1, R, xadd(cc1.x, ox), xadd(cc1.y, oy), ref1));
-            light2 = xadd(light2, csm_pcf(b2, R, xadd(cc2.x, ox), xadd(cc2.y, oy), ref2));
-            samples = xadd(samples, 1.0f);
-        }
-    }
+    const float light1 = csm_pcf9(b1, R, cc1.x, cc1.y, wh, ref1);
+    const float light2 = csm_pcf9(b2, R, cc2.x, cc2.y, wh, ref2);
+    const float samples = 9.0f;   // the nine samples counted one by one: exact
     return xmul(xmixf(light2, light1, weight), xdiv(1.0f, samples));
 }
 

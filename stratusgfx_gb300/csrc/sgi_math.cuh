@@ -428,7 +428,12 @@ SGI_D V3 lighting_burley_pxl(const BurleyPixel& b, V3 lightColor, V3 lightDir, f
 SGI_D float quadratic_atten_len(float d) { return 1.0f / (1.0f + d * d); }
 // quadraticAttenuation, pbr.glsl:255-258
 SGI_D float quadratic_atten(V3 lightDir) { float d = length(lightDir); return 1.0f / (1.0f + d * d); }
-// vplDiffuseAttenuation / vplSpecularAttenuation, pbr.glsl:260-271
+// vplDiffuseAttenuation / vplSpecularAttenuation, pbr.glsl:260-271, with d = |lightDir|
+SGI_D float vpl_atten_len(float d, float radius) {
+    float ratio = gmin(d / radius, 1.0f);
+    float minDist = mixf(10.0f, 1.0f, expf_ieee(-3.0f * ratio)) * radius;
+    return 1.0f / (minDist + 1.0f * d * d);
+}
 SGI_D float vpl_atten(V3 lightDir, float radius) {
     float d = length(lightDir);
     float ratio = gmin(d / radius, 1.0f);
@@ -455,15 +460,27 @@ SGI_D VplPixel vpl_pixel(V3 fragPos, V3 baseColor, V3 N, V3 V, float viewDist, f
     q.fogAdd = fc * (1.0f - q.fogF);
     return q;
 }
-SGI_D V3 vpl_lighting2_sample(const VplPixel& q, V3 specPos, V3 diffPos, V3 lightColor, float radius) {
+// diffLen: |diffPos - fragPos| when the caller has it (the gather's distance to
+// the VPL, the same square root in the exact build), else negative
+SGI_D V3 vpl_lighting2_sample(const VplPixel& q, V3 specPos, V3 diffPos, V3 lightColor, float radius,
+                              float diffLen = -1.0f) {
     V3 specDir = specPos - q.fragPos;
     V3 diffDir = diffPos - q.fragPos;
-    float specAtten = vpl_atten(specDir, radius);
-    float diffAtten = vpl_atten(diffDir, radius);
+    const float specLen = length(specDir);
+    if (!(diffLen >= 0.0f)) diffLen = length(diffDir);
+    float specAtten = vpl_atten_len(specLen, radius);
+    float diffAtten = vpl_atten_len(diffLen, radius);
     float NdotV, NdotL, NdotH, LdotH;
-    brdf_dots(q.V, specDir, q.N, NdotV, NdotL, NdotH, LdotH);
+    {   // brdf_dots(q.V, specDir, ...) with normalize(specDir) = specDir * (1 / |specDir|)
+        const V3 L = specDir * (1.0f / specLen);
+        const V3 H = normalize(q.V + L);
+        NdotV = saturate(dot(q.N, q.V));
+        NdotL = saturate(dot(q.N, L));
+        NdotH = saturate(dot(q.N, H));
+        LdotH = saturate(dot(L, H));
+    }
     V3 Fr = spec_brdf(NdotV, NdotL, NdotH, LdotH, q.rr, q.f0) * NdotL;
-    brdf_dots(q.V, diffDir, q.N, NdotV, NdotL, NdotH, LdotH);
+    NdotL = saturate(dot(q.N, diffDir * (1.0f / diffLen)));   // brdf_dots(q.V, diffDir, ...): only N.L is used
     V3 Fd = (q.dc * (1.0f / kPi)) * NdotL;
     V3 bs = specAtten * Fr;
     V3 bd = diffAtten * Fd;

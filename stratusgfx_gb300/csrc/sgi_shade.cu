@@ -187,7 +187,7 @@ SGI_D void sample_vpls(const GatherParams& p, const PixelShade& px, float seedX,
         if (shadowFactor > 0.0f) reweight = (1.0f - distAttenuation) * minGi + distAttenuation;
         validSamples += reweight;
         const V3 tmp = px.ao * vpl_lighting2_sample(vp, v3(spec.x, spec.y, spec.z), lightPosition, lightColor,
-                                                    lightRadius);
+                                                    lightRadius, distance);
         vplColor = vplColor + (1.0f - shadowFactor) * tmp;
     }
 }

@@ -169,6 +169,7 @@ sgi::PViewDesc view_desc(const sgi_view& v, uint2** pass_buf, int parity) {
     d.gi_prev = c->gi_hist[cur]; d.gi_out = c->gi_hist[1 - cur];
     d.hist_prev = c->hist_depth[cur]; d.hist_out = c->hist_depth[1 - cur];
     d.hdr_out = v.hdr_out;
+    d.atrous_staged = v.ctx->atrous_staged ? 1 : 0;
     return d;
 }
 
@@ -193,8 +194,8 @@ sgi_status build_persistent(sgi_batch* b, int32_t tune_frames, cudaStream_t s) {
         for (int parity = 0; parity < 2; ++parity) {
             const sgi::PViewDesc d = view_desc(v, pass_buf, parity);
             unsigned char* out = host_views.data() + ((size_t)parity * n + i) * vb;
-            if (b->fast) sgi::fast::persistent_fill_view(d, out);
-            else sgi::exact::persistent_fill_view(d, out);
+            const bool filled = b->fast ? sgi::fast::persistent_fill_view(d, out) : sgi::exact::persistent_fill_view(d, out);
+            if (!filled) return bfail(b, SGI_ERR_CUDA, "tensor maps of the staged a-trous passes");
         }
         const int blocks = ((cfg.width + 15) / 16) * ((cfg.height + 15) / 16);
         const int chunks = (blocks + sgi::kPBlocksPerItem - 1) / sgi::kPBlocksPerItem;
@@ -204,7 +205,14 @@ sgi_status build_persistent(sgi_batch* b, int32_t tune_frames, cudaStream_t s) {
         c[sgi::kPDirect] = chunks;
         c[sgi::kPTile] = chunks;
         c[sgi::kPGather] = chunks;
-        for (int pass = 1; pass < cfg.denoise_passes; ++pass) c[sgi::kPAtrous + pass - 1] = chunks;
+        for (int pass = 1; pass < cfg.denoise_passes; ++pass) {
+            // staged a-trous passes (1..3, the context's staging on, even width) have lattice CTAs as items
+            int gx, gy, ntx, nty;
+            const int lat = pass < cfg.denoise_passes - 1 && v.ctx->atrous_staged
+                                ? sgi::atrous_lattice_grid(cfg.width, cfg.height, pass, &gx, &gy, &ntx, &nty)
+                                : 0;
+            c[sgi::kPAtrous + pass - 1] = lat > 0 ? (lat + sgi::kPBlocksPerItem - 1) / sgi::kPBlocksPerItem : chunks;
+        }
         if (cfg.max_visible > max_visible) max_visible = cfg.max_visible;
     }
     // dispatch order: pass by pass, every view's items of a pass before the next pass

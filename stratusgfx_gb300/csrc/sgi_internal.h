@@ -132,6 +132,7 @@ struct PViewDesc {
     uint2* direct;
     const uint2* gi_prev; uint2* gi_out; const uint16_t* hist_prev; uint16_t* hist_out;
     void* hdr_out;
+    int32_t atrous_staged;   // the context's a-trous staging (sgi_set_atrous_staging)
 };
 
 struct PPlan {
@@ -146,6 +147,18 @@ struct PPlan {
     const unsigned char* views;  // per-view parameter blocks of view_bytes each
     int32_t view_bytes;
 };
+
+// The CTA grid of the staged a-trous pass at stride 2^pass (sgi_shade.cu): lattice patches of 16 x 8 points
+// per two x remainders, (ntx * s / 2) x (nty * s) CTAs; 0 (no staged pass) for strides above 8 or odd widths.
+inline int atrous_lattice_grid(int W, int H, int pass, int* gx, int* gy, int* ntx, int* nty) {
+    const int st = pass >= 1 && pass <= 3 ? 1 << pass : 0;
+    if (!st || W < 2 || (W & 1) || H < 1) { *gx = *gy = *ntx = *nty = 0; return 0; }
+    *ntx = ((W + st - 1) / st + 15) / 16;
+    *nty = ((H + st - 1) / st + 7) / 8;
+    *gx = *ntx * (st / 2);
+    *gy = *nty * st;
+    return *gx * *gy;
+}
 
 // The shading kernels (sgi_shade.cu) exist twice: sgi::exact is bit-identical to
 // the CPU restatement of the shaders, sgi::fast is the tolerance mode (fast
@@ -171,7 +184,7 @@ struct PPlan {
                                 dim3 block = dim3(0, 0, 0)); \
     /* persistent multi-view frame: bytes of one view's parameter block, filling it, the launch */ \
     int32_t persistent_view_bytes(); \
-    void persistent_fill_view(const PViewDesc& d, unsigned char* out); \
+    bool persistent_fill_view(const PViewDesc& d, unsigned char* out); /* false: a tensor map failed */ \
     size_t persistent_smem(int32_t max_visible); \
     /* variant 0: registers for 4 CTAs per SM, 1: for 2 */ \
     cudaError_t persistent_occupancy(int variant, size_t smem, int* blocks_per_sm); \

@@ -48,11 +48,15 @@ struct PView {
     DenoiseLaunch dl;                            // the final pass
     const float4* guide;
     uint2* pass_buf[SGI_MAX_DENOISE_PASSES];     // output of each denoise pass
+    // a-trous passes 1..3 from the TMA-staged lattice (atrous_staged_cta): CTA grid per pass (gx = 0: the
+    // direct per-pixel filter) and the tensor maps of guide and input reservoir
+    int32_t lat_gx[3], lat_gy[3], lat_ntx[3], lat_nty[3];
+    alignas(64) CUtensorMap amap[3][2];
 };
 
 int32_t persistent_view_bytes() { return (int32_t)((sizeof(PView) + 255) & ~(size_t)255); }
 
-void persistent_fill_view(const PViewDesc& d, unsigned char* out) {
+bool persistent_fill_view(const PViewDesc& d, unsigned char* out) {
     PView v;
     memset(&v, 0, sizeof(v));
     const sgi_config& cfg = d.cfg;
@@ -86,7 +90,20 @@ void persistent_fill_view(const PViewDesc& d, unsigned char* out) {
     l.guide = d.guide;
     v.guide = d.guide;
     for (int k = 0; k < SGI_MAX_DENOISE_PASSES; ++k) v.pass_buf[k] = d.pass_buf[k];
+    bool ok = true;
+    for (int pass = 1; pass <= 3 && pass < cfg.denoise_passes - 1; ++pass) {
+        int gx = 0, gy = 0, ntx = 0, nty = 0;
+        if (d.atrous_staged && atrous_lattice_grid(cfg.width, cfg.height, pass, &gx, &gy, &ntx, &nty) > 0) {
+            if (encode_atrous_maps(cfg.width, cfg.height, pass, d.guide, d.pass_buf[pass - 1], &v.amap[pass - 1][0],
+                                   &v.amap[pass - 1][1]) != cudaSuccess) {
+                ok = false;
+                gx = gy = 0;
+            }
+        }
+        v.lat_gx[pass - 1] = gx; v.lat_gy[pass - 1] = gy; v.lat_ntx[pass - 1] = ntx; v.lat_nty[pass - 1] = nty;
+    }
     memcpy(out, &v, sizeof(v));
+    return ok;
 }
 
 size_t persistent_smem(int32_t max_visible) {
@@ -142,7 +159,13 @@ __global__ void __launch_bounds__(256, kMinBlocks) persistent_frame_kernel(PPlan
     __shared__ uint32_t s_item;
     __shared__ int s_go;
     __shared__ sgi_tile_stage1 s_tile;
+    __shared__ LightConst s_lc;
+    __shared__ __align__(8) unsigned long long s_bar;   // the staged a-trous copies
     const int tid = threadIdx.x;
+    const uint32_t bar = smem_u32(&s_bar);
+    uint32_t stage_uses = 0;   // completed phases of s_bar
+    if (tid == 0) stage_barrier_init(bar);
+    __syncthreads();
     // thread 0 takes the next queue position while the CTA works on the current item
     unsigned next = tid == 0 ? atomicAdd(&plan.q->next, 1u) : 0u;
     for (;;) {
@@ -171,15 +194,35 @@ __global__ void __launch_bounds__(256, kMinBlocks) persistent_frame_kernel(PPlan
             } else if (level == kPCompact) {
                 compact_vpls<256>(pv.vpls, pv.entries, pv.flags, pv.num_vpls, pv.max_visible, pv.cv, pv.ce,
                                   pv.visible_index, pv.vpr, tid);
+            } else if (level >= kPAtrous && level - kPAtrous < 3 && level < kPAtrous + pv.passes - 2 &&
+                       pv.lat_gx[level - kPAtrous] > 0) {
+                // a-trous pass 1..3 from the staged lattice: kPBlocksPerItem lattice CTAs an item
+                const int k = level - kPAtrous, pass = k + 1;
+                const int n = pv.lat_gx[k] * pv.lat_gy[k];
+                const int c1 = min((index + 1) * kPBlocksPerItem, n);
+                const AtrousStageWait wt{*(volatile const long long*)plan.wait_ns, 0, plan.status};
+                for (int c = index * kPBlocksPerItem; c < c1; ++c) {
+                    const bool ok = atrous_staged_cta(&pv.amap[k][0], &pv.amap[k][1], pv.width, pv.height, 1 << pass,
+                                                      pv.lat_ntx[k], pv.lat_nty[k], c % pv.lat_gx[k], c / pv.lat_gx[k],
+                                                      pv.guide, pv.pass_buf[pass - 1], pv.pass_buf[pass], bar,
+                                                      stage_uses & 1u, wt);
+                    ++stage_uses;
+                    __syncthreads();   // this use's reads of the staged lattice before the next use's copies
+                    if (!ok) break;    // the status word says so; every CTA leaves at its next fetch
+                }
             } else {
                 // the pixel passes: kPBlocksPerItem consecutive 16x16 blocks (tiles) an item
+                if (level == kPDirect) {   // the light constants of this view, once per item
+                    light_const_fill(pv.dp, s_lc, tid, 256);
+                    __syncthreads();
+                }
                 const int b1 = min((index + 1) * kPBlocksPerItem, pv.blocks);
                 for (int b = index * kPBlocksPerItem; b < b1; ++b) {
                     const int bx = b % pv.tiles_x, by = b / pv.tiles_x;
                     const int x = bx * 16 + (tid & 15), y = by * 16 + (tid >> 4);
                     const bool inside = x < pv.width && y < pv.height;
                     if (level == kPDirect) {
-                        if (inside) deferred_pixel(pv.dp, x, y);
+                        if (inside) deferred_pixel(pv.dp, x, y, &s_lc);
                     } else if (level == kPTile) {
                         tile_mean(pv.width, pv.height, 16, bx, by, tid, pv.g, pv.cam, nullptr, &s_tile);
                         __syncthreads();

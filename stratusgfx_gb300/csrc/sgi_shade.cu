@@ -434,15 +434,15 @@ struct AtrousStageWait {
 
 SGI_D uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-SGI_D bool stage_wait(uint32_t bar, const AtrousStageWait& w) {
+SGI_D bool stage_wait(uint32_t bar, uint32_t parity, const AtrousStageWait& w) {
     uint32_t done = 0;
     const long long t0 = global_ns();
     for (;;) {
         asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0, 20000;\n"
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 20000;\n"
             " selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
-            : "r"(bar)
+            : "r"(bar), "r"(parity)
             : "memory");
         if (done) return true;
         if (global_ns() - t0 > w.wait_ns) {
@@ -452,42 +452,39 @@ SGI_D bool stage_wait(uint32_t bar, const AtrousStageWait& w) {
     }
 }
 
-__global__ void __launch_bounds__(256, 5) atrous_staged_kernel(const __grid_constant__ CUtensorMap gmap,
-                                                             const __grid_constant__ CUtensorMap rmap, int W,
-                                                             int H, int s, int ntx, int nty,
-                                                             const float4* __restrict__ guide,
-                                                             const uint2* __restrict__ res_in,
-                                                             uint2* __restrict__ res_out, AtrousStageWait wt) {
+// One CTA of the staged pass (256 threads): lattice patch (bx, by) of the grid
+// (ntx * s / 2, nty * s). `bar` is an initialised mbarrier of this CTA whose
+// phase `parity` the copies complete. Returns false (nothing written) when the
+// wait ran out. The stand-alone kernel below and the persistent multi-view
+// kernel (sgi_persistent.cuh) run it.
+SGI_D bool atrous_staged_cta(const CUtensorMap* gmap, const CUtensorMap* rmap, int W, int H, int s, int ntx, int nty,
+                             int bx, int by, const float4* __restrict__ guide, const uint2* __restrict__ res_in,
+                             uint2* __restrict__ res_out, uint32_t bar, uint32_t parity, const AtrousStageWait& wt) {
     __shared__ __align__(128) float4 sg[kLatHY][kLatHX][2];
     __shared__ __align__(128) uint2 sr[kLatHY][kLatHX][2];
-    __shared__ __align__(8) unsigned long long bar;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int tqx = blockIdx.x % ntx, rp = blockIdx.x / ntx;
-    const int tqy = blockIdx.y % nty, ry = blockIdx.y / nty;
+    const int tqx = bx % ntx, rp = bx / ntx;
+    const int tqy = by % nty, ry = by / nty;
     const int qx0 = tqx * kLatX, qy0 = tqy * kLatY, rx = 2 * rp;
-    const uint32_t b = smem_u32(&bar);
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    __syncthreads();
     if (tid == 0 && !wt.skip_copies) {
         constexpr uint32_t kBytes = sizeof(sg) + sizeof(sr);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b), "r"(kBytes) : "memory");
+        // the block's earlier accesses of sg / sr (a previous use) before the copies overwrite them
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(kBytes) : "memory");
         const int c1 = rp + (s >> 1) * (qx0 - 2), c2 = ry + s * (qy0 - 2);
         asm volatile(
             "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
             "[%5];\n" ::"r"(smem_u32(sg)),
-            "l"(reinterpret_cast<uint64_t>(&gmap)), "r"(0), "r"(c1), "r"(c2), "r"(b)
+            "l"(reinterpret_cast<uint64_t>(gmap)), "r"(0), "r"(c1), "r"(c2), "r"(bar)
             : "memory");
         asm volatile(
             "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
             "[%5];\n" ::"r"(smem_u32(sr)),
-            "l"(reinterpret_cast<uint64_t>(&rmap)), "r"(0), "r"(c1), "r"(c2), "r"(b)
+            "l"(reinterpret_cast<uint64_t>(rmap)), "r"(0), "r"(c1), "r"(c2), "r"(bar)
             : "memory");
     }
-    const bool ok = __syncthreads_and(stage_wait(b, wt));
-    if (!ok) return;
+    const bool ok = __syncthreads_and(stage_wait(bar, parity, wt));
+    if (!ok) return false;
     // lattice points outside the image: the clamped pixel's values (CTA-uniform test)
     if (qx0 < 2 || qy0 < 2 || rx + s * (qx0 + kLatHX - 3) >= W || ry + s * (qy0 + kLatHY - 3) >= H) {
         for (int e = tid; e < kLatHX * kLatHY; e += blockDim.x) {
@@ -502,18 +499,38 @@ __global__ void __launch_bounds__(256, 5) atrous_staged_kernel(const __grid_cons
                 sr[ey][ex][h] = ld_u2(res_in, row + cx);
             }
         }
-        __syncthreads();
     }
+    __syncthreads();   // fix-ups written; also orders this use's reads before the next use's copies
     const int lx = lane >> 1, h = lane & 1, ly = warp;
     const int x = rx + h + s * (qx0 + lx), y = ry + s * (qy0 + ly);
-    if (x >= W || y >= H) return;
-    const float4 gc = sg[ly + 2][lx + 2][h];
-    float rf0, rf1, rf2, rf3;
-    atrous_taps([&](int t) { return sg[ly + t % 5][lx + t / 5][h]; },
-                [&](int t) { return sr[ly + t % 5][lx + t / 5][h]; }, v3(gc.x, gc.y, gc.z), gc.w, rf0, rf1, rf2,
-                rf3);
-    const float den = gmax(kEps, rf3);
-    res_out[(size_t)y * W + x] = pack_h4(rf0 / den, rf1 / den, rf2 / den, 1.0f);
+    if (x < W && y < H) {
+        const float4 gc = sg[ly + 2][lx + 2][h];
+        float rf0, rf1, rf2, rf3;
+        atrous_taps([&](int t) { return sg[ly + t % 5][lx + t / 5][h]; },
+                    [&](int t) { return sr[ly + t % 5][lx + t / 5][h]; }, v3(gc.x, gc.y, gc.z), gc.w, rf0, rf1,
+                    rf2, rf3);
+        const float den = gmax(kEps, rf3);
+        res_out[(size_t)y * W + x] = pack_h4(rf0 / den, rf1 / den, rf2 / den, 1.0f);
+    }
+    return true;
+}
+
+SGI_D void stage_barrier_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+__global__ void __launch_bounds__(256, 5) atrous_staged_kernel(const __grid_constant__ CUtensorMap gmap,
+                                                             const __grid_constant__ CUtensorMap rmap, int W,
+                                                             int H, int s, int ntx, int nty,
+                                                             const float4* __restrict__ guide,
+                                                             const uint2* __restrict__ res_in,
+                                                             uint2* __restrict__ res_out, AtrousStageWait wt) {
+    __shared__ __align__(8) unsigned long long bar;
+    const uint32_t b = smem_u32(&bar);
+    if (threadIdx.x == 0) stage_barrier_init(b);
+    __syncthreads();
+    atrous_staged_cta(&gmap, &rmap, W, H, s, ntx, nty, blockIdx.x, blockIdx.y, guide, res_in, res_out, b, 0u, wt);
 }
 
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
@@ -530,34 +547,39 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
+// The two tensor maps of the staged pass at stride 2^pass over `guide` and `res_in` (pixel-pair views).
+static cudaError_t encode_atrous_maps(int W, int H, int pass, const float4* guide, const uint2* res_in,
+                                      CUtensorMap* gm, CUtensorMap* rm) {
+    const int st = 1 << pass;
+    auto encode = tensor_map_encoder();
+    if (!encode) return cudaErrorNotSupported;
+    const cuuint64_t dim[3] = {8, (cuuint64_t)W / 2, (cuuint64_t)H};
+    const cuuint32_t box[3] = {8, (cuuint32_t)(kLatHX * st / 2), (cuuint32_t)(kLatHY * st)};
+    const cuuint32_t stride[3] = {1, (cuuint32_t)(st / 2), (cuuint32_t)st};
+    const cuuint64_t gstr[2] = {32, (cuuint64_t)W * 16};
+    const cuuint64_t rstr[2] = {16, (cuuint64_t)W * 8};
+    const bool ok = encode(gm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)guide, dim, gstr, box, stride,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS &&
+                    encode(rm, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, (void*)res_in, dim, rstr, box, stride,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    return ok ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 cudaError_t launch_atrous_staged(int32_t W, int32_t H, int32_t pass, const float4* guide, const uint2* res_in,
                                  uint2* res_out, long long wait_ns, int32_t skip_copies, int32_t* status,
                                  cudaStream_t s) {
     const int st = pass >= 1 && pass <= 3 ? 1 << pass : 0;
     if (!st || W < 2 || (W & 1) || H < 1 || ((uintptr_t)guide & 15) || ((uintptr_t)res_in & 15) || !status)
         return cudaErrorNotSupported;
-    auto encode = tensor_map_encoder();
-    if (!encode) return cudaErrorNotSupported;
-    // pixel-pair views {8 values, W / 2 pairs, H rows}; boxes {8, 20 pairs at stride s / 2, 12 rows at stride s}
-    const cuuint64_t dim[3] = {8, (cuuint64_t)W / 2, (cuuint64_t)H};
-    const cuuint32_t box[3] = {8, (cuuint32_t)(kLatHX * st / 2), (cuuint32_t)(kLatHY * st)};
-    const cuuint32_t stride[3] = {1, (cuuint32_t)(st / 2), (cuuint32_t)st};
-    const cuuint64_t gstr[2] = {32, (cuuint64_t)W * 16};
-    const cuuint64_t rstr[2] = {16, (cuuint64_t)W * 8};
     CUtensorMap gm, rm;
-    if (encode(&gm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)guide, dim, gstr, box, stride,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return cudaErrorInvalidValue;
-    if (encode(&rm, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, (void*)res_in, dim, rstr, box, stride,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return cudaErrorInvalidValue;
-    const int ntx = ((W + st - 1) / st + kLatX - 1) / kLatX;
-    const int nty = ((H + st - 1) / st + kLatY - 1) / kLatY;
+    const cudaError_t e = encode_atrous_maps(W, H, pass, guide, res_in, &gm, &rm);
+    if (e != cudaSuccess) return e;
+    int gx, gy, ntx, nty;
+    atrous_lattice_grid(W, H, pass, &gx, &gy, &ntx, &nty);
     const AtrousStageWait wt{wait_ns > 0 ? wait_ns : 200000000LL, skip_copies, status};
-    atrous_staged_kernel<<<dim3(ntx * (st / 2), nty * st), 256, 0, s>>>(gm, rm, W, H, st, ntx, nty, guide, res_in,
-                                                                        res_out, wt);
+    atrous_staged_kernel<<<dim3(gx, gy), 256, 0, s>>>(gm, rm, W, H, st, ntx, nty, guide, res_in, res_out, wt);
     return cudaGetLastError();
 }
 

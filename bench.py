@@ -159,7 +159,7 @@ def kernel_bytes(w) -> dict:
 
 
 # kernel (group) -> index into sgi_get_pass_times with the denoise split, and the CUDA kernels it holds
-KERNELS = {"vpl_cull": (0, "vpl_vis_flags_kernel + vpl_compact_kernel"),
+KERNELS = {"vpl_cull": (0, "vpl_cull_kernel (visibility flags and, in its last block, the compaction)"),
            "deferred_pbr_csm": (1, "deferred_pbr_csm_kernel"),
            "tile_cull": (2, "tile_stage1_kernel + tile_cull_kernel"),
            "vpl_gather": (3, "vpl_gather_kernel (gather + denoise pass 0 merge + guide)"),

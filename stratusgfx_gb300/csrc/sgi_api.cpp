@@ -105,7 +105,7 @@ void free_all(sgi_ctx* c) {
     void* ptrs[] = {c->vpls, c->entries, c->points, c->shadow_points, c->shadow_entries, c->taa_hist[0],
                     c->taa_hist[1], c->flags, c->cv, c->ce, c->visible_index, c->stage1, c->lists,
                     c->vpr, c->reservoir, c->ping[0], c->ping[1], c->merged, c->direct, c->guide, c->gi_hist[0], c->gi_hist[1],
-                    c->hist_depth[0], c->hist_depth[1], c->dev_status};
+                    c->hist_depth[0], c->hist_depth[1], c->dev_status, c->cull_finished};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto* p : c->pass_bufs) if (p) cudaFree(p);
     void* nnp[] = {c->nn_feat, c->nn_prev};
@@ -229,6 +229,7 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     chk(dalloc(&c->hist_depth[0], P));
     chk(dalloc(&c->hist_depth[1], P));
     chk(dalloc(&c->dev_status, 1));
+    chk(dalloc(&c->cull_finished, 1));
     if (cfg->debug_keep_passes)
         for (int k = 0; k < cfg->denoise_passes; ++k) chk(dalloc(&c->pass_bufs[k], P));
     for (auto& ev : c->ev) chk(cudaEventCreate(&ev));
@@ -238,6 +239,7 @@ sgi_status sgi_create(const sgi_config* cfg, sgi_ctx** out) {
     chk(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
     if (e == cudaSuccess) chk(cudaMemset(c->visible_index, 0, sizeof(int32_t) * (1 + (size_t)cfg->max_vpls)));
     if (e == cudaSuccess) chk(cudaMemset(c->dev_status, 0, sizeof(int32_t)));
+    if (e == cudaSuccess) chk(cudaMemset(c->cull_finished, 0, sizeof(unsigned)));
     if (e == cudaSuccess) chk(cudaMemset(c->gi_hist[0], 0, P * sizeof(uint2)));
     if (e == cudaSuccess) chk(cudaMemset(c->gi_hist[1], 0, P * sizeof(uint2)));
     if (e == cudaSuccess) chk(cudaMemset(c->hist_depth[0], 0, P * sizeof(uint16_t)));
@@ -306,10 +308,11 @@ sgi_status sgi_cull_vpls(sgi_ctx* ctx, void* stream) {
     if (ctx->num_vpls == 0) {
         SGI_CUDA(ctx, cudaMemsetAsync(ctx->visible_index, 0, sizeof(int32_t), s), "clear visible count");
     } else {
-        SGI_CUDA(ctx, sgi::launch_vis_flags(ctx->vpls, ctx->num_vpls, ctx->csm, ctx->flags, s), "vpl_vis_flags");
-        SGI_CUDA(ctx, sgi::launch_compact(ctx->vpls, ctx->entries, ctx->flags, ctx->num_vpls, ctx->cfg.max_visible,
-                                          ctx->cv, ctx->ce, ctx->visible_index, ctx->vpr, s), "vpl_compact");
-        ctx->launches += 2;
+        SGI_CUDA(ctx, sgi::launch_vpl_cull(ctx->vpls, ctx->entries, ctx->num_vpls, ctx->csm, ctx->flags,
+                                           ctx->cfg.max_visible, ctx->cv, ctx->ce, ctx->visible_index, ctx->vpr,
+                                           ctx->cull_finished, s),
+                 "vpl_cull");
+        ctx->launches += 1;
         if (ctx->coloring) {
             SGI_CUDA(ctx, sgi::launch_vpl_color(ctx->cv, ctx->ce, ctx->visible_index, ctx->cfg.max_visible,
                                                 ctx->cubes, ctx->diffuse, ctx->csm, s), "vpl_color");

@@ -67,6 +67,7 @@ struct sgi_ctx {
     long long wait_ns = 0;
     int32_t skip_copies = 0;
     int32_t* dev_status = nullptr;
+    unsigned* cull_finished = nullptr;   // finished-block count of the one-launch VPL cull (zero between launches)
 
     // timing
     bool timing = false;

@@ -35,7 +35,9 @@ SGI_D uint8_t vpl_visible(const sgi_vpl* __restrict__ vpls, int i, const sgi_csm
 // across chunks of NT flags. Replaces the 8-thread atomicAdd loop of
 // viscull_vpls.cs:85-98 (whose order is nondeterministic). With vpr given, the
 // (position, radius) of each kept VPL is also written there for the tile cull.
-template <int NT>
+// kCoherent: the flags were written by other blocks of the same launch, so they
+// are read through L2 (ld.global.cg), not a read-only or L1 path.
+template <int NT, bool kCoherent = false>
 SGI_D void compact_vpls(const sgi_vpl* __restrict__ vpls, const sgi_atlas_entry* __restrict__ entries,
                         const uint8_t* __restrict__ flags, int n, int cap, sgi_vpl* __restrict__ cv,
                         sgi_atlas_entry* __restrict__ ce, int32_t* __restrict__ visible_index,
@@ -48,7 +50,7 @@ SGI_D void compact_vpls(const sgi_vpl* __restrict__ vpls, const sgi_atlas_entry*
     int base = 0;
     for (int start = 0; start < n; start += NT) {
         const int i = start + tid;
-        const bool f = i < n && flags[i] != 0;
+        const bool f = i < n && (kCoherent ? __ldcg(flags + i) : flags[i]) != 0;
         const unsigned m = __ballot_sync(0xffffffffu, f);
         const int within = __popc(m & ((1u << lane) - 1u));
         if (lane == 0) warp_count[warp] = __popc(m);

@@ -69,6 +69,11 @@ cudaError_t launch_vpl_color(sgi_vpl* cv, const sgi_atlas_entry* ce, const int32
                              const sgi_cube_atlas& cubes, const sgi_diffuse_atlas& diffuse, const sgi_csm& csm,
                              cudaStream_t s);
 // vpr (may be null): (position, radius) of the kept VPLs for the tile cull
+// visibility flags and compaction in one launch (the last block compacts); `finished` is a zeroed device
+// counter owned by the caller, zero again after the launch
+cudaError_t launch_vpl_cull(const sgi_vpl* vpls, const sgi_atlas_entry* entries, int32_t n, const sgi_csm& csm,
+                            uint8_t* flags, int32_t cap, sgi_vpl* cv, sgi_atlas_entry* ce, int32_t* visible_index,
+                            float4* vpr, unsigned* finished, cudaStream_t s);
 cudaError_t launch_compact(const sgi_vpl* vpls, const sgi_atlas_entry* entries, const uint8_t* flags, int32_t n,
                            int32_t cap, sgi_vpl* cv, sgi_atlas_entry* ce, int32_t* visible_index, float4* vpr,
                            cudaStream_t s);

@@ -160,6 +160,39 @@ __global__ void __launch_bounds__(1024) vpl_compact_kernel(const sgi_vpl* __rest
     compact_vpls<1024>(vpls, entries, flags, n, cap, cv, ce, visible_index, vpr, threadIdx.x);
 }
 
+// Both steps in one launch: every block flags its 256 VPLs, and the last block
+// to finish (an atomic count of finished blocks, after a fence) compacts all
+// of them in index order and returns the count to zero for the next launch.
+// No block waits for another, and the compaction is the one above, so the
+// result is that of the two kernels.
+__global__ void __launch_bounds__(256) vpl_cull_kernel(const sgi_vpl* __restrict__ vpls,
+                                                       const sgi_atlas_entry* __restrict__ entries, int n,
+                                                       sgi_csm csm, uint8_t* __restrict__ flags, int cap,
+                                                       sgi_vpl* __restrict__ cv, sgi_atlas_entry* __restrict__ ce,
+                                                       int32_t* __restrict__ visible_index, float4* __restrict__ vpr,
+                                                       unsigned* __restrict__ finished) {
+    __shared__ bool last;
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i < n) flags[i] = vpl_visible(vpls, i, csm);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(finished, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    compact_vpls<256, true>(vpls, entries, flags, n, cap, cv, ce, visible_index, vpr, threadIdx.x);
+    if (threadIdx.x == 0) *finished = 0u;
+}
+
+cudaError_t launch_vpl_cull(const sgi_vpl* vpls, const sgi_atlas_entry* entries, int32_t n, const sgi_csm& csm,
+                            uint8_t* flags, int32_t cap, sgi_vpl* cv, sgi_atlas_entry* ce, int32_t* visible_index,
+                            float4* vpr, unsigned* finished, cudaStream_t s) {
+    if (n <= 0 || !finished) return cudaErrorInvalidValue;
+    vpl_cull_kernel<<<(n + 255) / 256, 256, 0, s>>>(vpls, entries, n, csm, flags, cap, cv, ce, visible_index, vpr,
+                                                    finished);
+    return cudaGetLastError();
+}
+
 // Flag array of sgi_cull_vpls_noalloc (one byte per VPL). vpl_vis_flags_kernel
 // writes every flag below the call's VPL count before vpl_compact_kernel reads
 // it, so the array is never cleared.

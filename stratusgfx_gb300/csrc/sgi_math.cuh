@@ -335,6 +335,29 @@ SGI_D V3 spec_brdf(float NdotV, float NdotL, float NdotH, float LdotH, float r, 
     float vis = vis_smith_ggx(NdotV, NdotL, r);
     return (ndf * vis) * fres;
 }
+// The view-side factors of spec_brdf, which depend only on the pixel: N.V,
+// a^2 and the square root of Visibility_G_SmithGGX's view term. spec_brdf_v
+// then evaluates the remaining operations of spec_brdf in their order, so a
+// pixel's lights or samples share the factors with the same results.
+struct SpecView {
+    float NdotV, a2, sqrtV;
+};
+SGI_D SpecView spec_view(V3 N, V3 V, float r) {
+    SpecView s;
+    s.NdotV = saturate(dot(N, V));
+    s.a2 = r * r;
+    s.sqrtV = sqrtf((s.NdotV - s.a2 * s.NdotV) * s.NdotV + s.a2);
+    return s;
+}
+SGI_D V3 spec_brdf_v(const SpecView& sv, float NdotL, float NdotH, float LdotH, V3 f0) {
+    float f = (NdotH * sv.a2 - NdotH) * NdotH + 1.0f;
+    float ndf = sv.a2 / gmax(kPi * f * f, kEps);
+    V3 fres = fr_fresnel(LdotH, f0);
+    float ggxv = NdotL * sv.sqrtV;
+    float ggxl = sv.NdotV * sqrtf((NdotL - sv.a2 * NdotL) * NdotL + sv.a2);
+    float vis = 0.5f / gmax(ggxv + ggxl, kEps);
+    return (ndf * vis) * fres;
+}
 // RemapRoughness, pbr2.glsl:139-144
 SGI_D float remap_roughness(float r, const ShadeParams& sp) {
     if (sp.perceptual) r = r * r;
@@ -379,25 +402,28 @@ SGI_D V3 lighting_burley(V3 lightColor, V3 lightDir, V3 V, V3 N, V3 baseColor, f
     return atten * (ambient + shadowFactor * apply_fog(finalB, viewDist, fogIntensity, sp));
 }
 // lighting_burley split like vpl_pixel / vpl_lighting2_sample: the part that
-// depends only on the pixel (BRDF_Base with unit divisors, and the fog factor
-// of the view distance) once per pixel, the rest per light; the operations and
-// their order per light are those of lighting_burley.
+// depends only on the pixel (BRDF_Base with unit divisors, the fog factor of
+// the view distance and the view-side specular factors) once per pixel, the
+// rest per light; the operations and their order per light are those of
+// lighting_burley. N and V are the pixel's normal and view direction.
 struct BurleyPixel {
     V3 dc, f0;
     float rr, fogF;
+    SpecView sv;
 };
-SGI_D BurleyPixel burley_pixel(V3 baseColor, V3 baseRefl, float roughness, float metallic, float viewDist,
-                               const ShadeParams& sp) {
+SGI_D BurleyPixel burley_pixel(V3 baseColor, V3 baseRefl, float roughness, float metallic, float viewDist, V3 N,
+                               V3 V, const ShadeParams& sp) {
     BurleyPixel b;
     brdf_base(baseColor, baseRefl, roughness, metallic, v3s(1.0f), v3s(1.0f), sp, b.rr, b.dc, b.f0);
     b.fogF = expf_ieee(-sp.fog_density * viewDist);
+    b.sv = spec_view(N, V, b.rr);
     return b;
 }
 SGI_D V3 lighting_burley_px(const BurleyPixel& b, V3 lightColor, V3 lightDir, V3 V, V3 N, float fogIntensity,
                             float ao, float shadowFactor, float atten, float ambientIntensity, const ShadeParams& sp) {
     float NdotV, NdotL, NdotH, LdotH;
-    brdf_dots(V, lightDir, N, NdotV, NdotL, NdotH, LdotH);
-    V3 Fr = spec_brdf(NdotV, NdotL, NdotH, LdotH, b.rr, b.f0);
+    brdf_dots(V, lightDir, N, NdotV, NdotL, NdotH, LdotH);   // NdotV is b.sv.NdotV
+    V3 Fr = spec_brdf_v(b.sv, NdotL, NdotH, LdotH, b.f0);
     V3 Fd = b.dc * fd_burley(NdotV, NdotL, LdotH, b.rr);
     V3 brdf = (Fd + Fr) * NdotL;
     V3 ambient = brdf * ao * lightColor * ambientIntensity;
@@ -414,9 +440,9 @@ SGI_D V3 lighting_burley_pxl(const BurleyPixel& b, V3 lightColor, V3 lightDir, f
                              const ShadeParams& sp) {
     const V3 L = lightDir * (1.0f / len);
     const V3 H = normalize(V + L);
-    const float NdotV = saturate(dot(N, V)), NdotL = saturate(dot(N, L));
+    const float NdotV = b.sv.NdotV, NdotL = saturate(dot(N, L));
     const float NdotH = saturate(dot(N, H)), LdotH = saturate(dot(L, H));
-    V3 Fr = spec_brdf(NdotV, NdotL, NdotH, LdotH, b.rr, b.f0);
+    V3 Fr = spec_brdf_v(b.sv, NdotL, NdotH, LdotH, b.f0);
     V3 Fd = b.dc * fd_burley(NdotV, NdotL, LdotH, b.rr);
     V3 brdf = (Fd + Fr) * NdotL;
     V3 ambient = brdf * ao * lightColor * ambientIntensity;
@@ -447,6 +473,7 @@ SGI_D float vpl_atten(V3 lightDir, float radius) {
 struct VplPixel {
     V3 fragPos, N, V, dc, f0, fogAdd;
     float rr, fogF, ao;
+    SpecView sv;
 };
 SGI_D VplPixel vpl_pixel(V3 fragPos, V3 baseColor, V3 N, V3 V, float viewDist, float roughness, float metallic,
                          float ao, V3 baseRefl, const ShadeParams& sp) {
@@ -454,6 +481,7 @@ SGI_D VplPixel vpl_pixel(V3 fragPos, V3 baseColor, V3 N, V3 V, float viewDist, f
     q.fragPos = fragPos; q.N = N; q.V = V; q.ao = ao;
     const V3 specMult = 1.0f / (baseColor + kEps);
     brdf_base(baseColor, baseRefl, roughness, metallic, baseColor, specMult, sp, q.rr, q.dc, q.f0);
+    q.sv = spec_view(N, V, q.rr);
     // applyFog(color, viewDist, 0) = color * f + fc * (1 - f), fc = fogColor * 0
     q.fogF = expf_ieee(-sp.fog_density * viewDist);
     const V3 fc = v3(sp.fog_color[0], sp.fog_color[1], sp.fog_color[2]) * 0.0f;
@@ -470,16 +498,15 @@ SGI_D V3 vpl_lighting2_sample(const VplPixel& q, V3 specPos, V3 diffPos, V3 ligh
     if (!(diffLen >= 0.0f)) diffLen = length(diffDir);
     float specAtten = vpl_atten_len(specLen, radius);
     float diffAtten = vpl_atten_len(diffLen, radius);
-    float NdotV, NdotL, NdotH, LdotH;
+    float NdotL, NdotH, LdotH;
     {   // brdf_dots(q.V, specDir, ...) with normalize(specDir) = specDir * (1 / |specDir|)
         const V3 L = specDir * (1.0f / specLen);
         const V3 H = normalize(q.V + L);
-        NdotV = saturate(dot(q.N, q.V));
         NdotL = saturate(dot(q.N, L));
         NdotH = saturate(dot(q.N, H));
         LdotH = saturate(dot(L, H));
     }
-    V3 Fr = spec_brdf(NdotV, NdotL, NdotH, LdotH, q.rr, q.f0) * NdotL;
+    V3 Fr = spec_brdf_v(q.sv, NdotL, NdotH, LdotH, q.f0) * NdotL;
     NdotL = saturate(dot(q.N, diffDir * (1.0f / diffLen)));   // brdf_dots(q.V, diffDir, ...): only N.L is used
     V3 Fd = (q.dc * (1.0f / kPi)) * NdotL;
     V3 bs = specAtten * Fr;

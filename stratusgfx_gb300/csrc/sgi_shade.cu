@@ -715,7 +715,7 @@ SGI_D void deferred_pixel(const DeferredParams& p, int x, int y, const LightCons
     const uint32_t br = __ldg(p.g.base_reflectivity + i);
     const float reflR = float(br & 0xffu) / 255.0f, reflG = float(br >> 8) / 255.0f;
     const V3 emissive = v3(albedoA, reflG, rmeB);
-    const BurleyPixel bp = burley_pixel(baseColor, v3s(reflR), roughness, metallic, viewDist, sp);
+    const BurleyPixel bp = burley_pixel(baseColor, v3s(reflR), roughness, metallic, viewDist, normal, viewDir, sp);
     V3 color = v3s(0.0f);
     for (int l = 0; l < p.num_points; ++l) {
         const float4* rec = reinterpret_cast<const float4*>(p.points + l);

@@ -68,6 +68,22 @@ SGI_D float xdiv(float a, float b) { return __fdiv_rn(a, b); }
 SGI_D float xsqrt(float a) { return __fsqrt_rn(a); }
 SGI_D float xmixf(float x, float y, float a) { return __fmaf_rn(y, a, xmul(x, xsub(1.0f, a))); }
 
+// expf_ieee's Taylor polynomial of the reduced argument r, in Horner form.
+SGI_D float exp_poly(float r) {
+    float p = __fmaf_rn(r, 1.0f / 5040.0f, 1.0f / 720.0f);
+    p = __fmaf_rn(p, r, 1.0f / 120.0f);
+    p = __fmaf_rn(p, r, 1.0f / 24.0f);
+    p = __fmaf_rn(p, r, 1.0f / 6.0f);
+    p = __fmaf_rn(p, r, 0.5f);
+    p = __fmaf_rn(p, r, 1.0f);
+    return __fmaf_rn(p, r, 1.0f);
+}
+// |x| < kExpNoReduce: x * log2(e) + 0.5 rounds into (0, 1), so k = 0, the
+// reduction returns r = x - 0 - 0 = x (signed zeros included) and the scaling
+// multiplies by 2^0 = 1: the result is exp_poly(x) alone. The bound is below
+// ln(2) / 2 = 0.3466 with room for the roundings of the product and the sum.
+constexpr float kExpNoReduce = 0.34f;
+
 // expf_ieee's arithmetic (below) with every operation explicitly rounded: the
 // same value in every build.
 SGI_D float expf_exact(float x) {
@@ -77,13 +93,7 @@ SGI_D float expf_exact(float x) {
     float kf = floorf(xadd(xmul(x, 1.44269502162933349609375f), 0.5f));
     int k = (int)kf;
     float r = xsub(xsub(x, xmul(kf, 0.693145751953125f)), xmul(kf, 1.428606765330187045037746429443359375e-06f));
-    float p = __fmaf_rn(r, 1.0f / 5040.0f, 1.0f / 720.0f);
-    p = __fmaf_rn(p, r, 1.0f / 120.0f);
-    p = __fmaf_rn(p, r, 1.0f / 24.0f);
-    p = __fmaf_rn(p, r, 1.0f / 6.0f);
-    p = __fmaf_rn(p, r, 0.5f);
-    p = __fmaf_rn(p, r, 1.0f);
-    p = __fmaf_rn(p, r, 1.0f);
+    float p = exp_poly(r);
     if (k > 127) { p = xmul(p, 1.7014118346046923e+38f); k -= 127; }
     if (k < -126) { p = xmul(p, 1.1754943508222875e-38f); k += 126; }
     return xmul(p, __int_as_float((k + 127) << 23));
@@ -95,8 +105,12 @@ SGI_D float expf_exact(float x) {
 // build of the shading kernels (SGI_FAST_MATH) it is the hardware exponential.
 #if SGI_FAST_MATH
 SGI_D float expf_ieee(float x) { return __expf(x); }
+SGI_D float expf_ieee_near0(float x) { return __expf(x); }
 #else
 SGI_D float expf_ieee(float x) { return expf_exact(x); }
+// expf_ieee for arguments that are mostly near 0 (the a-trous depth weight):
+// below kExpNoReduce the polynomial alone, the same value.
+SGI_D float expf_ieee_near0(float x) { return fabsf(x) < kExpNoReduce ? exp_poly(x) : expf_exact(x); }
 #endif
 SGI_D float pow5(float x) { float x2 = x * x; float x4 = x2 * x2; return x4 * x; }
 SGI_D float pow128(float x) {
@@ -149,20 +163,25 @@ SGI_D float exp_reduce(float x, float& kf) {
     kf = floorf(x * 1.44269502162933349609375f + 0.5f);
     return (x - kf * 0.693145751953125f) - kf * 1.428606765330187045037746429443359375e-06f;
 }
-SGI_D float2 expf_ieee2(float2 x) {
-#if SGI_FAST_MATH
-    return make_float2(__expf(x.x), __expf(x.y));
-#endif
-    if (!(exp_packable(x.x) && exp_packable(x.y))) return make_float2(expf_ieee(x.x), expf_ieee(x.y));
-    float2 kf;
-    const float2 r = make_float2(exp_reduce(x.x, kf.x), exp_reduce(x.y, kf.y));
+// exp_poly in both lanes.
+SGI_D float2 exp_poly2(float2 r) {
     float2 p = fma2(r, f2s(1.0f / 5040.0f), f2s(1.0f / 720.0f));
     p = fma2(p, r, f2s(1.0f / 120.0f));
     p = fma2(p, r, f2s(1.0f / 24.0f));
     p = fma2(p, r, f2s(1.0f / 6.0f));
     p = fma2(p, r, f2s(0.5f));
     p = fma2(p, r, f2s(1.0f));
-    p = fma2(p, r, f2s(1.0f));
+    return fma2(p, r, f2s(1.0f));
+}
+SGI_D float2 expf_ieee2(float2 x) {
+#if SGI_FAST_MATH
+    return make_float2(__expf(x.x), __expf(x.y));
+#endif
+    if (!(exp_packable(x.x) && exp_packable(x.y))) return make_float2(expf_ieee(x.x), expf_ieee(x.y));
+    if (fabsf(x.x) < kExpNoReduce && fabsf(x.y) < kExpNoReduce) return exp_poly2(x);   // k = 0 in both lanes
+    float2 kf;
+    const float2 r = make_float2(exp_reduce(x.x, kf.x), exp_reduce(x.y, kf.y));
+    const float2 p = exp_poly2(r);
     const int k0 = (int)kf.x, k1 = (int)kf.y;   // in [-126, 127]
     return mul2(p, make_float2(__int_as_float((k0 + 127) << 23), __int_as_float((k1 + 127) << 23)));
 }
@@ -239,7 +258,7 @@ SGI_D V3 world_from_depth(float u, float v, float depth, const float* inv_pv) {
 // (filterInput, vpl_pbr_gi_denoise.fs:142-190, sigmaZ = 1):
 // pow(max(0, cn . nq), 128) * exp(-|cd - zq|).
 SGI_D float atrous_weight(V3 cn, float cd, float4 gq) {
-    const float wz = expf_ieee(-gabs(cd - gq.w));
+    const float wz = expf_ieee_near0(-gabs(cd - gq.w));
     const float wn = pow128(gmax(0.0f, dot(cn, v3(gq.x, gq.y, gq.z))));
     return wn * wz;
 }

@@ -51,7 +51,7 @@ struct PView {
     // a-trous passes 1..3 from the TMA-staged lattice (atrous_staged_cta): CTA grid per pass (gx = 0: the
     // direct per-pixel filter) and the tensor maps of guide and input reservoir
     int32_t lat_gx[3], lat_gy[3], lat_ntx[3], lat_nty[3];
-    alignas(64) CUtensorMap amap[3][2];
+    CUtensorMap amap[3][2];                      // CUtensorMap is 128-byte aligned
 };
 
 int32_t persistent_view_bytes() { return (int32_t)((sizeof(PView) + 255) & ~(size_t)255); }

@@ -123,16 +123,21 @@ __global__ void lane_selftest_kernel(int n, unsigned* counts, float* first) {
         w[0] = __fmaf_rn(f0, a0, c0); w[1] = __fmaf_rn(f1, a1, c1);
         rec.check(11, g, w, 2, in, 4);
     }
-    // 6: exp over its whole range: normal, tiny, underflowing and special arguments
+    // 6: exp over its whole range: normal, tiny, underflowing and special arguments,
+    // and arguments around the bound below which the range reduction is skipped
+    // (packed, and the scalar expf_ieee_near0, against the full scalar path)
     {
         float x[2];
         for (int l = 0; l < 2; ++l) {
             const int c = (int)(d.unit() * 8.0f);
             x[l] = c == 0 ? -d.range(80.0f, 110.0f) : c == 1 ? d.range(80.0f, 90.0f) : c == 2 ? d.bits() * 1e-30f
-                 : c == 3 ? (d.unit() < 0.5f ? 0.0f : -0.0f) : c == 4 ? -d.range(86.0f, 88.0f) : -d.range(0.0f, 8.0f);
+                 : c == 3 ? (d.unit() < 0.5f ? 0.0f : -0.0f) : c == 4 ? -d.range(86.0f, 88.0f)
+                 : c == 5 ? d.range(-0.4f, 0.4f) : -d.range(0.0f, 8.0f);
         }
         put2(g, expf_ieee2(make_float2(x[0], x[1])));
-        w[0] = expf_ieee(x[0]); w[1] = expf_ieee(x[1]);
+        w[0] = expf_exact(x[0]); w[1] = expf_exact(x[1]);
+        rec.check(6, g, w, 2, x, 2);
+        g[0] = expf_ieee_near0(x[0]); g[1] = expf_ieee_near0(x[1]);
         rec.check(6, g, w, 2, x, 2);
     }
     // 7: x^128 for x in [0, 1.001], small values included

@@ -5,6 +5,11 @@ UNORM8 decode (device unorm8, csrc/sgi_math.cuh): for every byte b the
 product q = RN(b * RN(1/255)) followed by q' = RN(RN(b - q*255) * RN(1/255) + q)
 (two fused multiply-adds) equals RN(b / 255), the quotient the oracle computes.
 Checked exhaustively here in exact rational arithmetic.
+
+Exponential without range reduction (device expf_exact / expf_ieee2): for
+|x| < 0.34 the Cody & Waite step gives k = floor(RN(RN(x * log2 e) + 0.5)) = 0,
+the reduced argument (x - 0 * ln2_hi) - 0 * ln2_lo is x itself and the final
+scaling multiplies by 2^0, so the result is the Taylor polynomial of x alone.
 """
 from fractions import Fraction
 
@@ -41,3 +46,34 @@ def test_difference_magnitude_is_symmetric():
     # x - y*c == x + y*(-c): the negated constant's product is the negated product
     c = np.float32(0.693145751953125)
     assert np.array_equal((a - b * c).view(np.uint32), (a + b * (-c)).view(np.uint32))
+
+
+LOG2E = np.float32(1.44269502162933349609375)
+LN2_HI = np.float32(0.693145751953125)
+LN2_LO = np.float32(1.428606765330187045037746429443359375e-06)
+NO_REDUCE = np.float32(0.34)
+
+
+def _k(x):
+    return np.floor((x * LOG2E).astype(np.float32) + np.float32(0.5)).astype(np.float32)
+
+
+def test_exp_needs_no_reduction_below_the_bound():
+    # k(x) is monotone in x (a product with a positive constant, a sum and floor, each rounded
+    # monotonically), so k = 0 at the two extreme arguments below the bound gives k = 0 between them
+    top = np.nextafter(NO_REDUCE, np.float32(0))
+    ends = np.array([top, -top], np.float32)
+    assert np.all(_k(ends) == 0)
+    assert NO_REDUCE < np.float32(np.log(2.0) / 2.0)
+    # the reduced argument is x, bit for bit (signed zeros and subnormals included)
+    rng = np.random.default_rng(5)
+    x = (rng.uniform(-1, 1, 1_000_000) * NO_REDUCE).astype(np.float32)
+    x = np.concatenate([x, ends, np.array([0.0, -0.0, 1e-45, -1e-45, 2e-38, -2e-38], np.float32)])
+    x = x[np.abs(x) < NO_REDUCE]
+    kf = _k(x)
+    assert np.all(kf == 0) and not np.any(np.signbit(kf))
+    r = ((x - kf * LN2_HI).astype(np.float32) - kf * LN2_LO).astype(np.float32)
+    assert np.array_equal(r.view(np.uint32), x.view(np.uint32))
+    # and the scaling by 2^(k + 127 - 127) is a multiplication by 1
+    p = rng.uniform(0.5, 2.0, 1000).astype(np.float32)
+    assert np.array_equal((p * np.float32(1.0)).view(np.uint32), p.view(np.uint32))

@@ -103,14 +103,15 @@ SGI_D float expf_exact(float x) {
 // 15-bit head (exact products for |k| < 512) and a tail, exp(r) by its Taylor
 // series to r^7 in Horner form, then exact scaling by 2^k. In the tolerance
 // build of the shading kernels (SGI_FAST_MATH) it is the hardware exponential.
+// expf_exact for arguments that are mostly near 0 (depth weights): below
+// kExpNoReduce the polynomial alone, the same value.
+SGI_D float expf_exact_near0(float x) { return fabsf(x) < kExpNoReduce ? exp_poly(x) : expf_exact(x); }
 #if SGI_FAST_MATH
 SGI_D float expf_ieee(float x) { return __expf(x); }
 SGI_D float expf_ieee_near0(float x) { return __expf(x); }
 #else
 SGI_D float expf_ieee(float x) { return expf_exact(x); }
-// expf_ieee for arguments that are mostly near 0 (the a-trous depth weight):
-// below kExpNoReduce the polynomial alone, the same value.
-SGI_D float expf_ieee_near0(float x) { return fabsf(x) < kExpNoReduce ? exp_poly(x) : expf_exact(x); }
+SGI_D float expf_ieee_near0(float x) { return expf_exact_near0(x); }
 #endif
 SGI_D float pow5(float x) { float x2 = x * x; float x4 = x2 * x2; return x4 * x; }
 SGI_D float pow128(float x) {

@@ -633,7 +633,7 @@ SGI_D void denoise_final_pixel(const DenoiseLaunch& d, int x, int y) {
     const float prevId = __ldg(d.prev_id + (size_t)nearest_index(pv, H) * W + nearest_index(pu, W));
     // the temporal decision: similarity against 0.99, exact in both builds
     const float wn = gmax(0.0f, xdot(centerNormal, prevCenterNormal));
-    const float wz = expf_exact(-gabs(xsub(centerDepth, prevCenterDepth)));
+    const float wz = expf_exact_near0(-gabs(xsub(centerDepth, prevCenterDepth)));
     const float wid = currId != prevId ? 0.0f : 1.0f;
     float similarity = xmul(xmul(wn, wz), wid);
     if (similarity < 0.99f) { similarity = 0.0f; accumMultiplier = 0.0f; }

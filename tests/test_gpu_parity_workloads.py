@@ -5,8 +5,9 @@ cubes, 4 point lights, 4x2048^2 CSM, <= 64 VPLs per 16x16 tile, K = 8, 5
 denoise passes) renders two consecutive frames on one context, the second
 reading the first's history; the visible-VPL list, every per-tile list
 (vpl_tiled_deferred_culling_stage2.cs:61-129) and the HDR output must equal
-the FP32 oracle's bit for bit. The 3840x2160 workload (4096 VPLs) checks the
-visibility cull and the 32,400 per-tile lists.
+the FP32 oracle's bit for bit. The 3840x2160 workload (4096 VPLs, K = 4)
+checks the visibility cull and the 32,400 per-tile lists, and two whole
+frames the same way (the second reading the first's history).
 
 Inputs come from the device scene generator and are copied to the host for the
 oracle (the generator equals the oracle's CPU ray caster bit for bit, see
@@ -86,4 +87,34 @@ def test_uhd_workload_tile_lists_bit_exact():
     assert lists.shape == (32400, 1 + L)
     assert int((ref[:, 0] == L).sum()) > 100
     assert np.array_equal(lists, ref), f"{int((lists != ref).any(1).sum())} of 32400 tile lists differ"
+    st.close()
+
+
+def test_uhd_workload_two_frames_bit_exact():
+    w = S.UHD
+    sc = S.workload_scene(w, 1234 + 4)
+    ds = stage.DeviceScene(sc, w)
+    hs = host_scene_from_device(ds, (0, 1, 2))
+    cfg = stage.workload_config(w)
+    L = cfg.max_vpls_per_tile
+    st = stage.GiStage(cfg)
+    st.set_lights(ds.vpls, ds.entries, ds.points)
+    out = torch.empty((w.height, w.width, 4), dtype=torch.float16, device="cuda")
+    gi = np.zeros((w.height, w.width, 4), np.float32)
+    hist = np.zeros((w.height, w.width), np.float32)
+    for k in (1, 2):
+        t = 1000.0 + 16.0 * k
+        st.set_shadow_maps(ds.csms[k], ds.cubes)
+        st.render_frame(ds.gbuffers[k], ds.gbuffers[k - 1], ds.camera(k), out, t, FPS)
+        torch.cuda.synchronize()
+        assert st.lib.sgi_device_status(st.ctx) == abi.SGI_OK
+        ref = O.frame(32, cfg, hs, k, gi, hist, t, FPS)
+        idx = st.read_debug(abi.SGI_DEBUG_VISIBLE_INDEX, np.int32)
+        cnt = ref["count"]
+        assert idx[0] == cnt and cnt > 2000
+        lists = st.read_debug(abi.SGI_DEBUG_TILE_LISTS, np.int32).reshape(-1, 1 + L)
+        assert np.array_equal(lists, ref["lists"]), f"frame {k}"
+        got = out.cpu().numpy().astype(np.float32)[..., :3]
+        assert_bit_exact(got, ref["combined"][..., :3], f"3840x2160 frame {k} HDR")
+        gi, hist = ref["gi"], ref["hist"]
     st.close()

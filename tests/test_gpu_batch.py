@@ -192,6 +192,41 @@ def test_persistent_batch_in_the_tolerance_precision():
     run_persistent(fast=True)
 
 
+def test_persistent_batch_views_bit_exact_against_the_oracle():
+    """The persistent kernel's views against the FP32 oracle directly: each view renders its first frame
+    through the C ABI, then one launch of the persistent batch renders the next; the oracle runs the same
+    two frames (the second reading the first's history) and every view's HDR output must equal it."""
+    import numpy as np
+
+    from helpers import assert_bit_exact, host_scene_from_device
+    from oracle import binding as O
+    lib = abi.load()
+    sizes = [(96, 64, 51), (160, 96, 52), (200, 120, 53)]
+    views = [View(*view_scene(W, H, seed)) for W, H, seed in sizes]
+    for v in views:
+        v.frame()
+    arr = (abi.View * len(views))(*[v.struct() for v in views])
+    h = C.c_void_p()
+    assert lib.sgi_batch_create_persistent(arr, len(views), 0, None, C.byref(h)) == abi.SGI_OK
+    assert lib.sgi_batch_launch(h, None) == abi.SGI_OK
+    torch.cuda.synchronize()
+    assert lib.sgi_batch_status(h) == abi.SGI_OK
+    for v in views:
+        w = v.w
+        hs = host_scene_from_device(v.ds, (0, 1))
+        cfg = stage.workload_config(w)
+        gi = np.zeros((w.height, w.width, 4), np.float32)
+        hist = np.zeros((w.height, w.width), np.float32)
+        for _ in range(2):
+            ref = O.frame(32, cfg, hs, 1, gi, hist, v.params.time, v.params.frames_per_second)
+            gi, hist = ref["gi"], ref["hist"]
+        got = v.out.cpu().numpy().astype(np.float32)[..., :3]
+        assert_bit_exact(got, ref["combined"][..., :3], f"{w.name}: persistent batch frame")
+    assert lib.sgi_batch_destroy(h) == abi.SGI_OK
+    for v in views:
+        v.st.close()
+
+
 def test_persistent_batch_wait_gives_up_and_the_next_launch_succeeds():
     """The test switch holds back view 0's VPL compaction: the tile passes that wait for it give up after the
     batch's 20 ms limit, the launch ends with SGI_ERR_TIMEOUT, and with the switch cleared the next launch

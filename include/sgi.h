@@ -109,6 +109,7 @@ typedef struct sgi_tile_stage1 {
 #define SGI_MAX_TILE_LIST        64
 #define SGI_MAX_DENOISE_PASSES   8
 #define SGI_MAX_POINT_LIGHTS     256
+#define SGI_MAX_CUBE_FACE        16384 /* cube face size limit of the atlases (drivers allow 16384-32768) */
 
 typedef struct sgi_config {
     int32_t width;                 /* viewport width in pixels  */

@@ -24,6 +24,7 @@ SGI_CUBE_F32 = 0
 SGI_CUBE_F16 = 1
 SGI_CUBE_UNORM16 = 2
 SGI_MAX_ATLASES = 14
+SGI_MAX_CUBE_FACE = 16384
 SGI_MAX_VPLS_BEFORE_CULL = 10000
 SGI_MAX_VPLS_PER_FRAME = 4480
 SGI_NUM_PASS_TIMES = 5

@@ -291,6 +291,7 @@ sgi_status sgi_set_shadow_maps(sgi_ctx* ctx, const sgi_csm* csm, const sgi_cube_
     if (!csm->depth || csm->resolution < 1 || csm->num_cascades != 4)
         return fail(ctx, SGI_ERR_ARG, "csm needs a depth pointer, resolution >= 1 and 4 cascades");
     if (cubes->num_atlases < 0 || cubes->num_atlases > SGI_MAX_ATLASES || cubes->face_size < 1 ||
+        cubes->face_size > SGI_MAX_CUBE_FACE ||
         cubes->layers_per_atlas < 0 || cubes->format < SGI_CUBE_F32 || cubes->format > SGI_CUBE_UNORM16)
         return fail(ctx, SGI_ERR_ARG, "bad cube atlas description");
     for (int a = 0; a < cubes->num_atlases; ++a)
@@ -612,7 +613,8 @@ sgi_status sgi_set_shadow_point_lights(sgi_ctx* ctx, const sgi_point_light* ligh
     }
     if (!lights || !entries || !atlas) return fail(ctx, SGI_ERR_ARG, "NULL lights, entries or atlas");
     if (atlas->num_atlases < 1 || atlas->num_atlases > SGI_MAX_ATLASES || atlas->layers_per_atlas < 1 ||
-        atlas->face_size < 1 || atlas->format < SGI_CUBE_F32 || atlas->format > SGI_CUBE_UNORM16)
+        atlas->face_size < 1 || atlas->face_size > SGI_MAX_CUBE_FACE || atlas->format < SGI_CUBE_F32 ||
+        atlas->format > SGI_CUBE_UNORM16)
         return fail(ctx, SGI_ERR_ARG, "shadow atlas: bad dimensions or format");
     cudaStream_t s = (cudaStream_t)stream;
     SGI_CUDA(ctx, cudaMemcpyAsync(ctx->shadow_points, lights, sizeof(sgi_point_light) * n, cudaMemcpyDefault, s),
@@ -631,7 +633,7 @@ sgi_status sgi_set_vpl_coloring(sgi_ctx* ctx, const sgi_diffuse_atlas* diffuse) 
         return SGI_OK;
     }
     if (diffuse->num_atlases < 1 || diffuse->num_atlases > SGI_MAX_ATLASES || diffuse->layers_per_atlas < 1 ||
-        diffuse->face_size < 1)
+        diffuse->face_size < 1 || diffuse->face_size > SGI_MAX_CUBE_FACE)
         return fail(ctx, SGI_ERR_ARG, "diffuse atlas: bad dimensions");
     for (int a = 0; a < diffuse->num_atlases; ++a)
         if (!diffuse->atlas[a] || ((uintptr_t)diffuse->atlas[a] & 3))

@@ -294,6 +294,15 @@ SGI_D float unorm8(uint32_t t, int ch) {
     const float q = xmul(b, r);
     return __fmaf_rn(__fmaf_rn(-q, 255.0f, b), r, q);
 }
+// b / 65535 for a UNORM16 value b (a unorm16 depth cube texel): the same
+// reciprocal step returns the correctly rounded quotient for every one of the
+// 65536 values (checked exhaustively in exact rational arithmetic).
+SGI_D float unorm16(uint32_t b) {
+    const float x = float(b & 0xffffu);
+    const float r = 1.0f / 65535.0f;
+    const float q = xmul(x, r);
+    return __fmaf_rn(__fmaf_rn(-q, 65535.0f, x), r, q);
+}
 SGI_D V3 decode_normal(uint32_t t) {   // normalize(rgb * 2 - 1), common.glsl:216-220 (exact in every build)
     V3 c = v3(unorm8(t, 0), unorm8(t, 1), unorm8(t, 2));
     return xnormalize(V3{xsub(xmul(c.x, 2.0f), 1.0f), xsub(xmul(c.y, 2.0f), 1.0f), xsub(xmul(c.z, 2.0f), 1.0f)});

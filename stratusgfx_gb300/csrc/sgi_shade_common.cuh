@@ -180,6 +180,16 @@ SGI_D size_t cube_texel(int layer, int n, V3 d) {
     return (((size_t)layer * 6 + face) * n + j) * n + i;
 }
 
+// Offset of texel (i, j) of face `face` of cube `layer`, face size n:
+// ((layer * 6 + face) * n + j) * n + i = layer * 6n^2 + ((face * n + j) * n + i).
+// The second term is below 6n^2 < 2^31 (n <= SGI_MAX_CUBE_FACE, checked when the
+// atlas is set), so it is formed in 32-bit arithmetic and added to the 64-bit
+// layer offset: the same value with one wide multiply-add.
+SGI_D size_t cube_offset(int layer, int face, int n, int j, int i) {
+    const uint32_t in_cube = (uint32_t)((face * n + j) * n + i);
+    return (size_t)(uint32_t)layer * (size_t)(6u * (uint32_t)n * (uint32_t)n) + in_cube;
+}
+
 SGI_D float cube_fetch(const sgi_cube_atlas& at, sgi_atlas_entry e, V3 d) {
     if (e.index < 0 || e.index >= at.num_atlases || e.layer < 0 || e.layer >= at.layers_per_atlas) return 1.0f;
     float ax = gabs(d.x), ay = gabs(d.y), az = gabs(d.z);
@@ -198,11 +208,11 @@ SGI_D float cube_fetch(const sgi_cube_atlas& at, sgi_atlas_entry e, V3 d) {
     float t = xmul(0.5f, xadd(xdiv(tc, ma), 1.0f));
     const int n = at.face_size;
     int i = nearest_index(s, n), j = nearest_index(t, n);
-    size_t off = (((size_t)e.layer * 6 + face) * n + j) * n + i;
+    const size_t off = cube_offset(e.layer, face, n, j, i);   // 0 <= e.layer < layers_per_atlas
     const void* base = at.atlas[e.index];
     if (at.format == SGI_CUBE_F16) return h2f(__ldg((const unsigned short*)base + off));
     if (at.format == SGI_CUBE_F32) return __ldg((const float*)base + off);
-    return xdiv(float(__ldg((const unsigned short*)base + off)), 65535.0f);
+    return unorm16(__ldg((const unsigned short*)base + off));   // = b / 65535, correctly rounded
 }
 
 // calculateShadowValue1Sample, pbr.glsl:116-136 (1 = occluded), given the

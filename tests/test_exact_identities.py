@@ -4,7 +4,8 @@ for bit while using fewer instructions than the expression they replace.
 UNORM8 decode (device unorm8, csrc/sgi_math.cuh): for every byte b the
 product q = RN(b * RN(1/255)) followed by q' = RN(RN(b - q*255) * RN(1/255) + q)
 (two fused multiply-adds) equals RN(b / 255), the quotient the oracle computes.
-Checked exhaustively here in exact rational arithmetic.
+Checked exhaustively here in exact rational arithmetic, and the same step for
+the 65536 UNORM16 values b / 65535 (device unorm16, the unorm16 depth cubes).
 
 Exponential without range reduction (device expf_exact / expf_ieee2): for
 |x| < 0.34 the Cody & Waite step gives k = floor(RN(RN(x * log2 e) + 0.5)) = 0,
@@ -34,6 +35,17 @@ def test_unorm8_reciprocal_step_equals_division():
         want = np.float32(b) / np.float32(255.0)
         assert q2 == want, b
         assert q2 == rn32(Fraction(b, 255)), b
+
+
+def test_unorm16_reciprocal_step_equals_division():
+    r = rn32(Fraction(1, 65535))
+    assert r == np.float32(1.0) / np.float32(65535.0)
+    fr = Fraction(float(r))
+    for b in range(65536):
+        q = rn32(Fraction(b) * fr)
+        res = rn32(Fraction(b) - Fraction(float(q)) * 65535)          # fma(-q, 65535, b)
+        q2 = rn32(Fraction(float(res)) * fr + Fraction(float(q)))     # fma(res, r, q)
+        assert q2 == np.float32(b) / np.float32(65535.0), b
 
 
 def test_difference_magnitude_is_symmetric():

@@ -302,6 +302,19 @@ def test_abi_rejects_bad_arguments():
         assert lib.sgi_set_lights(h, C.c_void_p(v.data_ptr()), C.c_void_p(e.data_ptr()), cfg.max_vpls + 1, None, 0,
                                   None) == abi.SGI_ERR_CAP
         assert b"max_vpls" in lib.sgi_last_error(h)
+        # cube faces above SGI_MAX_CUBE_FACE are refused (the texel offsets assume 6 n^2 < 2^31)
+        d = torch.zeros(16, device="cuda")
+        csm = abi.Csm()
+        csm.depth = d.data_ptr()
+        csm.resolution = 1
+        csm.num_cascades = 4
+        cubes = abi.CubeAtlas()
+        cubes.atlas[0] = d.data_ptr()
+        cubes.num_atlases, cubes.layers_per_atlas, cubes.format = 1, 1, abi.SGI_CUBE_F32
+        cubes.face_size = abi.SGI_MAX_CUBE_FACE + 1
+        assert lib.sgi_set_shadow_maps(h, C.byref(csm), C.byref(cubes)) == abi.SGI_ERR_ARG
+        cubes.face_size = abi.SGI_MAX_CUBE_FACE
+        assert lib.sgi_set_shadow_maps(h, C.byref(csm), C.byref(cubes)) == abi.SGI_OK
     finally:
         lib.sgi_destroy(h)
 

@@ -97,10 +97,17 @@ SGI_D float csm_pcf9(const float* __restrict__ base, int R, float s, float t, fl
     float light = 0.0f;
     if (run) {
         float cmp[4][4];   // [row r0[0] + i R][column c0[0] + j]
+        bool any = false;
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) cmp[i][j] = ref <= __ldg(base + r0[0] + (size_t)i * R + c0[0] + j) ? 1.0f : 0.0f;
+            for (int j = 0; j < 4; ++j) {
+                cmp[i][j] = ref <= __ldg(base + r0[0] + (size_t)i * R + c0[0] + j) ? 1.0f : 0.0f;
+                any = any || cmp[i][j] != 0.0f;
+            }
+        // every compare 0 (the window is in shadow): each sample is fma(0, w, ... 0 * w00) = +0 for the
+        // weights in [0, 1], and so is their sum, which the loop below would form
+        if (!any) return 0.0f;
 #pragma unroll
         for (int yi = 0; yi < 3; ++yi)
 #pragma unroll

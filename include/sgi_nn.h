@@ -67,8 +67,9 @@ sgi_status sgi_nn_train_step(sgi_nn* net, const void* features, const float* noi
 
 /* Builds the network inputs of the frame last gathered by `ctx` (after
  * sgi_global_illumination or sgi_render_frame with this frame's G-buffer):
- * features, noisy and prev (as above, batch 1). `prev` warps the context's GI
- * history with the velocity buffer (bilinear), like the temporal pass. */
+ * features, noisy and prev (as above, batch 1), each 16-byte aligned (else
+ * SGI_ERR_ARG). `prev` warps the context's GI history with the velocity buffer
+ * (bilinear), like the temporal pass. */
 sgi_status sgi_nn_features(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_camera* cam, void* features,
                            float* noisy, float* prev, void* stream);
 

@@ -764,6 +764,8 @@ sgi_status sgi_nn_features(sgi_ctx* ctx, const sgi_gbuffer* cur, const sgi_camer
     if (!ctx) return SGI_ERR_ARG;
     if (!gbuffer_ok(cur, true) || !cam || !features || !noisy || !prev)
         return fail(ctx, SGI_ERR_ARG, "NULL G-buffer, camera or output");
+    if (((uintptr_t)features | (uintptr_t)noisy | (uintptr_t)prev) & 15)
+        return fail(ctx, SGI_ERR_ARG, "features, noisy and prev must be 16-byte aligned");
     if (!ctx->last_merged) return fail(ctx, SGI_ERR_STATE, "no gathered frame yet");
     return run_features(ctx, cur, cam, (__nv_bfloat16*)features, (float4*)noisy, (float4*)prev, (cudaStream_t)stream);
 }

@@ -706,9 +706,16 @@ __global__ void __launch_bounds__(256) features_kernel(FeatureArgs a) {
     f[11] = log1p_bf(var);
     f[12] = log1p_bf(pr.x); f[13] = log1p_bf(pr.y); f[14] = log1p_bf(pr.z);
     f[15] = ((rma >> 8) & 0xffu) * k255;
-    __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(a.features + i * 16);
+    // the pixel's 32 bytes as two 16-byte stores (a warp then writes whole sectors)
+    uint32_t w[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) o[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+    for (int k = 0; k < 8; ++k) {
+        const __nv_bfloat162 b = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+        w[k] = *reinterpret_cast<const uint32_t*>(&b);
+    }
+    uint4* o = reinterpret_cast<uint4*>(a.features + i * 16);
+    o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    o[1] = make_uint4(w[4], w[5], w[6], w[7]);
 }
 
 cudaError_t features(const FeatureArgs& a, cudaStream_t s) {

@@ -315,6 +315,15 @@ def test_abi_rejects_bad_arguments():
         assert lib.sgi_set_shadow_maps(h, C.byref(csm), C.byref(cubes)) == abi.SGI_ERR_ARG
         cubes.face_size = abi.SGI_MAX_CUBE_FACE
         assert lib.sgi_set_shadow_maps(h, C.byref(csm), C.byref(cubes)) == abi.SGI_OK
+        # the denoiser inputs are written with 16-byte stores: misaligned outputs are refused
+        g = abi.GBuffer(*([d.data_ptr()] * 8))
+        cam = abi.Camera()
+        buf = torch.zeros(64, device="cuda")
+        p0, p4 = buf.data_ptr(), buf.data_ptr() + 4
+        assert lib.sgi_nn_features(h, C.byref(g), C.byref(cam), p4, p0, p0, None) == abi.SGI_ERR_ARG
+        assert lib.sgi_nn_features(h, C.byref(g), C.byref(cam), p0, p4, p0, None) == abi.SGI_ERR_ARG
+        assert b"16-byte aligned" in lib.sgi_last_error(h)
+        assert lib.sgi_nn_features(h, C.byref(g), C.byref(cam), p0, p0, p0, None) == abi.SGI_ERR_STATE   # no frame
     finally:
         lib.sgi_destroy(h)
 

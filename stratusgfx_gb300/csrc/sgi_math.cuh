@@ -178,8 +178,11 @@ SGI_D float2 expf_ieee2(float2 x) {
 #if SGI_FAST_MATH
     return make_float2(__expf(x.x), __expf(x.y));
 #endif
+    // k = 0 in both lanes: the polynomial alone. Each lane equals exp_poly even for tiny or
+    // subnormal arguments: every Horner step then rounds to its constant and the result is 1,
+    // whether or not the packed operations flush the argument.
+    if (fabsf(x.x) < kExpNoReduce && fabsf(x.y) < kExpNoReduce) return exp_poly2(x);
     if (!(exp_packable(x.x) && exp_packable(x.y))) return make_float2(expf_ieee(x.x), expf_ieee(x.y));
-    if (fabsf(x.x) < kExpNoReduce && fabsf(x.y) < kExpNoReduce) return exp_poly2(x);   // k = 0 in both lanes
     float2 kf;
     const float2 r = make_float2(exp_reduce(x.x, kf.x), exp_reduce(x.y, kf.y));
     const float2 p = exp_poly2(r);

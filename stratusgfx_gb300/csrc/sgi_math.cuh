@@ -99,6 +99,18 @@ SGI_D float expf_exact(float x) {
     return xmul(p, __int_as_float((k + 127) << 23));
 }
 
+// expf_exact for |x| <= 87 with one test: there k lies in [-125, 126], so none of
+// the full path's range and scaling tests applies and 2^k and the result are
+// normal; NaN and larger arguments take the full path. The same value.
+SGI_D float expf_exact_mid(float x) {
+    if (!(fabsf(x) <= 87.0f)) return expf_exact(x);
+    const float kf = floorf(xadd(xmul(x, 1.44269502162933349609375f), 0.5f));
+    const int k = (int)kf;
+    const float r =
+        xsub(xsub(x, xmul(kf, 0.693145751953125f)), xmul(kf, 1.428606765330187045037746429443359375e-06f));
+    return xmul(exp_poly(r), __int_as_float((k + 127) << 23));
+}
+
 // exp(x): Cody & Waite (1980) reduction x = k*ln2 + r with ln2 split into a
 // 15-bit head (exact products for |k| < 512) and a tail, exp(r) by its Taylor
 // series to r^7 in Horner form, then exact scaling by 2^k. In the tolerance
@@ -489,7 +501,11 @@ SGI_D float quadratic_atten(V3 lightDir) { float d = length(lightDir); return 1.
 // vplDiffuseAttenuation / vplSpecularAttenuation, pbr.glsl:260-271, with d = |lightDir|
 SGI_D float vpl_atten_len(float d, float radius) {
     float ratio = gmin(d / radius, 1.0f);
+#if SGI_FAST_MATH
     float minDist = mixf(10.0f, 1.0f, expf_ieee(-3.0f * ratio)) * radius;
+#else
+    float minDist = mixf(10.0f, 1.0f, expf_exact_mid(-3.0f * ratio)) * radius;   // -3 <= x <= 0 or NaN
+#endif
     return 1.0f / (minDist + 1.0f * d * d);
 }
 SGI_D float vpl_atten(V3 lightDir, float radius) {

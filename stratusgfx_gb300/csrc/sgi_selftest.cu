@@ -125,7 +125,7 @@ __global__ void lane_selftest_kernel(int n, unsigned* counts, float* first) {
     }
     // 6: exp over its whole range: normal, tiny, underflowing and special arguments,
     // and arguments around the bound below which the range reduction is skipped
-    // (packed, and the scalar expf_exact_near0, against the full scalar path)
+    // (packed, and the scalar expf_exact_near0 and expf_exact_mid, against the full scalar path)
     {
         float x[2];
         for (int l = 0; l < 2; ++l) {
@@ -138,6 +138,8 @@ __global__ void lane_selftest_kernel(int n, unsigned* counts, float* first) {
         w[0] = expf_exact(x[0]); w[1] = expf_exact(x[1]);
         rec.check(6, g, w, 2, x, 2);
         g[0] = expf_exact_near0(x[0]); g[1] = expf_exact_near0(x[1]);
+        rec.check(6, g, w, 2, x, 2);
+        g[0] = expf_exact_mid(x[0]); g[1] = expf_exact_mid(x[1]);
         rec.check(6, g, w, 2, x, 2);
     }
     // 7: x^128 for x in [0, 1.001], small values included

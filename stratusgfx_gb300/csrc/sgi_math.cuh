@@ -331,6 +331,10 @@ SGI_D int tex_index(float f, int n) {
     if (f >= 0.0f) return (int)f;
     return 0;
 }
+// tex_index as a clamp of the coordinate (n - 1 at or above n - 1, (int) f in
+// between, 0 below 0; fmaxf returns 0 for a NaN f): the same index, the form
+// the CSM filter's twelve indices per cascade run faster with
+SGI_D int tex_index_clamped(float f, int n) { return (int)fminf(fmaxf(f, 0.0f), float(n - 1)); }
 SGI_D int nearest_index(float s, int n) { return tex_index(floorf(xmul(s, float(n))), n); }
 
 // ------------------------------------------------------- shading library --

@@ -87,10 +87,10 @@ SGI_D float csm_pcf9(const float* __restrict__ base, int R, float s, float t, fl
         const float fu = floorf(u), fv = floorf(v);
         a[k] = xsub(u, fu);
         b[k] = xsub(v, fv);
-        c0[k] = tex_index(fu, R);
-        c1[k] = tex_index(xadd(fu, 1.0f), R);
-        r0[k] = (size_t)tex_index(fv, R) * R;
-        r1[k] = (size_t)tex_index(xadd(fv, 1.0f), R) * R;
+        c0[k] = tex_index_clamped(fu, R);
+        c1[k] = tex_index_clamped(xadd(fu, 1.0f), R);
+        r0[k] = (size_t)tex_index_clamped(fv, R) * R;
+        r1[k] = (size_t)tex_index_clamped(xadd(fv, 1.0f), R) * R;
     }
     const bool run = c0[0] + 1 == c0[1] && c0[1] + 1 == c0[2] && c1[0] == c0[0] + 1 && c1[2] == c0[2] + 1 &&
                      r0[0] + R == r0[1] && r0[1] + R == r0[2] && r1[0] == r0[0] + R && r1[2] == r0[2] + R;
